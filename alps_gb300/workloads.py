@@ -1,0 +1,109 @@
+"""Synthetic plasmas used by the tests and the benchmark.
+
+Every f0 table is produced by a restatement of the reference's
+generate_distribution formulas (distribution/generate_distribution.f90:
+176-300); no dataset is involved.  A workload is a dict with
+
+  system   -- alps_system (the &system namelist)
+  dists    -- list of alps_dist_params, one per species
+  species  -- list of alps_species (the &spec_i / &ffit_i_j namelists)
+  k        -- (kperp, kpar) of the first evaluation
+  extra    -- scan / map / guess settings of the workload
+
+``build(workload, generate)`` turns it into the (system, [(species, pperp,
+ppar, f0)]) pair both the library and the oracle take; ``generate`` is a
+generator with the signature of alps_generate_f0.
+"""
+from . import _abi
+
+M_E_KPAR_FAST = 5.44662e-4   # m_e/m_p of the reference's quick test inputs
+
+
+def _dist(kind=1, ms=1.0, tau=1.0, alph=1.0, p_drift=0.0, kappa=8.0, beta=1.0, vA=1e-4, maxP=6.0,
+          autoscale=1, kappa1=8.0):
+    d = _abi.alps_dist_params()
+    d.kind = kind
+    d.ms = ms
+    d.tau = tau
+    d.alph = alph
+    d.p_drift = p_drift
+    d.kappa = kappa
+    d.beta = beta
+    d.vA = vA
+    d.maxP = maxP
+    d.autoscale = autoscale
+    d.maxPperp = 1.0
+    d.maxPpar = 1.0
+    d.kappa1 = kappa1
+    return d
+
+
+def kpar_fast(nproc=4):
+    """The reference's CI input tests/test_kpar_fast.in with the f0 tables of
+    distribution/test_kpar_fast_dist.in (2 species, 120x240, k_par scan)."""
+    sysd = _abi.system_defaults(
+        nspec=2, nperp=120, npar=240, kperp=1e-2, kpar=1e-2, vA=1e-4, Bessel_zero=1e-50,
+        secant_method=2, numiter=50, kperp_norm=1, D_threshold=1e-15, D_prec=1e-5, D_gap=1e-5,
+        D_tol=1e-7, positions_principal=3, n_resonance_interval=100, Tlim=0.01, maxsteps_fit=500,
+        lambda_initial_fit=1.0, lambdafac_fit=10.0, epsilon_fit=1e-8, nproc=nproc)
+    sp1 = _abi.species_defaults(ns=1.0, qs=1.0, ms=1.0, fits=[(1, [1.7959e-1, 1.0, 0, 0, 0], 1.0)])
+    sp2 = _abi.species_defaults(ns=1.0, qs=-1.0, ms=M_E_KPAR_FAST,
+                                fits=[(1, [1.4128e4, 1.836e3, 0, 0, 0], 1.836e3)])
+    return dict(system=sysd, dists=[_dist(ms=1.0), _dist(ms=M_E_KPAR_FAST)], species=[sp1, sp2],
+                k=(1e-2, 1e-2),
+                extra=dict(guess=[9.9e-3 - 5.5e-6j],
+                           scan=dict(type_s=4, swi=1e-3, swf=1e-1, log_scan=True, n_out=32, n_res=1)))
+
+
+def proton_electron(nperp, npar, kperp, kpar, Bessel_zero, me=1.0 / 1836.0, nproc=0, ideal_fits=True,
+                    gen=None):
+    """Two bi-Maxwellian species, protons (m=1,q=1,n=1) and electrons
+    (m=me,q=-1,n=1), beta_par=1, T_perp/T_par=1, no drift, maxP=6, vA/c=1e-4:
+    the plasma of the benchmark configurations."""
+    sysd = _abi.system_defaults(
+        nspec=2, nperp=nperp, npar=npar, kperp=kperp, kpar=kpar, vA=1e-4, Bessel_zero=Bessel_zero,
+        secant_method=2, numiter=50, kperp_norm=1, D_threshold=1e-15, D_prec=1e-5, D_gap=1e-5,
+        D_tol=1e-7, positions_principal=3, n_resonance_interval=100, Tlim=0.01, nproc=nproc)
+    dists = [_dist(ms=1.0), _dist(ms=me)]
+    species = []
+    for d, q in zip(dists, (1.0, -1.0)):
+        # The ideal fit parameters of generate_distribution seed the LM fit.
+        import math
+        norm = math.pi ** -1.5 / ((d.ms * d.beta * d.tau) ** 1.5 * d.alph)
+        species.append(_abi.species_defaults(
+            ns=1.0, qs=q, ms=d.ms,
+            fits=[(1, [norm, 1.0 / (d.beta * d.ms * d.tau), d.p_drift, 0, 0],
+                   1.0 / (d.tau * d.beta * d.ms * d.alph))]))
+    return dict(system=sysd, dists=dists, species=species, k=(kperp, kpar), extra={})
+
+
+def config_kscan():
+    """Plain-FP64 k-scan: 60x120 grid, k_perp d_p = 1, k_par d_p from 0.05 to
+    1 (log, 32 steps), Bessel cutoff 1e-50, guess 0.05-0.01i."""
+    w = proton_electron(60, 120, 1.0, 0.05, 1e-50)
+    w["extra"] = dict(guess=[0.05 - 0.01j],
+                      scan=dict(type_s=4, swi=0.05, swf=1.0, log_scan=True, n_out=32, n_res=1))
+    return w
+
+
+def config_map(nr=512, ni=512, Bessel_zero=1e-9):
+    """Complex-frequency map: 128x256 grid, k_perp d_p = 2, k_par d_p = 0.3,
+    det D on an nr x ni lattice Re(omega) in [0,3], Im(omega) in [-0.5,0.1];
+    the Bessel cutoff 1e-9 gives the stated nmax ~30 for protons."""
+    w = proton_electron(128, 256, 2.0, 0.3, Bessel_zero)
+    mp = _abi.alps_map_params()
+    mp.omi, mp.omf, mp.gami, mp.gamf = 0.0, 3.0, -0.5, 0.1
+    mp.nr, mp.ni = nr, ni
+    mp.loggridw = mp.loggridg = 0
+    w["extra"] = dict(map=mp, n_polish=8)
+    return w
+
+
+def build(w, generate):
+    """Returns (system, [(species, pperp, ppar, f0), ...])."""
+    s = w["system"]
+    out = []
+    for d, sp in zip(w["dists"], w["species"]):
+        pperp, ppar, f0, _ = generate(d, s.nperp, s.npar)
+        out.append((sp, pperp, ppar, f0))
+    return s, out

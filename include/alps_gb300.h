@@ -1,0 +1,227 @@
+/*
+ * alps_gb300.h -- C-ABI of the GB300-native dispersion-tensor library.
+ *
+ * This is the drop-in boundary beneath ALPS's disp()/root-search call surface.
+ * ALPS keeps all state in module globals (src/ALPS_var.f90:19-427) and calls
+ * module procedures; each entry point below replaces one of those procedures
+ * (cited per function).  Every call takes plain pointers and sizes; device
+ * state lives inside an opaque context, one context per plasma.
+ *
+ * Array conventions:
+ *   - complex values are {re, im} pairs of doubles (alps_complex), layout
+ *     compatible with Fortran `double complex` and C99 `double _Complex`;
+ *   - momentum grids are passed per species as (nperp+1)*(npar+1) arrays in
+ *     the order of the ALPS f0 table files (iperp outer, ipar inner,
+ *     src/ALPS_io.f90:679-684), i.e. index iperp*(npar+1)+ipar;
+ *   - tensors are 3x3 row-major: chi[s*9 + 3*i + j] = chi(s, i+1, j+1);
+ *     chi_low[s*27 + 9*(n+1) + 3*i + j] = chi_low(s, i+1, j+1, n), n=-1..1.
+ *   - species indices are 0-based.
+ *
+ * Errors: every int-returning function returns ALPS_OK or a status code.
+ * Codes 1..11 mirror the reference's fatal alps_error ids
+ * (src/ALPS_io.f90:937-1012); the reference aborts the MPI job on those, this
+ * library returns them instead.  Device code never traps.
+ */
+#ifndef ALPS_GB300_H
+#define ALPS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ALPS_MAX_FITS 4
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  ALPS_OK = 0,
+  ALPS_E_NAMELIST = 1,        /* alps_error(1): required namelist not found   */
+  ALPS_E_FIT_POINTS = 2,      /* alps_error(2): more fit parameters than data */
+  ALPS_E_SCAN_OPTION = 3,     /* alps_error(3): bad scan_option               */
+  ALPS_E_NSCAN = 4,           /* alps_error(4): n_scan != 2 for double scan   */
+  ALPS_E_SCAN_SAME_TYPE = 5,  /* alps_error(5)                                */
+  ALPS_E_SCAN_TYPE0 = 6,      /* alps_error(6)                                */
+  ALPS_E_FIT_FAILED = 7,      /* alps_error(7): fit for continuation failed   */
+  ALPS_E_SUBLUMINAL = 8,      /* alps_error(8)                                */
+  ALPS_E_ROOTS_DIVERGED = 9,  /* alps_error(9): all roots diverged            */
+  ALPS_E_POLY_KIND = 10,      /* alps_error(10): unknown polynomial basis     */
+  ALPS_E_NPROC = 11,          /* alps_error(0): bad MPI rank count            */
+  ALPS_E_INVALID = 20,        /* bad argument / call order                    */
+  ALPS_E_CUDA = 21,           /* CUDA runtime error                           */
+  ALPS_E_OOM = 22,            /* device allocation failed                     */
+  ALPS_E_TIMEOUT = 23,        /* a bounded device wait ran out                */
+  ALPS_E_UNSUPPORTED = 24,    /* feature not implemented in this library      */
+  ALPS_E_GRID = 25,           /* grid is not a uniform tensor-product grid    */
+  ALPS_E_SINGULAR = 26,       /* fit matrix singular (reference: `stop`)      */
+  ALPS_E_IO = 27,             /* file input/output failed                     */
+  ALPS_E_NO_DEVICE = 28       /* no CUDA device / extension unusable          */
+};
+
+typedef struct alps_complex {
+  double re, im;
+} alps_complex;
+
+/* &system namelist (src/ALPS_io.f90:66-71, defaults src/ALPS_var.f90). */
+typedef struct alps_system {
+  int nspec;
+  int nperp, npar;
+  double kperp, kpar;
+  double vA;
+  double Bessel_zero;
+  int kperp_norm;             /* logical                                      */
+  int positions_principal;    /* M_I                                          */
+  int n_resonance_interval;   /* M_P                                          */
+  double Tlim;
+  int secant_method;          /* 0 secant, 1 rtsec, 2 secant_osc              */
+  int numiter;
+  double D_threshold, D_prec, D_gap, D_tol;
+  int maxsteps_fit;
+  double lambda_initial_fit, lambdafac_fit, epsilon_fit;
+  /* MPI rank count whose nmax adjustment (src/ALPS_fns.f90:4048-4071) is to
+   * be reproduced; 0 means no adjustment. */
+  int nproc;
+} alps_system;
+
+/* &spec_i, &ffit_i_j, &poly_spec_i, &bM_spec_i (src/ALPS_io.f90:302-419,
+ * 563-596). */
+typedef struct alps_species {
+  double ns, qs, ms;
+  int ac_method;              /* 0 analytic, 1 fitted functions, 2 Chebyshev */
+  int n_fits;
+  int relat, log_fit, use_bM;
+  int fit_type[ALPS_MAX_FITS];
+  double fit_init[ALPS_MAX_FITS][5];
+  double perp_correction[ALPS_MAX_FITS];
+  int poly_kind, poly_order;
+  double poly_log_max;
+  int bM_nmaxs;
+  double bM_Bessel_zeros, bM_betas, bM_alphas, bM_pdrifts;
+} alps_species;
+
+/* Default &system values (src/ALPS_var.f90:83-314). */
+void alps_system_defaults(alps_system* sys);
+void alps_species_defaults(alps_species* sp);
+
+typedef struct alps_ctx alps_ctx;
+
+/* Library build tag and the device the context would use. */
+const char* alps_version(void);
+const char* alps_error_string(int status);
+
+/* Creates a context on the current CUDA device.
+ * Replaces init_param (src/ALPS_io.f90:46-277) + pass_instructions
+ * (src/ALPS_com.f90:28-204): the parameters are copied into the context. */
+int alps_create(const alps_system* sys, alps_ctx** out);
+void alps_destroy(alps_ctx* ctx);
+
+/* Loads one species' grid and f0 table (host arrays, (nperp+1)*(npar+1)).
+ * Replaces read_f0 (src/ALPS_io.f90:643-692) + pass_distribution
+ * (src/ALPS_com.f90:208-284).  The grid must be a uniform tensor-product grid
+ * (pperp depends on iperp only, ppar on ipar only), as the reference assumes
+ * (src/ALPS_fns.f90:835-836, 4244); ALPS_E_GRID otherwise. */
+int alps_set_species(alps_ctx* ctx, int is, const alps_species* sp,
+                     const double* pperp, const double* ppar, const double* f0);
+
+/* Per-run preprocessing on the device: central-difference derivatives,
+ * Levenberg-Marquardt fits for the analytic continuation, ee term.
+ * Replaces derivative_f0 (src/ALPS_fns.f90:34-248) and determine_param_fit
+ * (src/ALPS_analyt.f90:365-728). */
+int alps_prepare(alps_ctx* ctx);
+
+/* Reads back the fitted continuation parameters of species is:
+ * out[(iperp*5 + ip)*n_fits + ifit], iperp=0..nperp (param_fit of
+ * src/ALPS_var.f90:276). */
+int alps_get_fit(alps_ctx* ctx, int is, double* out);
+
+/* Per-wavevector setup on the device: nmax from the Bessel cutoff, Bessel
+ * table, and the omega-independent p_perp contraction.
+ * Replaces determine_nmax + determine_bessel_array
+ * (src/ALPS_fns.f90:3971-4075, 4214-4255); split_processes
+ * (src/ALPS_fns.f90:4079-4207) has no counterpart: one device does all n. */
+int alps_set_k(alps_ctx* ctx, double kperp, double kpar);
+int alps_get_nmax(alps_ctx* ctx, int* nmax /* [nspec] */);
+
+/* Precision of the omega pass.  ALPS_PREC_FP64: every operation in FP64
+ * (the parity path).  ALPS_PREC_MIXED: the non-resonant pole sums run in
+ * double-float arithmetic on the FP32 pipes; pole, residue, det stay FP64. */
+enum { ALPS_PREC_FP64 = 0, ALPS_PREC_MIXED = 1 };
+int alps_set_precision(alps_ctx* ctx, int precision);
+
+/* det D(omega,k) for one omega, with the side results of the reference's
+ * disp(): chi0 (S x 3 x 3), chi0_low (S x 3 x 3 x {-1,0,1}) and wave (3x3).
+ * Any of chi0/chi0_low/wave may be NULL.
+ * Replaces disp (src/ALPS_fns.f90:252-636). */
+int alps_disp(alps_ctx* ctx, alps_complex om, alps_complex* D,
+              alps_complex* chi0, alps_complex* chi0_low, alps_complex* wave);
+
+/* det D for n frequencies from host memory (copies in the call). */
+int alps_disp_batch(alps_ctx* ctx, int n, const alps_complex* om,
+                    alps_complex* D);
+
+/* det D for n frequencies already in device memory; stream is a
+ * cudaStream_t (NULL = the context's stream).  Asynchronous. */
+int alps_disp_batch_device(alps_ctx* ctx, int n, const alps_complex* d_om,
+                           alps_complex* d_D, void* stream);
+
+/* Root polishing of nroots guesses in place (om[], host memory).
+ * method: 0 secant (src/ALPS_fns.f90:1815-1917), 1 rtsec (:2105-2195),
+ * 2 secant_osc (:1919-2101).  iters[r] (may be NULL) receives the number of
+ * iterations; Dfinal[r] (may be NULL) the det at the returned root.
+ * All roots advance together: each iteration evaluates every active root's
+ * det in one batched launch. */
+int alps_secant(alps_ctx* ctx, int method, int nroots, alps_complex* om,
+                int* iters, alps_complex* Dfinal);
+
+/* Complex-frequency map (map_search, src/ALPS_fns.f90:3595-3788, without the
+ * file output): om[ir*ni+ii], cal = det D with NaN/Inf sentinels, val =
+ * log10|D| with sentinels.  Any output pointer may be NULL. */
+typedef struct alps_map_params {
+  double omi, omf, gami, gamf;
+  int nr, ni;
+  int loggridw, loggridg;
+} alps_map_params;
+int alps_map(alps_ctx* ctx, const alps_map_params* mp, alps_complex* om,
+             alps_complex* cal, double* val);
+
+/* Strict 4-neighbour minima of val[ir*ni+ii] in the reference's scan order
+ * (find_minima, src/ALPS_fns.f90:3860-3966).  iroots holds (ir,ii) pairs,
+ * 0-based; returns the count in *nfound.  Host-only. */
+int alps_find_minima(const double* val, int nr, int ni, int numroots,
+                     int* iroots, int* nfound);
+
+/* Runs a whole ALPS input file (ALPS.f90 main program: map or guesses,
+ * refine_guess, om_scan), reading f0 tables from <workdir>/distribution and
+ * writing the reference's output files under <workdir>/solution. */
+int alps_run_input(const char* input_path, const char* workdir);
+
+/* f0 table generator (distribution/generate_distribution.f90:176-300):
+ * kind 1 bi-Maxwellian, 2 bi-kappa, 3 Juettner, 4 bi-Moyal.  Writes
+ * (nperp+1)*(npar+1) values into pperp/ppar/f0 and, if ideal!=NULL, the
+ * "ideal" fit parameters {fit_1..fit_5, perpcorr}.  Host-only. */
+typedef struct alps_dist_params {
+  int kind;
+  double ms, tau, alph, p_drift, kappa;
+  double beta, vA, maxP;
+  int autoscale;
+  double maxPperp, maxPpar;
+  double kappa1;              /* kappa of species 1 (autoscale of bi-kappa) */
+} alps_dist_params;
+int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar,
+                     double* pperp, double* ppar, double* f0, double* ideal);
+
+/* Device work counters of the last disp batch (for measurement). */
+typedef struct alps_stats {
+  int64_t n_eval;             /* frequencies evaluated                        */
+  int64_t n_pole_terms;       /* (omega, n, j) terms of the non-resonant sums */
+  int64_t n_resonant;         /* resonant (omega, species, n) work items      */
+  int64_t n_landau;           /* of which with a Landau term                  */
+  int kernels_launched;       /* kernels launched by the last disp batch      */
+} alps_stats;
+int alps_get_stats(alps_ctx* ctx, alps_stats* st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ALPS_GB300_H */
