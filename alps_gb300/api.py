@@ -1,0 +1,242 @@
+"""Python front end of the GB300 library, mirroring the reference's call
+surface (src/ALPS_fns.f90): disp, secant / secant_osc / rtsec, refine_guess,
+map_search, find_minima, om_scan.  Every evaluation goes through the native
+library (alps_gb300/lib/libalps_gb300.so); nothing here computes det D.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+
+from . import _abi
+from ._native import check, lib
+
+alps_complex = _abi.alps_complex
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _cptr(a):
+    return a.ctypes.data_as(C.POINTER(alps_complex))
+
+
+def generate_f0(dist, nperp, npar):
+    """f0 table of generate_distribution: (pperp, ppar, f0, ideal[6])."""
+    n = (nperp + 1) * (npar + 1)
+    pperp, ppar, f0, ideal = np.zeros(n), np.zeros(n), np.zeros(n), np.zeros(6)
+    check(lib().alps_generate_f0(C.byref(dist), nperp, npar, _dptr(pperp), _dptr(ppar), _dptr(f0), _dptr(ideal)),
+          "alps_generate_f0")
+    return pperp, ppar, f0, ideal
+
+
+def find_minima(val, nr, ni, numroots=100):
+    """find_minima (src/ALPS_fns.f90:3860-3966); val[ir*ni+ii]; returns
+    0-based (ir, ii) pairs in the reference's scan order."""
+    val = np.ascontiguousarray(val, dtype=np.float64)
+    iroots = (C.c_int * (2 * max(1, numroots)))()
+    nf = C.c_int()
+    check(lib().alps_find_minima(_dptr(val), nr, ni, numroots, iroots, C.byref(nf)), "alps_find_minima")
+    return [(iroots[2 * k], iroots[2 * k + 1]) for k in range(nf.value)]
+
+
+class Plasma:
+    """One plasma (an alps_ctx on the current CUDA device).
+
+    species: list of (alps_species, pperp, ppar, f0), arrays of length
+    (nperp+1)*(npar+1) in f0-file order.  prepare() runs derivative_f0 and
+    the continuation fits on the device; set_k() runs determine_nmax, the
+    Bessel table and the p_perp contraction.
+    """
+
+    def __init__(self, system, species, prepare=True, precision="fp64"):
+        L = lib()
+        self.sys = system
+        self.nspec = system.nspec
+        self._h = C.c_void_p()
+        check(L.alps_create(C.byref(system), C.byref(self._h)), "alps_create")
+        self.species = []
+        for i, (sp, pperp, ppar, f0) in enumerate(species):
+            a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pperp, ppar, f0)]
+            check(L.alps_set_species(self._h, i, C.byref(sp), *[_dptr(x) for x in a]), "alps_set_species")
+            self.species.append(sp)
+        self.set_precision(precision)
+        if prepare:
+            self.prepare()
+        self.kperp, self.kpar = system.kperp, system.kpar
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().alps_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_precision(self, precision):
+        p = {"fp64": 0, "mixed": 1}[precision]
+        check(lib().alps_set_precision(self._h, p), "alps_set_precision")
+        self.precision = precision
+
+    def prepare(self):
+        check(lib().alps_prepare(self._h), "alps_prepare")
+
+    def fit_size(self, i):
+        nf = self.species[i].n_fits if self.species[i].ac_method == 1 else 1
+        return (self.sys.nperp + 1) * 5 * nf
+
+    def get_fit(self, i):
+        out = np.zeros(self.fit_size(i))
+        check(lib().alps_get_fit(self._h, i, _dptr(out)), "alps_get_fit")
+        return out
+
+    def set_fit(self, i, arr):
+        arr = np.ascontiguousarray(arr, dtype=np.float64)
+        check(lib().alps_set_fit(self._h, i, _dptr(arr)), "alps_set_fit")
+
+    def set_k(self, kperp, kpar):
+        check(lib().alps_set_k(self._h, float(kperp), float(kpar)), "alps_set_k")
+        self.kperp, self.kpar = kperp, kpar
+
+    def nmax(self):
+        out = (C.c_int * self.nspec)()
+        check(lib().alps_get_nmax(self._h, out), "alps_get_nmax")
+        return list(out)
+
+    def disp(self, om):
+        """det D(om) with chi0 [s,i,j], chi0_low [s,n+1,i,j] (n = -1,0,1) and
+        the wave tensor [i,j] (the side results of disp)."""
+        D = alps_complex()
+        chi0 = np.zeros(self.nspec * 9, dtype=np.complex128)
+        chil = np.zeros(self.nspec * 27, dtype=np.complex128)
+        wave = np.zeros(9, dtype=np.complex128)
+        check(lib().alps_disp(self._h, alps_complex(om.real, om.imag), C.byref(D), _cptr(chi0), _cptr(chil),
+                              _cptr(wave)), "alps_disp")
+        return complex(D.re, D.im), chi0.reshape(self.nspec, 3, 3), chil.reshape(self.nspec, 3, 3, 3), \
+            wave.reshape(3, 3)
+
+    def disp_batch(self, oms):
+        oms = np.ascontiguousarray(oms, dtype=np.complex128)
+        out = np.zeros_like(oms)
+        check(lib().alps_disp_batch(self._h, len(oms), _cptr(oms), _cptr(out)), "alps_disp_batch")
+        return out
+
+    def disp_batch_device(self, n, d_om_ptr, d_D_ptr, stream_ptr=None):
+        check(lib().alps_disp_batch_device(self._h, n, C.c_void_p(d_om_ptr), C.c_void_p(d_D_ptr),
+                                           C.c_void_p(stream_ptr or 0)), "alps_disp_batch_device")
+
+    def secant(self, oms, method=None):
+        """Polishes roots in place; returns (roots, iterations, det at root)."""
+        if method is None:
+            method = self.sys.secant_method
+        oms = np.atleast_1d(np.ascontiguousarray(oms, dtype=np.complex128)).copy()
+        it = (C.c_int * len(oms))()
+        Df = np.zeros_like(oms)
+        check(lib().alps_secant(self._h, method, len(oms), _cptr(oms), it, _cptr(Df)), "alps_secant")
+        return oms, list(it), Df
+
+    def map_search(self, mp):
+        """(om, cal, val) of map_search (src/ALPS_fns.f90:3595-3788)."""
+        n = mp.nr * mp.ni
+        om = np.zeros(n, dtype=np.complex128)
+        cal = np.zeros(n, dtype=np.complex128)
+        val = np.zeros(n)
+        check(lib().alps_map(self._h, C.byref(mp), _cptr(om), _cptr(cal), _dptr(val)), "alps_map")
+        return om, cal, val
+
+    def set_profiling(self, on):
+        check(lib().alps_set_profiling(self._h, int(bool(on))), "alps_set_profiling")
+
+    def profile(self):
+        """Summed device ms of (classify, pole sums, resonant, finalize) and
+        the number of batches since profiling was switched on."""
+        ms = np.zeros(4)
+        nb = C.c_int64()
+        check(lib().alps_get_profile(self._h, _dptr(ms), C.byref(nb)), "alps_get_profile")
+        return ms, nb.value
+
+    def stats(self):
+        s = _abi.alps_stats()
+        check(lib().alps_get_stats(self._h, C.byref(s)), "alps_get_stats")
+        return s
+
+    def om_scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots):
+        """k-scan with root following (om_scan, src/ALPS_fns.f90:2198-2600,
+        step sizes of scan_read, src/ALPS_io.f90:426-552) without the eigen /
+        heating output.  Returns rows[it, root, (kperp, kpar, Re, Im)]."""
+        sy = self.sys
+        wr = np.array(wroots, dtype=np.complex128)
+        nroots = len(wr)
+        kperp_last, kpar_last = self.kperp, self.kpar
+        ns, nres = n_out, n_res
+        theta_0 = math.atan(kperp_last / kpar_last)
+        k_0 = math.sqrt(kperp_last ** 2 + kpar_last ** 2)
+        d = 1.0 * ns * nres
+        lg = math.log10
+        diff = diff2 = 0.0
+        if type_s == 0:
+            diff = (lg(swi) - lg(kperp_last)) / d if log_scan else (swi - kperp_last) / d
+            diff2 = (lg(swf) - lg(kpar_last)) / d if log_scan else (swf - kpar_last) / d
+        elif type_s == 1:
+            tf = swf * 4.0 * math.atan(1.0) / 180.0
+            diff = (lg(tf) - lg(theta_0)) / d if log_scan else (tf - theta_0) / d
+        elif type_s == 2:
+            diff = (lg(swf) - lg(k_0)) / d if log_scan else (swf - k_0) / d
+        elif type_s == 3:
+            diff = (lg(swf) - lg(kperp_last)) / d if log_scan else (swf - kperp_last) / d
+        elif type_s == 4:
+            diff = (lg(swf) - lg(kpar_last)) / d if log_scan else (swf - kpar_last) / d
+        else:
+            raise ValueError("scan_type must be 0..4")
+        rows = np.zeros((ns + 1, nroots, 4))
+        rows[0, :, 0] = self.kperp
+        rows[0, :, 1] = self.kpar
+        rows[0, :, 2] = wr.real
+        rows[0, :, 3] = wr.imag
+        jump = np.ones(nroots, dtype=bool)
+        out_row = 1
+        for it in range(1, ns * nres + 1):
+            kperp, kpar = self.kperp, self.kpar
+            if type_s == 0:
+                if log_scan:
+                    kperp = 10.0 ** (lg(kperp_last) + diff * it)
+                    kpar = 10.0 ** (lg(kpar_last) + diff2 * it)
+                else:
+                    kperp = kperp_last + diff * it
+                    kpar = kpar_last + diff2 * it
+            elif type_s == 1:
+                th = 10.0 ** (lg(theta_0) + diff * it) if log_scan else theta_0 + diff * it
+                kperp, kpar = k_0 * math.sin(th), k_0 * math.cos(th)
+            elif type_s == 2:
+                kt = 10.0 ** (lg(k_0) + diff * it) if log_scan else k_0 + diff * it
+                kperp, kpar = kt * math.sin(theta_0), kt * math.cos(theta_0)
+            elif type_s == 3:
+                kperp = 10.0 ** (lg(kperp_last) + diff * it) if log_scan else kperp_last + diff * it
+            else:
+                kpar = 10.0 ** (lg(kpar_last) + diff * it) if log_scan else kpar_last + diff * it
+            self.set_k(kperp, kpar)
+            if not jump.any():
+                raise _abi.AlpsError(9, "om_scan")
+            idx = [i for i in range(nroots) if jump[i]]
+            new, _, _ = self.secant(wr[idx], sy.secant_method)
+            for q, i in enumerate(idx):
+                wr[i] = new[q]
+                if not math.isfinite(wr[i].real):
+                    jump[i] = False
+                for imm in range(i):
+                    if abs(wr[i] - wr[imm]) < sy.D_gap:
+                        wr[i] = 0.0
+                        jump[i] = False
+                if it % nres == 0:
+                    rows[out_row, i] = (kperp, kpar, wr[i].real, wr[i].imag)
+            if it % nres == 0:
+                out_row += 1
+        return rows, wr

@@ -1,0 +1,742 @@
+// alps_api.cu -- the extern "C" entry points declared in include/alps_gb300.h.
+//
+// Host-side orchestration only: argument checks, device buffers, and the
+// root finders' control flow.  Every det D evaluation runs on the device
+// through launch_disp_batch (disp_kernels.cu); there is no host fallback.
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "alps_internal.cuh"
+
+namespace {
+thread_local char g_last_err[512] = "";
+typedef std::complex<double> cplx;
+inline cplx C(const double2& v) { return cplx(v.x, v.y); }
+inline double2 D2(const cplx& v) { return make_double2(v.real(), v.imag()); }
+}  // namespace
+
+void alps_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line) {
+  snprintf(g_last_err, sizeof(g_last_err), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+}
+
+extern "C" {
+
+const char* alps_version(void) { return "alps_gb300 0.1 (sm_103a)"; }
+
+const char* alps_error_string(int st) {
+  switch (st) {
+    case ALPS_OK: return "ok";
+    case ALPS_E_NAMELIST: return "required input namelist not found";
+    case ALPS_E_FIT_POINTS: return "more fit parameters than data points";
+    case ALPS_E_SCAN_OPTION: return "scan_option not set to allowable value";
+    case ALPS_E_NSCAN: return "n_scan .ne. 2 for scan_option=2";
+    case ALPS_E_SCAN_SAME_TYPE: return "scan(1)%type_s==scan(2)%type_s for double k scan";
+    case ALPS_E_SCAN_TYPE0: return "scan(*)%type_s=0 not allowed for double k scan";
+    case ALPS_E_FIT_FAILED: return "fit for analytical continuation failed";
+    case ALPS_E_SUBLUMINAL: return "resonance integration covers entire subluminal cone";
+    case ALPS_E_ROOTS_DIVERGED: return "all roots diverged";
+    case ALPS_E_POLY_KIND: return "unspecified orthogonal representation";
+    case ALPS_E_NPROC: return "number of processors must be even and greater than 2";
+    case ALPS_E_INVALID: return "invalid argument or call order";
+    case ALPS_E_CUDA: return g_last_err[0] ? g_last_err : "CUDA error";
+    case ALPS_E_OOM: return "device memory allocation failed";
+    case ALPS_E_TIMEOUT: return "device wait timed out";
+    case ALPS_E_UNSUPPORTED: return "feature not supported by this library";
+    case ALPS_E_GRID: return "grid is not a uniform tensor-product grid";
+    case ALPS_E_SINGULAR: return "fit matrix is numerically singular";
+    case ALPS_E_IO: return "file input/output failed";
+    case ALPS_E_NO_DEVICE: return "no usable CUDA device";
+  }
+  return "unknown status";
+}
+
+void alps_system_defaults(alps_system* s) {
+  memset(s, 0, sizeof(*s));
+  s->nspec = 1;
+  s->Bessel_zero = 1.0e-45;
+  s->kperp_norm = 1;
+  s->positions_principal = 5;
+  s->n_resonance_interval = 100;
+  s->Tlim = 0.01;
+  s->secant_method = 2;
+  s->numiter = 50;
+  s->D_threshold = 1.0e-5;
+  s->D_prec = 1.0e-5;
+  s->D_gap = 1.0e-5;
+  s->D_tol = 1.0e-7;
+  s->maxsteps_fit = 500;
+  s->lambda_initial_fit = 1.0;
+  s->lambdafac_fit = 10.0;
+  s->epsilon_fit = 1.0e-8;
+}
+
+void alps_species_defaults(alps_species* sp) {
+  memset(sp, 0, sizeof(*sp));
+  sp->ns = sp->qs = sp->ms = 1.0;
+  sp->ac_method = 1;
+  sp->n_fits = 1;
+  sp->log_fit = 1;
+  sp->bM_nmaxs = 500;
+  sp->bM_Bessel_zeros = 1.0e-50;
+  sp->bM_betas = 1.0;
+  sp->bM_alphas = 1.0;
+}
+
+int alps_create(const alps_system* sys, alps_ctx** out) {
+  if (!sys || !out) return ALPS_E_INVALID;
+  *out = nullptr;
+  if (sys->nspec < 1 || sys->nspec > ALPS_MAX_SPECIES) return ALPS_E_INVALID;
+  if (sys->positions_principal < 0 || sys->n_resonance_interval < 1) return ALPS_E_INVALID;
+  if (sys->nperp < 4 || sys->npar < 2 * sys->positions_principal + 8) return ALPS_E_INVALID;
+  if (sys->secant_method < 0 || sys->secant_method > 2) return ALPS_E_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return ALPS_E_NO_DEVICE;
+  alps_ctx* c = new alps_ctx();
+  c->sys = *sys;
+  c->spec.resize(sys->nspec);
+  c->kperp = sys->kperp;
+  c->kpar = sys->kpar;
+  cudaGetDevice(&c->device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return ALPS_E_CUDA;
+  }
+  *out = c;
+  return ALPS_OK;
+}
+
+void alps_destroy(alps_ctx* c) {
+  if (!c) return;
+  cudaStreamSynchronize(c->stream);
+  for (auto& S : c->spec) {
+    cudaFree(S.d_pperp);
+    cudaFree(S.d_ppar);
+    cudaFree(S.d_f0);
+    cudaFree(S.d_g1);
+    cudaFree(S.d_g2);
+    cudaFree(S.d_fit);
+    cudaFree(S.d_bessel);
+    cudaFree(S.d_V);
+    cudaFree(S.d_A);
+    cudaFree(S.d_Rw);
+    cudaFree(S.d_G);
+  }
+  cudaFree(c->d_om);
+  cudaFree(c->d_D);
+  cudaFree(c->d_part);
+  cudaFree(c->d_low);
+  cudaFree(c->d_count);
+  cudaFree(c->d_slot_nn);
+  cudaFree(c->d_items);
+  cudaFree(c->d_ext);
+  cudaFree(c->d_flags);
+  if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  for (auto& ev : c->ev_pending)
+    for (auto e : ev) cudaEventDestroy(e);
+  for (auto e : c->ev_pool) cudaEventDestroy(e);
+  cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* pperp, const double* ppar,
+                     const double* f0) {
+  if (!c || !sp || !pperp || !ppar || !f0 || is < 0 || is >= c->sys.nspec) return ALPS_E_INVALID;
+  if (sp->use_bM || sp->relat) return ALPS_E_UNSUPPORTED;
+  if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
+  if (sp->ac_method != 0 && sp->ac_method != 1) return ALPS_E_INVALID;
+  if (sp->ac_method == 1) {
+    if (sp->n_fits < 1 || sp->n_fits > ALPS_MAX_FITS) return ALPS_E_INVALID;
+    for (int f = 0; f < sp->n_fits; ++f) {
+      int t = sp->fit_type[f];
+      if (t != 1 && t != 2 && t != 3 && t != 6) return ALPS_E_UNSUPPORTED;
+    }
+  }
+  if (sp->qs == 0.0 || sp->ms <= 0.0) return ALPS_E_INVALID;
+  int N = c->sys.nperp, M = c->sys.npar, L = M + 1;
+  // tensor-product, uniform, increasing grid (the reference's assumption)
+  std::vector<double> pv(N + 1), qv(M + 1);
+  for (int i = 0; i <= N; ++i) pv[i] = pperp[i * L];
+  for (int j = 0; j <= M; ++j) qv[j] = ppar[j];
+  for (int i = 0; i <= N; ++i)
+    for (int j = 0; j <= M; ++j)
+      if (pperp[i * L + j] != pv[i] || ppar[i * L + j] != qv[j]) return ALPS_E_GRID;
+  double dp = pv[1] - pv[0], dq = qv[1] - qv[0];
+  if (!(dp > 0.0) || !(dq > 0.0)) return ALPS_E_GRID;
+  for (int i = 1; i <= N; ++i)
+    if (std::fabs((pv[i] - pv[i - 1]) - dp) > 1e-9 * dp) return ALPS_E_GRID;
+  for (int j = 1; j <= M; ++j)
+    if (std::fabs((qv[j] - qv[j - 1]) - dq) > 1e-9 * dq) return ALPS_E_GRID;
+  SpeciesHost& S = c->spec[is];
+  S.sp = *sp;
+  if (sp->ac_method != 1) S.sp.n_fits = 1;
+  S.pperp = pv;
+  S.ppar = qv;
+  S.f0.assign(f0, f0 + (size_t)(N + 1) * L);
+  size_t nn = (size_t)(N + 1) * L;
+  if (!S.d_pperp) ALPS_CUDA_TRY(cudaMalloc(&S.d_pperp, (N + 1) * sizeof(double)));
+  if (!S.d_ppar) ALPS_CUDA_TRY(cudaMalloc(&S.d_ppar, (M + 1) * sizeof(double)));
+  if (!S.d_f0) ALPS_CUDA_TRY(cudaMalloc(&S.d_f0, nn * sizeof(double)));
+  int nf = S.sp.n_fits;
+  if (S.d_fit) cudaFree(S.d_fit);
+  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)(N + 1) * 5 * nf * sizeof(double)));
+  std::vector<double> fit((size_t)(N + 1) * 5 * nf, 0.0);
+  for (int ip = 0; ip < 5; ++ip)
+    for (int f = 0; f < nf; ++f) fit[(0 * 5 + ip) * nf + f] = sp->fit_init[f][ip];
+  ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_pperp, pv.data(), (N + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_ppar, qv.data(), (M + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_f0, S.f0.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, fit.data(), fit.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  S.loaded = true;
+  c->prepared = false;
+  c->kset = false;
+  return ALPS_OK;
+}
+
+int alps_prepare(alps_ctx* c) {
+  if (!c) return ALPS_E_INVALID;
+  for (int is = 0; is < c->sys.nspec; ++is)
+    if (!c->spec[is].loaded) return ALPS_E_INVALID;
+  for (int is = 0; is < c->sys.nspec; ++is) {
+    int st = launch_prepare_species(c, is);
+    if (st) return st;
+  }
+  c->prepared = true;
+  c->kset = false;
+  return ALPS_OK;
+}
+
+int alps_get_fit(alps_ctx* c, int is, double* out) {
+  if (!c || !out || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
+  const SpeciesHost& S = c->spec[is];
+  size_t n = (size_t)(c->sys.nperp + 1) * 5 * S.sp.n_fits;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(out, S.d_fit, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return ALPS_OK;
+}
+
+int alps_set_fit(alps_ctx* c, int is, const double* in) {
+  if (!c || !in || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
+  const SpeciesHost& S = c->spec[is];
+  size_t n = (size_t)(c->sys.nperp + 1) * 5 * S.sp.n_fits;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return ALPS_OK;
+}
+
+int alps_set_k(alps_ctx* c, double kperp, double kpar) {
+  if (!c || !c->prepared) return ALPS_E_INVALID;
+  if (!(kperp > 0.0) || kpar == 0.0 || !std::isfinite(kperp) || !std::isfinite(kpar)) return ALPS_E_INVALID;
+  int S_ = c->sys.nspec;
+  std::vector<int> nm(S_);
+  for (int is = 0; is < S_; ++is) {
+    int st = launch_set_k_species(c, is, kperp, &nm[is]);
+    if (st) return st;
+  }
+  // nmax adjustment of a run on nproc MPI ranks (src/ALPS_fns.f90:4048-4071)
+  if (c->sys.nproc > 0) {
+    int max_procs = S_;
+    for (int is = 0; is < S_; ++is) max_procs += nm[is];
+    int is = 0;
+    while (max_procs < c->sys.nproc - 1) {
+      nm[is] += 1;
+      is = (is + 1) % S_;
+      max_procs++;
+    }
+  }
+  for (int is = 0; is < S_; ++is) {
+    SpeciesHost& S = c->spec[is];
+    S.nmax = nm[is];
+    int st = launch_build_bessel_and_reduced(c, is, kperp);
+    if (st) return st;
+    // resonant orders per omega: p_res moves by |q/k_par| per order, so at
+    // most width*|k_par/q| + 1 orders fall in the resonance window
+    int M = c->sys.npar;
+    double dq = S.ppar[2] - S.ppar[1];
+    double width = (S.ppar[M] - S.ppar[1]) + 2.0 * c->sys.positions_principal * dq + 2.0 * dq;
+    double cnt = std::floor(width * std::fabs(kpar / S.sp.qs)) + 3.0;
+    S.rcap = (int)std::min<double>(2.0 * S.nmax + 1.0, cnt);
+  }
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->kperp = kperp;
+  c->kpar = kpar;
+  c->kset = true;
+  return ALPS_OK;
+}
+
+int alps_get_nmax(alps_ctx* c, int* nmax) {
+  if (!c || !nmax || !c->kset) return ALPS_E_INVALID;
+  for (int is = 0; is < c->sys.nspec; ++is) nmax[is] = c->spec[is].nmax;
+  return ALPS_OK;
+}
+
+int alps_set_precision(alps_ctx* c, int precision) {
+  if (!c) return ALPS_E_INVALID;
+  if (precision != ALPS_PREC_FP64 && precision != ALPS_PREC_MIXED) return ALPS_E_INVALID;
+  c->precision = precision;
+  return ALPS_OK;
+}
+
+static int ensure_batch(alps_ctx* c, int n, bool ext) {
+  if ((size_t)n > c->batch_cap) {
+    cudaFree(c->d_om);
+    cudaFree(c->d_D);
+    c->d_om = c->d_D = nullptr;
+    c->batch_cap = 0;
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_om, (size_t)n * sizeof(double2)));
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_D, (size_t)n * sizeof(double2)));
+    c->batch_cap = n;
+  }
+  size_t need_pin = (size_t)2 * n;
+  if (need_pin > c->pinned_cap) {
+    if (c->h_pinned) cudaFreeHost(c->h_pinned);
+    c->h_pinned = nullptr;
+    c->pinned_cap = 0;
+    ALPS_CUDA_TRY(cudaMallocHost(&c->h_pinned, need_pin * sizeof(double2)));
+    c->pinned_cap = need_pin;
+  }
+  if (ext) {
+    size_t ne = (size_t)n * (c->sys.nspec * 36 + 9);
+    if (ne > c->ext_cap) {
+      cudaFree(c->d_ext);
+      c->d_ext = nullptr;
+      c->ext_cap = 0;
+      ALPS_CUDA_TRY(cudaMalloc(&c->d_ext, ne * sizeof(double2)));
+      c->ext_cap = ne;
+    }
+  }
+  return ALPS_OK;
+}
+
+static int check_flags(alps_ctx* c) {
+  int f = 0;
+  ALPS_CUDA_TRY(cudaMemcpy(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  return f ? ALPS_E_INVALID : ALPS_OK;
+}
+
+// Evaluates n frequencies from host memory through pinned staging.
+static int disp_host(alps_ctx* c, int n, const alps_complex* om, alps_complex* D, alps_complex* ext_out) {
+  int st = ensure_batch(c, n, ext_out != nullptr);
+  if (st) return st;
+  double2* pin = c->h_pinned;
+  memcpy(pin, om, (size_t)n * sizeof(double2));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_om, pin, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  st = launch_disp_batch(c, n, c->d_om, c->d_D, ext_out ? c->d_ext : nullptr, c->stream);
+  if (st) return st;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(pin + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+  if (ext_out)
+    ALPS_CUDA_TRY(cudaMemcpyAsync(ext_out, c->d_ext, (size_t)n * (c->sys.nspec * 36 + 9) * sizeof(double2),
+                                  cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  if ((st = check_flags(c))) return st;
+  memcpy(D, pin + n, (size_t)n * sizeof(double2));
+  return ALPS_OK;
+}
+
+int alps_disp(alps_ctx* c, alps_complex om, alps_complex* D, alps_complex* chi0, alps_complex* chi0_low,
+              alps_complex* wave) {
+  if (!c || !D || !c->kset) return ALPS_E_INVALID;
+  int S_ = c->sys.nspec;
+  std::vector<alps_complex> ext((size_t)S_ * 36 + 9);
+  int st = disp_host(c, 1, &om, D, ext.data());
+  if (st) return st;
+  if (chi0) memcpy(chi0, ext.data(), (size_t)S_ * 9 * sizeof(alps_complex));
+  if (chi0_low) memcpy(chi0_low, ext.data() + S_ * 9, (size_t)S_ * 27 * sizeof(alps_complex));
+  if (wave) memcpy(wave, ext.data() + S_ * 36, 9 * sizeof(alps_complex));
+  return ALPS_OK;
+}
+
+int alps_disp_batch(alps_ctx* c, int n, const alps_complex* om, alps_complex* D) {
+  if (!c || n < 0 || (n > 0 && (!om || !D)) || !c->kset) return ALPS_E_INVALID;
+  if (n == 0) return ALPS_OK;
+  return disp_host(c, n, om, D, nullptr);
+}
+
+int alps_disp_batch_device(alps_ctx* c, int n, const alps_complex* d_om, alps_complex* d_D, void* stream) {
+  if (!c || n < 0 || !c->kset) return ALPS_E_INVALID;
+  if (n == 0) return ALPS_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  return launch_disp_batch(c, n, reinterpret_cast<const double2*>(d_om), reinterpret_cast<double2*>(d_D), nullptr,
+                           st);
+}
+
+int alps_set_profiling(alps_ctx* c, int on) {
+  if (!c) return ALPS_E_INVALID;
+  int st = collect_profile(c);
+  if (st) return st;
+  c->profiling = on != 0;
+  for (int q = 0; q < 4; ++q) c->prof_ms[q] = 0.0;
+  c->prof_batches = 0;
+  return ALPS_OK;
+}
+
+int alps_get_profile(alps_ctx* c, double* ms, int64_t* batches) {
+  if (!c || !ms) return ALPS_E_INVALID;
+  int st = collect_profile(c);
+  if (st) return st;
+  for (int q = 0; q < 4; ++q) ms[q] = c->prof_ms[q];
+  if (batches) *batches = c->prof_batches;
+  return ALPS_OK;
+}
+
+int alps_get_stats(alps_ctx* c, alps_stats* st) {
+  if (!c || !st) return ALPS_E_INVALID;
+  *st = c->stats;
+  return ALPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Root finders.  Each root runs the reference's control flow as a state
+// machine that yields the frequencies it needs; all pending requests of all
+// roots go to the device in one batch per round.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Req {
+  std::vector<cplx> om;
+  std::vector<cplx> D;
+};
+
+// secant_osc (src/ALPS_fns.f90:1919-2101)
+struct SecantOsc {
+  const alps_system* sy;
+  int state = 0;
+  cplx om, D, minom, minD, prevom, prev2om, prev3om, prev4om, prevD, jump, delta;
+  int iter = 0, osc = 0;
+  double damping = 1.0;
+  bool done = false;
+  cplx Dfin;
+  const double lambda = (double)0.1f, osc_thr = (double)1.E-3f;
+  bool close(cplx a, cplx b) const {
+    return (std::fabs(a.real() - b.real()) < std::fabs(a.real()) * osc_thr) &&
+           (std::fabs(a.imag() - b.imag()) < std::fabs(a.imag()) * osc_thr);
+  }
+  // returns frequencies to evaluate (empty when finished)
+  std::vector<cplx> step(const std::vector<cplx>& got) {
+    for (;;) {
+      switch (state) {
+        case 0:
+          delta = cplx(1.0e-6, 1.0e-8);
+          state = 1;
+          return {om};
+        case 1:
+          D = got[0];
+          minom = om;
+          minD = D;
+          prevom = om * (1.0 - sy->D_prec);
+          prev2om = prev3om = prev4om = om;
+          state = 2;
+          return {prevom};
+        case 2:
+          prevD = got[0];
+          if (std::abs(prevD) < std::abs(minD)) { minom = prevom; minD = prevD; }
+          iter = 0;
+          state = 3;
+          break;
+        case 3:  // loop head
+          if (!(iter <= sy->numiter - 1)) { state = 9; break; }
+          iter++;
+          state = 4;
+          return {om};
+        case 4:
+          D = got[0];
+          if (std::abs(D - prevD) < 1.0e-80) {
+            prevom = prevom + 1.0e-8;
+            state = 5;
+            return {prevom};
+          }
+          state = 6;
+          break;
+        case 5:
+          prevD = got[0];
+          state = 6;
+          break;
+        case 6:
+          if (std::abs(D) < sy->D_threshold) {
+            jump = 0.0;
+            Dfin = D;
+            if (iter >= sy->numiter) {  // after-loop rule of the reference
+              om = minom;
+              Dfin = minD;
+            }
+            done = true;
+            state = 10;
+            return {};
+          }
+          if (iter > 4) {
+            if (close(om, prevom) || close(om, prev2om) || close(om, prev3om) || close(om, prev4om)) {
+              osc++;
+              damping = std::min(0.5, damping * 0.75);
+            }
+          }
+          if (osc > 1) {
+            state = 7;
+            return {om * (1.0 + delta), om * (1.0 - delta)};
+          }
+          jump = damping * D * (om - prevom) / (D - prevD);
+          state = 8;
+          break;
+        case 7: {
+          cplx Dprime = (got[0] - got[1]) / (2.0 * om * delta);
+          jump = D / (Dprime + lambda * D);
+          state = 8;
+          break;
+        }
+        case 8:
+          if (std::abs(jump) > (double)0.1f * std::abs(om)) jump = ((double)0.1f * std::abs(om)) * (jump / std::abs(jump));
+          if (std::abs(D) > std::abs(prevD)) jump = (double)0.5f * jump;
+          prev4om = prev3om;
+          prev3om = prev2om;
+          prev2om = prevom;
+          prevom = om;
+          prevD = D;
+          if (std::abs(D) < std::abs(minD)) { minom = om; minD = D; }
+          om = om - jump;
+          state = 3;
+          break;
+        case 9:  // numiter exhausted
+          om = minom;
+          Dfin = minD;
+          done = true;
+          state = 10;
+          return {};
+        default:
+          return {};
+      }
+    }
+  }
+};
+
+// secant (src/ALPS_fns.f90:1815-1917)
+struct SecantPlain {
+  const alps_system* sy;
+  int state = 0;
+  cplx om, prevom, Dprev, minD, minom, D, jump;
+  int iter = 0;
+  bool done = false;
+  cplx Dfin;
+  std::vector<cplx> step(const std::vector<cplx>& got) {
+    for (;;) {
+      switch (state) {
+        case 0:
+          prevom = om * (1.0 - sy->D_prec);
+          state = 1;
+          return {prevom, om};
+        case 1:
+          Dprev = got[0];
+          minD = got[1];
+          minom = om;
+          if (std::abs(Dprev) < std::abs(minD)) { minom = prevom; minD = Dprev; }
+          iter = 0;
+          state = 2;
+          break;
+        case 2:
+          if (!(iter <= sy->numiter - 1)) {
+            om = minom;
+            Dfin = minD;
+            done = true;
+            state = 9;
+            return {};
+          }
+          iter++;
+          state = 3;
+          return {om};
+        case 3:
+          D = got[0];
+          if (std::abs(D - Dprev) < 1.0e-80) {
+            prevom = prevom + 1.0e-8;
+            state = 4;
+            return {prevom};
+          }
+          state = 5;
+          break;
+        case 4:
+          Dprev = got[0];
+          state = 5;
+          break;
+        case 5: {
+          bool conv = std::abs(D) < sy->D_threshold;
+          jump = conv ? cplx(0.0) : D * (om - prevom) / (D - Dprev);
+          prevom = om;
+          om = om - jump;
+          Dprev = D;
+          if (std::abs(D) < std::abs(minD)) { minom = om; minD = D; }
+          if (conv) {
+            Dfin = D;
+            if (iter >= sy->numiter) {
+              om = minom;
+              Dfin = minD;
+            }
+            done = true;
+            state = 9;
+            return {};
+          }
+          state = 2;
+          break;
+        }
+        default:
+          return {};
+      }
+    }
+  }
+};
+
+// rtsec (src/ALPS_fns.f90:2105-2195)
+struct Rtsec {
+  const alps_system* sy;
+  int state = 0;
+  cplx xin, x1, x2, fl, f, rts, xl, dx;
+  int j = 0;
+  bool done = false;
+  cplx om, Dfin;
+  std::vector<cplx> step(const std::vector<cplx>& got) {
+    for (;;) {
+      switch (state) {
+        case 0:
+          x1 = xin * 1.0;
+          x2 = xin * (1.0 + sy->D_prec);
+          state = 1;
+          return {x1, x2};
+        case 1:
+          fl = got[0];
+          f = got[1];
+          if (std::abs(fl) < std::abs(f)) {
+            rts = x1;
+            xl = x2;
+            std::swap(fl, f);
+          } else {
+            xl = x1;
+            rts = x2;
+          }
+          j = 0;
+          state = 2;
+          break;
+        case 2:
+          j++;
+          if (j > sy->numiter - 1) {
+            om = rts;
+            Dfin = f;
+            done = true;
+            state = 9;
+            return {};
+          }
+          if (std::abs(f - fl) > 1.0e-40) dx = (xl - rts) * f / (f - fl);
+          else dx = (x2 - x1) / 25.0;
+          xl = rts;
+          fl = f;
+          rts = rts + dx / 2.0;
+          state = 3;
+          return {rts};
+        case 3:
+          f = got[0];
+          if ((std::abs(dx) < sy->D_tol) || (std::abs(f) == 0.0)) {
+            om = rts;
+            Dfin = f;
+            done = true;
+            state = 9;
+            return {};
+          }
+          state = 2;
+          break;
+        default:
+          return {};
+      }
+    }
+  }
+};
+
+}  // namespace
+
+int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iters, alps_complex* Dfinal) {
+  if (!c || !c->kset || nroots < 0 || (nroots > 0 && !om)) return ALPS_E_INVALID;
+  if (method < 0 || method > 2) return ALPS_E_INVALID;
+  std::vector<SecantOsc> so(method == 2 ? nroots : 0);
+  std::vector<SecantPlain> sp(method == 0 ? nroots : 0);
+  std::vector<Rtsec> rt(method == 1 ? nroots : 0);
+  std::vector<std::vector<cplx>> want(nroots), got(nroots);
+  for (int r = 0; r < nroots; ++r) {
+    cplx o(om[r].re, om[r].im);
+    if (method == 2) { so[r].sy = &c->sys; so[r].om = o; want[r] = so[r].step({}); }
+    if (method == 0) { sp[r].sy = &c->sys; sp[r].om = o; want[r] = sp[r].step({}); }
+    if (method == 1) { rt[r].sy = &c->sys; rt[r].xin = o; want[r] = rt[r].step({}); }
+  }
+  std::vector<alps_complex> bom, bD;
+  for (int round = 0; round < 100000; ++round) {
+    bom.clear();
+    for (int r = 0; r < nroots; ++r)
+      for (auto& w : want[r]) bom.push_back(alps_complex{w.real(), w.imag()});
+    if (bom.empty()) break;
+    bD.resize(bom.size());
+    int st = disp_host(c, (int)bom.size(), bom.data(), bD.data(), nullptr);
+    if (st) return st;
+    size_t k = 0;
+    for (int r = 0; r < nroots; ++r) {
+      got[r].clear();
+      for (size_t q = 0; q < want[r].size(); ++q, ++k) got[r].push_back(cplx(bD[k].re, bD[k].im));
+      if (want[r].empty()) continue;
+      if (method == 2) want[r] = so[r].step(got[r]);
+      if (method == 0) want[r] = sp[r].step(got[r]);
+      if (method == 1) want[r] = rt[r].step(got[r]);
+    }
+  }
+  for (int r = 0; r < nroots; ++r) {
+    cplx o, df;
+    int it;
+    if (method == 2) { o = so[r].om; df = so[r].Dfin; it = so[r].iter; }
+    else if (method == 0) { o = sp[r].om; df = sp[r].Dfin; it = sp[r].iter; }
+    else { o = rt[r].om; df = rt[r].Dfin; it = rt[r].j; }
+    om[r] = alps_complex{o.real(), o.imag()};
+    if (iters) iters[r] = it;
+    if (Dfinal) Dfinal[r] = alps_complex{df.real(), df.imag()};
+  }
+  return ALPS_OK;
+}
+
+// map_search values (src/ALPS_fns.f90:3595-3788)
+int alps_map(alps_ctx* c, const alps_map_params* mp, alps_complex* om_out, alps_complex* cal, double* val) {
+  if (!c || !mp || !c->kset || mp->nr < 1 || mp->ni < 1) return ALPS_E_INVALID;
+  int nr = mp->nr, ni = mp->ni, n = nr * ni;
+  std::vector<alps_complex> oms(n), D(n);
+  double dr = mp->omf - mp->omi, di = mp->gamf - mp->gami;
+  if (nr > 1) dr = (mp->omf - mp->omi) / (1.0 * (nr - 1));
+  if (ni > 1) di = (mp->gamf - mp->gami) / (1.0 * (ni - 1));
+  for (int ir = 1; ir <= nr; ++ir) {
+    double wr = mp->loggridw ? (nr > 1 ? mp->omi * std::pow(mp->omf / mp->omi, (1.0 * (ir - 1)) / (1.0 * (nr - 1)))
+                                       : mp->omi)
+                             : mp->omi + dr * (1.0 * (ir - 1));
+    for (int ii = 1; ii <= ni; ++ii) {
+      double wi = mp->loggridg
+                      ? (ni > 1 ? mp->gami * std::pow(mp->gamf / mp->gami, (1.0 * (ii - 1)) / (1.0 * (ni - 1)))
+                                : mp->gami)
+                      : mp->gami + di * (1.0 * (ii - 1));
+      oms[(ir - 1) * ni + (ii - 1)] = alps_complex{wr, wi};
+    }
+  }
+  int st = disp_host(c, n, oms.data(), D.data(), nullptr);
+  if (st) return st;
+  for (int k = 0; k < n; ++k) {
+    cplx cc(D[k].re, D[k].im);
+    double v = std::log10(std::abs(cc));
+    double tmp = cc.real();
+    if (cc.imag() == 0.0 && tmp != tmp) {
+      cc = 999999.0;
+      v = 999999.0;
+    }
+    if (std::fabs(tmp) > 1.0e100) {
+      cc = 899999.0;
+      v = 899999.0;
+    }
+    if (om_out) om_out[k] = oms[k];
+    if (cal) cal[k] = alps_complex{cc.real(), cc.imag()};
+    if (val) val[k] = v;
+  }
+  return ALPS_OK;
+}
+
+}  // extern "C"

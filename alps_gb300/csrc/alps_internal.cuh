@@ -1,0 +1,163 @@
+// alps_internal.cuh -- shared declarations of the GB300 dispersion library.
+//
+// Layout of the device state of one context (all FP64):
+//   per species s (grid N = nperp, M = npar):
+//     pperp[N+1], ppar[M+1]           tensor-product grid vectors
+//     f0[(N+1)(M+1)]                  f0 table, iperp-major
+//     g1, g2 [(N+1)(M+1)]             df0/dpperp and pperp*df0/dppar -
+//                                     ppar*df0/dpperp (interior nodes valid)
+//     fit[(N+1)*5*nf]                 continuation fit parameters
+//     bessel[(nmax+3)(N+1)]           J_n(k_perp pperp_i / q), n = -1..nmax+1
+//     V[(nmax+1)(M-1)*12]             reduced vectors of the p_perp
+//                                     contraction, see build_reduced()
+//   per omega batch: partial sums, resonant-item slots, results.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/alps_gb300.h"
+
+#define ALPS_MAX_SPECIES 8
+#define ALPS_PI 3.141592653589793115997963468544185161590576171875
+
+// ---------------------------------------------------------------------------
+// complex helpers on double2
+// ---------------------------------------------------------------------------
+__host__ __device__ inline double2 cmk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ inline double2 cadd(double2 a, double2 b) { return cmk(a.x + b.x, a.y + b.y); }
+__host__ __device__ inline double2 csub(double2 a, double2 b) { return cmk(a.x - b.x, a.y - b.y); }
+__host__ __device__ inline double2 cmul(double2 a, double2 b) {
+  return cmk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ inline double2 cscale(double2 a, double s) { return cmk(a.x * s, a.y * s); }
+__host__ __device__ inline double2 cneg(double2 a) { return cmk(-a.x, -a.y); }
+// Smith's division (the Fortran rule for complex division).
+__host__ __device__ inline double2 cdiv(double2 a, double2 b) {
+  if (fabs(b.x) >= fabs(b.y)) {
+    double r = b.y / b.x, den = b.x + b.y * r;
+    return cmk((a.x + a.y * r) / den, (a.y - a.x * r) / den);
+  } else {
+    double r = b.x / b.y, den = b.x * r + b.y;
+    return cmk((a.x * r + a.y) / den, (a.y * r - a.x) / den);
+  }
+}
+__host__ __device__ inline double cabs_(double2 a) { return hypot(a.x, a.y); }
+
+// ---------------------------------------------------------------------------
+// per-species constants visible to kernels (one copy per species)
+// ---------------------------------------------------------------------------
+struct SpecDev {
+  int N, M, nmax, nf;
+  int ac_method, log_fit;
+  int fit_type[ALPS_MAX_FITS];
+  double perp_corr[ALPS_MAX_FITS];
+  double qs, ms, ns;
+  double dpperp;      // pp(2,2,1) - pp(1,2,1)
+  double dppar;       // pp(2,2,2) - pp(2,1,2)  (signed; positive grids)
+  double dppar_abs;   // abs of the above
+  int species_index;  // 1-based index (distribution_analyt selects on it)
+  double int_ee;      // ee term (omega and k independent)
+  const double* pperp;
+  const double* ppar;
+  const double* f0;
+  const double* g1;
+  const double* g2;
+  const double* fit;
+  const double* bessel;
+  const double* V;
+  int rcap;           // resonant-item slots per (omega, species)
+};
+
+struct SysDev {
+  int nspec;
+  int kperp_norm;
+  int M_I, M_P;
+  double Tlim, vA;
+  double kperp, kpar;
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct SpeciesHost {
+  alps_species sp;
+  bool loaded = false;
+  std::vector<double> pperp, ppar, f0;   // host copies (grid vectors, table)
+  double *d_pperp = nullptr, *d_ppar = nullptr, *d_f0 = nullptr;
+  double *d_g1 = nullptr, *d_g2 = nullptr, *d_fit = nullptr;
+  double* d_bessel = nullptr;
+  size_t bessel_cap = 0;
+  double* d_V = nullptr;
+  size_t V_cap = 0;
+  double* d_A = nullptr;                  // contraction output scratch
+  size_t A_cap = 0;
+  double* d_Rw = nullptr;                 // weighted Bessel rows scratch
+  size_t Rw_cap = 0;
+  double* d_G = nullptr;                  // contraction RHS [2][N-1][M-1]
+  int nmax = 0;
+  double int_ee = 0.0;
+  int rcap = 1;
+};
+
+struct alps_ctx {
+  alps_system sys;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<SpeciesHost> spec;
+  bool prepared = false, kset = false;
+  double kperp = 0, kpar = 0;
+  int precision = ALPS_PREC_FP64;
+  // batch buffers
+  size_t batch_cap = 0;
+  double2* d_om = nullptr;      // [n]
+  double2* d_D = nullptr;       // [n]
+  double2* d_part = nullptr;    // [n][S][nchunk][6]
+  size_t part_cap = 0;
+  double2* d_low = nullptr;     // [n][S][nchunk][3][6]
+  size_t low_cap = 0;
+  int* d_count = nullptr;       // [n][S]
+  size_t count_cap = 0;
+  int* d_slot_nn = nullptr;     // [n][S][rcap]
+  double2* d_items = nullptr;   // [n][S][rcap][6]
+  size_t items_cap = 0;
+  double2* d_ext = nullptr;     // [n][S*9 + S*27 + 9] extended outputs
+  size_t ext_cap = 0;
+  int* d_flags = nullptr;       // error flags
+  alps_stats stats = {};
+  // profiling: pending event sets (5 events per batch) and totals
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::vector<cudaEvent_t>> ev_pending;
+  double prof_ms[4] = {0, 0, 0, 0};
+  int64_t prof_batches = 0;
+  // host pinned staging
+  double2* h_pinned = nullptr;
+  size_t pinned_cap = 0;
+};
+
+// ---------------------------------------------------------------------------
+// kernels / launchers (setup_kernels.cu, disp_kernels.cu)
+// ---------------------------------------------------------------------------
+int launch_prepare_species(alps_ctx* c, int is);
+int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
+int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
+int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
+                      cudaStream_t st);
+void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);
+int collect_profile(alps_ctx* c);
+void fill_sys_dev(const alps_ctx* c, SysDev* out);
+
+#define ALPS_CUDA_TRY(x)                                  \
+  do {                                                    \
+    cudaError_t _e = (x);                                 \
+    if (_e != cudaSuccess) {                              \
+      alps_set_last_cuda_error(_e, #x, __FILE__, __LINE__); \
+      return (_e == cudaErrorMemoryAllocation) ? ALPS_E_OOM : ALPS_E_CUDA; \
+    }                                                     \
+  } while (0)
+
+void alps_set_last_cuda_error(cudaError_t e, const char* what, const char* file, int line);

@@ -1,0 +1,709 @@
+// disp_kernels.cu -- the omega pass: det D(omega, k) for a batch of
+// frequencies (disp, src/ALPS_fns.f90:252-636).
+//
+// For fixed k the reference's double loop
+//     sum_{i,j} w_i w_j resU(i,j) int_T(n,i,j,mode)
+// factorises: resU's denominator depends on ppar_j only and its numerator is
+// linear in omega, so the p_perp sum was done once per k into the reduced
+// vectors V[n][j][12] (setup_kernels.cu).  What is left per omega is a 1-D
+// pole sum over ppar per Bessel order:
+//     S_{e,g}(n) = sum_j (w_j/2) V_{e,g}(n,j) / (m omega - k_par ppar_j - n q)
+// plus, for resonant orders, the principal-value window and the Landau term.
+//
+// Kernels of one batch (launched on one stream, in this order):
+//   k_classify    resonant orders of each (omega, species) into fixed slots
+//   k_pole_sums   the FP64-bound pole sums, all orders, one thread per omega
+//   k_resonant    principal value + Landau per resonant (omega, species, n),
+//                 one warp per item
+//   k_finalize    chi, epsilon, wave tensor and det, one thread per omega;
+//                 sums in a fixed order, so results do not depend on timing.
+#include <cmath>
+#include <cstdio>
+
+#include "alps_internal.cuh"
+#include "device_math.cuh"
+
+struct DispArgs {
+  SysDev sys;
+  SpecDev sp[ALPS_MAX_SPECIES];
+  int nchunk;    // order chunks per species
+  int csize;     // orders per chunk
+  int rcap;      // max resonant slots over species
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+__global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om, int* count, int* slot_nn,
+                           int* flags) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = blockIdx.y;
+  if (t >= n_om) return;
+  const SpecDev& S = a.sp[s];
+  double2 o = om[t];
+  int cnt = 0;
+  int* slots = slot_nn + ((size_t)t * a.sys.nspec + s) * a.rcap;
+  for (int nn = -S.nmax; nn <= S.nmax; ++nn) {
+    ResGeom g = res_geometry(S, a.sys.M_I, o, nn, a.sys.kpar);
+    if (g.res) {
+      if (cnt < a.rcap) slots[cnt] = nn;
+      cnt++;
+    }
+  }
+  if (cnt > a.rcap) {
+    atomicOr(flags, 1);
+    cnt = a.rcap;
+  }
+  count[(size_t)t * a.sys.nspec + s] = cnt;
+}
+
+// ---------------------------------------------------------------------------
+// Pole sums.  Block = TW omegas x JS slices of j.  grid = (omega tiles,
+// species, order chunks).  Each thread accumulates the six chi entries of its
+// omega over the orders of its chunk (and the n = -1,0,1 parts for chi_low).
+// ---------------------------------------------------------------------------
+template <bool LOW>
+__global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __restrict__ om, int n_om,
+                                                   int js_count, double2* part, double2* low) {
+  const int s = blockIdx.y;
+  const SpecDev& S = a.sp[s];
+  const int chunk = blockIdx.z;
+  const int n_begin = chunk * a.csize;
+  const int n_end = min(S.nmax + 1, n_begin + a.csize);
+  const int TW = blockDim.x / js_count;
+  const int wl = threadIdx.x % TW, js = threadIdx.x / TW;
+  const int w = blockIdx.x * TW + wl;
+  const bool active = (w < n_om);
+  const double2 o = active ? om[w] : cmk(0.0, 0.0);
+  const int M = S.M;
+  const double kpar = a.sys.kpar;
+  const double kappa = kpar / S.ms;
+  const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
+  const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+  const double Di = S.ms * o.y;
+  const double Di2 = Di * Di;
+  const double* __restrict__ pp = S.ppar;
+  double2 acc[6];
+  double2 lacc[LOW ? 3 : 1][6];
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    acc[e] = cmk(0.0, 0.0);
+#pragma unroll
+    for (int q = 0; q < (LOW ? 3 : 1); ++q) lacc[q][e] = cmk(0.0, 0.0);
+  }
+  if (active) {
+    for (int n = n_begin; n < n_end; ++n) {
+      const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
+      for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
+        const int nn = sg ? -n : n;
+        ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+        const double Ar = S.ms * o.x - (double)nn * S.qs;
+        double2 Sx[12];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) Sx[q] = cmk(0.0, 0.0);
+        for (int j = 1 + js; j <= M - 1; j += js_count) {
+          bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
+          if (!in) continue;
+          double dr = fma(-kpar, pp[j], Ar);
+          double r = rcp_fast(fma(dr, dr, Di2));
+          double Rr = dr * r, Ri = -Di * r;
+          const double2* v2 = reinterpret_cast<const double2*>(Vn + (size_t)(j - 1) * 12);
+#pragma unroll
+          for (int q = 0; q < 6; ++q) {
+            double2 v = __ldg(v2 + q);
+            Sx[2 * q].x = fma(v.x, Rr, Sx[2 * q].x);
+            Sx[2 * q].y = fma(v.x, Ri, Sx[2 * q].y);
+            Sx[2 * q + 1].x = fma(v.y, Rr, Sx[2 * q + 1].x);
+            Sx[2 * q + 1].y = fma(v.y, Ri, Sx[2 * q + 1].y);
+          }
+        }
+        // trapezoid end weights: the range ends carry half weight unless the
+        // range is a single node (integrate(a,a) weighs it fully)
+        int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+#pragma unroll
+        for (int r2 = 0; r2 < 2; ++r2) {
+          int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
+          if (lo >= hi) continue;
+#pragma unroll
+          for (int side = 0; side < 2; ++side) {
+            int j = side ? hi : lo;
+            if (((j - 1) % js_count) != js) continue;
+            double dr = fma(-kpar, pp[j], Ar);
+            double r = rcp_fast(fma(dr, dr, Di2));
+            double Rr = -0.5 * dr * r, Ri = 0.5 * Di * r;
+            const double* v = Vn + (size_t)(j - 1) * 12;
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+              Sx[q].x = fma(v[q], Rr, Sx[q].x);
+              Sx[q].y = fma(v[q], Ri, Sx[q].y);
+            }
+          }
+        }
+        double2 pref[6];
+        t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          if (n == 0 && (e == 0 || e == 3 || e == 4)) continue;
+          // integrate = C0 * pref * (omega S_e1 + kappa S_e2)
+          double2 t1 = cadd(cmul(o, Sx[2 * e]), cscale(Sx[2 * e + 1], kappa));
+          double2 val = cscale(cmul(pref[e], t1), C0);
+          acc[e] = cadd(acc[e], val);
+          if (LOW && nn >= -1 && nn <= 1) lacc[LOW ? nn + 1 : 0][e] = cadd(lacc[LOW ? nn + 1 : 0][e], val);
+        }
+      }
+    }
+  }
+  // reduce over the j slices
+  __shared__ double2 red[128 * 6];
+  if (js_count > 1) {
+    for (int e = 0; e < 6; ++e) red[threadIdx.x * 6 + e] = acc[e];
+    __syncthreads();
+    if (js == 0)
+      for (int q = 1; q < js_count; ++q)
+        for (int e = 0; e < 6; ++e) acc[e] = cadd(acc[e], red[(q * TW + wl) * 6 + e]);
+    if (LOW) {
+      for (int l = 0; l < 3; ++l) {
+        __syncthreads();
+        for (int e = 0; e < 6; ++e) red[threadIdx.x * 6 + e] = lacc[LOW ? l : 0][e];
+        __syncthreads();
+        if (js == 0)
+          for (int q = 1; q < js_count; ++q)
+            for (int e = 0; e < 6; ++e)
+              lacc[LOW ? l : 0][e] = cadd(lacc[LOW ? l : 0][e], red[(q * TW + wl) * 6 + e]);
+      }
+    }
+  }
+  if (js == 0 && active) {
+    size_t base = ((size_t)w * a.sys.nspec + s) * a.nchunk + chunk;
+    for (int e = 0; e < 6; ++e) part[base * 6 + e] = acc[e];
+    if (LOW)
+      for (int l = 0; l < 3; ++l)
+        for (int e = 0; e < 6; ++e) low[(base * 3 + l) * 6 + e] = lacc[LOW ? l : 0][e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Analytic continuation f(pperp_i, complex ppar) (eval_fit,
+// src/ALPS_analyt.f90:32-181; fit_function :185-266).
+// ---------------------------------------------------------------------------
+__device__ double2 eval_fit_d(const SpecDev& S, double vA, int iperp, double2 p) {
+  double pperp = S.pperp[iperp];
+  if (S.ac_method == 0) {
+    // distribution_analyt (distribution/distribution_analyt.f90:59-79)
+    double ms;
+    if (S.species_index == 1) ms = 1.0;
+    else if (S.species_index == 2) ms = 1.0 / 1836.0;
+    else return cmk(0.0, 0.0);
+    double norm = pow(ALPS_PI, -1.5) / pow(ms * 1.0, 1.5);
+    double2 p2 = cmul(p, p);
+    double2 arg = cneg(cadd(cscale(p2, 1.0 / (1.0 * ms)), cmk((pperp * pperp) / (1.0 * ms), 0.0)));
+    arg = cmk(-(p2.x / ms + (pperp * pperp) / ms), -(p2.y / ms));
+    return cscale(cexp_d(arg), norm);
+  }
+  double2 ff = cmk(0.0, 0.0);
+  const double* fit = S.fit;
+  int nf = S.nf;
+  for (int f = 0; f < nf; ++f) {
+    int t = S.fit_type[f];
+    double pc = S.perp_corr[f];
+    auto P = [&](int k) { return fit[(iperp * 5 + k) * nf + f]; };
+    double2 d = csub(p, cmk(P(2), 0.0));
+    double2 d2 = cmul(d, d);
+    if (t == 1) {
+      double a0 = P(0) * exp(-pc * (pperp * pperp));
+      ff = cadd(ff, cscale(cexp_d(cscale(d2, -P(1))), a0));
+    } else if (t == 2) {
+      double2 kp = cadd(cmk(1.0 + pc * P(4) * (pperp * pperp), 0.0), cscale(d2, P(1)));
+      kp = cadd(cmk(1.0, 0.0), cadd(cscale(d2, P(1)), cmk(pc * P(4) * (pperp * pperp), 0.0)));
+      ff = cadd(ff, cscale(cexp_d(cscale(clog_d(kp), P(3))), P(0)));
+    } else if (t == 3) {
+      double2 in = cadd(cmk(1.0, 0.0), cscale(cadd(cmk(pperp * pperp, 0.0), d2), vA * vA / (S.ms * S.ms)));
+      double2 sq = csqrt_d(in);
+      ff = cadd(ff, cscale(cexp_d(cscale(sq, -P(1))), P(0)));
+    } else if (t == 6) {
+      double2 q = cadd(cmk(P(3) * pc * (pperp * pperp), 0.0), cscale(d2, P(1)));
+      double2 arg = cscale(csub(q, cexp_d(q)), 0.5);
+      ff = cadd(ff, cscale(cexp_d(arg), P(0)));
+    }
+  }
+  return ff;
+}
+
+// h_e(j) = omega V_{e,1}(j) + kappa V_{e,2}(j)
+__device__ inline double2 h_node(const double* Vn, int j, int e, double2 o, double kappa) {
+  const double* v = Vn + (size_t)(j - 1) * 12 + 2 * e;
+  return cmk(o.x * v[0] + kappa * v[1], o.y * v[0]);
+}
+
+// ---------------------------------------------------------------------------
+// Resonant items: the principal-value part of integrate_res
+// (src/ALPS_fns.f90:1000-1236) and landau_integrate (:1327-1452) for one
+// (omega, species, n).  One warp per item.
+// ---------------------------------------------------------------------------
+#define RES_WARPS 4
+#define RES_WIN 64
+
+__global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const double2* __restrict__ om,
+                                                              int n_om, const int* __restrict__ count,
+                                                              const int* __restrict__ slot_nn, double2* items,
+                                                              int* flags) {
+  extern __shared__ double2 sm[];
+  const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int S_ = a.sys.nspec;
+  long item = (long)blockIdx.x * RES_WARPS + warp;
+  long total = (long)n_om * S_ * a.rcap;
+  if (item >= total) return;
+  int r = (int)(item % a.rcap);
+  int s = (int)((item / a.rcap) % S_);
+  int w = (int)(item / ((long)a.rcap * S_));
+  if (r >= count[(size_t)w * S_ + s]) return;
+  const SpecDev& S = a.sp[s];
+  const int nn = slot_nn[((size_t)w * S_ + s) * a.rcap + r];
+  const int n = nn < 0 ? -nn : nn;
+  const double2 o = om[w];
+  const int M = S.M, N = S.N;
+  const double kpar = a.sys.kpar, kappa = kpar / S.ms;
+  const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+  double2 pref[6];
+  t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
+  ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+  const double* Vn = S.V + (size_t)n * (M - 1) * 12;
+  double2* win = sm + (size_t)warp * (RES_WIN * 6 + (size_t)(N + 1));  // h window, then f0 row values
+  double2* frow = win + RES_WIN * 6;
+  double2 res[6];
+  for (int e = 0; e < 6; ++e) res[e] = cmk(0.0, 0.0);
+  const int nent = 6;
+
+  // ---- principal value window (case 3) ----
+  if (g.kind == 3) {
+    const double pr = g.pr, pim = g.pi;
+    const double dpa = S.dppar_abs, dps = S.dppar;
+    const int jw0 = max(1, g.lower - 2), jw1 = min(M - 1, g.upper + 2);
+    const int nw = jw1 - jw0 + 1;
+    const bool winok = nw <= RES_WIN;
+    if (winok)
+      for (int t = lane; t < nw * 6; t += 32) {
+        int jj = t / 6, e = t % 6;
+        win[jj * 6 + e] = h_node(Vn, jw0 + jj, e, o, kappa);
+      }
+    __syncwarp();
+    auto hget = [&](int j, int e) -> double2 {
+      if (winok && j >= jw0 && j <= jw1) return win[(j - jw0) * 6 + e];
+      return h_node(Vn, j, e, o, kappa);
+    };
+    // funct_g summed over iperp: H_e(p) (src/ALPS_fns.f90:1243-1321)
+    auto Hc = [&](double p, double2* H) {
+      int jc = 0;
+      double jd = floor((p - S.ppar[0]) / dpa + 0.5);
+      if (jd > -10.0 && jd < (double)M + 10.0) {
+        int j0 = (int)jd;
+        int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
+        for (int jj = hi; jj >= lo; --jj)
+          if (fabs(S.ppar[jj] - p) <= 0.5 * dpa) { jc = jj; break; }
+      } else if (!(jd > -10.0)) {
+        jc = 0;
+      }
+      if (jc >= M - 1) jc = M - 2;
+      if (jc <= 1) jc = 2;
+      double dx = p - S.ppar[jc];
+      for (int e = 0; e < nent; ++e) {
+        double2 hp = hget(jc + 1, e), h0 = hget(jc, e), hm = hget(jc - 1, e);
+        double2 slope = cscale(csub(hp, hm), 1.0 / dpa);
+        H[e] = cadd(h0, cscale(slope, 0.5 * dx));
+      }
+    };
+    const double capDelta = pr - S.ppar[g.lower];
+    const double smdelta = capDelta / (1.0 * a.sys.M_P);
+    double2 T[6];
+    for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
+    double2 H1[6], H2[6];
+    if (fabs(pim) > a.sys.Tlim) {
+      for (int k = lane; k <= a.sys.M_P; k += 32) {
+        double p = (k == 0) ? pr : ((k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k);
+        double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
+        // K = 1/(p - pr - i pim); the mirrored term uses conj(K)
+        double dx = p - pr;
+        double rr = 1.0 / (dx * dx + pim * pim);
+        double2 K = cmk(dx * rr, pim * rr);
+        double2 Kc = cmk(dx * rr, -pim * rr);
+        Hc(p, H1);
+        Hc(2.0 * pr - p, H2);
+        for (int e = 0; e < nent; ++e)
+          T[e] = cadd(T[e], cscale(csub(cmul(H1[e], K), cmul(H2[e], Kc)), wk));
+      }
+    } else {
+      // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
+      double fr = 0.0;
+      for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
+        double p = (k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k;
+        double wk = (k == a.sys.M_P) ? 1.0 : 2.0;
+        double d = p - pr;
+        fr += wk * ((d * d) / (d * d + pim * pim));
+      }
+      for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
+      if (lane == 0) {
+        Hc(pr + dps, H1);
+        Hc(pr - dps, H2);
+        double2 H0[6];
+        Hc(pr, H0);
+        double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
+        for (int e = 0; e < nent; ++e) {
+          double2 gp = cscale(csub(H1[e], H2[e]), 1.0 / (2.0 * dps));
+          T[e] = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0[e]));
+        }
+      }
+    }
+    // tiny rest between pr + capDelta and ppar[upper]
+    int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
+    if (ntiny > 0) {
+      double corr = ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta;
+      for (int k = lane; k <= ntiny; k += 32) {
+        double p = (k == 0) ? pr + capDelta : pr + capDelta + corr * smdelta * k;
+        double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
+        double dx = p - pr;
+        double rr = 1.0 / (dx * dx + pim * pim);
+        double2 K = cmk(dx * rr, pim * rr);
+        Hc(p, H1);
+        for (int e = 0; e < nent; ++e) T[e] = cadd(T[e], cscale(cmul(H1[e], K), wk * corr));
+      }
+    }
+    for (int e = 0; e < nent; ++e)
+      for (int off = 16; off > 0; off >>= 1) {
+        T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
+        T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
+      }
+    // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
+    double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
+    for (int e = 0; e < nent; ++e) res[e] = cscale(cmul(pref[e], T[e]), scale);
+  }
+
+  // ---- Landau term ----
+  int lf = (o.y < 0.0) ? 2 : ((o.y == 0.0) ? 1 : 0);
+  if (lf > 0) {
+    const double2 p = cmk(g.pr, g.pi);
+    const double pd = S.dppar_abs, dpp = S.dpperp;
+    const double vA = a.sys.vA;
+    for (int i = lane; i <= N; i += 32) frow[i] = eval_fit_d(S, vA, i, p);
+    __syncwarp();
+    bool zero = false;
+    double2 sums[3] = {cmk(0, 0), cmk(0, 0), cmk(0, 0)};
+    const double ql = S.qs / fabs(kpar);
+    const int L = N + 1;
+    for (int i = lane; i <= N; i += 32) {
+      double2 fpi = eval_fit_d(S, vA, i, cadd(p, cmk(pd, 0.0)));
+      double2 fpf = eval_fit_d(S, vA, i, csub(p, cmk(pd, 0.0)));
+      double2 dfperp, dfpar;
+      double h;
+      if (i == 0) {
+        dfperp = cscale(csub(frow[1], frow[0]), 1.0 / dpp);
+        h = 0.5;
+      } else if (i == N) {
+        dfperp = cscale(csub(frow[N], frow[N - 1]), 1.0 / dpp);
+        h = 0.5;
+      } else {
+        if (cabs_(fpi) == 0.0 || cabs_(fpf) == 0.0 || cabs_(frow[i + 1]) == 0.0) zero = true;
+        dfperp = cscale(csub(frow[i + 1], frow[i - 1]), 1.0 / (2.0 * dpp));
+        h = (i == N - 1) ? 0.5 : 1.0;
+      }
+      dfpar = cscale(csub(fpi, fpf), 1.0 / (2.0 * pd));
+      double pp_i = S.pperp[i];
+      // (q/|kpar|) ((pperp dfpar - p dfperp) kpar/m + omega dfperp)
+      double2 Lv = cscale(cadd(cscale(csub(cscale(dfpar, pp_i), cmul(p, dfperp)), kpar / S.ms), cmul(o, dfperp)),
+                          ql);
+      double J = S.bessel[(size_t)(n + 1) * L + i];
+      double Jp = (n == 0) ? -S.bessel[(size_t)2 * L + i]
+                           : 0.5 * (S.bessel[(size_t)n * L + i] - S.bessel[(size_t)(n + 2) * L + i]);
+      sums[0] = cadd(sums[0], cscale(Lv, h * (J * J)));
+      sums[1] = cadd(sums[1], cscale(Lv, h * ((pp_i * pp_i) * Jp * Jp)));
+      sums[2] = cadd(sums[2], cscale(Lv, h * (pp_i * J * Jp)));
+    }
+    zero = __any_sync(0xffffffffu, zero);
+    for (int F = 0; F < 3; ++F)
+      for (int off = 16; off > 0; off >>= 1) {
+        sums[F].x += __shfl_xor_sync(0xffffffffu, sums[F].x, off);
+        sums[F].y += __shfl_xor_sync(0xffffffffu, sums[F].y, off);
+      }
+    if (!zero) {
+      // landau_e = -pref_e c_e(p) Sigma_F(e) * i dpperp 2 pi^2
+      double2 c1 = cmk(1.0, 0.0), cp = p, cp2 = cmul(p, p);
+      double2 cfac[6] = {c1, c1, cp2, c1, cp, cp};
+      int fam[6] = {0, 1, 0, 2, 0, 2};
+      double2 ifac = cmk(0.0, -dpp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+      for (int e = 0; e < 6; ++e) {
+        double2 land = cmul(cmul(pref[e], cfac[e]), sums[fam[e]]);
+        res[e] = cadd(res[e], cmul(land, ifac));
+      }
+    }
+  }
+  if (lane == 0) {
+    double2* out = items + (((size_t)w * S_ + s) * a.rcap + r) * 6;
+    for (int e = 0; e < 6; ++e) {
+      bool skip = (n == 0 && (e == 0 || e == 3 || e == 4));
+      out[e] = skip ? cmk(0.0, 0.0) : res[e];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// chi, epsilon, wave tensor, det (src/ALPS_fns.f90:500-626)
+// ---------------------------------------------------------------------------
+__global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om, const double2* __restrict__ part,
+                           const double2* __restrict__ low, const int* __restrict__ count,
+                           const int* __restrict__ slot_nn, const double2* __restrict__ items, double2* D,
+                           double2* ext) {
+  int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= n_om) return;
+  const int S_ = a.sys.nspec;
+  const double2 o = om[w];
+  double2 eps[6];
+  for (int e = 0; e < 6; ++e) eps[e] = cmk(0.0, 0.0);
+  const double kperp = a.sys.kperp, kpar = a.sys.kpar, vA = a.sys.vA;
+  double2 denom = cmul(o, o);
+  denom = a.sys.kperp_norm ? cscale(cscale(denom, vA), vA) : cscale(cscale(cscale(cscale(denom, vA), vA), kperp), kperp);
+  for (int s = 0; s < S_; ++s) {
+    const SpecDev& S = a.sp[s];
+    double2 chi[6], cl[3][6];
+    for (int e = 0; e < 6; ++e) {
+      chi[e] = cmk(0.0, 0.0);
+      for (int l = 0; l < 3; ++l) cl[l][e] = cmk(0.0, 0.0);
+    }
+    size_t base = ((size_t)w * S_ + s) * a.nchunk;
+    for (int ch = 0; ch < a.nchunk; ++ch)
+      for (int e = 0; e < 6; ++e) chi[e] = cadd(chi[e], part[(base + ch) * 6 + e]);
+    if (ext && low)
+      for (int ch = 0; ch < a.nchunk; ++ch)
+        for (int l = 0; l < 3; ++l)
+          for (int e = 0; e < 6; ++e) cl[l][e] = cadd(cl[l][e], low[((base + ch) * 3 + l) * 6 + e]);
+    int cnt = count[(size_t)w * S_ + s];
+    for (int r = 0; r < cnt; ++r) {
+      size_t ib = ((size_t)w * S_ + s) * a.rcap + r;
+      int nn = slot_nn[ib];
+      for (int e = 0; e < 6; ++e) {
+        double2 v = items[ib * 6 + e];
+        chi[e] = cadd(chi[e], v);
+        if (nn >= -1 && nn <= 1) cl[nn + 1][e] = cadd(cl[nn + 1][e], v);
+      }
+    }
+    double ee = a.sys.kperp_norm ? S.int_ee : kperp * kperp * S.int_ee;
+    chi[2] = cadd(chi[2], cmk(ee, 0.0));
+    cl[1][2] = cadd(cl[1][2], cmk(ee, 0.0));
+    double norm = S.ns * S.qs;
+    for (int e = 0; e < 6; ++e) {
+      chi[e] = cscale(chi[e], norm);
+      for (int l = 0; l < 3; ++l) cl[l][e] = cscale(cl[l][e], norm);
+      eps[e] = cadd(eps[e], chi[e]);
+    }
+    if (ext) {
+      // chi0 (S x 3 x 3) then chi0_low (S x 3 x 3 x 3), then wave (9)
+      double2* c0 = ext + (size_t)w * (S_ * 36 + 9) + s * 9;
+      const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
+      double2 t[9];
+      for (int e = 0; e < 6; ++e) t[3 * ii[e] + jj[e]] = cdiv(chi[e], denom);
+      t[3] = cneg(t[1]);
+      t[6] = t[2];
+      t[7] = cneg(t[5]);
+      for (int q = 0; q < 9; ++q) c0[q] = t[q];
+      double2* c1 = ext + (size_t)w * (S_ * 36 + 9) + S_ * 9 + s * 27;
+      for (int l = 0; l < 3; ++l) {
+        double2 u[9];
+        for (int e = 0; e < 6; ++e) u[3 * ii[e] + jj[e]] = cdiv(cl[l][e], denom);
+        u[3] = cneg(u[1]);
+        u[6] = u[2];
+        u[7] = cneg(u[5]);
+        for (int q = 0; q < 9; ++q) c1[l * 9 + q] = u[q];
+      }
+    }
+  }
+  // eps entries: xx yy zz xy xz yz
+  double2 unit = a.sys.kperp_norm ? cmul(cscale(o, vA), cscale(o, vA))
+                                  : cmul(cscale(cscale(o, kperp), vA), cscale(cscale(o, kperp), vA));
+  double enx2, enz2, enxnz;
+  if (a.sys.kperp_norm) {
+    enx2 = kperp * kperp;
+    enz2 = kpar * kpar;
+    enxnz = kpar * kperp;
+  } else {
+    enx2 = kperp * kperp * kperp * kperp;
+    enz2 = kpar * kpar * kperp * kperp;
+    enxnz = kpar * kperp * kperp * kperp;
+  }
+  double2 w11 = csub(cadd(eps[0], unit), cmk(enz2, 0.0));
+  double2 w22 = csub(csub(cadd(eps[1], unit), cmk(enz2, 0.0)), cmk(enx2, 0.0));
+  double2 w33 = csub(cadd(eps[2], unit), cmk(enx2, 0.0));
+  double2 w13 = cadd(eps[4], cmk(enxnz, 0.0));
+  double2 w12 = eps[3];
+  double2 w23 = eps[5];
+  double2 det = cadd(cadd(csub(cadd(cmul(w11, cadd(cmul(w22, w33), cmul(w23, w23))),
+                                    cscale(cmul(cmul(w12, w23), w13), 2.0)),
+                               cmul(cmul(w13, w13), w22)),
+                          cmul(cmul(w12, w12), w33)),
+                     cmk(0.0, 0.0));
+  D[w] = det;
+  if (ext) {
+    double2* wv = ext + (size_t)w * (S_ * 36 + 9) + S_ * 36;
+    wv[0] = w11;
+    wv[1] = w12;
+    wv[2] = w13;
+    wv[3] = cneg(w12);
+    wv[4] = w22;
+    wv[5] = w23;
+    wv[6] = w13;
+    wv[7] = cneg(w23);
+    wv[8] = w33;
+  }
+}
+
+template <typename T>
+int ensure_buf(T*& ptr, size_t& cap, size_t n) {
+  if (n <= cap && ptr) return ALPS_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  ALPS_CUDA_TRY(cudaMalloc(&ptr, (n ? n : 1) * sizeof(T)));
+  cap = n;
+  return ALPS_OK;
+}
+
+}  // namespace
+
+void fill_sys_dev(const alps_ctx* c, SysDev* o) {
+  o->nspec = c->sys.nspec;
+  o->kperp_norm = c->sys.kperp_norm;
+  o->M_I = c->sys.positions_principal;
+  o->M_P = c->sys.n_resonance_interval;
+  o->Tlim = c->sys.Tlim;
+  o->vA = c->sys.vA;
+  o->kperp = c->kperp;
+  o->kpar = c->kpar;
+}
+
+void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
+  const SpeciesHost& S = c->spec[is];
+  o->N = c->sys.nperp;
+  o->M = c->sys.npar;
+  o->nmax = S.nmax;
+  o->nf = S.sp.ac_method == 1 ? S.sp.n_fits : 1;
+  o->ac_method = S.sp.ac_method;
+  o->log_fit = S.sp.log_fit;
+  for (int f = 0; f < ALPS_MAX_FITS; ++f) {
+    o->fit_type[f] = S.sp.fit_type[f];
+    o->perp_corr[f] = S.sp.perp_correction[f];
+  }
+  o->qs = S.sp.qs;
+  o->ms = S.sp.ms;
+  o->ns = S.sp.ns;
+  o->dpperp = S.pperp[2] - S.pperp[1];
+  o->dppar = S.ppar[2] - S.ppar[1];
+  o->dppar_abs = std::fabs(o->dppar);
+  o->species_index = is + 1;
+  o->int_ee = S.int_ee;
+  o->pperp = S.d_pperp;
+  o->ppar = S.d_ppar;
+  o->f0 = S.d_f0;
+  o->g1 = S.d_g1;
+  o->g2 = S.d_g2;
+  o->fit = S.d_fit;
+  o->bessel = S.d_bessel;
+  o->V = S.d_V;
+  o->rcap = S.rcap;
+}
+
+int collect_profile(alps_ctx* c) {
+  for (auto& ev : c->ev_pending) {
+    ALPS_CUDA_TRY(cudaEventSynchronize(ev[4]));
+    for (int q = 0; q < 4; ++q) {
+      float ms = 0.f;
+      ALPS_CUDA_TRY(cudaEventElapsedTime(&ms, ev[q], ev[q + 1]));
+      c->prof_ms[q] += ms;
+    }
+    c->prof_batches++;
+    for (auto e : ev) c->ev_pool.push_back(e);
+  }
+  c->ev_pending.clear();
+  return ALPS_OK;
+}
+
+// Runs the four kernels of one batch on stream st.
+int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext, cudaStream_t st) {
+  if (n <= 0) return ALPS_OK;
+  const int S_ = c->sys.nspec;
+  DispArgs a;
+  fill_sys_dev(c, &a.sys);
+  int maxn = 0, rc = 1;
+  for (int s = 0; s < S_; ++s) {
+    fill_spec_dev(c, s, &a.sp[s]);
+    maxn = std::max(maxn, c->spec[s].nmax);
+    rc = std::max(rc, c->spec[s].rcap);
+  }
+  a.rcap = rc;
+  // order chunks: enough blocks to fill the device for small batches
+  int js = 1;
+  if (n < 32) js = 32;
+  else if (n < 64) js = 4;
+  else if (n < 128) js = 2;
+  int TW = 128 / js;
+  int tiles = (n + TW - 1) / TW;
+  int want_blocks = 152 * 4;
+  int nchunk = std::max(1, std::min(maxn + 1, (want_blocks + tiles * S_ - 1) / (tiles * S_)));
+  a.csize = (maxn + 1 + nchunk - 1) / nchunk;
+  a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
+  int rcode;
+  if ((rcode = ensure_buf(c->d_part, c->part_cap, (size_t)n * S_ * a.nchunk * 6))) return rcode;
+  if ((rcode = ensure_buf(c->d_count, c->count_cap, (size_t)n * S_))) return rcode;
+  size_t nslots = (size_t)n * S_ * rc;
+  if (nslots * 6 > c->items_cap || !c->d_slot_nn) {
+    if (c->d_slot_nn) cudaFree(c->d_slot_nn);
+    c->d_slot_nn = nullptr;
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_slot_nn, nslots * sizeof(int)));
+    if ((rcode = ensure_buf(c->d_items, c->items_cap, nslots * 6))) return rcode;
+  }
+  bool want_low = d_ext != nullptr;
+  if (want_low)
+    if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * a.nchunk * 18))) return rcode;
+  if (!c->d_flags) ALPS_CUDA_TRY(cudaMalloc(&c->d_flags, sizeof(int)));
+  ALPS_CUDA_TRY(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
+
+  std::vector<cudaEvent_t> ev;
+  if (c->profiling) {
+    for (int q = 0; q < 5; ++q) {
+      cudaEvent_t e;
+      if (!c->ev_pool.empty()) {
+        e = c->ev_pool.back();
+        c->ev_pool.pop_back();
+      } else {
+        ALPS_CUDA_TRY(cudaEventCreate(&e));
+      }
+      ev.push_back(e);
+    }
+    ALPS_CUDA_TRY(cudaEventRecord(ev[0], st));
+  }
+  k_classify<<<dim3((n + 127) / 128, S_), 128, 0, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_flags);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[1], st));
+  dim3 g2(tiles, S_, a.nchunk);
+  if (want_low)
+    k_pole_sums<true><<<g2, 128, 0, st>>>(a, d_om, n, js, c->d_part, c->d_low);
+  else
+    k_pole_sums<false><<<g2, 128, 0, st>>>(a, d_om, n, js, c->d_part, nullptr);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
+  int maxN = c->sys.nperp;
+  size_t smem = (size_t)RES_WARPS * (RES_WIN * 6 + (maxN + 1)) * sizeof(double2);
+  if (smem > 48 * 1024) ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  long total = (long)nslots;
+  long blocks = (total + RES_WARPS - 1) / RES_WARPS;
+  k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_items,
+                                                             c->d_flags);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[3], st));
+  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, d_om, n, c->d_part, want_low ? c->d_low : nullptr, c->d_count,
+                                              c->d_slot_nn, c->d_items, d_D, d_ext);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  if (c->profiling) {
+    ALPS_CUDA_TRY(cudaEventRecord(ev[4], st));
+    c->ev_pending.push_back(ev);
+  }
+  c->stats.n_eval = n;
+  c->stats.kernels_launched = 4;
+  return ALPS_OK;
+}

@@ -1,0 +1,537 @@
+// setup_kernels.cu -- per-run and per-wavevector device preprocessing.
+//
+//   k_derivatives     derivative_f0 (src/ALPS_fns.f90:103-115), plus the
+//                     second RHS vector pperp*df/dppar - ppar*df/dpperp of resU
+//   k_int_ee          int_ee (src/ALPS_fns.f90:1457-1555)
+//   k_lm_fit          determine_param_fit + LM_nonlinear_fit
+//                     (src/ALPS_analyt.f90:365-728, 1183-1636)
+//   k_nmax            determine_nmax (src/ALPS_fns.f90:3971-4075)
+//   k_bessel_table    determine_bessel_array (src/ALPS_fns.f90:4214-4255)
+//   k_bessel_rows     weighted Bessel-product rows of the p_perp contraction
+//   k_dgemm           FP64 tiled GEMM for the contraction
+//   k_fold_reduced    reduced vectors V[n][j][12] of the omega pass
+#include <cmath>
+#include <cstdio>
+
+#include "alps_internal.cuh"
+#include "device_math.cuh"
+
+namespace {
+
+__global__ void k_derivatives(const double* __restrict__ f0, const double* __restrict__ pperp,
+                              const double* __restrict__ ppar, int N, int M, double* g1, double* g2,
+                              double* G) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int i = blockIdx.y + 1;
+  if (i > N - 1 || j > M - 1) return;
+  int L = M + 1;
+  double df1 = __ddiv_rn(__dsub_rn(f0[(i + 1) * L + j], f0[(i - 1) * L + j]),
+                         __dsub_rn(pperp[i + 1], pperp[i - 1]));
+  double df2 = __ddiv_rn(__dsub_rn(f0[i * L + j + 1], f0[i * L + j - 1]),
+                         __dsub_rn(ppar[j + 1], ppar[j - 1]));
+  double gg2 = __dsub_rn(__dmul_rn(pperp[i], df2), __dmul_rn(ppar[j], df1));
+  g1[i * L + j] = df1;
+  g2[i * L + j] = gg2;
+  // contraction RHS, row-major [(i-1)][g*(M-1) + (j-1)]
+  size_t row = (size_t)(i - 1) * 2 * (M - 1);
+  G[row + (j - 1)] = df1;
+  G[row + (M - 1) + (j - 1)] = gg2;
+}
+
+// ee term; weights w_perp(i) * w_par(j) of the reference's trapezoid.
+__global__ void k_int_ee(const double* __restrict__ g2, const double* __restrict__ ppar, int N, int M,
+                         double scale, double* out) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  int L = M + 1;
+  long total = (long)(N - 1) * (M - 1);
+  for (long t = threadIdx.x; t < total; t += blockDim.x) {
+    int i = (int)(t / (M - 1)) + 1, j = (int)(t % (M - 1)) + 1;
+    double wperp = (i <= N - 2) ? 2.0 : 1.0;
+    double wpar = (j == 1 || j == M - 1) ? 1.0 : 2.0;
+    acc += wperp * wpar * (ppar[j] * g2[i * L + j]);
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0] * scale;
+}
+
+// ---------------------------------------------------------------------------
+// Levenberg-Marquardt fit of the analytic continuation.  One thread walks the
+// iperp rows of one species in order (each row starts from the previous
+// result, src/ALPS_analyt.f90:518), with the reference's sums in its order.
+// ---------------------------------------------------------------------------
+struct FitArgs {
+  int N, M, nf, log_fit;
+  int fit_type[ALPS_MAX_FITS];
+  double pc[ALPS_MAX_FITS];
+  double ms, vA;
+  int maxsteps;
+  double lambda0, lambdafac, eps;
+};
+
+__device__ int fit_nparams(const FitArgs& a, int t) {
+  return (t == 1 || t == 3 || t == 5) ? 3 : (t == 2 ? 5 : (t == 6 ? 4 : 1));
+}
+
+// fit_function (src/ALPS_analyt.f90:185-266) at real ppar
+__device__ double fit_value_real(const FitArgs& a, const double* params, double pperp, double ppar) {
+  double ff = 0.0;
+  int par_ind = 0;
+  for (int ifit = 1; ifit <= a.nf; ++ifit) {
+    int t = a.fit_type[ifit - 1];
+    double pc = a.pc[ifit - 1];
+    const double* p = params + (ifit + par_ind) - 1;
+    double d = ppar - p[2];
+    if (t == 1) {
+      ff = ff + (p[0] * exp(-pc * (pperp * pperp))) * exp(-p[1] * (d * d));
+      par_ind += 2;
+    } else if (t == 2) {
+      double kp = 1.0 + p[1] * (d * d) + pc * p[4] * (pperp * pperp);
+      ff = ff + p[0] * exp(p[3] * log(kp));
+      par_ind += 4;
+    } else if (t == 3) {
+      double sq = sqrt(1.0 + ((pperp * pperp) + d * d) * a.vA * a.vA / (a.ms * a.ms));
+      ff = ff + p[0] * exp(-p[1] * sq);
+      par_ind += 2;
+    } else if (t == 6) {
+      double q = p[3] * pc * (pperp * pperp) + p[1] * (d * d);
+      ff = ff + p[0] * exp(0.5 * (q - exp(q)));
+      par_ind += 3;
+    }
+  }
+  return ff;
+}
+
+// determine_JT (src/ALPS_analyt.f90:1183-1389) for one ppar node
+__device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, double pperp, double ppar,
+                             double* J /* nJT */) {
+  int par_ind = 0, JT_ind = 0;
+  for (int ifit = 1; ifit <= a.nf; ++ifit) {
+    int t = a.fit_type[ifit - 1];
+    double pc = a.pc[ifit - 1];
+    const double* p = params + (ifit + par_ind) - 1;
+    double* Jp = J + (ifit + JT_ind) - 1;
+    double d = ppar - p[2];
+    if (t == 1) {
+      double e = exp(-p[1] * (d * d) - pc * (pperp * pperp));
+      Jp[0] = e;
+      Jp[1] = -((d * d)) * p[0] * e;
+      Jp[2] = 2.0 * p[1] * d * p[0] * e;
+      par_ind += 2;
+      JT_ind += 2;
+    } else if (t == 2) {
+      double kp = 1.0 + p[1] * (d * d) + pc * p[4] * (pperp * pperp);
+      double kpm = pow(kp, p[3] - 1.0);
+      Jp[0] = pow(kp, p[3]);
+      Jp[1] = p[0] * p[3] * kpm * (d * d);
+      Jp[2] = p[0] * p[3] * kpm * 2.0 * p[1] * (p[2] - ppar);
+      Jp[3] = log(kp) * p[0] * pow(kp, p[3]);
+      if (iperp == 0) {
+        JT_ind += 3;
+      } else {
+        Jp[4] = p[0] * p[3] * kpm * pc * (pperp * pperp);
+        JT_ind += 4;
+      }
+      par_ind += 4;
+    } else if (t == 3) {
+      double sq = sqrt(1.0 + ((pperp * pperp) + d * d) * a.vA * a.vA / (a.ms * a.ms));
+      Jp[0] = exp(-p[1] * sq);
+      Jp[1] = -p[0] * exp(-p[1] * sq) * sq;
+      Jp[2] = p[0] * exp(-p[1] * sq) * (p[1] / sq) * d * a.vA * a.vA / (a.ms * a.ms);
+      par_ind += 2;
+      JT_ind += 2;
+    } else if (t == 6) {
+      double q = p[3] * pc * (pperp * pperp) + p[1] * (d * d);
+      double e = exp(0.5 * (q - exp(q)));
+      Jp[0] = e;
+      Jp[1] = p[0] * e * 0.5 * (d * d) * (1.0 - exp(q));
+      Jp[2] = p[0] * e * p[1] * (p[2] - ppar) * (1.0 - exp(q));
+      if (iperp == 0) {
+        JT_ind += 2;
+      } else {
+        Jp[3] = p[0] * e * 0.5 * pc * (pperp * pperp) * (1.0 - exp(q));
+        JT_ind += 3;
+      }
+      par_ind += 3;
+    }
+  }
+}
+
+#define FIT_MAXP (5 * ALPS_MAX_FITS)
+
+// One thread per species: fit[(i*5+ip)*nf + ifit] holds the seeds at row 0
+// on entry and the fitted rows on exit.  scratch: (M+1)*(FIT_MAXP+1).
+__global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double* __restrict__ pperp,
+                         const double* __restrict__ ppar, double* fit, double* scratch, int* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int nf = a.nf, N = a.N, M = a.M;
+  int n_params = 0;
+  for (int f = 0; f < nf; ++f) n_params += fit_nparams(a, a.fit_type[f]);
+  double params[FIT_MAXP];
+  bool mask[FIT_MAXP];
+  double* JT = scratch;                         // [(M+1)][nJT]
+  double* resid = scratch + (size_t)(M + 1) * FIT_MAXP;
+  if ((1 + M) < n_params) {
+    *status = ALPS_E_FIT_POINTS;
+    return;
+  }
+  for (int iperp = 0; iperp <= N; ++iperp) {
+    if (iperp != 0)
+      for (int ip = 0; ip < 5; ++ip)
+        for (int f = 0; f < nf; ++f) fit[(iperp * 5 + ip) * nf + f] = fit[((iperp - 1) * 5 + ip) * nf + f];
+    int par_ind = 0, nJT = 0;
+    for (int k = 0; k < n_params; ++k) mask[k] = true;
+    for (int ifit = 1; ifit <= nf; ++ifit) {
+      int t = a.fit_type[ifit - 1];
+      int np = fit_nparams(a, t);
+      for (int k = 0; k < np; ++k) params[ifit + par_ind + k - 1] = fit[(iperp * 5 + k) * nf + ifit - 1];
+      if (t == 2 && iperp == 0) { nJT -= 1; mask[ifit + par_ind + 4 - 1] = false; }
+      if (t == 6 && iperp == 0) { nJT -= 1; mask[ifit + par_ind + 3 - 1] = false; }
+      par_ind += np - 1;
+    }
+    nJT += n_params;
+    double pp_perp = pperp[iperp];
+    double lambda_fit = a.lambda0, LSQ = 0.0, LSQnew;
+    int counter = 0;
+    bool converged = false;
+    while (!converged) {
+      counter++;
+      LSQ = 0.0;
+      for (int j = 0; j <= M; ++j) {
+        double* Jc = JT + (size_t)j * FIT_MAXP;
+        fit_jacobian(a, params, iperp, pp_perp, ppar[j], Jc);
+        double g = a.log_fit ? log(f0[iperp * (M + 1) + j]) : f0[iperp * (M + 1) + j];
+        double fv = fit_value_real(a, params, pp_perp, ppar[j]);
+        if (a.log_fit) {
+          for (int k = 0; k < nJT; ++k) Jc[k] = Jc[k] / fv;
+          resid[j] = g - log(fv);
+        } else {
+          resid[j] = g - fv;
+        }
+        LSQ = LSQ + resid[j] * resid[j];
+      }
+      double Am[FIT_MAXP * FIT_MAXP], jr[FIT_MAXP];
+      for (int k = 0; k < nJT; ++k) {
+        for (int l = 0; l < nJT; ++l) {
+          double acc = 0.0;
+          for (int j = 0; j <= M; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * JT[(size_t)j * FIT_MAXP + l];
+          Am[k + nJT * l] = acc;
+        }
+        double acc = 0.0;
+        for (int j = 0; j <= M; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * resid[j];
+        jr[k] = acc;
+      }
+      for (int k = 0; k < nJT; ++k) Am[k + nJT * k] = Am[k + nJT * k] + lambda_fit * Am[k + nJT * k];
+      // LU with partial pivoting (dgetrf), then inverse (dgetri) times JT*r
+      int piv[FIT_MAXP];
+      bool singular = false;
+      for (int k = 0; k < nJT && !singular; ++k) {
+        int p = k;
+        double mx = fabs(Am[k + nJT * k]);
+        for (int i = k + 1; i < nJT; ++i)
+          if (fabs(Am[i + nJT * k]) > mx) { mx = fabs(Am[i + nJT * k]); p = i; }
+        piv[k] = p;
+        if (Am[p + nJT * k] == 0.0) { singular = true; break; }
+        if (p != k)
+          for (int jj = 0; jj < nJT; ++jj) {
+            double tmp = Am[k + nJT * jj];
+            Am[k + nJT * jj] = Am[p + nJT * jj];
+            Am[p + nJT * jj] = tmp;
+          }
+        for (int i = k + 1; i < nJT; ++i) {
+          Am[i + nJT * k] /= Am[k + nJT * k];
+          for (int jj = k + 1; jj < nJT; ++jj) Am[i + nJT * jj] -= Am[i + nJT * k] * Am[k + nJT * jj];
+        }
+      }
+      if (singular) {
+        *status = ALPS_E_SINGULAR;
+        return;
+      }
+      double inv[FIT_MAXP * FIT_MAXP];
+      for (int cc = 0; cc < nJT; ++cc) {
+        double x[FIT_MAXP];
+        for (int i = 0; i < nJT; ++i) x[i] = (i == cc) ? 1.0 : 0.0;
+        for (int k = 0; k < nJT; ++k) {
+          double tmp = x[k];
+          x[k] = x[piv[k]];
+          x[piv[k]] = tmp;
+        }
+        for (int i = 0; i < nJT; ++i)
+          for (int k = 0; k < i; ++k) x[i] -= Am[i + nJT * k] * x[k];
+        for (int i = nJT - 1; i >= 0; --i) {
+          for (int k = i + 1; k < nJT; ++k) x[i] -= Am[i + nJT * k] * x[k];
+          x[i] /= Am[i + nJT * i];
+        }
+        for (int i = 0; i < nJT; ++i) inv[i + nJT * cc] = x[i];
+      }
+      double delta[FIT_MAXP];
+      for (int k = 0; k < nJT; ++k) {
+        double acc = 0.0;
+        for (int l = 0; l < nJT; ++l) acc += inv[k + nJT * l] * jr[l];
+        delta[k] = acc;
+      }
+      int l = 0;
+      for (int k = 0; k < n_params; ++k)
+        if (mask[k]) params[k] = params[k] + delta[l++];
+      LSQnew = 0.0;
+      for (int j = 0; j <= M; ++j) {
+        double g = a.log_fit ? log(f0[iperp * (M + 1) + j]) : f0[iperp * (M + 1) + j];
+        double fv = fit_value_real(a, params, pp_perp, ppar[j]);
+        double r = a.log_fit ? g - log(fv) : g - fv;
+        LSQnew = LSQnew + r * r;
+      }
+      if (LSQnew > LSQ) {
+        l = 0;
+        for (int k = 0; k < n_params; ++k)
+          if (mask[k]) params[k] = params[k] - delta[l++];
+        lambda_fit = lambda_fit * a.lambdafac;
+      } else {
+        lambda_fit = lambda_fit / a.lambdafac;
+      }
+      if (fabs(LSQnew - LSQ) < a.eps) converged = true;
+      if (counter == a.maxsteps) converged = true;
+    }
+    par_ind = 0;
+    for (int ifit = 1; ifit <= nf; ++ifit) {
+      int np = fit_nparams(a, a.fit_type[ifit - 1]);
+      for (int k = 0; k < np; ++k) fit[(iperp * 5 + k) * nf + ifit - 1] = params[ifit + par_ind + k - 1];
+      par_ind += np - 1;
+    }
+  }
+}
+
+// determine_nmax for one species: smallest n >= 1 with max_i |J_n(z_i)| <=
+// Bessel_zero.  One block, threads over iperp.
+__global__ void k_nmax(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero,
+                       int limit, int* nmax_out) {
+  __shared__ double red[256];
+  __shared__ int done;
+  int nn = 0;
+  if (threadIdx.x == 0) done = 0;
+  __syncthreads();
+  while (true) {
+    nn++;
+    double m = 0.0;
+    for (int i = threadIdx.x; i <= N; i += blockDim.x) {
+      double z = __ddiv_rn(__dmul_rn(kperp, pperp[i]), qs);
+      m = fmax(m, fabs(alps_bessj(nn, z)));
+    }
+    red[threadIdx.x] = m;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) done = !(red[0] > bzero) || nn >= limit;
+    __syncthreads();
+    if (done) break;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *nmax_out = nn;
+}
+
+// bessel[(n+1)*(N+1)+i] = J_n(k_perp pperp_i / q), n = -1 .. nmax+1
+__global__ void k_bessel_table(const double* __restrict__ pperp, int N, int nmax, double kperp, double qs,
+                               double* bessel) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int n = (int)blockIdx.y - 1;
+  if (i > N || n > nmax + 1) return;
+  double z = __ddiv_rn(__dmul_rn(kperp, pperp[i]), qs);
+  bessel[(size_t)(n + 1) * (N + 1) + i] = (n == -1) ? -alps_bessj(1, z) : alps_bessj(n, z);
+}
+
+// Rw[(F*(nmax+1) + n)*(N-1) + (i-1)] = w_perp(i) * R_F(n,i), F = 0: J_n^2,
+// 1: pperp^2 J_n'^2, 2: pperp J_n J_n' (the three Bessel-product families of
+// int_T), w_perp = 2 for i < N-1 and 1 at i = N-1.
+__global__ void k_bessel_rows(const double* __restrict__ bessel, const double* __restrict__ pperp, int N,
+                              int nmax, double* Rw) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int n = blockIdx.y;
+  if (i > N - 1 || n > nmax) return;
+  const double* B = bessel;
+  int L = N + 1;
+  double J = B[(size_t)(n + 1) * L + i];
+  double Jp = (n == 0) ? -B[(size_t)2 * L + i] : 0.5 * (B[(size_t)n * L + i] - B[(size_t)(n + 2) * L + i]);
+  double w = (i <= N - 2) ? 2.0 : 1.0;
+  double p = pperp[i];
+  size_t stride = (size_t)(nmax + 1) * (N - 1);
+  size_t o = (size_t)n * (N - 1) + (i - 1);
+  Rw[o] = w * (J * J);
+  Rw[stride + o] = w * ((p * p) * Jp * Jp);
+  Rw[2 * stride + o] = w * (p * J * Jp);
+}
+
+// C[m][n] = sum_k A[m][k] B[k][n], row-major, FP64, 32x32 tiles, 2x2 per thread.
+__global__ void k_dgemm(int Mr, int Nc, int K, const double* __restrict__ A, const double* __restrict__ B,
+                        double* C) {
+  __shared__ double As[32][17];
+  __shared__ double Bs[16][33];
+  int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  int row0 = blockIdx.y * 32, col0 = blockIdx.x * 32;
+  double acc[2][2] = {{0, 0}, {0, 0}};
+  for (int k0 = 0; k0 < K; k0 += 16) {
+    for (int t = threadIdx.x; t < 32 * 16; t += 256) {
+      int r = t / 16, kk = t % 16;
+      int gr = row0 + r, gk = k0 + kk;
+      As[r][kk] = (gr < Mr && gk < K) ? A[(size_t)gr * K + gk] : 0.0;
+    }
+    for (int t = threadIdx.x; t < 16 * 32; t += 256) {
+      int kk = t / 32, cc = t % 32;
+      int gk = k0 + kk, gc = col0 + cc;
+      Bs[kk][cc] = (gk < K && gc < Nc) ? B[(size_t)gk * Nc + gc] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      double a0 = As[ty * 2][kk], a1 = As[ty * 2 + 1][kk];
+      double b0 = Bs[kk][tx * 2], b1 = Bs[kk][tx * 2 + 1];
+      acc[0][0] = fma(a0, b0, acc[0][0]);
+      acc[0][1] = fma(a0, b1, acc[0][1]);
+      acc[1][0] = fma(a1, b0, acc[1][0]);
+      acc[1][1] = fma(a1, b1, acc[1][1]);
+    }
+    __syncthreads();
+  }
+  for (int a = 0; a < 2; ++a)
+    for (int b = 0; b < 2; ++b) {
+      int r = row0 + ty * 2 + a, cidx = col0 + tx * 2 + b;
+      if (r < Mr && cidx < Nc) C[(size_t)r * Nc + cidx] = acc[a][b];
+    }
+}
+
+// V[((n*(M-1)) + (j-1))*12 + 2*e + g] = 2 * c_e(j) * A[F(e)][n][g][j],
+// entries e = xx, yy, zz, xy, xz, yz; c = 1, 1, ppar^2, 1, ppar, ppar.
+__global__ void k_fold_reduced(const double* __restrict__ A, const double* __restrict__ ppar, int M, int nmax,
+                               double* V) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  int n = blockIdx.y;
+  if (j > M - 1 || n > nmax) return;
+  size_t ncol = 2 * (size_t)(M - 1);
+  auto Aat = [&](int F, int g) { return A[((size_t)F * (nmax + 1) + n) * ncol + (size_t)g * (M - 1) + (j - 1)]; };
+  double p = ppar[j];
+  double* v = V + ((size_t)n * (M - 1) + (j - 1)) * 12;
+  for (int g = 0; g < 2; ++g) {
+    double a0 = Aat(0, g), a1 = Aat(1, g), a2 = Aat(2, g);
+    v[0 + g] = 2.0 * a0;
+    v[2 + g] = 2.0 * a1;
+    v[4 + g] = 2.0 * ((p * p) * a0);
+    v[6 + g] = 2.0 * a2;
+    v[8 + g] = 2.0 * (p * a0);
+    v[10 + g] = 2.0 * (p * a2);
+  }
+}
+
+template <typename T>
+int ensure(T*& ptr, size_t& cap, size_t n) {
+  if (n <= cap && ptr) return ALPS_OK;
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+  cap = 0;
+  ALPS_CUDA_TRY(cudaMalloc(&ptr, n * sizeof(T)));
+  cap = n;
+  return ALPS_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+int launch_prepare_species(alps_ctx* c, int is) {
+  SpeciesHost& S = c->spec[is];
+  int N = c->sys.nperp, M = c->sys.npar;
+  cudaStream_t st = c->stream;
+  size_t nn = (size_t)(N + 1) * (M + 1);
+  if (!S.d_g1) ALPS_CUDA_TRY(cudaMalloc(&S.d_g1, nn * sizeof(double)));
+  if (!S.d_g2) ALPS_CUDA_TRY(cudaMalloc(&S.d_g2, nn * sizeof(double)));
+  if (!S.d_G) ALPS_CUDA_TRY(cudaMalloc(&S.d_G, (size_t)(N - 1) * 2 * (M - 1) * sizeof(double)));
+  ALPS_CUDA_TRY(cudaMemsetAsync(S.d_g1, 0, nn * sizeof(double), st));
+  ALPS_CUDA_TRY(cudaMemsetAsync(S.d_g2, 0, nn * sizeof(double), st));
+  dim3 grid((M - 1 + 127) / 128, N - 1);
+  k_derivatives<<<grid, 128, 0, st>>>(S.d_f0, S.d_pperp, S.d_ppar, N, M, S.d_g1, S.d_g2, S.d_G);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  // ee term: int_ee * 2*pi*q/m * dpperp*dppar/4
+  double dpperp = S.pperp[2] - S.pperp[1];
+  double dppar = std::fabs(S.ppar[2] - S.ppar[1]);
+  double scale = 2.0 * ALPS_PI * S.sp.qs / S.sp.ms * dpperp * dppar * 0.25;
+  double* d_ee = nullptr;
+  ALPS_CUDA_TRY(cudaMalloc(&d_ee, sizeof(double)));
+  k_int_ee<<<1, 256, 0, st>>>(S.d_g2, S.d_ppar, N, M, scale, d_ee);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  // LM fit of the analytic continuation (ACmethod 1)
+  int st_fit = ALPS_OK;
+  if (S.sp.ac_method == 1) {
+    FitArgs a;
+    a.N = N;
+    a.M = M;
+    a.nf = S.sp.n_fits;
+    a.log_fit = S.sp.log_fit;
+    for (int f = 0; f < ALPS_MAX_FITS; ++f) {
+      a.fit_type[f] = S.sp.fit_type[f];
+      a.pc[f] = S.sp.perp_correction[f];
+    }
+    a.ms = S.sp.ms;
+    a.vA = c->sys.vA;
+    a.maxsteps = c->sys.maxsteps_fit;
+    a.lambda0 = c->sys.lambda_initial_fit;
+    a.lambdafac = c->sys.lambdafac_fit;
+    a.eps = c->sys.epsilon_fit;
+    double* scratch = nullptr;
+    int* d_status = nullptr;
+    ALPS_CUDA_TRY(cudaMalloc(&scratch, (size_t)(M + 1) * (FIT_MAXP + 1) * sizeof(double)));
+    ALPS_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
+    ALPS_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+    k_lm_fit<<<1, 32, 0, st>>>(a, S.d_f0, S.d_pperp, S.d_ppar, S.d_fit, scratch, d_status);
+    ALPS_CUDA_TRY(cudaGetLastError());
+    ALPS_CUDA_TRY(cudaMemcpyAsync(&st_fit, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+    ALPS_CUDA_TRY(cudaStreamSynchronize(st));
+    cudaFree(scratch);
+    cudaFree(d_status);
+  }
+  double ee = 0.0;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(&ee, d_ee, sizeof(double), cudaMemcpyDeviceToHost, st));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(d_ee);
+  S.int_ee = ee;
+  return st_fit;
+}
+
+int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out) {
+  SpeciesHost& S = c->spec[is];
+  int* d_n = nullptr;
+  ALPS_CUDA_TRY(cudaMalloc(&d_n, sizeof(int)));
+  k_nmax<<<1, 256, 0, c->stream>>>(S.d_pperp, c->sys.nperp, kperp, S.sp.qs, c->sys.Bessel_zero, 2000, d_n);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  int nm = 0;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(&nm, d_n, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  cudaFree(d_n);
+  if (nm >= 2000) return ALPS_E_INVALID;  // orders beyond 2000 are outside the supported range
+  *nmax_out = nm;
+  return ALPS_OK;
+}
+
+int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
+  SpeciesHost& S = c->spec[is];
+  int N = c->sys.nperp, M = c->sys.npar, nmax = S.nmax;
+  cudaStream_t st = c->stream;
+  int rc;
+  if ((rc = ensure(S.d_bessel, S.bessel_cap, (size_t)(nmax + 3) * (N + 1)))) return rc;
+  if ((rc = ensure(S.d_Rw, S.Rw_cap, (size_t)3 * (nmax + 1) * (N - 1)))) return rc;
+  if ((rc = ensure(S.d_A, S.A_cap, (size_t)3 * (nmax + 1) * 2 * (M - 1)))) return rc;
+  if ((rc = ensure(S.d_V, S.V_cap, (size_t)(nmax + 1) * (M - 1) * 12))) return rc;
+  k_bessel_table<<<dim3((N + 1 + 127) / 128, nmax + 3), 128, 0, st>>>(S.d_pperp, N, nmax, kperp, S.sp.qs,
+                                                                       S.d_bessel);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_bessel_rows<<<dim3((N - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_bessel, S.d_pperp, N, nmax, S.d_Rw);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  int Mr = 3 * (nmax + 1), Nc = 2 * (M - 1), K = N - 1;
+  k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_fold_reduced<<<dim3((M - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_A, S.d_ppar, M, nmax, S.d_V);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  return ALPS_OK;
+}

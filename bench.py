@@ -1,0 +1,302 @@
+"""Benchmark of the det D(omega, k) hot path on one GB300 (or N replicas).
+
+Workload (one "step"): the complex-frequency map of the two-species plasma
+(protons + electrons, bi-Maxwellian, beta=1) on a 128x256 (p_perp, p_par)
+grid at k_perp d_p = 2, k_par d_p = 0.3, det D on a 512 x 512 lattice of
+omega in [0,3] x [-0.5,0.1] Omega_p; after the timed steps the 8 deepest map
+minima are polished by the secant method (roots/s, latency).  Inputs are
+synthetic (f0 tables from the restated generate_distribution formulas).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU oracle (the restatement of the Fortran
+reference, which cannot be built on this image) on the host cores, on a
+bounded sample of the same lattice.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from alps_gb300 import workloads  # noqa: E402
+from alps_gb300.sharding import shard_range  # noqa: E402
+
+METRIC = "D(omega,k) evals/s & roots/s at <=1e-8 rel vs FP64, vs plain GPU; p50/p99 latency"
+UNIT = "evals/s"
+
+
+def lattice(mp):
+    dr = (mp.omf - mp.omi) / (mp.nr - 1)
+    di = (mp.gamf - mp.gami) / (mp.ni - 1)
+    wr = mp.omi + dr * np.arange(mp.nr)
+    wi = mp.gami + di * np.arange(mp.ni)
+    return (wr[:, None] + 1j * wi[None, :]).ravel()
+
+
+def config_dict(w, nr, ni, world):
+    s = w["system"]
+    return {"workload": "map%dx%d_grid%dx%d_kperp%g_kpar%g" % (nr, ni, s.nperp, s.npar, s.kperp, s.kpar),
+            "species": 2, "nperp": s.nperp, "npar": s.npar, "kperp": s.kperp, "kpar": s.kpar,
+            "Bessel_zero": s.Bessel_zero, "lattice": [nr, ni], "omega_re": [0.0, 3.0], "omega_im": [-0.5, 0.1],
+            "l2": "inputs < L2; a 256 MiB buffer is written between timed steps",
+            "parallelism": "replicas%d" % world}
+
+
+class Clocks:
+    """nvidia-smi sampling (200 ms) during the timed region."""
+
+    def __init__(self, idx):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(idx), "--query-gpu=" + q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.f.read().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def fp64_peak_tflops(torch):
+    """Measured FP64 throughput of a cuBLAS DGEMM on this GPU (burst)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def pole_sum_flops(nmax, npar):
+    """Algorithmic FP64 flops of the non-resonant pole sums per evaluation:
+    150 per (order n >= 0, p_par node) covering +n and -n (2 complex
+    reciprocals, 3 numerators, 12 entry MACs; complex mul 6, add 2,
+    reciprocal 8)."""
+    return sum(150.0 * (n + 1) * (npar - 1) for n in nmax)
+
+
+def cpu_sample(P, oms, budget_s, nthreads):
+    """Times the oracle on a bounded sample of the lattice; returns evals/s."""
+    t0 = time.perf_counter()
+    P.disp_batch(oms[:1], nthreads=1)
+    t1 = time.perf_counter() - t0
+    m = int(max(nthreads, min(len(oms), budget_s * nthreads / max(t1, 1e-6))))
+    m = min(m, 512)
+    idx = np.linspace(0, len(oms) - 1, m).astype(int)
+    t0 = time.perf_counter()
+    P.disp_batch(oms[idx], nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    return m / dt, m, dt
+
+
+def run_reference(args, w, mp, rank, world):
+    if rank != 0:
+        return
+    from oracle import pyoracle as po
+    nthreads = os.cpu_count() or 1
+    system, species = workloads.build(w, po.generate_f0)
+    P = po.OraclePlasma(system, species)
+    P.set_k(system.kperp, system.kpar)
+    oms = lattice(mp)
+    budget = float(os.environ.get("ALPS_REF_STEP_S", "8"))
+    for _ in range(args.warmup):
+        cpu_sample(P, oms, min(budget, 2.0), nthreads)
+    rates, ms = [], []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r, m, dt = cpu_sample(P, oms, budget, nthreads)
+        rates.append(r)
+        ms.append(dt * 1e3)
+    wall = time.perf_counter() - t0
+    value = float(np.mean(rates))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(ms)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference", "config": config_dict(w, mp.nr, mp.ni, world),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "sample": "per step %d lattice points of the map, oracle threads over points" % m},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nr", type=int, default=512)
+    ap.add_argument("--ni", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus else 1)))
+    if "RANK" not in os.environ:
+        world = 1
+    w = workloads.config_map(args.nr, args.ni)
+    mp = w["extra"]["map"]
+    if args.impl == "reference":
+        run_reference(args, w, mp, rank, world)
+        return
+
+    import torch
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from alps_gb300 import api
+    # weak scaling: every replica evaluates a full lattice at its own k_par
+    s = w["system"]
+    kpar = s.kpar * (1.0 + 0.01 * rank)
+    system, species = workloads.build(w, api.generate_f0)
+    G = api.Plasma(system, species)
+    G.set_k(s.kperp, kpar)
+    nmax = G.nmax()
+    oms = lattice(mp)
+    n = len(oms)
+    om_dev = torch.from_numpy(np.stack([oms.real, oms.imag], 1).copy()).cuda()
+    D_dev = torch.empty_like(om_dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+
+    def step():
+        G.disp_batch_device(n, om_dev.data_ptr(), D_dev.data_ptr(), sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    peak64 = fp64_peak_tflops(torch)
+    G.set_profiling(True)
+    clocks = Clocks(local)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+        flush.fill_(1.0)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    t = e0.elapsed_time(e1) / 1e3
+    if dist:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    prof_ms, nb = G.profile()
+    G.set_profiling(False)
+    value = world * n * args.steps / t
+    ms_step = t / args.steps * 1e3
+    st = G.stats()
+
+    # roofline of the dominant kernel (pole sums): FP64 pipe
+    pole_ms = prof_ms[1] / max(nb, 1)
+    flops = pole_sum_flops(nmax, s.npar) * n
+    achieved = flops / (pole_ms / 1e3) / 1e12
+    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
+                "frac": achieved / peak64, "traffic": None,
+                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (burst)",
+                "kernel": "k_pole_sums", "kernel_ms": pole_ms,
+                "kernel_share": prof_ms[1] / max(sum(prof_ms), 1e-30),
+                "per_kernel_ms": dict(zip(["classify", "pole_sums", "resonant", "finalize"],
+                                          [x / max(nb, 1) for x in prof_ms]))}
+
+    # end to end through the C-ABI with host buffers (copies included)
+    Dh = G.disp_batch(oms)
+    t0 = time.perf_counter()
+    for _ in range(max(1, args.steps)):
+        Dh = G.disp_batch(oms)
+    e2e_t = (time.perf_counter() - t0) / max(1, args.steps)
+    e2e = {"value": n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
+
+    # polish the 8 deepest minima (roots/s, latency per root solve)
+    val = np.log10(np.abs(Dh))
+    mins = api.find_minima(val, mp.nr, mp.ni, numroots=100)
+    mins = sorted(mins, key=lambda ij: val[ij[0] * mp.ni + ij[1]])[:w["extra"]["n_polish"]]
+    guesses = np.array([oms[i * mp.ni + j] for i, j in mins])
+    lat = []
+    for g in guesses:
+        t0 = time.perf_counter()
+        G.secant([g])
+        lat.append((time.perf_counter() - t0) * 1e3)
+    t0 = time.perf_counter()
+    roots, iters, _ = G.secant(guesses)
+    t_roots = time.perf_counter() - t0
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import pyoracle as po
+        nthreads = os.cpu_count() or 1
+        P = po.OraclePlasma(system, species)
+        P.set_k(s.kperp, kpar)
+        r, m, dt = cpu_sample(P, oms, float(os.environ.get("ALPS_CPU_BASELINE_S", "10")), nthreads)
+        cpu = {"value": r, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": "%d lattice points of the same map (every %d-th), oracle threads over points, %.1f s"
+                         % (m, max(1, n // m), dt)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "precision_path": G.precision,
+                "config": config_dict(w, mp.nr, mp.ni, world), "nmax": nmax,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": int(st.kernels_launched) * args.steps,
+                "roots": {"count": len(roots), "roots_per_s": len(roots) / t_roots, "iterations": iters,
+                          "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
+                                         "p99": float(np.percentile(lat, 99)) if lat else None},
+                          "roots": [[r.real, r.imag] for r in roots]}}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

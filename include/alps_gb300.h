@@ -135,6 +135,11 @@ int alps_prepare(alps_ctx* ctx);
  * src/ALPS_var.f90:276). */
 int alps_get_fit(alps_ctx* ctx, int is, double* out);
 
+/* Replaces the fitted parameters of species is (same layout as
+ * alps_get_fit), e.g. to share one fit between two evaluators.  No reference
+ * counterpart: there the fit lives in the param_fit global. */
+int alps_set_fit(alps_ctx* ctx, int is, const double* in);
+
 /* Per-wavevector setup on the device: nmax from the Bessel cutoff, Bessel
  * table, and the omega-independent p_perp contraction.
  * Replaces determine_nmax + determine_bessel_array
@@ -220,6 +225,13 @@ typedef struct alps_stats {
   int kernels_launched;       /* kernels launched by the last disp batch      */
 } alps_stats;
 int alps_get_stats(alps_ctx* ctx, alps_stats* st);
+
+/* Measurement support: when on, every disp batch records CUDA events around
+ * its four kernels (classify, pole sums, resonant items, finalize) on the
+ * stream it runs on; alps_get_profile returns the summed device milliseconds
+ * per kernel and the number of batches since profiling was switched on. */
+int alps_set_profiling(alps_ctx* ctx, int on);
+int alps_get_profile(alps_ctx* ctx, double* ms /* [4] */, int64_t* batches);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,161 @@
+"""Parity of the CUDA path with the CPU oracle (FP64 plain path).
+
+Tolerances (FP64 path):
+  chi entries: |chi_gpu - chi_oracle| <= 1e-10 * max(|chi_oracle|, floor),
+  with floor = 1e-9 * max|chi| of the species (entries that cancel to ~0);
+  det D: relative 1e-10 to max(|D|, 1e-9 * sum of |terms|) -- same idea;
+  roots: relative 1e-9 in complex omega.
+The summation order differs from the reference (the p_perp sum runs first),
+so results agree to rounding, not bitwise; index decisions (nmax, resonance
+windows) are bitwise identical.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from alps_gb300 import _abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+CHI_RTOL = 1e-10
+ROOT_RTOL = 1e-9
+
+
+def _oracle():
+    from oracle import pyoracle as po
+    po.set_threads(os.cpu_count() or 1)
+    return po
+
+
+@pytest.fixture(scope="module")
+def api():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from alps_gb300 import api as A
+    return A
+
+
+def _pair(api, w, share_fit=True):
+    po = _oracle()
+    system, species = workloads.build(w, po.generate_f0)
+    O = po.OraclePlasma(system, species)
+    G = api.Plasma(system, species)
+    if share_fit:
+        for i in range(system.nspec):
+            G.set_fit(i, O.get_fit(i))
+    return O, G
+
+
+def _small(kperp=1.0, kpar=0.3, nperp=24, npar=48, bz=1e-14, me=1.0 / 1836.0):
+    return workloads.proton_electron(nperp, npar, kperp, kpar, bz, me=me)
+
+
+def _chi_close(a, b, what):
+    for s in range(a.shape[0]):
+        scale = max(np.abs(b[s]).max(), 1e-300)
+        err = np.abs(a[s] - b[s])
+        tol = CHI_RTOL * np.maximum(np.abs(b[s]), 1e-9 * scale)
+        assert np.all(err <= tol), (what, s, (err / np.maximum(np.abs(b[s]), 1e-9 * scale)).max())
+
+
+OMEGAS = [0.45 - 0.2j, 0.45 + 0.2j, 1.3 - 0.004j, 0.9 + 0.003j, 0.7 + 0.0j, 2.2 - 0.35j, 0.05 - 0.01j,
+          1.0 + 0.05j]
+
+
+def test_nmax_and_bessel_table_match(api):
+    O, G = _pair(api, _small())
+    for k in [(1.0, 0.3), (2.0, 0.3), (0.3, 1.0)]:
+        O.set_k(*k)
+        G.set_k(*k)
+        assert O.nmax() == G.nmax()
+
+
+def test_fit_matches_oracle(api):
+    po = _oracle()
+    w = _small()
+    system, species = workloads.build(w, po.generate_f0)
+    O = po.OraclePlasma(system, species)
+    G = api.Plasma(system, species)
+    for i in range(system.nspec):
+        a, b = G.get_fit(i), O.get_fit(i)
+        scale = np.abs(b).max()
+        assert np.abs(a - b).max() <= 1e-10 * scale
+
+
+@pytest.mark.parametrize("k", [(1.0, 0.3), (2.0, 0.15)])
+def test_disp_chi_parity_small(api, k):
+    O, G = _pair(api, _small())
+    O.set_k(*k)
+    G.set_k(*k)
+    for om in OMEGAS:
+        Do, co, clo, wo = O.disp(om)
+        Dg, cg, clg, wg = G.disp(om)
+        _chi_close(cg, co, "chi0 %s" % om)
+        _chi_close(clg.reshape(-1, 9), clo.reshape(-1, 9), "chi0_low %s" % om)
+        scale = np.abs(wo).max() ** 3
+        assert abs(Dg - Do) <= CHI_RTOL * max(abs(Do), 1e-6 * scale), (om, Dg, Do)
+
+
+def test_disp_batch_matches_single(api):
+    O, G = _pair(api, _small())
+    G.set_k(1.0, 0.3)
+    oms = np.array(OMEGAS)
+    Db = G.disp_batch(oms)
+    for om, d in zip(oms, Db):
+        assert G.disp(om)[0] == d
+
+
+def test_disp_parity_kpar_fast(api):
+    w = workloads.kpar_fast(nproc=4)
+    O, G = _pair(api, w)
+    O.set_k(*w["k"])
+    G.set_k(*w["k"])
+    assert G.nmax() == [21, 13]
+    for om in [9.9e-3 - 5.5e-6j, 1.2e-2 - 1e-6j, 9.9e-3 + 2e-4j]:
+        Do, co, _, _ = O.disp(om)
+        Dg, cg, _, _ = G.disp(om)
+        _chi_close(cg, co, "chi0 kpar_fast %s" % om)
+
+
+def test_secant_parity(api):
+    O, G = _pair(api, _small())
+    O.set_k(1.0, 0.3)
+    G.set_k(1.0, 0.3)
+    for method in (2, 0, 1):
+        guess = 0.3 - 0.05j
+        ro, ito, _ = O.secant(guess, method)
+        rg, itg, _ = G.secant([guess], method)
+        assert abs(rg[0] - ro) <= ROOT_RTOL * abs(ro), (method, rg[0], ro)
+
+
+def test_map_and_minima_parity(api):
+    po = _oracle()
+    O, G = _pair(api, _small(nperp=16, npar=32, bz=1e-10))
+    O.set_k(1.0, 0.3)
+    G.set_k(1.0, 0.3)
+    mp = _abi.alps_map_params()
+    mp.omi, mp.omf, mp.gami, mp.gamf, mp.nr, mp.ni = 0.05, 1.5, -0.3, 0.05, 12, 8
+    mp.loggridw = mp.loggridg = 0
+    omo, calo, valo = O.map(mp, nthreads=os.cpu_count() or 1)
+    omg, calg, valg = G.map_search(mp)
+    assert np.array_equal(omo, omg)
+    rel = np.abs(calg - calo) / np.maximum(np.abs(calo), 1e-300)
+    assert rel.max() < 1e-9
+    assert po.find_minima(valo, 12, 8) == api.find_minima(valg, 12, 8)
+
+
+@pytest.mark.slow
+def test_kpar_fast_scan_on_gpu_matches_golden(api, golden_dir):
+    w = workloads.kpar_fast(nproc=4)
+    system, species = workloads.build(w, api.generate_f0)
+    G = api.Plasma(system, species)
+    G.set_k(*w["k"])
+    om, _, _ = G.secant([w["extra"]["guess"][0]])
+    sc = w["extra"]["scan"]
+    rows, _ = G.om_scan(sc["type_s"], sc["swi"], sc["swf"], sc["log_scan"], sc["n_out"], sc["n_res"], om)
+    gold = np.loadtxt(os.path.join(golden_dir, "ref", "test_kpar_fast.scan_kpara_1.root_1"))
+    rows = rows[:, 0, :]
+    np.testing.assert_allclose(rows, gold, rtol=1e-2)
+    for a, b in zip(rows.ravel(), gold.ravel()):
+        assert ("%.4E" % a) == ("%.4E" % b), (a, b)
