@@ -18,10 +18,13 @@ HEADERS = ["alps_internal.cuh", "device_math.cuh"]
 
 
 def _flags(src):
-    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-I", os.path.join(HERE, "..", "include")]
+    # host code: no FMA contraction (aarch64 g++ contracts a+b*c by default),
+    # so host-side grids and scan steps round like the reference's
+    common = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+              "-I", os.path.join(HERE, "..", "include")]
     if src.endswith(".cu"):
         return ARCH + ["-lineinfo", "-Xptxas", "-O3"] + common
-    return common
+    return ["-x", "c++"] + common
 
 
 def _compile(src):

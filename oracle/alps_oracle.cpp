@@ -761,7 +761,8 @@ void nmax_bump(oracle_ctx* c) {
 }
 
 // disp (src/ALPS_fns.f90:252-636)
-cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx* wave_out) {
+cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx* wave_out,
+          double* mag_out = nullptr) {
   int nspec = c->sys.nspec;
   double kperp = c->kperp, kpar = c->kpar, vA = c->sys.vA;
   std::vector<cplx> chi(nspec * 9, cplx(0, 0)), chi_low(nspec * 27, cplx(0, 0));
@@ -806,6 +807,19 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
     for (size_t w = 0; w < work.size(); ++w) do_item(w);
   }
   size_t wi = 0;
+  // mag[s][i][j]: sum over orders of |contribution| * |n q| (the scale of the
+  // rounding error of any summation order of chi_ij)
+  std::vector<double> mag(nspec * 9, 0.0);
+  for (size_t w = 0; w < work.size(); ++w) {
+    const Rank& r = ranks[work[w].first];
+    double nrm = std::fabs(c->spec[r.sproc - 1].sp.ns * c->spec[r.sproc - 1].sp.qs);
+    const int ent[6][3] = {{0, 0, 1}, {1, 1, 2}, {2, 2, 3}, {0, 1, 4}, {0, 2, 5}, {1, 2, 6}};
+    for (int q = 0; q < 6; ++q) {
+      int mode = ent[q][2];
+      double m = std::abs(res[w].plus[mode]) + std::abs(res[w].minus[mode]);
+      mag[(r.sproc - 1) * 9 + 3 * ent[q][0] + ent[q][1]] += m * nrm;
+    }
+  }
   for (const Rank& r : ranks) {
     int sproc = r.sproc;
     const Species& s = c->spec[sproc - 1];
@@ -838,6 +852,8 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
     }
     if (r.nlim1 == 0) {
       cplx ee = int_ee(e);
+      mag[(sproc - 1) * 9 + 8] += std::abs(ee) * std::fabs(s.sp.ns * s.sp.qs) *
+                                  (c->sys.kperp_norm ? 1.0 : kperp * kperp);
       if (c->sys.kperp_norm) {
         CH(schi, sproc, 3, 3) = CH(schi, sproc, 3, 3) + ee;
         CL(slow, sproc, 3, 3, 0) = CL(slow, sproc, 3, 3, 0) + ee;
@@ -856,6 +872,15 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
     // MPI_REDUCE (:519-523), summed in rank order
     for (size_t k = 0; k < chi.size(); ++k) chi[k] += schi[k];
     for (size_t k = 0; k < chi_low.size(); ++k) chi_low[k] += slow[k];
+  }
+  if (mag_out) {
+    for (int is = 0; is < nspec; ++is) {
+      double* m = &mag[is * 9];
+      m[3] = m[1];
+      m[6] = m[2];
+      m[7] = m[5];
+    }
+    std::copy(mag.begin(), mag.end(), mag_out);
   }
   cplx enx2, enz2, enxnz;
   if (c->sys.kperp_norm) {
@@ -1380,6 +1405,12 @@ int oracle_disp(oracle_ctx* c, alps_complex om, alps_complex* D, alps_complex* c
   if (chi0) for (int k = 0; k < ns * 9; ++k) chi0[k] = to_c(a[k]);
   if (chi0_low) for (int k = 0; k < ns * 27; ++k) chi0_low[k] = to_c(b[k]);
   if (wave) for (int k = 0; k < 9; ++k) wave[k] = to_c(w[k]);
+  return ALPS_OK;
+}
+
+int oracle_disp_mag(oracle_ctx* c, alps_complex om, double* mag) {
+  if (!c || !c->kset || !mag) return ALPS_E_INVALID;
+  disp(c, from_c(om), nullptr, nullptr, nullptr, mag);
   return ALPS_OK;
 }
 

@@ -38,6 +38,10 @@ int oracle_get_bessel(oracle_ctx* ctx, int is, double* out);
 int oracle_disp(oracle_ctx* ctx, alps_complex om, alps_complex* D,
                 alps_complex* chi0, alps_complex* chi0_low,
                 alps_complex* wave);
+/* Per species and entry, the sum over Bessel orders of |contribution| (times
+ * |n_s q_s|), i.e. the scale of the rounding error of chi_ij under any
+ * summation order: mag[s*9 + 3*i + j]. */
+int oracle_disp_mag(oracle_ctx* ctx, alps_complex om, double* mag);
 int oracle_disp_batch(oracle_ctx* ctx, int n, const alps_complex* om,
                       alps_complex* D, int nthreads);
 int oracle_full_integrate(oracle_ctx* ctx, int is, alps_complex om, int nn,

@@ -55,6 +55,7 @@ def lib():
             L.oracle_get_nmax.argtypes = [C.c_void_p, P(C.c_int)]
             L.oracle_get_bessel.argtypes = [C.c_void_p, C.c_int, dp]
             L.oracle_disp.argtypes = [C.c_void_p, alps_complex, cp, cp, cp, cp]
+            L.oracle_disp_mag.argtypes = [C.c_void_p, alps_complex, dp]
             L.oracle_disp_batch.argtypes = [C.c_void_p, C.c_int, cp, cp, C.c_int]
             L.oracle_full_integrate.argtypes = [C.c_void_p, C.c_int, alps_complex, C.c_int, C.c_int, cp, P(C.c_int)]
             L.oracle_int_ee.argtypes = [C.c_void_p, C.c_int, alps_complex, cp]
@@ -180,6 +181,12 @@ class OraclePlasma:
                                _cptr(wave)), "oracle_disp")
         return complex(D.re, D.im), chi0.reshape(self.nspec, 3, 3), chil.reshape(self.nspec, 3, 3, 3), \
             wave.reshape(3, 3)
+
+    def disp_mag(self, om):
+        """Sum over orders of |chi_ij contributions| per species [s,i,j]."""
+        out = np.zeros(self.nspec * 9)
+        _chk(lib().oracle_disp_mag(self._h, alps_complex(om.real, om.imag), _dptr(out)), "oracle_disp_mag")
+        return out.reshape(self.nspec, 3, 3)
 
     def disp_batch(self, oms, nthreads=1):
         oms = np.ascontiguousarray(oms, dtype=np.complex128)

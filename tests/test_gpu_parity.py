@@ -1,9 +1,15 @@
 """Parity of the CUDA path with the CPU oracle (FP64 plain path).
 
 Tolerances (FP64 path):
-  chi entries: |chi_gpu - chi_oracle| <= 1e-10 * max(|chi_oracle|, floor),
-  with floor = 1e-9 * max|chi| of the species (entries that cancel to ~0);
-  det D: relative 1e-10 to max(|D|, 1e-9 * sum of |terms|) -- same idea;
+  chi entries: |chi_gpu - chi_oracle| <= 1e-10 * max(|chi_ij|, 1e-3 * mag_ij)
+    where mag_ij = sum over Bessel orders of |contribution to chi_ij| (the
+    oracle reports it).  Entries that are small differences of large order
+    terms (e.g. electron chi_xx at omega << Omega_e, where the n = +-1 terms
+    cancel to 1 part in 1e5) carry rounding of order eps * mag_ij in ANY FP64
+    summation order, the reference's included; the floor keeps the 1e-10
+    relative gate meaningful for them.
+  det D: first-order propagation of the chi bound through the cofactors of
+    the wave tensor, |dD| <= 1e-10 * sum_ij |cof_ij| * max(|w_ij|, 1e-3 mag_ij).
   roots: relative 1e-9 in complex omega.
 The summation order differs from the reference (the p_perp sum runs first),
 so results agree to rounding, not bitwise; index decisions (nmax, resonance
@@ -51,12 +57,30 @@ def _small(kperp=1.0, kpar=0.3, nperp=24, npar=48, bz=1e-14, me=1.0 / 1836.0):
     return workloads.proton_electron(nperp, npar, kperp, kpar, bz, me=me)
 
 
-def _chi_close(a, b, what):
-    for s in range(a.shape[0]):
-        scale = max(np.abs(b[s]).max(), 1e-300)
-        err = np.abs(a[s] - b[s])
-        tol = CHI_RTOL * np.maximum(np.abs(b[s]), 1e-9 * scale)
-        assert np.all(err <= tol), (what, s, (err / np.maximum(np.abs(b[s]), 1e-9 * scale)).max())
+def _chi_close(a, b, mag, what):
+    """a, b: [S, 9] chi values (GPU, oracle); mag: [S, 9] order-sum scales
+    (in the same units as a and b)."""
+    a, b, mag = (np.asarray(x).reshape(len(x), -1) for x in (a, b, mag))
+    scale = np.maximum(np.abs(b), 1e-3 * mag)
+    err = np.abs(a - b)
+    ok = err <= CHI_RTOL * scale + 1e-300
+    assert np.all(ok), (what, (err / np.maximum(scale, 1e-300)).max())
+
+
+def _disp_close(O, G, om, what):
+    Do, co, clo, wo = O.disp(om)
+    Dg, cg, clg, wg = G.disp(om)
+    mag = O.disp_mag(om)                       # units of chi (before / om^2 vA^2)
+    denom = abs(om * om) * O.sys.vA ** 2 if O.sys.kperp_norm else abs(om * om) * O.sys.vA ** 2 * O.sys.kperp ** 2
+    mag0 = mag / denom                        # units of chi0
+    _chi_close(cg, co, mag0, "chi0 " + what)
+    _chi_close(clg.reshape(len(clg), 3, 9), clo.reshape(len(clo), 3, 9),
+               np.repeat(mag0.reshape(len(mag0), 1, 9), 3, axis=1), "chi0_low " + what)
+    # det D: cofactor propagation of the chi bound
+    cof = np.array([[np.linalg.det(np.delete(np.delete(wo, i, 0), j, 1)) for j in range(3)] for i in range(3)])
+    magw = mag.sum(axis=0)
+    bound = CHI_RTOL * np.sum(np.abs(cof) * np.maximum(np.abs(wo), 1e-3 * magw))
+    assert abs(Dg - Do) <= max(bound, 1e-12 * abs(Do)), (what, Dg, Do, bound)
 
 
 OMEGAS = [0.45 - 0.2j, 0.45 + 0.2j, 1.3 - 0.004j, 0.9 + 0.003j, 0.7 + 0.0j, 2.2 - 0.35j, 0.05 - 0.01j,
@@ -89,21 +113,21 @@ def test_disp_chi_parity_small(api, k):
     O.set_k(*k)
     G.set_k(*k)
     for om in OMEGAS:
-        Do, co, clo, wo = O.disp(om)
-        Dg, cg, clg, wg = G.disp(om)
-        _chi_close(cg, co, "chi0 %s" % om)
-        _chi_close(clg.reshape(-1, 9), clo.reshape(-1, 9), "chi0_low %s" % om)
-        scale = np.abs(wo).max() ** 3
-        assert abs(Dg - Do) <= CHI_RTOL * max(abs(Do), 1e-6 * scale), (om, Dg, Do)
+        _disp_close(O, G, om, "%s k=%s" % (om, k))
 
 
 def test_disp_batch_matches_single(api):
+    # the split of the p_par sums over threads depends on the batch size, so a
+    # value alone and in a batch agree to rounding; the same batch twice is
+    # bitwise identical (fixed summation order, no atomics)
     O, G = _pair(api, _small())
     G.set_k(1.0, 0.3)
     oms = np.array(OMEGAS)
     Db = G.disp_batch(oms)
+    assert np.array_equal(Db, G.disp_batch(oms))
     for om, d in zip(oms, Db):
-        assert G.disp(om)[0] == d
+        s = G.disp(om)[0]
+        assert abs(s - d) <= 1e-13 * abs(d)
 
 
 def test_disp_parity_kpar_fast(api):
@@ -113,9 +137,7 @@ def test_disp_parity_kpar_fast(api):
     G.set_k(*w["k"])
     assert G.nmax() == [21, 13]
     for om in [9.9e-3 - 5.5e-6j, 1.2e-2 - 1e-6j, 9.9e-3 + 2e-4j]:
-        Do, co, _, _ = O.disp(om)
-        Dg, cg, _, _ = G.disp(om)
-        _chi_close(cg, co, "chi0 kpar_fast %s" % om)
+        _disp_close(O, G, om, "kpar_fast %s" % om)
 
 
 def test_secant_parity(api):
