@@ -59,6 +59,7 @@ def lib():
             "alps_generate_f0": ([P(_abi.alps_dist_params), C.c_int, C.c_int, dp, dp, dp, dp], C.c_int),
             "alps_get_stats": ([vp, P(_abi.alps_stats)], C.c_int),
             "alps_set_profiling": ([vp, C.c_int], C.c_int),
+            "alps_disp_batch_noalloc": ([vp, C.c_int, vp, vp, vp, P(C.c_size_t)], C.c_int),
             "alps_get_profile": ([vp, dp, P(C.c_int64)], C.c_int),
         }
         for name, (args, res) in sig.items():
@@ -82,5 +83,5 @@ def exported_symbols():
         "alps_destroy", "alps_set_species", "alps_prepare", "alps_get_fit", "alps_set_fit", "alps_set_k",
         "alps_get_nmax", "alps_set_precision", "alps_disp", "alps_disp_batch", "alps_disp_batch_device",
         "alps_secant", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
-        "alps_set_profiling", "alps_get_profile",
+        "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc",
     ]

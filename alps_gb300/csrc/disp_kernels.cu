@@ -17,8 +17,10 @@
 //                 one warp per item
 //   k_finalize    chi, epsilon, wave tensor and det, one thread per omega;
 //                 sums in a fixed order, so results do not depend on timing.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "alps_internal.cuh"
 #include "device_math.cuh"
@@ -705,5 +707,120 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   }
   c->stats.n_eval = n;
   c->stats.kernels_launched = 4;
+  return ALPS_OK;
+}
+
+// ===========================================================================
+// det D batch without any device allocation.
+//
+// Some callers cannot let this library allocate device memory while they
+// run: a host application whose own caching allocator owns the device heap
+// and must see every byte, a real-time loop that cannot afford the implicit
+// device-wide synchronisation of cudaMalloc/cudaFree, or a plugin host that
+// forbids plugins from creating allocations behind its back.  For them,
+// alps_disp_batch_noalloc runs the same four kernels as
+// alps_disp_batch_device with all of their scratch (partial sums,
+// resonant-order slots, resonant results, error flag) carved from the
+// file-scope device array below instead of context buffers.
+//
+// The array is ALPS_NOALLOC_SCRATCH_BYTES (16 MiB) and lives on every device
+// that loads this library until the process exits.  Its device address is
+// looked up once per device with cudaGetSymbolAddress, by the first call on
+// that device (with that device current); make that first call before any
+// stream capture.  Every call shares the one array: two calls whose kernels
+// overlap on the GPU (different streams, or different host threads) race on
+// it and must be ordered by the caller.  The error flag is cleared at the
+// start of every call; every other word a call reads it writes first.
+// ===========================================================================
+#define ALPS_NOALLOC_SCRATCH_BYTES (16u << 20)
+#define ALPS_NOALLOC_MAX_DEVICES 64
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ALPS_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noalloc_mu;
+void* g_noalloc_addr[ALPS_NOALLOC_MAX_DEVICES] = {nullptr};
+
+// 256-byte aligned carve-out of n bytes from the scratch array
+inline size_t carve(size_t& off, size_t bytes) {
+  size_t at = (off + 255) & ~(size_t)255;
+  off = at + bytes;
+  return at;
+}
+}  // namespace
+
+extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d_om, alps_complex* d_D,
+                                       void* stream, size_t* scratch_bytes) {
+  if (!c || n < 0 || !c->kset) return ALPS_E_INVALID;
+  if (n == 0) return ALPS_OK;
+  if (!d_om || !d_D) return ALPS_E_INVALID;
+  int dev = -1;
+  ALPS_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= ALPS_NOALLOC_MAX_DEVICES) return ALPS_E_INVALID;
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        alps_set_last_cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)", __FILE__, __LINE__);
+        return ALPS_E_CUDA;
+      }
+      g_noalloc_addr[dev] = p;
+    }
+    base = g_noalloc_addr[dev];
+  }
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  const int S_ = c->sys.nspec;
+  DispArgs a;
+  fill_sys_dev(c, &a.sys);
+  int maxn = 0, rc = 1;
+  for (int s = 0; s < S_; ++s) {
+    fill_spec_dev(c, s, &a.sp[s]);
+    maxn = std::max(maxn, c->spec[s].nmax);
+    rc = std::max(rc, c->spec[s].rcap);
+  }
+  a.rcap = rc;
+  int js = 1;
+  if (n < 32) js = 32;
+  else if (n < 64) js = 4;
+  else if (n < 128) js = 2;
+  int TW = 128 / js;
+  int tiles = (n + TW - 1) / TW;
+  int nchunk = std::max(1, std::min(maxn + 1, (152 * 4 + tiles * S_ - 1) / (tiles * S_)));
+  a.csize = (maxn + 1 + nchunk - 1) / nchunk;
+  a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
+  // scratch layout: flags | count | slot_nn | part | items
+  size_t off = 0;
+  size_t o_flags = carve(off, sizeof(int));
+  size_t o_count = carve(off, (size_t)n * S_ * sizeof(int));
+  size_t nslots = (size_t)n * S_ * rc;
+  size_t o_slots = carve(off, nslots * sizeof(int));
+  size_t o_part = carve(off, (size_t)n * S_ * a.nchunk * 6 * sizeof(double2));
+  size_t o_items = carve(off, nslots * 6 * sizeof(double2));
+  if (scratch_bytes) *scratch_bytes = off;
+  if (off > ALPS_NOALLOC_SCRATCH_BYTES) return ALPS_E_INVALID;  // batch too large for the static scratch
+  unsigned char* b = static_cast<unsigned char*>(base);
+  int* flags = reinterpret_cast<int*>(b + o_flags);
+  int* count = reinterpret_cast<int*>(b + o_count);
+  int* slots = reinterpret_cast<int*>(b + o_slots);
+  double2* part = reinterpret_cast<double2*>(b + o_part);
+  double2* items = reinterpret_cast<double2*>(b + o_items);
+  const double2* om = reinterpret_cast<const double2*>(d_om);
+  double2* D = reinterpret_cast<double2*>(d_D);
+  ALPS_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), st));
+  k_classify<<<dim3((n + 127) / 128, S_), 128, 0, st>>>(a, om, n, count, slots, flags);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_pole_sums<false><<<dim3(tiles, S_, a.nchunk), 128, 0, st>>>(a, om, n, js, part, nullptr);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  size_t smem = (size_t)RES_WARPS * (RES_WIN * 6 + (c->sys.nperp + 1)) * sizeof(double2);
+  if (smem > 48 * 1024)
+    ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  long blocks = ((long)nslots + RES_WARPS - 1) / RES_WARPS;
+  k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, om, n, count, slots, items, flags);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, D, nullptr);
+  ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -170,6 +170,24 @@ int alps_disp_batch(alps_ctx* ctx, int n, const alps_complex* om,
 int alps_disp_batch_device(alps_ctx* ctx, int n, const alps_complex* d_om,
                            alps_complex* d_D, void* stream);
 
+/* det D for n frequencies in device memory, allocating nothing.
+ * No counterpart in the reference; it exists for callers that cannot let a
+ * library allocate device memory while they run (an application whose own
+ * caching allocator must own the whole device heap, a real-time loop that
+ * cannot absorb the device-wide synchronisation of cudaMalloc/cudaFree, a
+ * plugin host that forbids allocations by plugins).  Same kernels and results
+ * as alps_disp_batch_device; the scratch they need comes from one static
+ * 16 MiB device array per device (held until the process exits).  The first
+ * call on a device looks up that array's address (cudaGetSymbolAddress) with
+ * the device current; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised by the
+ * caller.  Batches whose scratch would exceed 16 MiB return ALPS_E_INVALID
+ * without launching; *scratch_bytes (may be NULL) receives the bytes the
+ * batch needs.  stream: cudaStream_t, NULL = the context's stream. */
+int alps_disp_batch_noalloc(alps_ctx* ctx, int n, const alps_complex* d_om,
+                            alps_complex* d_D, void* stream,
+                            size_t* scratch_bytes);
+
 /* Root polishing of nroots guesses in place (om[], host memory).
  * method: 0 secant (src/ALPS_fns.f90:1815-1917), 1 rtsec (:2105-2195),
  * 2 secant_osc (:1919-2101).  iters[r] (may be NULL) receives the number of
