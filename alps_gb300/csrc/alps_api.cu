@@ -126,6 +126,9 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_A);
     cudaFree(S.d_Rw);
     cudaFree(S.d_G);
+    cudaFree(S.d_X);
+    cudaFree(S.d_mom);
+    cudaFree(S.d_fit_aux);
   }
   cudaFree(c->d_om);
   cudaFree(c->d_D);
@@ -223,9 +226,11 @@ int alps_get_fit(alps_ctx* c, int is, double* out) {
 
 int alps_set_fit(alps_ctx* c, int is, const double* in) {
   if (!c || !in || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
-  const SpeciesHost& S = c->spec[is];
+  SpeciesHost& S = c->spec[is];
   size_t n = (size_t)(c->sys.nperp + 1) * 5 * S.sp.n_fits;
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  int st = launch_fit_aux(c, is);
+  if (st) return st;
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ALPS_OK;
 }
@@ -255,6 +260,7 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     S.nmax = nm[is];
     int st = launch_build_bessel_and_reduced(c, is, kperp);
     if (st) return st;
+    if ((st = launch_fit_aux(c, is))) return st;
     // resonant orders per omega: p_res moves by |q/k_par| per order, so at
     // most width*|k_par/q| + 1 orders fall in the resonance window
     int M = c->sys.npar;

@@ -9,7 +9,9 @@
 //     fit[(N+1)*5*nf]                 continuation fit parameters
 //     bessel[(nmax+3)(N+1)]           J_n(k_perp pperp_i / q), n = -1..nmax+1
 //     V[(nmax+1)(M-1)*12]             reduced vectors of the p_perp
-//                                     contraction, see build_reduced()
+//                                     contraction (k_fold_reduced)
+//     mom[(nmax+1)*ALPS_KFAR*12]      Laurent moments of V about the grid
+//                                     centre (k_moments)
 //   per omega batch: partial sums, resonant-item slots, results.
 #pragma once
 
@@ -22,6 +24,8 @@
 #include "../../include/alps_gb300.h"
 
 #define ALPS_MAX_SPECIES 8
+// Laurent terms kept per order for poles far from the p_par grid
+#define ALPS_KFAR 128
 #define ALPS_PI 3.141592653589793115997963468544185161590576171875
 
 // ---------------------------------------------------------------------------
@@ -69,7 +73,13 @@ struct SpecDev {
   const double* fit;
   const double* bessel;
   const double* V;
+  const double* mom;  // Laurent moments [(nmax+1)][ALPS_KFAR][12]
+  double pcen, prad;  // centre and half-width of ppar[1..M-1]
+  int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)
+  // [(N+1)][nf][4] = {p1 exp(-pc pperp^2), p2, p3, exp(-p2 dppar^2)} when
+  // every fit term is a Maxwellian (ACmethod 1, type 1); else null
+  const double* fit_aux;
 };
 
 struct SysDev {
@@ -98,6 +108,10 @@ struct SpeciesHost {
   double* d_Rw = nullptr;                 // weighted Bessel rows scratch
   size_t Rw_cap = 0;
   double* d_G = nullptr;                  // contraction RHS [2][N-1][M-1]
+  double* d_X = nullptr;                  // x_j^k, x_j = (ppar_j - pcen)/prad
+  double* d_mom = nullptr;                // Laurent moments
+  double* d_fit_aux = nullptr;            // Maxwellian continuation factors
+  size_t mom_cap = 0;
   int nmax = 0;
   double int_ee = 0.0;
   int rcap = 1;
@@ -145,6 +159,7 @@ struct alps_ctx {
 int launch_prepare_species(alps_ctx* c, int is);
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
+int launch_fit_aux(alps_ctx* c, int is);
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
                       cudaStream_t st);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);

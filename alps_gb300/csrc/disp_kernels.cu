@@ -103,41 +103,76 @@ __global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __
         double2 Sx[12];
 #pragma unroll
         for (int q = 0; q < 12; ++q) Sx[q] = cmk(0.0, 0.0);
-        for (int j = 1 + js; j <= M - 1; j += js_count) {
-          bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
-          if (!in) continue;
-          double dr = fma(-kpar, pp[j], Ar);
-          double r = rcp_fast(fma(dr, dr, Di2));
-          double Rr = dr * r, Ri = -Di * r;
-          const double2* v2 = reinterpret_cast<const double2*>(Vn + (size_t)(j - 1) * 12);
-#pragma unroll
-          for (int q = 0; q < 6; ++q) {
-            double2 v = __ldg(v2 + q);
-            Sx[2 * q].x = fma(v.x, Rr, Sx[2 * q].x);
-            Sx[2 * q].y = fma(v.x, Ri, Sx[2 * q].y);
-            Sx[2 * q + 1].x = fma(v.y, Rr, Sx[2 * q + 1].x);
-            Sx[2 * q + 1].y = fma(v.y, Ri, Sx[2 * q + 1].y);
-          }
+        // Laurent series for a pole far outside the grid: truncation
+        // rho^K <= 2^-53 (1 - rho), rho = prad/|p_res - pcen|
+        int K = S.kfar + 1;
+        double2 d = cmk(g.pr - S.pcen, g.pi);
+        double dd = d.x * d.x + d.y * d.y;
+        if (!g.res && S.prad * S.prad < 0.5 * dd) {
+          double rho = S.prad * rsqrt(dd);
+          K = (int)ceil((36.7368005696771 - log1p(-rho)) / -log(rho));
         }
-        // trapezoid end weights: the range ends carry half weight unless the
-        // range is a single node (integrate(a,a) weighs it fully)
-        int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+        if (K <= S.kfar) {
+          const double* __restrict__ mom = S.mom + (size_t)n * ALPS_KFAR * 12;
+          double idd = 1.0 / dd;
+          double2 inv = cmk(d.x * idd, -d.y * idd);
+          double2 t = cscale(inv, S.prad);
+          double2 tk = cmk(1.0, 0.0), step = t;
+          for (int q = 0; q < js; ++q) tk = cmul(tk, t);
+          for (int q = 1; q < js_count; ++q) step = cmul(step, t);
+          for (int k = js; k < K; k += js_count) {
+            const double2* m2 = reinterpret_cast<const double2*>(mom + (size_t)k * 12);
 #pragma unroll
-        for (int r2 = 0; r2 < 2; ++r2) {
-          int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
-          if (lo >= hi) continue;
+            for (int q = 0; q < 6; ++q) {
+              double2 m = __ldg(m2 + q);
+              Sx[2 * q].x = fma(m.x, tk.x, Sx[2 * q].x);
+              Sx[2 * q].y = fma(m.x, tk.y, Sx[2 * q].y);
+              Sx[2 * q + 1].x = fma(m.y, tk.x, Sx[2 * q + 1].x);
+              Sx[2 * q + 1].y = fma(m.y, tk.y, Sx[2 * q + 1].y);
+            }
+            tk = cmul(tk, step);
+          }
+          // S = (1/(k_par d)) sum_k mom_k t^k
+          double2 f = cscale(inv, 1.0 / kpar);
 #pragma unroll
-          for (int side = 0; side < 2; ++side) {
-            int j = side ? hi : lo;
-            if (((j - 1) % js_count) != js) continue;
+          for (int q = 0; q < 12; ++q) Sx[q] = cmul(Sx[q], f);
+        } else {
+          for (int j = 1 + js; j <= M - 1; j += js_count) {
+            bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
+            if (!in) continue;
             double dr = fma(-kpar, pp[j], Ar);
             double r = rcp_fast(fma(dr, dr, Di2));
-            double Rr = -0.5 * dr * r, Ri = 0.5 * Di * r;
-            const double* v = Vn + (size_t)(j - 1) * 12;
+            double Rr = dr * r, Ri = -Di * r;
+            const double2* v2 = reinterpret_cast<const double2*>(Vn + (size_t)(j - 1) * 12);
 #pragma unroll
-            for (int q = 0; q < 12; ++q) {
-              Sx[q].x = fma(v[q], Rr, Sx[q].x);
-              Sx[q].y = fma(v[q], Ri, Sx[q].y);
+            for (int q = 0; q < 6; ++q) {
+              double2 v = __ldg(v2 + q);
+              Sx[2 * q].x = fma(v.x, Rr, Sx[2 * q].x);
+              Sx[2 * q].y = fma(v.x, Ri, Sx[2 * q].y);
+              Sx[2 * q + 1].x = fma(v.y, Rr, Sx[2 * q + 1].x);
+              Sx[2 * q + 1].y = fma(v.y, Ri, Sx[2 * q + 1].y);
+            }
+          }
+          // trapezoid end weights: the range ends carry half weight unless the
+          // range is a single node (integrate(a,a) weighs it fully)
+          int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+#pragma unroll
+          for (int r2 = 0; r2 < 2; ++r2) {
+            int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
+            if (lo >= hi) continue;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+              int j = side ? hi : lo;
+              if (((j - 1) % js_count) != js) continue;
+              double dr = fma(-kpar, pp[j], Ar);
+              double r = rcp_fast(fma(dr, dr, Di2));
+              double Rr = -0.5 * dr * r, Ri = 0.5 * Di * r;
+              const double* v = Vn + (size_t)(j - 1) * 12;
+#pragma unroll
+              for (int q = 0; q < 12; ++q) {
+                Sx[q].x = fma(v[q], Rr, Sx[q].x);
+                Sx[q].y = fma(v[q], Ri, Sx[q].y);
+              }
             }
           }
         }
@@ -241,9 +276,27 @@ __device__ inline double2 h_node(const double* Vn, int j, int e, double2 o, doub
 // Resonant items: the principal-value part of integrate_res
 // (src/ALPS_fns.f90:1000-1236) and landau_integrate (:1327-1452) for one
 // (omega, species, n).  One warp per item.
+//
+// Principal value: summed over iperp, funct_g (:1243-1321) is the linear
+// interpolation H_e(p) = h_e(jc) + s_e(jc) (p - ppar_jc) on the node values
+// h_e(j) = omega V_{e,1}(j) + kappa V_{e,2}(j) with the centred slope
+// s_e(j) = (h_e(j+1) - h_e(j-1)) / (2 dppar); both are staged per window node
+// in shared memory.  Landau: for Maxwellian fit terms the three continuation
+// values a row needs share one Gaussian, exp(-p2 (d +- D)^2) =
+// exp(-p2 d^2) exp(-+2 p2 D d) exp(-p2 D^2), so a row costs two complex
+// exponentials; the omega-independent factors come from k_fit_aux.
 // ---------------------------------------------------------------------------
 #define RES_WARPS 4
-#define RES_WIN 64
+#define RES_WIN 32
+
+__host__ __device__ inline size_t res_warp_smem(int N) {
+  return (size_t)RES_WIN * 12 + 3 * (size_t)(N + 1);  // in double2
+}
+
+__device__ inline double2 crcp(double2 z) {
+  double r = 1.0 / (z.x * z.x + z.y * z.y);
+  return cmk(z.x * r, -z.y * r);
+}
 
 __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const double2* __restrict__ om,
                                                               int n_om, const int* __restrict__ count,
@@ -270,11 +323,13 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
   t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
   ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
   const double* Vn = S.V + (size_t)n * (M - 1) * 12;
-  double2* win = sm + (size_t)warp * (RES_WIN * 6 + (size_t)(N + 1));  // h window, then f0 row values
-  double2* frow = win + RES_WIN * 6;
+  double2* wh = sm + (size_t)warp * res_warp_smem(N);  // node values h
+  double2* ws = wh + RES_WIN * 6;                       // node slopes s
+  double2* frow = ws + RES_WIN * 6;                     // f(i, p_res)
+  double2* fpr = frow + (N + 1);                        // f(i, p_res + dppar)
+  double2* fmr = fpr + (N + 1);                         // f(i, p_res - dppar)
   double2 res[6];
   for (int e = 0; e < 6; ++e) res[e] = cmk(0.0, 0.0);
-  const int nent = 6;
 
   // ---- principal value window (case 3) ----
   if (g.kind == 3) {
@@ -283,17 +338,19 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
     const int jw0 = max(1, g.lower - 2), jw1 = min(M - 1, g.upper + 2);
     const int nw = jw1 - jw0 + 1;
     const bool winok = nw <= RES_WIN;
-    if (winok)
+    if (winok) {
       for (int t = lane; t < nw * 6; t += 32) {
         int jj = t / 6, e = t % 6;
-        win[jj * 6 + e] = h_node(Vn, jw0 + jj, e, o, kappa);
+        wh[jj * 6 + e] = h_node(Vn, jw0 + jj, e, o, kappa);
       }
+      __syncwarp();
+      for (int t = lane; t < nw * 6; t += 32) {
+        int jj = t / 6, e = t % 6;
+        if (jj >= 1 && jj + 1 < nw) ws[jj * 6 + e] = cscale(csub(wh[(jj + 1) * 6 + e], wh[(jj - 1) * 6 + e]), 0.5 / dpa);
+      }
+    }
     __syncwarp();
-    auto hget = [&](int j, int e) -> double2 {
-      if (winok && j >= jw0 && j <= jw1) return win[(j - jw0) * 6 + e];
-      return h_node(Vn, j, e, o, kappa);
-    };
-    // funct_g summed over iperp: H_e(p) (src/ALPS_fns.f90:1243-1321)
+    // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321)
     auto Hc = [&](double p, double2* H) {
       int jc = 0;
       double jd = floor((p - S.ppar[0]) / dpa + 0.5);
@@ -302,16 +359,22 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
         int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
         for (int jj = hi; jj >= lo; --jj)
           if (fabs(S.ppar[jj] - p) <= 0.5 * dpa) { jc = jj; break; }
-      } else if (!(jd > -10.0)) {
-        jc = 0;
       }
       if (jc >= M - 1) jc = M - 2;
       if (jc <= 1) jc = 2;
       double dx = p - S.ppar[jc];
-      for (int e = 0; e < nent; ++e) {
-        double2 hp = hget(jc + 1, e), h0 = hget(jc, e), hm = hget(jc - 1, e);
-        double2 slope = cscale(csub(hp, hm), 1.0 / dpa);
-        H[e] = cadd(h0, cscale(slope, 0.5 * dx));
+      if (winok && jc - 1 >= jw0 && jc + 1 <= jw1) {
+        const double2* h0 = wh + (jc - jw0) * 6;
+        const double2* s0 = ws + (jc - jw0) * 6;
+#pragma unroll
+        for (int e = 0; e < 6; ++e) H[e] = cmk(fma(s0[e].x, dx, h0[e].x), fma(s0[e].y, dx, h0[e].y));
+      } else {
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          double2 hp = h_node(Vn, jc + 1, e, o, kappa), h0 = h_node(Vn, jc, e, o, kappa),
+                  hm = h_node(Vn, jc - 1, e, o, kappa);
+          H[e] = cadd(h0, cscale(csub(hp, hm), 0.5 * dx / dpa));
+        }
       }
     };
     const double capDelta = pr - S.ppar[g.lower];
@@ -323,15 +386,18 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
       for (int k = lane; k <= a.sys.M_P; k += 32) {
         double p = (k == 0) ? pr : ((k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k);
         double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-        // K = 1/(p - pr - i pim); the mirrored term uses conj(K)
+        // K = 1/(p - pr - i pim); the mirrored point uses conj(K)
         double dx = p - pr;
-        double rr = 1.0 / (dx * dx + pim * pim);
-        double2 K = cmk(dx * rr, pim * rr);
-        double2 Kc = cmk(dx * rr, -pim * rr);
+        double rr = wk / (dx * dx + pim * pim);
+        double kr = dx * rr, ki = pim * rr;
         Hc(p, H1);
         Hc(2.0 * pr - p, H2);
-        for (int e = 0; e < nent; ++e)
-          T[e] = cadd(T[e], cscale(csub(cmul(H1[e], K), cmul(H2[e], Kc)), wk));
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          // H1 K - H2 conj(K)
+          T[e].x += (H1[e].x - H2[e].x) * kr - (H1[e].y + H2[e].y) * ki;
+          T[e].y += (H1[e].x + H2[e].x) * ki + (H1[e].y - H2[e].y) * kr;
+        }
       }
     } else {
       // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
@@ -349,7 +415,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
         double2 H0[6];
         Hc(pr, H0);
         double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
-        for (int e = 0; e < nent; ++e) {
+        for (int e = 0; e < 6; ++e) {
           double2 gp = cscale(csub(H1[e], H2[e]), 1.0 / (2.0 * dps));
           T[e] = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0[e]));
         }
@@ -363,20 +429,21 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
         double p = (k == 0) ? pr + capDelta : pr + capDelta + corr * smdelta * k;
         double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
         double dx = p - pr;
-        double rr = 1.0 / (dx * dx + pim * pim);
+        double rr = wk * corr / (dx * dx + pim * pim);
         double2 K = cmk(dx * rr, pim * rr);
         Hc(p, H1);
-        for (int e = 0; e < nent; ++e) T[e] = cadd(T[e], cscale(cmul(H1[e], K), wk * corr));
+#pragma unroll
+        for (int e = 0; e < 6; ++e) T[e] = cadd(T[e], cmul(H1[e], K));
       }
     }
-    for (int e = 0; e < nent; ++e)
+    for (int e = 0; e < 6; ++e)
       for (int off = 16; off > 0; off >>= 1) {
         T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
         T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
       }
     // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
     double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
-    for (int e = 0; e < nent; ++e) res[e] = cscale(cmul(pref[e], T[e]), scale);
+    for (int e = 0; e < 6; ++e) res[e] = cscale(cmul(pref[e], T[e]), scale);
   }
 
   // ---- Landau term ----
@@ -385,15 +452,50 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
     const double2 p = cmk(g.pr, g.pi);
     const double pd = S.dppar_abs, dpp = S.dpperp;
     const double vA = a.sys.vA;
-    for (int i = lane; i <= N; i += 32) frow[i] = eval_fit_d(S, vA, i, p);
+    if (S.fit_aux) {
+      // Maxwellian terms: f = sum_f a0 exp(-p2 (p - p3)^2)
+      const int nf = S.nf;
+      for (int i = lane; i <= N; i += 32) {
+        double2 f0 = cmk(0, 0), fp = cmk(0, 0), fm = cmk(0, 0);
+        for (int f = 0; f < nf; ++f) {
+          const double* aux = S.fit_aux + ((size_t)i * nf + f) * 4;  // a0, p2, p3, exp(-p2 D^2)
+          double p2 = aux[1];
+          double2 d = cmk(p.x - aux[2], p.y);
+          double2 E0 = cexp_d(cscale(cmul(d, d), -p2));
+          double2 G = cscale(E0, aux[0]);
+          double2 ax = cscale(d, -2.0 * p2 * pd);
+          double2 X, Xi;
+          if (fabs(ax.x) < 600.0) {
+            X = cexp_d(ax);
+            Xi = crcp(X);
+            double2 Gc = cscale(G, aux[3]);
+            fp = cadd(fp, cmul(Gc, X));
+            fm = cadd(fm, cmul(Gc, Xi));
+          } else {
+            double2 dp = cadd(d, cmk(pd, 0.0)), dm = csub(d, cmk(pd, 0.0));
+            fp = cadd(fp, cscale(cexp_d(cscale(cmul(dp, dp), -p2)), aux[0]));
+            fm = cadd(fm, cscale(cexp_d(cscale(cmul(dm, dm), -p2)), aux[0]));
+          }
+          f0 = cadd(f0, G);
+        }
+        frow[i] = f0;
+        fpr[i] = fp;
+        fmr[i] = fm;
+      }
+    } else {
+      for (int i = lane; i <= N; i += 32) {
+        frow[i] = eval_fit_d(S, vA, i, p);
+        fpr[i] = eval_fit_d(S, vA, i, cadd(p, cmk(pd, 0.0)));
+        fmr[i] = eval_fit_d(S, vA, i, csub(p, cmk(pd, 0.0)));
+      }
+    }
     __syncwarp();
     bool zero = false;
     double2 sums[3] = {cmk(0, 0), cmk(0, 0), cmk(0, 0)};
     const double ql = S.qs / fabs(kpar);
     const int L = N + 1;
     for (int i = lane; i <= N; i += 32) {
-      double2 fpi = eval_fit_d(S, vA, i, cadd(p, cmk(pd, 0.0)));
-      double2 fpf = eval_fit_d(S, vA, i, csub(p, cmk(pd, 0.0)));
+      double2 fpi = fpr[i], fpf = fmr[i];
       double2 dfperp, dfpar;
       double h;
       if (i == 0) {
@@ -607,7 +709,13 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->fit = S.d_fit;
   o->bessel = S.d_bessel;
   o->V = S.d_V;
+  o->mom = S.d_mom;
+  o->pcen = 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
+  o->prad = 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
+  // the series is used only where it is cheaper than the node sum
+  o->kfar = (c->precision == ALPS_PREC_FP64) ? 0 : std::min(ALPS_KFAR, (int)(0.8 * (c->sys.npar - 1)));
   o->rcap = S.rcap;
+  o->fit_aux = S.d_fit_aux;
 }
 
 int collect_profile(alps_ctx* c) {
@@ -690,7 +798,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
   int maxN = c->sys.nperp;
-  size_t smem = (size_t)RES_WARPS * (RES_WIN * 6 + (maxN + 1)) * sizeof(double2);
+  size_t smem = (size_t)RES_WARPS * res_warp_smem(maxN) * sizeof(double2);
   if (smem > 48 * 1024) ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   long total = (long)nslots;
   long blocks = (total + RES_WARPS - 1) / RES_WARPS;
@@ -814,7 +922,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   ALPS_CUDA_TRY(cudaGetLastError());
   k_pole_sums<false><<<dim3(tiles, S_, a.nchunk), 128, 0, st>>>(a, om, n, js, part, nullptr);
   ALPS_CUDA_TRY(cudaGetLastError());
-  size_t smem = (size_t)RES_WARPS * (RES_WIN * 6 + (c->sys.nperp + 1)) * sizeof(double2);
+  size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp) * sizeof(double2);
   if (smem > 48 * 1024)
     ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   long blocks = ((long)nslots + RES_WARPS - 1) / RES_WARPS;

@@ -426,6 +426,58 @@ __global__ void k_fold_reduced(const double* __restrict__ A, const double* __res
   }
 }
 
+// X[(j-1)*ALPS_KFAR + k] = x_j^k with x_j = (ppar_j - pcen)/prad, j = 1..M-1
+__global__ void k_powers(const double* __restrict__ ppar, int M, double pcen, double prad, double* X) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
+  if (j > M - 1) return;
+  double x = (ppar[j] - pcen) / prad;
+  double p = 1.0;
+  double* o = X + (size_t)(j - 1) * ALPS_KFAR;
+  for (int k = 0; k < ALPS_KFAR; ++k) {
+    o[k] = p;
+    p *= x;
+  }
+}
+
+// Laurent moments of the full-range trapezoid pole sum:
+// mom[(n*ALPS_KFAR + k)*12 + q] = sum_j f_j V[n][j][q] x_j^k, f_j = 1/2 at
+// j = 1, M-1 and 1 inside (the reduced vectors carry the interior weight 2).
+// For a pole p far from the grid, sum_j f_j V_j / (p - ppar_j) =
+//   (1/d) sum_k mom_k (prad/d)^k,  d = p - pcen.
+__global__ void k_moments(const double* __restrict__ V, const double* __restrict__ X, int M, int nmax,
+                          double* mom) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int total = (nmax + 1) * ALPS_KFAR * 12;
+  if (t >= total) return;
+  int q = t % 12, k = (t / 12) % ALPS_KFAR, n = t / (12 * ALPS_KFAR);
+  const double* v = V + (size_t)n * (M - 1) * 12 + q;
+  double acc = 0.0;
+  for (int j = 1; j <= M - 1; ++j) {
+    double f = (j == 1 || j == M - 1) ? 0.5 : 1.0;
+    acc = fma(f * v[(size_t)(j - 1) * 12], X[(size_t)(j - 1) * ALPS_KFAR + k], acc);
+  }
+  mom[t] = acc;
+}
+
+// omega-independent factors of Maxwellian continuation terms, per row and
+// fit: a0 = p1 exp(-pc pperp^2) (the reference's left-to-right product),
+// p2, p3, exp(-p2 dppar^2)
+__global__ void k_fit_aux(const double* __restrict__ fit, const double* __restrict__ pperp, int N, int nf,
+                          double pc0, double pc1, double pc2, double pc3, double dppar, double* aux) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > N) return;
+  double pcs[4] = {pc0, pc1, pc2, pc3};
+  double p = pperp[i];
+  for (int f = 0; f < nf; ++f) {
+    double p1 = fit[(i * 5 + 0) * nf + f], p2 = fit[(i * 5 + 1) * nf + f], p3 = fit[(i * 5 + 2) * nf + f];
+    double* o = aux + ((size_t)i * nf + f) * 4;
+    o[0] = p1 * exp(-pcs[f] * (p * p));
+    o[1] = p2;
+    o[2] = p3;
+    o[3] = exp(-p2 * (dppar * dppar));
+  }
+}
+
 template <typename T>
 int ensure(T*& ptr, size_t& cap, size_t n) {
   if (n <= cap && ptr) return ALPS_OK;
@@ -532,6 +584,33 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);
   ALPS_CUDA_TRY(cudaGetLastError());
   k_fold_reduced<<<dim3((M - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_A, S.d_ppar, M, nmax, S.d_V);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  double pcen = 0.5 * (S.ppar[1] + S.ppar[M - 1]), prad = 0.5 * (S.ppar[M - 1] - S.ppar[1]);
+  if (!S.d_X) ALPS_CUDA_TRY(cudaMalloc(&S.d_X, (size_t)(M - 1) * ALPS_KFAR * sizeof(double)));
+  if ((rc = ensure(S.d_mom, S.mom_cap, (size_t)(nmax + 1) * ALPS_KFAR * 12))) return rc;
+  k_powers<<<(M - 1 + 127) / 128, 128, 0, st>>>(S.d_ppar, M, pcen, prad, S.d_X);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  int tot = (nmax + 1) * ALPS_KFAR * 12;
+  k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_mom);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  return ALPS_OK;
+}
+
+int launch_fit_aux(alps_ctx* c, int is) {
+  SpeciesHost& S = c->spec[is];
+  bool maxw = S.sp.ac_method == 1;
+  for (int f = 0; f < S.sp.n_fits && maxw; ++f) maxw = S.sp.fit_type[f] == 1;
+  if (!maxw) {
+    if (S.d_fit_aux) cudaFree(S.d_fit_aux);
+    S.d_fit_aux = nullptr;
+    return ALPS_OK;
+  }
+  int N = c->sys.nperp, nf = S.sp.n_fits;
+  if (!S.d_fit_aux) ALPS_CUDA_TRY(cudaMalloc(&S.d_fit_aux, (size_t)(N + 1) * ALPS_MAX_FITS * 4 * sizeof(double)));
+  double dppar = std::fabs(S.ppar[2] - S.ppar[1]);
+  k_fit_aux<<<(N + 1 + 127) / 128, 128, 0, c->stream>>>(S.d_fit, S.d_pperp, N, nf, S.sp.perp_correction[0],
+                                                         S.sp.perp_correction[1], S.sp.perp_correction[2],
+                                                         S.sp.perp_correction[3], dppar, S.d_fit_aux);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

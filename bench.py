@@ -219,49 +219,65 @@ def main():
     def step():
         G.disp_batch_device(n, om_dev.data_ptr(), D_dev.data_ptr(), sp)
 
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
+    peak64 = None
+
+    def timed(precision):
+        """warmup + K timed steps of one evaluation mode; returns seconds,
+        per-kernel profile and the D values of the last step"""
+        G.set_precision(precision)
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        G.set_profiling(True)
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            flush.fill_(1.0)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        t = e0.elapsed_time(e1) / 1e3
+        if dist:
+            tt = torch.tensor([t], device="cuda")
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t = float(tt.item())
+        prof = G.profile()
+        G.set_profiling(False)
+        Dv = D_dev[:, 0].cpu().numpy() + 1j * D_dev[:, 1].cpu().numpy()
+        return t, prof, Dv
+
+    # plain FP64 path (node sums everywhere): the baseline of the fast path
+    t_plain, prof_plain, D_plain = timed("fp64")
     peak64 = fp64_peak_tflops(torch)
-    G.set_profiling(True)
     clocks = Clocks(local)
-    if dist:
-        dist.barrier()
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-        flush.fill_(1.0)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
+    t, (prof_ms, nb), D_fast = timed("mixed")
     clk = clocks.stop()
-    t = e0.elapsed_time(e1) / 1e3
-    if dist:
-        tt = torch.tensor([t], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t = float(tt.item())
-    prof_ms, nb = G.profile()
-    G.set_profiling(False)
     value = world * n * args.steps / t
+    value_plain = world * n * args.steps / t_plain
     ms_step = t / args.steps * 1e3
     st = G.stats()
+    rel = np.abs(D_fast - D_plain) / np.maximum(np.abs(D_plain), 1e-300)
 
-    # roofline of the dominant kernel (pole sums): FP64 pipe
-    pole_ms = prof_ms[1] / max(nb, 1)
+    # roofline of the dominant kernel of the plain path (pole sums): FP64 pipe
+    pm_plain, nb_plain = prof_plain
+    pole_ms = pm_plain[1] / max(nb_plain, 1)
     flops = pole_sum_flops(nmax, s.npar) * n
     achieved = flops / (pole_ms / 1e3) / 1e12
     achieved_issued = pole_sum_flops_issued(nmax, s.npar) * n / (pole_ms / 1e3) / 1e12
+    names = ["classify", "pole_sums", "resonant", "finalize"]
     roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
                 "frac": achieved / peak64, "traffic": None,
                 "achieved_issued": achieved_issued, "frac_issued": achieved_issued / peak64,
                 "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (burst)",
-                "kernel": "k_pole_sums", "kernel_ms": pole_ms,
-                "kernel_share": prof_ms[1] / max(sum(prof_ms), 1e-30),
-                "per_kernel_ms": dict(zip(["classify", "pole_sums", "resonant", "finalize"],
-                                          [x / max(nb, 1) for x in prof_ms]))}
+                "kernel": "k_pole_sums (plain FP64 path)", "kernel_ms": pole_ms,
+                "kernel_share": pm_plain[1] / max(sum(pm_plain), 1e-30),
+                "per_kernel_ms_plain": dict(zip(names, [x / max(nb_plain, 1) for x in pm_plain])),
+                "per_kernel_ms_fast": dict(zip(names, [x / max(nb, 1) for x in prof_ms]))}
 
     # end to end through the C-ABI with host buffers (copies included)
     Dh = G.disp_batch(oms)
@@ -284,6 +300,11 @@ def main():
     t0 = time.perf_counter()
     roots, iters, _ = G.secant(guesses)
     t_roots = time.perf_counter() - t0
+    # the same solves on the plain FP64 path: root agreement of the fast path
+    G.set_precision("fp64")
+    roots_plain, _, _ = G.secant(guesses)
+    G.set_precision("mixed")
+    root_rel = float(np.max(np.abs(roots - roots_plain) / np.maximum(np.abs(roots_plain), 1e-300)))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -300,6 +321,10 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64", "data": "synthetic", "precision_path": G.precision,
                 "config": config_dict(w, mp.nr, mp.ni, world), "nmax": nmax,
+                "plain_fp64": {"value": value_plain, "unit": UNIT, "ms_per_step": t_plain / args.steps * 1e3,
+                               "speedup_of_fast_path": value / value_plain,
+                               "max_rel_diff_det_D_fast_vs_plain": float(rel.max()),
+                               "max_rel_diff_roots_fast_vs_plain": root_rel},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": int(st.kernels_launched) * args.steps,
                 "roots": {"count": len(roots), "roots_per_s": len(roots) / t_roots, "iterations": iters,

@@ -148,9 +148,14 @@ int alps_set_fit(alps_ctx* ctx, int is, const double* in);
 int alps_set_k(alps_ctx* ctx, double kperp, double kpar);
 int alps_get_nmax(alps_ctx* ctx, int* nmax /* [nspec] */);
 
-/* Precision of the omega pass.  ALPS_PREC_FP64: every operation in FP64
- * (the parity path).  ALPS_PREC_MIXED: the non-resonant pole sums run in
- * double-float arithmetic on the FP32 pipes; pole, residue, det stay FP64. */
+/* Evaluation mode of the omega pass.
+ * ALPS_PREC_FP64 (plain): every p_par pole sum is the trapezoid node sum of
+ *   the reference, in FP64 (the parity path).
+ * ALPS_PREC_MIXED (fast): for non-resonant orders whose pole lies well
+ *   outside the p_par grid the node sum is replaced by its Laurent series
+ *   about the grid centre, truncated where the remainder is below FP64
+ *   rounding (rho^K <= 2^-53 (1-rho)); pole, principal value, Landau
+ *   residue and det are computed as in the plain mode. */
 enum { ALPS_PREC_FP64 = 0, ALPS_PREC_MIXED = 1 };
 int alps_set_precision(alps_ctx* ctx, int precision);
 

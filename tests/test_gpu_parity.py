@@ -42,11 +42,14 @@ def api():
     return A
 
 
-def _pair(api, w, share_fit=True):
+PRECISIONS = ["fp64", "mixed"]
+
+
+def _pair(api, w, share_fit=True, precision="fp64"):
     po = _oracle()
     system, species = workloads.build(w, po.generate_f0)
     O = po.OraclePlasma(system, species)
-    G = api.Plasma(system, species)
+    G = api.Plasma(system, species, precision=precision)
     if share_fit:
         for i in range(system.nspec):
             G.set_fit(i, O.get_fit(i))
@@ -107,9 +110,10 @@ def test_fit_matches_oracle(api):
         assert np.abs(a - b).max() <= 1e-10 * scale
 
 
-@pytest.mark.parametrize("k", [(1.0, 0.3), (2.0, 0.15)])
-def test_disp_chi_parity_small(api, k):
-    O, G = _pair(api, _small())
+@pytest.mark.parametrize("precision", PRECISIONS)
+@pytest.mark.parametrize("k", [(1.0, 0.3), (2.0, 0.15), (0.5, 0.05)])
+def test_disp_chi_parity_small(api, k, precision):
+    O, G = _pair(api, _small(), precision=precision)
     O.set_k(*k)
     G.set_k(*k)
     for om in OMEGAS:
@@ -130,9 +134,10 @@ def test_disp_batch_matches_single(api):
         assert abs(s - d) <= 1e-13 * abs(d)
 
 
-def test_disp_parity_kpar_fast(api):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_disp_parity_kpar_fast(api, precision):
     w = workloads.kpar_fast(nproc=4)
-    O, G = _pair(api, w)
+    O, G = _pair(api, w, precision=precision)
     O.set_k(*w["k"])
     G.set_k(*w["k"])
     assert G.nmax() == [21, 13]
@@ -140,8 +145,9 @@ def test_disp_parity_kpar_fast(api):
         _disp_close(O, G, om, "kpar_fast %s" % om)
 
 
-def test_secant_parity(api):
-    O, G = _pair(api, _small())
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_secant_parity(api, precision):
+    O, G = _pair(api, _small(), precision=precision)
     O.set_k(1.0, 0.3)
     G.set_k(1.0, 0.3)
     for method in (2, 0, 1):
@@ -151,9 +157,10 @@ def test_secant_parity(api):
         assert abs(rg[0] - ro) <= ROOT_RTOL * abs(ro), (method, rg[0], ro)
 
 
-def test_map_and_minima_parity(api):
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_map_and_minima_parity(api, precision):
     po = _oracle()
-    O, G = _pair(api, _small(nperp=16, npar=32, bz=1e-10))
+    O, G = _pair(api, _small(nperp=16, npar=32, bz=1e-10), precision=precision)
     O.set_k(1.0, 0.3)
     G.set_k(1.0, 0.3)
     mp = _abi.alps_map_params()
@@ -165,6 +172,20 @@ def test_map_and_minima_parity(api):
     rel = np.abs(calg - calo) / np.maximum(np.abs(calo), 1e-300)
     assert rel.max() < 1e-9
     assert po.find_minima(valo, 12, 8) == api.find_minima(valg, 12, 8)
+
+
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_disp_parity_map_config_samples(api, precision):
+    """The benchmark plasma (128x256 grid, nmax 30/7) at a few lattice
+    points covering Im omega < 0, = 0 (none on the lattice) and > 0."""
+    w = workloads.config_map(8, 8)
+    O, G = _pair(api, w, precision=precision)
+    s = w["system"]
+    O.set_k(s.kperp, s.kpar)
+    G.set_k(s.kperp, s.kpar)
+    assert O.nmax() == G.nmax() == [30, 7]
+    for om in [1.5 - 0.3j, 0.2 - 0.01j, 2.9 + 0.05j, 0.75 - 0.004j]:
+        _disp_close(O, G, om, "map config %s" % om)
 
 
 @pytest.mark.slow
