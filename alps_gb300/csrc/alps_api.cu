@@ -129,6 +129,7 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_X);
     cudaFree(S.d_mom);
     cudaFree(S.d_fit_aux);
+    cudaFree(S.d_lmom);
   }
   cudaFree(c->d_om);
   cudaFree(c->d_D);
@@ -231,6 +232,7 @@ int alps_set_fit(alps_ctx* c, int is, const double* in) {
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int st = launch_fit_aux(c, is);
   if (st) return st;
+  if (c->kset && (st = launch_landau_moments(c, is))) return st;
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ALPS_OK;
 }
@@ -261,6 +263,7 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     int st = launch_build_bessel_and_reduced(c, is, kperp);
     if (st) return st;
     if ((st = launch_fit_aux(c, is))) return st;
+    if ((st = launch_landau_moments(c, is))) return st;
     // resonant orders per omega: p_res moves by |q/k_par| per order, so at
     // most width*|k_par/q| + 1 orders fall in the resonance window
     int M = c->sys.npar;

@@ -80,6 +80,11 @@ struct SpecDev {
   // [(N+1)][nf][4] = {p1 exp(-pc pperp^2), p2, p3, exp(-p2 dppar^2)} when
   // every fit term is a Maxwellian (ACmethod 1, type 1); else null
   const double* fit_aux;
+  // factorised Landau sums (one Maxwellian term): moments
+  // lmom[((n*3 + F)*2 + w)*5 + m], reference row Gaussian exp(-p2r (p-p3r)^2),
+  // bounds of the row deviation delta_i(p) = la p^2 + lb p + lc, smallest a0
+  const double* lmom;
+  double p2r, p3r, la, lb, lc, min_a0;
 };
 
 struct SysDev {
@@ -111,6 +116,10 @@ struct SpeciesHost {
   double* d_X = nullptr;                  // x_j^k, x_j = (ppar_j - pcen)/prad
   double* d_mom = nullptr;                // Laurent moments
   double* d_fit_aux = nullptr;            // Maxwellian continuation factors
+  double* d_lmom = nullptr;               // factorised Landau moments
+  size_t lmom_cap = 0;
+  double p2r = 0, p3r = 0, la = 0, lb = 0, lc = 0, min_a0 = 0;
+  bool lfact = false;
   size_t mom_cap = 0;
   int nmax = 0;
   double int_ee = 0.0;
@@ -160,6 +169,7 @@ int launch_prepare_species(alps_ctx* c, int is);
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
 int launch_fit_aux(alps_ctx* c, int is);
+int launch_landau_moments(alps_ctx* c, int is);
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
                       cudaStream_t st);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);

@@ -448,7 +448,50 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
 
   // ---- Landau term ----
   int lf = (o.y < 0.0) ? 2 : ((o.y == 0.0) ? 1 : 0);
-  if (lf > 0) {
+  bool landau_done = false;
+  if (lf > 0 && S.lmom) {
+    // factorised rows: valid when the row deviation |delta_i(p')| <= 1e-5
+    // for p' = p, p +- dppar (second-order remainder <= 1.7e-16)
+    const double2 p = cmk(g.pr, g.pi);
+    const double pd = S.dppar_abs;
+    double ap = hypot(p.x, p.y) + pd;
+    double bound = S.la * ap * ap + S.lb * ap + S.lc;
+    if (bound <= 1e-5) {
+      landau_done = true;
+      if (lane == 0) {
+        auto gauss = [&](double2 x) {
+          double2 d = cmk(x.x - S.p3r, x.y);
+          return cexp_d(cscale(cmul(d, d), -S.p2r));
+        };
+        auto poly = [&](const double* m, double2 x) {
+          double2 acc = cmk(m[4], 0.0);
+          for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
+          return acc;
+        };
+        double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
+        double2 G0 = gauss(p), Gp = gauss(xp), Gm = gauss(xm);
+        bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
+                    (cabs_(G0) * S.min_a0 == 0.0);
+        if (!zero) {
+          const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
+          double2 sums[3];
+          for (int F = 0; F < 3; ++F) {
+            const double* lm = S.lmom + ((size_t)n * 3 + F) * 10;
+            double2 Spar = cscale(csub(cmul(Gp, poly(lm, xp)), cmul(Gm, poly(lm, xm))), 1.0 / (2.0 * pd));
+            double2 Sperp = cmul(G0, poly(lm + 5, p));
+            // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp)
+            sums[F] = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
+          }
+          double2 c1 = cmk(1.0, 0.0), cp = p, cp2 = cmul(p, p);
+          double2 cfac[6] = {c1, c1, cp2, c1, cp, cp};
+          int fam[6] = {0, 1, 0, 2, 0, 2};
+          double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+          for (int e = 0; e < 6; ++e) res[e] = cadd(res[e], cmul(cmul(cmul(pref[e], cfac[e]), sums[fam[e]]), ifac));
+        }
+      }
+    }
+  }
+  if (lf > 0 && !landau_done) {
     const double2 p = cmk(g.pr, g.pi);
     const double pd = S.dppar_abs, dpp = S.dpperp;
     const double vA = a.sys.vA;
@@ -716,6 +759,13 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->kfar = (c->precision == ALPS_PREC_FP64) ? 0 : std::min(ALPS_KFAR, (int)(0.8 * (c->sys.npar - 1)));
   o->rcap = S.rcap;
   o->fit_aux = S.d_fit_aux;
+  o->lmom = (S.lfact && c->precision != ALPS_PREC_FP64) ? S.d_lmom : nullptr;
+  o->p2r = S.p2r;
+  o->p3r = S.p3r;
+  o->la = S.la;
+  o->lb = S.lb;
+  o->lc = S.lc;
+  o->min_a0 = S.min_a0;
 }
 
 int collect_profile(alps_ctx* c) {

@@ -478,6 +478,55 @@ __global__ void k_fit_aux(const double* __restrict__ fit, const double* __restri
   }
 }
 
+// Moments of the factorised Landau sums (one Maxwellian term per row,
+// f(i,p) = a0_i exp(u_r(p)) exp(delta_i(p)), delta_i = a_i p^2 + b_i p + c_i,
+// exp(delta) ~ 1 + delta + delta^2/2 = sum_m kappa_{i,m} p^m, m = 0..4):
+//   w = 0: sum_i h_i R_F(n,i) pperp_i a0_i kappa_{i,m}   (the dfpar sum)
+//   w = 1: sum_i c_i a0_i kappa_{i,m}, c = the transpose of landau_integrate's
+//          p_perp difference operator applied to h_i R_F(n,i)  (the dfperp sum)
+// h_i = 1/2 at i = 0, N-1, N and 1 otherwise (src/ALPS_fns.f90:1389-1444).
+__global__ void k_landau_moments(const double* __restrict__ bessel, const double* __restrict__ pperp,
+                                 const double* __restrict__ aux, int N, int nmax, double dpperp, double* lmom) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (nmax + 1) * 3) return;
+  int n = t / 3, F = t % 3;
+  int L = N + 1;
+  auto Rw = [&](int i) {
+    double J = bessel[(size_t)(n + 1) * L + i];
+    double Jp = (n == 0) ? -bessel[(size_t)2 * L + i]
+                         : 0.5 * (bessel[(size_t)n * L + i] - bessel[(size_t)(n + 2) * L + i]);
+    double p = pperp[i];
+    double h = (i == 0 || i == N - 1 || i == N) ? 0.5 : 1.0;
+    double R = (F == 0) ? J * J : (F == 1 ? (p * p) * Jp * Jp : p * J * Jp);
+    return h * R;
+  };
+  double p2r = aux[1], p3r = aux[2];
+  double m0[5] = {0, 0, 0, 0, 0}, m1[5] = {0, 0, 0, 0, 0};
+  for (int i = 0; i <= N; ++i) {
+    const double* ai = aux + (size_t)i * 4;
+    double a0 = ai[0], p2 = ai[1], p3 = ai[2];
+    double a = -(p2 - p2r), b = 2.0 * (p2 * p3 - p2r * p3r), c = -(p2 * p3 * p3 - p2r * p3r * p3r);
+    double k[5] = {1.0 + c + 0.5 * c * c, b * (1.0 + c), a + 0.5 * b * b + a * c, a * b, 0.5 * a * a};
+    double w0 = Rw(i) * pperp[i];
+    double cc = 0.0;  // transpose of the difference operator at i
+    if (i - 1 >= 1 && i - 1 <= N - 1) cc += Rw(i - 1) / (2.0 * dpperp);
+    if (i + 1 >= 1 && i + 1 <= N - 1) cc -= Rw(i + 1) / (2.0 * dpperp);
+    if (i == 1) cc += Rw(0) / dpperp;
+    if (i == 0) cc -= Rw(0) / dpperp;
+    if (i == N) cc += Rw(N) / dpperp;
+    if (i == N - 1) cc -= Rw(N) / dpperp;
+    for (int m = 0; m < 5; ++m) {
+      m0[m] += w0 * a0 * k[m];
+      m1[m] += cc * a0 * k[m];
+    }
+  }
+  double* o = lmom + (size_t)t * 10;
+  for (int m = 0; m < 5; ++m) {
+    o[m] = m0[m];
+    o[5 + m] = m1[m];
+  }
+}
+
 template <typename T>
 int ensure(T*& ptr, size_t& cap, size_t n) {
   if (n <= cap && ptr) return ALPS_OK;
@@ -612,5 +661,42 @@ int launch_fit_aux(alps_ctx* c, int is) {
                                                          S.sp.perp_correction[1], S.sp.perp_correction[2],
                                                          S.sp.perp_correction[3], dppar, S.d_fit_aux);
   ALPS_CUDA_TRY(cudaGetLastError());
+  return ALPS_OK;
+}
+
+// Factorised Landau moments for species whose continuation is one Maxwellian
+// term; the per-item validity bound uses max |a_i|, |b_i|, |c_i| (host).
+int launch_landau_moments(alps_ctx* c, int is) {
+  SpeciesHost& S = c->spec[is];
+  S.lfact = false;
+  if (!S.d_fit_aux || S.sp.n_fits != 1 || !S.d_bessel) return ALPS_OK;
+  int N = c->sys.nperp, nmax = S.nmax;
+  std::vector<double> aux((size_t)(N + 1) * 4);
+  ALPS_CUDA_TRY(cudaMemcpyAsync(aux.data(), S.d_fit_aux, aux.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  double p2r = aux[1], p3r = aux[2], la = 0, lb = 0, lc = 0, mina0 = 1e308;
+  for (int i = 0; i <= N; ++i) {
+    double p2 = aux[i * 4 + 1], p3 = aux[i * 4 + 2];
+    la = std::max(la, std::fabs(p2 - p2r));
+    lb = std::max(lb, std::fabs(2.0 * (p2 * p3 - p2r * p3r)));
+    lc = std::max(lc, std::fabs(p2 * p3 * p3 - p2r * p3r * p3r));
+    if (i >= 1) mina0 = std::min(mina0, std::fabs(aux[i * 4 + 0]));
+    if (!std::isfinite(p2) || !std::isfinite(p3) || !std::isfinite(aux[i * 4])) return ALPS_OK;
+  }
+  int rc;
+  if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(nmax + 1) * 30))) return rc;
+  int tot = (nmax + 1) * 3;
+  double dpperp = S.pperp[2] - S.pperp[1];
+  k_landau_moments<<<(tot + 63) / 64, 64, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, N, nmax, dpperp,
+                                                          S.d_lmom);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  S.p2r = p2r;
+  S.p3r = p3r;
+  S.la = la;
+  S.lb = lb;
+  S.lc = lc;
+  S.min_a0 = mina0;
+  S.lfact = true;
   return ALPS_OK;
 }
