@@ -76,6 +76,30 @@ class alps_dist_params(C.Structure):
     ]
 
 
+MAX_ROOTS = 100
+MAX_SCANS = 8
+MAX_INPUT_SPECIES = 8
+
+
+class alps_scan_def(C.Structure):
+    _fields_ = [
+        ("type_s", C.c_int), ("swi", C.c_double), ("swf", C.c_double), ("log_scan", C.c_int),
+        ("n_out", C.c_int), ("n_res", C.c_int), ("heating", C.c_int), ("eigen", C.c_int),
+        ("diff", C.c_double), ("diff2", C.c_double),
+    ]
+
+
+class alps_input(C.Structure):
+    _fields_ = [
+        ("sys", alps_system), ("species", alps_species * MAX_INPUT_SPECIES),
+        ("runname", C.c_char * 256), ("arrayName", C.c_char * 256),
+        ("nroots", C.c_int), ("use_map", C.c_int), ("determine_minima", C.c_int),
+        ("scan_option", C.c_int), ("n_scan", C.c_int), ("ngamma", C.c_int), ("npparbar", C.c_int),
+        ("writeOut", C.c_int), ("guess", alps_complex * MAX_ROOTS), ("map", alps_map_params),
+        ("scan", alps_scan_def * MAX_SCANS),
+    ]
+
+
 class alps_stats(C.Structure):
     _fields_ = [
         ("n_eval", C.c_int64), ("n_pole_terms", C.c_int64),

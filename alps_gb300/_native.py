@@ -56,6 +56,8 @@ def lib():
             "alps_map": ([vp, P(_abi.alps_map_params), cp, cp, dp], C.c_int),
             "alps_find_minima": ([dp, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),
             "alps_run_input": ([C.c_char_p, C.c_char_p], C.c_int),
+            "alps_read_input": ([C.c_char_p, P(_abi.alps_input)], C.c_int),
+            "alps_read_f0": ([C.c_char_p, C.c_int, C.c_int, dp, dp, dp], C.c_int),
             "alps_generate_f0": ([P(_abi.alps_dist_params), C.c_int, C.c_int, dp, dp, dp, dp], C.c_int),
             "alps_get_stats": ([vp, P(_abi.alps_stats)], C.c_int),
             "alps_set_profiling": ([vp, C.c_int], C.c_int),
@@ -83,5 +85,5 @@ def exported_symbols():
         "alps_destroy", "alps_set_species", "alps_prepare", "alps_get_fit", "alps_set_fit", "alps_set_k",
         "alps_get_nmax", "alps_set_precision", "alps_disp", "alps_disp_batch", "alps_disp_batch_device",
         "alps_secant", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
-        "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc",
+        "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_read_input", "alps_read_f0",
     ]

@@ -41,6 +41,35 @@ def find_minima(val, nr, ni, numroots=100):
     return [(iroots[2 * k], iroots[2 * k + 1]) for k in range(nf.value)]
 
 
+def read_input(path):
+    """Parses an ALPS input file (init_param + scan_read) into alps_input."""
+    inp = _abi.alps_input()
+    check(lib().alps_read_input(path.encode(), C.byref(inp)), "alps_read_input")
+    return inp
+
+
+def read_f0(path, nperp, npar):
+    """Reads an f0 table file (read_f0): (pperp, ppar, f0)."""
+    n = (nperp + 1) * (npar + 1)
+    a, b, c = np.zeros(n), np.zeros(n), np.zeros(n)
+    check(lib().alps_read_f0(path.encode(), nperp, npar, _dptr(a), _dptr(b), _dptr(c)), "alps_read_f0")
+    return a, b, c
+
+
+def write_f0(path, pperp, ppar, f0):
+    """Writes an f0 table in the list-directed layout generate_distribution
+    produces (one "pperp ppar f0" line per node, 17 significant digits)."""
+    with open(path, "w") as fh:
+        for x, y, z in zip(pperp, ppar, f0):
+            fh.write("%25.17E %25.17E %25.17E\n" % (x, y, z))
+
+
+def run_input(input_path, workdir):
+    """Runs an ALPS input file end to end (map or guesses, refine_guess,
+    scans), writing the reference's output files under workdir/solution."""
+    check(lib().alps_run_input(input_path.encode(), workdir.encode()), "alps_run_input")
+
+
 class Plasma:
     """One plasma (an alps_ctx on the current CUDA device).
 

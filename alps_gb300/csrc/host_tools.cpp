@@ -118,10 +118,4 @@ int alps_find_minima(const double* val, int nr, int ni, int numroots, int* iroot
   return ALPS_OK;
 }
 
-int alps_run_input(const char* input_path, const char* workdir) {
-  (void)input_path;
-  (void)workdir;
-  return ALPS_E_UNSUPPORTED;
-}
-
 }  // extern "C"

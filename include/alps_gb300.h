@@ -219,9 +219,46 @@ int alps_map(alps_ctx* ctx, const alps_map_params* mp, alps_complex* om,
 int alps_find_minima(const double* val, int nr, int ni, int numroots,
                      int* iroots, int* nfound);
 
-/* Runs a whole ALPS input file (ALPS.f90 main program: map or guesses,
- * refine_guess, om_scan), reading f0 tables from <workdir>/distribution and
- * writing the reference's output files under <workdir>/solution. */
+/* Contents of an ALPS input file (the namelists read by init_param,
+ * src/ALPS_io.f90:46-552): &system, &guess_i or &maps_1, &spec_i,
+ * &ffit_i_j, &poly_spec_i, &bM_spec_i, &scan_input_i. */
+#define ALPS_MAX_ROOTS 100
+#define ALPS_MAX_SCANS 8
+#define ALPS_MAX_INPUT_SPECIES 8
+typedef struct alps_scan_def {
+  int type_s;                 /* scan_type 0..4                               */
+  double swi, swf;
+  int log_scan;               /* swlog                                        */
+  int n_out, n_res;           /* ns, nres                                     */
+  int heating, eigen;
+  double diff, diff2;         /* step sizes of scan_read (:426-552)           */
+} alps_scan_def;
+typedef struct alps_input {
+  alps_system sys;
+  alps_species species[ALPS_MAX_INPUT_SPECIES];
+  char runname[256], arrayName[256];
+  int nroots, use_map, determine_minima, scan_option, n_scan;
+  int ngamma, npparbar, writeOut;
+  alps_complex guess[ALPS_MAX_ROOTS];
+  alps_map_params map;
+  alps_scan_def scan[ALPS_MAX_SCANS];
+} alps_input;
+
+/* Parses an ALPS input file (init_param + scan_read, src/ALPS_io.f90:46-552):
+ * defaults of src/ALPS_var.f90, Fortran literals (1.d-2, .true., T, 'str'),
+ * `!` comments.  Missing required namelists return ALPS_E_NAMELIST. */
+int alps_read_input(const char* path, alps_input* in);
+
+/* Reads one f0 table file (read_f0, src/ALPS_io.f90:643-692): (nperp+1)*(npar+1)
+ * lines "pperp ppar f0", iperp outer. */
+int alps_read_f0(const char* path, int nperp, int npar, double* pperp,
+                 double* ppar, double* f0);
+
+/* Runs a whole ALPS input file (the main program src/ALPS.f90:19-147): map
+ * search or guesses, refine_guess, and the k scans (scan_option 1), reading
+ * f0 tables from <workdir>/distribution/<arrayName>.<is>.array and writing
+ * <workdir>/solution/<runname>.roots, .map and .scan_<id><ik>.root_<in> in
+ * the reference's formats (src/ALPS_fns.f90:2346-2584, 3745, 3849). */
 int alps_run_input(const char* input_path, const char* workdir);
 
 /* f0 table generator (distribution/generate_distribution.f90:176-300):

@@ -202,3 +202,20 @@ def test_kpar_fast_scan_on_gpu_matches_golden(api, golden_dir):
     np.testing.assert_allclose(rows, gold, rtol=1e-2)
     for a, b in zip(rows.ravel(), gold.ravel()):
         assert ("%.4E" % a) == ("%.4E" % b), (a, b)
+
+
+def test_run_input_kpar_fast_reproduces_golden_files(api, golden_dir, tmp_path):
+    """alps_run_input on the reference's CI input writes the .scan file the
+    reference's CI asserts on, byte for byte."""
+    import shutil
+    from alps_gb300.distribution import generate_distribution
+    ref = os.path.join(golden_dir, "ref")
+    generate_distribution(os.path.join(ref, "inputs", "distribution", "test_kpar_fast_dist.in"),
+                          str(tmp_path / "distribution"))
+    shutil.copyfile(os.path.join(ref, "inputs", "tests", "test_kpar_fast.in"), str(tmp_path / "test_kpar_fast.in"))
+    api.run_input(str(tmp_path / "test_kpar_fast.in"), str(tmp_path))
+    got = open(str(tmp_path / "solution" / "test_kpar_fast.scan_kpara_1.root_1")).read()
+    want = open(os.path.join(ref, "test_kpar_fast.scan_kpara_1.root_1")).read()
+    assert got == want
+    roots = open(str(tmp_path / "solution" / "test_kpar_fast.roots")).read().split()
+    assert roots[0] == "1" and len(roots) == 6
