@@ -39,7 +39,7 @@ class alps_system(C.Structure):
         ("D_gap", C.c_double), ("D_tol", C.c_double),
         ("maxsteps_fit", C.c_int), ("lambda_initial_fit", C.c_double),
         ("lambdafac_fit", C.c_double), ("epsilon_fit", C.c_double),
-        ("nproc", C.c_int),
+        ("nproc", C.c_int), ("ngamma", C.c_int), ("npparbar", C.c_int),
     ]
 
 
@@ -133,6 +133,8 @@ def system_defaults(**kw):
     s.lambdafac_fit = 10.0
     s.epsilon_fit = 1.0e-8
     s.nproc = 0
+    s.ngamma = 100
+    s.npparbar = 200
     for k, v in kw.items():
         if not hasattr(s, k):
             raise KeyError(k)

@@ -74,6 +74,8 @@ void alps_system_defaults(alps_system* s) {
   s->lambda_initial_fit = 1.0;
   s->lambdafac_fit = 10.0;
   s->epsilon_fit = 1.0e-8;
+  s->ngamma = 100;
+  s->npparbar = 200;
 }
 
 void alps_species_defaults(alps_species* sp) {

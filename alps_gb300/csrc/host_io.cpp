@@ -233,6 +233,8 @@ int alps_read_input(const char* path, alps_input* in) {
   r.i("npar", s.npar);
   r.i("ngamma", in->ngamma);
   r.i("npparbar", in->npparbar);
+  s.ngamma = in->ngamma;
+  s.npparbar = in->npparbar;
   r.d("va", s.vA);
   r.s("arrayname", in->arrayName, sizeof(in->arrayName));
   r.d("bessel_zero", s.Bessel_zero);

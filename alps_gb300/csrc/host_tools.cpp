@@ -5,6 +5,60 @@
 
 #include "../../include/alps_gb300.h"
 
+namespace {
+// Modified Bessel functions of generate_distribution
+// (distribution/generate_distribution.f90:708-868): Numerical-Recipes
+// polynomial approximations, used by the Juettner normalisation.
+double g_bessi0(double x) {
+  if (std::fabs(x) < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return 1.0 + y * (3.5156229 + y * (3.0899424 + y * (1.2067429 + y * (0.2659732 + y * (0.360768e-1 + y * 0.45813e-2)))));
+  }
+  double ax = std::fabs(x), y = 3.75 / ax, bx = std::exp(ax) / std::sqrt(ax);
+  return (0.39894228 + y * (0.1328592e-1 + y * (0.225319e-2 + y * (-0.157565e-2 + y * (0.916281e-2 +
+          y * (-0.2057706e-1 + y * (0.2635537e-1 + y * (-0.1647633e-1 + y * 0.392377e-2)))))))) * bx;
+}
+double g_bessi1(double x) {
+  if (std::fabs(x) < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return x * (0.5 + y * (0.87890594 + y * (0.51498869 + y * (0.15084934 + y * (0.2658733e-1 + y * (0.301532e-2 + y * 0.32411e-3))))));
+  }
+  double ax = std::fabs(x), y = 3.75 / ax, bx = std::exp(ax) / std::sqrt(ax);
+  return (0.39894228 + y * (-0.3988024e-1 + y * (-0.362018e-2 + y * (0.163801e-2 + y * (-0.1031555e-1 +
+          y * (0.2282967e-1 + y * (-0.2895312e-1 + y * (0.1787654e-1 + y * -0.420059e-2)))))))) * bx;
+}
+double g_bessk0(double x) {
+  if (x == 0.0) return 1.0e30;
+  if (x <= 2.0) {
+    double y = x * x / 4.0, ax = -std::log(x / 2.0) * g_bessi0(x);
+    return ax + (-0.57721566 + y * (0.42278420 + y * (0.23069756 + y * (0.3488590e-1 + y * (0.262698e-2 + y * (0.10750e-3 + y * 0.74e-5))))));
+  }
+  double y = (2.0 / x), ax = std::exp(-x) / std::sqrt(x);
+  return ax * (1.25331414 + y * (-0.7832358e-1 + y * (0.2189568e-1 + y * (-0.1062446e-1 + y * (0.587872e-2 + y * (-0.251540e-2 + y * 0.53208e-3))))));
+}
+double g_bessk1(double x) {
+  if (x == 0.0) return 1.0e32;
+  if (x <= 2.0) {
+    double y = x * x / 4.0, ax = std::log(x / 2.0) * g_bessi1(x);
+    return ax + (1.0 / x) * (1.0 + y * (0.15443144 + y * (-0.67278579 + y * (-0.18156897 + y * (-0.1919402e-1 + y * (-0.110404e-2 + y * -0.4686e-4))))));
+  }
+  double y = (2.0 / x), ax = std::exp(-x) / std::sqrt(x);
+  return ax * (1.25331414 + y * (0.23498619 + y * (-0.3655620e-1 + y * (0.1504268e-1 + y * (-0.780353e-2 + y * (0.325614e-2 + y * -0.68245e-3))))));
+}
+double g_bessk(int n, double x) {
+  if (n == 0) return g_bessk0(x);
+  if (n == 1) return g_bessk1(x);
+  if (x == 0.0) return 1.0e30;
+  double tox = 2.0 / x, bk = g_bessk1(x), bkm = g_bessk0(x), bkp;
+  for (int j = 1; j <= n - 1; ++j) {
+    bkp = bkm + (double)j * tox * bk;
+    bkm = bk;
+    bk = bkp;
+  }
+  return bk;
+}
+}  // namespace
+
 extern "C" {
 
 // generate_distribution (distribution/generate_distribution.f90:176-300):
@@ -43,6 +97,18 @@ int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* pp
     fit[3] = -1.0 - kap;
     fit[4] = 1.0;
     perpcorr = 1.0 / (tau * beta * ms * kap * a * a * alph);
+  } else if (dp->kind == 3) {  // Juettner
+    const double vA = dp->vA;
+    norm = vA / (2.0 * pi * std::sqrt(alph) * (ms * ms) * beta * tau);
+    norm = norm / g_bessk(2, 2.0 * ms / (vA * vA * alph * beta * tau));
+    if (dp->autoscale) {
+      pperp_max = std::sqrt(maxP * maxP * tau + (tau - ms * ms) / (vA * vA)) * std::sqrt(alph);
+      ppar_max = std::sqrt(maxP * maxP * tau + (tau - ms * ms) / (vA * vA));
+    }
+    fit[0] = norm;
+    fit[1] = vA * vA * alph / (ms * ms);
+    fit[2] = pd;
+    perpcorr = (2.0 * ms / (vA * vA * beta * tau * alph));
   } else if (dp->kind == 4) {  // bi-Moyal, renormalised numerically below
     if (dp->autoscale) {
       pperp_max = maxP * std::sqrt(ms * tau * alph);
@@ -64,6 +130,11 @@ int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* pp
     if (dp->kind == 2)
       return std::pow(1.0 + (d * d / (beta * ms * kap * a * a * tau)) + (p1 * p1) / (tau * beta * ms * kap * a * a * alph),
                       -1.0 - kap);
+    if (dp->kind == 3) {
+      const double vA = dp->vA;
+      return std::exp(-(2.0 * ms / (vA * vA * beta * tau * alph)) *
+                      std::sqrt(1.0 + p1 * p1 * vA * vA / (ms * ms) + d * d * vA * vA * alph / (ms * ms)));
+    }
     double q = (d * d) / (beta * ms * tau) + (p1 * p1) / (tau * beta * ms * alph);
     return std::exp(0.5 * (q - std::exp(q)));
   };

@@ -82,6 +82,8 @@ typedef struct alps_system {
   /* MPI rank count whose nmax adjustment (src/ALPS_fns.f90:4048-4071) is to
    * be reproduced; 0 means no adjustment. */
   int nproc;
+  /* (Gamma, pparbar) grid of relativistic species (src/ALPS_var.f90:128-132) */
+  int ngamma, npparbar;
 } alps_system;
 
 /* &spec_i, &ffit_i_j, &poly_spec_i, &bM_spec_i (src/ALPS_io.f90:302-419,

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <complex>
 #include <cstring>
+#include <functional>
 #include <thread>
 #include <vector>
 
@@ -133,6 +134,133 @@ double bessj(int n, double x) {
   return result;
 }
 
+// Gamma (src/ALPS_fns_rel.f90:1738-1791): the reference's Lanczos form.
+double gamma_fn(double xx) {
+  const double ONE = 1.0, FPF = 5.5, HALF = 0.5;
+  double cof[6] = {76.18009173, -86.50532033, 24.01409822, -1.231739516, 0.120858003e-2, -0.536382e-5};
+  double stp = 2.50662827465;
+  double x = xx - ONE;
+  double tmp = x + FPF;
+  tmp = (x + HALF) * std::log(tmp) - tmp;
+  double ser = ONE;
+  for (int j = 0; j < 6; ++j) {
+    x = x + ONE;
+    ser = ser + cof[j] / x;
+  }
+  return std::exp(tmp + std::log(stp * ser));
+}
+
+// Fact (src/ALPS_fns_rel.f90:1556-1574)
+double fact(int k) {
+  double f = 1.0;
+  for (int i = 2; i <= k; ++i) f = f * (1.0 * i);
+  return f;
+}
+
+// complex ** integer by binary powering (the libgfortran algorithm)
+cplx cpowi(cplx x, int n) {
+  cplx pw(1.0, 0.0);
+  if (n == 0) return pw;
+  unsigned u = (unsigned)(n < 0 ? -n : n);
+  for (;;) {
+    if (u & 1) pw = pw * x;
+    u >>= 1;
+    if (u) x = x * x;
+    else break;
+  }
+  if (n < 0) pw = 1.0 / pw;
+  return pw;
+}
+
+// CBESSJ (src/ALPS_fns_rel.f90:1502-1553): 21-term power series
+cplx cbessj(cplx z, int nu) {
+  const int MAXK = 20;
+  cplx sum(0.0, 0.0), tmp;
+  for (int k = 0; k <= MAXK; ++k) {
+    tmp = cpowi(-z * z / 4.0, k);
+    tmp = tmp / fact(k);
+    tmp = tmp / gamma_fn(1.0 * (nu + k + 1));
+    sum = sum + tmp;
+  }
+  tmp = cpowi(z / 2.0, nu);
+  return tmp * sum;
+}
+
+// Modified Bessel functions of generate_distribution (distribution/
+// generate_distribution.f90:708-868), used by the Juettner normalisation.
+double bessi0(double x) {
+  const double P1 = 1.0, P2 = 3.5156229, P3 = 3.0899424, P4 = 1.2067429, P5 = 0.2659732, P6 = 0.360768e-1,
+               P7 = 0.45813e-2;
+  const double Q1 = 0.39894228, Q2 = 0.1328592e-1, Q3 = 0.225319e-2, Q4 = -0.157565e-2, Q5 = 0.916281e-2,
+               Q6 = -0.2057706e-1, Q7 = 0.2635537e-1, Q8 = -0.1647633e-1, Q9 = 0.392377e-2;
+  if (std::fabs(x) < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7)))));
+  }
+  double ax = std::fabs(x);
+  double y = 3.75 / ax;
+  double bx = std::exp(ax) / std::sqrt(ax);
+  ax = Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * (Q7 + y * (Q8 + y * Q9)))))));
+  return ax * bx;
+}
+double bessi1(double x) {
+  const double P1 = 0.5, P2 = 0.87890594, P3 = 0.51498869, P4 = 0.15084934, P5 = 0.2658733e-1, P6 = 0.301532e-2,
+               P7 = 0.32411e-3;
+  const double Q1 = 0.39894228, Q2 = -0.3988024e-1, Q3 = -0.362018e-2, Q4 = 0.163801e-2, Q5 = -0.1031555e-1,
+               Q6 = 0.2282967e-1, Q7 = -0.2895312e-1, Q8 = 0.1787654e-1, Q9 = -0.420059e-2;
+  if (std::fabs(x) < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return x * (P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7))))));
+  }
+  double ax = std::fabs(x);
+  double y = 3.75 / ax;
+  double bx = std::exp(ax) / std::sqrt(ax);
+  ax = Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * (Q7 + y * (Q8 + y * Q9)))))));
+  return ax * bx;
+}
+double bessk0(double x) {
+  const double P1 = -0.57721566, P2 = 0.42278420, P3 = 0.23069756, P4 = 0.3488590e-1, P5 = 0.262698e-2,
+               P6 = 0.10750e-3, P7 = 0.74e-5;
+  const double Q1 = 1.25331414, Q2 = -0.7832358e-1, Q3 = 0.2189568e-1, Q4 = -0.1062446e-1, Q5 = 0.587872e-2,
+               Q6 = -0.251540e-2, Q7 = 0.53208e-3;
+  if (x == 0.0) return 1.0e30;
+  if (x <= 2.0) {
+    double y = x * x / 4.0;
+    double ax = -std::log(x / 2.0) * bessi0(x);
+    return ax + (P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7))))));
+  }
+  double y = (2.0 / x);
+  double ax = std::exp(-x) / std::sqrt(x);
+  return ax * (Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * Q7))))));
+}
+double bessk1(double x) {
+  const double P1 = 1.0, P2 = 0.15443144, P3 = -0.67278579, P4 = -0.18156897, P5 = -0.1919402e-1,
+               P6 = -0.110404e-2, P7 = -0.4686e-4;
+  const double Q1 = 1.25331414, Q2 = 0.23498619, Q3 = -0.3655620e-1, Q4 = 0.1504268e-1, Q5 = -0.780353e-2,
+               Q6 = 0.325614e-2, Q7 = -0.68245e-3;
+  if (x == 0.0) return 1.0e32;
+  if (x <= 2.0) {
+    double y = x * x / 4.0;
+    double ax = std::log(x / 2.0) * bessi1(x);
+    return ax + (1.0 / x) * (P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7))))));
+  }
+  double y = (2.0 / x);
+  double ax = std::exp(-x) / std::sqrt(x);
+  return ax * (Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * Q7))))));
+}
+double bessk(int n, double x) {
+  if (n == 0) return bessk0(x);
+  if (n == 1) return bessk1(x);
+  if (x == 0.0) return 1.0e30;
+  double tox = 2.0 / x, bk = bessk1(x), bkm = bessk0(x), bkp;
+  for (int j = 1; j <= n - 1; ++j) {
+    bkp = bkm + (double)j * tox * bk;
+    bkm = bk;
+    bk = bkp;
+  }
+  return bk;
+}
+
 // ---------------------------------------------------------------------------
 // Small LU helpers standing in for LAPACK dgetrf/dgetri/dgesv
 // (src/ALPS_analyt.f90:1571-1575, 830-839): Gaussian elimination with
@@ -196,6 +324,17 @@ struct Species {
   double& PF(int i, int ip, int ifit) { return param_fit[(i * 5 + ip) * nf() + ifit]; }
   double PFc(int i, int ip, int ifit) const { return param_fit[(i * 5 + ip) * nf() + ifit]; }
   double B(int n, int i) const { return bessel[(n + 1) * (nperp + 1) + i]; }
+  // relativistic (Gamma, pparbar) grid, src/ALPS_fns_rel.f90:36-289
+  int ng = 0, np = 0;
+  std::vector<double> grel, prel, f0rel, dfr1, dfr2;  // [(ng+1)*(np+1)]
+  int ridx(int ig, int ip) const { return ig * (np + 1) + ip; }
+  double G(int ig, int ip) const { return grel[ridx(ig, ip)]; }
+  double PB(int ig, int ip) const { return prel[ridx(ig, ip)]; }
+  // f0_rel with out-of-range reads treated as outside the subluminal cone
+  double FR(int ig, int ip) const {
+    if (ip < 0 || ip > np || ig < 0 || ig > ng) return -1.0;
+    return f0rel[ridx(ig, ip)];
+  }
 };
 
 }  // namespace
@@ -240,6 +379,12 @@ cplx fit_function(const Species& s, const double* params, double pperp_val,
       cplx d = ppar_val - p[2];
       cplx sqrtpart = std::sqrt(1.0 + ((pperp_val * pperp_val) + d * d) * vA * vA / (s.sp.ms * s.sp.ms));
       ff = ff + p[0] * std::exp(-p[1] * sqrtpart);
+      par_ind += 2;
+    } else if (t == 4) {
+      ff = ff + p[0] * std::exp(-pc * pperp_val);
+    } else if (t == 5) {
+      cplx d = ppar_val - p[2];
+      ff = ff + p[0] * std::exp(-pc * pperp_val) * std::exp(-p[1] * (d * d));
       par_ind += 2;
     } else if (t == 6) {
       cplx d = ppar_val - p[2];
@@ -292,7 +437,14 @@ cplx eval_fit(const Eval& e, int is1, int iperp, cplx ppar_valC) {
   if (s.sp.ac_method == 0) return distribution_analyt(is1, s.P1(iperp, 1), ppar_valC);
   double params[5 * ALPS_MAX_FITS];
   gather_params(s, iperp, params);
-  return fit_function(s, params, s.P1(iperp, 1), ppar_valC, e.c->sys.vA);
+  // pperp_val: pp(is,iperp,1,1), or gamma_rel(.,iperp,1) for the (Gamma,
+  // pparbar) fit types 4 and 5 (the last fit term decides, as in the loop)
+  double pperp_val = 0.0;
+  for (int f = 0; f < s.sp.n_fits; ++f) {
+    int t = s.sp.fit_type[f];
+    pperp_val = (t == 4 || t == 5) ? s.G(iperp, 1) : s.P1(iperp, 1);
+  }
+  return fit_function(s, params, pperp_val, ppar_valC, e.c->sys.vA);
 }
 
 // ---------------------------------------------------------------------------
@@ -302,6 +454,10 @@ inline cplx resU(const Eval& e, cplx om, int nn, int iperp, int ipar) {
   const Species& s = *e.s;
   int k = s.idx(iperp, ipar);
   double gamma = 1.0;
+  if (s.sp.relat) {
+    double vA = e.c->sys.vA;
+    gamma = std::sqrt((s.pp1[k] * s.pp1[k] + s.pp2[k] * s.pp2[k]) * (vA * vA) / (s.sp.ms * s.sp.ms) + 1.0);
+  }
   return s.sp.qs * (om * s.df1[k] + (e.kpar / (gamma * s.sp.ms)) *
                                       (s.pp1[k] * s.df2[k] - s.pp2[k] * s.df1[k])) /
          (gamma * s.sp.ms * om - e.kpar * s.pp2[k] - (1.0 * nn) * s.sp.qs);
@@ -623,6 +779,461 @@ cplx landau_integrate(const Eval& e, int is1, cplx om, int nn, int mode) {
   return land;
 }
 
+// ===========================================================================
+// Relativistic branch (src/ALPS_fns_rel.f90)
+// ===========================================================================
+inline double cube(double x) { return x * x * x; }
+
+// resU_rel (src/ALPS_fns_rel.f90:1220-1249)
+cplx resU_rel(const Eval& e, cplx om, int nn, int ig, int ip) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA, kpar = e.kpar;
+  int k = s.ridx(ig, ip);
+  return -2.0 * PI * cube(ms / vA) * (qs * vA / (kpar * ms)) * (om * s.dfr1[k] + (kpar / (vA)) * s.dfr2[k]) /
+         (s.prel[k] - s.grel[k] * om * vA / kpar + (1.0 * nn) * qs * vA / (kpar * ms));
+}
+
+// Bessel lookups by direct BESSJ calls (int_T_rel, :1297-1329)
+template <typename T, typename F>
+void bessel_pair_fn(int nn, F J, T& bessel, T& besselP) {
+  if (nn < 0) bessel = ((nn % 2 == 0) ? 1.0 : -1.0) * J(-nn);
+  else bessel = J(nn);
+  if (nn >= 1) {
+    besselP = 0.5 * (J(nn - 1) - J(nn + 1));
+  } else if (nn < -1) {
+    double sm1 = ((nn - 1) % 2 == 0) ? 1.0 : -1.0;
+    double sp1 = ((nn + 1) % 2 == 0) ? 1.0 : -1.0;
+    besselP = 0.5 * ((sm1 * J(-(nn - 1))) - (sp1 * J(-(nn + 1))));
+  } else if (nn == 0) {
+    besselP = -J(1);
+  } else {
+    besselP = 0.5 * (J(2) - J(0));
+  }
+}
+
+// int_T_rel (src/ALPS_fns_rel.f90:1256-1369)
+cplx int_T_rel(const Eval& e, int nn, int ig, int ip, int mode) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA, kperp = e.kperp;
+  bool kn = e.c->sys.kperp_norm != 0;
+  double g = s.G(ig, ip), pb = s.PB(ig, ip);
+  double pperpbar = std::sqrt(g * g - 1.0 - pb * pb);
+  double z = (kperp * ms / (vA * qs)) * pperpbar;
+  double zbar = kn ? kperp * ms / (vA * qs) : ms / (vA * qs);
+  double bessel, besselP;
+  bessel_pair_fn(nn, [&](int n) { return bessj(n, z); }, bessel, besselP);
+  switch (mode) {
+    case 1: return cplx(1.0 * (nn * nn) * bessel * bessel / (zbar * zbar), 0.0);
+    case 2:
+      return kn ? cplx(besselP * besselP * pperpbar * pperpbar, 0.0)
+                : cplx(kperp * kperp * besselP * besselP * pperpbar * pperpbar, 0.0);
+    case 3:
+      return kn ? cplx(bessel * bessel * (pb * pb), 0.0) : cplx(kperp * kperp * bessel * bessel * (pb * pb), 0.0);
+    case 4:
+      return kn ? II * (1.0 * (nn)) * bessel * besselP * pperpbar / zbar
+                : II * (1.0 * (nn)) * kperp * bessel * besselP * pperpbar / zbar;
+    case 5:
+      return kn ? cplx((1.0 * nn) * bessel * bessel * pb / zbar, 0.0)
+                : cplx((1.0 * nn) * kperp * bessel * bessel * pb / zbar, 0.0);
+    case 6:
+      return kn ? (-1.0 * II) * bessel * besselP * pb * pperpbar
+                : (-1.0 * II) * kperp * kperp * bessel * besselP * pb * pperpbar;
+  }
+  return cplx(0, 0);
+}
+
+// int_T_res_rel (src/ALPS_fns_rel.f90:1374-1495)
+cplx int_T_res_rel(const Eval& e, int nn, int ig, cplx pparbar, int mode) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA, kperp = e.kperp;
+  bool kn = e.c->sys.kperp_norm != 0;
+  double g = s.G(ig, 1);
+  cplx pperpbar = std::sqrt(g * g - 1.0 - pparbar * pparbar);
+  cplx z = (kperp * ms / (vA * qs)) * pperpbar;
+  double zbar = kn ? kperp * ms / (vA * qs) : ms / (vA * qs);
+  cplx bessel, besselP;
+  bessel_pair_fn(nn, [&](int n) { return cbessj(z, n); }, bessel, besselP);
+  switch (mode) {
+    case 1: return 1.0 * (nn * nn) * bessel * bessel / (zbar * zbar);
+    case 2:
+      return kn ? besselP * besselP * pperpbar * pperpbar : kperp * kperp * besselP * besselP * pperpbar * pperpbar;
+    case 3: return kn ? bessel * bessel * (pparbar * pparbar) : kperp * kperp * bessel * bessel * (pparbar * pparbar);
+    case 4:
+      return kn ? II * (1.0 * (nn)) * bessel * besselP * pperpbar / zbar
+                : II * (1.0 * (nn)) * kperp * bessel * besselP * pperpbar / zbar;
+    case 5:
+      return kn ? (1.0 * nn) * bessel * bessel * pparbar / zbar : (1.0 * nn) * kperp * bessel * bessel * pparbar / zbar;
+    case 6:
+      return kn ? (-1.0 * II) * bessel * besselP * pparbar * pperpbar
+                : (-1.0 * II) * kperp * kperp * bessel * besselP * pparbar * pperpbar;
+  }
+  return cplx(0, 0);
+}
+
+// pparbar limits of the subluminal cone on row ig (:603-617)
+void cone_limits(const Species& s, int ig, int& lower, int& upper) {
+  bool fl = false, fu = false;
+  lower = 1;
+  upper = s.np - 1;
+  for (int ip = 1; ip <= s.np - 1; ++ip) {
+    if (!fl && s.FR(ig, ip - 1) <= -1.0 && s.FR(ig, ip) > -1.0) { lower = ip; fl = true; }
+    if (!fu && s.FR(ig, ip) > -1.0 && s.FR(ig, ip + 1) <= -1.0) { upper = ip; fu = true; }
+  }
+}
+
+// funct_g_rel (src/ALPS_fns_rel.f90:918-999)
+cplx funct_g_rel(const Eval& e, double pparbar, int ig, cplx om, int nn, int mode) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA, kpar = e.kpar;
+  int np = s.np;
+  double dpparbar = s.PB(2, 2) - s.PB(2, 1);
+  // the unique ip in 0..np-1 with prel(ip) <= pparbar < prel(ip+1) on the
+  // increasing grid (the reference loops over all ip, last match wins)
+  int close = -2;
+  if (pparbar >= s.PB(ig, 0) && pparbar < s.PB(ig, np)) {
+    int lo = 0, hi = np - 1;
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (s.PB(ig, mid) <= pparbar) lo = mid;
+      else hi = mid - 1;
+    }
+    close = lo;
+  }
+  if (s.FR(ig, close + 1) <= -1.0) close = close - 1;
+  if (s.FR(ig, close - 1) <= -1.0) close = close + 1;
+  if (pparbar == s.PB(ig, np)) close = np - 2;
+  if (close >= (np - 1)) close = np - 2;
+  if (close <= 1) close = 2;
+  auto integrand = [&](int ip) {
+    int k = s.ridx(ig, ip);
+    return -2.0 * PI * cube(ms / vA) * (qs * vA / (kpar * ms)) * (om * s.dfr1[k] + (kpar / (vA)) * s.dfr2[k]) *
+           int_T_rel(e, nn, ig, ip, mode);
+  };
+  cplx plus = integrand(close + 1), mid = integrand(close), minus = integrand(close - 1);
+  return mid + 0.5 * ((plus - minus) / dpparbar) * (pparbar - s.PB(ig, close));
+}
+
+// principal_integral_rel (src/ALPS_fns_rel.f90:724-913)
+cplx principal_integral_rel(const Eval& e, cplx om, int nn, int mode, int ig, int ipres, int upperlimit) {
+  const Species& s = *e.s;
+  const alps_system& sy = e.c->sys;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = sy.vA, kpar = e.kpar;
+  int M_I = sy.positions_principal, M_P = sy.n_resonance_interval;
+  cplx pi_(0.0, 0.0);
+  double dpparbar = s.PB(2, 2) - s.PB(2, 1);
+  cplx t1 = s.G(ig, ipres) * om * vA / kpar;
+  double denomR = (t1 - (1.0 * nn) * (qs / ms) * vA / kpar).real();
+  double denomI = (s.G(ig, ipres) * om * vA / kpar).imag();
+  double capDelta = denomR - s.PB(1, ipres - M_I);
+  double smdelta = capDelta / (1.0 * M_P);
+  auto G = [&](double p) { return funct_g_rel(e, p, ig, om, nn, mode); };
+  double pp;
+  if (std::fabs(denomI) > sy.Tlim) {
+    pp = denomR;
+    pi_ = pi_ + 1.0 * G(pp) / (pp - denomR - II * denomI);
+    pi_ = pi_ - 1.0 * G(2.0 * denomR - pp) / (pp - denomR + II * denomI);
+    pp = denomR + capDelta;
+    pi_ = pi_ + 1.0 * G(pp) / (pp - denomR - II * denomI);
+    pi_ = pi_ - 1.0 * G(2.0 * denomR - pp) / (pp - denomR + II * denomI);
+    for (int ip = 1; ip <= M_P - 1; ++ip) {
+      pp = denomR + smdelta * ip;
+      pi_ = pi_ + 2.0 * G(pp) / (pp - denomR - II * denomI);
+      pi_ = pi_ - 2.0 * G(2.0 * denomR - pp) / (pp - denomR + II * denomI);
+    }
+  } else {
+    cplx gp = (G(denomR + dpparbar) - G(denomR - dpparbar)) / (2.0 * dpparbar);
+    pp = denomR + capDelta;
+    pi_ = pi_ + 2.0 * gp * (pp - denomR) * (pp - denomR) / ((pp - denomR) * (pp - denomR) + denomI * denomI);
+    for (int ip = 1; ip <= M_P - 1; ++ip) {
+      pp = denomR + smdelta * ip;
+      pi_ = pi_ + 2.0 * 2.0 * gp * (pp - denomR) * (pp - denomR) / ((pp - denomR) * (pp - denomR) + denomI * denomI);
+    }
+    if (denomI > 0.0) pi_ = pi_ + 2.0 * II * PI * G(denomR) / smdelta;
+    else if (denomI < 0.0) pi_ = pi_ - 2.0 * II * PI * G(denomR) / smdelta;
+  }
+  int ntiny = (int)((s.PB(ig, upperlimit) - denomR - capDelta) / smdelta);
+  if (ntiny > 0) {
+    double correction = ((s.PB(ig, upperlimit) - denomR - capDelta) / (1.0 * ntiny)) / smdelta;
+    pp = denomR + capDelta;
+    pi_ = pi_ + 1.0 * correction * (G(pp) / (pp - denomR - II * denomI));
+    pp = denomR + capDelta + correction * smdelta * ntiny;
+    pi_ = pi_ + 1.0 * correction * (G(pp) / (pp - denomR - II * denomI));
+    for (int ip = 1; ip <= ntiny - 1; ++ip) {
+      pp = denomR + capDelta + correction * smdelta * ip;
+      pi_ = pi_ + 2.0 * correction * (G(pp) / (pp - denomR - II * denomI));
+    }
+  }
+  return pi_ * smdelta;
+}
+
+// integrate_resU_rel (src/ALPS_fns_rel.f90:516-719); err set on alps_error(8)
+cplx integrate_resU_rel(const Eval& e, cplx om, int nn, int mode, int ig, int& err) {
+  const Species& s = *e.s;
+  const alps_system& sy = e.c->sys;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = sy.vA, kpar = e.kpar;
+  int M_I = sy.positions_principal, np = s.np;
+  cplx res(0.0, 0.0);
+  double dpparbar = s.PB(2, 2) - s.PB(2, 1);
+  int ipres = 0;
+  bool found = false;
+  cplx pres = (s.G(ig, 1) * om - (1.0 * nn) * qs / ms) * vA / kpar;
+  double x = pres.real();
+  if ((x * x) <= (s.G(ig, 1) * s.G(ig, 1) - 1.0)) {
+    int ip = 0;
+    while ((ip < (np - 2)) && (!found)) {
+      ip = ip + 1;
+      if ((s.PB(2, ip + 1) > x) && (s.PB(2, ip) <= x)) {
+        ipres = ip;
+        found = true;
+      }
+    }
+  }
+  for (int ip = 0; ip <= M_I; ++ip) {
+    if ((x >= (s.PB(2, 0) - dpparbar * ip)) && (x < (s.PB(2, 0) - dpparbar * (ip - 1)))) {
+      ipres = -ip;
+      found = true;
+    }
+    if ((x >= (s.PB(2, np - 1) + dpparbar * ip)) && (x < (s.PB(2, np - 1) + dpparbar * (ip + 1)))) {
+      ipres = np - 1 + ip;
+      found = true;
+    }
+  }
+  int lowerC, upperC;
+  cone_limits(s, ig, lowerC, upperC);
+  int int_start, int_end, lowerlimit, upperlimit;
+  if (found) {
+    int_start = lowerC;
+    int_end = upperC;
+    lowerlimit = ipres - M_I;
+    upperlimit = ipres + M_I + 1;
+    if ((ipres >= 0) && (ipres <= np))
+      if (std::fabs(x - s.PB(2, ipres)) > (0.5 * dpparbar)) upperlimit = upperlimit + 1;
+    if ((lowerlimit < lowerC) && (upperlimit > upperC)) {
+      err = ALPS_E_SUBLUMINAL;
+      return cplx(0, 0);
+    } else if (lowerlimit <= lowerC) {
+      int_start = 1;
+      lowerlimit = 0;
+      upperlimit = lowerC;
+    } else if (upperlimit >= upperC) {
+      lowerlimit = upperC;
+      upperlimit = np;
+      int_end = np - 1;
+    }
+  } else {
+    int_start = lowerC;
+    lowerlimit = upperC;
+    int_end = np - 1;
+    upperlimit = np;
+  }
+  auto term = [&](int ip) { return resU_rel(e, om, nn, ig, ip) * int_T_rel(e, nn, ig, ip, mode); };
+  if (int_start <= lowerlimit) res = res + term(int_start);
+  for (int ip = int_start + 1; ip <= lowerlimit - 1; ++ip) res = res + 2.0 * term(ip);
+  if (int_start < lowerlimit) res = res + term(lowerlimit);
+  if (upperlimit <= int_end) res = res + term(upperlimit);
+  for (int ip = upperlimit + 1; ip <= int_end - 1; ++ip) res = res + 2.0 * term(ip);
+  if (upperlimit < int_end) res = res + term(int_end);
+  res = res * dpparbar;
+  if (found && (lowerlimit >= int_start) && (upperlimit <= int_end))
+    res = res + principal_integral_rel(e, om, nn, mode, ig, ipres, upperlimit);
+  return res;
+}
+
+// integrate_res_rel (src/ALPS_fns_rel.f90:460-511)
+cplx integrate_res_rel(const Eval& e, cplx om, int nn, int mode, int& err) {
+  const Species& s = *e.s;
+  cplx res(0.0, 0.0);
+  double dgamma = s.G(2, 2) - s.G(1, 2);
+  for (int ig = 1; ig <= s.ng - 2; ++ig) res = res + 2.0 * integrate_resU_rel(e, om, nn, mode, ig, err);
+  res = res + integrate_resU_rel(e, om, nn, mode, s.ng - 1, err);
+  return res * dgamma * 0.25;
+}
+
+// landau_integrate_rel (src/ALPS_fns_rel.f90:1005-1092)
+cplx landau_integrate_rel(const Eval& e, int is1, cplx om, int nn, int mode) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA, kpar = e.kpar;
+  cplx land(0.0, 0.0);
+  double dgamma = s.G(2, 2) - s.G(1, 2);
+  double dpparbar = s.PB(2, 2) - s.PB(2, 1);
+  for (int ig = 1; ig <= s.ng - 1; ++ig) {
+    cplx pres = s.G(ig, 1) * om * vA / kpar - (1.0 * nn) * qs * vA / (kpar * ms);
+    if ((pres.real() * pres.real()) <= (s.G(ig, 1) * s.G(ig, 1) - 1.0)) {
+      double h = 1.0;
+      if (ig == (s.ng - 1)) h = 0.5;
+      cplx dfg;
+      if (ig == 1) dfg = (eval_fit(e, is1, ig + 1, pres) - eval_fit(e, is1, ig, pres)) / dgamma;
+      else dfg = (eval_fit(e, is1, ig + 1, pres) - eval_fit(e, is1, ig - 1, pres)) / (2.0 * dgamma);
+      cplx dfp = (eval_fit(e, is1, ig, pres + dpparbar) - eval_fit(e, is1, ig, pres - dpparbar)) / (2.0 * dpparbar);
+      land = land - h * (om * dfg + (kpar / (vA)) * dfp) * int_T_res_rel(e, nn, ig, pres, mode);
+    }
+  }
+  return land * II * dgamma * PI * 2.0 * PI * (qs * vA / (kpar * ms)) * cube(ms / vA);
+}
+
+// int_ee_rel (src/ALPS_fns_rel.f90:1097-1215)
+cplx int_ee_rel(const Eval& e) {
+  const Species& s = *e.s;
+  double ms = s.sp.ms, qs = s.sp.qs, vA = e.c->sys.vA;
+  double dgamma = s.G(2, 2) - s.G(1, 2);
+  double dpparbar = s.PB(2, 2) - s.PB(2, 1);
+  cplx ie(0.0, 0.0);
+  int ig = s.ng - 1, lo, up;
+  cone_limits(s, ig, lo, up);
+  auto t = [&](int g, int p) { return s.PB(g, p) * s.dfr2[s.ridx(g, p)]; };
+  ie = ie + t(ig, lo);
+  ie = ie + t(ig, up);
+  for (int ip = lo + 1; ip <= up - 1; ++ip) ie = ie + 2.0 * t(ig, ip);
+  for (ig = 1; ig <= s.ng - 2; ++ig) {
+    cone_limits(s, ig, lo, up);
+    for (int ip = lo + 1; ip <= up - 1; ++ip) ie = ie + 4.0 * t(ig, ip);
+    ie = ie + 2.0 * t(ig, lo);
+    ie = ie + 2.0 * t(ig, up);
+  }
+  ie = ie * 2.0 * PI * qs / (ms);
+  ie = ie * dgamma * dpparbar * 0.25 * cube(ms / vA);
+  return ie;
+}
+
+// polyharmonic_spline (src/ALPS_fns_rel.f90:293-426): thin-plate spline of
+// the coarse samples, solved densely (dgesv), evaluated on the fine grid.
+int polyharmonic_spline(const std::vector<double>& grid, const std::vector<double>& gc,
+                        const std::vector<double>& pc, Species& s, std::vector<double>& out) {
+  int n = (int)grid.size(), m = n + 3;
+  auto phi = [](double r) {
+    if (r >= 1.0) return r * r * std::log(r);
+    if (r == 0.0) return 0.0;
+    return r * std::log(std::pow(r, r));
+  };
+  std::vector<double> A((size_t)m * m, 0.0), w(m, 0.0);  // column-major
+  for (int i = 0; i < n; ++i) {
+    w[i] = grid[i];
+    for (int j = 0; j < n; ++j) {
+      double dg = gc[i] - gc[j], dp = pc[i] - pc[j];
+      A[(size_t)i + (size_t)m * j] = phi(std::sqrt(dg * dg + dp * dp));
+    }
+    A[(size_t)i + (size_t)m * n] = 1.0;
+    A[(size_t)i + (size_t)m * (n + 1)] = gc[i];
+    A[(size_t)i + (size_t)m * (n + 2)] = pc[i];
+    A[(size_t)n + (size_t)m * i] = 1.0;
+    A[(size_t)(n + 1) + (size_t)m * i] = gc[i];
+    A[(size_t)(n + 2) + (size_t)m * i] = pc[i];
+  }
+  // LU with partial pivoting, column-oriented updates
+  std::vector<int> piv(m);
+  for (int k = 0; k < m; ++k) {
+    int p = k;
+    double mx = std::fabs(A[(size_t)k + (size_t)m * k]);
+    for (int i = k + 1; i < m; ++i)
+      if (std::fabs(A[(size_t)i + (size_t)m * k]) > mx) { mx = std::fabs(A[(size_t)i + (size_t)m * k]); p = i; }
+    piv[k] = p;
+    if (A[(size_t)p + (size_t)m * k] == 0.0) return ALPS_E_SINGULAR;
+    if (p != k)
+      for (int j = 0; j < m; ++j) std::swap(A[(size_t)k + (size_t)m * j], A[(size_t)p + (size_t)m * j]);
+    double dk = A[(size_t)k + (size_t)m * k];
+    for (int i = k + 1; i < m; ++i) A[(size_t)i + (size_t)m * k] /= dk;
+    for (int j = k + 1; j < m; ++j) {
+      double f = A[(size_t)k + (size_t)m * j];
+      if (f == 0.0) continue;
+      double* colj = &A[(size_t)m * j];
+      const double* colk = &A[(size_t)m * k];
+      for (int i = k + 1; i < m; ++i) colj[i] -= colk[i] * f;
+    }
+  }
+  for (int k = 0; k < m; ++k) std::swap(w[k], w[piv[k]]);
+  for (int j = 0; j < m; ++j)
+    for (int i = j + 1; i < m; ++i) w[i] -= A[(size_t)i + (size_t)m * j] * w[j];
+  for (int j = m - 1; j >= 0; --j) {
+    w[j] /= A[(size_t)j + (size_t)m * j];
+    for (int i = 0; i < j; ++i) w[i] -= A[(size_t)i + (size_t)m * j] * w[j];
+  }
+  out.assign((size_t)(s.ng + 1) * (s.np + 1), 0.0);
+  for (int i = 0; i <= s.ng; ++i)
+    for (int j = 0; j <= s.np; ++j) {
+      double f = 0.0, gi = s.G(i, j), pj = s.PB(i, j);
+      for (int k = 0; k < n; ++k) {
+        double dg = gi - gc[k], dp = pj - pc[k];
+        double r = std::sqrt(dg * dg + dp * dp);
+        if (r >= 1.0) f = f + w[k] * r * r * std::log(r);
+        else if (r != 0.0) f = f + w[k] * r * std::log(std::pow(r, r));
+      }
+      f = f + w[n] + w[n + 1] * gi + w[n + 2] * pj;
+      out[s.ridx(i, j)] = f;
+    }
+  return ALPS_OK;
+}
+
+// derivative_f0_rel (src/ALPS_fns_rel.f90:36-289)
+int derivative_f0_rel(Species& s, double vA) {
+  double ms = s.sp.ms;
+  double pmin = 999999.0, pmax = -999999.0, gmin = 999999.0, gmax = -1.0;
+  for (int i = 0; i <= s.nperp; ++i)
+    for (int j = 0; j <= s.npar; ++j) {
+      double p1 = s.P1(i, j), p2 = s.P2(i, j);
+      double g = std::sqrt((p1 * p1 + p2 * p2) * (vA * vA) / (ms * ms) + 1.0);
+      if (g > gmax) gmax = g;
+      if (g < gmin) gmin = g;
+      if (p2 < pmin) pmin = p2;
+      if (p2 > pmax) pmax = p2;
+    }
+  pmin = pmin * vA / ms;
+  pmax = pmax * vA / ms;
+  double pn = s.P1(s.nperp, 1);
+  double gmax_use = std::sqrt(1.0 + pn * pn * (vA * vA) / (ms * ms));
+  int n = (s.nperp + 1) * (s.npar + 1);
+  std::vector<double> gc(n), pc(n), grid(n);
+  int cnt = 0;
+  for (int i = 0; i <= s.nperp; ++i)
+    for (int j = 0; j <= s.npar; ++j) {
+      double p1 = s.P1(i, j), p2 = s.P2(i, j);
+      gc[cnt] = std::sqrt(1.0 + (p1 * p1 + p2 * p2) * vA * vA / (ms * ms));
+      pc[cnt] = p2 * vA / ms;
+      grid[cnt] = std::log(s.f0[s.idx(i, j)]);
+      ++cnt;
+    }
+  s.grel.assign((size_t)(s.ng + 1) * (s.np + 1), 0.0);
+  s.prel.assign((size_t)(s.ng + 1) * (s.np + 1), 0.0);
+  for (int ig = 0; ig <= s.ng; ++ig)
+    for (int ip = 0; ip <= s.np; ++ip) {
+      s.grel[s.ridx(ig, ip)] = gmin + ((gmax_use - gmin) * ig) / (1.0 * s.ng);
+      s.prel[s.ridx(ig, ip)] = pmin + ((pmax - pmin) * ip) / (1.0 * s.np);
+    }
+  int st = polyharmonic_spline(grid, gc, pc, s, s.f0rel);
+  if (st) return st;
+  for (int ig = 0; ig <= s.ng; ++ig)
+    for (int ip = 0; ip <= s.np; ++ip) {
+      double& f = s.f0rel[s.ridx(ig, ip)];
+      f = std::exp(f);
+      double g = s.G(ig, ip), pb = s.PB(ig, ip);
+      if ((g * g - 1.0) < (pb * pb)) f = -1.0;
+    }
+  double integ = 0.0;
+  double dgamma = s.G(2, 2) - s.G(1, 2), dpb = s.PB(2, 2) - s.PB(2, 1);
+  for (int ig = 0; ig <= s.ng; ++ig)
+    for (int ip = 0; ip <= s.np; ++ip)
+      if (s.FR(ig, ip) > -1.0)
+        integ = integ + s.G(ig, ip) * s.FR(ig, ip) * 2.0 * PI * dgamma * dpb * cube(ms / vA);
+  for (auto& f : s.f0rel)
+    if (f != -1.0) f = f / integ;
+  s.dfr1.assign(s.f0rel.size(), 0.0);
+  s.dfr2.assign(s.f0rel.size(), 0.0);
+  for (int ig = 1; ig <= s.ng - 1; ++ig)
+    for (int ip = 1; ip <= s.np - 1; ++ip) {
+      int k = s.ridx(ig, ip);
+      if ((s.FR(ig - 1, ip) > 0.0) && (s.FR(ig + 1, ip) > 0.0))
+        s.dfr1[k] = (s.FR(ig + 1, ip) - s.FR(ig - 1, ip)) / (s.G(ig + 1, ip) - s.G(ig - 1, ip));
+      if ((s.FR(ig, ip + 1) > 0.0) && (s.FR(ig, ip - 1) > 0.0))
+        s.dfr2[k] = (s.FR(ig, ip + 1) - s.FR(ig, ip - 1)) / (s.PB(ig, ip + 1) - s.PB(ig, ip - 1));
+      if (s.FR(ig, ip) >= 0.0) {
+        if ((s.FR(ig, ip + 1) <= 0.0) && (s.FR(ig, ip - 1) > 0.0))
+          s.dfr2[k] = (s.FR(ig, ip) - s.FR(ig, ip - 1)) / (s.PB(ig, ip) - s.PB(ig, ip - 1));
+        if ((s.FR(ig, ip + 1) > 0.0) && (s.FR(ig, ip - 1) <= 0.0))
+          s.dfr2[k] = (s.FR(ig, ip + 1) - s.FR(ig, ip)) / (s.PB(ig, ip + 1) - s.PB(ig, ip));
+      }
+    }
+  return ALPS_OK;
+}
+
 // determine_resonances (src/ALPS_fns.f90:641-745), non-relativistic branch
 void determine_resonances(const Eval& e, cplx om, int nn, bool& plus, bool& minus) {
   const Species& s = *e.s;
@@ -630,6 +1241,19 @@ void determine_resonances(const Eval& e, cplx om, int nn, bool& plus, bool& minu
   double dppar = s.P2(2, 2) - s.P2(2, 1);
   plus = false;
   minus = false;
+  if (s.sp.relat) {
+    double vA = e.c->sys.vA, ms = s.sp.ms;
+    for (int iperp = 0; iperp <= s.nperp; ++iperp)
+      for (int ip = 0; ip <= npar - 1; ++ip) {
+        double p1 = s.P1(iperp, ip), p2 = s.P2(iperp, ip);
+        double gamma = std::sqrt((p1 * p1 + p2 * p2) * (vA * vA) / (ms * ms) + 1.0);
+        cplx pr = (gamma * ms * om - 1.0 * nn * s.sp.qs) / e.kpar;
+        if ((s.P2(2, ip) <= pr.real()) && (s.P2(2, ip + 1) > pr.real())) plus = true;
+        pr = (gamma * ms * om + 1.0 * nn * s.sp.qs) / e.kpar;
+        if ((s.P2(2, ip) <= pr.real()) && (s.P2(2, ip + 1) > pr.real())) minus = true;
+      }
+    return;
+  }
   int ipar = 0;
   cplx p_res = (s.sp.ms * om - 1.0 * nn * s.sp.qs) / e.kpar;
   while ((ipar <= (npar - 2)) && (!plus)) {
@@ -653,8 +1277,18 @@ void determine_resonances(const Eval& e, cplx om, int nn, bool& plus, bool& minu
 }
 
 // full_integrate (src/ALPS_fns.f90:750-792), non-relativistic branch
+int g_rel_err = 0;  // alps_error(8) raised inside a relativistic integral
+
 cplx full_integrate(const Eval& e, int is1, cplx om, int nn, int mode, bool found_res) {
   if (!found_res) return integrate(e, om, nn, mode, 1, e.s->npar - 1);
+  if (e.s->sp.relat) {
+    int err = 0;
+    cplx r = integrate_res_rel(e, om, nn, mode, err);
+    if (err) g_rel_err = err;
+    if (om.imag() > 0.0) return r;
+    if (om.imag() < 0.0) return r + 2.0 * landau_integrate_rel(e, is1, om, nn, mode);
+    return r + landau_integrate_rel(e, is1, om, nn, mode);
+  }
   if (om.imag() > 0.0) return integrate_res(e, om, nn, mode);
   if (om.imag() < 0.0) return integrate_res(e, om, nn, mode) + 2.0 * landau_integrate(e, is1, om, nn, mode);
   return integrate_res(e, om, nn, mode) + landau_integrate(e, is1, om, nn, mode);
@@ -850,7 +1484,10 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
         }
       }
     }
-    if (r.nlim1 == 0) {
+    if (r.nlim1 == 0 && s.sp.relat) {
+      cplx ee = int_ee_rel(e);
+      CH(schi, sproc, 3, 3) = CH(schi, sproc, 3, 3) + (c->sys.kperp_norm ? ee : kperp * kperp * ee);
+    } else if (r.nlim1 == 0) {
       cplx ee = int_ee(e);
       mag[(sproc - 1) * 9 + 8] += std::abs(ee) * std::fabs(s.sp.ns * s.sp.qs) *
                                   (c->sys.kperp_norm ? 1.0 : kperp * kperp);
@@ -962,11 +1599,14 @@ void derivative_f0(Species& s) {
 }
 
 // determine_JT (src/ALPS_analyt.f90:1183-1389), non-relativistic types
+typedef std::function<void(int, double&, double&)> Coords;
+
 void determine_JT(const Species& s, int nJT, std::vector<double>& JT, const double* params, int iperp,
-                  int upper_limit, double vA) {
+                  int upper_limit, double vA, const Coords& coords) {
   // JT[(k-1) + nJT*ipar], k=1..nJT, ipar=0..upper_limit
   for (int ipar = 0; ipar <= upper_limit; ++ipar) {
-    double pperp_val = s.P1(iperp, ipar), ppar_val = s.P2(iperp, ipar);
+    double pperp_val, ppar_val;
+    coords(ipar, pperp_val, ppar_val);
     int par_ind = 0, JT_ind = 0;
     for (int ifit = 1; ifit <= s.sp.n_fits; ++ifit) {
       int t = s.sp.fit_type[ifit - 1];
@@ -1004,6 +1644,16 @@ void determine_JT(const Species& s, int nJT, std::vector<double>& JT, const doub
         J(2) = p[0] * std::exp(-p[1] * sq) * (p[1] / sq) * (d)*vA * vA / (ms * ms);
         par_ind += 2;
         JT_ind += 2;
+      } else if (t == 4) {
+        J(0) = std::exp(-pc * pperp_val);
+      } else if (t == 5) {
+        double d = ppar_val - p[2];
+        double expterm = std::exp(-p[1] * (d * d)) * std::exp(-pc * pperp_val);
+        J(0) = expterm;
+        J(1) = -p[0] * expterm * (d * d);
+        J(2) = 2.0 * p[0] * (d)*p[1] * expterm;
+        par_ind += 2;
+        JT_ind += 2;
       } else if (t == 6) {
         double d = ppar_val - p[2];
         double a = p[3] * pc * (pperp_val * pperp_val) + p[1] * (d * d);
@@ -1026,7 +1676,7 @@ void determine_JT(const Species& s, int nJT, std::vector<double>& JT, const doub
 // LM_nonlinear_fit (src/ALPS_analyt.f90:1395-1636), non-relativistic
 int LM_nonlinear_fit(const oracle_ctx* c, const Species& s, const std::vector<double>& g, int n_params,
                      int nJT, double* params, const std::vector<char>& mask, int iperp, int npar,
-                     double& quality) {
+                     double& quality, const Coords& coords) {
   const alps_system& sy = c->sys;
   bool converged = false;
   int counter = 0;
@@ -1036,12 +1686,14 @@ int LM_nonlinear_fit(const oracle_ctx* c, const Species& s, const std::vector<do
   std::vector<int> piv;
   double LSQ = 0.0, LSQnew;
   auto fitval = [&](int ipar) {
-    return fit_function(s, params, s.P1(iperp, ipar), cplx(s.P2(iperp, ipar), 0.0), sy.vA).real();
+    double a, b;
+    coords(ipar, a, b);
+    return fit_function(s, params, a, cplx(b, 0.0), sy.vA).real();
   };
   while (!converged) {
     counter = counter + 1;
     LSQ = 0.0;
-    determine_JT(s, nJT, JT, params, iperp, npar, sy.vA);
+    determine_JT(s, nJT, JT, params, iperp, npar, sy.vA, coords);
     for (int ipar = 0; ipar <= npar; ++ipar) {
       if (s.sp.log_fit) {
         double fv = fitval(ipar);
@@ -1104,7 +1756,9 @@ int determine_param_fit(const oracle_ctx* c, Species& s) {
   std::vector<double> params(n_params);
   std::vector<char> mask(n_params);
   int nf = s.nf();
-  for (int iperp = 0; iperp <= s.nperp; ++iperp) {
+  bool rel = s.sp.relat != 0;
+  int upper = rel ? s.ng : s.nperp;
+  for (int iperp = 0; iperp <= upper; ++iperp) {
     if (iperp != 0)
       for (int ip = 0; ip < 5; ++ip)
         for (int ifit = 0; ifit < nf; ++ifit) s.PF(iperp, ip, ifit) = s.PF(iperp - 1, ip, ifit);
@@ -1119,11 +1773,48 @@ int determine_param_fit(const oracle_ctx* c, Species& s) {
       par_ind += np - 1;
     }
     nJT += n_params;
-    std::vector<double> g(s.npar + 1);
-    for (int j = 0; j <= s.npar; ++j) g[j] = s.sp.log_fit ? std::log(s.f0[s.idx(iperp, j)]) : s.f0[s.idx(iperp, j)];
-    double quality;
-    int st = LM_nonlinear_fit(c, s, g, n_params, nJT, params.data(), mask, iperp, s.npar, quality);
-    if (st) return st;
+    if (!rel) {
+      std::vector<double> g(s.npar + 1);
+      for (int j = 0; j <= s.npar; ++j) g[j] = s.sp.log_fit ? std::log(s.f0[s.idx(iperp, j)]) : s.f0[s.idx(iperp, j)];
+      double quality;
+      Coords co = [&](int j, double& a, double& b) {
+        a = s.P1(iperp, j);
+        b = s.P2(iperp, j);
+      };
+      int st = LM_nonlinear_fit(c, s, g, n_params, nJT, params.data(), mask, iperp, s.npar, quality, co);
+      if (st) return st;
+    } else {
+      // relevant pparbar range of this Gamma row (src/ALPS_analyt.f90:563-585)
+      bool fl = false, fu = false;
+      int lower = 1, upp = s.np - 1;
+      for (int ip = 1; ip <= s.np - 1; ++ip) {
+        if (!fl && s.FR(iperp, ip - 1) <= -1.0 && s.FR(iperp, ip) > -1.0) { lower = ip; fl = true; }
+        if (!fu && s.FR(iperp, ip) > -1.0 && s.FR(iperp, ip + 1) <= -1.0) { upp = ip; fu = true; }
+      }
+      if ((upp - lower) > 2) {
+        int npr = upp - lower;
+        std::vector<double> g(npr + 1);
+        for (int j = 0; j <= npr; ++j) g[j] = s.sp.log_fit ? std::log(s.FR(iperp, lower + j)) : s.FR(iperp, lower + j);
+        double quality;
+        Coords co = [&](int j, double& a, double& b) {
+          a = s.G(iperp, j + lower);
+          b = s.PB(iperp, j + lower);
+        };
+        int st = LM_nonlinear_fit(c, s, g, n_params, nJT, params.data(), mask, iperp, npr, quality, co);
+        if (st) return st;
+      } else {
+        int pi2 = 0;
+        for (int ifit = 1; ifit <= nf; ++ifit) {
+          params[ifit + pi2 - 1] = s.FR(iperp, (upp + lower) / 2) /
+                                   std::exp(-s.sp.perp_correction[ifit - 1] * s.G(iperp, 1));
+          if (s.sp.fit_type[ifit - 1] == 5) {
+            params[ifit + pi2 + 1 - 1] = 1.0e-12;
+            params[ifit + pi2 + 2 - 1] = 0.0;
+            pi2 += 2;
+          }
+        }
+      }
+    }
     par_ind = 0;
     for (int ifit = 1; ifit <= nf; ++ifit) {
       int t = s.sp.fit_type[ifit - 1];
@@ -1292,15 +1983,16 @@ void oracle_destroy(oracle_ctx* c) { delete c; }
 int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const double* pperp,
                        const double* ppar, const double* f0) {
   if (!c || is < 0 || is >= c->sys.nspec || !sp) return ALPS_E_INVALID;
-  if (sp->use_bM || sp->relat) return ALPS_E_UNSUPPORTED;
+  if (sp->use_bM) return ALPS_E_UNSUPPORTED;
   if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
   if (sp->ac_method == 1) {
     if (sp->n_fits < 1 || sp->n_fits > ALPS_MAX_FITS) return ALPS_E_INVALID;
     for (int f = 0; f < sp->n_fits; ++f) {
       int t = sp->fit_type[f];
-      if (t != 1 && t != 2 && t != 3 && t != 6) return ALPS_E_UNSUPPORTED;
+      if (t < 1 || t > 6) return ALPS_E_UNSUPPORTED;
     }
   }
+  if (sp->relat && (c->sys.ngamma < 4 || c->sys.npparbar < 6)) return ALPS_E_INVALID;
   Species& s = c->spec[is];
   s.sp = *sp;
   s.nperp = c->sys.nperp;
@@ -1311,7 +2003,10 @@ int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const doub
   s.f0.assign(f0, f0 + n);
   int nf = std::max(1, sp->n_fits);
   s.sp.n_fits = (sp->ac_method == 1) ? sp->n_fits : 1;
-  s.param_fit.assign((size_t)(s.nperp + 1) * 5 * nf, 0.0);
+  s.ng = c->sys.ngamma;
+  s.np = c->sys.npparbar;
+  int rows = sp->relat ? std::max(s.nperp, s.ng) : s.nperp;
+  s.param_fit.assign((size_t)(rows + 1) * 5 * nf, 0.0);
   for (int ip = 0; ip < 5; ++ip)
     for (int f = 0; f < s.sp.n_fits; ++f) s.PF(0, ip, f) = sp->fit_init[f][ip];
   s.loaded = true;
@@ -1323,6 +2018,10 @@ int oracle_prepare(oracle_ctx* c) {
   for (auto& s : c->spec) {
     if (!s.loaded) return ALPS_E_INVALID;
     derivative_f0(s);
+    if (s.sp.relat) {
+      int st = derivative_f0_rel(s, c->sys.vA);
+      if (st) return st;
+    }
     int st = determine_param_fit(c, s);
     if (st) return st;
   }
@@ -1709,6 +2408,21 @@ int oracle_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* 
       ifit[4] = 1.0;
       iperpcorr = 1.0 / (tau * beta * ms * kap * a * a * alph);
       break;
+    case 3:
+      norm = vA / (2.0 * pi * std::sqrt(alph) * (ms * ms) * beta * tau);
+      norm = norm / bessk(2, 2.0 * ms / (vA * vA * alph * beta * tau));
+      if (dp->autoscale) {
+        pperp_max = std::sqrt(maxP * maxP * tau + (tau - ms * ms) / (vA * vA)) * std::sqrt(alph);
+        ppar_max = std::sqrt(maxP * maxP * tau + (tau - ms * ms) / (vA * vA));
+      } else {
+        pperp_max = dp->maxPperp;
+        ppar_max = dp->maxPpar;
+      }
+      ifit[0] = norm;
+      ifit[1] = vA * vA * alph / (ms * ms);
+      ifit[2] = pd;
+      iperpcorr = (2.0 * ms / (vA * vA * beta * tau * alph));
+      break;
     case 4:
       norm = 1.0;
       if (dp->autoscale) {
@@ -1738,6 +2452,9 @@ int oracle_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* 
         return std::pow(1.0 + (d * d / (beta * ms * kap * a * a * tau)) +
                             (pp_ * pp_) / (tau * beta * ms * kap * a * a * alph),
                         -1.0 - kap);
+      case 3:
+        return std::exp(-(2.0 * ms / (vA * vA * beta * tau * alph)) *
+                        std::sqrt(1.0 + pp_ * pp_ * vA * vA / (ms * ms) + d * d * vA * vA * alph / (ms * ms)));
       default: {
         double q = (d * d) / (beta * ms * tau) + (pp_ * pp_) / (tau * beta * ms * alph);
         return std::exp(0.5 * (q - std::exp(q)));

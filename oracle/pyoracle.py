@@ -141,7 +141,9 @@ class OraclePlasma:
             pass
 
     def fit_size(self, i):
-        return (self.sys.nperp + 1) * 5 * max(1, self.species[i].n_fits)
+        sp = self.species[i]
+        rows = max(self.sys.nperp, self.sys.ngamma) if sp.relat else self.sys.nperp
+        return (rows + 1) * 5 * (max(1, sp.n_fits) if sp.ac_method == 1 else 1)
 
     def get_fit(self, i):
         out = np.zeros(self.fit_size(i))

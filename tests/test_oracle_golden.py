@@ -63,3 +63,47 @@ def test_kpar_fast_scan_matches_golden(kpar_fast_plasma, golden_dir):
     # every printed digit
     for a, b in zip(rows.ravel(), gold.ravel()):
         assert _fortran_es(a) == _fortran_es(b), (a, b)
+
+
+def test_relativistic_oracle_runs_reference_input(golden_dir):
+    """The relativistic branch (derivative_f0_rel with the thin-plate-spline
+    remap, fits of type 4, integrate_res_rel, landau_integrate_rel,
+    int_ee_rel) on the reference's tests/test_relativistic.in with its
+    Juettner tables, on a coarser (Gamma, pparbar) grid.  The reference ships
+    no golden output for this input: values are checked for finiteness and
+    against the non-relativistic limit in test_relativistic_limit."""
+    from alps_gb300 import api
+    from alps_gb300.distribution import read_distribution_input
+    po.set_threads(os.cpu_count() or 1)
+    ref = os.path.join(golden_dir, "ref", "inputs")
+    inp = api.read_input(os.path.join(ref, "tests", "test_relativistic.in"))
+    dist = read_distribution_input(os.path.join(ref, "distribution", "test_relativistic_dist.in"))
+    s = inp.sys
+    s.ngamma = s.npparbar = 60
+    species = [(inp.species[i],) + po.generate_f0(dist["species"][i], s.nperp, s.npar)[:3] for i in range(s.nspec)]
+    P = po.OraclePlasma(s, species)
+    P.set_k(s.kperp, s.kpar)
+    for g in inp.guess[:2]:
+        D, chi, _, _ = P.disp(complex(g.re, g.im))
+        assert np.isfinite(D) and np.all(np.isfinite(chi))
+
+
+def test_relativistic_limit():
+    """At v_A/c = 0.1 a Maxwellian evaluated through the relativistic branch
+    tracks the non-relativistic branch (chi_yy within 15 %, Im omega > 0)."""
+    from alps_gb300 import _abi, workloads
+    vA, N, M = 0.1, 30, 60
+    d = workloads._dist(kind=1, ms=1.0, vA=vA, maxP=5.0)
+    pp, pl, f0, ideal = po.generate_f0(d, N, M)
+    sysd = _abi.system_defaults(nspec=1, nperp=N, npar=M, kperp=0.3, kpar=0.2, vA=vA, Bessel_zero=1e-20,
+                                positions_principal=3, ngamma=80, npparbar=80)
+    spF = _abi.species_defaults(ns=1, qs=1, ms=1, fits=[(1, list(ideal[:3]) + [0, 0], ideal[5])])
+    pc = 2.0 / (vA * vA)
+    spT = _abi.species_defaults(ns=1, qs=1, ms=1, relat=1, fits=[(5, [ideal[0] * np.exp(pc), 1e-12, 0, 0, 0], pc)])
+    PF = po.OraclePlasma(sysd, [(spF, pp, pl, f0)])
+    PT = po.OraclePlasma(sysd, [(spT, pp, pl, f0)])
+    PF.set_k(0.3, 0.2)
+    PT.set_k(0.3, 0.2)
+    for om in [0.5 + 0.1j, 1.2 + 0.05j]:
+        a, b = PF.disp(om)[1][0], PT.disp(om)[1][0]
+        assert abs(b[1, 1] - a[1, 1]) < 0.15 * abs(a[1, 1])
