@@ -119,8 +119,10 @@ class Plasma:
         check(lib().alps_prepare(self._h), "alps_prepare")
 
     def fit_size(self, i):
-        nf = self.species[i].n_fits if self.species[i].ac_method == 1 else 1
-        return (self.sys.nperp + 1) * 5 * nf
+        sp = self.species[i]
+        nf = sp.n_fits if sp.ac_method == 1 else 1
+        rows = max(self.sys.nperp, self.sys.ngamma) if sp.relat else self.sys.nperp
+        return (rows + 1) * 5 * nf
 
     def get_fit(self, i):
         out = np.zeros(self.fit_size(i))
@@ -130,6 +132,17 @@ class Plasma:
     def set_fit(self, i, arr):
         arr = np.ascontiguousarray(arr, dtype=np.float64)
         check(lib().alps_set_fit(self._h, i, _dptr(arr)), "alps_set_fit")
+
+    def get_f0_rel(self, i):
+        """(gamma, pparbar, f0_rel, df/dGamma, df/dpparbar) of a relativistic
+        species: the tables derivative_f0_rel writes."""
+        ng, npb = self.sys.ngamma, self.sys.npparbar
+        g, p = np.zeros(ng + 1), np.zeros(npb + 1)
+        f, a, b = (np.zeros((ng + 1) * (npb + 1)) for _ in range(3))
+        check(lib().alps_get_f0_rel(self._h, i, _dptr(g), _dptr(p), _dptr(f), _dptr(a), _dptr(b)),
+              "alps_get_f0_rel")
+        shape = (ng + 1, npb + 1)
+        return g, p, f.reshape(shape), a.reshape(shape), b.reshape(shape)
 
     def set_k(self, kperp, kpar):
         check(lib().alps_set_k(self._h, float(kperp), float(kpar)), "alps_set_k")

@@ -132,6 +132,13 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_mom);
     cudaFree(S.d_fit_aux);
     cudaFree(S.d_lmom);
+    cudaFree(S.d_grel);
+    cudaFree(S.d_prel);
+    cudaFree(S.d_f0rel);
+    cudaFree(S.d_dfr1);
+    cudaFree(S.d_dfr2);
+    cudaFree(S.d_jrel);
+    cudaFree(S.d_cone);
   }
   cudaFree(c->d_om);
   cudaFree(c->d_D);
@@ -141,6 +148,7 @@ void alps_destroy(alps_ctx* c) {
   cudaFree(c->d_slot_nn);
   cudaFree(c->d_items);
   cudaFree(c->d_ext);
+  cudaFree(c->d_rel);
   cudaFree(c->d_flags);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   for (auto& ev : c->ev_pending)
@@ -150,17 +158,30 @@ void alps_destroy(alps_ctx* c) {
   delete c;
 }
 
+// rows of the fit parameter table: the pperp rows, or for a relativistic
+// species the Gamma rows when there are more of them
+static int fit_rows(const alps_ctx* c, int is) {
+  int r = c->sys.nperp;
+  if (c->spec[is].sp.relat) r = std::max(r, c->sys.ngamma);
+  return r + 1;
+}
+
 int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* pperp, const double* ppar,
                      const double* f0) {
   if (!c || !sp || !pperp || !ppar || !f0 || is < 0 || is >= c->sys.nspec) return ALPS_E_INVALID;
-  if (sp->use_bM || sp->relat) return ALPS_E_UNSUPPORTED;
+  if (sp->use_bM) return ALPS_E_UNSUPPORTED;
   if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
   if (sp->ac_method != 0 && sp->ac_method != 1) return ALPS_E_INVALID;
+  // relativistic species: continuation on the (Gamma, pparbar) rows, fit
+  // types 4 and 5 (the types whose pperp argument is Gamma)
+  if (sp->relat && sp->ac_method != 1) return ALPS_E_UNSUPPORTED;
+  if (sp->relat && (c->sys.ngamma < 4 || c->sys.npparbar < 6)) return ALPS_E_INVALID;
   if (sp->ac_method == 1) {
     if (sp->n_fits < 1 || sp->n_fits > ALPS_MAX_FITS) return ALPS_E_INVALID;
     for (int f = 0; f < sp->n_fits; ++f) {
       int t = sp->fit_type[f];
-      if (t != 1 && t != 2 && t != 3 && t != 6) return ALPS_E_UNSUPPORTED;
+      bool ok = sp->relat ? (t == 4 || t == 5) : (t == 1 || t == 2 || t == 3 || t == 6);
+      if (!ok) return ALPS_E_UNSUPPORTED;
     }
   }
   if (sp->qs == 0.0 || sp->ms <= 0.0) return ALPS_E_INVALID;
@@ -181,6 +202,7 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   SpeciesHost& S = c->spec[is];
   S.sp = *sp;
   if (sp->ac_method != 1) S.sp.n_fits = 1;
+  S.sp.relat = sp->relat ? 1 : 0;
   S.pperp = pv;
   S.ppar = qv;
   S.f0.assign(f0, f0 + (size_t)(N + 1) * L);
@@ -189,9 +211,10 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   if (!S.d_ppar) ALPS_CUDA_TRY(cudaMalloc(&S.d_ppar, (M + 1) * sizeof(double)));
   if (!S.d_f0) ALPS_CUDA_TRY(cudaMalloc(&S.d_f0, nn * sizeof(double)));
   int nf = S.sp.n_fits;
+  int rows = fit_rows(c, is);
   if (S.d_fit) cudaFree(S.d_fit);
-  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)(N + 1) * 5 * nf * sizeof(double)));
-  std::vector<double> fit((size_t)(N + 1) * 5 * nf, 0.0);
+  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)rows * 5 * nf * sizeof(double)));
+  std::vector<double> fit((size_t)rows * 5 * nf, 0.0);
   for (int ip = 0; ip < 5; ++ip)
     for (int f = 0; f < nf; ++f) fit[(0 * 5 + ip) * nf + f] = sp->fit_init[f][ip];
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_pperp, pv.data(), (N + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -221,7 +244,7 @@ int alps_prepare(alps_ctx* c) {
 int alps_get_fit(alps_ctx* c, int is, double* out) {
   if (!c || !out || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
   const SpeciesHost& S = c->spec[is];
-  size_t n = (size_t)(c->sys.nperp + 1) * 5 * S.sp.n_fits;
+  size_t n = (size_t)fit_rows(c, is) * 5 * S.sp.n_fits;
   ALPS_CUDA_TRY(cudaMemcpyAsync(out, S.d_fit, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ALPS_OK;
@@ -230,11 +253,27 @@ int alps_get_fit(alps_ctx* c, int is, double* out) {
 int alps_set_fit(alps_ctx* c, int is, const double* in) {
   if (!c || !in || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
   SpeciesHost& S = c->spec[is];
-  size_t n = (size_t)(c->sys.nperp + 1) * 5 * S.sp.n_fits;
+  size_t n = (size_t)fit_rows(c, is) * 5 * S.sp.n_fits;
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int st = launch_fit_aux(c, is);
   if (st) return st;
   if (c->kset && (st = launch_landau_moments(c, is))) return st;
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  return ALPS_OK;
+}
+
+int alps_get_f0_rel(alps_ctx* c, int is, double* gamma, double* pparbar, double* f0_rel, double* df_dgamma,
+                    double* df_dpparbar) {
+  if (!c || is < 0 || is >= c->sys.nspec || !c->prepared || !c->spec[is].sp.relat) return ALPS_E_INVALID;
+  const SpeciesHost& S = c->spec[is];
+  size_t ng = c->sys.ngamma, np = c->sys.npparbar, nf = (ng + 1) * (np + 1);
+  if (gamma) memcpy(gamma, S.grel.data(), (ng + 1) * sizeof(double));
+  if (pparbar) memcpy(pparbar, S.prel.data(), (np + 1) * sizeof(double));
+  if (f0_rel) ALPS_CUDA_TRY(cudaMemcpyAsync(f0_rel, S.d_f0rel, nf * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (df_dgamma)
+    ALPS_CUDA_TRY(cudaMemcpyAsync(df_dgamma, S.d_dfr1, nf * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  if (df_dpparbar)
+    ALPS_CUDA_TRY(cudaMemcpyAsync(df_dpparbar, S.d_dfr2, nf * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ALPS_OK;
 }
@@ -264,6 +303,7 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     S.nmax = nm[is];
     int st = launch_build_bessel_and_reduced(c, is, kperp);
     if (st) return st;
+    if (S.sp.relat && (st = launch_rel_bessel(c, is, kperp))) return st;
     if ((st = launch_fit_aux(c, is))) return st;
     if ((st = launch_landau_moments(c, is))) return st;
     // resonant orders per omega: p_res moves by |q/k_par| per order, so at
@@ -328,6 +368,7 @@ static int ensure_batch(alps_ctx* c, int n, bool ext) {
 static int check_flags(alps_ctx* c) {
   int f = 0;
   ALPS_CUDA_TRY(cudaMemcpy(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (f & 2) return ALPS_E_SUBLUMINAL;  // resonance window wider than the subluminal cone
   return f ? ALPS_E_INVALID : ALPS_OK;
 }
 

@@ -85,6 +85,16 @@ struct SpecDev {
   // bounds of the row deviation delta_i(p) = la p^2 + lb p + lc, smallest a0
   const double* lmom;
   double p2r, p3r, la, lb, lc, min_a0;
+  // relativistic species (src/ALPS_fns_rel.f90): (Gamma, pparbar) grid
+  int relat, ng, np;
+  const double* grel;   // [ng+1]
+  const double* prel;   // [np+1]
+  const double* f0rel;  // [(ng+1)*(np+1)], -1 outside the subluminal cone
+  const double* dfr1;   // d f0_rel / d Gamma
+  const double* dfr2;   // d f0_rel / d pparbar
+  const double* jrel;   // [(n)*(ng+1)*(np+1)], n = 0..nmax+1: J_n at each node
+  const int2* cone;     // [ng+1] first and last pparbar index inside the cone
+  double int_ee_rel;
 };
 
 struct SysDev {
@@ -120,6 +130,13 @@ struct SpeciesHost {
   size_t lmom_cap = 0;
   double p2r = 0, p3r = 0, la = 0, lb = 0, lc = 0, min_a0 = 0;
   bool lfact = false;
+  // relativistic species
+  std::vector<double> grel, prel;         // host copies of the grid vectors
+  double *d_grel = nullptr, *d_prel = nullptr, *d_f0rel = nullptr, *d_dfr1 = nullptr, *d_dfr2 = nullptr;
+  double* d_jrel = nullptr;
+  int2* d_cone = nullptr;
+  size_t jrel_cap = 0;
+  double int_ee_rel = 0.0;
   size_t mom_cap = 0;
   int nmax = 0;
   double int_ee = 0.0;
@@ -148,6 +165,8 @@ struct alps_ctx {
   double2* d_items = nullptr;   // [n][S][rcap][6]
   size_t items_cap = 0;
   double2* d_ext = nullptr;     // [n][S*9 + S*27 + 9] extended outputs
+  double2* d_rel = nullptr;     // [n][S][2*nmax+1][6] relativistic orders
+  size_t rel_cap = 0;
   size_t ext_cap = 0;
   int* d_flags = nullptr;       // error flags
   alps_stats stats = {};
@@ -170,6 +189,11 @@ int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
 int launch_fit_aux(alps_ctx* c, int is);
 int launch_landau_moments(alps_ctx* c, int is);
+int launch_rel_prepare(alps_ctx* c, int is);
+int launch_rel_bessel(alps_ctx* c, int is, double kperp);
+// per-order relativistic results out[((w*nspec + s)*relcap + n)*2 + sign][6]
+int launch_rel_orders(const SysDev& sys, const SpecDev* sp, int relcap, int n, const double2* d_om, double2* d_out,
+                      int* d_flags, cudaStream_t st);
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
                       cudaStream_t st);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);

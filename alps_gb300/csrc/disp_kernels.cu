@@ -31,6 +31,7 @@ struct DispArgs {
   int nchunk;    // order chunks per species
   int csize;     // orders per chunk
   int rcap;      // max resonant slots over species
+  int relcap;    // order slots per relativistic species (max nmax + 1), 0 if none
 };
 
 namespace {
@@ -42,6 +43,10 @@ __global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om,
   int s = blockIdx.y;
   if (t >= n_om) return;
   const SpecDev& S = a.sp[s];
+  if (S.relat) {  // relativistic orders run in k_rel_orders
+    count[(size_t)t * a.sys.nspec + s] = 0;
+    return;
+  }
   double2 o = om[t];
   int cnt = 0;
   int* slots = slot_nn + ((size_t)t * a.sys.nspec + s) * a.rcap;
@@ -71,7 +76,7 @@ __global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __
   const SpecDev& S = a.sp[s];
   const int chunk = blockIdx.z;
   const int n_begin = chunk * a.csize;
-  const int n_end = min(S.nmax + 1, n_begin + a.csize);
+  const int n_end = S.relat ? n_begin : min(S.nmax + 1, n_begin + a.csize);
   const int TW = blockDim.x / js_count;
   const int wl = threadIdx.x % TW, js = threadIdx.x / TW;
   const int w = blockIdx.x * TW + wl;
@@ -596,8 +601,8 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
 // ---------------------------------------------------------------------------
 __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om, const double2* __restrict__ part,
                            const double2* __restrict__ low, const int* __restrict__ count,
-                           const int* __restrict__ slot_nn, const double2* __restrict__ items, double2* D,
-                           double2* ext) {
+                           const int* __restrict__ slot_nn, const double2* __restrict__ items,
+                           const double2* __restrict__ rel, double2* D, double2* ext) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= n_om) return;
   const int S_ = a.sys.nspec;
@@ -631,9 +636,37 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
         if (nn >= -1 && nn <= 1) cl[nn + 1][e] = cadd(cl[nn + 1][e], v);
       }
     }
-    double ee = a.sys.kperp_norm ? S.int_ee : kperp * kperp * S.int_ee;
-    chi[2] = cadd(chi[2], cmk(ee, 0.0));
-    cl[1][2] = cadd(cl[1][2], cmk(ee, 0.0));
+    if (S.relat) {
+      // orders in the reference's order; n = 0 adds yy, zz, yz only, and the
+      // ee term goes into chi alone (src/ALPS_fns.f90:461-497)
+      for (int n = 0; n <= S.nmax; ++n) {
+        const double2* pl = rel + ((((size_t)w * S_ + s) * a.relcap + n) * 2 + 0) * 6;
+        const double2* mi = pl + 6;
+        if (n == 0) {
+          const int e0[3] = {1, 2, 5};
+          for (int q = 0; q < 3; ++q) {
+            chi[e0[q]] = cadd(chi[e0[q]], pl[e0[q]]);
+            cl[1][e0[q]] = pl[e0[q]];
+          }
+        } else {
+          for (int e = 0; e < 6; ++e) {
+            if (n == 1) {
+              cl[2][e] = pl[e];
+              cl[0][e] = mi[e];
+              chi[e] = cadd(chi[e], cadd(pl[e], mi[e]));
+            } else {
+              chi[e] = cadd(cadd(chi[e], pl[e]), mi[e]);
+            }
+          }
+        }
+      }
+      double ee = a.sys.kperp_norm ? S.int_ee_rel : kperp * kperp * S.int_ee_rel;
+      chi[2] = cadd(chi[2], cmk(ee, 0.0));
+    } else {
+      double ee = a.sys.kperp_norm ? S.int_ee : kperp * kperp * S.int_ee;
+      chi[2] = cadd(chi[2], cmk(ee, 0.0));
+      cl[1][2] = cadd(cl[1][2], cmk(ee, 0.0));
+    }
     double norm = S.ns * S.qs;
     for (int e = 0; e < 6; ++e) {
       chi[e] = cscale(chi[e], norm);
@@ -766,6 +799,25 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->lb = S.lb;
   o->lc = S.lc;
   o->min_a0 = S.min_a0;
+  o->relat = S.sp.relat ? 1 : 0;
+  o->ng = c->sys.ngamma;
+  o->np = c->sys.npparbar;
+  o->grel = S.d_grel;
+  o->prel = S.d_prel;
+  o->f0rel = S.d_f0rel;
+  o->dfr1 = S.d_dfr1;
+  o->dfr2 = S.d_dfr2;
+  o->jrel = S.d_jrel;
+  o->cone = S.d_cone;
+  o->int_ee_rel = S.int_ee_rel;
+}
+
+// order slots of the relativistic per-order results (0 when no species is)
+int rel_capacity(const alps_ctx* c) {
+  int cap = 0;
+  for (int s = 0; s < c->sys.nspec; ++s)
+    if (c->spec[s].sp.relat) cap = std::max(cap, c->spec[s].nmax + 1);
+  return cap;
 }
 
 int collect_profile(alps_ctx* c) {
@@ -796,6 +848,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     rc = std::max(rc, c->spec[s].rcap);
   }
   a.rcap = rc;
+  a.relcap = rel_capacity(c);
   // order chunks: enough blocks to fill the device for small batches
   int js = 1;
   if (n < 32) js = 32;
@@ -820,6 +873,8 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   bool want_low = d_ext != nullptr;
   if (want_low)
     if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * a.nchunk * 18))) return rcode;
+  if (a.relcap)
+    if ((rcode = ensure_buf(c->d_rel, c->rel_cap, (size_t)n * S_ * a.relcap * 2 * 6))) return rcode;
   if (!c->d_flags) ALPS_CUDA_TRY(cudaMalloc(&c->d_flags, sizeof(int)));
   ALPS_CUDA_TRY(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
 
@@ -855,16 +910,18 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_items,
                                                              c->d_flags);
   ALPS_CUDA_TRY(cudaGetLastError());
+  if (a.relcap && (rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, d_om, c->d_rel, c->d_flags, st)))
+    return rcode;
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[3], st));
   k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, d_om, n, c->d_part, want_low ? c->d_low : nullptr, c->d_count,
-                                              c->d_slot_nn, c->d_items, d_D, d_ext);
+                                              c->d_slot_nn, c->d_items, c->d_rel, d_D, d_ext);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) {
     ALPS_CUDA_TRY(cudaEventRecord(ev[4], st));
     c->ev_pending.push_back(ev);
   }
   c->stats.n_eval = n;
-  c->stats.kernels_launched = 4;
+  c->stats.kernels_launched = a.relcap ? 5 : 4;
   return ALPS_OK;
 }
 
@@ -876,7 +933,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
 // and must see every byte, a real-time loop that cannot afford the implicit
 // device-wide synchronisation of cudaMalloc/cudaFree, or a plugin host that
 // forbids plugins from creating allocations behind its back.  For them,
-// alps_disp_batch_noalloc runs the same four kernels as
+// alps_disp_batch_noalloc runs the same kernels as
 // alps_disp_batch_device with all of their scratch (partial sums,
 // resonant-order slots, resonant results, error flag) carved from the
 // file-scope device array below instead of context buffers.
@@ -940,6 +997,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
     rc = std::max(rc, c->spec[s].rcap);
   }
   a.rcap = rc;
+  a.relcap = rel_capacity(c);
   int js = 1;
   if (n < 32) js = 32;
   else if (n < 64) js = 4;
@@ -949,7 +1007,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   int nchunk = std::max(1, std::min(maxn + 1, (152 * 4 + tiles * S_ - 1) / (tiles * S_)));
   a.csize = (maxn + 1 + nchunk - 1) / nchunk;
   a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
-  // scratch layout: flags | count | slot_nn | part | items
+  // scratch layout: flags | count | slot_nn | part | items | relativistic orders
   size_t off = 0;
   size_t o_flags = carve(off, sizeof(int));
   size_t o_count = carve(off, (size_t)n * S_ * sizeof(int));
@@ -957,6 +1015,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   size_t o_slots = carve(off, nslots * sizeof(int));
   size_t o_part = carve(off, (size_t)n * S_ * a.nchunk * 6 * sizeof(double2));
   size_t o_items = carve(off, nslots * 6 * sizeof(double2));
+  size_t o_rel = carve(off, (size_t)n * S_ * a.relcap * 2 * 6 * sizeof(double2));
   if (scratch_bytes) *scratch_bytes = off;
   if (off > ALPS_NOALLOC_SCRATCH_BYTES) return ALPS_E_INVALID;  // batch too large for the static scratch
   unsigned char* b = static_cast<unsigned char*>(base);
@@ -965,6 +1024,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   int* slots = reinterpret_cast<int*>(b + o_slots);
   double2* part = reinterpret_cast<double2*>(b + o_part);
   double2* items = reinterpret_cast<double2*>(b + o_items);
+  double2* relb = reinterpret_cast<double2*>(b + o_rel);
   const double2* om = reinterpret_cast<const double2*>(d_om);
   double2* D = reinterpret_cast<double2*>(d_D);
   ALPS_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), st));
@@ -978,7 +1038,11 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   long blocks = ((long)nslots + RES_WARPS - 1) / RES_WARPS;
   k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, om, n, count, slots, items, flags);
   ALPS_CUDA_TRY(cudaGetLastError());
-  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, D, nullptr);
+  if (a.relcap) {
+    int rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, om, relb, flags, st);
+    if (rcode) return rcode;
+  }
+  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, relb, D, nullptr);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -72,6 +72,11 @@ struct FitArgs {
   double ms, vA;
   int maxsteps;
   double lambda0, lambdafac, eps;
+  // relativistic species: rows of the (Gamma, pparbar) grid
+  int rel, ng, np;
+  const double* f0rel;  // [(ng+1)*(np+1)]
+  const double* grel;   // [ng+1]
+  const double* prel;   // [np+1]
 };
 
 __device__ int fit_nparams(const FitArgs& a, int t) {
@@ -97,6 +102,11 @@ __device__ double fit_value_real(const FitArgs& a, const double* params, double 
     } else if (t == 3) {
       double sq = sqrt(1.0 + ((pperp * pperp) + d * d) * a.vA * a.vA / (a.ms * a.ms));
       ff = ff + p[0] * exp(-p[1] * sq);
+      par_ind += 2;
+    } else if (t == 4) {
+      ff = ff + p[0] * exp(-pc * pperp);
+    } else if (t == 5) {
+      ff = ff + p[0] * exp(-pc * pperp) * exp(-p[1] * (d * d));
       par_ind += 2;
     } else if (t == 6) {
       double q = p[3] * pc * (pperp * pperp) + p[1] * (d * d);
@@ -145,6 +155,15 @@ __device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, 
       Jp[2] = p[0] * exp(-p[1] * sq) * (p[1] / sq) * d * a.vA * a.vA / (a.ms * a.ms);
       par_ind += 2;
       JT_ind += 2;
+    } else if (t == 4) {
+      Jp[0] = exp(-pc * pperp);
+    } else if (t == 5) {
+      double e = exp(-p[1] * (d * d)) * exp(-pc * pperp);
+      Jp[0] = e;
+      Jp[1] = -p[0] * e * (d * d);
+      Jp[2] = 2.0 * p[0] * d * p[1] * e;
+      par_ind += 2;
+      JT_ind += 2;
     } else if (t == 6) {
       double q = p[3] * pc * (pperp * pperp) + p[1] * (d * d);
       double e = exp(0.5 * (q - exp(q)));
@@ -165,18 +184,22 @@ __device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, 
 #define FIT_MAXP (5 * ALPS_MAX_FITS)
 
 // One thread per species: fit[(i*5+ip)*nf + ifit] holds the seeds at row 0
-// on entry and the fitted rows on exit.  scratch: (M+1)*(FIT_MAXP+1).
+// on entry and the fitted rows on exit.  scratch: (M+1)*(FIT_MAXP+1), with M
+// the largest row length.  Rows are the iperp rows of the f0 table, or for a
+// relativistic species the Gamma rows of f0_rel restricted to the subluminal
+// cone (src/ALPS_analyt.f90:546-607).
 __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double* __restrict__ pperp,
                          const double* __restrict__ ppar, double* fit, double* scratch, int* status) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int nf = a.nf, N = a.N, M = a.M;
+  int nf = a.nf, N = a.rel ? a.ng : a.N;
   int n_params = 0;
   for (int f = 0; f < nf; ++f) n_params += fit_nparams(a, a.fit_type[f]);
   double params[FIT_MAXP];
   bool mask[FIT_MAXP];
-  double* JT = scratch;                         // [(M+1)][nJT]
-  double* resid = scratch + (size_t)(M + 1) * FIT_MAXP;
-  if ((1 + M) < n_params) {
+  double* JT = scratch;                         // [(npts)][FIT_MAXP]
+  int maxpts = a.rel ? a.np : a.M;
+  double* resid = scratch + (size_t)(maxpts + 1) * FIT_MAXP;
+  if (!a.rel && (1 + a.M) < n_params) {
     *status = ALPS_E_FIT_POINTS;
     return;
   }
@@ -195,106 +218,141 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
       par_ind += np - 1;
     }
     nJT += n_params;
-    double pp_perp = pperp[iperp];
-    double lambda_fit = a.lambda0, LSQ = 0.0, LSQnew;
-    int counter = 0;
-    bool converged = false;
-    while (!converged) {
-      counter++;
-      LSQ = 0.0;
-      for (int j = 0; j <= M; ++j) {
-        double* Jc = JT + (size_t)j * FIT_MAXP;
-        fit_jacobian(a, params, iperp, pp_perp, ppar[j], Jc);
-        double g = a.log_fit ? log(f0[iperp * (M + 1) + j]) : f0[iperp * (M + 1) + j];
-        double fv = fit_value_real(a, params, pp_perp, ppar[j]);
-        if (a.log_fit) {
-          for (int k = 0; k < nJT; ++k) Jc[k] = Jc[k] / fv;
-          resid[j] = g - log(fv);
-        } else {
-          resid[j] = g - fv;
-        }
-        LSQ = LSQ + resid[j] * resid[j];
+    // points of this row: coordinates and fitted values
+    int npts, off = 0;
+    double xperp;
+    if (a.rel) {
+      const double* fr = a.f0rel + (size_t)iperp * (a.np + 1);
+      bool fl = false, fu = false;
+      int lower = 1, upper = a.np - 1;
+      for (int ip = 1; ip <= a.np - 1; ++ip) {
+        if (!fl && fr[ip - 1] <= -1.0 && fr[ip] > -1.0) { lower = ip; fl = true; }
+        if (!fu && fr[ip] > -1.0 && fr[ip + 1] <= -1.0) { upper = ip; fu = true; }
       }
-      double Am[FIT_MAXP * FIT_MAXP], jr[FIT_MAXP];
-      for (int k = 0; k < nJT; ++k) {
-        for (int l = 0; l < nJT; ++l) {
-          double acc = 0.0;
-          for (int j = 0; j <= M; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * JT[(size_t)j * FIT_MAXP + l];
-          Am[k + nJT * l] = acc;
-        }
-        double acc = 0.0;
-        for (int j = 0; j <= M; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * resid[j];
-        jr[k] = acc;
-      }
-      for (int k = 0; k < nJT; ++k) Am[k + nJT * k] = Am[k + nJT * k] + lambda_fit * Am[k + nJT * k];
-      // LU with partial pivoting (dgetrf), then inverse (dgetri) times JT*r
-      int piv[FIT_MAXP];
-      bool singular = false;
-      for (int k = 0; k < nJT && !singular; ++k) {
-        int p = k;
-        double mx = fabs(Am[k + nJT * k]);
-        for (int i = k + 1; i < nJT; ++i)
-          if (fabs(Am[i + nJT * k]) > mx) { mx = fabs(Am[i + nJT * k]); p = i; }
-        piv[k] = p;
-        if (Am[p + nJT * k] == 0.0) { singular = true; break; }
-        if (p != k)
-          for (int jj = 0; jj < nJT; ++jj) {
-            double tmp = Am[k + nJT * jj];
-            Am[k + nJT * jj] = Am[p + nJT * jj];
-            Am[p + nJT * jj] = tmp;
+      xperp = a.grel[iperp];
+      if ((upper - lower) <= 2) {
+        int pi2 = 0;
+        for (int ifit = 1; ifit <= nf; ++ifit) {
+          params[ifit + pi2 - 1] = fr[(upper + lower) / 2] / exp(-a.pc[ifit - 1] * a.grel[iperp]);
+          if (a.fit_type[ifit - 1] == 5) {
+            params[ifit + pi2] = 1.0e-12;
+            params[ifit + pi2 + 1] = 0.0;
+            pi2 += 2;
           }
-        for (int i = k + 1; i < nJT; ++i) {
-          Am[i + nJT * k] /= Am[k + nJT * k];
-          for (int jj = k + 1; jj < nJT; ++jj) Am[i + nJT * jj] -= Am[i + nJT * k] * Am[k + nJT * jj];
         }
-      }
-      if (singular) {
-        *status = ALPS_E_SINGULAR;
-        return;
-      }
-      double inv[FIT_MAXP * FIT_MAXP];
-      for (int cc = 0; cc < nJT; ++cc) {
-        double x[FIT_MAXP];
-        for (int i = 0; i < nJT; ++i) x[i] = (i == cc) ? 1.0 : 0.0;
-        for (int k = 0; k < nJT; ++k) {
-          double tmp = x[k];
-          x[k] = x[piv[k]];
-          x[piv[k]] = tmp;
-        }
-        for (int i = 0; i < nJT; ++i)
-          for (int k = 0; k < i; ++k) x[i] -= Am[i + nJT * k] * x[k];
-        for (int i = nJT - 1; i >= 0; --i) {
-          for (int k = i + 1; k < nJT; ++k) x[i] -= Am[i + nJT * k] * x[k];
-          x[i] /= Am[i + nJT * i];
-        }
-        for (int i = 0; i < nJT; ++i) inv[i + nJT * cc] = x[i];
-      }
-      double delta[FIT_MAXP];
-      for (int k = 0; k < nJT; ++k) {
-        double acc = 0.0;
-        for (int l = 0; l < nJT; ++l) acc += inv[k + nJT * l] * jr[l];
-        delta[k] = acc;
-      }
-      int l = 0;
-      for (int k = 0; k < n_params; ++k)
-        if (mask[k]) params[k] = params[k] + delta[l++];
-      LSQnew = 0.0;
-      for (int j = 0; j <= M; ++j) {
-        double g = a.log_fit ? log(f0[iperp * (M + 1) + j]) : f0[iperp * (M + 1) + j];
-        double fv = fit_value_real(a, params, pp_perp, ppar[j]);
-        double r = a.log_fit ? g - log(fv) : g - fv;
-        LSQnew = LSQnew + r * r;
-      }
-      if (LSQnew > LSQ) {
-        l = 0;
-        for (int k = 0; k < n_params; ++k)
-          if (mask[k]) params[k] = params[k] - delta[l++];
-        lambda_fit = lambda_fit * a.lambdafac;
+        npts = -1;
       } else {
-        lambda_fit = lambda_fit / a.lambdafac;
+        npts = upper - lower;
+        off = lower;
       }
-      if (fabs(LSQnew - LSQ) < a.eps) converged = true;
-      if (counter == a.maxsteps) converged = true;
+    } else {
+      npts = a.M;
+      xperp = pperp[iperp];
+    }
+    auto xpar = [&](int j) { return a.rel ? a.prel[off + j] : ppar[j]; };
+    auto gval = [&](int j) {
+      double v = a.rel ? a.f0rel[(size_t)iperp * (a.np + 1) + off + j] : f0[iperp * (a.M + 1) + j];
+      return a.log_fit ? log(v) : v;
+    };
+    if (npts >= 0) {
+      double lambda_fit = a.lambda0, LSQ = 0.0, LSQnew;
+      int counter = 0;
+      bool converged = false;
+      while (!converged) {
+        counter++;
+        LSQ = 0.0;
+        for (int j = 0; j <= npts; ++j) {
+          double* Jc = JT + (size_t)j * FIT_MAXP;
+          fit_jacobian(a, params, iperp, xperp, xpar(j), Jc);
+          double fv = fit_value_real(a, params, xperp, xpar(j));
+          if (a.log_fit) {
+            for (int k = 0; k < nJT; ++k) Jc[k] = Jc[k] / fv;
+            resid[j] = gval(j) - log(fv);
+          } else {
+            resid[j] = gval(j) - fv;
+          }
+          LSQ = LSQ + resid[j] * resid[j];
+        }
+        double Am[FIT_MAXP * FIT_MAXP], jr[FIT_MAXP];
+        for (int k = 0; k < nJT; ++k) {
+          for (int l = 0; l < nJT; ++l) {
+            double acc = 0.0;
+            for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * JT[(size_t)j * FIT_MAXP + l];
+            Am[k + nJT * l] = acc;
+          }
+          double acc = 0.0;
+          for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * resid[j];
+          jr[k] = acc;
+        }
+        for (int k = 0; k < nJT; ++k) Am[k + nJT * k] = Am[k + nJT * k] + lambda_fit * Am[k + nJT * k];
+        // LU with partial pivoting (dgetrf), then inverse (dgetri) times JT*r
+        int piv[FIT_MAXP];
+        bool singular = false;
+        for (int k = 0; k < nJT && !singular; ++k) {
+          int p = k;
+          double mx = fabs(Am[k + nJT * k]);
+          for (int i = k + 1; i < nJT; ++i)
+            if (fabs(Am[i + nJT * k]) > mx) { mx = fabs(Am[i + nJT * k]); p = i; }
+          piv[k] = p;
+          if (Am[p + nJT * k] == 0.0) { singular = true; break; }
+          if (p != k)
+            for (int jj = 0; jj < nJT; ++jj) {
+              double tmp = Am[k + nJT * jj];
+              Am[k + nJT * jj] = Am[p + nJT * jj];
+              Am[p + nJT * jj] = tmp;
+            }
+          for (int i = k + 1; i < nJT; ++i) {
+            Am[i + nJT * k] /= Am[k + nJT * k];
+            for (int jj = k + 1; jj < nJT; ++jj) Am[i + nJT * jj] -= Am[i + nJT * k] * Am[k + nJT * jj];
+          }
+        }
+        if (singular) {
+          *status = ALPS_E_SINGULAR;
+          return;
+        }
+        double inv[FIT_MAXP * FIT_MAXP];
+        for (int cc = 0; cc < nJT; ++cc) {
+          double x[FIT_MAXP];
+          for (int i = 0; i < nJT; ++i) x[i] = (i == cc) ? 1.0 : 0.0;
+          for (int k = 0; k < nJT; ++k) {
+            double tmp = x[k];
+            x[k] = x[piv[k]];
+            x[piv[k]] = tmp;
+          }
+          for (int i = 0; i < nJT; ++i)
+            for (int k = 0; k < i; ++k) x[i] -= Am[i + nJT * k] * x[k];
+          for (int i = nJT - 1; i >= 0; --i) {
+            for (int k = i + 1; k < nJT; ++k) x[i] -= Am[i + nJT * k] * x[k];
+            x[i] /= Am[i + nJT * i];
+          }
+          for (int i = 0; i < nJT; ++i) inv[i + nJT * cc] = x[i];
+        }
+        double delta[FIT_MAXP];
+        for (int k = 0; k < nJT; ++k) {
+          double acc = 0.0;
+          for (int l = 0; l < nJT; ++l) acc += inv[k + nJT * l] * jr[l];
+          delta[k] = acc;
+        }
+        int l = 0;
+        for (int k = 0; k < n_params; ++k)
+          if (mask[k]) params[k] = params[k] + delta[l++];
+        LSQnew = 0.0;
+        for (int j = 0; j <= npts; ++j) {
+          double fv = fit_value_real(a, params, xperp, xpar(j));
+          double r = a.log_fit ? gval(j) - log(fv) : gval(j) - fv;
+          LSQnew = LSQnew + r * r;
+        }
+        if (LSQnew > LSQ) {
+          l = 0;
+          for (int k = 0; k < n_params; ++k)
+            if (mask[k]) params[k] = params[k] - delta[l++];
+          lambda_fit = lambda_fit * a.lambdafac;
+        } else {
+          lambda_fit = lambda_fit / a.lambdafac;
+        }
+        if (fabs(LSQnew - LSQ) < a.eps) converged = true;
+        if (counter == a.maxsteps) converged = true;
+      }
     }
     par_ind = 0;
     for (int ifit = 1; ifit <= nf; ++ifit) {
@@ -562,9 +620,11 @@ int launch_prepare_species(alps_ctx* c, int is) {
   ALPS_CUDA_TRY(cudaMalloc(&d_ee, sizeof(double)));
   k_int_ee<<<1, 256, 0, st>>>(S.d_g2, S.d_ppar, N, M, scale, d_ee);
   ALPS_CUDA_TRY(cudaGetLastError());
-  // LM fit of the analytic continuation (ACmethod 1)
+  // relativistic species: (Gamma, pparbar) grid, f0_rel and its derivatives
   int st_fit = ALPS_OK;
-  if (S.sp.ac_method == 1) {
+  if (S.sp.relat) st_fit = launch_rel_prepare(c, is);
+  // LM fit of the analytic continuation (ACmethod 1)
+  if (S.sp.ac_method == 1 && st_fit == ALPS_OK) {
     FitArgs a;
     a.N = N;
     a.M = M;
@@ -580,9 +640,16 @@ int launch_prepare_species(alps_ctx* c, int is) {
     a.lambda0 = c->sys.lambda_initial_fit;
     a.lambdafac = c->sys.lambdafac_fit;
     a.eps = c->sys.epsilon_fit;
+    a.rel = S.sp.relat ? 1 : 0;
+    a.ng = c->sys.ngamma;
+    a.np = c->sys.npparbar;
+    a.f0rel = S.d_f0rel;
+    a.grel = S.d_grel;
+    a.prel = S.d_prel;
+    int maxpts = a.rel ? a.np : M;
     double* scratch = nullptr;
     int* d_status = nullptr;
-    ALPS_CUDA_TRY(cudaMalloc(&scratch, (size_t)(M + 1) * (FIT_MAXP + 1) * sizeof(double)));
+    ALPS_CUDA_TRY(cudaMalloc(&scratch, (size_t)(maxpts + 1) * (FIT_MAXP + 1) * sizeof(double)));
     ALPS_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
     ALPS_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), st));
     k_lm_fit<<<1, 32, 0, st>>>(a, S.d_f0, S.d_pperp, S.d_ppar, S.d_fit, scratch, d_status);

@@ -142,6 +142,16 @@ int alps_get_fit(alps_ctx* ctx, int is, double* out);
  * counterpart: there the fit lives in the param_fit global. */
 int alps_set_fit(alps_ctx* ctx, int is, const double* in);
 
+/* The (Gamma, pparbar) grid of a relativistic species after alps_prepare:
+ * gamma[ngamma+1], pparbar[npparbar+1], and f0_rel (-1 outside the
+ * subluminal cone), df0_rel/dGamma, df0_rel/dpparbar on
+ * [(igamma)*(npparbar+1) + ipparbar].  The tables the reference writes to
+ * distribution/<arrayName>_f0_rel.<is>.array and _df0_rel.<is>.array
+ * (derivative_f0_rel, src/ALPS_fns_rel.f90:211-289).  Any pointer may be
+ * NULL.  ALPS_E_INVALID for a non-relativistic species. */
+int alps_get_f0_rel(alps_ctx* ctx, int is, double* gamma, double* pparbar, double* f0_rel, double* df_dgamma,
+                    double* df_dpparbar);
+
 /* Per-wavevector setup on the device: nmax from the Bessel cutoff, Bessel
  * table, and the omega-independent p_perp contraction.
  * Replaces determine_nmax + determine_bessel_array

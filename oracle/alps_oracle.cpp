@@ -18,6 +18,7 @@
 #include "alps_oracle.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -1277,7 +1278,7 @@ void determine_resonances(const Eval& e, cplx om, int nn, bool& plus, bool& minu
 }
 
 // full_integrate (src/ALPS_fns.f90:750-792), non-relativistic branch
-int g_rel_err = 0;  // alps_error(8) raised inside a relativistic integral
+std::atomic<int> g_rel_err{0};  // alps_error(8) raised inside a relativistic integral
 
 cplx full_integrate(const Eval& e, int is1, cplx om, int nn, int mode, bool found_res) {
   if (!found_res) return integrate(e, om, nn, mode, 1, e.s->npar - 1);
@@ -2048,6 +2049,21 @@ int oracle_get_df0(oracle_ctx* c, int is, double* df1, double* df2) {
   return ALPS_OK;
 }
 
+// f0_rel tables of derivative_f0_rel (src/ALPS_fns_rel.f90:211-289)
+int oracle_get_f0_rel(oracle_ctx* c, int is, double* gamma, double* pparbar, double* f0_rel, double* df1,
+                      double* df2) {
+  if (!c || is < 0 || is >= c->sys.nspec || !c->prepared || !c->spec[is].sp.relat) return ALPS_E_INVALID;
+  const Species& s = c->spec[is];
+  if (gamma)
+    for (int ig = 0; ig <= s.ng; ++ig) gamma[ig] = s.G(ig, 0);
+  if (pparbar)
+    for (int ip = 0; ip <= s.np; ++ip) pparbar[ip] = s.PB(0, ip);
+  if (f0_rel) std::copy(s.f0rel.begin(), s.f0rel.end(), f0_rel);
+  if (df1) std::copy(s.dfr1.begin(), s.dfr1.end(), df1);
+  if (df2) std::copy(s.dfr2.begin(), s.dfr2.end(), df2);
+  return ALPS_OK;
+}
+
 // determine_nmax + determine_bessel_array (src/ALPS_fns.f90:3971-4075,
 // 4214-4255)
 int oracle_set_k(oracle_ctx* c, double kperp, double kpar) {
@@ -2099,12 +2115,13 @@ int oracle_disp(oracle_ctx* c, alps_complex om, alps_complex* D, alps_complex* c
   if (!c || !c->kset) return ALPS_E_INVALID;
   int ns = c->sys.nspec;
   std::vector<cplx> a(ns * 9), b(ns * 27), w(9);
+  g_rel_err = 0;
   cplx d = disp(c, from_c(om), a.data(), b.data(), w.data());
   if (D) *D = to_c(d);
   if (chi0) for (int k = 0; k < ns * 9; ++k) chi0[k] = to_c(a[k]);
   if (chi0_low) for (int k = 0; k < ns * 27; ++k) chi0_low[k] = to_c(b[k]);
   if (wave) for (int k = 0; k < 9; ++k) wave[k] = to_c(w[k]);
-  return ALPS_OK;
+  return g_rel_err.load();  // the reference stops with alps_error(8) here
 }
 
 int oracle_disp_mag(oracle_ctx* c, alps_complex om, double* mag) {
@@ -2116,9 +2133,10 @@ int oracle_disp_mag(oracle_ctx* c, alps_complex om, double* mag) {
 int oracle_disp_batch(oracle_ctx* c, int n, const alps_complex* om, alps_complex* D, int nthreads) {
   if (!c || !c->kset) return ALPS_E_INVALID;
   if (nthreads < 1) nthreads = 1;
+  g_rel_err = 0;
   if (nthreads == 1) {
     for (int k = 0; k < n; ++k) D[k] = to_c(disp_c(c, from_c(om[k])));
-    return ALPS_OK;
+    return g_rel_err.load();
   }
   int saved = g_threads;
   g_threads = 1;
@@ -2129,7 +2147,7 @@ int oracle_disp_batch(oracle_ctx* c, int n, const alps_complex* om, alps_complex
     });
   for (auto& x : th) x.join();
   g_threads = saved;
-  return ALPS_OK;
+  return g_rel_err.load();
 }
 
 int oracle_full_integrate(oracle_ctx* c, int is, alps_complex om, int nn, int mode, alps_complex* out,

@@ -51,6 +51,7 @@ def lib():
             L.oracle_get_fit.argtypes = [C.c_void_p, C.c_int, dp]
             L.oracle_set_fit.argtypes = [C.c_void_p, C.c_int, dp]
             L.oracle_get_df0.argtypes = [C.c_void_p, C.c_int, dp, dp]
+            L.oracle_get_f0_rel.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
             L.oracle_set_k.argtypes = [C.c_void_p, C.c_double, C.c_double]
             L.oracle_get_nmax.argtypes = [C.c_void_p, P(C.c_int)]
             L.oracle_get_bessel.argtypes = [C.c_void_p, C.c_int, dp]
@@ -159,6 +160,16 @@ class OraclePlasma:
         a, b = np.zeros(n), np.zeros(n)
         _chk(lib().oracle_get_df0(self._h, i, _dptr(a), _dptr(b)), "oracle_get_df0")
         return a, b
+
+    def get_f0_rel(self, i):
+        """(gamma, pparbar, f0_rel, df/dGamma, df/dpparbar) of a relativistic species."""
+        ng, npb = self.sys.ngamma, self.sys.npparbar
+        g, p = np.zeros(ng + 1), np.zeros(npb + 1)
+        f, a, b = (np.zeros((ng + 1) * (npb + 1)) for _ in range(3))
+        _chk(lib().oracle_get_f0_rel(self._h, i, _dptr(g), _dptr(p), _dptr(f), _dptr(a), _dptr(b)),
+             "oracle_get_f0_rel")
+        shape = (ng + 1, npb + 1)
+        return g, p, f.reshape(shape), a.reshape(shape), b.reshape(shape)
 
     def set_k(self, kperp, kpar):
         _chk(lib().oracle_set_k(self._h, kperp, kpar), "oracle_set_k")
