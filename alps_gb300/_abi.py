@@ -100,6 +100,38 @@ class alps_input(C.Structure):
     ]
 
 
+EIGEN_MAX_SPECIES = 8
+
+
+class alps_eigen(C.Structure):
+    _fields_ = [
+        ("electric", alps_complex * 3), ("magnetic", alps_complex * 3),
+        ("vmean", (alps_complex * 3) * EIGEN_MAX_SPECIES), ("ds", alps_complex * EIGEN_MAX_SPECIES),
+        ("Ps", C.c_double * EIGEN_MAX_SPECIES), ("Ps_split", (C.c_double * 4) * EIGEN_MAX_SPECIES),
+        ("ewave", C.c_double),
+    ]
+
+
+def eigen_columns(e, nspec):
+    """Values of one output row after (kperp, kpar, Re om, Im om), in the
+    order om_scan writes them (src/ALPS_fns.f90:2361-2381):
+    eigen (ef, bf, Us(1:3,1:nspec), ds), heat (Ps, W_EM), heat_mech
+    (Ps_split(1:4,1:nspec))."""
+    def cx(z):
+        return [z.re, z.im]
+    eig = []
+    for z in list(e.electric) + list(e.magnetic):
+        eig += cx(z)
+    for s in range(nspec):
+        for j in range(3):
+            eig += cx(e.vmean[s][j])
+    for s in range(nspec):
+        eig += cx(e.ds[s])
+    heat = [e.Ps[s] for s in range(nspec)] + [e.ewave]
+    mech = [e.Ps_split[s][q] for s in range(nspec) for q in range(4)]
+    return eig, heat, mech
+
+
 class alps_stats(C.Structure):
     _fields_ = [
         ("n_eval", C.c_int64), ("n_pole_terms", C.c_int64),

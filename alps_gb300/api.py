@@ -185,6 +185,14 @@ class Plasma:
         check(lib().alps_secant(self._h, method, len(oms), _cptr(oms), it, _cptr(Df)), "alps_secant")
         return oms, list(it), Df
 
+    def calc_eigen(self, oms, eigen=True, heat=True):
+        """calc_eigen for each root in oms: a list of alps_eigen (fields
+        relative to E_x, U_s, delta n_s, heating rates and their split)."""
+        oms = np.atleast_1d(np.ascontiguousarray(oms, dtype=np.complex128))
+        out = (_abi.alps_eigen * len(oms))()
+        check(lib().alps_calc_eigen(self._h, len(oms), _cptr(oms), int(eigen), int(heat), out), "alps_calc_eigen")
+        return list(out)
+
     def map_search(self, mp):
         """(om, cal, val) of map_search (src/ALPS_fns.f90:3595-3788)."""
         n = mp.nr * mp.ni
@@ -210,10 +218,11 @@ class Plasma:
         check(lib().alps_get_stats(self._h, C.byref(s)), "alps_get_stats")
         return s
 
-    def om_scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots):
+    def om_scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots, eigen=False, heat=False):
         """k-scan with root following (om_scan, src/ALPS_fns.f90:2198-2600,
-        step sizes of scan_read, src/ALPS_io.f90:426-552) without the eigen /
-        heating output.  Returns rows[it, root, (kperp, kpar, Re, Im)]."""
+        step sizes of scan_read, src/ALPS_io.f90:426-552).  Returns
+        rows[it, root, (kperp, kpar, Re, Im)] and the final roots; with eigen
+        or heat also eig[it][root] (alps_eigen of calc_eigen at that row)."""
         sy = self.sys
         wr = np.array(wroots, dtype=np.complex128)
         nroots = len(wr)
@@ -244,6 +253,10 @@ class Plasma:
         rows[0, :, 2] = wr.real
         rows[0, :, 3] = wr.imag
         jump = np.ones(nroots, dtype=bool)
+        want = eigen or heat
+        eig = [[None] * nroots for _ in range(ns + 1)] if want else None
+        if want:
+            eig[0] = self.calc_eigen(wr, eigen, heat)
         out_row = 1
         for it in range(1, ns * nres + 1):
             kperp, kpar = self.kperp, self.kpar
@@ -269,8 +282,11 @@ class Plasma:
                 raise _abi.AlpsError(9, "om_scan")
             idx = [i for i in range(nroots) if jump[i]]
             new, _, _ = self.secant(wr[idx], sy.secant_method)
+            ev = self.calc_eigen(new, eigen, heat) if (want and it % nres == 0) else None
             for q, i in enumerate(idx):
                 wr[i] = new[q]
+                if ev is not None:
+                    eig[out_row][i] = ev[q]
                 if not math.isfinite(wr[i].real):
                     jump[i] = False
                 for imm in range(i):
@@ -281,4 +297,6 @@ class Plasma:
                     rows[out_row, i] = (kperp, kpar, wr[i].real, wr[i].imag)
             if it % nres == 0:
                 out_row += 1
+        if want:
+            return rows, wr, eig
         return rows, wr

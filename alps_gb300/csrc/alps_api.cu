@@ -222,6 +222,16 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_f0, S.f0.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, fit.data(), fit.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // parallel current moment of derivative_f0 (src/ALPS_fns.f90:157-190),
+  // summed in the reference's node order
+  {
+    double dpperp = pv[2] - pv[1], dppar = std::fabs(qv[2] - qv[1]), ci = 0.0;
+    for (int i = 0; i <= N; ++i)
+      for (int j = 0; j <= M; ++j)
+        ci = ci + (sp->ns * sp->qs / sp->ms) * pv[i] * qv[j] * S.f0[(size_t)i * L + j] * 2.0 * ALPS_PI * dpperp *
+                      dppar;
+    S.current_int = ci;
+  }
   S.loaded = true;
   c->prepared = false;
   c->kset = false;
@@ -416,6 +426,141 @@ int alps_disp_batch_device(alps_ctx* c, int n, const alps_complex* d_om, alps_co
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   return launch_disp_batch(c, n, reinterpret_cast<const double2*>(d_om), reinterpret_cast<double2*>(d_D), nullptr,
                            st);
+}
+
+// calc_eigen (src/ALPS_fns.f90:2605-2899) for n roots; the det D evaluations
+// at om, Re(om) and Re(om*1.000001) of every root go out as one batch.
+int alps_calc_eigen(alps_ctx* c, int n, const alps_complex* om, int eigen, int heat, alps_eigen* out) {
+  if (!c || n < 0 || (n > 0 && (!om || !out)) || !c->kset) return ALPS_E_INVALID;
+  const int S_ = c->sys.nspec;
+  if (S_ > ALPS_EIGEN_MAX_SPECIES) return ALPS_E_INVALID;
+  if (n == 0) return ALPS_OK;
+  const int per = heat ? 3 : 1;
+  std::vector<alps_complex> oms((size_t)n * per), D((size_t)n * per);
+  for (int r = 0; r < n; ++r) {
+    oms[r] = om[r];
+    if (heat) {
+      oms[n + r] = alps_complex{om[r].re, 0.0};
+      oms[2 * n + r] = alps_complex{(cplx(om[r].re, om[r].im) * 1.000001).real(), 0.0};
+    }
+  }
+  const size_t ne = (size_t)S_ * 36 + 9;
+  std::vector<alps_complex> ext(oms.size() * ne);
+  int st = disp_host(c, (int)oms.size(), oms.data(), D.data(), ext.data());
+  if (st) return st;
+  const double vA = c->sys.vA, kperp = c->kperp, kpar = c->kpar;
+  const cplx I(0.0, 1.0), h(-0.0, -0.5);
+  auto X = [](const alps_complex& z) { return cplx(z.re, z.im); };
+  for (int r = 0; r < n; ++r) {
+    alps_eigen& o = out[r];
+    std::memset(&o, 0, sizeof(o));
+    const alps_complex* e0 = ext.data() + (size_t)r * ne;
+    auto chi = [&](const alps_complex* e, int s, int i, int j) { return X(e[s * 9 + 3 * i + j]); };
+    auto low = [&](const alps_complex* e, int s, int i, int j, int nn) {
+      return X(e[S_ * 9 + s * 27 + (nn + 1) * 9 + 3 * i + j]);
+    };
+    auto W = [&](int i, int j) { return X(e0[S_ * 36 + 3 * i + j]); };
+    const cplx w(om[r].re, om[r].im);
+    // fields relative to E_x from the wave tensor at the root
+    cplx E[3], B[3];
+    E[0] = cplx(1.0, 0.0);
+    E[2] = -E[0] * (W(1, 0) * W(2, 1) - W(2, 0) * W(1, 1));
+    E[2] = E[2] / (W(1, 2) * W(2, 1) - W(2, 2) * W(1, 1));
+    if (std::abs(W(2, 1)) != 0.0) {
+      E[1] = -E[2] * W(2, 2) - E[0] * W(2, 0);
+      E[1] = E[1] / W(2, 1);
+    } else {  // cold plasma without drifts
+      E[1] = W(1, 0) * W(0, 2) - W(0, 0) * W(1, 2);
+      E[1] = E[1] / (W(1, 2) * W(0, 1) - W(1, 1) * W(0, 2));
+    }
+    B[0] = -1.0 * kpar * E[1] / (w * vA);
+    B[1] = -1.0 * (kperp * E[2] - kpar * E[0]) / (w * vA);
+    B[2] = kperp * E[1] / (w * vA);
+    for (int i = 0; i < 3; ++i) {
+      o.electric[i] = alps_complex{E[i].real(), E[i].imag()};
+      o.magnetic[i] = alps_complex{B[i].real(), B[i].imag()};
+    }
+    if (eigen) {
+      for (int s = 0; s < S_; ++s) {
+        const SpeciesHost& Sp = c->spec[s];
+        const double qn = Sp.sp.qs * Sp.sp.ns;
+        const double pf = Sp.current_int / (Sp.sp.ns * Sp.sp.qs);
+        auto vm = [&](int j) {
+          cplx sum(0.0, 0.0);
+          for (int k = 0; k < 3; ++k) sum = sum + E[k] * chi(e0, s, j, k);
+          return -((vA * vA) / qn) * I * w * sum;
+        };
+        cplx U[3] = {vm(0), vm(1), vm(2)};
+        if (pf != 0.0) {
+          U[2] = U[2] - pf * kperp * U[0] / (w - kpar * pf);
+          U[2] = U[2] / (1.0 + (kpar * pf) / (w - kpar * pf));
+        }
+        cplx d = (1.0 / vA) * (U[0] * kperp + U[2] * kpar) / (w - kpar * pf);
+        for (int j = 0; j < 3; ++j) o.vmean[s][j] = alps_complex{U[j].real(), U[j].imag()};
+        o.ds[s] = alps_complex{d.real(), d.imag()};
+      }
+    }
+    if (!heat) continue;
+    const alps_complex* e1 = ext.data() + (size_t)(n + r) * ne;      // Re(om)
+    const alps_complex* e2 = ext.data() + (size_t)(2 * n + r) * ne;  // Re(om*1.000001)
+    // anti-Hermitian part per species at Re(om), Hermitian part of the sum
+    double Ps[ALPS_EIGEN_MAX_SPECIES];
+    for (int s = 0; s < S_; ++s) {
+      cplx sum(0.0, 0.0);
+      for (int ii = 0; ii < 3; ++ii) {
+        cplx term(0.0, 0.0);
+        for (int k = 0; k < 3; ++k)
+          term = term + std::conj(E[k]) * (-0.5 * I * (chi(e1, s, k, ii) - std::conj(chi(e1, s, ii, k))));
+        sum = sum + term * E[ii];
+      }
+      Ps[s] = sum.real();
+    }
+    auto herm = [&](const alps_complex* e, int i, int j) {
+      cplx a(0.0, 0.0), b(0.0, 0.0);
+      for (int s = 0; s < S_; ++s) a = a + chi(e, s, i, j);
+      for (int s = 0; s < S_; ++s) b = b + std::conj(chi(e, s, j, i));
+      return 0.5 * (a + b);
+    };
+    cplx s1(0.0, 0.0), s2(0.0, 0.0);
+    for (int ii = 0; ii < 3; ++ii) {
+      cplx term(0.0, 0.0);
+      for (int k = 0; k < 3; ++k) {
+        cplx dchih = (1.000001 * herm(e2, k, ii) - herm(e1, k, ii)) / 0.000001;
+        term = term + std::conj(E[k]) * dchih;
+      }
+      s1 = s1 + term * E[ii];
+    }
+    for (int ii = 0; ii < 3; ++ii) s2 = s2 + B[ii] * std::conj(B[ii]);
+    const double ewave = (s1 + s2).real();
+    o.ewave = ewave;
+    // split by mechanism from chi0_low at Re(om*1.000001)
+    for (int s = 0; s < S_; ++s) {
+      cplx c22 = low(e2, s, 1, 1, 0), c23 = low(e2, s, 1, 2, 0), c32 = low(e2, s, 2, 1, 0), c33 = low(e2, s, 2, 2, 0);
+      double p1 = (h * std::conj(E[1]) * E[1] * (c22 - std::conj(c22))).real();
+      p1 = (p1 - 0.5 * I * (E[2] * std::conj(E[1]) * c23 - std::conj(E[2]) * E[1] * std::conj(c23))).real();
+      double p2 = (h * (E[1] * std::conj(E[2]) * c32 - std::conj(E[1]) * E[2] * std::conj(c32))).real();
+      p2 = (p2 - 0.5 * I * std::conj(E[2]) * E[2] * (c33 - std::conj(c33))).real();
+      const cplx Exy[3] = {E[0], E[1], cplx(0.0, 0.0)};
+      double pc[2];
+      for (int q = 0; q < 2; ++q) {
+        int nn = q == 0 ? 1 : -1;
+        cplx sum(0.0, 0.0);
+        for (int ii = 0; ii < 3; ++ii) {
+          cplx term(0.0, 0.0);
+          for (int k = 0; k < 3; ++k)
+            term = term + std::conj(Exy[k]) * (h * (low(e2, s, k, ii, nn) - std::conj(low(e2, s, ii, k, nn))));
+          sum = sum + term * Exy[ii];
+        }
+        pc[q] = sum.real();
+      }
+      o.Ps[s] = Ps[s] / ewave;
+      o.Ps_split[s][0] = p1 / ewave;
+      o.Ps_split[s][1] = p2 / ewave;
+      o.Ps_split[s][2] = pc[0] / ewave;
+      o.Ps_split[s][3] = pc[1] / ewave;
+    }
+  }
+  return ALPS_OK;
 }
 
 int alps_set_profiling(alps_ctx* c, int on) {

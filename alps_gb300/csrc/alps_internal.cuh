@@ -140,6 +140,7 @@ struct SpeciesHost {
   size_t mom_cap = 0;
   int nmax = 0;
   double int_ee = 0.0;
+  double current_int = 0.0;  // n q P_par / m moment of the f0 table
   int rcap = 1;
 };
 

@@ -174,6 +174,7 @@ std::string fmt_es(double x, int w, int d, int e) {
   } else if (std::isinf(x)) {
     s = x < 0 ? "-Infinity" : "Infinity";
   } else {
+    if (x == 0.0) x = 0.0;  // exact zeros print unsigned, as in the reference's files
     std::snprintf(buf, sizeof(buf), "%.*E", d, x);
     std::string t(buf);
     size_t ep = t.find('E');
@@ -186,6 +187,42 @@ std::string fmt_es(double x, int w, int d, int e) {
   }
   if ((int)s.size() < w) s = std::string(w - s.size(), ' ') + s;
   return s;
+}
+
+// one output row: es14.4e3 fields (om_scan's eigen/heat formats,
+// src/ALPS_fns.f90:2261-2268)
+void write_row(FILE* f, const std::vector<double>& v) {
+  for (double x : v) std::fputs(fmt_es(x, 14, 4, 3).c_str(), f);
+  std::fputc('\n', f);
+}
+
+// columns of the .eigen_, .heat_ and .heat_mech_ rows after (kperp, kpar, om)
+void eigen_columns(const alps_eigen& e, int nspec, std::vector<double>& eig, std::vector<double>& heat,
+                   std::vector<double>& mech) {
+  eig.clear();
+  heat.clear();
+  mech.clear();
+  for (int i = 0; i < 3; ++i) {
+    eig.push_back(e.electric[i].re);
+    eig.push_back(e.electric[i].im);
+  }
+  for (int i = 0; i < 3; ++i) {
+    eig.push_back(e.magnetic[i].re);
+    eig.push_back(e.magnetic[i].im);
+  }
+  for (int s = 0; s < nspec; ++s)
+    for (int j = 0; j < 3; ++j) {
+      eig.push_back(e.vmean[s][j].re);
+      eig.push_back(e.vmean[s][j].im);
+    }
+  for (int s = 0; s < nspec; ++s) {
+    eig.push_back(e.ds[s].re);
+    eig.push_back(e.ds[s].im);
+  }
+  for (int s = 0; s < nspec; ++s) heat.push_back(e.Ps[s]);
+  heat.push_back(e.ewave);
+  for (int s = 0; s < nspec; ++s)
+    for (int q = 0; q < 4; ++q) mech.push_back(e.Ps_split[s][q]);
 }
 
 bool file_exists(const std::string& p) {
@@ -494,6 +531,35 @@ int alps_run_input(const char* input_path, const char* workdir) {
                    fmt_es(wroots[r].re, 14, 4, 3).c_str(), fmt_es(wroots[r].im, 14, 4, 3).c_str());
       std::fclose(fo);
     }
+    // eigenfunctions and heating rates (calc_eigen) on every output row
+    const bool want_eig = sc.eigen || sc.heating;
+    auto eig_name = [&](const char* kind, int r) {
+      return soldir + "/" + run + "." + kind + "_" + ids[sc.type_s] + std::to_string(ik) + ".root_" +
+             std::to_string(r + 1);
+    };
+    auto write_eigen = [&](int r, const alps_eigen& e, const char* mode) -> int {
+      std::vector<double> head = {kperp, kpar, wroots[r].re, wroots[r].im}, ev, hv, mv;
+      eigen_columns(e, s.nspec, ev, hv, mv);
+      const char* kinds[3] = {"eigen", "heat", "heat_mech"};
+      const std::vector<double>* cols[3] = {&ev, &hv, &mv};
+      for (int q = 0; q < 3; ++q) {
+        if (q == 0 && !sc.eigen) continue;
+        if (q > 0 && !sc.heating) continue;
+        FILE* f = std::fopen(eig_name(kinds[q], r).c_str(), mode);
+        if (!f) return ALPS_E_IO;
+        std::vector<double> row = head;
+        row.insert(row.end(), cols[q]->begin(), cols[q]->end());
+        write_row(f, row);
+        std::fclose(f);
+      }
+      return ALPS_OK;
+    };
+    if (want_eig) {
+      std::vector<alps_eigen> eg(nroots);
+      if ((st = alps_calc_eigen(ctx, nroots, wroots.data(), sc.eigen, sc.heating, eg.data()))) return st;
+      for (int r = 0; r < nroots; ++r)
+        if ((st = write_eigen(r, eg[r], "w"))) return st;
+    }
     int nt = sc.n_out * sc.n_res;
     double kperp_last = kperp, kpar_last = kpar;
     double theta_0 = std::atan(kperp_last / kpar_last);
@@ -541,6 +607,11 @@ int alps_run_input(const char* input_path, const char* workdir) {
           sub.push_back(wroots[r]);
         }
       if ((st = alps_secant(ctx, s.secant_method, (int)sub.size(), sub.data(), nullptr, nullptr))) return st;
+      std::vector<alps_eigen> eg;
+      if (want_eig && it % sc.n_res == 0) {
+        eg.resize(sub.size());
+        if ((st = alps_calc_eigen(ctx, (int)sub.size(), sub.data(), sc.eigen, sc.heating, eg.data()))) return st;
+      }
       for (size_t q = 0; q < idx.size(); ++q) {
         int r = idx[q];
         wroots[r] = sub[q];
@@ -557,6 +628,7 @@ int alps_run_input(const char* input_path, const char* workdir) {
           std::fprintf(fo, "%s%s%s%s\n", fmt_es(kperp, 14, 4, 3).c_str(), fmt_es(kpar, 14, 4, 3).c_str(),
                        fmt_es(wroots[r].re, 14, 4, 3).c_str(), fmt_es(wroots[r].im, 14, 4, 3).c_str());
           std::fclose(fo);
+          if (!eg.empty() && (st = write_eigen(r, eg[q], "a"))) return st;
         }
       }
     }

@@ -214,6 +214,35 @@ int alps_disp_batch_noalloc(alps_ctx* ctx, int n, const alps_complex* d_om,
 int alps_secant(alps_ctx* ctx, int method, int nroots, alps_complex* om,
                 int* iters, alps_complex* Dfinal);
 
+/* Eigenfunctions and heating rates of roots (calc_eigen,
+ * src/ALPS_fns.f90:2605-2899).  Fields are relative to E_x; velocities and
+ * densities per species; Ps the heating rate per species over the wave
+ * energy ewave (W_EM); Ps_split per species: [0] transit-time damping (the
+ * n = 0 yy and yz terms), [1] Landau damping (n = 0 zy and zz), [2] n = +1
+ * and [3] n = -1 cyclotron terms with E_z removed.  As in the reference,
+ * electric/magnetic/vmean/ds come from det D at the complex root, Ps from
+ * det D at Re(om), and ewave and Ps_split from det D at Re(om)*1.000001
+ * (the last evaluation of the reference's sequence). */
+#define ALPS_EIGEN_MAX_SPECIES 8
+typedef struct alps_eigen {
+  alps_complex electric[3];
+  alps_complex magnetic[3];
+  alps_complex vmean[ALPS_EIGEN_MAX_SPECIES][3];
+  alps_complex ds[ALPS_EIGEN_MAX_SPECIES];
+  double Ps[ALPS_EIGEN_MAX_SPECIES];
+  double Ps_split[ALPS_EIGEN_MAX_SPECIES][4];
+  double ewave;
+} alps_eigen;
+
+/* calc_eigen for n roots at once: all det D evaluations (n, or 3n with
+ * heat) go to the device in one batch.  eigen / heat select the outputs
+ * like the scan flags eigen_s / heat_s; with heat = 0 Ps, Ps_split and
+ * ewave are zero, with eigen = 0 vmean and ds are zero.  The parallel flow
+ * U_s = current_int/(n_s q_s) of each species is the p_par moment of its f0
+ * table (derivative_f0, src/ALPS_fns.f90:157-190). */
+int alps_calc_eigen(alps_ctx* ctx, int n, const alps_complex* om, int eigen,
+                    int heat, alps_eigen* out);
+
 /* Complex-frequency map (map_search, src/ALPS_fns.f90:3595-3788, without the
  * file output): om[ir*ni+ii], cal = det D with NaN/Inf sentinels, val =
  * log10|D| with sentinels.  Any output pointer may be NULL. */
@@ -269,8 +298,9 @@ int alps_read_f0(const char* path, int nperp, int npar, double* pperp,
 /* Runs a whole ALPS input file (the main program src/ALPS.f90:19-147): map
  * search or guesses, refine_guess, and the k scans (scan_option 1), reading
  * f0 tables from <workdir>/distribution/<arrayName>.<is>.array and writing
- * <workdir>/solution/<runname>.roots, .map and .scan_<id><ik>.root_<in> in
- * the reference's formats (src/ALPS_fns.f90:2346-2584, 3745, 3849). */
+ * <workdir>/solution/<runname>.roots, .map, .scan_<id><ik>.root_<in> and,
+ * for scans with eigen / heating, .eigen_*, .heat_* and .heat_mech_* in the
+ * reference's formats (src/ALPS_fns.f90:2346-2584, 3745, 3849). */
 int alps_run_input(const char* input_path, const char* workdir);
 
 /* f0 table generator (distribution/generate_distribution.f90:176-300):

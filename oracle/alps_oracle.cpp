@@ -312,6 +312,7 @@ void lu_inverse(int n, const std::vector<double>& lu, const std::vector<int>& pi
 struct Species {
   alps_species sp;
   int nperp = 0, npar = 0;
+  double current_int = 0.0;            // n q P_par / m moment of f0
   std::vector<double> pp1, pp2, f0;    // [(nperp+1)*(npar+1)]
   std::vector<double> df1, df2;        // same layout, interior valid
   std::vector<double> param_fit;       // [(iperp*5+ip)*nf + ifit]
@@ -1588,6 +1589,17 @@ cplx disp_c(const oracle_ctx* c, cplx om) { return disp(c, om, nullptr, nullptr,
 // ---------------------------------------------------------------------------
 void derivative_f0(Species& s) {
   int N = s.nperp, M = s.npar;
+  // parallel current moment (:157-190), summed in the reference's order
+  {
+    double dpperp = s.P1(2, 2) - s.P1(1, 2);
+    double dppar = std::fabs(s.P2(2, 2) - s.P2(2, 1));
+    double ci = 0.0;
+    for (int i = 0; i <= N; ++i)
+      for (int j = 0; j <= M; ++j)
+        ci = ci + (s.sp.ns * s.sp.qs / s.sp.ms) * s.P1(i, j) * s.P2(i, j) * s.f0[s.idx(i, j)] * 2.0 * PI * dpperp *
+                      dppar;
+    s.current_int = ci;
+  }
   s.df1.assign((N + 1) * (M + 1), 0.0);
   s.df2.assign((N + 1) * (M + 1), 0.0);
   for (int i = 1; i <= N - 1; ++i)
@@ -2263,8 +2275,152 @@ int oracle_find_minima(const double* val, int nr, int ni, int numroots, int* iro
   return ALPS_OK;
 }
 
-// om_scan (src/ALPS_fns.f90:2198-2600) without eigen/heat output
-int oracle_scan(oracle_ctx* c, const oracle_scan_def* sd, int nroots, alps_complex* wroots, double* rows) {
+// calc_eigen (src/ALPS_fns.f90:2605-2899), with the det D evaluation at the
+// root that precedes it in om_scan (:2340, :2523)
+int calc_eigen(oracle_ctx* c, cplx omega, bool eigen_L, bool heat_L, alps_eigen* o) {
+  const int ns = c->sys.nspec;
+  if (ns > ALPS_EIGEN_MAX_SPECIES) return ALPS_E_INVALID;
+  const double vA = c->sys.vA, kperp = c->kperp, kpar = c->kpar;
+  std::memset(o, 0, sizeof(*o));
+  std::vector<cplx> chi0(ns * 9), chil(ns * 27), wv(9);
+  g_rel_err = 0;
+  disp(c, omega, chi0.data(), chil.data(), wv.data());
+  auto W = [&](int i, int j) { return wv[3 * (i - 1) + (j - 1)]; };
+  auto C0 = [&](const std::vector<cplx>& a, int s, int i, int j) { return a[(s - 1) * 9 + 3 * (i - 1) + (j - 1)]; };
+  auto CL = [&](const std::vector<cplx>& a, int s, int i, int j, int n) {
+    return a[(s - 1) * 27 + 9 * (n + 1) + 3 * (i - 1) + (j - 1)];
+  };
+  cplx E[4], B[4];  // 1-based
+  E[1] = cplx(1.0, 0.0);
+  E[3] = -E[1] * (W(2, 1) * W(3, 2) - W(3, 1) * W(2, 2));
+  E[3] = E[3] / (W(2, 3) * W(3, 2) - W(3, 3) * W(2, 2));
+  if (std::abs(W(3, 2)) != 0.0) {
+    E[2] = -E[3] * W(3, 3) - E[1] * W(3, 1);
+    E[2] = E[2] / W(3, 2);
+  } else {
+    E[2] = W(2, 1) * W(1, 3) - W(1, 1) * W(2, 3);
+    E[2] = E[2] / (W(2, 3) * W(1, 2) - W(2, 2) * W(1, 3));
+  }
+  B[1] = -1.0 * kpar * E[2] / (omega * vA);
+  B[2] = -1.0 * (kperp * E[3] - kpar * E[1]) / (omega * vA);
+  B[3] = kperp * E[2] / (omega * vA);
+  for (int i = 1; i <= 3; ++i) {
+    o->electric[i - 1] = to_c(E[i]);
+    o->magnetic[i - 1] = to_c(B[i]);
+  }
+  const cplx I(0.0, 1.0);
+  if (eigen_L) {
+    for (int jj = 1; jj <= ns; ++jj) {
+      const Species& s = c->spec[jj - 1];
+      double qn = s.sp.qs * s.sp.ns;
+      double pf = s.current_int / (s.sp.ns * s.sp.qs);
+      cplx U[4];
+      auto vm = [&](int j) {
+        cplx sum(0.0, 0.0);
+        for (int k = 1; k <= 3; ++k) sum = sum + E[k] * C0(chi0, jj, j, k);
+        return -((vA * vA) / qn) * I * omega * sum;
+      };
+      if (pf == 0.0) {
+        for (int j = 1; j <= 3; ++j) U[j] = vm(j);
+      } else {
+        U[1] = vm(1);
+        U[2] = vm(2);
+        U[3] = vm(3) - pf * kperp * U[1] / (omega - kpar * pf);
+        U[3] = U[3] / (1.0 + (kpar * pf) / (omega - kpar * pf));
+      }
+      cplx d = (1.0 / vA) * (U[1] * kperp + U[3] * kpar) / (omega - kpar * pf);
+      for (int j = 1; j <= 3; ++j) o->vmean[jj - 1][j - 1] = to_c(U[j]);
+      o->ds[jj - 1] = to_c(d);
+    }
+  }
+  if (heat_L) {
+    std::vector<cplx> chr(ns * 9), chlr(ns * 27), w2(9);
+    disp(c, cplx(omega.real(), 0.0), chr.data(), chlr.data(), w2.data());
+    cplx chihold[4][4];
+    std::vector<double> Ps(ns + 1, 0.0);
+    for (int jj = 1; jj <= ns; ++jj) {
+      cplx chia[4][4];
+      for (int ii = 1; ii <= 3; ++ii)
+        for (int j = 1; j <= 3; ++j) chia[ii][j] = -0.5 * I * (C0(chr, jj, ii, j) - std::conj(C0(chr, jj, j, ii)));
+      cplx term[4];
+      for (int ii = 1; ii <= 3; ++ii) {
+        cplx sum(0.0, 0.0);
+        for (int k = 1; k <= 3; ++k) sum = sum + std::conj(E[k]) * chia[k][ii];
+        term[ii] = sum;
+      }
+      cplx sum(0.0, 0.0);
+      for (int ii = 1; ii <= 3; ++ii) sum = sum + term[ii] * E[ii];
+      Ps[jj] = sum.real();
+    }
+    for (int ii = 1; ii <= 3; ++ii)
+      for (int j = 1; j <= 3; ++j) {
+        cplx a(0.0, 0.0), b(0.0, 0.0);
+        for (int jj = 1; jj <= ns; ++jj) a = a + C0(chr, jj, ii, j);
+        for (int jj = 1; jj <= ns; ++jj) b = b + std::conj(C0(chr, jj, j, ii));
+        chihold[ii][j] = 0.5 * (a + b);
+      }
+    std::vector<cplx> chp(ns * 9), chlp(ns * 27), w3(9);
+    disp(c, cplx((omega * 1.000001).real(), 0.0), chp.data(), chlp.data(), w3.data());
+    cplx dchih[4][4];
+    for (int ii = 1; ii <= 3; ++ii)
+      for (int j = 1; j <= 3; ++j) {
+        cplx a(0.0, 0.0), b(0.0, 0.0);
+        for (int jj = 1; jj <= ns; ++jj) a = a + C0(chp, jj, ii, j);
+        for (int jj = 1; jj <= ns; ++jj) b = b + std::conj(C0(chp, jj, j, ii));
+        cplx chih = 0.5 * (a + b);
+        dchih[ii][j] = (1.000001 * chih - chihold[ii][j]) / 0.000001;
+      }
+    cplx term1[4];
+    for (int ii = 1; ii <= 3; ++ii) {
+      cplx sum(0.0, 0.0);
+      for (int k = 1; k <= 3; ++k) sum = sum + std::conj(E[k]) * dchih[k][ii];
+      term1[ii] = sum;
+    }
+    cplx s1(0.0, 0.0), s2(0.0, 0.0);
+    for (int ii = 1; ii <= 3; ++ii) s1 = s1 + term1[ii] * E[ii];
+    for (int ii = 1; ii <= 3; ++ii) s2 = s2 + B[ii] * std::conj(B[ii]);
+    double ewave = (s1 + s2).real();
+    const cplx h(-0.0, -0.5);  // -0.5*cmplx(0.,1.) in single precision
+    for (int jj = 1; jj <= ns; ++jj) {
+      double ps[5] = {0, 0, 0, 0, 0};
+      cplx c22 = CL(chlp, jj, 2, 2, 0), c23 = CL(chlp, jj, 2, 3, 0), c32 = CL(chlp, jj, 3, 2, 0),
+           c33 = CL(chlp, jj, 3, 3, 0);
+      ps[1] = (h * std::conj(E[2]) * E[2] * (c22 - std::conj(c22))).real();
+      ps[1] = (ps[1] - 0.5 * I * (E[3] * std::conj(E[2]) * c23 - std::conj(E[3]) * E[2] * std::conj(c23))).real();
+      ps[2] = (h * (E[2] * std::conj(E[3]) * c32 - std::conj(E[2]) * E[3] * std::conj(c32))).real();
+      ps[2] = (ps[2] - 0.5 * I * std::conj(E[3]) * E[3] * (c33 - std::conj(c33))).real();
+      cplx Exy[4] = {cplx(0, 0), E[1], E[2], cplx(0.0, 0.0)};
+      for (int q = 0; q < 2; ++q) {
+        int n = q == 0 ? 1 : -1;
+        cplx chia[4][4];
+        for (int ii = 1; ii <= 3; ++ii)
+          for (int j = 1; j <= 3; ++j) chia[ii][j] = h * (CL(chlp, jj, ii, j, n) - std::conj(CL(chlp, jj, j, ii, n)));
+        cplx term[4];
+        for (int ii = 1; ii <= 3; ++ii) {
+          cplx sum(0.0, 0.0);
+          for (int k = 1; k <= 3; ++k) sum = sum + std::conj(Exy[k]) * chia[k][ii];
+          term[ii] = sum;
+        }
+        cplx sum(0.0, 0.0);
+        for (int ii = 1; ii <= 3; ++ii) sum = sum + term[ii] * Exy[ii];
+        ps[3 + q] = sum.real();
+      }
+      o->Ps[jj - 1] = Ps[jj] / ewave;
+      for (int q = 0; q < 4; ++q) o->Ps_split[jj - 1][q] = ps[q + 1] / ewave;
+    }
+    o->ewave = ewave;
+  }
+  return g_rel_err.load();
+}
+
+int oracle_calc_eigen(oracle_ctx* c, alps_complex om, int eigen, int heat, alps_eigen* out) {
+  if (!c || !c->kset || !out) return ALPS_E_INVALID;
+  return calc_eigen(c, from_c(om), eigen != 0, heat != 0, out);
+}
+
+// om_scan (src/ALPS_fns.f90:2198-2600)
+int oracle_scan(oracle_ctx* c, const oracle_scan_def* sd, int nroots, alps_complex* wroots, double* rows,
+                alps_eigen* eig) {
   if (!c || !c->kset || !sd) return ALPS_E_INVALID;
   const alps_system& sy = c->sys;
   int ns = sd->n_out, nres = sd->n_res;
@@ -2306,11 +2462,16 @@ int oracle_scan(oracle_ctx* c, const oracle_scan_def* sd, int nroots, alps_compl
   }
   (void)pi;
   std::vector<char> jump(nroots, 1);
+  const bool want_eig = eig && (sd->eigen || sd->heat);
   for (int in = 0; in < nroots; ++in) {
     rows[in * 4 + 0] = c->kperp;
     rows[in * 4 + 1] = c->kpar;
     rows[in * 4 + 2] = wroots[in].re;
     rows[in * 4 + 3] = wroots[in].im;
+    if (want_eig) {
+      int st = calc_eigen(c, from_c(wroots[in]), sd->eigen != 0, sd->heat != 0, &eig[in]);
+      if (st) return st;
+    }
   }
   int nt = ns * nres;
   theta_0 = std::atan(kperp_last / kpar_last);
@@ -2363,7 +2524,13 @@ int oracle_scan(oracle_ctx* c, const oracle_scan_def* sd, int nroots, alps_compl
       else if (sy.secant_method == 1) omega = rtsec(c, omega, &it2, nullptr);
       else omega = secant_osc(c, omega, &it2, nullptr);
       wroots[in] = to_c(omega);
-      (void)disp_c(c, omega);  // the final disp of the reference (:2523)
+      // the final disp of the reference (:2523), then calc_eigen on output rows
+      if (want_eig && it % nres == 0) {
+        int st = calc_eigen(c, omega, sd->eigen != 0, sd->heat != 0, &eig[(size_t)out_row * nroots + in]);
+        if (st) return st;
+      } else {
+        (void)disp_c(c, omega);
+      }
       double re = omega.real();
       if (std::fabs(re) >= 1.79769313486231571e308 || re != re) { omega = 0.0; jump[in] = 0; }
       for (int imm = 0; imm < in; ++imm)

@@ -64,9 +64,16 @@ typedef struct oracle_scan_def {
   double swi, swf;
   int log_scan;
   int n_out, n_res;
+  int eigen, heat; /* calc_eigen on every output row (eig[it*nroots + in]) */
 } oracle_scan_def;
 int oracle_scan(oracle_ctx* ctx, const oracle_scan_def* sd, int nroots,
-                alps_complex* wroots, double* rows);
+                alps_complex* wroots, double* rows, alps_eigen* eig);
+
+/* calc_eigen (src/ALPS_fns.f90:2605-2899) at one root, including the det D
+ * evaluations at om, Re(om) and Re(om*1.000001) that the reference makes
+ * around it. */
+int oracle_calc_eigen(oracle_ctx* ctx, alps_complex om, int eigen, int heat,
+                      alps_eigen* out);
 
 double oracle_bessj(int n, double x);
 /* Threads used inside one disp() call (orders in parallel, summed in the

@@ -63,7 +63,8 @@ def lib():
             L.oracle_secant.argtypes = [C.c_void_p, C.c_int, cp, P(C.c_int), cp]
             L.oracle_map.argtypes = [C.c_void_p, P(_abi.alps_map_params), cp, cp, dp, C.c_int]
             L.oracle_find_minima.argtypes = [dp, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int)]
-            L.oracle_scan.argtypes = [C.c_void_p, C.c_void_p, C.c_int, cp, dp]
+            L.oracle_scan.argtypes = [C.c_void_p, C.c_void_p, C.c_int, cp, dp, C.c_void_p]
+            L.oracle_calc_eigen.argtypes = [C.c_void_p, alps_complex, C.c_int, C.c_int, P(_abi.alps_eigen)]
             L.oracle_set_threads.argtypes = [C.c_int]
             L.oracle_set_threads.restype = None
             L.oracle_bessj.argtypes = [C.c_int, C.c_double]
@@ -75,7 +76,8 @@ def lib():
 
 class ScanDef(C.Structure):
     _fields_ = [("type_s", C.c_int), ("swi", C.c_double), ("swf", C.c_double),
-                ("log_scan", C.c_int), ("n_out", C.c_int), ("n_res", C.c_int)]
+                ("log_scan", C.c_int), ("n_out", C.c_int), ("n_res", C.c_int),
+                ("eigen", C.c_int), ("heat", C.c_int)]
 
 
 def _chk(st, where):
@@ -236,12 +238,25 @@ class OraclePlasma:
         _chk(lib().oracle_map(self._h, C.byref(mp), _cptr(om), _cptr(cal), _dptr(val), nthreads), "oracle_map")
         return om, cal, val
 
-    def scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots):
-        sd = ScanDef(type_s, swi, swf, int(log_scan), n_out, n_res)
+    def scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots, eigen=False, heat=False):
+        """om_scan: rows [it, root, (kperp, kpar, re, im)] and the updated
+        roots; with eigen/heat also a list [it][root] of alps_eigen."""
+        sd = ScanDef(type_s, swi, swf, int(log_scan), n_out, n_res, int(eigen), int(heat))
         wr = np.ascontiguousarray(wroots, dtype=np.complex128)
         rows = np.zeros((n_out + 1) * len(wr) * 4)
-        _chk(lib().oracle_scan(self._h, C.byref(sd), len(wr), _cptr(wr), _dptr(rows)), "oracle_scan")
-        return rows.reshape(n_out + 1, len(wr), 4), wr
+        eig = (_abi.alps_eigen * ((n_out + 1) * len(wr)))() if (eigen or heat) else None
+        _chk(lib().oracle_scan(self._h, C.byref(sd), len(wr), _cptr(wr), _dptr(rows),
+                               C.cast(eig, C.c_void_p) if eig is not None else None), "oracle_scan")
+        rows = rows.reshape(n_out + 1, len(wr), 4)
+        if eig is None:
+            return rows, wr
+        return rows, wr, [[eig[it * len(wr) + r] for r in range(len(wr))] for it in range(n_out + 1)]
+
+    def calc_eigen(self, om, eigen=True, heat=True):
+        out = _abi.alps_eigen()
+        _chk(lib().oracle_calc_eigen(self._h, alps_complex(om.real, om.imag), int(eigen), int(heat), C.byref(out)),
+             "oracle_calc_eigen")
+        return out
 
 
 def find_minima(val, nr, ni, numroots=100):

@@ -205,8 +205,9 @@ def test_kpar_fast_scan_on_gpu_matches_golden(api, golden_dir):
 
 
 def test_run_input_kpar_fast_reproduces_golden_files(api, golden_dir, tmp_path):
-    """alps_run_input on the reference's CI input writes the .scan file the
-    reference's CI asserts on, byte for byte."""
+    """alps_run_input on the reference's CI input writes the .scan and
+    .eigen files the reference's CI asserts on byte for byte, and the .heat
+    file to its last printed digit."""
     import shutil
     from alps_gb300.distribution import generate_distribution
     ref = os.path.join(golden_dir, "ref")
@@ -214,8 +215,20 @@ def test_run_input_kpar_fast_reproduces_golden_files(api, golden_dir, tmp_path):
                           str(tmp_path / "distribution"))
     shutil.copyfile(os.path.join(ref, "inputs", "tests", "test_kpar_fast.in"), str(tmp_path / "test_kpar_fast.in"))
     api.run_input(str(tmp_path / "test_kpar_fast.in"), str(tmp_path))
-    got = open(str(tmp_path / "solution" / "test_kpar_fast.scan_kpara_1.root_1")).read()
-    want = open(os.path.join(ref, "test_kpar_fast.scan_kpara_1.root_1")).read()
-    assert got == want
-    roots = open(str(tmp_path / "solution" / "test_kpar_fast.roots")).read().split()
+    sol = tmp_path / "solution"
+    for name in ("scan", "eigen"):
+        got = open(str(sol / ("test_kpar_fast.%s_kpara_1.root_1" % name))).read()
+        want = open(os.path.join(ref, "test_kpar_fast.%s_kpara_1.root_1" % name)).read()
+        assert got == want, name
+    # heating rates: a forward difference over 1e-6 Re(omega) amplifies the
+    # chi rounding, so the last printed digit may differ by one
+    got = np.loadtxt(str(sol / "test_kpar_fast.heat_kpara_1.root_1"))
+    want = np.loadtxt(os.path.join(ref, "test_kpar_fast.heat_kpara_1.root_1"))
+    np.testing.assert_allclose(got, want, rtol=1e-2)
+    np.testing.assert_allclose(got, want, rtol=2e-4)
+    got = np.loadtxt(str(sol / "test_kpar_fast.heat_mech_kpara_1.root_1"))
+    want = np.loadtxt(os.path.join(ref, "test_kpar_fast.heat_mech_kpara_1.root_1"))
+    np.testing.assert_allclose(got, want, rtol=1e-2)
+    assert np.array_equal(got == 0.0, want == 0.0)
+    roots = open(str(sol / "test_kpar_fast.roots")).read().split()
     assert roots[0] == "1" and len(roots) == 6
