@@ -87,8 +87,12 @@ class Plasma:
         check(L.alps_create(C.byref(system), C.byref(self._h)), "alps_create")
         self.species = []
         for i, (sp, pperp, ppar, f0) in enumerate(species):
-            a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pperp, ppar, f0)]
-            check(L.alps_set_species(self._h, i, C.byref(sp), *[_dptr(x) for x in a]), "alps_set_species")
+            if pperp is None:  # bi-Maxwellian / cold species (use_bM): no table
+                ptrs = [None, None, None]
+            else:
+                a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pperp, ppar, f0)]
+                ptrs = [_dptr(x) for x in a]
+            check(L.alps_set_species(self._h, i, C.byref(sp), *ptrs), "alps_set_species")
             self.species.append(sp)
         self.set_precision(precision)
         if prepare:

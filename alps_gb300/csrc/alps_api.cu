@@ -139,6 +139,7 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_dfr2);
     cudaFree(S.d_jrel);
     cudaFree(S.d_cone);
+    cudaFree(S.d_bmI);
   }
   cudaFree(c->d_om);
   cudaFree(c->d_D);
@@ -149,6 +150,7 @@ void alps_destroy(alps_ctx* c) {
   cudaFree(c->d_items);
   cudaFree(c->d_ext);
   cudaFree(c->d_rel);
+  cudaFree(c->d_bm);
   cudaFree(c->d_flags);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   for (auto& ev : c->ev_pending)
@@ -166,10 +168,42 @@ static int fit_rows(const alps_ctx* c, int is) {
   return r + 1;
 }
 
+// A bi-Maxwellian or cold species evaluated in closed form (use_bM = T): no
+// f0 table, no derivatives or fits (read_f0 and determine_param_fit skip
+// it, src/ALPS_io.f90:672-675, src/ALPS_analyt.f90:447-451).
+static int set_species_bm(alps_ctx* c, int is, const alps_species* sp) {
+  if (sp->relat) return ALPS_E_UNSUPPORTED;
+  if (sp->qs == 0.0 || !(sp->ms > 0.0) || !(sp->ns > 0.0) || sp->bM_betas < 0.0) return ALPS_E_INVALID;
+  if (sp->bM_betas > 0.0 && (!(sp->bM_alphas > 0.0) || sp->bM_nmaxs < 0)) return ALPS_E_INVALID;
+  // the cold closed form is written for kperp_norm = T (calc_chi_cold stops otherwise)
+  if (sp->bM_betas == 0.0 && !c->sys.kperp_norm) return ALPS_E_INVALID;
+  SpeciesHost& S = c->spec[is];
+  S.sp = *sp;
+  S.sp.n_fits = 1;
+  S.sp.relat = 0;
+  S.pperp.clear();
+  S.ppar.clear();
+  S.f0.clear();
+  int rows = fit_rows(c, is);
+  if (S.d_fit) cudaFree(S.d_fit);
+  S.d_fit = nullptr;
+  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)rows * 5 * sizeof(double)));
+  ALPS_CUDA_TRY(cudaMemsetAsync(S.d_fit, 0, (size_t)rows * 5 * sizeof(double), c->stream));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  // derivative_f0's current moment of a bi-Maxwellian (src/ALPS_fns.f90:162-166)
+  S.current_int = sp->ns * sp->qs * sp->bM_pdrifts / sp->ms;
+  S.int_ee = 0.0;
+  S.loaded = true;
+  c->prepared = false;
+  c->kset = false;
+  return ALPS_OK;
+}
+
 int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* pperp, const double* ppar,
                      const double* f0) {
-  if (!c || !sp || !pperp || !ppar || !f0 || is < 0 || is >= c->sys.nspec) return ALPS_E_INVALID;
-  if (sp->use_bM) return ALPS_E_UNSUPPORTED;
+  if (!c || !sp || is < 0 || is >= c->sys.nspec) return ALPS_E_INVALID;
+  if (sp->use_bM) return set_species_bm(c, is, sp);
+  if (!pperp || !ppar || !f0) return ALPS_E_INVALID;
   if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
   if (sp->ac_method != 0 && sp->ac_method != 1) return ALPS_E_INVALID;
   // relativistic species: continuation on the (Gamma, pparbar) rows, fit
@@ -303,7 +337,7 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     for (int is = 0; is < S_; ++is) max_procs += nm[is];
     int is = 0;
     while (max_procs < c->sys.nproc - 1) {
-      nm[is] += 1;
+      if (!c->spec[is].sp.use_bM) nm[is] += 1;
       is = (is + 1) % S_;
       max_procs++;
     }
@@ -311,6 +345,12 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
   for (int is = 0; is < S_; ++is) {
     SpeciesHost& S = c->spec[is];
     S.nmax = nm[is];
+    if (S.sp.use_bM) {  // closed form: only the I_n table of k_perp
+      S.rcap = 1;
+      int st = launch_nhds_bessel(c, is, kperp);
+      if (st) return st;
+      continue;
+    }
     int st = launch_build_bessel_and_reduced(c, is, kperp);
     if (st) return st;
     if (S.sp.relat && (st = launch_rel_bessel(c, is, kperp))) return st;

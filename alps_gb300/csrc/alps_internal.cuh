@@ -95,6 +95,11 @@ struct SpecDev {
   const double* jrel;   // [(n)*(ng+1)*(np+1)], n = 0..nmax+1: J_n at each node
   const int2* cone;     // [ng+1] first and last pparbar index inside the cone
   double int_ee_rel;
+  // bi-Maxwellian / cold species through the NHDS closed form (use_bM)
+  int bm;
+  int bm_nrun;          // Bessel orders -bm_nrun..bm_nrun
+  double bm_beta, bm_alpha, bm_pdrift;
+  const double* bmI;    // exp(-z) I_n(z), n = 0..bm_nrun+1, z from k_perp
 };
 
 struct SysDev {
@@ -135,6 +140,9 @@ struct SpeciesHost {
   double *d_grel = nullptr, *d_prel = nullptr, *d_f0rel = nullptr, *d_dfr1 = nullptr, *d_dfr2 = nullptr;
   double* d_jrel = nullptr;
   int2* d_cone = nullptr;
+  // NHDS species: exp(-z) I_n(z) table of the current k_perp
+  double* d_bmI = nullptr;
+  int bm_nrun = 0;
   size_t jrel_cap = 0;
   double int_ee_rel = 0.0;
   size_t mom_cap = 0;
@@ -168,6 +176,8 @@ struct alps_ctx {
   double2* d_ext = nullptr;     // [n][S*9 + S*27 + 9] extended outputs
   double2* d_rel = nullptr;     // [n][S][2*nmax+1][6] relativistic orders
   size_t rel_cap = 0;
+  double2* d_bm = nullptr;      // [n][S][24] NHDS chi (6) and chi_low (3 x 6)
+  size_t bm_cap = 0;
   size_t ext_cap = 0;
   int* d_flags = nullptr;       // error flags
   alps_stats stats = {};
@@ -192,6 +202,10 @@ int launch_fit_aux(alps_ctx* c, int is);
 int launch_landau_moments(alps_ctx* c, int is);
 int launch_rel_prepare(alps_ctx* c, int is);
 int launch_rel_bessel(alps_ctx* c, int is, double kperp);
+// NHDS species: the I_n table of k_perp (per k) and chi per omega,
+// out[(w*nspec + s)*24 + {0..5 chi, 6 + 6*(n+1) + e chi_low}]
+int launch_nhds_bessel(alps_ctx* c, int is, double kperp);
+int launch_nhds(const SysDev& sys, const SpecDev* sp, int n, const double2* d_om, double2* d_out, cudaStream_t st);
 // per-order relativistic results out[((w*nspec + s)*relcap + n)*2 + sign][6]
 int launch_rel_orders(const SysDev& sys, const SpecDev* sp, int relcap, int n, const double2* d_om, double2* d_out,
                       int* d_flags, cudaStream_t st);

@@ -32,6 +32,7 @@ struct DispArgs {
   int csize;     // orders per chunk
   int rcap;      // max resonant slots over species
   int relcap;    // order slots per relativistic species (max nmax + 1), 0 if none
+  int has_bm;    // some species go through the NHDS closed form
 };
 
 namespace {
@@ -43,7 +44,7 @@ __global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om,
   int s = blockIdx.y;
   if (t >= n_om) return;
   const SpecDev& S = a.sp[s];
-  if (S.relat) {  // relativistic orders run in k_rel_orders
+  if (S.relat || S.bm) {  // relativistic orders run in k_rel_orders, NHDS species in k_nhds
     count[(size_t)t * a.sys.nspec + s] = 0;
     return;
   }
@@ -76,7 +77,7 @@ __global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __
   const SpecDev& S = a.sp[s];
   const int chunk = blockIdx.z;
   const int n_begin = chunk * a.csize;
-  const int n_end = S.relat ? n_begin : min(S.nmax + 1, n_begin + a.csize);
+  const int n_end = (S.relat || S.bm) ? n_begin : min(S.nmax + 1, n_begin + a.csize);
   const int TW = blockDim.x / js_count;
   const int wl = threadIdx.x % TW, js = threadIdx.x / TW;
   const int w = blockIdx.x * TW + wl;
@@ -602,7 +603,8 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
 __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om, const double2* __restrict__ part,
                            const double2* __restrict__ low, const int* __restrict__ count,
                            const int* __restrict__ slot_nn, const double2* __restrict__ items,
-                           const double2* __restrict__ rel, double2* D, double2* ext) {
+                           const double2* __restrict__ rel, const double2* __restrict__ bmres, double2* D,
+                           double2* ext) {
   int w = blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= n_om) return;
   const int S_ = a.sys.nspec;
@@ -636,7 +638,15 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
         if (nn >= -1 && nn <= 1) cl[nn + 1][e] = cadd(cl[nn + 1][e], v);
       }
     }
-    if (S.relat) {
+    if (S.bm) {
+      // NHDS chi, divided by n q before the common normalisation as in disp
+      // (src/ALPS_fns.f90:344-358); no ee term
+      const double2* b = bmres + ((size_t)w * S_ + s) * 24;
+      const double nq = S.ns * S.qs;
+      for (int e = 0; e < 6; ++e) chi[e] = cadd(chi[e], cmk(b[e].x / nq, b[e].y / nq));
+      for (int l = 0; l < 3; ++l)
+        for (int e = 0; e < 6; ++e) cl[l][e] = cmk(b[6 + 6 * l + e].x / nq, b[6 + 6 * l + e].y / nq);
+    } else if (S.relat) {
       // orders in the reference's order; n = 0 adds yy, zz, yz only, and the
       // ee term goes into chi alone (src/ALPS_fns.f90:461-497)
       for (int n = 0; n <= S.nmax; ++n) {
@@ -772,8 +782,9 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->qs = S.sp.qs;
   o->ms = S.sp.ms;
   o->ns = S.sp.ns;
-  o->dpperp = S.pperp[2] - S.pperp[1];
-  o->dppar = S.ppar[2] - S.ppar[1];
+  const bool bm = S.sp.use_bM != 0;
+  o->dpperp = bm ? 0.0 : S.pperp[2] - S.pperp[1];
+  o->dppar = bm ? 0.0 : S.ppar[2] - S.ppar[1];
   o->dppar_abs = std::fabs(o->dppar);
   o->species_index = is + 1;
   o->int_ee = S.int_ee;
@@ -786,8 +797,8 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->bessel = S.d_bessel;
   o->V = S.d_V;
   o->mom = S.d_mom;
-  o->pcen = 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
-  o->prad = 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
+  o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
+  o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
   // the series is used only where it is cheaper than the node sum
   o->kfar = (c->precision == ALPS_PREC_FP64) ? 0 : std::min(ALPS_KFAR, (int)(0.8 * (c->sys.npar - 1)));
   o->rcap = S.rcap;
@@ -810,6 +821,18 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->jrel = S.d_jrel;
   o->cone = S.d_cone;
   o->int_ee_rel = S.int_ee_rel;
+  o->bm = bm ? 1 : 0;
+  o->bm_nrun = S.bm_nrun;
+  o->bm_beta = S.sp.bM_betas;
+  o->bm_alpha = S.sp.bM_alphas;
+  o->bm_pdrift = S.sp.bM_pdrifts;
+  o->bmI = S.d_bmI;
+}
+
+bool any_bm(const alps_ctx* c) {
+  for (int s = 0; s < c->sys.nspec; ++s)
+    if (c->spec[s].sp.use_bM) return true;
+  return false;
 }
 
 // order slots of the relativistic per-order results (0 when no species is)
@@ -849,6 +872,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   }
   a.rcap = rc;
   a.relcap = rel_capacity(c);
+  a.has_bm = any_bm(c) ? 1 : 0;
   // order chunks: enough blocks to fill the device for small batches
   int js = 1;
   if (n < 32) js = 32;
@@ -875,6 +899,8 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * a.nchunk * 18))) return rcode;
   if (a.relcap)
     if ((rcode = ensure_buf(c->d_rel, c->rel_cap, (size_t)n * S_ * a.relcap * 2 * 6))) return rcode;
+  if (a.has_bm)
+    if ((rcode = ensure_buf(c->d_bm, c->bm_cap, (size_t)n * S_ * 24))) return rcode;
   if (!c->d_flags) ALPS_CUDA_TRY(cudaMalloc(&c->d_flags, sizeof(int)));
   ALPS_CUDA_TRY(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
 
@@ -912,16 +938,17 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   ALPS_CUDA_TRY(cudaGetLastError());
   if (a.relcap && (rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, d_om, c->d_rel, c->d_flags, st)))
     return rcode;
+  if (a.has_bm && (rcode = launch_nhds(a.sys, a.sp, n, d_om, c->d_bm, st))) return rcode;
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[3], st));
   k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, d_om, n, c->d_part, want_low ? c->d_low : nullptr, c->d_count,
-                                              c->d_slot_nn, c->d_items, c->d_rel, d_D, d_ext);
+                                              c->d_slot_nn, c->d_items, c->d_rel, c->d_bm, d_D, d_ext);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) {
     ALPS_CUDA_TRY(cudaEventRecord(ev[4], st));
     c->ev_pending.push_back(ev);
   }
   c->stats.n_eval = n;
-  c->stats.kernels_launched = a.relcap ? 5 : 4;
+  c->stats.kernels_launched = 4 + (a.relcap ? 1 : 0) + (a.has_bm ? 1 : 0);
   return ALPS_OK;
 }
 
@@ -998,6 +1025,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   }
   a.rcap = rc;
   a.relcap = rel_capacity(c);
+  a.has_bm = any_bm(c) ? 1 : 0;
   int js = 1;
   if (n < 32) js = 32;
   else if (n < 64) js = 4;
@@ -1007,7 +1035,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   int nchunk = std::max(1, std::min(maxn + 1, (152 * 4 + tiles * S_ - 1) / (tiles * S_)));
   a.csize = (maxn + 1 + nchunk - 1) / nchunk;
   a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
-  // scratch layout: flags | count | slot_nn | part | items | relativistic orders
+  // scratch layout: flags | count | slot_nn | part | items | relativistic orders | NHDS
   size_t off = 0;
   size_t o_flags = carve(off, sizeof(int));
   size_t o_count = carve(off, (size_t)n * S_ * sizeof(int));
@@ -1016,6 +1044,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   size_t o_part = carve(off, (size_t)n * S_ * a.nchunk * 6 * sizeof(double2));
   size_t o_items = carve(off, nslots * 6 * sizeof(double2));
   size_t o_rel = carve(off, (size_t)n * S_ * a.relcap * 2 * 6 * sizeof(double2));
+  size_t o_bm = carve(off, (size_t)n * S_ * (a.has_bm ? 24 : 0) * sizeof(double2));
   if (scratch_bytes) *scratch_bytes = off;
   if (off > ALPS_NOALLOC_SCRATCH_BYTES) return ALPS_E_INVALID;  // batch too large for the static scratch
   unsigned char* b = static_cast<unsigned char*>(base);
@@ -1025,6 +1054,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   double2* part = reinterpret_cast<double2*>(b + o_part);
   double2* items = reinterpret_cast<double2*>(b + o_items);
   double2* relb = reinterpret_cast<double2*>(b + o_rel);
+  double2* bmb = reinterpret_cast<double2*>(b + o_bm);
   const double2* om = reinterpret_cast<const double2*>(d_om);
   double2* D = reinterpret_cast<double2*>(d_D);
   ALPS_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), st));
@@ -1042,7 +1072,11 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
     int rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, om, relb, flags, st);
     if (rcode) return rcode;
   }
-  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, relb, D, nullptr);
+  if (a.has_bm) {
+    int rcode = launch_nhds(a.sys, a.sp, n, om, bmb, st);
+    if (rcode) return rcode;
+  }
+  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, relb, bmb, D, nullptr);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

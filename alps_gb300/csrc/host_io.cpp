@@ -459,6 +459,10 @@ int alps_run_input(const char* input_path, const char* workdir) {
   size_t nn = (size_t)(N + 1) * (M + 1);
   std::vector<double> pperp(nn), ppar(nn), f0(nn);
   for (int is = 1; is <= s.nspec; ++is) {
+    if (in.species[is - 1].use_bM) {  // closed-form species read no table (src/ALPS_io.f90:672-675)
+      if ((st = alps_set_species(ctx, is - 1, &in.species[is - 1], nullptr, nullptr, nullptr))) return st;
+      continue;
+    }
     char fn[1024];
     std::snprintf(fn, sizeof(fn), "%s/distribution/%s.%d.array", workdir, in.arrayName, is);
     if ((st = alps_read_f0(fn, N, M, pperp.data(), ppar.data(), f0.data()))) return st;

@@ -601,6 +601,7 @@ int ensure(T*& ptr, size_t& cap, size_t n) {
 // ---------------------------------------------------------------------------
 int launch_prepare_species(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
+  if (S.sp.use_bM) return ALPS_OK;  // closed form: nothing to derive or fit
   int N = c->sys.nperp, M = c->sys.npar;
   cudaStream_t st = c->stream;
   size_t nn = (size_t)(N + 1) * (M + 1);
@@ -669,6 +670,10 @@ int launch_prepare_species(alps_ctx* c, int is) {
 
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out) {
   SpeciesHost& S = c->spec[is];
+  if (S.sp.use_bM) {  // determine_nmax gives a bi-Maxwellian species 1 (src/ALPS_fns.f90:4012-4014)
+    *nmax_out = 1;
+    return ALPS_OK;
+  }
   int* d_n = nullptr;
   ALPS_CUDA_TRY(cudaMalloc(&d_n, sizeof(int)));
   k_nmax<<<1, 256, 0, c->stream>>>(S.d_pperp, c->sys.nperp, kperp, S.sp.qs, c->sys.Bessel_zero, 2000, d_n);
@@ -714,7 +719,7 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
 
 int launch_fit_aux(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
-  bool maxw = S.sp.ac_method == 1;
+  bool maxw = S.sp.ac_method == 1 && !S.sp.use_bM;
   for (int f = 0; f < S.sp.n_fits && maxw; ++f) maxw = S.sp.fit_type[f] == 1;
   if (!maxw) {
     if (S.d_fit_aux) cudaFree(S.d_fit_aux);

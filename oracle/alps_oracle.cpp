@@ -1326,6 +1326,327 @@ cplx int_ee(const Eval& e) {
   return ie;
 }
 
+// ===========================================================================
+// NHDS branch for bi-Maxwellian and cold species (src/ALPS_NHDS.f90), used
+// for species with use_bM = T (dispatched at src/ALPS_fns.f90:338-360)
+// ===========================================================================
+// BESSI0 / BESSI1 (:806-862): exp(-|x|) I_0(x), exp(-|x|) I_1(x)
+double bessi0_s(double x) {
+  const double P1 = 1.0, P2 = 3.5156229, P3 = 3.0899424, P4 = 1.2067492, P5 = 0.2659732, P6 = 0.360768e-1,
+               P7 = 0.45813e-2;
+  const double Q1 = 0.39894228, Q2 = 0.1328592e-1, Q3 = 0.225319e-2, Q4 = -0.157565e-2, Q5 = 0.916281e-2,
+               Q6 = -0.2057706e-1, Q7 = 0.2635537e-1, Q8 = -0.1647633e-1, Q9 = 0.392377e-2;
+  double ax = std::fabs(x);
+  if (ax < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return (P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7)))))) * std::exp(-ax);
+  }
+  double y = 3.75 / ax, bx = 1.0 / std::sqrt(ax);
+  ax = Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * (Q7 + y * (Q8 + y * Q9)))))));
+  return ax * bx;
+}
+
+double bessi1_s(double x) {
+  const double P1 = 0.5, P2 = 0.87890594, P3 = 0.51498869, P4 = 0.15084934, P5 = 0.2658733e-1, P6 = 0.301532e-2,
+               P7 = 0.32411e-3;
+  const double Q1 = 0.39894228, Q2 = -0.3988024e-1, Q3 = -0.362018e-2, Q4 = 0.163801e-2, Q5 = -0.1031555e-1,
+               Q6 = 0.2282967e-1, Q7 = -0.2895312e-1, Q8 = 0.1787654e-1, Q9 = -0.420059e-2;
+  double ax = std::fabs(x);
+  if (ax < 3.75) {
+    double y = (x / 3.75) * (x / 3.75);
+    return x * (P1 + y * (P2 + y * (P3 + y * (P4 + y * (P5 + y * (P6 + y * P7)))))) * std::exp(-ax);
+  }
+  double y = 3.75 / ax, bx = 1.0 / std::sqrt(ax);
+  ax = Q1 + y * (Q2 + y * (Q3 + y * (Q4 + y * (Q5 + y * (Q6 + y * (Q7 + y * (Q8 + y * Q9)))))));
+  return ax * bx;
+}
+
+// BESSI (:760-801): exp(-x) I_n(x) by Miller's downward recurrence, rescaled
+// by 2^-512 whenever the binary exponent passes 512 (maxexponent/2)
+double bessi_s(int n, double x) {
+  if (n == 0) return bessi0_s(x);
+  if (n == 1) return bessi1_s(x);
+  if (x == 0.0) return 0.0;
+  const int IBIGNO = 512;
+  double tox = 2.0 / x, bip = 0.0, bi = 1.0, r = 0.0;
+  int m = 2 * (n + (int)std::sqrt((float)(40 * n)));
+  for (int j = m; j >= 1; --j) {
+    double bim = bip + (double)j * tox * bi;
+    bip = bi;
+    bi = bim;
+    int e = 0;
+    if (bi != 0.0) std::frexp(bi, &e);
+    if (e > IBIGNO) {
+      bi = std::ldexp(bi, -IBIGNO);
+      bip = std::ldexp(bip, -IBIGNO);
+      r = std::ldexp(r, -IBIGNO);
+    }
+    if (j == n) r = bip;
+  }
+  return bessi0_s(x) * (r / bi);
+}
+
+double besselI_s(int n, double x) { return n < 0 ? bessi_s(-n, x) : bessi_s(n, x); }
+
+// x**n for integer n by right-to-left binary powering (gfortran's integer
+// power of a real)
+double powi_d(double x, int m) {
+  unsigned n = m < 0 ? -(unsigned)m : (unsigned)m;
+  double y = (n % 2) ? x : 1.0;
+  while (n >>= 1) {
+    x = x * x;
+    if (n % 2) y = y * x;
+  }
+  return m < 0 ? 1.0 / y : y;
+}
+
+// WOFZ (:537-711): Faddeeva function w(z), algorithm 680 of Poppe and
+// Wijers (ACM TOMS 16, 47, 1990), with the reference's single-precision
+// literals (6.3, 4.4, 0.85, 1.88, 1.0/J) kept as such
+void wofz(double XI, double YI, double& U, double& V, bool& FLAG) {
+  const double FACTOR = 1.12837916709551257388, RMAXREAL = 0.5e154, RMAXEXP = 708.503061461606,
+               RMAXGONI = 3.53711887601422e15;
+  FLAG = false;
+  double XABS = std::fabs(XI), YABS = std::fabs(YI);
+  double X = XABS / (double)6.3f, Y = YABS / (double)4.4f;
+  if ((XABS > RMAXREAL) || (YABS > RMAXREAL)) {
+    FLAG = true;
+    return;
+  }
+  double QRHO = X * X + Y * Y;
+  double XABSQ = XABS * XABS;
+  double XQUAD = XABSQ - YABS * YABS;
+  double YQUAD = 2 * XABS * YABS;
+  bool A = QRHO < 0.085264;
+  double U2 = 0.0, V2 = 0.0;
+  if (A) {
+    QRHO = (1 - (double)0.85f * Y) * std::sqrt(QRHO);
+    int N = (int)std::lround(6 + 72 * QRHO);
+    int J = 2 * N + 1;
+    double XSUM = (double)(1.0f / (float)J);
+    double YSUM = 0.0;
+    for (int I = N; I >= 1; --I) {
+      J = J - 2;
+      double XAUX = (XSUM * XQUAD - YSUM * YQUAD) / I;
+      YSUM = (XSUM * YQUAD + YSUM * XQUAD) / I;
+      XSUM = XAUX + (double)(1.0f / (float)J);
+    }
+    double U1 = -FACTOR * (XSUM * YABS + YSUM * XABS) + 1.0;
+    double V1 = FACTOR * (XSUM * XABS - YSUM * YABS);
+    double DAUX = std::exp(-XQUAD);
+    U2 = DAUX * std::cos(YQUAD);
+    V2 = -DAUX * std::sin(YQUAD);
+    U = U1 * U2 - V1 * V2;
+    V = U1 * V2 + V1 * U2;
+  } else {
+    double H, H2 = 0.0, QLAMBDA = 0.0;
+    int KAPN, NU;
+    if (QRHO > 1.0) {
+      H = 0.0;
+      KAPN = 0;
+      QRHO = std::sqrt(QRHO);
+      NU = (int)(3 + (1442 / (26 * QRHO + 77)));
+    } else {
+      QRHO = (1 - Y) * std::sqrt(1 - QRHO);
+      H = (double)1.88f * QRHO;
+      H2 = 2 * H;
+      KAPN = (int)std::lround(7 + 34 * QRHO);
+      NU = (int)std::lround(16 + 26 * QRHO);
+    }
+    bool B = (H > 0.0);
+    if (B) QLAMBDA = powi_d(H2, KAPN);
+    double RX = 0.0, RY = 0.0, SX = 0.0, SY = 0.0;
+    for (int N = NU; N >= 0; --N) {
+      int NP1 = N + 1;
+      double TX = YABS + H + NP1 * RX;
+      double TY = XABS - NP1 * RY;
+      double C = 0.5 / (TX * TX + TY * TY);
+      RX = C * TX;
+      RY = C * TY;
+      if (B && (N <= KAPN)) {
+        TX = QLAMBDA + SX;
+        SX = RX * TX - RY * SY;
+        SY = RY * TX + RX * SY;
+        QLAMBDA = QLAMBDA / H2;
+      }
+    }
+    if (H == 0.0) {
+      U = FACTOR * RX;
+      V = FACTOR * RY;
+    } else {
+      U = FACTOR * SX;
+      V = FACTOR * SY;
+    }
+    if (YABS == 0.0) U = std::exp(-(XABS * XABS));
+  }
+  if (YI < 0.0) {
+    if (A) {
+      U2 = 2 * U2;
+      V2 = 2 * V2;
+    } else {
+      XQUAD = -XQUAD;
+      if ((YQUAD > RMAXGONI) || (XQUAD > RMAXEXP)) {
+        FLAG = true;
+        return;
+      }
+      double W1 = 2 * std::exp(XQUAD);
+      U2 = W1 * std::cos(YQUAD);
+      V2 = -W1 * std::sin(YQUAD);
+    }
+    U = U2 - U;
+    V = V2 - V;
+    if (XI > 0.0) V = -V;
+  } else {
+    if (XI < 0.0) V = -V;
+  }
+}
+
+// dispfunct (:487-531): plasma dispersion function Z from w
+cplx dispfunct(cplx zeta, bool kpos) {
+  double XI = 1.0 * zeta.real(), YI = 1.0 * zeta.imag(), U = 0.0, V = 0.0;
+  bool flag;
+  if (kpos) {
+    wofz(XI, YI, U, V, flag);
+    return II * std::sqrt(PI) * (U + II * V);
+  }
+  wofz(-XI, -YI, U, V, flag);
+  return -(II * std::sqrt(PI) * (U + II * V));
+}
+
+struct BMParams {
+  double Omega, ell, vtherm, vdrift, alpha;
+};
+
+BMParams bm_params(const alps_species& sp) {
+  BMParams b;
+  b.Omega = sp.qs / sp.ms;
+  b.ell = std::sqrt(sp.ms / (sp.ns * sp.qs * sp.qs));
+  b.vtherm = std::sqrt(sp.bM_betas / (sp.ns * sp.ms));
+  b.vdrift = sp.bM_pdrifts / sp.ms;
+  b.alpha = sp.bM_alphas;
+  return b;
+}
+
+// calc_ypsilon (:244-367): Stix's Y tensor of order n, [i][k] 0-based
+void calc_ypsilon(cplx Y[3][3], const alps_species& sp, int n, double kz, double kperp, cplx x, bool kn) {
+  BMParams b = bm_params(sp);
+  bool kpos = !(kz < 0.0);
+  const double Omega = b.Omega, vtherm = b.vtherm, vdrift = b.vdrift, alpha = b.alpha;
+  cplx zeta = (x - kz * vdrift - 1.0 * n * Omega) / (kz * vtherm);
+  cplx resfac = x - kz * vdrift - 1.0 * n * Omega;
+  double z = 0.5 * (kperp * vtherm / Omega) * (kperp * vtherm / Omega) * alpha;
+  double zp = 0.5 * (vtherm / Omega) * (vtherm / Omega) * alpha;
+  cplx Z = dispfunct(zeta, kpos);
+  cplx An = (alpha - 1.0);
+  An = An + (1.0 / (kz * vtherm)) * (alpha * resfac + 1.0 * n * Omega) * Z;
+  cplx Bn = (alpha * (x - 1.0 * n * Omega) - (kz * vdrift - 1.0 * n * Omega)) / kz;
+  Bn = Bn + ((x - 1.0 * n * Omega) * (alpha * resfac + 1.0 * n * Omega) / (kz * kz * vtherm)) * Z;
+  double BInz = 1.0 * besselI_s(n, z);
+  double dB = 5.0e-1 * (besselI_s(n + 1, z) + besselI_s(n - 1, z));
+  double nn = (double)(n * n);
+  if (kn) {
+    Y[0][0] = 1.0 * nn * BInz * An / z;
+    Y[0][1] = -(II * (double)n * (BInz - dB) * An);
+    Y[0][2] = kperp * n * BInz * Bn / (Omega * z);
+    Y[1][0] = II * (double)n * (BInz - dB) * An;
+    Y[1][1] = (1.0 * nn * BInz / z + 2.0 * z * BInz - 2.0 * z * dB) * An;
+    Y[1][2] = II * kperp * (BInz - dB) * Bn / Omega;
+    Y[2][0] = kperp * BInz * n * Bn / (Omega * z);
+    Y[2][1] = -(II * kperp * (BInz - dB) * Bn / Omega);
+    Y[2][2] = 2.0 * (x - 1.0 * n * Omega) * BInz * Bn / (kz * vtherm * vtherm * alpha);
+  } else {
+    Y[0][0] = 1.0 * nn * BInz * An / zp;
+    Y[0][1] = -(II * (double)n * (BInz - dB) * An * kperp * kperp);
+    Y[0][2] = kperp * n * BInz * Bn / (Omega * zp);
+    Y[1][0] = II * (double)n * (BInz - dB) * An * kperp * kperp;
+    Y[1][1] = (1.0 * nn * BInz / zp + kperp * kperp * 2.0 * z * BInz - kperp * kperp * 2.0 * z * dB) * An;
+    Y[1][2] = II * kperp * kperp * kperp * (BInz - dB) * Bn / Omega;
+    Y[2][0] = kperp * BInz * n * Bn / (Omega * zp);
+    Y[2][1] = -(II * kperp * kperp * kperp * (BInz - dB) * Bn / Omega);
+    Y[2][2] = kperp * kperp * 2.0 * (x - 1.0 * n * Omega) * BInz * Bn / (kz * vtherm * vtherm * alpha);
+  }
+}
+
+// the Bessel order range of calc_chi (:131-140): first n >= 0 with n >=
+// bM_nmaxs or exp(-z) I_n(z) < bM_Bessel_zeros
+int nhds_nmaxrun(const alps_species& sp, double kperp) {
+  BMParams b = bm_params(sp);
+  double z = 0.5 * (kperp * b.vtherm / b.Omega) * (kperp * b.vtherm / b.Omega) * b.alpha;
+  int n = 0;
+  while (true) {
+    if ((n >= sp.bM_nmaxs) || (besselI_s(n, z) < sp.bM_Bessel_zeros)) return n;
+    n = n + 1;
+  }
+}
+
+// calc_chi_cold (:371-455), kperp_norm = T only
+void calc_chi_cold(cplx chi[3][3], const alps_species& sp, double kz, double kperp, cplx x) {
+  BMParams b = bm_params(sp);
+  const double Omega = b.Omega, ell = b.ell, vdrift = b.vdrift;
+  cplx d = x - kz * vdrift;
+  cplx dispR = -(1.0 / (ell * ell)) * (x - kz * vdrift) / (x - kz * vdrift + Omega);
+  cplx dispL = -(1.0 / (ell * ell)) * (x - kz * vdrift) / (x - kz * vdrift - Omega);
+  cplx dispP = (x * x / (d * d)) + ((kperp * vdrift) * (kperp * vdrift) / (d * d - Omega * Omega));
+  dispP = -(1.0 / (ell * ell)) * dispP;
+  cplx dispJ = -(1.0 / (ell * ell)) * kperp * vdrift * (x - kz * vdrift) / (d * d - Omega * Omega);
+  cplx dispM = II * (1.0 / (ell * ell)) * kperp * vdrift * Omega / (d * d - Omega * Omega);
+  chi[0][0] = (dispR + dispL) / 2.0;
+  chi[0][1] = -(II * (dispR - dispL) / 2.0);
+  chi[0][2] = dispJ;
+  chi[1][0] = II * (dispR - dispL) / 2.0;
+  chi[1][1] = (dispR + dispL) / 2.0;
+  chi[1][2] = dispM;
+  chi[2][0] = dispJ;
+  chi[2][1] = -dispM;
+  chi[2][2] = dispP;
+}
+
+// calc_chi (:59-238): chi[i][k] and chi_low[n+1][i][k] of one species;
+// mag[i][k] receives sum over n of |Y_n(i,k)| / ell^2
+void calc_chi_nhds(cplx chi[3][3], cplx low[3][3][3], double mag[3][3], const alps_species& sp, double kz,
+                   double kperp, cplx x, bool kn) {
+  for (int l = 0; l < 3; ++l)
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) {
+        low[l][i][k] = cplx(0.0, 0.0);
+        if (l == 0) mag[i][k] = 0.0;
+      }
+  if (sp.bM_betas == 0.0) {
+    calc_chi_cold(chi, sp, kz, kperp, x);
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) mag[i][k] = std::abs(chi[i][k]);
+    return;
+  }
+  BMParams b = bm_params(sp);
+  const double ell = b.ell;
+  int nmaxrun = nhds_nmaxrun(sp, kperp);
+  cplx Y[3][3] = {}, Y0[3][3] = {}, Y1[3][3] = {}, Yn1[3][3] = {};
+  for (int n = -nmaxrun; n <= nmaxrun; ++n) {
+    cplx Yn[3][3];
+    calc_ypsilon(Yn, sp, n, kz, kperp, x, kn);
+    for (int i = 0; i < 3; ++i)
+      for (int k = 0; k < 3; ++k) {
+        Y[i][k] = Y[i][k] + Yn[i][k];
+        if (n == 0) Y0[i][k] = Yn[i][k];
+        if (n == 1) Y1[i][k] = Y1[i][k] + Yn[i][k];
+        if (n == -1) Yn1[i][k] = Yn1[i][k] + Yn[i][k];
+        mag[i][k] += std::abs(Yn[i][k]) / (ell * ell);
+      }
+  }
+  cplx drift = kn ? 2.0 * x * b.vdrift / (ell * ell * kz * b.vtherm * b.vtherm * b.alpha)
+                  : kperp * kperp * 2.0 * x * b.vdrift / (ell * ell * kz * b.vtherm * b.vtherm * b.alpha);
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) {
+      chi[i][k] = Y[i][k] / (ell * ell);
+      low[1][i][k] = Y0[i][k] / (ell * ell);
+      low[2][i][k] = Y1[i][k] / (ell * ell);
+      low[0][i][k] = Yn1[i][k] / (ell * ell);
+    }
+  chi[2][2] = drift + Y[2][2] / (ell * ell);
+  low[1][2][2] = Y0[2][2] / (ell * ell) + drift;
+  mag[2][2] += std::abs(drift);
+}
+
 // ---------------------------------------------------------------------------
 // Rank decomposition: determine_nmax bump + split_processes
 // (src/ALPS_fns.f90:4048-4071, 4079-4207).  With nproc == 0 every species is
@@ -1421,6 +1742,7 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
     const Rank& r = ranks[work[w].first];
     int nn = work[w].second;
     const Species& s = c->spec[r.sproc - 1];
+    if (s.sp.use_bM) return;  // the NHDS branch below covers every order
     Eval e{c, &s, kperp, kpar};
     bool fp, fm;
     determine_resonances(e, om, nn, fp, fm);
@@ -1461,6 +1783,24 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
     const Species& s = c->spec[sproc - 1];
     Eval e{c, &s, kperp, kpar};
     std::vector<cplx> schi(nspec * 9, cplx(0, 0)), slow(nspec * 27, cplx(0, 0));
+    if (s.sp.use_bM) {
+      // calc_chi for the rank that holds n = 0 (:338-360); the other ranks of
+      // the species integrate an all-zero table and add exact zeros
+      wi += (size_t)(r.nlim2 - r.nlim1 + 1);
+      if (r.nlim2 >= 0 && r.nlim1 == 0) {
+        cplx ch[3][3], lo[3][3][3];
+        double mg[3][3];
+        calc_chi_nhds(ch, lo, mg, s.sp, kpar, kperp, om, c->sys.kperp_norm != 0);
+        double nq = s.sp.ns * s.sp.qs;
+        const int ij[6][2] = {{1, 1}, {2, 2}, {3, 3}, {1, 2}, {1, 3}, {2, 3}};
+        for (int q = 0; q < 6; ++q) {
+          int i = ij[q][0], j = ij[q][1];
+          CH(schi, sproc, i, j) = ch[i - 1][j - 1] / nq;
+          for (int n = -1; n <= 1; ++n) CL(slow, sproc, i, j, n) = lo[n + 1][i - 1][j - 1] / nq;
+          mag[(sproc - 1) * 9 + 3 * (i - 1) + (j - 1)] += mg[i - 1][j - 1];
+        }
+      }
+    } else
     for (int nn = r.nlim1; nn <= r.nlim2; ++nn, ++wi) {
       const NRes& o = res[wi];
       if (nn == 0) {
@@ -1486,7 +1826,9 @@ cplx disp(const oracle_ctx* c, cplx om, cplx* chi0_out, cplx* chi0_low_out, cplx
         }
       }
     }
-    if (r.nlim1 == 0 && s.sp.relat) {
+    if (s.sp.use_bM) {
+      // no ee term in the NHDS branch
+    } else if (r.nlim1 == 0 && s.sp.relat) {
       cplx ee = int_ee_rel(e);
       CH(schi, sproc, 3, 3) = CH(schi, sproc, 3, 3) + (c->sys.kperp_norm ? ee : kperp * kperp * ee);
     } else if (r.nlim1 == 0) {
@@ -1590,7 +1932,9 @@ cplx disp_c(const oracle_ctx* c, cplx om) { return disp(c, om, nullptr, nullptr,
 void derivative_f0(Species& s) {
   int N = s.nperp, M = s.npar;
   // parallel current moment (:157-190), summed in the reference's order
-  {
+  if (s.sp.use_bM) {
+    s.current_int = s.sp.ns * s.sp.qs * s.sp.bM_pdrifts / s.sp.ms;
+  } else {
     double dpperp = s.P1(2, 2) - s.P1(1, 2);
     double dppar = std::fabs(s.P2(2, 2) - s.P2(2, 1));
     double ci = 0.0;
@@ -1602,6 +1946,7 @@ void derivative_f0(Species& s) {
   }
   s.df1.assign((N + 1) * (M + 1), 0.0);
   s.df2.assign((N + 1) * (M + 1), 0.0);
+  if (s.sp.use_bM) return;  // no derivatives for NHDS species (:98-100)
   for (int i = 1; i <= N - 1; ++i)
     for (int j = 1; j <= M - 1; ++j) {
       s.df1[s.idx(i, j)] = (s.f0[s.idx(i + 1, j)] - s.f0[s.idx(i - 1, j)]) /
@@ -1764,6 +2109,10 @@ int LM_nonlinear_fit(const oracle_ctx* c, const Species& s, const std::vector<do
 
 // determine_param_fit (src/ALPS_analyt.f90:365-728), ACmethod = 1, non-rel.
 int determine_param_fit(const oracle_ctx* c, Species& s) {
+  if (s.sp.use_bM) {  // no fit (src/ALPS_analyt.f90:447-451)
+    std::fill(s.param_fit.begin(), s.param_fit.end(), 0.0);
+    return ALPS_OK;
+  }
   if (s.sp.ac_method != 1) return ALPS_OK;
   int n_params = n_params_of(s);
   std::vector<double> params(n_params);
@@ -1979,6 +2328,12 @@ extern "C" {
 void oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
 
 double oracle_bessj(int n, double x) { return bessj(n, x); }
+double oracle_bessi_scaled(int n, double x) { return besselI_s(n, x); }
+int oracle_wofz(double x, double y, double* u, double* v) {
+  bool flag = false;
+  wofz(x, y, *u, *v, flag);
+  return flag ? 1 : 0;
+}
 
 int oracle_create(const alps_system* sys, oracle_ctx** out) {
   if (!sys || !out || sys->nspec < 1 || sys->nperp < 4 || sys->npar < 6) return ALPS_E_INVALID;
@@ -1996,9 +2351,12 @@ void oracle_destroy(oracle_ctx* c) { delete c; }
 int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const double* pperp,
                        const double* ppar, const double* f0) {
   if (!c || is < 0 || is >= c->sys.nspec || !sp) return ALPS_E_INVALID;
-  if (sp->use_bM) return ALPS_E_UNSUPPORTED;
-  if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
-  if (sp->ac_method == 1) {
+  // NHDS species: no table; the cold branch needs kperp_norm (:445-452)
+  if (sp->use_bM && sp->bM_betas == 0.0 && !c->sys.kperp_norm) return ALPS_E_INVALID;
+  if (!sp->use_bM && (!pperp || !ppar || !f0)) return ALPS_E_INVALID;
+  if (sp->use_bM && sp->relat) return ALPS_E_UNSUPPORTED;
+  if (sp->ac_method == 2 && !sp->use_bM) return ALPS_E_UNSUPPORTED;
+  if (sp->ac_method == 1 && !sp->use_bM) {
     if (sp->n_fits < 1 || sp->n_fits > ALPS_MAX_FITS) return ALPS_E_INVALID;
     for (int f = 0; f < sp->n_fits; ++f) {
       int t = sp->fit_type[f];
@@ -2011,9 +2369,15 @@ int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const doub
   s.nperp = c->sys.nperp;
   s.npar = c->sys.npar;
   size_t n = (size_t)(s.nperp + 1) * (s.npar + 1);
-  s.pp1.assign(pperp, pperp + n);
-  s.pp2.assign(ppar, ppar + n);
-  s.f0.assign(f0, f0 + n);
+  if (sp->use_bM) {  // read_f0 skips the table and zeroes pp and f0 (src/ALPS_io.f90:672-675)
+    s.pp1.assign(n, 0.0);
+    s.pp2.assign(n, 0.0);
+    s.f0.assign(n, 0.0);
+  } else {
+    s.pp1.assign(pperp, pperp + n);
+    s.pp2.assign(ppar, ppar + n);
+    s.f0.assign(f0, f0 + n);
+  }
   int nf = std::max(1, sp->n_fits);
   s.sp.n_fits = (sp->ac_method == 1) ? sp->n_fits : 1;
   s.ng = c->sys.ngamma;
@@ -2083,6 +2447,10 @@ int oracle_set_k(oracle_ctx* c, double kperp, double kpar) {
   c->kperp = kperp;
   c->kpar = kpar;
   for (auto& s : c->spec) {
+    if (s.sp.use_bM) {  // determine_nmax (:4012-4014)
+      s.nmax = 1;
+      continue;
+    }
     int nn = 0;
     double besselmax = 10.0;
     while (besselmax > c->sys.Bessel_zero) {

@@ -76,6 +76,10 @@ int oracle_calc_eigen(oracle_ctx* ctx, alps_complex om, int eigen, int heat,
                       alps_eigen* out);
 
 double oracle_bessj(int n, double x);
+/* exp(-x) I_n(x) and the Faddeeva function of the NHDS branch
+ * (src/ALPS_NHDS.f90:537-862); oracle_wofz returns its overflow flag. */
+double oracle_bessi_scaled(int n, double x);
+int oracle_wofz(double x, double y, double* u, double* v);
 /* Threads used inside one disp() call (orders in parallel, summed in the
  * reference's order).  Default 1. */
 void oracle_set_threads(int n);

@@ -69,6 +69,9 @@ def lib():
             L.oracle_set_threads.restype = None
             L.oracle_bessj.argtypes = [C.c_int, C.c_double]
             L.oracle_bessj.restype = C.c_double
+            L.oracle_bessi_scaled.argtypes = [C.c_int, C.c_double]
+            L.oracle_bessi_scaled.restype = C.c_double
+            L.oracle_wofz.argtypes = [C.c_double, C.c_double, P(C.c_double), P(C.c_double)]
             L.oracle_generate_f0.argtypes = [P(_abi.alps_dist_params), C.c_int, C.c_int, dp, dp, dp, dp]
             _lib = L
     return _lib
@@ -91,6 +94,18 @@ def _dptr(a):
 
 def _cptr(a):
     return a.ctypes.data_as(C.POINTER(alps_complex))
+
+
+def bessi_scaled(n, x):
+    """exp(-x) I_n(x) of the NHDS branch."""
+    return lib().oracle_bessi_scaled(int(n), float(x))
+
+
+def wofz(z):
+    """Faddeeva function w(z) of the NHDS branch (algorithm 680)."""
+    u, v = C.c_double(), C.c_double()
+    lib().oracle_wofz(z.real, z.imag, C.byref(u), C.byref(v))
+    return complex(u.value, v.value)
 
 
 def set_threads(n):
@@ -125,9 +140,13 @@ class OraclePlasma:
         _chk(L.oracle_create(C.byref(system), C.byref(self._h)), "oracle_create")
         self._keep = []
         for i, (sp, pperp, ppar, f0) in enumerate(species):
-            a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pperp, ppar, f0)]
-            self._keep.append(a)
-            _chk(L.oracle_set_species(self._h, i, C.byref(sp), *[_dptr(x) for x in a]), "oracle_set_species")
+            if pperp is None:  # NHDS species: no table
+                ptrs = [None, None, None]
+            else:
+                a = [np.ascontiguousarray(x, dtype=np.float64) for x in (pperp, ppar, f0)]
+                self._keep.append(a)
+                ptrs = [_dptr(x) for x in a]
+            _chk(L.oracle_set_species(self._h, i, C.byref(sp), *ptrs), "oracle_set_species")
         self.species = [s[0] for s in species]
         if prepare:
             _chk(L.oracle_prepare(self._h), "oracle_prepare")
