@@ -69,7 +69,7 @@ def _bm(**kw):
 def test_bimaxwellian_species(api, kperp_norm):
     """Drifting anisotropic protons and electrons in closed form, both
     kperp normalisations, frequencies above, on and below the real axis."""
-    sysd = _abi.system_defaults(nspec=2, nperp=8, npar=16, kperp=0.4, kpar=0.25, vA=1e-4, kperp_norm=kperp_norm)
+    sysd = _abi.system_defaults(nspec=2, nperp=8, npar=24, kperp=0.4, kpar=0.25, vA=1e-4, kperp_norm=kperp_norm)
     sp = [(_bm(bM_betas=0.8, bM_alphas=2.0, bM_pdrifts=0.2), None, None, None),
           (_bm(qs=-1, ms=1 / 1836.0, bM_betas=1.2, bM_alphas=0.7), None, None, None)]
     O, G = _pair(api, sysd, sp)
@@ -79,7 +79,7 @@ def test_bimaxwellian_species(api, kperp_norm):
 
 
 def test_cold_species(api):
-    sysd = _abi.system_defaults(nspec=2, nperp=8, npar=16, kperp=0.3, kpar=0.2, vA=1e-4)
+    sysd = _abi.system_defaults(nspec=2, nperp=8, npar=24, kperp=0.3, kpar=0.2, vA=1e-4)
     sp = [(_bm(bM_betas=0.0, bM_pdrifts=0.1), None, None, None),
           (_bm(qs=-1, ms=1 / 1836.0, bM_betas=0.0), None, None, None)]
     O, G = _pair(api, sysd, sp)
