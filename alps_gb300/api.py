@@ -124,6 +124,8 @@ class Plasma:
 
     def fit_size(self, i):
         sp = self.species[i]
+        if sp.ac_method == 2 and not sp.use_bM:
+            return (self.sys.nperp + 1) * (sp.poly_order + 1)
         nf = sp.n_fits if sp.ac_method == 1 else 1
         rows = max(self.sys.nperp, self.sys.ngamma) if sp.relat else self.sys.nperp
         return (rows + 1) * 5 * nf

@@ -168,6 +168,14 @@ static int fit_rows(const alps_ctx* c, int is) {
   return r + 1;
 }
 
+// doubles in the continuation table: rows x 5 x n_fits fit parameters, or
+// (nperp+1) x (poly_order+1) Chebyshev coefficients for ACmethod 2
+static size_t fit_size(const alps_ctx* c, int is) {
+  const alps_species& sp = c->spec[is].sp;
+  if (sp.ac_method == 2 && !sp.use_bM) return (size_t)(c->sys.nperp + 1) * (sp.poly_order + 1);
+  return (size_t)fit_rows(c, is) * 5 * sp.n_fits;
+}
+
 // A bi-Maxwellian or cold species evaluated in closed form (use_bM = T): no
 // f0 table, no derivatives or fits (read_f0 and determine_param_fit skip
 // it, src/ALPS_io.f90:672-675, src/ALPS_analyt.f90:447-451).
@@ -204,8 +212,11 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   if (!c || !sp || is < 0 || is >= c->sys.nspec) return ALPS_E_INVALID;
   if (sp->use_bM) return set_species_bm(c, is, sp);
   if (!pperp || !ppar || !f0) return ALPS_E_INVALID;
-  if (sp->ac_method == 2) return ALPS_E_UNSUPPORTED;
-  if (sp->ac_method != 0 && sp->ac_method != 1) return ALPS_E_INVALID;
+  if (sp->ac_method != 0 && sp->ac_method != 1 && sp->ac_method != 2) return ALPS_E_INVALID;
+  if (sp->ac_method == 2) {  // Chebyshev continuation: kind 1 only (alps_error(10) otherwise)
+    if (sp->poly_kind != 1) return ALPS_E_POLY_KIND;
+    if (sp->poly_order < 1 || sp->poly_order > 255 || sp->relat) return ALPS_E_INVALID;
+  }
   // relativistic species: continuation on the (Gamma, pparbar) rows, fit
   // types 4 and 5 (the types whose pperp argument is Gamma)
   if (sp->relat && sp->ac_method != 1) return ALPS_E_UNSUPPORTED;
@@ -245,12 +256,13 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   if (!S.d_ppar) ALPS_CUDA_TRY(cudaMalloc(&S.d_ppar, (M + 1) * sizeof(double)));
   if (!S.d_f0) ALPS_CUDA_TRY(cudaMalloc(&S.d_f0, nn * sizeof(double)));
   int nf = S.sp.n_fits;
-  int rows = fit_rows(c, is);
   if (S.d_fit) cudaFree(S.d_fit);
-  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)rows * 5 * nf * sizeof(double)));
-  std::vector<double> fit((size_t)rows * 5 * nf, 0.0);
-  for (int ip = 0; ip < 5; ++ip)
-    for (int f = 0; f < nf; ++f) fit[(0 * 5 + ip) * nf + f] = sp->fit_init[f][ip];
+  S.d_fit = nullptr;
+  std::vector<double> fit(fit_size(c, is), 0.0);
+  ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, fit.size() * sizeof(double)));
+  if (sp->ac_method == 1)
+    for (int ip = 0; ip < 5; ++ip)
+      for (int f = 0; f < nf; ++f) fit[(0 * 5 + ip) * nf + f] = sp->fit_init[f][ip];
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_pperp, pv.data(), (N + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_ppar, qv.data(), (M + 1) * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_f0, S.f0.data(), nn * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -288,7 +300,7 @@ int alps_prepare(alps_ctx* c) {
 int alps_get_fit(alps_ctx* c, int is, double* out) {
   if (!c || !out || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
   const SpeciesHost& S = c->spec[is];
-  size_t n = (size_t)fit_rows(c, is) * 5 * S.sp.n_fits;
+  size_t n = fit_size(c, is);
   ALPS_CUDA_TRY(cudaMemcpyAsync(out, S.d_fit, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   return ALPS_OK;
@@ -297,7 +309,7 @@ int alps_get_fit(alps_ctx* c, int is, double* out) {
 int alps_set_fit(alps_ctx* c, int is, const double* in) {
   if (!c || !in || is < 0 || is >= c->sys.nspec || !c->spec[is].loaded) return ALPS_E_INVALID;
   SpeciesHost& S = c->spec[is];
-  size_t n = (size_t)fit_rows(c, is) * 5 * S.sp.n_fits;
+  size_t n = fit_size(c, is);
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
   int st = launch_fit_aux(c, is);
   if (st) return st;

@@ -95,6 +95,9 @@ struct SpecDev {
   const double* jrel;   // [(n)*(ng+1)*(np+1)], n = 0..nmax+1: J_n at each node
   const int2* cone;     // [ng+1] first and last pparbar index inside the cone
   double int_ee_rel;
+  // Chebyshev continuation (ACmethod 2): order, log10 cut, p_par end points
+  int poly_order;
+  double poly_log_max, ppar_lo, ppar_hi;
   // bi-Maxwellian / cold species through the NHDS closed form (use_bM)
   int bm;
   int bm_nrun;          // Bessel orders -bm_nrun..bm_nrun
@@ -196,6 +199,7 @@ struct alps_ctx {
 // kernels / launchers (setup_kernels.cu, disp_kernels.cu)
 // ---------------------------------------------------------------------------
 int launch_prepare_species(alps_ctx* c, int is);
+int launch_glls(alps_ctx* c, int is);
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
 int launch_fit_aux(alps_ctx* c, int is);

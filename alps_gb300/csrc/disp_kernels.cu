@@ -229,7 +229,33 @@ __global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __
 // Analytic continuation f(pperp_i, complex ppar) (eval_fit,
 // src/ALPS_analyt.f90:32-181; fit_function :185-266).
 // ---------------------------------------------------------------------------
+// fit_function_poly (src/ALPS_analyt.f90:268-363): Chebyshev series in
+// t = (p - centre)/half-width, zero for |t| > 1; with log_fit the series is
+// log10 f, cut to zero beyond +-poly_log_max
+__device__ double2 eval_fit_poly(const SpecDev& S, int iperp, double2 p) {
+  const int np = S.poly_order;
+  const double* c = S.fit + (size_t)iperp * (np + 1);
+  const double n1 = 5.0e-1 * (S.ppar_hi + S.ppar_lo), n2 = 5.0e-1 * (S.ppar_hi - S.ppar_lo);
+  double2 t = cmk((p.x - n1) / n2, p.y / n2);
+  if (cabs_(t) > 1.0) return cmk(0.0, 0.0);
+  double2 b0 = cmk(1.0, 0.0), b1 = t;
+  double2 f = cadd(cscale(b0, c[0]), cscale(b1, c[1]));
+  for (int n = 2; n <= np; ++n) {
+    double2 b2 = csub(cmul(cscale(t, 2.0), b1), b0);
+    f = cadd(f, cscale(b2, c[n]));
+    b0 = b1;
+    b1 = b2;
+  }
+  if (S.log_fit) {
+    const double L = S.poly_log_max;
+    if ((f.x < -L) || (f.y < -L) || (f.x > L) || (f.y > L)) return cmk(0.0, 0.0);
+    f = cexp_d(cscale(f, 2.302585092994045684));  // 10^f = exp(f ln 10)
+  }
+  return f;
+}
+
 __device__ double2 eval_fit_d(const SpecDev& S, double vA, int iperp, double2 p) {
+  if (S.ac_method == 2) return eval_fit_poly(S, iperp, p);
   double pperp = S.pperp[iperp];
   if (S.ac_method == 0) {
     // distribution_analyt (distribution/distribution_analyt.f90:59-79)
@@ -821,6 +847,10 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->jrel = S.d_jrel;
   o->cone = S.d_cone;
   o->int_ee_rel = S.int_ee_rel;
+  o->poly_order = S.sp.poly_order;
+  o->poly_log_max = S.sp.poly_log_max;
+  o->ppar_lo = bm ? 0.0 : S.ppar[0];
+  o->ppar_hi = bm ? 0.0 : S.ppar[c->sys.npar];
   o->bm = bm ? 1 : 0;
   o->bm_nrun = S.bm_nrun;
   o->bm_beta = S.sp.bM_betas;

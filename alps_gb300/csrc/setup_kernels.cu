@@ -596,6 +596,120 @@ int ensure(T*& ptr, size_t& cap, size_t n) {
   return ALPS_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Chebyshev continuation (ACmethod 2): set_polynomial_basis + determine_GLLS
+// + least_squares_fit (src/ALPS_analyt.f90:731-889).  The basis on the
+// uniform p_par nodes, and so the normal matrix A^T A, is the same on every
+// p_perp row: it is built and LU-factored once (partial pivoting, dgetrf);
+// each row then only forms A^T b and back-substitutes.  Sums run over p_par
+// in ascending order without contraction.
+// ---------------------------------------------------------------------------
+__global__ void k_glls_basis(int M, int np, double* A /* [(M+1)][(np+1)] */) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > M) return;
+  double yy = __dadd_rn(-1.0, __dmul_rn((double)j, 2.0 / M));
+  double* a = A + (size_t)j * (np + 1);
+  a[0] = 1.0;
+  if (np >= 1) a[1] = yy;
+  for (int n = 2; n <= np; ++n) a[n] = __dsub_rn(__dmul_rn(__dmul_rn(2.0, yy), a[n - 1]), a[n - 2]);
+}
+
+// alpha = A^T A (column-major m x m), then its LU in place; one block
+__global__ void k_glls_normal(const double* __restrict__ A, int M, int np, double* alpha, int* piv, int* status) {
+  const int m = np + 1;
+  for (int t = threadIdx.x; t < m * m; t += blockDim.x) {
+    int k = t % m, l = t / m;
+    double acc = 0.0;
+    for (int j = 0; j <= M; ++j) acc = __dadd_rn(acc, __dmul_rn(A[(size_t)j * m + k], A[(size_t)j * m + l]));
+    alpha[t] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < m; ++k) {
+    int p = k;
+    double mx = fabs(alpha[k + m * k]);
+    for (int i = k + 1; i < m; ++i)
+      if (fabs(alpha[i + m * k]) > mx) {
+        mx = fabs(alpha[i + m * k]);
+        p = i;
+      }
+    piv[k] = p;
+    if (alpha[p + m * k] == 0.0) {
+      *status = ALPS_E_SINGULAR;
+      return;
+    }
+    if (p != k)
+      for (int j = 0; j < m; ++j) {
+        double tmp = alpha[k + m * j];
+        alpha[k + m * j] = alpha[p + m * j];
+        alpha[p + m * j] = tmp;
+      }
+    double dk = alpha[k + m * k];
+    for (int i = k + 1; i < m; ++i) alpha[i + m * k] = __ddiv_rn(alpha[i + m * k], dk);
+    for (int j = k + 1; j < m; ++j) {
+      double f = alpha[k + m * j];
+      if (f == 0.0) continue;
+      for (int i = k + 1; i < m; ++i) alpha[i + m * j] = __dsub_rn(alpha[i + m * j], __dmul_rn(alpha[i + m * k], f));
+    }
+  }
+}
+
+// one block per p_perp row: b = log10 f0 (zeros replaced by 0.01 x the
+// smallest positive value of the row) or f0, w = A^T b, LU solve
+__global__ void k_glls_rows(const double* __restrict__ f0, const double* __restrict__ A,
+                            const double* __restrict__ alpha, const int* __restrict__ piv, int M, int np, int log_fit,
+                            const int* status, double* coeffs) {
+  extern __shared__ double sm[];
+  double* b = sm;            // [M+1]
+  double* w = sm + (M + 1);  // [np+1]
+  __shared__ double smin[128], spos[128];
+  if (*status) return;
+  const int i = blockIdx.x, m = np + 1;
+  const double* row = f0 + (size_t)i * (M + 1);
+  for (int j = threadIdx.x; j <= M; j += blockDim.x) b[j] = row[j];
+  __syncthreads();
+  if (log_fit) {
+    double mn = 1.0e308, mp = 1.0e308;
+    for (int j = threadIdx.x; j <= M; j += blockDim.x) {
+      mn = fmin(mn, b[j]);
+      if (b[j] > 0.0) mp = fmin(mp, b[j]);
+    }
+    smin[threadIdx.x] = mn;
+    spos[threadIdx.x] = mp;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) {
+        smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + s]);
+        spos[threadIdx.x] = fmin(spos[threadIdx.x], spos[threadIdx.x + s]);
+      }
+      __syncthreads();
+    }
+    const bool fix = !(smin[0] > 0.0);
+    const double repl = 0.01 * (spos[0] < 1.0e308 ? spos[0] : 1.0e-40);
+    for (int j = threadIdx.x; j <= M; j += blockDim.x) b[j] = log10((fix && b[j] == 0.0) ? repl : b[j]);
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    double acc = 0.0;
+    for (int j = 0; j <= M; ++j) acc = __dadd_rn(acc, __dmul_rn(A[(size_t)j * m + k], b[j]));
+    w[k] = acc;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int k = 0; k < m; ++k) {
+    double t = w[k];
+    w[k] = w[piv[k]];
+    w[piv[k]] = t;
+  }
+  for (int j = 0; j < m; ++j)
+    for (int r = j + 1; r < m; ++r) w[r] = __dsub_rn(w[r], __dmul_rn(alpha[r + m * j], w[j]));
+  for (int j = m - 1; j >= 0; --j) {
+    w[j] = __ddiv_rn(w[j], alpha[j + m * j]);
+    for (int r = 0; r < j; ++r) w[r] = __dsub_rn(w[r], __dmul_rn(alpha[r + m * j], w[j]));
+  }
+  for (int k = 0; k < m; ++k) coeffs[(size_t)i * m + k] = w[k];
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -624,6 +738,8 @@ int launch_prepare_species(alps_ctx* c, int is) {
   // relativistic species: (Gamma, pparbar) grid, f0_rel and its derivatives
   int st_fit = ALPS_OK;
   if (S.sp.relat) st_fit = launch_rel_prepare(c, is);
+  // Chebyshev continuation (ACmethod 2)
+  if (S.sp.ac_method == 2 && st_fit == ALPS_OK) st_fit = launch_glls(c, is);
   // LM fit of the analytic continuation (ACmethod 1)
   if (S.sp.ac_method == 1 && st_fit == ALPS_OK) {
     FitArgs a;
@@ -666,6 +782,33 @@ int launch_prepare_species(alps_ctx* c, int is) {
   cudaFree(d_ee);
   S.int_ee = ee;
   return st_fit;
+}
+
+int launch_glls(alps_ctx* c, int is) {
+  SpeciesHost& S = c->spec[is];
+  const int N = c->sys.nperp, M = c->sys.npar, np = S.sp.poly_order, m = np + 1;
+  cudaStream_t st = c->stream;
+  double *d_A = nullptr, *d_alpha = nullptr;
+  int *d_piv = nullptr, *d_status = nullptr;
+  ALPS_CUDA_TRY(cudaMalloc(&d_A, (size_t)(M + 1) * m * sizeof(double)));
+  ALPS_CUDA_TRY(cudaMalloc(&d_alpha, (size_t)m * m * sizeof(double)));
+  ALPS_CUDA_TRY(cudaMalloc(&d_piv, m * sizeof(int)));
+  ALPS_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
+  ALPS_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), st));
+  k_glls_basis<<<(M + 1 + 127) / 128, 128, 0, st>>>(M, np, d_A);
+  k_glls_normal<<<1, 256, 0, st>>>(d_A, M, np, d_alpha, d_piv, d_status);
+  size_t smem = (size_t)(M + 1 + m) * sizeof(double);
+  if (smem > 48 * 1024) ALPS_CUDA_TRY(cudaFuncSetAttribute(k_glls_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  k_glls_rows<<<N + 1, 128, smem, st>>>(S.d_f0, d_A, d_alpha, d_piv, M, np, S.sp.log_fit, d_status, S.d_fit);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  int status = 0;
+  ALPS_CUDA_TRY(cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  ALPS_CUDA_TRY(cudaStreamSynchronize(st));
+  cudaFree(d_A);
+  cudaFree(d_alpha);
+  cudaFree(d_piv);
+  cudaFree(d_status);
+  return status;
 }
 
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out) {

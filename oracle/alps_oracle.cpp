@@ -434,9 +434,37 @@ cplx distribution_analyt(int is1, double pperp, cplx ppar) {
 }
 
 // eval_fit (src/ALPS_analyt.f90:32-181)
+// fit_function_poly (src/ALPS_analyt.f90:268-363): Chebyshev series on
+// [pp(npar), pp(0)] mapped to [-1,1], zero outside; with log_fit the series
+// is log10 f and is cut to zero beyond +-poly_log_max
+cplx fit_function_poly(const Species& s, int iperp, cplx p) {
+  const int n_poly = s.sp.poly_order;
+  const double* c = &s.param_fit[(size_t)iperp * (n_poly + 1)];
+  double norm_1 = 5.0e-1 * (s.P2(iperp, s.npar) + s.P2(iperp, 0));
+  double norm_2 = 5.0e-1 * (s.P2(iperp, s.npar) - s.P2(iperp, 0));
+  cplx t = (p - norm_1) / norm_2;
+  if (std::abs(t) > 1.0) return cplx(0.0, 0.0);
+  cplx f(0.0, 0.0), b0(1.0, 0.0), b1 = t;
+  f = f + c[0] * b0;
+  f = f + c[1] * b1;
+  for (int n = 2; n <= n_poly; ++n) {
+    cplx b2 = cplx(2.0, 0.0) * t * b1 - b0;
+    f = f + c[n] * b2;
+    b0 = b1;
+    b1 = b2;
+  }
+  if (s.sp.log_fit) {
+    double L = s.sp.poly_log_max;
+    if ((f.real() < -L) || (f.imag() < -L) || (f.real() > L) || (f.imag() > L)) return cplx(0.0, 0.0);
+    f = std::pow(cplx(10.0, 0.0), f);
+  }
+  return f;
+}
+
 cplx eval_fit(const Eval& e, int is1, int iperp, cplx ppar_valC) {
   const Species& s = *e.s;
   if (s.sp.ac_method == 0) return distribution_analyt(is1, s.P1(iperp, 1), ppar_valC);
+  if (s.sp.ac_method == 2) return fit_function_poly(s, iperp, ppar_valC);
   double params[5 * ALPS_MAX_FITS];
   gather_params(s, iperp, params);
   // pperp_val: pp(is,iperp,1,1), or gamma_rel(.,iperp,1) for the (Gamma,
@@ -2108,11 +2136,91 @@ int LM_nonlinear_fit(const oracle_ctx* c, const Species& s, const std::vector<do
 }
 
 // determine_param_fit (src/ALPS_analyt.f90:365-728), ACmethod = 1, non-rel.
+// set_polynomial_basis + determine_GLLS + least_squares_fit
+// (src/ALPS_analyt.f90:731-889): per p_perp row the normal equations
+// (A^T A) c = A^T b of a Chebyshev basis on the uniform p_par nodes, b =
+// log10 f0 (zeros replaced by 0.01 x the smallest positive value) or f0,
+// solved by LU with partial pivoting (dgesv).  The BLAS sums (dgemm, dgemv)
+// run over p_par in ascending order.
+int determine_glls(Species& s) {
+  const int M = s.npar, np = s.sp.poly_order;
+  if (s.sp.poly_kind != 1) return ALPS_E_POLY_KIND;
+  std::vector<double> A((size_t)(M + 1) * (np + 1));  // A[j*(np+1) + n]
+  for (int j = 0; j <= M; ++j) {
+    double yy = -1.0 + j * (2.0 / M);
+    double* a = &A[(size_t)j * (np + 1)];
+    a[0] = 1.0;
+    if (np >= 1) a[1] = yy;
+    for (int n = 2; n <= np; ++n) a[n] = 2.0 * yy * a[n - 1] - a[n - 2];
+  }
+  const int m = np + 1;
+  std::vector<double> alpha((size_t)m * m);  // column-major
+  for (int k = 0; k < m; ++k)
+    for (int l = 0; l < m; ++l) {
+      double acc = 0.0;
+      for (int j = 0; j <= M; ++j) acc = acc + A[(size_t)j * m + k] * A[(size_t)j * m + l];
+      alpha[(size_t)k + (size_t)m * l] = acc;
+    }
+  // dgetrf once: the basis, and so A^T A, is the same on every row
+  std::vector<int> piv(m);
+  for (int k = 0; k < m; ++k) {
+    int p = k;
+    double mx = std::fabs(alpha[(size_t)k + (size_t)m * k]);
+    for (int i = k + 1; i < m; ++i)
+      if (std::fabs(alpha[(size_t)i + (size_t)m * k]) > mx) { mx = std::fabs(alpha[(size_t)i + (size_t)m * k]); p = i; }
+    piv[k] = p;
+    if (alpha[(size_t)p + (size_t)m * k] == 0.0) return ALPS_E_SINGULAR;
+    if (p != k)
+      for (int j = 0; j < m; ++j) std::swap(alpha[(size_t)k + (size_t)m * j], alpha[(size_t)p + (size_t)m * j]);
+    double dk = alpha[(size_t)k + (size_t)m * k];
+    for (int i = k + 1; i < m; ++i) alpha[(size_t)i + (size_t)m * k] /= dk;
+    for (int j = k + 1; j < m; ++j) {
+      double f = alpha[(size_t)k + (size_t)m * j];
+      if (f == 0.0) continue;
+      for (int i = k + 1; i < m; ++i) alpha[(size_t)i + (size_t)m * j] -= alpha[(size_t)i + (size_t)m * k] * f;
+    }
+  }
+  s.param_fit.assign((size_t)(s.nperp + 1) * m, 0.0);
+  std::vector<double> b(M + 1), w(m);
+  for (int i = 0; i <= s.nperp; ++i) {
+    for (int j = 0; j <= M; ++j) b[j] = s.f0[s.idx(i, j)];
+    if (s.sp.log_fit) {
+      double mn = b[0];
+      for (int j = 1; j <= M; ++j) mn = std::min(mn, b[j]);
+      if (!(mn > 0.0)) {
+        double mp = 0.0;
+        bool any = false;
+        for (int j = 0; j <= M; ++j)
+          if (b[j] > 0.0 && (!any || b[j] < mp)) { mp = b[j]; any = true; }
+        if (!any) mp = 1.0e-40;
+        for (int j = 0; j <= M; ++j)
+          if (b[j] == 0.0) b[j] = 0.01 * mp;
+      }
+      for (int j = 0; j <= M; ++j) b[j] = std::log10(b[j]);
+    }
+    for (int k = 0; k < m; ++k) {
+      double acc = 0.0;
+      for (int j = 0; j <= M; ++j) acc = acc + A[(size_t)j * m + k] * b[j];
+      w[k] = acc;
+    }
+    for (int k = 0; k < m; ++k) std::swap(w[k], w[piv[k]]);
+    for (int j = 0; j < m; ++j)
+      for (int r = j + 1; r < m; ++r) w[r] -= alpha[(size_t)r + (size_t)m * j] * w[j];
+    for (int j = m - 1; j >= 0; --j) {
+      w[j] /= alpha[(size_t)j + (size_t)m * j];
+      for (int r = 0; r < j; ++r) w[r] -= alpha[(size_t)r + (size_t)m * j] * w[j];
+    }
+    for (int k = 0; k < m; ++k) s.param_fit[(size_t)i * m + k] = w[k];
+  }
+  return ALPS_OK;
+}
+
 int determine_param_fit(const oracle_ctx* c, Species& s) {
   if (s.sp.use_bM) {  // no fit (src/ALPS_analyt.f90:447-451)
     std::fill(s.param_fit.begin(), s.param_fit.end(), 0.0);
     return ALPS_OK;
   }
+  if (s.sp.ac_method == 2) return determine_glls(s);
   if (s.sp.ac_method != 1) return ALPS_OK;
   int n_params = n_params_of(s);
   std::vector<double> params(n_params);
@@ -2355,7 +2463,8 @@ int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const doub
   if (sp->use_bM && sp->bM_betas == 0.0 && !c->sys.kperp_norm) return ALPS_E_INVALID;
   if (!sp->use_bM && (!pperp || !ppar || !f0)) return ALPS_E_INVALID;
   if (sp->use_bM && sp->relat) return ALPS_E_UNSUPPORTED;
-  if (sp->ac_method == 2 && !sp->use_bM) return ALPS_E_UNSUPPORTED;
+  if (sp->ac_method == 2 && !sp->use_bM && (sp->poly_kind != 1 || sp->poly_order < 1 || sp->relat))
+    return sp->poly_kind != 1 ? ALPS_E_POLY_KIND : ALPS_E_INVALID;
   if (sp->ac_method == 1 && !sp->use_bM) {
     if (sp->n_fits < 1 || sp->n_fits > ALPS_MAX_FITS) return ALPS_E_INVALID;
     for (int f = 0; f < sp->n_fits; ++f) {
@@ -2383,7 +2492,10 @@ int oracle_set_species(oracle_ctx* c, int is, const alps_species* sp, const doub
   s.ng = c->sys.ngamma;
   s.np = c->sys.npparbar;
   int rows = sp->relat ? std::max(s.nperp, s.ng) : s.nperp;
-  s.param_fit.assign((size_t)(rows + 1) * 5 * nf, 0.0);
+  if (sp->ac_method == 2 && !sp->use_bM)  // Chebyshev coefficients per p_perp row
+    s.param_fit.assign((size_t)(s.nperp + 1) * (sp->poly_order + 1), 0.0);
+  else
+    s.param_fit.assign((size_t)(rows + 1) * 5 * nf, 0.0);
   for (int ip = 0; ip < 5; ++ip)
     for (int f = 0; f < s.sp.n_fits; ++f) s.PF(0, ip, f) = sp->fit_init[f][ip];
   s.loaded = true;

@@ -164,6 +164,8 @@ class OraclePlasma:
 
     def fit_size(self, i):
         sp = self.species[i]
+        if sp.ac_method == 2 and not sp.use_bM:
+            return (self.sys.nperp + 1) * (sp.poly_order + 1)
         rows = max(self.sys.nperp, self.sys.ngamma) if sp.relat else self.sys.nperp
         return (rows + 1) * 5 * (max(1, sp.n_fits) if sp.ac_method == 1 else 1)
 

@@ -1,8 +1,9 @@
-"""The oracle's NHDS branch (src/ALPS_NHDS.f90: bi-Maxwellian and cold
-species in closed form, use_bM = T).
+"""The oracle's closed-form and polynomial continuations: the NHDS branch
+(src/ALPS_NHDS.f90: bi-Maxwellian and cold species, use_bM = T) and the
+Chebyshev continuation (ACmethod 2, src/ALPS_analyt.f90:268-363, 731-889).
 
-The reference ships no golden output for it; the restatement is pinned
-instead by independent evaluations:
+The reference ships no golden output for either; the restatements are
+pinned instead by independent evaluations:
   * WOFZ against scipy's Faddeeva function.  The reference keeps several
     single-precision literals (6.3, 4.4, 0.85, 1.88 and 1.0/J in the power
     series), which limits it to ~3e-7 relative; held to 1e-6.
@@ -13,6 +14,8 @@ instead by independent evaluations:
     integration of the same distribution sampled on a 60x120 grid (second
     order in the grid spacing: measured 3e-3 to 1e-2); held to 2e-2.
   * the cold closed form against the bi-Maxwellian closed form at beta ->0.
+  * the Chebyshev continuation of a Maxwellian table against the Maxwellian
+    continuation (exact up to rounding when nothing is cut by poly_log_max).
 """
 import os
 
@@ -95,3 +98,46 @@ def test_cold_limit_of_bimaxwellian():
     assert diffs[1e-5].max() < 5e-6
     ratio = diffs[1e-4] / diffs[1e-5]
     assert np.all((ratio > 5) & (ratio < 20)), ratio
+
+
+def _cheb_pair(log_max, N=40, M=80):
+    d = workloads._dist(kind=1, ms=1.0, vA=1e-4, maxP=6.0)
+    pp, pl, f0, ideal = po.generate_f0(d, N, M)
+    sysd = _abi.system_defaults(nspec=1, nperp=N, npar=M, kperp=0.5, kpar=0.3, vA=1e-4, Bessel_zero=1e-30)
+    sp1 = _abi.species_defaults(ns=1, qs=1, ms=1, fits=[(1, list(ideal[:3]) + [0, 0], ideal[5])])
+    sp2 = _abi.species_defaults(ns=1, qs=1, ms=1, ac_method=2, poly_kind=1, poly_order=30, poly_log_max=log_max)
+    P1 = po.OraclePlasma(sysd, [(sp1, pp, pl, f0)])
+    P2 = po.OraclePlasma(sysd, [(sp2, pp, pl, f0)])
+    P1.set_k(0.5, 0.3)
+    P2.set_k(0.5, 0.3)
+    return P1, P2
+
+
+def test_chebyshev_continuation_reproduces_maxwellian():
+    """ACmethod 2 (Chebyshev GLLS fit of log10 f0 per p_perp row, the
+    reference's fit_function_poly) against the Maxwellian continuation of
+    the same table: log10 of a Maxwellian row is a parabola, which the
+    order-30 series represents exactly, so chi agrees to rounding when no
+    value falls below the log cut (poly_log_max 40 here)."""
+    P1, P2 = _cheb_pair(40.0)
+    coeffs = P2.get_fit(0).reshape(41, 31)
+    assert np.abs(coeffs[:, 3:]).max() < 1e-12
+    for om in [0.9 - 0.01j, 0.9 - 0.05j, 0.5 - 0.2j, 1.5 + 0j, 1.2 + 0.05j]:
+        a = P1.disp(om)[1][0]
+        b = P2.disp(om)[1][0]
+        assert (np.abs(a - b) / np.abs(a).max()).max() < 1e-10, om
+
+
+def test_chebyshev_log_cut_drops_landau_terms():
+    """With the reference's default cut (poly_log_max 18) the outer p_perp
+    rows fall below 10^-18 at the resonant momentum, the continuation is zero
+    there and landau_integrate returns zero for that order (the reference's
+    early return); above the real axis the Landau term is not used at all,
+    so both continuations give the same chi."""
+    P1, P2 = _cheb_pair(18.0)
+    a = P1.disp(1.2 + 0.05j)[1][0]
+    b = P2.disp(1.2 + 0.05j)[1][0]
+    assert np.array_equal(a, b)
+    a0 = P1.full_integrate(0, 0.9 - 0.01j, 0, 3)[0]
+    b0 = P2.full_integrate(0, 0.9 - 0.01j, 0, 3)[0]
+    assert abs(a0 - b0) > 1e-3 * abs(a0)
