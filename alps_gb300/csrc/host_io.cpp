@@ -232,6 +232,188 @@ bool file_exists(const std::string& p) {
 
 void ensure_dir(const std::string& p) { mkdir(p.c_str(), 0755); }
 
+
+
+// One step of a k scan (the select case of om_scan / om_double_scan):
+// sets the components the scan type moves, from the start point (kp0, kz0)
+// or, for types 1 and 2, from its angle th0 and magnitude k0.
+void scan_k(const alps_scan_def& sc, int it, double kp0, double kz0, double th0, double k0, double& kperp,
+            double& kpar) {
+  switch (sc.type_s) {
+    case 0:
+      if (sc.log_scan) {
+        kperp = std::pow(10.0, std::log10(kp0) + sc.diff * it);
+        kpar = std::pow(10.0, std::log10(kz0) + sc.diff2 * it);
+      } else {
+        kperp = kp0 + sc.diff * it;
+        kpar = kz0 + sc.diff2 * it;
+      }
+      break;
+    case 1: {
+      double th = sc.log_scan ? std::pow(10.0, std::log10(th0) + sc.diff * it) : th0 + sc.diff * it;
+      kperp = k0 * std::sin(th);
+      kpar = k0 * std::cos(th);
+      break;
+    }
+    case 2: {
+      double kt = sc.log_scan ? std::pow(10.0, std::log10(k0) + sc.diff * it) : (k0) + sc.diff * it;
+      kperp = kt * std::sin(th0);
+      kpar = kt * std::cos(th0);
+      break;
+    }
+    case 3:
+      kperp = sc.log_scan ? std::pow(10.0, std::log10(kp0) + sc.diff * it) : kp0 + sc.diff * it;
+      break;
+    case 4:
+      kpar = sc.log_scan ? std::pow(10.0, std::log10(kz0) + sc.diff * it) : kz0 + sc.diff * it;
+      break;
+  }
+}
+
+int append_line(const std::string& path, const std::vector<double>* row) {
+  FILE* f = std::fopen(path.c_str(), "a");
+  if (!f) return ALPS_E_IO;
+  if (row) write_row(f, *row);
+  else std::fputc('\n', f);
+  std::fclose(f);
+  return ALPS_OK;
+}
+
+// om_double_scan (src/ALPS_fns.f90:2904-3591), scan_option 2: scan 2 runs
+// from every output point of scan 1.  Outer steps start from the roots of
+// the previous outer step (omlast), inner steps from the previous inner
+// step; files are <run>.scan_<id1><id2>.root_<n> (and .eigen_/.heat_/
+// .heat_mech_ when scan 1 asks for them) with a blank line after every
+// inner scan, as in the reference.
+int double_scan(alps_ctx* ctx, const alps_input& in, const std::string& soldir, const std::string& run, int nroots,
+                std::vector<alps_complex>& wroots, double kperp, double kpar) {
+  const alps_system& s = in.sys;
+  const alps_scan_def& s1 = in.scan[0];
+  const alps_scan_def& s2 = in.scan[1];
+  const char* ids1[5] = {"k1_k2_", "theta_", "kcstq_", "kperp_", "kpara_"};
+  const char* ids2[5] = {"k1_k2", "theta", "kcstq", "kperp", "kpara"};
+  const std::string tag = std::string(ids1[s1.type_s]) + ids2[s2.type_s];
+  auto name = [&](const char* kind, int r) {
+    return soldir + "/" + run + "." + kind + "_" + tag + ".root_" + std::to_string(r + 1);
+  };
+  const bool want_eig = s1.eigen || s1.heating;
+  int st;
+  for (int r = 0; r < nroots; ++r) {
+    const char* kinds[4] = {"scan", "eigen", "heat", "heat_mech"};
+    for (int q = 0; q < 4; ++q) {
+      if (q == 1 && !s1.eigen) continue;
+      if (q >= 2 && !s1.heating) continue;
+      FILE* f = std::fopen(name(kinds[q], r).c_str(), "w");
+      if (!f) return ALPS_E_IO;
+      std::fclose(f);
+    }
+  }
+  // (the reference also evaluates calc_eigen at the start point here but
+  // writes nothing from it)
+  const int nt = s1.n_out * s1.n_res, nt2 = s2.n_out * s2.n_res;
+  const double kperp_last = kperp, kpar_last = kpar;
+  const double theta_0 = std::atan(kperp_last / kpar_last);
+  const double k_0 = std::sqrt(kperp_last * kperp_last + kpar_last * kpar_last);
+  std::vector<alps_complex> omlast(wroots.begin(), wroots.begin() + nroots);
+  std::vector<char> jump(nroots, 1);
+  // the roots still followed
+  auto active = [&](std::vector<int>& idx, std::vector<alps_complex>& sub) {
+    idx.clear();
+    sub.clear();
+    for (int r = 0; r < nroots; ++r)
+      if (jump[r]) idx.push_back(r);
+  };
+  for (int it = 0; it <= nt; ++it) {
+    scan_k(s1, it, kperp_last, kpar_last, theta_0, k_0, kperp, kpar);
+    if ((st = alps_set_k(ctx, kperp, kpar))) return st;
+    bool alljump = false;
+    for (int r = 0; r < nroots; ++r) alljump = alljump || jump[r];
+    if (!alljump) return ALPS_E_ROOTS_DIVERGED;
+    std::vector<int> idx;
+    std::vector<alps_complex> sub;
+    active(idx, sub);
+    for (int r : idx) sub.push_back(omlast[r]);
+    if ((st = alps_secant(ctx, s.secant_method, (int)sub.size(), sub.data(), nullptr, nullptr))) return st;
+    for (size_t q = 0; q < idx.size(); ++q) {
+      int r = idx[q];
+      wroots[r] = omlast[r] = sub[q];
+      double re = sub[q].re;
+      if (std::fabs(re) >= 1.79769313486231571e308 || re != re) jump[r] = 0;
+      for (int imm = 0; imm < r; ++imm)
+        if (std::hypot(wroots[r].re - wroots[imm].re, wroots[r].im - wroots[imm].im) < s.D_gap) {
+          wroots[r] = alps_complex{0.0, 0.0};
+          jump[r] = 0;
+        }
+    }
+    if (it % s1.n_res == 0) {
+      double kperpi = kperp, kpari = kpar, theta_i = 0.0, k_i = 0.0;
+      for (int it2 = 0; it2 <= nt2; ++it2) {
+        if (it2 == 0) {
+          kperpi = kperp;
+          kpari = kpar;
+          theta_i = std::atan(kperpi / kpari);
+          k_i = std::sqrt(kperpi * kperpi + kpari * kpari);
+          for (int r = 0; r < nroots; ++r) wroots[r] = omlast[r];
+        }
+        scan_k(s2, it2, kperpi, kpari, theta_i, k_i, kperp, kpar);
+        if ((st = alps_set_k(ctx, kperp, kpar))) return st;
+        active(idx, sub);
+        for (int r : idx) sub.push_back(wroots[r]);
+        if ((st = alps_secant(ctx, s.secant_method, (int)sub.size(), sub.data(), nullptr, nullptr))) return st;
+        std::vector<alps_complex> Dr(sub.size());
+        if (!sub.empty() && (st = alps_disp_batch(ctx, (int)sub.size(), sub.data(), Dr.data()))) return st;
+        const bool out = (it % s1.n_res == 0) && (it2 % s2.n_res == 0);
+        std::vector<alps_eigen> eg;
+        if (out && want_eig && !sub.empty()) {
+          eg.resize(sub.size());
+          if ((st = alps_calc_eigen(ctx, (int)sub.size(), sub.data(), s1.eigen, s1.heating, eg.data()))) return st;
+        }
+        for (size_t q = 0; q < idx.size(); ++q) {
+          int r = idx[q];
+          wroots[r] = sub[q];
+          double re = sub[q].re;
+          if (std::fabs(re) >= 1.79769313486231571e308 || re != re) jump[r] = 0;
+          if (std::hypot(Dr[q].re, Dr[q].im) > 1.0e100) jump[r] = 0;
+          for (int imm = 0; imm < r; ++imm)
+            if (std::hypot(wroots[r].re - wroots[imm].re, wroots[r].im - wroots[imm].im) < s.D_gap) {
+              wroots[r] = alps_complex{0.0, 0.0};
+              jump[r] = 0;
+            }
+          if (!out) continue;
+          std::vector<double> head = {kperp, kpar, wroots[r].re, wroots[r].im};
+          if ((st = append_line(name("scan", r), &head))) return st;
+          if (want_eig) {
+            std::vector<double> ev, hv, mv;
+            eigen_columns(eg[q], s.nspec, ev, hv, mv);
+            const char* kinds[3] = {"eigen", "heat", "heat_mech"};
+            const std::vector<double>* cols[3] = {&ev, &hv, &mv};
+            for (int c = 0; c < 3; ++c) {
+              if ((c == 0 && !s1.eigen) || (c > 0 && !s1.heating)) continue;
+              std::vector<double> row = head;
+              row.insert(row.end(), cols[c]->begin(), cols[c]->end());
+              if ((st = append_line(name(kinds[c], r), &row))) return st;
+            }
+          }
+        }
+      }
+      for (int r = 0; r < nroots; ++r) {
+        if ((st = append_line(name("scan", r), nullptr))) return st;
+        if (s1.eigen && (st = append_line(name("eigen", r), nullptr))) return st;
+        if (s1.heating && (st = append_line(name("heat", r), nullptr))) return st;
+        if (s1.heating && (st = append_line(name("heat_mech", r), nullptr))) return st;
+      }
+    }
+    // back to the start of scan 2's parameter (itt = 0 with the original k)
+    scan_k(s2, 0, kperp_last, kpar_last, theta_0, k_0, kperp, kpar);
+    if (s2.type_s == 2) {  // the reset of type 2 reuses the type-0 formulas
+      alps_scan_def t0 = s2;
+      t0.type_s = 0;
+      scan_k(t0, 0, kperp_last, kpar_last, theta_0, k_0, kperp, kpar);
+    }
+  }
+  return ALPS_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -444,7 +626,8 @@ int alps_run_input(const char* input_path, const char* workdir) {
   alps_input in;
   int st = alps_read_input(input_path, &in);
   if (st) return st;
-  if (in.scan_option != 1 && in.n_scan > 0) return in.scan_option == 2 ? ALPS_E_UNSUPPORTED : ALPS_E_SCAN_OPTION;
+  if (in.n_scan > 0 && in.scan_option != 1 && in.scan_option != 2) return ALPS_E_SCAN_OPTION;
+  if (in.n_scan > 0 && in.scan_option == 2 && in.n_scan != 2) return ALPS_E_NSCAN;
   const alps_system& s = in.sys;
   std::string wd(workdir);
   std::string soldir = wd + "/solution";
@@ -522,6 +705,8 @@ int alps_run_input(const char* input_path, const char* workdir) {
     }
     std::fclose(fr);
   }
+  if (in.n_scan > 0 && in.scan_option == 2)
+    return double_scan(ctx, in, soldir, run, nroots, wroots, kperp, kpar);
   // om_scan (src/ALPS_fns.f90:2198-2600), scan_option 1: scans in sequence
   const char* ids[5] = {"k1_k2_", "theta_", "kcstq_", "kperp_", "kpara_"};
   for (int ik = 1; ik <= in.n_scan; ++ik) {
