@@ -99,6 +99,63 @@ def config_map(nr=512, ni=512, Bessel_zero=1e-9):
     return w
 
 
+def uneven_plasma(rng, grid=None, Bessel_zero=1e-20):
+    """One solve of the uneven-batch draw: 1-3 species from {bi-Maxwellian
+    with T_perp/T_par in U[0.3,3] and beta in logU[0.01,10]; a drifting proton
+    beam with n_b/n_p in U[0.02,0.2] and drift in U[0,2] v_A; bi-kappa with
+    kappa in U[3,10] (fit type 2)}, grid N_perp in {64,96,128,192,256} with
+    N_par = 2 N_perp (or ``grid``), k_perp rho_p in logU[0.01,10] and a
+    propagation angle in U[20,88] degrees.  ``rng`` is a numpy Generator."""
+    import math
+    nspec = int(rng.integers(1, 4))
+    N = int(rng.choice([64, 96, 128, 192, 256])) if grid is None else grid[0]
+    M = 2 * N if grid is None else grid[1]
+    beta_p = 10.0 ** rng.uniform(-2.0, 1.0)
+    dists, species = [], []
+    kinds = ["bimax"] + [str(rng.choice(["bimax", "beam", "kappa"])) for _ in range(nspec - 1)]
+    for k, kind in enumerate(kinds):
+        electron = (k == 1 and kind == "bimax")
+        ms, qs = (1.0 / 1836.0, -1.0) if electron else (1.0, 1.0)
+        ns = 1.0
+        # the generator's autoscale spans maxP sqrt(m tau alpha) whatever the
+        # beta, so maxP = 6 sqrt(beta) keeps six thermal momenta on the grid
+        if kind == "bimax":
+            beta = beta_p if k == 0 else 10.0 ** rng.uniform(-2, 1)
+            d = _dist(kind=1, ms=ms, alph=rng.uniform(0.3, 3.0), beta=beta, maxP=6.0 * math.sqrt(beta))
+        elif kind == "beam":
+            ns = rng.uniform(0.02, 0.2)
+            d = _dist(kind=1, ms=1.0, beta=beta_p, p_drift=rng.uniform(0.0, 2.0), maxP=6.0 * math.sqrt(beta_p))
+        else:
+            kap = rng.uniform(3.0, 10.0)
+            d = _dist(kind=2, ms=ms, beta=beta_p, kappa=kap, kappa1=kap, maxP=6.0 * math.sqrt(beta_p))
+        dists.append(d)
+        species.append((kind, ns, qs, ms))
+    krho = 10.0 ** rng.uniform(-2.0, 1.0)
+    kperp = krho / math.sqrt(beta_p)
+    theta = math.radians(rng.uniform(20.0, 88.0))
+    kpar = kperp / math.tan(theta)
+    sysd = _abi.system_defaults(
+        nspec=nspec, nperp=N, npar=M, kperp=kperp, kpar=kpar, vA=1e-4, Bessel_zero=Bessel_zero,
+        secant_method=2, numiter=50, kperp_norm=1, D_threshold=1e-15, positions_principal=3,
+        n_resonance_interval=100, Tlim=0.01)
+    return dict(system=sysd, dists=dists, species_kinds=species, k=(kperp, kpar),
+                extra=dict(theta_deg=math.degrees(theta), krho=krho, beta_p=beta_p))
+
+
+def build_uneven(w, generate):
+    """(system, [(species, pperp, ppar, f0)]) of an uneven_plasma draw, the
+    continuation seeded with generate_distribution's ideal parameters (fit
+    type 1 for the Maxwellians and the beam, type 2 for bi-kappa)."""
+    s = w["system"]
+    out = []
+    for d, (kind, ns, qs, ms) in zip(w["dists"], w["species_kinds"]):
+        pperp, ppar, f0, ideal = generate(d, s.nperp, s.npar)
+        ftype = 2 if kind == "kappa" else 1
+        sp = _abi.species_defaults(ns=ns, qs=qs, ms=ms, fits=[(ftype, list(ideal[:5]), ideal[5])])
+        out.append((sp, pperp, ppar, f0))
+    return s, out
+
+
 def build(w, generate):
     """Returns (system, [(species, pperp, ppar, f0), ...])."""
     s = w["system"]
