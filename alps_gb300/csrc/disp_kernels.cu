@@ -330,7 +330,7 @@ __device__ inline double2 crcp(double2 z) {
   return cmk(z.x * r, -z.y * r);
 }
 
-__global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const double2* __restrict__ om,
+__global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, const double2* __restrict__ om,
                                                               int n_om, const int* __restrict__ count,
                                                               const int* __restrict__ slot_nn, double2* items,
                                                               int* flags) {
@@ -382,8 +382,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
       }
     }
     __syncwarp();
-    // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321)
-    auto Hc = [&](double p, double2* H) {
+    double2 T[6];
+    for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
+    // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
+    // interpolant serves p is "the last ipar in 1..npar-1 with
+    // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
+    auto piece = [&](double p) {
       int jc = 0;
       double jd = floor((p - S.ppar[0]) / dpa + 0.5);
       if (jd > -10.0 && jd < (double)M + 10.0) {
@@ -394,43 +398,79 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
       }
       if (jc >= M - 1) jc = M - 2;
       if (jc <= 1) jc = 2;
-      double dx = p - S.ppar[jc];
+      return jc;
+    };
+    // node value h and centred slope s of the six entries at node jc
+    auto node = [&](int jc, double2* h, double2* sl) {
       if (winok && jc - 1 >= jw0 && jc + 1 <= jw1) {
-        const double2* h0 = wh + (jc - jw0) * 6;
-        const double2* s0 = ws + (jc - jw0) * 6;
 #pragma unroll
-        for (int e = 0; e < 6; ++e) H[e] = cmk(fma(s0[e].x, dx, h0[e].x), fma(s0[e].y, dx, h0[e].y));
+        for (int e = 0; e < 6; ++e) {
+          h[e] = wh[(jc - jw0) * 6 + e];
+          sl[e] = ws[(jc - jw0) * 6 + e];
+        }
       } else {
 #pragma unroll
         for (int e = 0; e < 6; ++e) {
-          double2 hp = h_node(Vn, jc + 1, e, o, kappa), h0 = h_node(Vn, jc, e, o, kappa),
-                  hm = h_node(Vn, jc - 1, e, o, kappa);
-          H[e] = cadd(h0, cscale(csub(hp, hm), 0.5 * dx / dpa));
+          h[e] = h_node(Vn, jc, e, o, kappa);
+          sl[e] = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
         }
       }
     };
+    auto Hc = [&](double p, double2* H) {
+      int jc = piece(p);
+      double2 h[6], sl[6];
+      node(jc, h, sl);
+      double dx = p - S.ppar[jc];
+#pragma unroll
+      for (int e = 0; e < 6; ++e) H[e] = cmk(fma(sl[e].x, dx, h[e].x), fma(sl[e].y, dx, h[e].y));
+    };
+    // Sum_k c_k H(p_k) with H linear on each piece: per piece only
+    // A = Sum c_k and B = Sum c_k (p_k - pp(jc)) are accumulated, and
+    // T += h A + s B when the piece changes (each lane walks consecutive k)
+    struct Acc {
+      int jc;
+      double2 A, B;
+    };
+    auto flush = [&](Acc& q, double sign) {
+      if (q.jc < 0) return;
+      double2 h[6], sl[6];
+      node(q.jc, h, sl);
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        double2 t = cadd(cmul(h[e], q.A), cmul(sl[e], q.B));
+        T[e] = cmk(fma(sign, t.x, T[e].x), fma(sign, t.y, T[e].y));
+      }
+      q.A = q.B = cmk(0.0, 0.0);
+    };
+    auto add = [&](Acc& q, double p, double2 c, double sign) {
+      int jc = piece(p);
+      if (jc != q.jc) {
+        flush(q, sign);
+        q.jc = jc;
+      }
+      double dx = p - S.ppar[jc];
+      q.A = cadd(q.A, c);
+      q.B = cmk(fma(c.x, dx, q.B.x), fma(c.y, dx, q.B.y));
+    };
     const double capDelta = pr - S.ppar[g.lower];
     const double smdelta = capDelta / (1.0 * a.sys.M_P);
-    double2 T[6];
-    for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
     double2 H1[6], H2[6];
     if (fabs(pim) > a.sys.Tlim) {
-      for (int k = lane; k <= a.sys.M_P; k += 32) {
+      // w_k [H(p) K - H(2 pr - p) conj(K)], K = 1/(p - pr - i pim)
+      const int NP = a.sys.M_P + 1, per = (NP + 31) / 32;
+      const int k0 = lane * per, k1 = min(NP, k0 + per);
+      Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
+      for (int k = k0; k < k1; ++k) {
         double p = (k == 0) ? pr : ((k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k);
         double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-        // K = 1/(p - pr - i pim); the mirrored point uses conj(K)
         double dx = p - pr;
         double rr = wk / (dx * dx + pim * pim);
-        double kr = dx * rr, ki = pim * rr;
-        Hc(p, H1);
-        Hc(2.0 * pr - p, H2);
-#pragma unroll
-        for (int e = 0; e < 6; ++e) {
-          // H1 K - H2 conj(K)
-          T[e].x += (H1[e].x - H2[e].x) * kr - (H1[e].y + H2[e].y) * ki;
-          T[e].y += (H1[e].x + H2[e].x) * ki + (H1[e].y - H2[e].y) * kr;
-        }
+        double2 K = cmk(dx * rr, pim * rr);
+        add(up, p, K, 1.0);
+        add(dn, 2.0 * pr - p, cmk(K.x, -K.y), -1.0);
       }
+      flush(up, 1.0);
+      flush(dn, -1.0);
     } else {
       // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
       double fr = 0.0;
@@ -457,16 +497,17 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
     int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
     if (ntiny > 0) {
       double corr = ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta;
-      for (int k = lane; k <= ntiny; k += 32) {
+      const int per = (ntiny + 1 + 31) / 32;
+      const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
+      Acc q{-1, cmk(0, 0), cmk(0, 0)};
+      for (int k = k0; k < k1; ++k) {
         double p = (k == 0) ? pr + capDelta : pr + capDelta + corr * smdelta * k;
         double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
         double dx = p - pr;
         double rr = wk * corr / (dx * dx + pim * pim);
-        double2 K = cmk(dx * rr, pim * rr);
-        Hc(p, H1);
-#pragma unroll
-        for (int e = 0; e < 6; ++e) T[e] = cadd(T[e], cmul(H1[e], K));
+        add(q, p, cmk(dx * rr, pim * rr), 1.0);
       }
+      flush(q, 1.0);
     }
     for (int e = 0; e < 6; ++e)
       for (int off = 16; off > 0; off >>= 1) {
@@ -490,35 +531,59 @@ __global__ void __launch_bounds__(RES_WARPS * 32) k_resonant(DispArgs a, const d
     double bound = S.la * ap * ap + S.lb * ap + S.lc;
     if (bound <= 1e-5) {
       landau_done = true;
-      if (lane == 0) {
-        auto gauss = [&](double2 x) {
-          double2 d = cmk(x.x - S.p3r, x.y);
-          return cexp_d(cscale(cmul(d, d), -S.p2r));
-        };
-        auto poly = [&](const double* m, double2 x) {
-          double2 acc = cmk(m[4], 0.0);
-          for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
-          return acc;
-        };
-        double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
-        double2 G0 = gauss(p), Gp = gauss(xp), Gm = gauss(xm);
-        bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
-                    (cabs_(G0) * S.min_a0 == 0.0);
-        if (!zero) {
-          const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
-          double2 sums[3];
-          for (int F = 0; F < 3; ++F) {
-            const double* lm = S.lmom + ((size_t)n * 3 + F) * 10;
-            double2 Spar = cscale(csub(cmul(Gp, poly(lm, xp)), cmul(Gm, poly(lm, xm))), 1.0 / (2.0 * pd));
-            double2 Sperp = cmul(G0, poly(lm + 5, p));
-            // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp)
-            sums[F] = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
+      auto gauss = [&](double2 x) {
+        double2 d = cmk(x.x - S.p3r, x.y);
+        return cexp_d(cscale(cmul(d, d), -S.p2r));
+      };
+      auto poly = [&](const double* m, double2 x) {
+        double2 acc = cmk(m[4], 0.0);
+        for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
+        return acc;
+      };
+      auto shfl2 = [&](double2 v, int src) {
+        return cmk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+      };
+      const double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
+      // lanes 0-2: the row Gaussian at p, p + dppar, p - dppar
+      double2 Gl = cmk(0.0, 0.0);
+      if (lane < 3) Gl = gauss(lane == 1 ? xp : (lane == 2 ? xm : p));
+      const double2 G0 = shfl2(Gl, 0), Gp = shfl2(Gl, 1), Gm = shfl2(Gl, 2);
+      bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
+                  (cabs_(G0) * S.min_a0 == 0.0);
+      if (!zero) {
+        // lanes 0-8: the moment polynomials of family F = lane/3 at p + dppar,
+        // p - dppar (d/dp_par moments) and p (d/dp_perp moments)
+        double2 Pv = cmk(0.0, 0.0);
+        if (lane < 9) {
+          const double* lm = S.lmom + ((size_t)n * 3 + lane / 3) * 10;
+          const int wch = lane % 3;
+          Pv = (wch == 0) ? poly(lm, xp) : ((wch == 1) ? poly(lm, xm) : poly(lm + 5, p));
+        }
+        const int Fl = min(lane, 2);
+        const double2 Pxp = shfl2(Pv, 3 * Fl), Pxm = shfl2(Pv, 3 * Fl + 1), Ppp = shfl2(Pv, 3 * Fl + 2);
+        const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
+        double2 Spar = cscale(csub(cmul(Gp, Pxp), cmul(Gm, Pxm)), 1.0 / (2.0 * pd));
+        double2 Sperp = cmul(G0, Ppp);
+        // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp), family Fl
+        const double2 sumF = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
+        // lanes 0-5: entry e = lane
+        const int fam[6] = {0, 1, 0, 2, 0, 2};
+        double2 pe = pref[0], ce = cmk(1.0, 0.0);
+        int fe = 0;
+#pragma unroll
+        for (int e = 0; e < 6; ++e)
+          if (lane == e) {
+            pe = pref[e];
+            fe = fam[e];
+            ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
           }
-          double2 c1 = cmk(1.0, 0.0), cp = p, cp2 = cmul(p, p);
-          double2 cfac[6] = {c1, c1, cp2, c1, cp, cp};
-          int fam[6] = {0, 1, 0, 2, 0, 2};
-          double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
-          for (int e = 0; e < 6; ++e) res[e] = cadd(res[e], cmul(cmul(cmul(pref[e], cfac[e]), sums[fam[e]]), ifac));
+        const double2 sf = shfl2(sumF, fe);
+        const double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+        const double2 contrib = cmul(cmul(cmul(pe, ce), sf), ifac);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          double2 c = shfl2(contrib, e);
+          if (lane == 0) res[e] = cadd(res[e], c);
         }
       }
     }
