@@ -387,18 +387,34 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
     // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
     // interpolant serves p is "the last ipar in 1..npar-1 with
     // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
-    auto piece = [&](double p) {
-      int jc = 0;
-      double jd = floor((p - S.ppar[0]) / dpa + 0.5);
+    const double idpa = 1.0 / dpa, half = 0.5 * dpa;
+    // last node in 1..M-1 within half a spacing of p, or 0 (the search of
+    // funct_g before its clamp); the candidates bracket the nearest node
+    auto piece_raw = [&](double p) {
+      int jr = 0;
+      double jd = floor((p - S.ppar[0]) * idpa + 0.5);
       if (jd > -10.0 && jd < (double)M + 10.0) {
         int j0 = (int)jd;
         int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
         for (int jj = hi; jj >= lo; --jj)
-          if (fabs(S.ppar[jj] - p) <= 0.5 * dpa) { jc = jj; break; }
+          if (fabs(S.ppar[jj] - p) <= half) { jr = jj; break; }
       }
-      if (jc >= M - 1) jc = M - 2;
-      if (jc <= 1) jc = 2;
-      return jc;
+      return jr;
+    };
+    auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
+    auto piece = [&](double p) { return clampj(piece_raw(p)); };
+    // the same index for p increasing (up) or decreasing (down) from a known
+    // raw index: |pp(j) - p| is monotone in p, so the last valid node moves
+    // by single steps
+    auto piece_up = [&](int jr, double p) {
+      if (jr == 0) return piece_raw(p);
+      while (jr < M - 1 && fabs(S.ppar[jr + 1] - p) <= half) ++jr;
+      return (fabs(S.ppar[jr] - p) <= half) ? jr : piece_raw(p);
+    };
+    auto piece_down = [&](int jr, double p) {
+      if (jr == 0) return piece_raw(p);
+      while (jr >= 1 && !(fabs(S.ppar[jr] - p) <= half)) --jr;
+      return (jr >= 1) ? jr : piece_raw(p);
     };
     // node value h and centred slope s of the six entries at node jc
     auto node = [&](int jc, double2* h, double2* sl) {
@@ -442,8 +458,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
       }
       q.A = q.B = cmk(0.0, 0.0);
     };
-    auto add = [&](Acc& q, double p, double2 c, double sign) {
-      int jc = piece(p);
+    auto add = [&](Acc& q, int jc, double p, double2 c, double sign) {
       if (jc != q.jc) {
         flush(q, sign);
         q.jc = jc;
@@ -460,14 +475,18 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
       const int NP = a.sys.M_P + 1, per = (NP + 31) / 32;
       const int k0 = lane * per, k1 = min(NP, k0 + per);
       Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
+      int ju = -1, jd = -1;  // raw node indices of the direct and mirrored points
+      const double pim2 = pim * pim;
       for (int k = k0; k < k1; ++k) {
         double p = (k == 0) ? pr : ((k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k);
         double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-        double dx = p - pr;
-        double rr = wk / (dx * dx + pim * pim);
+        double dx = p - pr, pm = 2.0 * pr - p;
+        double rr = wk * rcp_fast(fma(dx, dx, pim2));
         double2 K = cmk(dx * rr, pim * rr);
-        add(up, p, K, 1.0);
-        add(dn, 2.0 * pr - p, cmk(K.x, -K.y), -1.0);
+        ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
+        jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
+        add(up, clampj(ju), p, K, 1.0);
+        add(dn, clampj(jd), pm, cmk(K.x, -K.y), -1.0);
       }
       flush(up, 1.0);
       flush(dn, -1.0);
@@ -500,12 +519,14 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
       const int per = (ntiny + 1 + 31) / 32;
       const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
       Acc q{-1, cmk(0, 0), cmk(0, 0)};
+      int jt = -1;
       for (int k = k0; k < k1; ++k) {
         double p = (k == 0) ? pr + capDelta : pr + capDelta + corr * smdelta * k;
         double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
         double dx = p - pr;
-        double rr = wk * corr / (dx * dx + pim * pim);
-        add(q, p, cmk(dx * rr, pim * rr), 1.0);
+        double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
+        jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
+        add(q, clampj(jt), p, cmk(dx * rr, pim * rr), 1.0);
       }
       flush(q, 1.0);
     }
