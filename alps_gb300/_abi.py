@@ -132,6 +132,18 @@ def eigen_columns(e, nspec):
     return eig, heat, mech
 
 
+REQ_POLISH, REQ_MAP, REQ_SCAN = 0, 1, 2
+
+
+class alps_request(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int), ("ctx", C.c_void_p), ("n", C.c_int), ("om", C.POINTER(alps_complex)),
+        ("iters", C.POINTER(C.c_int)), ("map", alps_map_params), ("map_cal", C.POINTER(alps_complex)),
+        ("map_val", C.POINTER(C.c_double)), ("scan", alps_scan_def), ("scan_rows", C.POINTER(C.c_double)),
+        ("status", C.c_int), ("latency_ms", C.c_double), ("rounds", C.c_int),
+    ]
+
+
 class alps_stats(C.Structure):
     _fields_ = [
         ("n_eval", C.c_int64), ("n_pole_terms", C.c_int64),

@@ -49,6 +49,12 @@ def lib():
             "alps_get_f0_rel": ([vp, C.c_int, dp, dp, dp, dp, dp], C.c_int),
             "alps_calc_eigen": ([vp, C.c_int, C.POINTER(_abi.alps_complex), C.c_int, C.c_int,
                                  C.POINTER(_abi.alps_eigen)], C.c_int),
+            "alps_server_create": ([C.c_size_t, C.c_int, P(vp)], C.c_int),
+            "alps_server_destroy": ([vp], None),
+            "alps_server_submit": ([vp, P(_abi.alps_request), P(C.c_int64)], C.c_int),
+            "alps_server_poll": ([vp, C.c_int64, P(C.c_int)], C.c_int),
+            "alps_server_wait": ([vp, C.c_int64], C.c_int),
+            "alps_server_stats": ([vp, P(C.c_int64), P(C.c_int), P(C.c_size_t)], C.c_int),
             "alps_set_k": ([vp, C.c_double, C.c_double], C.c_int),
             "alps_get_nmax": ([vp, P(C.c_int)], C.c_int),
             "alps_set_precision": ([vp, C.c_int], C.c_int),
@@ -89,5 +95,6 @@ def exported_symbols():
         "alps_get_nmax", "alps_set_precision", "alps_disp", "alps_disp_batch", "alps_disp_batch_device",
         "alps_secant", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
         "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_read_input", "alps_read_f0",
-        "alps_get_f0_rel", "alps_calc_eigen",
+        "alps_get_f0_rel", "alps_calc_eigen", "alps_server_create", "alps_server_destroy", "alps_server_submit",
+        "alps_server_poll", "alps_server_wait", "alps_server_stats",
     ]

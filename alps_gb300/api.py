@@ -306,3 +306,127 @@ class Plasma:
         if want:
             return rows, wr, eig
         return rows, wr
+
+
+class Request:
+    """A request submitted to a Server; its buffers live here until done."""
+
+    def __init__(self, server, kind, plasma, **kw):
+        self._server = server
+        self.plasma = plasma
+        self.kind = kind
+        rq = _abi.alps_request()
+        rq.kind = kind
+        rq.ctx = plasma.handle.value if isinstance(plasma.handle, C.c_void_p) else plasma.handle
+        self._bufs = []
+        if kind in (_abi.REQ_POLISH, _abi.REQ_SCAN):
+            om = np.ascontiguousarray(np.atleast_1d(kw["guesses"]), dtype=np.complex128).copy()
+            self.om = om
+            rq.n = len(om)
+            rq.om = _cptr(om)
+            self.iters = (C.c_int * max(1, len(om)))()
+            rq.iters = C.cast(self.iters, C.POINTER(C.c_int))
+        if kind == _abi.REQ_MAP:
+            mp = kw["map"]
+            rq.map = mp
+            n = mp.nr * mp.ni
+            self.cal = np.zeros(n, dtype=np.complex128)
+            self.val = np.zeros(n)
+            rq.map_cal = _cptr(self.cal)
+            rq.map_val = _dptr(self.val)
+        if kind == _abi.REQ_SCAN:
+            sc = kw["scan"]
+            rq.scan = sc
+            self.rows = np.zeros((sc.n_out + 1) * len(self.om) * 4)
+            rq.scan_rows = _dptr(self.rows)
+        self._rq = rq
+        self.id = C.c_int64()
+        check(lib().alps_server_submit(server._h, C.byref(rq), C.byref(self.id)), "alps_server_submit")
+
+    def done(self):
+        d = C.c_int()
+        check(lib().alps_server_poll(self._server._h, self.id, C.byref(d)), "alps_server_poll")
+        return bool(d.value)
+
+    def wait(self):
+        """Blocks until done; returns the result (roots; (cal, val) of a map;
+        the scan rows [it, root, (kperp, kpar, Re, Im)] and final roots)."""
+        check(lib().alps_server_wait(self._server._h, self.id), "alps_server_wait")
+        if self.kind == _abi.REQ_POLISH:
+            return self.om.copy()
+        if self.kind == _abi.REQ_MAP:
+            return self.cal.copy(), self.val.copy()
+        n = len(self.om)
+        return self.rows.reshape(-1, n, 4).copy(), self.om.copy()
+
+    @property
+    def latency_ms(self):
+        return self._rq.latency_ms
+
+    @property
+    def rounds(self):
+        return self._rq.rounds
+
+
+class Server:
+    """Continuous batching of root polishes, k scans and maps over many
+    plasmas (alps_server_*): requests run as they arrive, their batches
+    overlap on the GPU, each result equals the request's result alone.
+    A plasma serves one request at a time and must not be used elsewhere
+    while it does."""
+
+    def __init__(self, hbm_budget=0, max_active=0):
+        self._h = C.c_void_p()
+        check(lib().alps_server_create(int(hbm_budget), int(max_active), C.byref(self._h)), "alps_server_create")
+
+    def polish(self, plasma, guesses):
+        return Request(self, _abi.REQ_POLISH, plasma, guesses=guesses)
+
+    def map(self, plasma, mp):
+        return Request(self, _abi.REQ_MAP, plasma, map=mp)
+
+    def scan(self, plasma, scan_def, roots):
+        """scan_def: alps_scan_def with the step sizes of scan_read (diff,
+        diff2), e.g. from scan_def(); roots: the refined roots at the
+        plasma's current k."""
+        return Request(self, _abi.REQ_SCAN, plasma, scan=scan_def, guesses=roots)
+
+    def stats(self):
+        r, a, b = C.c_int64(), C.c_int(), C.c_size_t()
+        check(lib().alps_server_stats(self._h, C.byref(r), C.byref(a), C.byref(b)), "alps_server_stats")
+        return {"rounds": r.value, "peak_active": a.value, "peak_bytes": b.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().alps_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def scan_def(type_s, swi, swf, log_scan, n_out, n_res, kperp, kpar):
+    """alps_scan_def with scan_read's step sizes (src/ALPS_io.f90:426-552)
+    for a scan starting at (kperp, kpar)."""
+    lg = math.log10
+    sc = _abi.alps_scan_def()
+    sc.type_s, sc.swi, sc.swf, sc.log_scan, sc.n_out, sc.n_res = type_s, swi, swf, int(log_scan), n_out, n_res
+    d = 1.0 * n_out * n_res
+    theta_0 = math.atan(kperp / kpar)
+    k_0 = math.sqrt(kperp ** 2 + kpar ** 2)
+    if type_s == 0:
+        sc.diff = (lg(swi) - lg(kperp)) / d if log_scan else (swi - kperp) / d
+        sc.diff2 = (lg(swf) - lg(kpar)) / d if log_scan else (swf - kpar) / d
+    elif type_s == 1:
+        tf = swf * 4.0 * math.atan(1.0) / 180.0
+        sc.diff = (lg(tf) - lg(theta_0)) / d if log_scan else (tf - theta_0) / d
+    elif type_s == 2:
+        sc.diff = (lg(swf) - lg(k_0)) / d if log_scan else (swf - k_0) / d
+    elif type_s == 3:
+        sc.diff = (lg(swf) - lg(kperp)) / d if log_scan else (swf - kperp) / d
+    else:
+        sc.diff = (lg(swf) - lg(kpar)) / d if log_scan else (swf - kpar) / d
+    return sc

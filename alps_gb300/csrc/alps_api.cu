@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "alps_internal.cuh"
+#include "root_finders.h"
 
 namespace {
 thread_local char g_last_err[512] = "";
@@ -396,7 +397,7 @@ int alps_set_precision(alps_ctx* c, int precision) {
   return ALPS_OK;
 }
 
-static int ensure_batch(alps_ctx* c, int n, bool ext) {
+int ctx_ensure_batch(alps_ctx* c, int n, bool ext) {
   if ((size_t)n > c->batch_cap) {
     cudaFree(c->d_om);
     cudaFree(c->d_D);
@@ -427,7 +428,7 @@ static int ensure_batch(alps_ctx* c, int n, bool ext) {
   return ALPS_OK;
 }
 
-static int check_flags(alps_ctx* c) {
+int ctx_check_flags(alps_ctx* c) {
   int f = 0;
   ALPS_CUDA_TRY(cudaMemcpy(&f, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
   if (f & 2) return ALPS_E_SUBLUMINAL;  // resonance window wider than the subluminal cone
@@ -436,7 +437,7 @@ static int check_flags(alps_ctx* c) {
 
 // Evaluates n frequencies from host memory through pinned staging.
 static int disp_host(alps_ctx* c, int n, const alps_complex* om, alps_complex* D, alps_complex* ext_out) {
-  int st = ensure_batch(c, n, ext_out != nullptr);
+  int st = ctx_ensure_batch(c, n, ext_out != nullptr);
   if (st) return st;
   double2* pin = c->h_pinned;
   memcpy(pin, om, (size_t)n * sizeof(double2));
@@ -448,7 +449,7 @@ static int disp_host(alps_ctx* c, int n, const alps_complex* om, alps_complex* D
     ALPS_CUDA_TRY(cudaMemcpyAsync(ext_out, c->d_ext, (size_t)n * (c->sys.nspec * 36 + 9) * sizeof(double2),
                                   cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  if ((st = check_flags(c))) return st;
+  if ((st = ctx_check_flags(c))) return st;
   memcpy(D, pin + n, (size_t)n * sizeof(double2));
   return ALPS_OK;
 }
@@ -640,267 +641,6 @@ int alps_get_stats(alps_ctx* c, alps_stats* st) {
   return ALPS_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Root finders.  Each root runs the reference's control flow as a state
-// machine that yields the frequencies it needs; all pending requests of all
-// roots go to the device in one batch per round.
-// ---------------------------------------------------------------------------
-namespace {
-
-struct Req {
-  std::vector<cplx> om;
-  std::vector<cplx> D;
-};
-
-// secant_osc (src/ALPS_fns.f90:1919-2101)
-struct SecantOsc {
-  const alps_system* sy;
-  int state = 0;
-  cplx om, D, minom, minD, prevom, prev2om, prev3om, prev4om, prevD, jump, delta;
-  int iter = 0, osc = 0;
-  double damping = 1.0;
-  bool done = false;
-  cplx Dfin;
-  const double lambda = (double)0.1f, osc_thr = (double)1.E-3f;
-  bool close(cplx a, cplx b) const {
-    return (std::fabs(a.real() - b.real()) < std::fabs(a.real()) * osc_thr) &&
-           (std::fabs(a.imag() - b.imag()) < std::fabs(a.imag()) * osc_thr);
-  }
-  // returns frequencies to evaluate (empty when finished)
-  std::vector<cplx> step(const std::vector<cplx>& got) {
-    for (;;) {
-      switch (state) {
-        case 0:
-          delta = cplx(1.0e-6, 1.0e-8);
-          state = 1;
-          return {om};
-        case 1:
-          D = got[0];
-          minom = om;
-          minD = D;
-          prevom = om * (1.0 - sy->D_prec);
-          prev2om = prev3om = prev4om = om;
-          state = 2;
-          return {prevom};
-        case 2:
-          prevD = got[0];
-          if (std::abs(prevD) < std::abs(minD)) { minom = prevom; minD = prevD; }
-          iter = 0;
-          state = 3;
-          break;
-        case 3:  // loop head
-          if (!(iter <= sy->numiter - 1)) { state = 9; break; }
-          iter++;
-          state = 4;
-          return {om};
-        case 4:
-          D = got[0];
-          if (std::abs(D - prevD) < 1.0e-80) {
-            prevom = prevom + 1.0e-8;
-            state = 5;
-            return {prevom};
-          }
-          state = 6;
-          break;
-        case 5:
-          prevD = got[0];
-          state = 6;
-          break;
-        case 6:
-          if (std::abs(D) < sy->D_threshold) {
-            jump = 0.0;
-            Dfin = D;
-            if (iter >= sy->numiter) {  // after-loop rule of the reference
-              om = minom;
-              Dfin = minD;
-            }
-            done = true;
-            state = 10;
-            return {};
-          }
-          if (iter > 4) {
-            if (close(om, prevom) || close(om, prev2om) || close(om, prev3om) || close(om, prev4om)) {
-              osc++;
-              damping = std::min(0.5, damping * 0.75);
-            }
-          }
-          if (osc > 1) {
-            state = 7;
-            return {om * (1.0 + delta), om * (1.0 - delta)};
-          }
-          jump = damping * D * (om - prevom) / (D - prevD);
-          state = 8;
-          break;
-        case 7: {
-          cplx Dprime = (got[0] - got[1]) / (2.0 * om * delta);
-          jump = D / (Dprime + lambda * D);
-          state = 8;
-          break;
-        }
-        case 8:
-          if (std::abs(jump) > (double)0.1f * std::abs(om)) jump = ((double)0.1f * std::abs(om)) * (jump / std::abs(jump));
-          if (std::abs(D) > std::abs(prevD)) jump = (double)0.5f * jump;
-          prev4om = prev3om;
-          prev3om = prev2om;
-          prev2om = prevom;
-          prevom = om;
-          prevD = D;
-          if (std::abs(D) < std::abs(minD)) { minom = om; minD = D; }
-          om = om - jump;
-          state = 3;
-          break;
-        case 9:  // numiter exhausted
-          om = minom;
-          Dfin = minD;
-          done = true;
-          state = 10;
-          return {};
-        default:
-          return {};
-      }
-    }
-  }
-};
-
-// secant (src/ALPS_fns.f90:1815-1917)
-struct SecantPlain {
-  const alps_system* sy;
-  int state = 0;
-  cplx om, prevom, Dprev, minD, minom, D, jump;
-  int iter = 0;
-  bool done = false;
-  cplx Dfin;
-  std::vector<cplx> step(const std::vector<cplx>& got) {
-    for (;;) {
-      switch (state) {
-        case 0:
-          prevom = om * (1.0 - sy->D_prec);
-          state = 1;
-          return {prevom, om};
-        case 1:
-          Dprev = got[0];
-          minD = got[1];
-          minom = om;
-          if (std::abs(Dprev) < std::abs(minD)) { minom = prevom; minD = Dprev; }
-          iter = 0;
-          state = 2;
-          break;
-        case 2:
-          if (!(iter <= sy->numiter - 1)) {
-            om = minom;
-            Dfin = minD;
-            done = true;
-            state = 9;
-            return {};
-          }
-          iter++;
-          state = 3;
-          return {om};
-        case 3:
-          D = got[0];
-          if (std::abs(D - Dprev) < 1.0e-80) {
-            prevom = prevom + 1.0e-8;
-            state = 4;
-            return {prevom};
-          }
-          state = 5;
-          break;
-        case 4:
-          Dprev = got[0];
-          state = 5;
-          break;
-        case 5: {
-          bool conv = std::abs(D) < sy->D_threshold;
-          jump = conv ? cplx(0.0) : D * (om - prevom) / (D - Dprev);
-          prevom = om;
-          om = om - jump;
-          Dprev = D;
-          if (std::abs(D) < std::abs(minD)) { minom = om; minD = D; }
-          if (conv) {
-            Dfin = D;
-            if (iter >= sy->numiter) {
-              om = minom;
-              Dfin = minD;
-            }
-            done = true;
-            state = 9;
-            return {};
-          }
-          state = 2;
-          break;
-        }
-        default:
-          return {};
-      }
-    }
-  }
-};
-
-// rtsec (src/ALPS_fns.f90:2105-2195)
-struct Rtsec {
-  const alps_system* sy;
-  int state = 0;
-  cplx xin, x1, x2, fl, f, rts, xl, dx;
-  int j = 0;
-  bool done = false;
-  cplx om, Dfin;
-  std::vector<cplx> step(const std::vector<cplx>& got) {
-    for (;;) {
-      switch (state) {
-        case 0:
-          x1 = xin * 1.0;
-          x2 = xin * (1.0 + sy->D_prec);
-          state = 1;
-          return {x1, x2};
-        case 1:
-          fl = got[0];
-          f = got[1];
-          if (std::abs(fl) < std::abs(f)) {
-            rts = x1;
-            xl = x2;
-            std::swap(fl, f);
-          } else {
-            xl = x1;
-            rts = x2;
-          }
-          j = 0;
-          state = 2;
-          break;
-        case 2:
-          j++;
-          if (j > sy->numiter - 1) {
-            om = rts;
-            Dfin = f;
-            done = true;
-            state = 9;
-            return {};
-          }
-          if (std::abs(f - fl) > 1.0e-40) dx = (xl - rts) * f / (f - fl);
-          else dx = (x2 - x1) / 25.0;
-          xl = rts;
-          fl = f;
-          rts = rts + dx / 2.0;
-          state = 3;
-          return {rts};
-        case 3:
-          f = got[0];
-          if ((std::abs(dx) < sy->D_tol) || (std::abs(f) == 0.0)) {
-            om = rts;
-            Dfin = f;
-            done = true;
-            state = 9;
-            return {};
-          }
-          state = 2;
-          break;
-        default:
-          return {};
-      }
-    }
-  }
-};
-
-}  // namespace
 
 int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iters, alps_complex* Dfinal) {
   if (!c || !c->kset || nroots < 0 || (nroots > 0 && !om)) return ALPS_E_INVALID;
@@ -948,10 +688,10 @@ int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iter
 }
 
 // map_search values (src/ALPS_fns.f90:3595-3788)
-int alps_map(alps_ctx* c, const alps_map_params* mp, alps_complex* om_out, alps_complex* cal, double* val) {
-  if (!c || !mp || !c->kset || mp->nr < 1 || mp->ni < 1) return ALPS_E_INVALID;
-  int nr = mp->nr, ni = mp->ni, n = nr * ni;
-  std::vector<alps_complex> oms(n), D(n);
+// the (nr x ni) frequency lattice of map_search (src/ALPS_fns.f90:3684-3716)
+void map_lattice(const alps_map_params* mp, std::vector<alps_complex>& oms) {
+  int nr = mp->nr, ni = mp->ni;
+  oms.resize((size_t)nr * ni);
   double dr = mp->omf - mp->omi, di = mp->gamf - mp->gami;
   if (nr > 1) dr = (mp->omf - mp->omi) / (1.0 * (nr - 1));
   if (ni > 1) di = (mp->gamf - mp->gami) / (1.0 * (ni - 1));
@@ -964,11 +704,13 @@ int alps_map(alps_ctx* c, const alps_map_params* mp, alps_complex* om_out, alps_
                       ? (ni > 1 ? mp->gami * std::pow(mp->gamf / mp->gami, (1.0 * (ii - 1)) / (1.0 * (ni - 1)))
                                 : mp->gami)
                       : mp->gami + di * (1.0 * (ii - 1));
-      oms[(ir - 1) * ni + (ii - 1)] = alps_complex{wr, wi};
+      oms[(size_t)(ir - 1) * ni + (ii - 1)] = alps_complex{wr, wi};
     }
   }
-  int st = disp_host(c, n, oms.data(), D.data(), nullptr);
-  if (st) return st;
+}
+
+// map_search's sentinels on det D (:3720-3743): cal and log10 of its modulus
+void map_finish(int n, const alps_complex* D, alps_complex* cal, double* val) {
   for (int k = 0; k < n; ++k) {
     cplx cc(D[k].re, D[k].im);
     double v = std::log10(std::abs(cc));
@@ -981,10 +723,20 @@ int alps_map(alps_ctx* c, const alps_map_params* mp, alps_complex* om_out, alps_
       cc = 899999.0;
       v = 899999.0;
     }
-    if (om_out) om_out[k] = oms[k];
     if (cal) cal[k] = alps_complex{cc.real(), cc.imag()};
     if (val) val[k] = v;
   }
+}
+
+int alps_map(alps_ctx* c, const alps_map_params* mp, alps_complex* om_out, alps_complex* cal, double* val) {
+  if (!c || !mp || !c->kset || mp->nr < 1 || mp->ni < 1) return ALPS_E_INVALID;
+  int n = mp->nr * mp->ni;
+  std::vector<alps_complex> oms, D(n);
+  map_lattice(mp, oms);
+  int st = disp_host(c, n, oms.data(), D.data(), nullptr);
+  if (st) return st;
+  if (om_out) std::copy(oms.begin(), oms.end(), om_out);
+  map_finish(n, D.data(), cal, val);
   return ALPS_OK;
 }
 

@@ -199,6 +199,15 @@ struct alps_ctx {
 // kernels / launchers (setup_kernels.cu, disp_kernels.cu)
 // ---------------------------------------------------------------------------
 int launch_prepare_species(alps_ctx* c, int is);
+// host helpers shared by the entry points and the request server (defined
+// inside the extern "C" block of alps_api.cu and server.cu)
+extern "C" {
+int ctx_ensure_batch(alps_ctx* c, int n, bool ext);  // d_om, d_D, pinned staging for n frequencies
+int ctx_check_flags(alps_ctx* c);                    // device error flags of the last batch
+size_t ctx_device_bytes(const alps_ctx* c);          // device memory a context holds (estimate)
+void map_lattice(const alps_map_params* mp, std::vector<alps_complex>& oms);
+void map_finish(int n, const alps_complex* D, alps_complex* cal, double* val);
+}
 int launch_glls(alps_ctx* c, int is);
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);

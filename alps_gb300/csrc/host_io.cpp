@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "../../include/alps_gb300.h"
+#include "root_finders.h"
 
 namespace {
 
@@ -233,42 +234,6 @@ bool file_exists(const std::string& p) {
 void ensure_dir(const std::string& p) { mkdir(p.c_str(), 0755); }
 
 
-
-// One step of a k scan (the select case of om_scan / om_double_scan):
-// sets the components the scan type moves, from the start point (kp0, kz0)
-// or, for types 1 and 2, from its angle th0 and magnitude k0.
-void scan_k(const alps_scan_def& sc, int it, double kp0, double kz0, double th0, double k0, double& kperp,
-            double& kpar) {
-  switch (sc.type_s) {
-    case 0:
-      if (sc.log_scan) {
-        kperp = std::pow(10.0, std::log10(kp0) + sc.diff * it);
-        kpar = std::pow(10.0, std::log10(kz0) + sc.diff2 * it);
-      } else {
-        kperp = kp0 + sc.diff * it;
-        kpar = kz0 + sc.diff2 * it;
-      }
-      break;
-    case 1: {
-      double th = sc.log_scan ? std::pow(10.0, std::log10(th0) + sc.diff * it) : th0 + sc.diff * it;
-      kperp = k0 * std::sin(th);
-      kpar = k0 * std::cos(th);
-      break;
-    }
-    case 2: {
-      double kt = sc.log_scan ? std::pow(10.0, std::log10(k0) + sc.diff * it) : (k0) + sc.diff * it;
-      kperp = kt * std::sin(th0);
-      kpar = kt * std::cos(th0);
-      break;
-    }
-    case 3:
-      kperp = sc.log_scan ? std::pow(10.0, std::log10(kp0) + sc.diff * it) : kp0 + sc.diff * it;
-      break;
-    case 4:
-      kpar = sc.log_scan ? std::pow(10.0, std::log10(kz0) + sc.diff * it) : kz0 + sc.diff * it;
-      break;
-  }
-}
 
 int append_line(const std::string& path, const std::vector<double>* row) {
   FILE* f = std::fopen(path.c_str(), "a");

@@ -1,0 +1,440 @@
+// server.cu -- continuous batching of root solves, k scans and maps over
+// many plasmas (alps_server_*, declared in include/alps_gb300.h).
+//
+// One host thread runs rounds.  In a round every active request contributes
+// one batch of frequencies (the pending evaluations of its root finders, or
+// its whole lattice) on its own context's stream; all batches are launched
+// before any is waited for, so the kernels of different plasmas overlap on
+// the GPU.  The determinants then go back into the requests' state machines
+// (root_finders.h: the reference's secant_osc / secant / rtsec), k scans move
+// to their next step, finished requests are released, and queued requests
+// are admitted while their footprint fits the budget.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "alps_internal.cuh"
+#include "root_finders.h"
+
+namespace {
+
+double now_ms() {
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+struct Active {
+  alps_request* rq = nullptr;
+  int64_t id = 0;
+  double t0 = 0.0;
+  size_t bytes = 0;
+  bool started = false;
+  // root finders (POLISH, SCAN)
+  std::vector<RootMachine> rm;
+  std::vector<int> idx;                  // request root index of each machine
+  std::vector<std::vector<cplx>> want;   // pending evaluations per machine
+  // SCAN state (om_scan, src/ALPS_fns.f90:2198-2600)
+  int it = 0, nt = 0, out_row = 0;
+  double kp0 = 0, kz0 = 0, th0 = 0, k0 = 0, kperp = 0, kpar = 0;
+  std::vector<char> jump;
+  bool map_done = false;
+  // this round's batch
+  std::vector<alps_complex> bom, bD;
+};
+
+// device bytes of a batch of n frequencies on context c (the per-batch
+// buffers of launch_disp_batch plus the staging)
+size_t batch_bytes(const alps_ctx* c, size_t n) {
+  int S = c->sys.nspec, maxn = 0, rc = 1, relcap = 0;
+  for (int s = 0; s < S; ++s) {
+    maxn = std::max(maxn, c->spec[s].nmax);
+    rc = std::max(rc, c->spec[s].rcap);
+    if (c->spec[s].sp.relat) relcap = std::max(relcap, c->spec[s].nmax + 1);
+  }
+  size_t per = 32 + (size_t)S * ((size_t)(maxn + 1) * 6 * 16 + (size_t)rc * (6 * 16 + 4) + 4 +
+                                 (size_t)relcap * 12 * 16 + 24 * 16);
+  return n * per;
+}
+
+}  // namespace
+
+extern "C" {
+
+// Device memory a context holds: its tables (grids, derivatives, fits,
+// Bessel tables, reduced vectors, moments, relativistic and closed-form
+// tables) and its batch buffers.
+size_t ctx_device_bytes(const alps_ctx* c) {
+  const size_t N = c->sys.nperp, M = c->sys.npar, d = sizeof(double);
+  size_t b = 0;
+  for (const SpeciesHost& S : c->spec) {
+    size_t nm = S.nmax + 1;
+    if (S.sp.use_bM) {
+      b += ((size_t)std::max(S.sp.bM_nmaxs, 0) + 2) * d + (N + 1) * 5 * d;
+      continue;
+    }
+    b += (N + 1 + M + 1) * d + 3 * (N + 1) * (M + 1) * d + (N - 1) * 2 * (M - 1) * d;  // grid, f0, g1, g2, G
+    b += (N + 1) * 5 * 4 * d + (N + 1) * 16 * d;                                          // fit, fit_aux
+    b += (nm + 2) * (N + 1) * d + 3 * nm * (N - 1) * d + 3 * nm * 2 * (M - 1) * d;       // bessel, Rw, A
+    b += nm * (M - 1) * 12 * d + (M - 1) * ALPS_KFAR * d + nm * ALPS_KFAR * 12 * d;        // V, X, mom
+    b += nm * 30 * d;                                                                      // lmom
+    if (S.sp.relat) {
+      size_t nf = (size_t)(c->sys.ngamma + 1) * (c->sys.npparbar + 1);
+      b += 3 * nf * d + (nm + 1) * nf * d + (c->sys.ngamma + 1) * 8;
+    }
+  }
+  b += c->batch_cap * 2 * sizeof(double2) + c->ext_cap * sizeof(double2);
+  b += (c->part_cap + c->low_cap + c->items_cap + c->rel_cap + c->bm_cap) * sizeof(double2);
+  return b;
+}
+
+}  // extern "C"
+
+struct alps_server {
+  size_t budget = 0;
+  int max_active = 64;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::pair<int64_t, alps_request*>> queue;
+  std::map<int64_t, alps_request*> pending;  // submitted, not finished
+  std::map<int64_t, int> finished;           // id -> status
+  int64_t next_id = 1;
+  bool stop = false;
+  std::thread th;
+  // statistics
+  int64_t rounds = 0;
+  int peak_active = 0;
+  size_t peak_bytes = 0;
+  std::map<int64_t, double> t_submit;
+
+  void run();
+  void start_request(Active& a);
+  void advance(Active& a);
+  void finish(Active& a, int status);
+};
+
+// Sets up a newly admitted request: root finders of a polish, first row of
+// a scan (a map needs nothing).
+void alps_server::start_request(Active& a) {
+  alps_request* rq = a.rq;
+  alps_ctx* c = rq->ctx;
+  rq->rounds = 0;
+  if (rq->kind == ALPS_REQ_POLISH) {
+    a.rm.resize(rq->n);
+    a.want.resize(rq->n);
+    a.idx.resize(rq->n);
+    for (int r = 0; r < rq->n; ++r) {
+      a.idx[r] = r;
+      a.want[r] = a.rm[r].start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im));
+    }
+    return;
+  }
+  if (rq->kind == ALPS_REQ_MAP) return;
+  // SCAN: the first row is the starting point (om_scan :2318-2331)
+  const alps_scan_def& sc = rq->scan;
+  a.nt = sc.n_out * sc.n_res;
+  a.kp0 = a.kperp = c->kperp;
+  a.kz0 = a.kpar = c->kpar;
+  a.th0 = std::atan(a.kp0 / a.kz0);
+  a.k0 = std::sqrt(a.kp0 * a.kp0 + a.kz0 * a.kz0);
+  a.jump.assign(rq->n, 1);
+  for (int r = 0; r < rq->n; ++r) {
+    double* row = rq->scan_rows + (size_t)r * 4;
+    row[0] = a.kperp;
+    row[1] = a.kpar;
+    row[2] = rq->om[r].re;
+    row[3] = rq->om[r].im;
+  }
+  a.out_row = 1;
+  a.it = 0;
+}
+
+void alps_server::finish(Active& a, int status) {
+  a.rq->status = status;
+  a.rq->latency_ms = now_ms() - a.t0;
+  std::lock_guard<std::mutex> lk(mu);
+  finished[a.id] = status;
+  pending.erase(a.id);
+  t_submit.erase(a.id);
+  cv_done.notify_all();
+}
+
+// Moves a request forward after its batch (or with no batch this round).
+void alps_server::advance(Active& a) {
+  alps_request* rq = a.rq;
+  if (rq->kind == ALPS_REQ_MAP) return;
+  // feed determinants back
+  size_t k = 0;
+  std::vector<cplx> got;
+  for (size_t q = 0; q < a.rm.size(); ++q) {
+    if (a.want[q].empty()) continue;
+    got.clear();
+    for (size_t w = 0; w < a.want[q].size(); ++w, ++k) got.push_back(cplx(a.bD[k].re, a.bD[k].im));
+    a.want[q] = a.rm[q].step(got);
+  }
+}
+
+void alps_server::run() {
+  std::vector<Active*> active;
+  size_t in_use = 0;
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      // admission: FIFO, one request per context, within the budget
+      for (auto itq = queue.begin(); itq != queue.end() && (int)active.size() < max_active;) {
+        alps_request* rq = itq->second;
+        bool busy = false;
+        for (Active* a : active) busy = busy || a->rq->ctx == rq->ctx;
+        size_t nb = (rq->kind == ALPS_REQ_MAP) ? (size_t)rq->map.nr * rq->map.ni : (size_t)2 * std::max(rq->n, 1);
+        size_t need = ctx_device_bytes(rq->ctx) + batch_bytes(rq->ctx, nb);
+        if (busy || (in_use + need > budget && !active.empty())) {
+          ++itq;
+          continue;
+        }
+        Active* a = new Active();
+        a->rq = rq;
+        a->id = itq->first;
+        a->t0 = t_submit[itq->first];
+        a->bytes = need;
+        in_use += need;
+        active.push_back(a);
+        itq = queue.erase(itq);
+      }
+      peak_active = std::max(peak_active, (int)active.size());
+      peak_bytes = std::max(peak_bytes, in_use);
+      if (active.empty()) {
+        if (stop && queue.empty()) return;
+        cv_work.wait(lk);
+        continue;
+      }
+    }
+    // start newly admitted requests (outside the lock: set_k may run)
+    for (Active* a : active)
+      if (!a->started) {
+        start_request(*a);
+        a->started = true;
+      }
+    // SCAN: start the next k step when the previous one is done
+    for (Active* a : active) {
+      if (a->rq->kind != ALPS_REQ_SCAN) continue;
+      bool busy = false;
+      for (auto& w : a->want) busy = busy || !w.empty();
+      if (busy || a->it > a->nt) continue;
+      alps_request* rq = a->rq;
+      alps_ctx* c = rq->ctx;
+      if (!a->rm.empty()) {
+        // the step just polished: NaN and root-too-close checks, output row (:2540-2580)
+        for (size_t q = 0; q < a->rm.size(); ++q) {
+          int r = a->idx[q];
+          cplx o = a->rm[q].root();
+          rq->om[r] = alps_complex{o.real(), o.imag()};
+          double re = o.real();
+          if (std::fabs(re) >= 1.79769313486231571e308 || re != re) a->jump[r] = 0;
+          for (int imm = 0; imm < r; ++imm)
+            if (std::hypot(rq->om[r].re - rq->om[imm].re, rq->om[r].im - rq->om[imm].im) < c->sys.D_gap) {
+              rq->om[r] = alps_complex{0.0, 0.0};
+              a->jump[r] = 0;
+            }
+          if (a->it % rq->scan.n_res == 0) {
+            double* row = rq->scan_rows + ((size_t)a->out_row * rq->n + r) * 4;
+            row[0] = a->kperp;
+            row[1] = a->kpar;
+            row[2] = rq->om[r].re;
+            row[3] = rq->om[r].im;
+          }
+        }
+        if (a->it % rq->scan.n_res == 0) ++a->out_row;
+        a->rm.clear();
+        a->want.clear();
+        a->idx.clear();
+      }
+      a->it += 1;
+      if (a->it > a->nt) continue;
+      scan_k(rq->scan, a->it, a->kp0, a->kz0, a->th0, a->k0, a->kperp, a->kpar);
+      int st = alps_set_k(c, a->kperp, a->kpar);
+      if (st) {
+        a->it = a->nt + 2;
+        a->rq->status = st;
+        continue;
+      }
+      bool any = false;
+      for (int r = 0; r < rq->n; ++r) any = any || a->jump[r];
+      if (!any) {
+        a->it = a->nt + 2;
+        a->rq->status = ALPS_E_ROOTS_DIVERGED;
+        continue;
+      }
+      for (int r = 0; r < rq->n; ++r) {
+        if (!a->jump[r]) continue;
+        a->idx.push_back(r);
+        a->rm.emplace_back();
+        a->want.push_back(a->rm.back().start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im)));
+      }
+    }
+    // this round's batches, launched on every context before any wait
+    for (Active* a : active) {
+      a->bom.clear();
+      alps_request* rq = a->rq;
+      if (rq->kind == ALPS_REQ_MAP) {
+        if (!a->map_done) map_lattice(&rq->map, a->bom);
+      } else {
+        for (auto& w : a->want)
+          for (auto& o : w) a->bom.push_back(alps_complex{o.real(), o.imag()});
+      }
+      int n = (int)a->bom.size();
+      a->bD.resize(n);
+      if (n == 0) continue;
+      alps_ctx* c = rq->ctx;
+      int st = ctx_ensure_batch(c, n, false);
+      if (!st) {
+        std::memcpy(c->h_pinned, a->bom.data(), (size_t)n * sizeof(double2));
+        if (cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream) !=
+            cudaSuccess)
+          st = ALPS_E_CUDA;
+      }
+      if (!st) st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream);
+      if (!st && cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost,
+                                 c->stream) != cudaSuccess)
+        st = ALPS_E_CUDA;
+      if (st) a->rq->status = st;
+      rq->rounds += 1;
+    }
+    ++rounds;
+    for (Active* a : active) {
+      int n = (int)a->bom.size();
+      if (n == 0) continue;
+      alps_ctx* c = a->rq->ctx;
+      int st = (cudaStreamSynchronize(c->stream) == cudaSuccess) ? ALPS_OK : ALPS_E_CUDA;
+      if (!st) st = ctx_check_flags(c);
+      if (st && !a->rq->status) a->rq->status = st;
+      std::memcpy(a->bD.data(), c->h_pinned + n, (size_t)n * sizeof(double2));
+      if (a->rq->kind == ALPS_REQ_MAP) {
+        map_finish(n, a->bD.data(), a->rq->map_cal, a->rq->map_val);
+        a->map_done = true;
+      } else {
+        advance(*a);
+      }
+    }
+    // release finished requests
+    for (size_t q = 0; q < active.size();) {
+      Active* a = active[q];
+      alps_request* rq = a->rq;
+      bool done = rq->status != ALPS_OK;
+      if (!done) {
+        if (rq->kind == ALPS_REQ_MAP) {
+          done = a->map_done;
+        } else if (rq->kind == ALPS_REQ_POLISH) {
+          done = true;
+          for (auto& w : a->want) done = done && w.empty();
+          if (done)
+            for (size_t k = 0; k < a->rm.size(); ++k) {
+              cplx o = a->rm[k].root();
+              rq->om[k] = alps_complex{o.real(), o.imag()};
+              if (rq->iters) rq->iters[k] = a->rm[k].iters();
+            }
+        } else {
+          done = a->it > a->nt;
+        }
+      }
+      if (done) {
+        finish(*a, rq->status);
+        in_use -= a->bytes;
+        delete a;
+        active.erase(active.begin() + q);
+      } else {
+        ++q;
+      }
+    }
+  }
+}
+
+extern "C" {
+
+int alps_server_create(size_t hbm_budget, int max_active, alps_server** out) {
+  if (!out) return ALPS_E_INVALID;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return ALPS_E_NO_DEVICE;
+  alps_server* s = new alps_server();
+  if (hbm_budget == 0) {
+    size_t fr = 0, tot = 0;
+    ALPS_CUDA_TRY(cudaMemGetInfo(&fr, &tot));
+    hbm_budget = (size_t)(0.9 * (double)fr);
+  }
+  s->budget = hbm_budget;
+  s->max_active = max_active > 0 ? max_active : 64;
+  s->th = std::thread([s]() { s->run(); });
+  *out = s;
+  return ALPS_OK;
+}
+
+void alps_server_destroy(alps_server* s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    s->cv_work.notify_all();
+  }
+  if (s->th.joinable()) s->th.join();
+  delete s;
+}
+
+int alps_server_submit(alps_server* s, alps_request* rq, int64_t* id) {
+  if (!s || !rq || !rq->ctx || !rq->ctx->kset) return ALPS_E_INVALID;
+  if (rq->kind == ALPS_REQ_POLISH && (rq->n < 0 || (rq->n > 0 && !rq->om))) return ALPS_E_INVALID;
+  if (rq->kind == ALPS_REQ_MAP && (rq->map.nr < 1 || rq->map.ni < 1)) return ALPS_E_INVALID;
+  if (rq->kind == ALPS_REQ_SCAN &&
+      (rq->n < 1 || !rq->om || !rq->scan_rows || rq->scan.n_out < 0 || rq->scan.n_res < 1 || rq->scan.type_s < 0 ||
+       rq->scan.type_s > 4))
+    return ALPS_E_INVALID;
+  if (rq->kind < ALPS_REQ_POLISH || rq->kind > ALPS_REQ_SCAN) return ALPS_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->stop) return ALPS_E_INVALID;
+  rq->status = ALPS_OK;
+  rq->latency_ms = 0.0;
+  int64_t k = s->next_id++;
+  s->t_submit[k] = now_ms();
+  s->queue.push_back({k, rq});
+  s->pending[k] = rq;
+  if (id) *id = k;
+  s->cv_work.notify_all();
+  return ALPS_OK;
+}
+
+int alps_server_poll(alps_server* s, int64_t id, int* done) {
+  if (!s || !done) return ALPS_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (s->finished.count(id)) {
+    *done = 1;
+    return ALPS_OK;
+  }
+  if (!s->pending.count(id)) return ALPS_E_INVALID;
+  *done = 0;
+  return ALPS_OK;
+}
+
+int alps_server_wait(alps_server* s, int64_t id) {
+  if (!s) return ALPS_E_INVALID;
+  std::unique_lock<std::mutex> lk(s->mu);
+  if (!s->finished.count(id) && !s->pending.count(id)) return ALPS_E_INVALID;
+  s->cv_done.wait(lk, [&]() { return s->finished.count(id) > 0; });
+  return s->finished[id];
+}
+
+int alps_server_stats(alps_server* s, int64_t* rounds, int* peak_active, size_t* peak_bytes) {
+  if (!s) return ALPS_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->mu);
+  if (rounds) *rounds = s->rounds;
+  if (peak_active) *peak_active = s->peak_active;
+  if (peak_bytes) *peak_bytes = s->peak_bytes;
+  return ALPS_OK;
+}
+
+}  // extern "C"

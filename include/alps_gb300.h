@@ -285,6 +285,60 @@ typedef struct alps_input {
   alps_scan_def scan[ALPS_MAX_SCANS];
 } alps_input;
 
+/* ------------------------------------------------------------------------
+ * Request server: continuous batching of root solves, k scans and maps on
+ * many plasmas.  No reference counterpart (the reference runs one plasma
+ * per MPI job); each request does what the named reference driver does for
+ * its plasma.
+ *
+ * A background thread keeps a set of active requests.  In every round, each
+ * active request puts the frequencies its root finders (or its lattice)
+ * need into one batch on its context's stream; the batches of all active
+ * requests run on the GPU together; the thread then feeds the determinants
+ * back and advances every request.  Requests that arrive while others run
+ * are admitted between rounds, while their estimated device footprint (the
+ * context's tables and the largest batch they will launch) fits the budget
+ * and their context is not serving another request.  Every request on a
+ * context evaluates exactly the kernels it would evaluate alone, so results
+ * do not depend on what else is in flight.
+ * ------------------------------------------------------------------------ */
+typedef struct alps_server alps_server;
+
+#define ALPS_REQ_POLISH 0  /* refine_guess: polish n roots (secant method of the context) */
+#define ALPS_REQ_MAP 1     /* map_search lattice: det D with the reference's sentinels   */
+#define ALPS_REQ_SCAN 2    /* om_scan: k steps with root following                       */
+
+typedef struct alps_request {
+  int kind;                 /* ALPS_REQ_*                                                 */
+  alps_ctx* ctx;            /* prepared plasma with k set; one request at a time per ctx */
+  int n;                    /* POLISH, SCAN: number of roots                               */
+  alps_complex* om;         /* POLISH, SCAN: guesses in, roots out (host memory)           */
+  int* iters;               /* POLISH: iterations per root (may be NULL)                   */
+  alps_map_params map;      /* MAP                                                        */
+  alps_complex* map_cal;    /* MAP out: nr*ni det D with sentinels (may be NULL)           */
+  double* map_val;          /* MAP out: nr*ni log10 |det D| with sentinels (may be NULL)   */
+  alps_scan_def scan;       /* SCAN: type, steps and diff/diff2 as alps_read_input sets    */
+  double* scan_rows;        /* SCAN out: [(n_out+1) * n * 4] kperp, kpar, Re, Im           */
+  int status;               /* out: ALPS_OK or an error code                               */
+  double latency_ms;        /* out: submit to completion                                   */
+  int rounds;               /* out: batched rounds the request took part in                */
+} alps_request;
+
+/* hbm_budget: bytes of device memory requests may hold at once (0: 90 % of
+ * the free memory at creation); max_active: requests in flight (0: 64). */
+int alps_server_create(size_t hbm_budget, int max_active, alps_server** out);
+/* Waits for every submitted request, then stops the thread. */
+void alps_server_destroy(alps_server* srv);
+/* Queues a request (the struct and its buffers must stay valid until it is
+ * done) and returns its id. */
+int alps_server_submit(alps_server* srv, alps_request* req, int64_t* id);
+/* *done = 1 once the request has finished (its status and outputs are set). */
+int alps_server_poll(alps_server* srv, int64_t id, int* done);
+/* Blocks until the request has finished; returns its status. */
+int alps_server_wait(alps_server* srv, int64_t id);
+/* Rounds run, peak requests in flight and peak estimated footprint so far. */
+int alps_server_stats(alps_server* srv, int64_t* rounds, int* peak_active, size_t* peak_bytes);
+
 /* Parses an ALPS input file (init_param + scan_read, src/ALPS_io.f90:46-552):
  * defaults of src/ALPS_var.f90, Fortran literals (1.d-2, .true., T, 'str'),
  * `!` comments.  Missing required namelists return ALPS_E_NAMELIST. */

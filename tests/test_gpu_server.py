@@ -1,0 +1,97 @@
+"""The request server (alps_server_*): continuous batching of root
+polishes, k scans and maps over several plasmas.  Every result must equal
+the same request run alone through the single-plasma entry points, bit for
+bit, whatever else is in flight; admission by device footprint only delays
+requests."""
+import numpy as np
+import pytest
+
+from alps_gb300 import _abi, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def api():
+    import torch
+    assert torch.cuda.is_available(), "GPU tests need a CUDA device"
+    from alps_gb300 import api as A
+    return A
+
+
+def _plasmas(api, n=6, seed=11):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        w = workloads.uneven_plasma(rng, grid=(32, 64) if i % 2 else (48, 96))
+        s, sp = workloads.build_uneven(w, api.generate_f0)
+        G = api.Plasma(s, sp, precision="mixed" if i % 3 == 0 else "fp64")
+        G.set_k(*w["k"])
+        out.append(G)
+    return out
+
+
+def _map(nr=24, ni=16):
+    mp = _abi.alps_map_params()
+    mp.omi, mp.omf, mp.gami, mp.gamf = 0.05, 2.0, -0.3, 0.05
+    mp.nr, mp.ni = nr, ni
+    return mp
+
+
+GUESSES = [0.3 - 0.02j, 1.1 - 0.05j]
+
+
+def test_mixed_stream_equals_alone(api):
+    P = _plasmas(api)
+    # alone
+    alone_roots = [P[i].secant(GUESSES)[0] for i in range(4)]
+    alone_map = P[4].map_search(_map())
+    r0 = P[5].secant([0.5 - 0.01j])[0]
+    sc = api.scan_def(4, 0.0, P[5].kpar * 1.5, True, 4, 1, P[5].kperp, P[5].kpar)
+    alone_scan = P[5].om_scan(4, 0.0, P[5].kpar * 1.5, True, 4, 1, r0)
+    P[5].set_k(P[5].kperp, alone_scan[0][0, 0, 1])  # back to the scan's start
+    # in the mix
+    srv = api.Server()
+    reqs = [srv.polish(P[i], GUESSES) for i in range(4)]
+    rmap = srv.map(P[4], _map())
+    rscan = srv.scan(P[5], sc, r0)
+    got = [r.wait() for r in reqs]
+    cal, val = rmap.wait()
+    rows, _ = rscan.wait()
+    for a, b in zip(got, alone_roots):
+        assert np.array_equal(a, b, equal_nan=True)
+    assert np.array_equal(cal, alone_map[1], equal_nan=True)
+    assert np.array_equal(val, alone_map[2], equal_nan=True)
+    assert np.array_equal(rows, alone_scan[0], equal_nan=True)
+    st = srv.stats()
+    assert st["peak_active"] >= 2
+    assert all(r.latency_ms > 0 for r in reqs)
+    srv.close()
+
+
+def test_budget_serialises_but_keeps_results(api):
+    P = _plasmas(api, n=3, seed=12)
+    alone = [G.secant(GUESSES)[0] for G in P]
+    srv = api.Server(hbm_budget=1)  # below any request: one at a time
+    reqs = [srv.polish(G, GUESSES) for G in P]
+    for r, a in zip(reqs, alone):
+        assert np.array_equal(r.wait(), a, equal_nan=True)
+    assert srv.stats()["peak_active"] == 1
+    srv.close()
+
+
+def test_requests_arriving_while_others_run(api):
+    """Continuous batching: requests submitted after the first ones started
+    join later rounds and still match their lone runs."""
+    P = _plasmas(api, n=4, seed=13)
+    alone = [G.secant(GUESSES)[0] for G in P]
+    srv = api.Server()
+    first = [srv.polish(P[0], GUESSES), srv.polish(P[1], GUESSES)]
+    later = []
+    while not first[0].done() and len(later) < 2:
+        later.append(srv.polish(P[2 + len(later)], GUESSES))
+    later += [srv.polish(P[2 + k], GUESSES) for k in range(len(later), 2)]
+    res = [r.wait() for r in first + later]
+    for a, b in zip(res, alone):
+        assert np.array_equal(a, b, equal_nan=True)
+    srv.close()
