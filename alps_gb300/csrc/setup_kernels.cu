@@ -61,9 +61,10 @@ __global__ void k_int_ee(const double* __restrict__ g2, const double* __restrict
 }
 
 // ---------------------------------------------------------------------------
-// Levenberg-Marquardt fit of the analytic continuation.  One thread walks the
+// Levenberg-Marquardt fit of the analytic continuation.  One warp walks the
 // iperp rows of one species in order (each row starts from the previous
-// result, src/ALPS_analyt.f90:518), with the reference's sums in its order.
+// result, src/ALPS_analyt.f90:518); within a row the lanes share the points
+// and the entries of J^T J, and every sum keeps the reference's order.
 // ---------------------------------------------------------------------------
 struct FitArgs {
   int N, M, nf, log_fit;
@@ -190,7 +191,12 @@ __device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, 
 // cone (src/ALPS_analyt.f90:546-607).
 __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double* __restrict__ pperp,
                          const double* __restrict__ ppar, double* fit, double* scratch, int* status) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  // one warp: the points of a row are spread over the lanes; the scalar
+  // control flow (LM step, LU, parameter update) runs identically in every
+  // lane, and every sum over points runs in the reference's order
+  if (blockIdx.x != 0) return;
+  const int lane = threadIdx.x;
+  __shared__ double Am_sh[FIT_MAXP * FIT_MAXP], jr_sh[FIT_MAXP];
   int nf = a.nf, N = a.rel ? a.ng : a.N;
   int n_params = 0;
   for (int f = 0; f < nf; ++f) n_params += fit_nparams(a, a.fit_type[f]);
@@ -200,13 +206,14 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
   int maxpts = a.rel ? a.np : a.M;
   double* resid = scratch + (size_t)(maxpts + 1) * FIT_MAXP;
   if (!a.rel && (1 + a.M) < n_params) {
-    *status = ALPS_E_FIT_POINTS;
+    if (lane == 0) *status = ALPS_E_FIT_POINTS;
     return;
   }
   for (int iperp = 0; iperp <= N; ++iperp) {
-    if (iperp != 0)
+    if (iperp != 0 && lane == 0)
       for (int ip = 0; ip < 5; ++ip)
         for (int f = 0; f < nf; ++f) fit[(iperp * 5 + ip) * nf + f] = fit[((iperp - 1) * 5 + ip) * nf + f];
+    __syncwarp();
     int par_ind = 0, nJT = 0;
     for (int k = 0; k < n_params; ++k) mask[k] = true;
     for (int ifit = 1; ifit <= nf; ++ifit) {
@@ -260,8 +267,7 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
       bool converged = false;
       while (!converged) {
         counter++;
-        LSQ = 0.0;
-        for (int j = 0; j <= npts; ++j) {
+        for (int j = lane; j <= npts; j += 32) {
           double* Jc = JT + (size_t)j * FIT_MAXP;
           fit_jacobian(a, params, iperp, xperp, xpar(j), Jc);
           double fv = fit_value_real(a, params, xperp, xpar(j));
@@ -271,19 +277,27 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
           } else {
             resid[j] = gval(j) - fv;
           }
-          LSQ = LSQ + resid[j] * resid[j];
         }
+        __syncwarp();
+        LSQ = 0.0;
+        for (int j = 0; j <= npts; ++j) LSQ = LSQ + resid[j] * resid[j];
         double Am[FIT_MAXP * FIT_MAXP], jr[FIT_MAXP];
-        for (int k = 0; k < nJT; ++k) {
-          for (int l = 0; l < nJT; ++l) {
-            double acc = 0.0;
-            for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * JT[(size_t)j * FIT_MAXP + l];
-            Am[k + nJT * l] = acc;
-          }
+        for (int t = lane; t < nJT * nJT + nJT; t += 32) {
           double acc = 0.0;
-          for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * resid[j];
-          jr[k] = acc;
+          if (t < nJT * nJT) {
+            int k = t % nJT, l = t / nJT;
+            for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * JT[(size_t)j * FIT_MAXP + l];
+            Am_sh[t] = acc;
+          } else {
+            int k = t - nJT * nJT;
+            for (int j = 0; j <= npts; ++j) acc += JT[(size_t)j * FIT_MAXP + k] * resid[j];
+            jr_sh[k] = acc;
+          }
         }
+        __syncwarp();
+        for (int t = 0; t < nJT * nJT; ++t) Am[t] = Am_sh[t];
+        for (int k = 0; k < nJT; ++k) jr[k] = jr_sh[k];
+        __syncwarp();
         for (int k = 0; k < nJT; ++k) Am[k + nJT * k] = Am[k + nJT * k] + lambda_fit * Am[k + nJT * k];
         // LU with partial pivoting (dgetrf), then inverse (dgetri) times JT*r
         int piv[FIT_MAXP];
@@ -307,7 +321,7 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
           }
         }
         if (singular) {
-          *status = ALPS_E_SINGULAR;
+          if (lane == 0) *status = ALPS_E_SINGULAR;
           return;
         }
         double inv[FIT_MAXP * FIT_MAXP];
@@ -336,12 +350,14 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
         int l = 0;
         for (int k = 0; k < n_params; ++k)
           if (mask[k]) params[k] = params[k] + delta[l++];
-        LSQnew = 0.0;
-        for (int j = 0; j <= npts; ++j) {
+        for (int j = lane; j <= npts; j += 32) {
           double fv = fit_value_real(a, params, xperp, xpar(j));
-          double r = a.log_fit ? gval(j) - log(fv) : gval(j) - fv;
-          LSQnew = LSQnew + r * r;
+          resid[j] = a.log_fit ? gval(j) - log(fv) : gval(j) - fv;
         }
+        __syncwarp();
+        LSQnew = 0.0;
+        for (int j = 0; j <= npts; ++j) LSQnew = LSQnew + resid[j] * resid[j];
+        __syncwarp();
         if (LSQnew > LSQ) {
           l = 0;
           for (int k = 0; k < n_params; ++k)
@@ -355,11 +371,12 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
       }
     }
     par_ind = 0;
-    for (int ifit = 1; ifit <= nf; ++ifit) {
+    for (int ifit = 1; ifit <= nf && lane == 0; ++ifit) {
       int np = fit_nparams(a, a.fit_type[ifit - 1]);
       for (int k = 0; k < np; ++k) fit[(iperp * 5 + k) * nf + ifit - 1] = params[ifit + par_ind + k - 1];
       par_ind += np - 1;
     }
+    __syncwarp();
   }
 }
 
