@@ -27,7 +27,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-from alps_gb300 import workloads  # noqa: E402
+from alps_gb300 import _abi, workloads  # noqa: E402
 from alps_gb300.sharding import shard_range  # noqa: E402
 
 METRIC = "D(omega,k) evals/s & roots/s at <=1e-8 rel vs FP64, vs plain GPU; p50/p99 latency"
@@ -169,6 +169,72 @@ def run_reference(args, w, mp, rank, world):
     print(json.dumps(line))
 
 
+def served_stream(api, args):
+    """A served stream of the served-stream configuration's kinds, scaled to
+    a few seconds: Poisson arrivals of 70 % single-root polishes, 25 % k scans
+    (8 steps, root following) and 5 % 32x32 omega maps, each on a plasma
+    drawn from a pool of uneven-batch plasmas (1-3 species, 64x128 to
+    128x256 grids), all through one alps_server.  Returns latency
+    percentiles per kind (arrival to result) and throughput."""
+    import torch
+    rng = np.random.default_rng(5)
+    pool = []
+    for i in range(12):
+        N = (64, 96, 128)[i % 3]
+        w = workloads.uneven_plasma(rng, grid=(N, 2 * N))
+        s, sp = workloads.build_uneven(w, api.generate_f0)
+        G = api.Plasma(s, sp, precision="mixed")
+        G.set_k(*w["k"])
+        pool.append(G)
+    torch.cuda.synchronize()
+    mp = _abi.alps_map_params()
+    mp.omi, mp.omf, mp.gami, mp.gamf, mp.nr, mp.ni = 0.05, 2.0, -0.3, 0.05, 32, 32
+    srv = api.Server()
+    nreq, rate = args.served_requests, args.served_rate
+    t_arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    kinds = rng.choice(3, nreq, p=[0.70, 0.25, 0.05])
+    reqs = []
+    # a plasma's requests run in submission order; its scans alternate up
+    # and down in k_par so that k stays near the drawn value
+    kpar_now = [G.kpar for G in pool]
+    nscan = [0] * len(pool)
+    t0 = time.perf_counter()
+    for k in range(nreq):
+        wait = t_arr[k] - (time.perf_counter() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        i = int(rng.integers(len(pool)))
+        G = pool[i]
+        g = complex(rng.uniform(0.1, 1.5), -rng.uniform(0.0, 0.1))
+        if kinds[k] == 0:
+            reqs.append(("polish", srv.polish(G, [g])))
+        elif kinds[k] == 1:
+            target = kpar_now[i] * (1.3 if nscan[i] % 2 == 0 else 1.0 / 1.3)
+            sc = api.scan_def(4, 0.0, target, True, 8, 1, G.kperp, kpar_now[i])
+            kpar_now[i] = 10.0 ** (np.log10(kpar_now[i]) + sc.diff * 8)
+            nscan[i] += 1
+            reqs.append(("scan", srv.scan(G, sc, [g])))
+        else:
+            reqs.append(("map", srv.map(G, mp)))
+    for _, r in reqs:
+        r.wait()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    out = {"requests": nreq, "arrival_rate_per_s": rate, "wall_s": wall, "rounds": st["rounds"],
+           "peak_in_flight": st["peak_active"], "peak_footprint_bytes": st["peak_bytes"], "latency_ms": {}}
+    for kind in ("polish", "scan", "map"):
+        lat = [r.latency_ms for kk, r in reqs if kk == kind]
+        if lat:
+            out["latency_ms"][kind] = {"count": len(lat), "p50": float(np.percentile(lat, 50)),
+                                       "p99": float(np.percentile(lat, 99))}
+    nroots = sum(1 for kk, _ in reqs if kk == "polish") + 8 * sum(1 for kk, _ in reqs if kk == "scan")
+    out["roots_per_s"] = nroots / wall
+    out["note"] = ("latency from submission to result, requests overlapping on the GPU; "
+                   "the pool's plasmas are prepared before the stream starts")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,6 +242,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nr", type=int, default=512)
+    ap.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
+    ap.add_argument("--served-requests", type=int, default=400)
+    ap.add_argument("--served-rate", type=float, default=400.0, help="Poisson arrival rate of the served stream")
     ap.add_argument("--ni", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
@@ -306,6 +375,8 @@ def main():
     G.set_precision("mixed")
     root_rel = float(np.max(np.abs(roots - roots_plain) / np.maximum(np.abs(roots_plain), 1e-300)))
 
+    served = None if args.no_served else served_stream(api, args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import pyoracle as po
@@ -330,7 +401,8 @@ def main():
                 "roots": {"count": len(roots), "roots_per_s": len(roots) / t_roots, "iterations": iters,
                           "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
                                          "p99": float(np.percentile(lat, 99)) if lat else None},
-                          "roots": [[r.real, r.imag] for r in roots]}}
+                          "roots": [[r.real, r.imag] for r in roots]},
+                "served": served}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()
