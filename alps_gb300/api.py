@@ -394,7 +394,7 @@ class Server:
     def stats(self):
         r, a, b = C.c_int64(), C.c_int(), C.c_size_t()
         check(lib().alps_server_stats(self._h, C.byref(r), C.byref(a), C.byref(b)), "alps_server_stats")
-        return {"rounds": r.value, "peak_active": a.value, "peak_bytes": b.value}
+        return {"batches": r.value, "peak_active": a.value, "peak_bytes": b.value}
 
     def close(self):
         if getattr(self, "_h", None):

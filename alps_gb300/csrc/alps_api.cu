@@ -154,6 +154,8 @@ void alps_destroy(alps_ctx* c) {
   cudaFree(c->d_bm);
   cudaFree(c->d_flags);
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
+  if (c->h_flag) cudaFreeHost(c->h_flag);
+  if (c->ev_done) cudaEventDestroy(c->ev_done);
   for (auto& ev : c->ev_pending)
     for (auto e : ev) cudaEventDestroy(e);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
@@ -415,6 +417,8 @@ int ctx_ensure_batch(alps_ctx* c, int n, bool ext) {
     ALPS_CUDA_TRY(cudaMallocHost(&c->h_pinned, need_pin * sizeof(double2)));
     c->pinned_cap = need_pin;
   }
+  if (!c->h_flag) ALPS_CUDA_TRY(cudaMallocHost(&c->h_flag, sizeof(int)));
+  if (!c->ev_done) ALPS_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));
   if (ext) {
     size_t ne = (size_t)n * (c->sys.nspec * 36 + 9);
     if (ne > c->ext_cap) {

@@ -193,6 +193,8 @@ struct alps_ctx {
   // host pinned staging
   double2* h_pinned = nullptr;
   size_t pinned_cap = 0;
+  int* h_flag = nullptr;                // pinned copy of the device error flags
+  cudaEvent_t ev_done = nullptr;        // completion of an asynchronous batch
 };
 
 // ---------------------------------------------------------------------------

@@ -1,14 +1,17 @@
 // server.cu -- continuous batching of root solves, k scans and maps over
 // many plasmas (alps_server_*, declared in include/alps_gb300.h).
 //
-// One host thread runs rounds.  In a round every active request contributes
-// one batch of frequencies (the pending evaluations of its root finders, or
-// its whole lattice) on its own context's stream; all batches are launched
-// before any is waited for, so the kernels of different plasmas overlap on
-// the GPU.  The determinants then go back into the requests' state machines
-// (root_finders.h: the reference's secant_osc / secant / rtsec), k scans move
-// to their next step, finished requests are released, and queued requests
-// are admitted while their footprint fits the budget.
+// One host thread drives every admitted request independently: a request
+// whose context is idle puts the frequencies its root finders (or its
+// lattice) need into one batch on that context's stream and records an
+// event; the thread polls those events and, as each batch lands, feeds the
+// determinants back into the request's state machines (root_finders.h: the
+// reference's secant_osc / secant / rtsec) and launches its next batch.
+// Batches of different plasmas therefore overlap on the GPU without any
+// request waiting for a slower one.  The k steps of scans (alps_set_k, which
+// synchronises its context) run on short-lived worker threads so they do not
+// stall the others.  Queued requests are admitted while their footprint fits
+// the budget.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -16,6 +19,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <future>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -46,7 +50,12 @@ struct Active {
   double kp0 = 0, kz0 = 0, th0 = 0, k0 = 0, kperp = 0, kpar = 0;
   std::vector<char> jump;
   bool map_done = false;
-  // this round's batch
+  // progress: idle (ready for the next batch), a batch in flight, or a k
+  // step running on a worker thread
+  enum { IDLE, IN_FLIGHT, STEPPING } state = IDLE;
+  std::future<void> step;
+  int status = ALPS_OK;
+  // the batch in flight
   std::vector<alps_complex> bom, bD;
 };
 
@@ -109,7 +118,7 @@ struct alps_server {
   bool stop = false;
   std::thread th;
   // statistics
-  int64_t rounds = 0;
+  int64_t rounds = 0;  // batches launched
   int peak_active = 0;
   size_t peak_bytes = 0;
   std::map<int64_t, double> t_submit;
@@ -181,6 +190,99 @@ void alps_server::advance(Active& a) {
   }
 }
 
+// The next k step of a scan: checks and output row of the step just
+// polished (om_scan :2540-2580), alps_set_k, root finders for the roots
+// still followed.  Runs on a worker thread; touches only this request.
+static void scan_step(Active* a) {
+  alps_request* rq = a->rq;
+  alps_ctx* c = rq->ctx;
+  if (!a->rm.empty()) {
+    for (size_t q = 0; q < a->rm.size(); ++q) {
+      int r = a->idx[q];
+      cplx o = a->rm[q].root();
+      rq->om[r] = alps_complex{o.real(), o.imag()};
+      double re = o.real();
+      if (std::fabs(re) >= 1.79769313486231571e308 || re != re) a->jump[r] = 0;
+      for (int imm = 0; imm < r; ++imm)
+        if (std::hypot(rq->om[r].re - rq->om[imm].re, rq->om[r].im - rq->om[imm].im) < c->sys.D_gap) {
+          rq->om[r] = alps_complex{0.0, 0.0};
+          a->jump[r] = 0;
+        }
+      if (a->it % rq->scan.n_res == 0) {
+        double* row = rq->scan_rows + ((size_t)a->out_row * rq->n + r) * 4;
+        row[0] = a->kperp;
+        row[1] = a->kpar;
+        row[2] = rq->om[r].re;
+        row[3] = rq->om[r].im;
+      }
+    }
+    if (a->it % rq->scan.n_res == 0) ++a->out_row;
+    a->rm.clear();
+    a->want.clear();
+    a->idx.clear();
+  }
+  a->it += 1;
+  if (a->it > a->nt) return;
+  scan_k(rq->scan, a->it, a->kp0, a->kz0, a->th0, a->k0, a->kperp, a->kpar);
+  int st = alps_set_k(c, a->kperp, a->kpar);
+  if (st) {
+    a->status = st;
+    return;
+  }
+  bool any = false;
+  for (int r = 0; r < rq->n; ++r) any = any || a->jump[r];
+  if (!any) {
+    a->status = ALPS_E_ROOTS_DIVERGED;
+    return;
+  }
+  for (int r = 0; r < rq->n; ++r) {
+    if (!a->jump[r]) continue;
+    a->idx.push_back(r);
+    a->rm.emplace_back();
+    a->want.push_back(a->rm.back().start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im)));
+  }
+}
+
+// Launches the request's next batch on its context's stream; ALPS_OK with
+// nothing launched when it has nothing to evaluate.
+static int launch(Active* a) {
+  alps_request* rq = a->rq;
+  a->bom.clear();
+  if (rq->kind == ALPS_REQ_MAP) {
+    if (!a->map_done) map_lattice(&rq->map, a->bom);
+  } else {
+    for (auto& w : a->want)
+      for (auto& o : w) a->bom.push_back(alps_complex{o.real(), o.imag()});
+  }
+  int n = (int)a->bom.size();
+  a->bD.resize(n);
+  if (n == 0) return ALPS_OK;
+  alps_ctx* c = rq->ctx;
+  int st = ctx_ensure_batch(c, n, false);
+  if (st) return st;
+  std::memcpy(c->h_pinned, a->bom.data(), (size_t)n * sizeof(double2));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  if ((st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream))) return st;
+  ALPS_CUDA_TRY(
+      cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(c->h_flag, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaEventRecord(c->ev_done, c->stream));
+  rq->rounds += 1;
+  a->state = Active::IN_FLIGHT;
+  return ALPS_OK;
+}
+
+// True once the request has nothing left to do.
+static bool finished_work(Active* a) {
+  alps_request* rq = a->rq;
+  if (a->status != ALPS_OK) return true;
+  if (rq->kind == ALPS_REQ_MAP) return a->map_done;
+  if (rq->kind == ALPS_REQ_SCAN) return a->it > a->nt;
+  for (auto& w : a->want)
+    if (!w.empty()) return false;
+  return true;
+}
+
 void alps_server::run() {
   std::vector<Active*> active;
   size_t in_use = 0;
@@ -215,143 +317,81 @@ void alps_server::run() {
         continue;
       }
     }
-    // start newly admitted requests (outside the lock: set_k may run)
-    for (Active* a : active)
+    bool progressed = false;
+    for (Active* a : active) {
+      alps_request* rq = a->rq;
       if (!a->started) {
         start_request(*a);
         a->started = true;
       }
-    // SCAN: start the next k step when the previous one is done
-    for (Active* a : active) {
-      if (a->rq->kind != ALPS_REQ_SCAN) continue;
-      bool busy = false;
-      for (auto& w : a->want) busy = busy || !w.empty();
-      if (busy || a->it > a->nt) continue;
-      alps_request* rq = a->rq;
-      alps_ctx* c = rq->ctx;
-      if (!a->rm.empty()) {
-        // the step just polished: NaN and root-too-close checks, output row (:2540-2580)
-        for (size_t q = 0; q < a->rm.size(); ++q) {
-          int r = a->idx[q];
-          cplx o = a->rm[q].root();
-          rq->om[r] = alps_complex{o.real(), o.imag()};
-          double re = o.real();
-          if (std::fabs(re) >= 1.79769313486231571e308 || re != re) a->jump[r] = 0;
-          for (int imm = 0; imm < r; ++imm)
-            if (std::hypot(rq->om[r].re - rq->om[imm].re, rq->om[r].im - rq->om[imm].im) < c->sys.D_gap) {
-              rq->om[r] = alps_complex{0.0, 0.0};
-              a->jump[r] = 0;
-            }
-          if (a->it % rq->scan.n_res == 0) {
-            double* row = rq->scan_rows + ((size_t)a->out_row * rq->n + r) * 4;
-            row[0] = a->kperp;
-            row[1] = a->kpar;
-            row[2] = rq->om[r].re;
-            row[3] = rq->om[r].im;
-          }
+      if (a->state == Active::STEPPING) {
+        if (a->step.wait_for(std::chrono::seconds(0)) != std::future_status::ready) continue;
+        a->step.get();
+        a->state = Active::IDLE;
+        progressed = true;
+      }
+      if (a->state == Active::IN_FLIGHT) {
+        cudaError_t q = cudaEventQuery(rq->ctx->ev_done);
+        if (q == cudaErrorNotReady) continue;
+        progressed = true;
+        a->state = Active::IDLE;
+        if (q != cudaSuccess) {
+          alps_set_last_cuda_error(q, "cudaEventQuery", __FILE__, __LINE__);
+          a->status = ALPS_E_CUDA;
+          continue;
         }
-        if (a->it % rq->scan.n_res == 0) ++a->out_row;
-        a->rm.clear();
-        a->want.clear();
-        a->idx.clear();
+        int f = *rq->ctx->h_flag;
+        if (f) {
+          a->status = (f & 2) ? ALPS_E_SUBLUMINAL : ALPS_E_INVALID;
+          continue;
+        }
+        int n = (int)a->bom.size();
+        std::memcpy(a->bD.data(), rq->ctx->h_pinned + n, (size_t)n * sizeof(double2));
+        if (rq->kind == ALPS_REQ_MAP) {
+          map_finish(n, a->bD.data(), rq->map_cal, rq->map_val);
+          a->map_done = true;
+        } else {
+          advance(*a);
+        }
       }
-      a->it += 1;
-      if (a->it > a->nt) continue;
-      scan_k(rq->scan, a->it, a->kp0, a->kz0, a->th0, a->k0, a->kperp, a->kpar);
-      int st = alps_set_k(c, a->kperp, a->kpar);
-      if (st) {
-        a->it = a->nt + 2;
-        a->rq->status = st;
-        continue;
+      if (a->state != Active::IDLE || a->status != ALPS_OK) continue;
+      // a scan whose step is polished moves to its next k on a worker thread
+      if (rq->kind == ALPS_REQ_SCAN && a->it <= a->nt) {
+        bool pending_evals = false;
+        for (auto& w : a->want) pending_evals = pending_evals || !w.empty();
+        if (!pending_evals) {
+          a->state = Active::STEPPING;
+          a->step = std::async(std::launch::async, scan_step, a);
+          progressed = true;
+          continue;
+        }
       }
-      bool any = false;
-      for (int r = 0; r < rq->n; ++r) any = any || a->jump[r];
-      if (!any) {
-        a->it = a->nt + 2;
-        a->rq->status = ALPS_E_ROOTS_DIVERGED;
-        continue;
-      }
-      for (int r = 0; r < rq->n; ++r) {
-        if (!a->jump[r]) continue;
-        a->idx.push_back(r);
-        a->rm.emplace_back();
-        a->want.push_back(a->rm.back().start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im)));
-      }
-    }
-    // this round's batches, launched on every context before any wait
-    for (Active* a : active) {
-      a->bom.clear();
-      alps_request* rq = a->rq;
-      if (rq->kind == ALPS_REQ_MAP) {
-        if (!a->map_done) map_lattice(&rq->map, a->bom);
-      } else {
-        for (auto& w : a->want)
-          for (auto& o : w) a->bom.push_back(alps_complex{o.real(), o.imag()});
-      }
-      int n = (int)a->bom.size();
-      a->bD.resize(n);
-      if (n == 0) continue;
-      alps_ctx* c = rq->ctx;
-      int st = ctx_ensure_batch(c, n, false);
-      if (!st) {
-        std::memcpy(c->h_pinned, a->bom.data(), (size_t)n * sizeof(double2));
-        if (cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream) !=
-            cudaSuccess)
-          st = ALPS_E_CUDA;
-      }
-      if (!st) st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream);
-      if (!st && cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost,
-                                 c->stream) != cudaSuccess)
-        st = ALPS_E_CUDA;
-      if (st) a->rq->status = st;
-      rq->rounds += 1;
-    }
-    ++rounds;
-    for (Active* a : active) {
-      int n = (int)a->bom.size();
-      if (n == 0) continue;
-      alps_ctx* c = a->rq->ctx;
-      int st = (cudaStreamSynchronize(c->stream) == cudaSuccess) ? ALPS_OK : ALPS_E_CUDA;
-      if (!st) st = ctx_check_flags(c);
-      if (st && !a->rq->status) a->rq->status = st;
-      std::memcpy(a->bD.data(), c->h_pinned + n, (size_t)n * sizeof(double2));
-      if (a->rq->kind == ALPS_REQ_MAP) {
-        map_finish(n, a->bD.data(), a->rq->map_cal, a->rq->map_val);
-        a->map_done = true;
-      } else {
-        advance(*a);
-      }
+      if (finished_work(a)) continue;
+      int st = launch(a);
+      if (st) a->status = st;
+      if (a->state == Active::IN_FLIGHT) ++rounds;
+      progressed = true;
     }
     // release finished requests
     for (size_t q = 0; q < active.size();) {
       Active* a = active[q];
-      alps_request* rq = a->rq;
-      bool done = rq->status != ALPS_OK;
-      if (!done) {
-        if (rq->kind == ALPS_REQ_MAP) {
-          done = a->map_done;
-        } else if (rq->kind == ALPS_REQ_POLISH) {
-          done = true;
-          for (auto& w : a->want) done = done && w.empty();
-          if (done)
-            for (size_t k = 0; k < a->rm.size(); ++k) {
-              cplx o = a->rm[k].root();
-              rq->om[k] = alps_complex{o.real(), o.imag()};
-              if (rq->iters) rq->iters[k] = a->rm[k].iters();
-            }
-        } else {
-          done = a->it > a->nt;
-        }
-      }
-      if (done) {
-        finish(*a, rq->status);
+      if (a->state == Active::IDLE && finished_work(a)) {
+        if (a->rq->kind == ALPS_REQ_POLISH && a->status == ALPS_OK)
+          for (size_t k = 0; k < a->rm.size(); ++k) {
+            cplx o = a->rm[k].root();
+            a->rq->om[k] = alps_complex{o.real(), o.imag()};
+            if (a->rq->iters) a->rq->iters[k] = a->rm[k].iters();
+          }
+        finish(*a, a->status);
         in_use -= a->bytes;
         delete a;
         active.erase(active.begin() + q);
+        progressed = true;
       } else {
         ++q;
       }
     }
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
 }
 

@@ -133,6 +133,13 @@ def uneven_plasma(rng, grid=None, Bessel_zero=1e-20):
     krho = 10.0 ** rng.uniform(-2.0, 1.0)
     kperp = krho / math.sqrt(beta_p)
     theta = math.radians(rng.uniform(20.0, 88.0))
+    # keep the largest Bessel argument k_perp pperp_max/|q| <= 60 (nmax up
+    # to ~80, the stated range): species with their own larger beta would
+    # otherwise push it into the thousands
+    zmax = max(kperp * d.maxP * math.sqrt(d.ms * d.tau * d.alph) / abs(q)
+               for d, (_, _, q, _) in zip(dists, species))
+    if zmax > 60.0:
+        kperp *= 60.0 / zmax
     kpar = kperp / math.tan(theta)
     sysd = _abi.system_defaults(
         nspec=nspec, nperp=N, npar=M, kperp=kperp, kpar=kpar, vA=1e-4, Bessel_zero=Bessel_zero,

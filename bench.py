@@ -173,13 +173,13 @@ def served_stream(api, args):
     """A served stream of the served-stream configuration's kinds, scaled to
     a few seconds: Poisson arrivals of 70 % single-root polishes, 25 % k scans
     (8 steps, root following) and 5 % 32x32 omega maps, each on a plasma
-    drawn from a pool of uneven-batch plasmas (1-3 species, 64x128 to
+    drawn from a pool of 32 uneven-batch plasmas (1-3 species, 64x128 to
     128x256 grids), all through one alps_server.  Returns latency
     percentiles per kind (arrival to result) and throughput."""
     import torch
     rng = np.random.default_rng(5)
     pool = []
-    for i in range(12):
+    for i in range(32):
         N = (64, 96, 128)[i % 3]
         w = workloads.uneven_plasma(rng, grid=(N, 2 * N))
         s, sp = workloads.build_uneven(w, api.generate_f0)
@@ -221,7 +221,7 @@ def served_stream(api, args):
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    out = {"requests": nreq, "arrival_rate_per_s": rate, "wall_s": wall, "rounds": st["rounds"],
+    out = {"requests": nreq, "arrival_rate_per_s": rate, "wall_s": wall, "batches": st["batches"],
            "peak_in_flight": st["peak_active"], "peak_footprint_bytes": st["peak_bytes"], "latency_ms": {}}
     for kind in ("polish", "scan", "map"):
         lat = [r.latency_ms for kk, r in reqs if kk == kind]

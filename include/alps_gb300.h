@@ -291,16 +291,17 @@ typedef struct alps_input {
  * per MPI job); each request does what the named reference driver does for
  * its plasma.
  *
- * A background thread keeps a set of active requests.  In every round, each
- * active request puts the frequencies its root finders (or its lattice)
- * need into one batch on its context's stream; the batches of all active
- * requests run on the GPU together; the thread then feeds the determinants
- * back and advances every request.  Requests that arrive while others run
- * are admitted between rounds, while their estimated device footprint (the
- * context's tables and the largest batch they will launch) fits the budget
- * and their context is not serving another request.  Every request on a
- * context evaluates exactly the kernels it would evaluate alone, so results
- * do not depend on what else is in flight.
+ * A background thread drives the active requests independently: a request
+ * whose context is idle launches one batch (the frequencies its root
+ * finders, or its lattice, need) on that context's stream; as each batch
+ * lands the determinants go back into the request's root finders and its
+ * next batch goes out, so batches of different plasmas overlap on the GPU
+ * and no request waits for a slower one.  The k steps of scans run on
+ * worker threads.  Requests that arrive while others run are admitted as
+ * soon as their estimated device footprint (the context's tables and the
+ * largest batch they will launch) fits the budget and their context is not
+ * serving another request.  Every request evaluates exactly the kernels it
+ * would evaluate alone, so results do not depend on what else is in flight.
  * ------------------------------------------------------------------------ */
 typedef struct alps_server alps_server;
 
@@ -321,7 +322,7 @@ typedef struct alps_request {
   double* scan_rows;        /* SCAN out: [(n_out+1) * n * 4] kperp, kpar, Re, Im           */
   int status;               /* out: ALPS_OK or an error code                               */
   double latency_ms;        /* out: submit to completion                                   */
-  int rounds;               /* out: batched rounds the request took part in                */
+  int rounds;               /* out: batches the request launched                           */
 } alps_request;
 
 /* hbm_budget: bytes of device memory requests may hold at once (0: 90 % of
@@ -336,7 +337,8 @@ int alps_server_submit(alps_server* srv, alps_request* req, int64_t* id);
 int alps_server_poll(alps_server* srv, int64_t id, int* done);
 /* Blocks until the request has finished; returns its status. */
 int alps_server_wait(alps_server* srv, int64_t id);
-/* Rounds run, peak requests in flight and peak estimated footprint so far. */
+/* Batches launched, peak requests in flight and peak estimated footprint so
+ * far. */
 int alps_server_stats(alps_server* srv, int64_t* rounds, int* peak_active, size_t* peak_bytes);
 
 /* Parses an ALPS input file (init_param + scan_read, src/ALPS_io.f90:46-552):
