@@ -1,17 +1,18 @@
 // server.cu -- continuous batching of root solves, k scans and maps over
 // many plasmas (alps_server_*, declared in include/alps_gb300.h).
 //
-// One host thread drives every admitted request independently: a request
-// whose context is idle puts the frequencies its root finders (or its
-// lattice) need into one batch on that context's stream and records an
-// event; the thread polls those events and, as each batch lands, feeds the
-// determinants back into the request's state machines (root_finders.h: the
-// reference's secant_osc / secant / rtsec) and launches its next batch.
-// Batches of different plasmas therefore overlap on the GPU without any
-// request waiting for a slower one.  The k steps of scans (alps_set_k, which
-// synchronises its context) run on short-lived worker threads so they do not
-// stall the others.  Queued requests are admitted while their footprint fits
-// the budget.
+// Admitted requests are grouped by context.  One host thread drives every
+// group independently: an idle group puts the frequencies all its requests
+// need next (the pending evaluations of their root finders, or a lattice)
+// into one batch on the context's stream and records an event; the thread
+// polls the events and, as each batch lands, hands every request its slice
+// of the determinants (root_finders.h: the reference's secant_osc / secant /
+// rtsec), releases the finished requests, lets queued requests on that
+// plasma join, and launches the group's next batch.  Groups of different
+// plasmas overlap on the GPU and never wait for each other.  A k scan moves
+// its context's k, so it runs alone on its context, and its k steps
+// (alps_set_k, which synchronises the context) run on worker threads.
+// Requests join while their estimated device footprint fits the budget.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -40,23 +41,31 @@ struct Active {
   int64_t id = 0;
   double t0 = 0.0;
   size_t bytes = 0;
-  bool started = false;
+  int status = ALPS_OK;
   // root finders (POLISH, SCAN)
   std::vector<RootMachine> rm;
-  std::vector<int> idx;                  // request root index of each machine
-  std::vector<std::vector<cplx>> want;   // pending evaluations per machine
+  std::vector<int> idx;                 // request root index of each machine
+  std::vector<std::vector<cplx>> want;  // pending evaluations per machine
   // SCAN state (om_scan, src/ALPS_fns.f90:2198-2600)
   int it = 0, nt = 0, out_row = 0;
   double kp0 = 0, kz0 = 0, th0 = 0, k0 = 0, kperp = 0, kpar = 0;
   std::vector<char> jump;
   bool map_done = false;
-  // progress: idle (ready for the next batch), a batch in flight, or a k
-  // step running on a worker thread
+  size_t off = 0, cnt = 0;  // slice of the group's batch in flight
+};
+
+// The requests admitted on one context.
+struct Group {
+  alps_ctx* ctx = nullptr;
+  std::vector<Active*> members;
   enum { IDLE, IN_FLIGHT, STEPPING } state = IDLE;
-  std::future<void> step;
-  int status = ALPS_OK;
-  // the batch in flight
+  std::future<void> step;  // a scan's k step
   std::vector<alps_complex> bom, bD;
+  bool has_scan() const {
+    for (Active* a : members)
+      if (a->rq->kind == ALPS_REQ_SCAN) return true;
+    return false;
+  }
 };
 
 // device bytes of a batch of n frequencies on context c (the per-batch
@@ -106,94 +115,53 @@ size_t ctx_device_bytes(const alps_ctx* c) {
 
 }  // extern "C"
 
-struct alps_server {
-  size_t budget = 0;
-  int max_active = 64;
-  std::mutex mu;
-  std::condition_variable cv_work, cv_done;
-  std::deque<std::pair<int64_t, alps_request*>> queue;
-  std::map<int64_t, alps_request*> pending;  // submitted, not finished
-  std::map<int64_t, int> finished;           // id -> status
-  int64_t next_id = 1;
-  bool stop = false;
-  std::thread th;
-  // statistics
-  int64_t rounds = 0;  // batches launched
-  int peak_active = 0;
-  size_t peak_bytes = 0;
-  std::map<int64_t, double> t_submit;
-
-  void run();
-  void start_request(Active& a);
-  void advance(Active& a);
-  void finish(Active& a, int status);
-};
+namespace {
 
 // Sets up a newly admitted request: root finders of a polish, first row of
-// a scan (a map needs nothing).
-void alps_server::start_request(Active& a) {
-  alps_request* rq = a.rq;
+// a scan (om_scan :2318-2331; a map needs nothing).
+void start_request(Active* a) {
+  alps_request* rq = a->rq;
   alps_ctx* c = rq->ctx;
   rq->rounds = 0;
   if (rq->kind == ALPS_REQ_POLISH) {
-    a.rm.resize(rq->n);
-    a.want.resize(rq->n);
-    a.idx.resize(rq->n);
+    a->rm.resize(rq->n);
+    a->want.resize(rq->n);
+    a->idx.resize(rq->n);
     for (int r = 0; r < rq->n; ++r) {
-      a.idx[r] = r;
-      a.want[r] = a.rm[r].start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im));
+      a->idx[r] = r;
+      a->want[r] = a->rm[r].start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im));
     }
     return;
   }
   if (rq->kind == ALPS_REQ_MAP) return;
-  // SCAN: the first row is the starting point (om_scan :2318-2331)
   const alps_scan_def& sc = rq->scan;
-  a.nt = sc.n_out * sc.n_res;
-  a.kp0 = a.kperp = c->kperp;
-  a.kz0 = a.kpar = c->kpar;
-  a.th0 = std::atan(a.kp0 / a.kz0);
-  a.k0 = std::sqrt(a.kp0 * a.kp0 + a.kz0 * a.kz0);
-  a.jump.assign(rq->n, 1);
+  a->nt = sc.n_out * sc.n_res;
+  a->kp0 = a->kperp = c->kperp;
+  a->kz0 = a->kpar = c->kpar;
+  a->th0 = std::atan(a->kp0 / a->kz0);
+  a->k0 = std::sqrt(a->kp0 * a->kp0 + a->kz0 * a->kz0);
+  a->jump.assign(rq->n, 1);
   for (int r = 0; r < rq->n; ++r) {
     double* row = rq->scan_rows + (size_t)r * 4;
-    row[0] = a.kperp;
-    row[1] = a.kpar;
+    row[0] = a->kperp;
+    row[1] = a->kpar;
     row[2] = rq->om[r].re;
     row[3] = rq->om[r].im;
   }
-  a.out_row = 1;
-  a.it = 0;
+  a->out_row = 1;
+  a->it = 0;
 }
 
-void alps_server::finish(Active& a, int status) {
-  a.rq->status = status;
-  a.rq->latency_ms = now_ms() - a.t0;
-  std::lock_guard<std::mutex> lk(mu);
-  finished[a.id] = status;
-  pending.erase(a.id);
-  t_submit.erase(a.id);
-  cv_done.notify_all();
-}
-
-// Moves a request forward after its batch (or with no batch this round).
-void alps_server::advance(Active& a) {
-  alps_request* rq = a.rq;
-  if (rq->kind == ALPS_REQ_MAP) return;
-  // feed determinants back
-  size_t k = 0;
-  std::vector<cplx> got;
-  for (size_t q = 0; q < a.rm.size(); ++q) {
-    if (a.want[q].empty()) continue;
-    got.clear();
-    for (size_t w = 0; w < a.want[q].size(); ++w, ++k) got.push_back(cplx(a.bD[k].re, a.bD[k].im));
-    a.want[q] = a.rm[q].step(got);
-  }
+bool evals_pending(const Active* a) {
+  for (auto& w : a->want)
+    if (!w.empty()) return true;
+  return false;
 }
 
 // The next k step of a scan: checks and output row of the step just
 // polished (om_scan :2540-2580), alps_set_k, root finders for the roots
 // still followed.  Runs on a worker thread; touches only this request.
-static void scan_step(Active* a) {
+void scan_step(Active* a) {
   alps_request* rq = a->rq;
   alps_ctx* c = rq->ctx;
   if (!a->rm.empty()) {
@@ -243,153 +211,228 @@ static void scan_step(Active* a) {
   }
 }
 
-// Launches the request's next batch on its context's stream; ALPS_OK with
-// nothing launched when it has nothing to evaluate.
-static int launch(Active* a) {
-  alps_request* rq = a->rq;
-  a->bom.clear();
-  if (rq->kind == ALPS_REQ_MAP) {
-    if (!a->map_done) map_lattice(&rq->map, a->bom);
-  } else {
-    for (auto& w : a->want)
-      for (auto& o : w) a->bom.push_back(alps_complex{o.real(), o.imag()});
+// True once the request has nothing left to do.
+bool request_done(const Active* a) {
+  const alps_request* rq = a->rq;
+  if (a->status != ALPS_OK) return true;
+  if (rq->kind == ALPS_REQ_MAP) return a->map_done;
+  if (rq->kind == ALPS_REQ_SCAN) return a->it > a->nt;
+  return !evals_pending(a);
+}
+
+// One batch with the next evaluations of every request of the group, on
+// the group's context stream; nothing launched when no request needs any.
+int launch_group(Group& g) {
+  g.bom.clear();
+  for (Active* a : g.members) {
+    a->off = g.bom.size();
+    if (a->status == ALPS_OK) {
+      if (a->rq->kind == ALPS_REQ_MAP) {
+        if (!a->map_done) {
+          std::vector<alps_complex> lat;
+          map_lattice(&a->rq->map, lat);
+          g.bom.insert(g.bom.end(), lat.begin(), lat.end());
+        }
+      } else {
+        for (auto& w : a->want)
+          for (auto& o : w) g.bom.push_back(alps_complex{o.real(), o.imag()});
+      }
+    }
+    a->cnt = g.bom.size() - a->off;
+    if (a->cnt) a->rq->rounds += 1;
   }
-  int n = (int)a->bom.size();
-  a->bD.resize(n);
+  int n = (int)g.bom.size();
+  g.bD.resize(n);
   if (n == 0) return ALPS_OK;
-  alps_ctx* c = rq->ctx;
+  alps_ctx* c = g.ctx;
   int st = ctx_ensure_batch(c, n, false);
   if (st) return st;
-  std::memcpy(c->h_pinned, a->bom.data(), (size_t)n * sizeof(double2));
+  std::memcpy(c->h_pinned, g.bom.data(), (size_t)n * sizeof(double2));
   ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
   if ((st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream))) return st;
   ALPS_CUDA_TRY(
       cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaMemcpyAsync(c->h_flag, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaEventRecord(c->ev_done, c->stream));
-  rq->rounds += 1;
-  a->state = Active::IN_FLIGHT;
+  g.state = Group::IN_FLIGHT;
   return ALPS_OK;
 }
 
-// True once the request has nothing left to do.
-static bool finished_work(Active* a) {
+// Hands every request its slice of a landed batch.
+void land_group(Group& g) {
+  alps_ctx* c = g.ctx;
+  int n = (int)g.bom.size();
+  int f = *c->h_flag;
+  std::memcpy(g.bD.data(), c->h_pinned + n, (size_t)n * sizeof(double2));
+  for (Active* a : g.members) {
+    if (!a->cnt) continue;
+    if (f) {
+      a->status = (f & 2) ? ALPS_E_SUBLUMINAL : ALPS_E_INVALID;
+      continue;
+    }
+    const alps_complex* D = g.bD.data() + a->off;
+    if (a->rq->kind == ALPS_REQ_MAP) {
+      map_finish((int)a->cnt, D, a->rq->map_cal, a->rq->map_val);
+      a->map_done = true;
+      continue;
+    }
+    size_t k = 0;
+    std::vector<cplx> got;
+    for (size_t q = 0; q < a->rm.size(); ++q) {
+      if (a->want[q].empty()) continue;
+      got.clear();
+      for (size_t w = 0; w < a->want[q].size(); ++w, ++k) got.push_back(cplx(D[k].re, D[k].im));
+      a->want[q] = a->rm[q].step(got);
+    }
+  }
+}
+
+}  // namespace
+
+
+struct alps_server {
+  size_t budget = 0;
+  int max_active = 64;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  std::deque<std::pair<int64_t, alps_request*>> queue;
+  std::map<int64_t, alps_request*> pending;  // submitted, not finished
+  std::map<int64_t, int> finished;           // id -> status
+  std::map<int64_t, double> t_submit;
+  int64_t next_id = 1;
+  bool stop = false;
+  std::thread th;
+  // statistics
+  int64_t batches = 0;
+  int peak_active = 0;
+  size_t peak_bytes = 0;
+
+  void run();
+  void finish(Active* a);
+};
+
+void alps_server::finish(Active* a) {
   alps_request* rq = a->rq;
-  if (a->status != ALPS_OK) return true;
-  if (rq->kind == ALPS_REQ_MAP) return a->map_done;
-  if (rq->kind == ALPS_REQ_SCAN) return a->it > a->nt;
-  for (auto& w : a->want)
-    if (!w.empty()) return false;
-  return true;
+  if (rq->kind == ALPS_REQ_POLISH && a->status == ALPS_OK)
+    for (size_t k = 0; k < a->rm.size(); ++k) {
+      cplx o = a->rm[k].root();
+      rq->om[k] = alps_complex{o.real(), o.imag()};
+      if (rq->iters) rq->iters[k] = a->rm[k].iters();
+    }
+  rq->status = a->status;
+  rq->latency_ms = now_ms() - a->t0;
+  std::lock_guard<std::mutex> lk(mu);
+  finished[a->id] = a->status;
+  pending.erase(a->id);
+  t_submit.erase(a->id);
+  cv_done.notify_all();
 }
 
 void alps_server::run() {
-  std::vector<Active*> active;
+  std::map<alps_ctx*, Group> groups;
   size_t in_use = 0;
+  int n_active = 0;
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(mu);
-      // admission: FIFO, one request per context, within the budget
-      for (auto itq = queue.begin(); itq != queue.end() && (int)active.size() < max_active;) {
+      // admission, in submission order: a request joins its context's group
+      // while the group is between batches, holds no scan, and (for a scan)
+      // is empty, and while the footprint fits the budget
+      std::vector<alps_ctx*> blocked;  // contexts whose earlier request waits
+      for (auto itq = queue.begin(); itq != queue.end() && n_active < max_active;) {
         alps_request* rq = itq->second;
-        bool busy = false;
-        for (Active* a : active) busy = busy || a->rq->ctx == rq->ctx;
+        auto gi = groups.find(rq->ctx);
+        bool ok = std::find(blocked.begin(), blocked.end(), rq->ctx) == blocked.end();
+        if (ok && gi != groups.end()) {
+          Group& g = gi->second;
+          ok = g.state == Group::IDLE && !g.has_scan() && (rq->kind != ALPS_REQ_SCAN || g.members.empty());
+        }
         size_t nb = (rq->kind == ALPS_REQ_MAP) ? (size_t)rq->map.nr * rq->map.ni : (size_t)2 * std::max(rq->n, 1);
-        size_t need = ctx_device_bytes(rq->ctx) + batch_bytes(rq->ctx, nb);
-        if (busy || (in_use + need > budget && !active.empty())) {
+        size_t need = batch_bytes(rq->ctx, nb) + (gi == groups.end() ? ctx_device_bytes(rq->ctx) : 0);
+        if (!ok || (in_use + need > budget && n_active > 0)) {
+          // keep the context's order: later requests on it wait too
+          blocked.push_back(rq->ctx);
           ++itq;
           continue;
         }
+        Group& g = groups[rq->ctx];
+        g.ctx = rq->ctx;
         Active* a = new Active();
         a->rq = rq;
         a->id = itq->first;
         a->t0 = t_submit[itq->first];
         a->bytes = need;
         in_use += need;
-        active.push_back(a);
+        ++n_active;
+        g.members.push_back(a);
+        start_request(a);
         itq = queue.erase(itq);
       }
-      peak_active = std::max(peak_active, (int)active.size());
+      peak_active = std::max(peak_active, n_active);
       peak_bytes = std::max(peak_bytes, in_use);
-      if (active.empty()) {
+      if (groups.empty()) {
         if (stop && queue.empty()) return;
         cv_work.wait(lk);
         continue;
       }
     }
     bool progressed = false;
-    for (Active* a : active) {
-      alps_request* rq = a->rq;
-      if (!a->started) {
-        start_request(*a);
-        a->started = true;
-      }
-      if (a->state == Active::STEPPING) {
-        if (a->step.wait_for(std::chrono::seconds(0)) != std::future_status::ready) continue;
-        a->step.get();
-        a->state = Active::IDLE;
-        progressed = true;
-      }
-      if (a->state == Active::IN_FLIGHT) {
-        cudaError_t q = cudaEventQuery(rq->ctx->ev_done);
-        if (q == cudaErrorNotReady) continue;
-        progressed = true;
-        a->state = Active::IDLE;
-        if (q != cudaSuccess) {
-          alps_set_last_cuda_error(q, "cudaEventQuery", __FILE__, __LINE__);
-          a->status = ALPS_E_CUDA;
-          continue;
-        }
-        int f = *rq->ctx->h_flag;
-        if (f) {
-          a->status = (f & 2) ? ALPS_E_SUBLUMINAL : ALPS_E_INVALID;
-          continue;
-        }
-        int n = (int)a->bom.size();
-        std::memcpy(a->bD.data(), rq->ctx->h_pinned + n, (size_t)n * sizeof(double2));
-        if (rq->kind == ALPS_REQ_MAP) {
-          map_finish(n, a->bD.data(), rq->map_cal, rq->map_val);
-          a->map_done = true;
-        } else {
-          advance(*a);
-        }
-      }
-      if (a->state != Active::IDLE || a->status != ALPS_OK) continue;
-      // a scan whose step is polished moves to its next k on a worker thread
-      if (rq->kind == ALPS_REQ_SCAN && a->it <= a->nt) {
-        bool pending_evals = false;
-        for (auto& w : a->want) pending_evals = pending_evals || !w.empty();
-        if (!pending_evals) {
-          a->state = Active::STEPPING;
-          a->step = std::async(std::launch::async, scan_step, a);
+    for (auto gi = groups.begin(); gi != groups.end();) {
+      Group& g = gi->second;
+      if (g.state == Group::STEPPING) {
+        if (g.step.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+          g.step.get();
+          g.state = Group::IDLE;
           progressed = true;
-          continue;
+        }
+      } else if (g.state == Group::IN_FLIGHT) {
+        cudaError_t q = cudaEventQuery(g.ctx->ev_done);
+        if (q != cudaErrorNotReady) {
+          g.state = Group::IDLE;
+          progressed = true;
+          if (q == cudaSuccess) {
+            land_group(g);
+          } else {
+            alps_set_last_cuda_error(q, "cudaEventQuery", __FILE__, __LINE__);
+            for (Active* a : g.members) a->status = ALPS_E_CUDA;
+          }
         }
       }
-      if (finished_work(a)) continue;
-      int st = launch(a);
-      if (st) a->status = st;
-      if (a->state == Active::IN_FLIGHT) ++rounds;
-      progressed = true;
-    }
-    // release finished requests
-    for (size_t q = 0; q < active.size();) {
-      Active* a = active[q];
-      if (a->state == Active::IDLE && finished_work(a)) {
-        if (a->rq->kind == ALPS_REQ_POLISH && a->status == ALPS_OK)
-          for (size_t k = 0; k < a->rm.size(); ++k) {
-            cplx o = a->rm[k].root();
-            a->rq->om[k] = alps_complex{o.real(), o.imag()};
-            if (a->rq->iters) a->rq->iters[k] = a->rm[k].iters();
+      if (g.state == Group::IDLE) {
+        // release the finished requests of the group
+        for (size_t q = 0; q < g.members.size();) {
+          Active* a = g.members[q];
+          if (request_done(a)) {
+            finish(a);
+            in_use -= a->bytes;
+            --n_active;
+            delete a;
+            g.members.erase(g.members.begin() + q);
+            progressed = true;
+          } else {
+            ++q;
           }
-        finish(*a, a->status);
-        in_use -= a->bytes;
-        delete a;
-        active.erase(active.begin() + q);
-        progressed = true;
-      } else {
-        ++q;
+        }
+        // a scan whose step is polished moves to its next k off this thread
+        Active* sc = nullptr;
+        for (Active* a : g.members)
+          if (a->rq->kind == ALPS_REQ_SCAN && !evals_pending(a)) sc = a;
+        if (sc) {
+          g.state = Group::STEPPING;
+          g.step = std::async(std::launch::async, scan_step, sc);
+          progressed = true;
+        } else if (!g.members.empty()) {
+          int st = launch_group(g);
+          if (st)
+            for (Active* a : g.members) a->status = st;
+          if (g.state == Group::IN_FLIGHT) ++batches;
+          progressed = true;
+        }
       }
+      if (g.state == Group::IDLE && g.members.empty())
+        gi = groups.erase(gi);
+      else
+        ++gi;
     }
     if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
@@ -471,7 +514,7 @@ int alps_server_wait(alps_server* s, int64_t id) {
 int alps_server_stats(alps_server* s, int64_t* rounds, int* peak_active, size_t* peak_bytes) {
   if (!s) return ALPS_E_INVALID;
   std::lock_guard<std::mutex> lk(s->mu);
-  if (rounds) *rounds = s->rounds;
+  if (rounds) *rounds = s->batches;
   if (peak_active) *peak_active = s->peak_active;
   if (peak_bytes) *peak_bytes = s->peak_bytes;
   return ALPS_OK;
