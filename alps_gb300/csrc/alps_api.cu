@@ -156,6 +156,7 @@ void alps_destroy(alps_ctx* c) {
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->h_flag) cudaFreeHost(c->h_flag);
   if (c->ev_done) cudaEventDestroy(c->ev_done);
+  for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.second);
   for (auto& ev : c->ev_pending)
     for (auto e : ev) cudaEventDestroy(e);
   for (auto e : c->ev_pool) cudaEventDestroy(e);
@@ -289,6 +290,7 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
 
 int alps_prepare(alps_ctx* c) {
   if (!c) return ALPS_E_INVALID;
+  c->gen++;
   for (int is = 0; is < c->sys.nspec; ++is)
     if (!c->spec[is].loaded) return ALPS_E_INVALID;
   for (int is = 0; is < c->sys.nspec; ++is) {
@@ -318,6 +320,7 @@ int alps_set_fit(alps_ctx* c, int is, const double* in) {
   if (st) return st;
   if (c->kset && (st = launch_landau_moments(c, is))) return st;
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
+  c->gen++;
   return ALPS_OK;
 }
 
@@ -383,6 +386,7 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
   c->kperp = kperp;
   c->kpar = kpar;
   c->kset = true;
+  c->gen++;
   return ALPS_OK;
 }
 
@@ -396,6 +400,7 @@ int alps_set_precision(alps_ctx* c, int precision) {
   if (!c) return ALPS_E_INVALID;
   if (precision != ALPS_PREC_FP64 && precision != ALPS_PREC_MIXED) return ALPS_E_INVALID;
   c->precision = precision;
+  c->gen++;
   return ALPS_OK;
 }
 
@@ -408,6 +413,7 @@ int ctx_ensure_batch(alps_ctx* c, int n, bool ext) {
     ALPS_CUDA_TRY(cudaMalloc(&c->d_om, (size_t)n * sizeof(double2)));
     ALPS_CUDA_TRY(cudaMalloc(&c->d_D, (size_t)n * sizeof(double2)));
     c->batch_cap = n;
+    c->gen++;
   }
   size_t need_pin = (size_t)2 * n;
   if (need_pin > c->pinned_cap) {
@@ -416,6 +422,7 @@ int ctx_ensure_batch(alps_ctx* c, int n, bool ext) {
     c->pinned_cap = 0;
     ALPS_CUDA_TRY(cudaMallocHost(&c->h_pinned, need_pin * sizeof(double2)));
     c->pinned_cap = need_pin;
+    c->gen++;
   }
   if (!c->h_flag) ALPS_CUDA_TRY(cudaMallocHost(&c->h_flag, sizeof(int)));
   if (!c->ev_done) ALPS_CUDA_TRY(cudaEventCreateWithFlags(&c->ev_done, cudaEventDisableTiming));

@@ -19,6 +19,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/alps_gb300.h"
@@ -195,6 +196,13 @@ struct alps_ctx {
   size_t pinned_cap = 0;
   int* h_flag = nullptr;                // pinned copy of the device error flags
   cudaEvent_t ev_done = nullptr;        // completion of an asynchronous batch
+  // CUDA graphs of whole batches (upload, kernels, download) by batch size,
+  // valid while gen (bumped by every change of the plasma, k, precision or
+  // any batch buffer address) is unchanged
+  uint64_t gen = 1;
+  std::map<int, std::pair<uint64_t, cudaGraphExec_t>> graphs;
+  std::map<int, uint64_t> graph_seen;  // gen of the last uncaptured batch of each size
+  int res_smem_set = 0;                 // dynamic shared memory opt-in of k_resonant done
 };
 
 // ---------------------------------------------------------------------------

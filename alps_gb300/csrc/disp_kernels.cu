@@ -1001,6 +1001,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   a.csize = (maxn + 1 + nchunk - 1) / nchunk;
   a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
   int rcode;
+  const void* before[8] = {c->d_part, c->d_count, c->d_slot_nn, c->d_items, c->d_low, c->d_rel, c->d_bm, c->d_flags};
   if ((rcode = ensure_buf(c->d_part, c->part_cap, (size_t)n * S_ * a.nchunk * 6))) return rcode;
   if ((rcode = ensure_buf(c->d_count, c->count_cap, (size_t)n * S_))) return rcode;
   size_t nslots = (size_t)n * S_ * rc;
@@ -1018,6 +1019,9 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   if (a.has_bm)
     if ((rcode = ensure_buf(c->d_bm, c->bm_cap, (size_t)n * S_ * 24))) return rcode;
   if (!c->d_flags) ALPS_CUDA_TRY(cudaMalloc(&c->d_flags, sizeof(int)));
+  const void* after[8] = {c->d_part, c->d_count, c->d_slot_nn, c->d_items, c->d_low, c->d_rel, c->d_bm, c->d_flags};
+  for (int q = 0; q < 8; ++q)
+    if (before[q] != after[q]) c->gen++;  // buffer addresses changed: cached graphs are stale
   ALPS_CUDA_TRY(cudaMemsetAsync(c->d_flags, 0, sizeof(int), st));
 
   std::vector<cudaEvent_t> ev;
@@ -1046,7 +1050,10 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
   int maxN = c->sys.nperp;
   size_t smem = (size_t)RES_WARPS * res_warp_smem(maxN) * sizeof(double2);
-  if (smem > 48 * 1024) ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (smem > 48 * 1024 && (size_t)c->res_smem_set < smem) {
+    ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    c->res_smem_set = (int)smem;
+  }
   long total = (long)nslots;
   long blocks = (total + RES_WARPS - 1) / RES_WARPS;
   k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_items,

@@ -220,6 +220,62 @@ bool request_done(const Active* a) {
   return !evals_pending(a);
 }
 
+// Upload of the staged frequencies, the batch kernels, download of det D
+// and of the error flags, on the context's stream.
+int enqueue_batch(alps_ctx* c, int n) {
+  ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
+  int st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream);
+  if (st) return st;
+  ALPS_CUDA_TRY(
+      cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(c->h_flag, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  return ALPS_OK;
+}
+
+// A root finder needs one batch per iteration, each a few frequencies: the
+// host cost of its ten or so calls dominates.  After one uncaptured batch of
+// a size has run at the context's current state (so every buffer is sized),
+// the next one is captured into a CUDA graph and later batches of that size
+// replay it with a single launch until the plasma, k, precision or a buffer
+// address changes (alps_ctx::gen).
+int run_batch(alps_ctx* c, int n) {
+  if (!c->profiling) {
+    auto it = c->graphs.find(n);
+    if (it != c->graphs.end() && it->second.first != c->gen) {
+      cudaGraphExecDestroy(it->second.second);
+      c->graphs.erase(it);
+      it = c->graphs.end();
+    }
+    if (it != c->graphs.end()) {
+      ALPS_CUDA_TRY(cudaGraphLaunch(it->second.second, c->stream));
+      return ALPS_OK;
+    }
+    auto seen = c->graph_seen.find(n);
+    if (seen != c->graph_seen.end() && seen->second == c->gen) {
+      const uint64_t gen0 = c->gen;
+      cudaGraph_t graph = nullptr;
+      bool launched = false;
+      if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        int st = enqueue_batch(c, n);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        cudaGraphExec_t exec = nullptr;
+        if (!st && e == cudaSuccess && graph && c->gen == gen0 &&
+            cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+          c->graphs[n] = {c->gen, exec};
+          launched = cudaGraphLaunch(exec, c->stream) == cudaSuccess;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();  // a refused capture falls back to plain launches
+      }
+      if (launched) return ALPS_OK;
+    }
+  }
+  int st = enqueue_batch(c, n);
+  if (st) return st;
+  c->graph_seen[n] = c->gen;
+  return ALPS_OK;
+}
+
 // One batch with the next evaluations of every request of the group, on
 // the group's context stream; nothing launched when no request needs any.
 int launch_group(Group& g) {
@@ -248,11 +304,7 @@ int launch_group(Group& g) {
   int st = ctx_ensure_batch(c, n, false);
   if (st) return st;
   std::memcpy(c->h_pinned, g.bom.data(), (size_t)n * sizeof(double2));
-  ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_om, c->h_pinned, (size_t)n * sizeof(double2), cudaMemcpyHostToDevice, c->stream));
-  if ((st = launch_disp_batch(c, n, c->d_om, c->d_D, nullptr, c->stream))) return st;
-  ALPS_CUDA_TRY(
-      cudaMemcpyAsync(c->h_pinned + n, c->d_D, (size_t)n * sizeof(double2), cudaMemcpyDeviceToHost, c->stream));
-  ALPS_CUDA_TRY(cudaMemcpyAsync(c->h_flag, c->d_flags, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  if ((st = run_batch(c, n))) return st;
   ALPS_CUDA_TRY(cudaEventRecord(c->ev_done, c->stream));
   g.state = Group::IN_FLIGHT;
   return ALPS_OK;

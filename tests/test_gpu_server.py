@@ -95,3 +95,27 @@ def test_requests_arriving_while_others_run(api):
     for a, b in zip(res, alone):
         assert np.array_equal(a, b, equal_nan=True)
     srv.close()
+
+
+def test_requests_on_one_plasma_share_batches(api):
+    """Polishes (and a map) on the same plasma run in shared batches; a
+    shared batch changes how the device splits the node sums, so results
+    agree with the lone runs to rounding (roots 1e-12, det D 1e-12)."""
+    w = workloads.kpar_fast(nproc=0)
+    s, sp = workloads.build(w, api.generate_f0)
+    G = api.Plasma(s, sp)
+    G.set_k(*w["k"])
+    guesses = [[0.0099881 - 2.3e-7j * (1 + 0.1 * k)] for k in range(5)]
+    alone = [G.secant(g)[0] for g in guesses]
+    mp = _map(16, 8)
+    mp.omi, mp.omf, mp.gami, mp.gamf = 0.005, 0.02, -1e-5, 1e-5
+    alone_map = G.map_search(mp)
+    srv = api.Server()
+    reqs = [srv.polish(G, g) for g in guesses]
+    rmap = srv.map(G, mp)
+    for r, a in zip(reqs, alone):
+        np.testing.assert_allclose(r.wait(), a, rtol=1e-12)
+    cal, val = rmap.wait()
+    np.testing.assert_allclose(cal, alone_map[1], rtol=1e-12)
+    assert srv.stats()["peak_active"] >= 2
+    srv.close()
