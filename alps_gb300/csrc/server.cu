@@ -344,7 +344,7 @@ void land_group(Group& g) {
 
 struct alps_server {
   size_t budget = 0;
-  int max_active = 64;
+  int max_active = 256;
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   std::deque<std::pair<int64_t, alps_request*>> queue;
@@ -504,7 +504,7 @@ int alps_server_create(size_t hbm_budget, int max_active, alps_server** out) {
     hbm_budget = (size_t)(0.9 * (double)fr);
   }
   s->budget = hbm_budget;
-  s->max_active = max_active > 0 ? max_active : 64;
+  s->max_active = max_active > 0 ? max_active : 256;
   s->th = std::thread([s]() { s->run(); });
   *out = s;
   return ALPS_OK;

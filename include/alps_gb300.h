@@ -326,7 +326,7 @@ typedef struct alps_request {
 } alps_request;
 
 /* hbm_budget: bytes of device memory requests may hold at once (0: 90 % of
- * the free memory at creation); max_active: requests in flight (0: 64). */
+ * the free memory at creation); max_active: requests in flight (0: 256). */
 int alps_server_create(size_t hbm_budget, int max_active, alps_server** out);
 /* Waits for every submitted request, then stops the thread. */
 void alps_server_destroy(alps_server* srv);
