@@ -148,7 +148,7 @@ class alps_stats(C.Structure):
     _fields_ = [
         ("n_eval", C.c_int64), ("n_pole_terms", C.c_int64),
         ("n_resonant", C.c_int64), ("n_landau", C.c_int64),
-        ("kernels_launched", C.c_int),
+        ("kernels_launched", C.c_int), ("graph_replays", C.c_int64), ("graph_captures", C.c_int64),
     ]
 
 

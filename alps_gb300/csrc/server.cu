@@ -248,6 +248,7 @@ int run_batch(alps_ctx* c, int n) {
     }
     if (it != c->graphs.end()) {
       ALPS_CUDA_TRY(cudaGraphLaunch(it->second.second, c->stream));
+      c->stats.graph_replays++;
       return ALPS_OK;
     }
     auto seen = c->graph_seen.find(n);
@@ -263,6 +264,7 @@ int run_batch(alps_ctx* c, int n) {
             cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
           c->graphs[n] = {c->gen, exec};
           launched = cudaGraphLaunch(exec, c->stream) == cudaSuccess;
+          if (launched) c->stats.graph_captures++;
         }
         if (graph) cudaGraphDestroy(graph);
         cudaGetLastError();  // a refused capture falls back to plain launches

@@ -381,6 +381,8 @@ typedef struct alps_stats {
   int64_t n_resonant;         /* resonant (omega, species, n) work items      */
   int64_t n_landau;           /* of which with a Landau term                  */
   int kernels_launched;       /* kernels launched by the last disp batch      */
+  int64_t graph_replays;      /* server batches replayed from a CUDA graph    */
+  int64_t graph_captures;     /* server batches captured into a CUDA graph    */
 } alps_stats;
 int alps_get_stats(alps_ctx* ctx, alps_stats* st);
 
