@@ -203,6 +203,7 @@ struct alps_ctx {
   std::map<int, std::pair<uint64_t, cudaGraphExec_t>> graphs;
   std::map<int, uint64_t> graph_seen;  // gen of the last uncaptured batch of each size
   int res_smem_set = 0;                 // dynamic shared memory opt-in of k_resonant done
+  int chunk_group = 1;                  // order chunks per pole-sum block (results unchanged)
 };
 
 // ---------------------------------------------------------------------------

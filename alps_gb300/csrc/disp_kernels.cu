@@ -33,36 +33,46 @@ struct DispArgs {
   int rcap;      // max resonant slots over species
   int relcap;    // order slots per relativistic species (max nmax + 1), 0 if none
   int has_bm;    // some species go through the NHDS closed form
+  int cgroup;    // order chunks per pole-sum block
 };
 
 namespace {
 
 // ---------------------------------------------------------------------------
+// One warp per (omega, species): the lanes test the orders -nmax..nmax
+// and a ballot prefix gives every resonant order its slot in increasing nn,
+// so the slot order does not depend on the launch shape.
 __global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om, int* count, int* slot_nn,
                            int* flags) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  int s = blockIdx.y;
-  if (t >= n_om) return;
+  const int lane = threadIdx.x & 31;
+  const long wid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int S_ = a.sys.nspec;
+  if (wid >= (long)n_om * S_) return;
+  const int t = (int)(wid / S_), s = (int)(wid % S_);
   const SpecDev& S = a.sp[s];
   if (S.relat || S.bm) {  // relativistic orders run in k_rel_orders, NHDS species in k_nhds
-    count[(size_t)t * a.sys.nspec + s] = 0;
+    if (lane == 0) count[(size_t)t * S_ + s] = 0;
     return;
   }
-  double2 o = om[t];
+  const double2 o = om[t];
+  int* slots = slot_nn + ((size_t)t * S_ + s) * a.rcap;
   int cnt = 0;
-  int* slots = slot_nn + ((size_t)t * a.sys.nspec + s) * a.rcap;
-  for (int nn = -S.nmax; nn <= S.nmax; ++nn) {
-    ResGeom g = res_geometry(S, a.sys.M_I, o, nn, a.sys.kpar);
-    if (g.res) {
-      if (cnt < a.rcap) slots[cnt] = nn;
-      cnt++;
+  for (int base = -S.nmax; base <= S.nmax; base += 32) {
+    const int nn = base + lane;
+    bool res = false;
+    if (nn <= S.nmax) res = res_geometry(S, a.sys.M_I, o, nn, a.sys.kpar).res;
+    const unsigned m = __ballot_sync(0xffffffffu, res);
+    const int at = cnt + __popc(m & ((1u << lane) - 1u));
+    if (res && at < a.rcap) slots[at] = nn;
+    cnt += __popc(m);
+  }
+  if (lane == 0) {
+    if (cnt > a.rcap) {
+      atomicOr(flags, 1);
+      cnt = a.rcap;
     }
+    count[(size_t)t * S_ + s] = cnt;
   }
-  if (cnt > a.rcap) {
-    atomicOr(flags, 1);
-    cnt = a.rcap;
-  }
-  count[(size_t)t * a.sys.nspec + s] = cnt;
 }
 
 // ---------------------------------------------------------------------------
@@ -71,11 +81,10 @@ __global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om,
 // omega over the orders of its chunk (and the n = -1,0,1 parts for chi_low).
 // ---------------------------------------------------------------------------
 template <bool LOW>
-__global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __restrict__ om, int n_om,
-                                                   int js_count, double2* part, double2* low) {
+__device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __restrict__ om, int n_om,
+                                           int js_count, double2* part, double2* low, const int chunk) {
   const int s = blockIdx.y;
   const SpecDev& S = a.sp[s];
-  const int chunk = blockIdx.z;
   const int n_begin = chunk * a.csize;
   const int n_end = (S.relat || S.bm) ? n_begin : min(S.nmax + 1, n_begin + a.csize);
   const int TW = blockDim.x / js_count;
@@ -222,6 +231,19 @@ __global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __
     if (LOW)
       for (int l = 0; l < 3; ++l)
         for (int e = 0; e < 6; ++e) low[(base * 3 + l) * 6 + e] = lacc[LOW ? l : 0][e];
+  }
+}
+
+// grid (omega tiles, species, chunk groups): a block sums a.cgroup order
+// chunks one after another, each into its own partial, so the grouping
+// changes the block count but not one rounding
+template <bool LOW>
+__global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __restrict__ om, int n_om,
+                                                   int js_count, double2* part, double2* low) {
+  const int c1 = min(a.nchunk, ((int)blockIdx.z + 1) * a.cgroup);
+  for (int chunk = blockIdx.z * a.cgroup; chunk < c1; ++chunk) {
+    pole_chunk<LOW>(a, om, n_om, js_count, part, low, chunk);
+    __syncthreads();
   }
 }
 
@@ -1038,10 +1060,12 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     }
     ALPS_CUDA_TRY(cudaEventRecord(ev[0], st));
   }
-  k_classify<<<dim3((n + 127) / 128, S_), 128, 0, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_flags);
+  k_classify<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(a, d_om, n, c->d_count, c->d_slot_nn,
+                                                                            c->d_flags);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[1], st));
-  dim3 g2(tiles, S_, a.nchunk);
+  a.cgroup = std::max(1, std::min(c->chunk_group, a.nchunk));
+  dim3 g2(tiles, S_, (a.nchunk + a.cgroup - 1) / a.cgroup);
   if (want_low)
     k_pole_sums<true><<<g2, 128, 0, st>>>(a, d_om, n, js, c->d_part, c->d_low);
   else
@@ -1181,8 +1205,9 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   const double2* om = reinterpret_cast<const double2*>(d_om);
   double2* D = reinterpret_cast<double2*>(d_D);
   ALPS_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), st));
-  k_classify<<<dim3((n + 127) / 128, S_), 128, 0, st>>>(a, om, n, count, slots, flags);
+  k_classify<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(a, om, n, count, slots, flags);
   ALPS_CUDA_TRY(cudaGetLastError());
+  a.cgroup = 1;
   k_pole_sums<false><<<dim3(tiles, S_, a.nchunk), 128, 0, st>>>(a, om, n, js, part, nullptr);
   ALPS_CUDA_TRY(cudaGetLastError());
   size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp) * sizeof(double2);
