@@ -341,10 +341,24 @@ __device__ inline double2 h_node(const double* Vn, int j, int e, double2 o, doub
 // exponentials; the omega-independent factors come from k_fit_aux.
 // ---------------------------------------------------------------------------
 #define RES_WARPS 4
-#define RES_WIN 32
+#define RES_WIN 32  // largest node window staged in shared memory
+// principal-value piece records per warp, in double2: (group, lane, slot)
+// sums A, B; run sums A, B; then the int tables (group, lane, slot) piece
+// and run start lane, slot, group, piece
+#define PV_GROUPS 3
+#define PV_RECV (PV_GROUPS * 32 * 2 * 2)
+#define PV_RUNV (32 * 2)
+#define PV_INTS (PV_GROUPS * 64 + 4 * 32)
+#define PV_SMEM (PV_RECV + PV_RUNV + (PV_INTS + 3) / 4)
 
-__host__ __device__ inline size_t res_warp_smem(int N) {
-  return (size_t)RES_WIN * 12 + 3 * (size_t)(N + 1);  // in double2
+// node window of the principal-value sum: nodes lower-2 .. upper+2
+__host__ __device__ inline int res_win(int M_I) { return (2 * M_I + 8 < RES_WIN) ? 2 * M_I + 8 : RES_WIN; }
+
+// per-warp shared memory in double2: the window (h, s) and a region used
+// first by the principal-value records, then by the Landau rows
+__host__ __device__ inline size_t res_warp_smem(int N, int W) {
+  const size_t rows = 3 * (size_t)(N + 1);
+  return (size_t)W * 12 + (rows > PV_SMEM ? rows : (size_t)PV_SMEM);
 }
 
 __device__ inline double2 crcp(double2 z) {
@@ -377,9 +391,11 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
   t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
   ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
   const double* Vn = S.V + (size_t)n * (M - 1) * 12;
-  double2* wh = sm + (size_t)warp * res_warp_smem(N);  // node values h
-  double2* ws = wh + RES_WIN * 6;                       // node slopes s
-  double2* frow = ws + RES_WIN * 6;                     // f(i, p_res)
+  const int W = res_win(a.sys.M_I);
+  double2* wh = sm + (size_t)warp * res_warp_smem(N, W);  // node values h
+  double2* ws = wh + W * 6;                                // node slopes s
+  double2* pvv = ws + W * 6;                               // principal-value records
+  double2* frow = pvv;                                     // f(i, p_res), after them
   double2* fpr = frow + (N + 1);                        // f(i, p_res + dppar)
   double2* fmr = fpr + (N + 1);                         // f(i, p_res - dppar)
   double2 res[6];
@@ -391,7 +407,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
     const double dpa = S.dppar_abs, dps = S.dppar;
     const int jw0 = max(1, g.lower - 2), jw1 = min(M - 1, g.upper + 2);
     const int nw = jw1 - jw0 + 1;
-    const bool winok = nw <= RES_WIN;
+    const bool winok = nw <= W;
     if (winok) {
       for (int t = lane; t < nw * 6; t += 32) {
         int jj = t / 6, e = t % 6;
@@ -438,21 +454,19 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
       while (jr >= 1 && !(fabs(S.ppar[jr] - p) <= half)) --jr;
       return (jr >= 1) ? jr : piece_raw(p);
     };
-    // node value h and centred slope s of the six entries at node jc
-    auto node = [&](int jc, double2* h, double2* sl) {
+    // node value h and centred slope s of entry e at node jc
+    auto node1 = [&](int jc, int e, double2& h, double2& sl) {
       if (winok && jc - 1 >= jw0 && jc + 1 <= jw1) {
-#pragma unroll
-        for (int e = 0; e < 6; ++e) {
-          h[e] = wh[(jc - jw0) * 6 + e];
-          sl[e] = ws[(jc - jw0) * 6 + e];
-        }
+        h = wh[(jc - jw0) * 6 + e];
+        sl = ws[(jc - jw0) * 6 + e];
       } else {
-#pragma unroll
-        for (int e = 0; e < 6; ++e) {
-          h[e] = h_node(Vn, jc, e, o, kappa);
-          sl[e] = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
-        }
+        h = h_node(Vn, jc, e, o, kappa);
+        sl = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
       }
+    };
+    auto node = [&](int jc, double2* h, double2* sl) {
+#pragma unroll
+      for (int e = 0; e < 6; ++e) node1(jc, e, h[e], sl[e]);
     };
     auto Hc = [&](double p, double2* H) {
       int jc = piece(p);
@@ -462,70 +476,137 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
 #pragma unroll
       for (int e = 0; e < 6; ++e) H[e] = cmk(fma(sl[e].x, dx, h[e].x), fma(sl[e].y, dx, h[e].y));
     };
-    // Sum_k c_k H(p_k) with H linear on each piece: per piece only
-    // A = Sum c_k and B = Sum c_k (p_k - pp(jc)) are accumulated, and
-    // T += h A + s B when the piece changes (each lane walks consecutive k)
-    struct Acc {
-      int jc;
-      double2 A, B;
-    };
-    auto flush = [&](Acc& q, double sign) {
-      if (q.jc < 0) return;
-      double2 h[6], sl[6];
-      node(q.jc, h, sl);
-#pragma unroll
-      for (int e = 0; e < 6; ++e) {
-        double2 t = cadd(cmul(h[e], q.A), cmul(sl[e], q.B));
-        T[e] = cmk(fma(sign, t.x, T[e].x), fma(sign, t.y, T[e].y));
-      }
-      q.A = q.B = cmk(0.0, 0.0);
-    };
-    auto add = [&](Acc& q, int jc, double p, double2 c, double sign) {
-      if (jc != q.jc) {
-        flush(q, sign);
-        q.jc = jc;
-      }
-      double dx = p - S.ppar[jc];
-      q.A = cadd(q.A, c);
-      q.B = cmk(fma(c.x, dx, q.B.x), fma(c.y, dx, q.B.y));
-    };
     const double capDelta = pr - S.ppar[g.lower];
     const double smdelta = capDelta / (1.0 * a.sys.M_P);
-    double2 H1[6], H2[6];
-    if (fabs(pim) > a.sys.Tlim) {
-      // w_k [H(p) K - H(2 pr - p) conj(K)], K = 1/(p - pr - i pim)
-      const int NP = a.sys.M_P + 1, per = (NP + 31) / 32;
+    const bool sym = fabs(pim) > a.sys.Tlim;
+    const int NP = a.sys.M_P + 1;
+    // tiny rest between pr + capDelta and ppar[upper]
+    const int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
+    const double corr = (ntiny > 0) ? ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
+    // the sample points: k in 0..M_P of the symmetric sum (group 0 direct,
+    // group 1 mirrored), k in 0..ntiny of the tiny rest (group 2).  Their
+    // coordinates are rounded as integrate_res writes them, without fused
+    // multiply-adds: a point can sit exactly on a piece boundary
+    // pp(j) + dppar/2, and its piece must be the reference's.
+    auto sym_point = [&](int k, double& p, double2& K) {
+      p = (k == 0) ? pr
+                   : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
+      double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
+      double dx = p - pr;
+      double rr = wk * rcp_fast(fma(dx, dx, pim * pim));
+      K = cmk(dx * rr, pim * rr);
+    };
+    auto tiny_point = [&](int k, double& p, double2& K) {
+      p = (k == 0) ? __dadd_rn(pr, capDelta)
+                   : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
+      double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
+      double dx = p - pr;
+      double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
+      K = cmk(dx * rr, pim * rr);
+    };
+
+    // Sum_k c_k H(p_k) with H linear on each piece jc needs, per piece, only
+    // A = Sum c_k and B = Sum c_k (p_k - pp(jc)); the piece adds h A + s B.
+    // Each lane walks a run of consecutive k and keeps the sums of at most
+    // two pieces (pieces are M_P/(M_I+1) or more points wide, far wider
+    // than a lane's run); the lanes' piece sums are merged per piece in
+    // shared memory in lane order, and each (piece, entry) pair is then one
+    // thread's h A + s B.  A lane that meets a third piece, or indices that
+    // are not monotone in k, send the item to the per-lane flush below.
+    struct PvSlot {
+      int jd, jc;          // finished piece (-1: none), current piece
+      double2 Ad, Bd, Ac, Bc;
+    };
+    bool bad = false;
+    auto put = [&](PvSlot& q, int j, double dx, double2 c, int dir) {
+      if (j != q.jc) {
+        if (q.jc >= 0) {
+          if (q.jd >= 0 || (dir > 0 ? j < q.jc : j > q.jc)) bad = true;
+          q.jd = q.jc;
+          q.Ad = q.Ac;
+          q.Bd = q.Bc;
+        }
+        q.jc = j;
+        q.Ac = q.Bc = cmk(0.0, 0.0);
+      }
+      q.Ac = cadd(q.Ac, c);
+      q.Bc = cmk(fma(c.x, dx, q.Bc.x), fma(c.y, dx, q.Bc.y));
+    };
+    int* recj = reinterpret_cast<int*>(pvv + PV_RECV + PV_RUNV);  // (group, lane, slot) piece
+    int* runL = recj + PV_GROUPS * 64;                               // run start lane
+    int* runS = runL + 32;                                           // run start slot
+    int* runG = runS + 32;                                           // run group
+    int* runJ = runG + 32;                                           // run piece
+    double2* recv = pvv;                                             // (group, lane, slot) A, B
+    double2* runv = pvv + PV_RECV;                                   // run A, B
+    int nruns = 0, nl[PV_GROUPS] = {0, 0, 0};
+    // a lane's two pieces to shared memory; run starts get ids in
+    // (lane, slot) order after the runs of the earlier groups
+    auto records = [&](int gi, const PvSlot& q, int dir) {
+      const int j0 = (q.jd >= 0) ? q.jd : q.jc, j1 = (q.jd >= 0) ? q.jc : -1;
+      const int rb = (gi * 32 + lane) * 2;
+      recj[rb] = j0;
+      recj[rb + 1] = j1;
+      recv[rb * 2] = (q.jd >= 0) ? q.Ad : q.Ac;
+      recv[rb * 2 + 1] = (q.jd >= 0) ? q.Bd : q.Bc;
+      recv[rb * 2 + 2] = (q.jd >= 0) ? q.Ac : cmk(0.0, 0.0);
+      recv[rb * 2 + 3] = (q.jd >= 0) ? q.Bc : cmk(0.0, 0.0);
+      const int last = (j1 >= 0) ? j1 : j0;
+      const int prev = __shfl_up_sync(0xffffffffu, last, 1);
+      const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
+      const bool st1 = (j1 >= 0);
+      if (j0 >= 0 && lane > 0 && (prev < 0 || (dir > 0 ? j0 < prev : j0 > prev))) bad = true;
+      const unsigned m0 = __ballot_sync(0xffffffffu, st0), m1 = __ballot_sync(0xffffffffu, st1);
+      const unsigned lt = (1u << lane) - 1u;
+      const int nr = __popc(m0) + __popc(m1);
+      if (nruns + nr <= 32) {
+        const int id0 = nruns + __popc(m0 & lt) + __popc(m1 & lt), id1 = id0 + (st0 ? 1 : 0);
+        if (st0) {
+          runL[id0] = lane;
+          runS[id0] = 0;
+          runG[id0] = gi;
+        }
+        if (st1) {
+          runL[id1] = lane;
+          runS[id1] = 1;
+          runG[id1] = gi;
+        }
+      }
+      nruns += nr;
+      nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
+    };
+    if (sym) {
+      const int per = (NP + 31) / 32;
       const int k0 = lane * per, k1 = min(NP, k0 + per);
-      Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
-      int ju = -1, jd = -1;  // raw node indices of the direct and mirrored points
-      const double pim2 = pim * pim;
+      PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
+      int ju = -1, jd = -1;
       for (int k = k0; k < k1; ++k) {
-        double p = (k == 0) ? pr : ((k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k);
-        double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-        double dx = p - pr, pm = 2.0 * pr - p;
-        double rr = wk * rcp_fast(fma(dx, dx, pim2));
-        double2 K = cmk(dx * rr, pim * rr);
+        double p;
+        double2 K;
+        sym_point(k, p, K);
+        const double pm = 2.0 * pr - p;
         ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
         jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
-        add(up, clampj(ju), p, K, 1.0);
-        add(dn, clampj(jd), pm, cmk(K.x, -K.y), -1.0);
+        const int cu = clampj(ju), cd = clampj(jd);
+        put(su, cu, p - S.ppar[cu], K, 1);
+        put(sd, cd, pm - S.ppar[cd], cmk(K.x, -K.y), -1);
       }
-      flush(up, 1.0);
-      flush(dn, -1.0);
+      records(0, su, 1);
+      records(1, sd, -1);
     } else {
       // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
       double fr = 0.0;
       for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
-        double p = (k == a.sys.M_P) ? pr + capDelta : pr + smdelta * k;
+        double p = (k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k));
         double wk = (k == a.sys.M_P) ? 1.0 : 2.0;
         double d = p - pr;
         fr += wk * ((d * d) / (d * d + pim * pim));
       }
       for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
       if (lane == 0) {
+        double2 H1[6], H2[6], H0[6];
         Hc(pr + dps, H1);
         Hc(pr - dps, H2);
-        double2 H0[6];
         Hc(pr, H0);
         double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
         for (int e = 0; e < 6; ++e) {
@@ -534,29 +615,133 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
         }
       }
     }
-    // tiny rest between pr + capDelta and ppar[upper]
-    int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
     if (ntiny > 0) {
-      double corr = ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta;
       const int per = (ntiny + 1 + 31) / 32;
       const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
-      Acc q{-1, cmk(0, 0), cmk(0, 0)};
+      PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
       int jt = -1;
       for (int k = k0; k < k1; ++k) {
-        double p = (k == 0) ? pr + capDelta : pr + capDelta + corr * smdelta * k;
-        double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
-        double dx = p - pr;
-        double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
+        double p;
+        double2 K;
+        tiny_point(k, p, K);
         jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
-        add(q, clampj(jt), p, cmk(dx * rr, pim * rr), 1.0);
+        const int ct = clampj(jt);
+        put(sq, ct, p - S.ppar[ct], K, 1);
       }
-      flush(q, 1.0);
+      records(2, sq, 1);
     }
-    for (int e = 0; e < 6; ++e)
-      for (int off = 16; off > 0; off >>= 1) {
-        T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
-        T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
+    const bool merged = !__any_sync(0xffffffffu, bad) && nruns <= 32;
+    if (merged && nruns > 0) {
+      __syncwarp();
+      // run totals in (lane, slot) order: the run's first slot, then slot 0
+      // of the following lanes up to the next run start of its group
+      if (lane < nruns) {
+        const int L = runL[lane], sl = runS[lane], gi = runG[lane];
+        int Ln = nl[0], sn = 0;
+        if (gi == 1) Ln = nl[1];
+        if (gi == 2) Ln = nl[2];
+        if (lane + 1 < nruns && runG[lane + 1] == gi) {
+          Ln = runL[lane + 1];
+          sn = runS[lane + 1];
+        }
+        const int rb = (gi * 32 + L) * 2 + sl;
+        double2 A = recv[rb * 2], B = recv[rb * 2 + 1];
+        for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
+          const int r2 = (gi * 32 + L2) * 2;
+          A = cadd(A, recv[r2 * 2]);
+          B = cadd(B, recv[r2 * 2 + 1]);
+        }
+        runJ[lane] = recj[rb];
+        runv[lane * 2] = A;
+        runv[lane * 2 + 1] = B;
       }
+      __syncwarp();
+      // (run, entry) pairs: h A + s B, mirrored runs with the minus sign;
+      // the products overwrite the lane records
+      double2* contrib = recv;
+      for (int q = lane; q < nruns * 6; q += 32) {
+        const int rho = q / 6, e = q % 6;
+        double2 h, sl;
+        node1(runJ[rho], e, h, sl);
+        double2 t = cadd(cmul(h, runv[rho * 2]), cmul(sl, runv[rho * 2 + 1]));
+        contrib[q] = (runG[rho] == 1) ? cmk(-t.x, -t.y) : t;
+      }
+      __syncwarp();
+      // component c of T: the runs in order
+      double acc = 0.0;
+      if (lane < 12) {
+        const int e = lane >> 1;
+        for (int rho = 0; rho < nruns; ++rho) acc += (lane & 1) ? contrib[rho * 6 + e].y : contrib[rho * 6 + e].x;
+      }
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        const double tx = __shfl_sync(0xffffffffu, acc, 2 * e), ty = __shfl_sync(0xffffffffu, acc, 2 * e + 1);
+        T[e] = cadd(T[e], cmk(tx, ty));
+      }
+    } else if (!merged) {
+      // per-lane piece sums flushed as the piece changes, then a warp sum
+      struct Acc {
+        int jc;
+        double2 A, B;
+      };
+      auto flush = [&](Acc& q, double sign) {
+        if (q.jc < 0) return;
+        double2 h[6], sl[6];
+        node(q.jc, h, sl);
+#pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          double2 t = cadd(cmul(h[e], q.A), cmul(sl[e], q.B));
+          T[e] = cmk(fma(sign, t.x, T[e].x), fma(sign, t.y, T[e].y));
+        }
+        q.A = q.B = cmk(0.0, 0.0);
+      };
+      auto add = [&](Acc& q, int jc, double p, double2 c, double sign) {
+        if (jc != q.jc) {
+          flush(q, sign);
+          q.jc = jc;
+        }
+        double dx = p - S.ppar[jc];
+        q.A = cadd(q.A, c);
+        q.B = cmk(fma(c.x, dx, q.B.x), fma(c.y, dx, q.B.y));
+      };
+      if (sym) {
+        const int per = (NP + 31) / 32;
+        const int k0 = lane * per, k1 = min(NP, k0 + per);
+        Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
+        int ju = -1, jd = -1;
+        for (int k = k0; k < k1; ++k) {
+          double p;
+          double2 K;
+          sym_point(k, p, K);
+          const double pm = 2.0 * pr - p;
+          ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
+          jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
+          add(up, clampj(ju), p, K, 1.0);
+          add(dn, clampj(jd), pm, cmk(K.x, -K.y), -1.0);
+        }
+        flush(up, 1.0);
+        flush(dn, -1.0);
+      }
+      if (ntiny > 0) {
+        const int per = (ntiny + 1 + 31) / 32;
+        const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
+        Acc q{-1, cmk(0, 0), cmk(0, 0)};
+        int jt = -1;
+        for (int k = k0; k < k1; ++k) {
+          double p;
+          double2 K;
+          tiny_point(k, p, K);
+          jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
+          add(q, clampj(jt), p, K, 1.0);
+        }
+        flush(q, 1.0);
+      }
+      for (int e = 0; e < 6; ++e)
+        for (int off = 16; off > 0; off >>= 1) {
+          T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
+          T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
+        }
+    }
     // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
     double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
     for (int e = 0; e < 6; ++e) res[e] = cscale(cmul(pref[e], T[e]), scale);
@@ -1073,7 +1258,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
   int maxN = c->sys.nperp;
-  size_t smem = (size_t)RES_WARPS * res_warp_smem(maxN) * sizeof(double2);
+  size_t smem = (size_t)RES_WARPS * res_warp_smem(maxN, res_win(c->sys.positions_principal)) * sizeof(double2);
   if (smem > 48 * 1024 && (size_t)c->res_smem_set < smem) {
     ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     c->res_smem_set = (int)smem;
@@ -1210,7 +1395,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   a.cgroup = 1;
   k_pole_sums<false><<<dim3(tiles, S_, a.nchunk), 128, 0, st>>>(a, om, n, js, part, nullptr);
   ALPS_CUDA_TRY(cudaGetLastError());
-  size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp) * sizeof(double2);
+  size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp, res_win(c->sys.positions_principal)) * sizeof(double2);
   if (smem > 48 * 1024)
     ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   long blocks = ((long)nslots + RES_WARPS - 1) / RES_WARPS;

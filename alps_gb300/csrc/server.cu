@@ -411,9 +411,6 @@ void alps_server::run() {
         }
         Group& g = groups[rq->ctx];
         g.ctx = rq->ctx;
-        // many small batches share the GPU: fewer, longer pole-sum blocks
-        // per batch (the partial sums, and so the results, are unchanged)
-        rq->ctx->chunk_group = 8;
         Active* a = new Active();
         a->rq = rq;
         a->id = itq->first;

@@ -120,6 +120,20 @@ def test_disp_chi_parity_small(api, k, precision):
         _disp_close(O, G, om, "%s k=%s" % (om, k))
 
 
+@pytest.mark.parametrize("precision", PRECISIONS)
+def test_principal_value_point_on_piece_boundary(api, precision):
+    """At omega = 1 + 0.05i, k = (1, 0.3) the proton order n = 2 resonates at
+    p_res = -10/3 and the symmetric sum's point k = 50 lands exactly on
+    p_par = -2.875 = pp(12) + dppar/2, the boundary between two pieces of
+    funct_g.  Rounding that point through a fused multiply-add moves it to
+    the other piece (chi off by ~1e-6); the reference's rounding keeps it."""
+    O, G = _pair(api, _small(), precision=precision)
+    O.set_k(1.0, 0.3)
+    G.set_k(1.0, 0.3)
+    for om in (1.0 + 0.05j, 2.0 - 0.1j, 1.0 - 0.05j):
+        _disp_close(O, G, om, "%s boundary point" % om)
+
+
 def test_disp_batch_matches_single(api):
     # the split of the p_par sums over threads depends on the batch size, so a
     # value alone and in a batch agree to rounding; the same batch twice is
