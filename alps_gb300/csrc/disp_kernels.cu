@@ -34,6 +34,7 @@ struct DispArgs {
   int relcap;    // order slots per relativistic species (max nmax + 1), 0 if none
   int has_bm;    // some species go through the NHDS closed form
   int cgroup;    // order chunks per pole-sum block
+  int ipw;       // resonant items per warp of k_resonant (1..32)
 };
 
 namespace {
@@ -354,11 +355,36 @@ __device__ inline double2 h_node(const double* Vn, int j, int e, double2 o, doub
 // node window of the principal-value sum: nodes lower-2 .. upper+2
 __host__ __device__ inline int res_win(int M_I) { return (2 * M_I + 8 < RES_WIN) ? 2 * M_I + 8 : RES_WIN; }
 
-// per-warp shared memory in double2: the window (h, s) and a region used
-// first by the principal-value records, then by the Landau rows
-__host__ __device__ inline size_t res_warp_smem(int N, int W) {
+// what the warp phase of k_resonant needs of one item
+struct __align__(16) ResItem {
+  double pr, pim;     // complex resonance momentum
+  int lower, upper;   // principal-value window
+  int nn, work;       // signed order; bit 0 principal value, bit 1 Landau rows, lf << 2
+  int w, s;           // omega, species
+  double2 pref[6];    // T-tensor prefactors
+};
+
+// the region used first by the principal-value records, then by the Landau
+// rows, in double2
+__host__ __device__ inline size_t res_region(int N) {
   const size_t rows = 3 * (size_t)(N + 1);
-  return (size_t)W * 12 + (rows > PV_SMEM ? rows : (size_t)PV_SMEM);
+  return rows > PV_SMEM ? rows : (size_t)PV_SMEM;
+}
+
+// per-warp shared memory in double2: the window (h, s), the records / rows
+// region, the warp's 32 items and 6 values handed to lanes 0-5
+__host__ __device__ inline size_t res_warp_smem(int N, int W) {
+  return (size_t)W * 12 + res_region(N) + 32 * (sizeof(ResItem) / sizeof(double2)) + 6;
+}
+
+// Items per warp: a warp does the per-item scalar work one item per lane,
+// then the vector work of its items one after another.  Large batches take
+// 32 per warp; small ones spread their items over more warps (a single
+// omega's few resonant orders run side by side, as latency wants).
+inline int res_items_per_warp(long nslots) {
+  const long warps_wanted = 152L * 12;  // SMs x resident warps of k_resonant
+  long ipw = nslots / warps_wanted;
+  return (int)(ipw < 1 ? 1 : (ipw > 32 ? 32 : ipw));
 }
 
 __device__ inline double2 crcp(double2 z) {
@@ -366,348 +392,306 @@ __device__ inline double2 crcp(double2 z) {
   return cmk(z.x * r, -z.y * r);
 }
 
-__global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, const double2* __restrict__ om,
+__global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, const double2* __restrict__ om,
                                                               int n_om, const int* __restrict__ count,
                                                               const int* __restrict__ slot_nn, double2* items,
                                                               int* flags) {
   extern __shared__ double2 sm[];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int S_ = a.sys.nspec;
-  long item = (long)blockIdx.x * RES_WARPS + warp;
-  long total = (long)n_om * S_ * a.rcap;
-  if (item >= total) return;
-  int r = (int)(item % a.rcap);
-  int s = (int)((item / a.rcap) % S_);
-  int w = (int)(item / ((long)a.rcap * S_));
-  if (r >= count[(size_t)w * S_ + s]) return;
-  const SpecDev& S = a.sp[s];
-  const int nn = slot_nn[((size_t)w * S_ + s) * a.rcap + r];
-  const int n = nn < 0 ? -nn : nn;
-  const double2 o = om[w];
-  const int M = S.M, N = S.N;
-  const double kpar = a.sys.kpar, kappa = kpar / S.ms;
-  const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
-  double2 pref[6];
-  t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
-  ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
-  const double* Vn = S.V + (size_t)n * (M - 1) * 12;
+  const int N = a.sp[0].N;  // every species has the same p_perp grid
   const int W = res_win(a.sys.M_I);
   double2* wh = sm + (size_t)warp * res_warp_smem(N, W);  // node values h
   double2* ws = wh + W * 6;                                // node slopes s
   double2* pvv = ws + W * 6;                               // principal-value records
   double2* frow = pvv;                                     // f(i, p_res), after them
-  double2* fpr = frow + (N + 1);                        // f(i, p_res + dppar)
-  double2* fmr = fpr + (N + 1);                         // f(i, p_res - dppar)
-  double2 res[6];
-  for (int e = 0; e < 6; ++e) res[e] = cmk(0.0, 0.0);
+  double2* fpr = frow + (N + 1);                           // f(i, p_res + dppar)
+  double2* fmr = fpr + (N + 1);                            // f(i, p_res - dppar)
+  ResItem* ri = reinterpret_cast<ResItem*>(pvv + res_region(N));
+  double2* tb = reinterpret_cast<double2*>(ri + 32);      // values handed to lanes 0-5
+  const long total = (long)n_om * S_ * a.rcap;
+  const long item0 = ((long)blockIdx.x * RES_WARPS + warp) * a.ipw;
+  const long item = item0 + lane;
 
-  // ---- principal value window (case 3) ----
-  if (g.kind == 3) {
-    const double pr = g.pr, pim = g.pi;
-    const double dpa = S.dppar_abs, dps = S.dppar;
-    const int jw0 = max(1, g.lower - 2), jw1 = min(M - 1, g.upper + 2);
-    const int nw = jw1 - jw0 + 1;
-    const bool winok = nw <= W;
-    if (winok) {
-      for (int t = lane; t < nw * 6; t += 32) {
-        int jj = t / 6, e = t % 6;
-        wh[jj * 6 + e] = h_node(Vn, jw0 + jj, e, o, kappa);
-      }
-      __syncwarp();
-      for (int t = lane; t < nw * 6; t += 32) {
-        int jj = t / 6, e = t % 6;
-        if (jj >= 1 && jj + 1 < nw) ws[jj * 6 + e] = cscale(csub(wh[(jj + 1) * 6 + e], wh[(jj - 1) * 6 + e]), 0.5 / dpa);
-      }
-    }
-    __syncwarp();
-    double2 T[6];
-    for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
-    // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
-    // interpolant serves p is "the last ipar in 1..npar-1 with
-    // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
-    const double idpa = 1.0 / dpa, half = 0.5 * dpa;
-    // last node in 1..M-1 within half a spacing of p, or 0 (the search of
-    // funct_g before its clamp); the candidates bracket the nearest node
-    auto piece_raw = [&](double p) {
-      int jr = 0;
-      double jd = floor((p - S.ppar[0]) * idpa + 0.5);
-      if (jd > -10.0 && jd < (double)M + 10.0) {
-        int j0 = (int)jd;
-        int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
-        for (int jj = hi; jj >= lo; --jj)
-          if (fabs(S.ppar[jj] - p) <= half) { jr = jj; break; }
-      }
-      return jr;
-    };
-    auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
-    auto piece = [&](double p) { return clampj(piece_raw(p)); };
-    // the same index for p increasing (up) or decreasing (down) from a known
-    // raw index: |pp(j) - p| is monotone in p, so the last valid node moves
-    // by single steps
-    auto piece_up = [&](int jr, double p) {
-      if (jr == 0) return piece_raw(p);
-      while (jr < M - 1 && fabs(S.ppar[jr + 1] - p) <= half) ++jr;
-      return (fabs(S.ppar[jr] - p) <= half) ? jr : piece_raw(p);
-    };
-    auto piece_down = [&](int jr, double p) {
-      if (jr == 0) return piece_raw(p);
-      while (jr >= 1 && !(fabs(S.ppar[jr] - p) <= half)) --jr;
-      return (jr >= 1) ? jr : piece_raw(p);
-    };
-    // node value h and centred slope s of entry e at node jc
-    auto node1 = [&](int jc, int e, double2& h, double2& sl) {
-      if (winok && jc - 1 >= jw0 && jc + 1 <= jw1) {
-        h = wh[(jc - jw0) * 6 + e];
-        sl = ws[(jc - jw0) * 6 + e];
-      } else {
-        h = h_node(Vn, jc, e, o, kappa);
-        sl = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
-      }
-    };
-    auto node = [&](int jc, double2* h, double2* sl) {
-#pragma unroll
-      for (int e = 0; e < 6; ++e) node1(jc, e, h[e], sl[e]);
-    };
-    auto Hc = [&](double p, double2* H) {
-      int jc = piece(p);
-      double2 h[6], sl[6];
-      node(jc, h, sl);
-      double dx = p - S.ppar[jc];
-#pragma unroll
-      for (int e = 0; e < 6; ++e) H[e] = cmk(fma(sl[e].x, dx, h[e].x), fma(sl[e].y, dx, h[e].y));
-    };
-    const double capDelta = pr - S.ppar[g.lower];
-    const double smdelta = capDelta / (1.0 * a.sys.M_P);
-    const bool sym = fabs(pim) > a.sys.Tlim;
-    const int NP = a.sys.M_P + 1;
-    // tiny rest between pr + capDelta and ppar[upper]
-    const int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
-    const double corr = (ntiny > 0) ? ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
-    // the sample points: k in 0..M_P of the symmetric sum (group 0 direct,
-    // group 1 mirrored), k in 0..ntiny of the tiny rest (group 2).  Their
-    // coordinates are rounded as integrate_res writes them, without fused
-    // multiply-adds: a point can sit exactly on a piece boundary
-    // pp(j) + dppar/2, and its piece must be the reference's.
-    auto sym_point = [&](int k, double& p, double2& K) {
-      p = (k == 0) ? pr
-                   : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
-      double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-      double dx = p - pr;
-      double rr = wk * rcp_fast(fma(dx, dx, pim * pim));
-      K = cmk(dx * rr, pim * rr);
-    };
-    auto tiny_point = [&](int k, double& p, double2& K) {
-      p = (k == 0) ? __dadd_rn(pr, capDelta)
-                   : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
-      double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
-      double dx = p - pr;
-      double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
-      K = cmk(dx * rr, pim * rr);
-    };
-
-    // Sum_k c_k H(p_k) with H linear on each piece jc needs, per piece, only
-    // A = Sum c_k and B = Sum c_k (p_k - pp(jc)); the piece adds h A + s B.
-    // Each lane walks a run of consecutive k and keeps the sums of at most
-    // two pieces (pieces are M_P/(M_I+1) or more points wide, far wider
-    // than a lane's run); the lanes' piece sums are merged per piece in
-    // shared memory in lane order, and each (piece, entry) pair is then one
-    // thread's h A + s B.  A lane that meets a third piece, or indices that
-    // are not monotone in k, send the item to the per-lane flush below.
-    struct PvSlot {
-      int jd, jc;          // finished piece (-1: none), current piece
-      double2 Ad, Bd, Ac, Bc;
-    };
-    bool bad = false;
-    auto put = [&](PvSlot& q, int j, double dx, double2 c, int dir) {
-      if (j != q.jc) {
-        if (q.jc >= 0) {
-          if (q.jd >= 0 || (dir > 0 ? j < q.jc : j > q.jc)) bad = true;
-          q.jd = q.jc;
-          q.Ad = q.Ac;
-          q.Bd = q.Bc;
-        }
-        q.jc = j;
-        q.Ac = q.Bc = cmk(0.0, 0.0);
-      }
-      q.Ac = cadd(q.Ac, c);
-      q.Bc = cmk(fma(c.x, dx, q.Bc.x), fma(c.y, dx, q.Bc.y));
-    };
-    int* recj = reinterpret_cast<int*>(pvv + PV_RECV + PV_RUNV);  // (group, lane, slot) piece
-    int* runL = recj + PV_GROUPS * 64;                               // run start lane
-    int* runS = runL + 32;                                           // run start slot
-    int* runG = runS + 32;                                           // run group
-    int* runJ = runG + 32;                                           // run piece
-    double2* recv = pvv;                                             // (group, lane, slot) A, B
-    double2* runv = pvv + PV_RECV;                                   // run A, B
-    int nruns = 0, nl[PV_GROUPS] = {0, 0, 0};
-    // a lane's two pieces to shared memory; run starts get ids in
-    // (lane, slot) order after the runs of the earlier groups
-    auto records = [&](int gi, const PvSlot& q, int dir) {
-      const int j0 = (q.jd >= 0) ? q.jd : q.jc, j1 = (q.jd >= 0) ? q.jc : -1;
-      const int rb = (gi * 32 + lane) * 2;
-      recj[rb] = j0;
-      recj[rb + 1] = j1;
-      recv[rb * 2] = (q.jd >= 0) ? q.Ad : q.Ac;
-      recv[rb * 2 + 1] = (q.jd >= 0) ? q.Bd : q.Bc;
-      recv[rb * 2 + 2] = (q.jd >= 0) ? q.Ac : cmk(0.0, 0.0);
-      recv[rb * 2 + 3] = (q.jd >= 0) ? q.Bc : cmk(0.0, 0.0);
-      const int last = (j1 >= 0) ? j1 : j0;
-      const int prev = __shfl_up_sync(0xffffffffu, last, 1);
-      const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
-      const bool st1 = (j1 >= 0);
-      if (j0 >= 0 && lane > 0 && (prev < 0 || (dir > 0 ? j0 < prev : j0 > prev))) bad = true;
-      const unsigned m0 = __ballot_sync(0xffffffffu, st0), m1 = __ballot_sync(0xffffffffu, st1);
-      const unsigned lt = (1u << lane) - 1u;
-      const int nr = __popc(m0) + __popc(m1);
-      if (nruns + nr <= 32) {
-        const int id0 = nruns + __popc(m0 & lt) + __popc(m1 & lt), id1 = id0 + (st0 ? 1 : 0);
-        if (st0) {
-          runL[id0] = lane;
-          runS[id0] = 0;
-          runG[id0] = gi;
-        }
-        if (st1) {
-          runL[id1] = lane;
-          runS[id1] = 1;
-          runG[id1] = gi;
+  // ---- one item per thread: geometry, prefactors, factorised Landau rows ----
+  int work = 0;
+  if (lane < a.ipw && item < total) {
+    const int r = (int)(item % a.rcap);
+    const int s = (int)((item / a.rcap) % S_);
+    const int w = (int)(item / ((long)a.rcap * S_));
+    if (r < count[(size_t)w * S_ + s]) {
+      const SpecDev& S = a.sp[s];
+      const int nn = slot_nn[((size_t)w * S_ + s) * a.rcap + r];
+      const int n = nn < 0 ? -nn : nn;
+      const double2 o = om[w];
+      const double kpar = a.sys.kpar;
+      const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+      double2 pref[6];
+      t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
+      const ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+      double2 res[6];
+      for (int e = 0; e < 6; ++e) res[e] = cmk(0.0, 0.0);
+      const int lf = (o.y < 0.0) ? 2 : ((o.y == 0.0) ? 1 : 0);
+      bool rows = lf > 0;
+      if (lf > 0 && S.lmom) {
+        // factorised rows: valid when the row deviation |delta_i(p')| <= 1e-5
+        // for p' = p, p +- dppar (second-order remainder <= 1.7e-16)
+        const double2 p = cmk(g.pr, g.pi);
+        const double pd = S.dppar_abs;
+        const double ap = hypot(p.x, p.y) + pd;
+        const double bound = S.la * ap * ap + S.lb * ap + S.lc;
+        if (bound <= 1e-5) {
+          rows = false;
+          auto gauss = [&](double2 x) {
+            double2 d = cmk(x.x - S.p3r, x.y);
+            return cexp_d(cscale(cmul(d, d), -S.p2r));
+          };
+          auto poly = [&](const double* m, double2 x) {
+            double2 acc = cmk(m[4], 0.0);
+            for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
+            return acc;
+          };
+          const double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
+          // the row Gaussian at p, p + dppar, p - dppar
+          const double2 G0 = gauss(p), Gp = gauss(xp), Gm = gauss(xm);
+          const bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
+                            (cabs_(G0) * S.min_a0 == 0.0);
+          if (!zero) {
+            // the moment polynomials of family F at p + dppar, p - dppar
+            // (d/dp_par moments) and p (d/dp_perp moments)
+            const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
+            double2 sumF[3];
+            for (int F = 0; F < 3; ++F) {
+              const double* lm = S.lmom + ((size_t)n * 3 + F) * 10;
+              const double2 Pxp = poly(lm, xp), Pxm = poly(lm, xm), Ppp = poly(lm + 5, p);
+              const double2 Spar = cscale(csub(cmul(Gp, Pxp), cmul(Gm, Pxm)), 1.0 / (2.0 * pd));
+              const double2 Sperp = cmul(G0, Ppp);
+              // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp)
+              sumF[F] = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
+            }
+            const double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+            for (int e = 0; e < 6; ++e) {
+              const double2 ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
+              const int fam = (e == 1) ? 1 : ((e == 3 || e == 5) ? 2 : 0);
+              res[e] = cmul(cmul(cmul(pref[e], ce), sumF[fam]), ifac);
+            }
+          }
         }
       }
-      nruns += nr;
-      nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
-    };
-    if (sym) {
-      const int per = (NP + 31) / 32;
-      const int k0 = lane * per, k1 = min(NP, k0 + per);
-      PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
-      int ju = -1, jd = -1;
-      for (int k = k0; k < k1; ++k) {
-        double p;
-        double2 K;
-        sym_point(k, p, K);
-        const double pm = 2.0 * pr - p;
-        ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
-        jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
-        const int cu = clampj(ju), cd = clampj(jd);
-        put(su, cu, p - S.ppar[cu], K, 1);
-        put(sd, cd, pm - S.ppar[cd], cmk(K.x, -K.y), -1);
-      }
-      records(0, su, 1);
-      records(1, sd, -1);
-    } else {
-      // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
-      double fr = 0.0;
-      for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
-        double p = (k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k));
-        double wk = (k == a.sys.M_P) ? 1.0 : 2.0;
-        double d = p - pr;
-        fr += wk * ((d * d) / (d * d + pim * pim));
-      }
-      for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
-      if (lane == 0) {
-        double2 H1[6], H2[6], H0[6];
-        Hc(pr + dps, H1);
-        Hc(pr - dps, H2);
-        Hc(pr, H0);
-        double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
-        for (int e = 0; e < 6; ++e) {
-          double2 gp = cscale(csub(H1[e], H2[e]), 1.0 / (2.0 * dps));
-          T[e] = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0[e]));
-        }
-      }
-    }
-    if (ntiny > 0) {
-      const int per = (ntiny + 1 + 31) / 32;
-      const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
-      PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
-      int jt = -1;
-      for (int k = k0; k < k1; ++k) {
-        double p;
-        double2 K;
-        tiny_point(k, p, K);
-        jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
-        const int ct = clampj(jt);
-        put(sq, ct, p - S.ppar[ct], K, 1);
-      }
-      records(2, sq, 1);
-    }
-    const bool merged = !__any_sync(0xffffffffu, bad) && nruns <= 32;
-    if (merged && nruns > 0) {
-      __syncwarp();
-      // run totals in (lane, slot) order: the run's first slot, then slot 0
-      // of the following lanes up to the next run start of its group
-      if (lane < nruns) {
-        const int L = runL[lane], sl = runS[lane], gi = runG[lane];
-        int Ln = nl[0], sn = 0;
-        if (gi == 1) Ln = nl[1];
-        if (gi == 2) Ln = nl[2];
-        if (lane + 1 < nruns && runG[lane + 1] == gi) {
-          Ln = runL[lane + 1];
-          sn = runS[lane + 1];
-        }
-        const int rb = (gi * 32 + L) * 2 + sl;
-        double2 A = recv[rb * 2], B = recv[rb * 2 + 1];
-        for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
-          const int r2 = (gi * 32 + L2) * 2;
-          A = cadd(A, recv[r2 * 2]);
-          B = cadd(B, recv[r2 * 2 + 1]);
-        }
-        runJ[lane] = recj[rb];
-        runv[lane * 2] = A;
-        runv[lane * 2 + 1] = B;
-      }
-      __syncwarp();
-      // (run, entry) pairs: h A + s B, mirrored runs with the minus sign;
-      // the products overwrite the lane records
-      double2* contrib = recv;
-      for (int q = lane; q < nruns * 6; q += 32) {
-        const int rho = q / 6, e = q % 6;
-        double2 h, sl;
-        node1(runJ[rho], e, h, sl);
-        double2 t = cadd(cmul(h, runv[rho * 2]), cmul(sl, runv[rho * 2 + 1]));
-        contrib[q] = (runG[rho] == 1) ? cmk(-t.x, -t.y) : t;
-      }
-      __syncwarp();
-      // component c of T: the runs in order
-      double acc = 0.0;
-      if (lane < 12) {
-        const int e = lane >> 1;
-        for (int rho = 0; rho < nruns; ++rho) acc += (lane & 1) ? contrib[rho * 6 + e].y : contrib[rho * 6 + e].x;
-      }
-#pragma unroll
+      work = ((g.kind == 3) ? 1 : 0) | (rows ? 2 : 0);
+      double2* out = items + item * 6;
       for (int e = 0; e < 6; ++e) {
-        const double tx = __shfl_sync(0xffffffffu, acc, 2 * e), ty = __shfl_sync(0xffffffffu, acc, 2 * e + 1);
-        T[e] = cadd(T[e], cmk(tx, ty));
+        const bool skip = (n == 0 && (e == 0 || e == 3 || e == 4));
+        out[e] = skip ? cmk(0.0, 0.0) : res[e];
       }
-    } else if (!merged) {
-      // per-lane piece sums flushed as the piece changes, then a warp sum
-      struct Acc {
-        int jc;
-        double2 A, B;
+      ResItem& it = ri[lane];
+      it.pr = g.pr;
+      it.pim = g.pi;
+      it.lower = g.lower;
+      it.upper = g.upper;
+      it.nn = nn;
+      it.work = work | (lf << 2);
+      it.w = w;
+      it.s = s;
+      for (int e = 0; e < 6; ++e) it.pref[e] = pref[e];
+    }
+  }
+  __syncwarp();
+
+  // ---- one item per warp: the principal-value sums and the Landau rows ----
+  unsigned pend = __ballot_sync(0xffffffffu, work != 0);
+  while (pend) {
+    const int il = __ffs(pend) - 1;
+    pend &= pend - 1;
+    const ResItem& it = ri[il];
+    const int s = it.s, w = it.w, nn = it.nn;
+    const int n = nn < 0 ? -nn : nn;
+    const int wk = it.work & 3, lf = it.work >> 2;
+    const SpecDev& S = a.sp[s];
+    const double2 o = om[w];
+    const int M = S.M;
+    const double kpar = a.sys.kpar, kappa = kpar / S.ms;
+    const double* Vn = S.V + (size_t)n * (M - 1) * 12;
+    double2* out = items + (item0 + il) * 6;
+
+    // ---- principal value window (case 3) ----
+    if (wk & 1) {
+      const double pr = it.pr, pim = it.pim;
+      const double dpa = S.dppar_abs, dps = S.dppar;
+      const int jw0 = max(1, it.lower - 2), jw1 = min(M - 1, it.upper + 2);
+      const int nw = jw1 - jw0 + 1;
+      const bool winok = nw <= W;
+      if (winok) {
+        for (int t = lane; t < nw * 6; t += 32) {
+          int jj = t / 6, e = t % 6;
+          wh[jj * 6 + e] = h_node(Vn, jw0 + jj, e, o, kappa);
+        }
+        __syncwarp();
+        for (int t = lane; t < nw * 6; t += 32) {
+          int jj = t / 6, e = t % 6;
+          if (jj >= 1 && jj + 1 < nw) ws[jj * 6 + e] = cscale(csub(wh[(jj + 1) * 6 + e], wh[(jj - 1) * 6 + e]), 0.5 / dpa);
+        }
+      }
+      __syncwarp();
+      double2 T[6];
+      for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
+      // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
+      // interpolant serves p is "the last ipar in 1..npar-1 with
+      // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
+      const double idpa = 1.0 / dpa, half = 0.5 * dpa;
+      // last node in 1..M-1 within half a spacing of p, or 0 (the search of
+      // funct_g before its clamp); the candidates bracket the nearest node
+      auto piece_raw = [&](double p) {
+        int jr = 0;
+        double jd = floor((p - S.ppar[0]) * idpa + 0.5);
+        if (jd > -10.0 && jd < (double)M + 10.0) {
+          int j0 = (int)jd;
+          int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
+          for (int jj = hi; jj >= lo; --jj)
+            if (fabs(S.ppar[jj] - p) <= half) { jr = jj; break; }
+        }
+        return jr;
       };
-      auto flush = [&](Acc& q, double sign) {
-        if (q.jc < 0) return;
+      auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
+      auto piece = [&](double p) { return clampj(piece_raw(p)); };
+      // the same index for p increasing (up) or decreasing (down) from a known
+      // raw index: |pp(j) - p| is monotone in p, so the last valid node moves
+      // by single steps
+      auto piece_up = [&](int jr, double p) {
+        if (jr == 0) return piece_raw(p);
+        while (jr < M - 1 && fabs(S.ppar[jr + 1] - p) <= half) ++jr;
+        return (fabs(S.ppar[jr] - p) <= half) ? jr : piece_raw(p);
+      };
+      auto piece_down = [&](int jr, double p) {
+        if (jr == 0) return piece_raw(p);
+        while (jr >= 1 && !(fabs(S.ppar[jr] - p) <= half)) --jr;
+        return (jr >= 1) ? jr : piece_raw(p);
+      };
+      // node value h and centred slope s of entry e at node jc
+      auto node1 = [&](int jc, int e, double2& h, double2& sl) {
+        if (winok && jc - 1 >= jw0 && jc + 1 <= jw1) {
+          h = wh[(jc - jw0) * 6 + e];
+          sl = ws[(jc - jw0) * 6 + e];
+        } else {
+          h = h_node(Vn, jc, e, o, kappa);
+          sl = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
+        }
+      };
+      auto node = [&](int jc, double2* h, double2* sl) {
+  #pragma unroll
+        for (int e = 0; e < 6; ++e) node1(jc, e, h[e], sl[e]);
+      };
+      auto Hc = [&](double p, double2* H) {
+        int jc = piece(p);
         double2 h[6], sl[6];
-        node(q.jc, h, sl);
-#pragma unroll
-        for (int e = 0; e < 6; ++e) {
-          double2 t = cadd(cmul(h[e], q.A), cmul(sl[e], q.B));
-          T[e] = cmk(fma(sign, t.x, T[e].x), fma(sign, t.y, T[e].y));
-        }
-        q.A = q.B = cmk(0.0, 0.0);
-      };
-      auto add = [&](Acc& q, int jc, double p, double2 c, double sign) {
-        if (jc != q.jc) {
-          flush(q, sign);
-          q.jc = jc;
-        }
+        node(jc, h, sl);
         double dx = p - S.ppar[jc];
-        q.A = cadd(q.A, c);
-        q.B = cmk(fma(c.x, dx, q.B.x), fma(c.y, dx, q.B.y));
+  #pragma unroll
+        for (int e = 0; e < 6; ++e) H[e] = cmk(fma(sl[e].x, dx, h[e].x), fma(sl[e].y, dx, h[e].y));
+      };
+      const double capDelta = pr - S.ppar[it.lower];
+      const double smdelta = capDelta / (1.0 * a.sys.M_P);
+      const bool sym = fabs(pim) > a.sys.Tlim;
+      const int NP = a.sys.M_P + 1;
+      // tiny rest between pr + capDelta and ppar[upper]
+      const int ntiny = (int)((S.ppar[it.upper] - pr - capDelta) / smdelta);
+      const double corr = (ntiny > 0) ? ((S.ppar[it.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
+      // the sample points: k in 0..M_P of the symmetric sum (group 0 direct,
+      // group 1 mirrored), k in 0..ntiny of the tiny rest (group 2).  Their
+      // coordinates are rounded as integrate_res writes them, without fused
+      // multiply-adds: a point can sit exactly on a piece boundary
+      // pp(j) + dppar/2, and its piece must be the reference's.
+      auto sym_point = [&](int k, double& p, double2& K) {
+        p = (k == 0) ? pr
+                     : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
+        double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
+        double dx = p - pr;
+        double rr = wk * rcp_fast(fma(dx, dx, pim * pim));
+        K = cmk(dx * rr, pim * rr);
+      };
+      auto tiny_point = [&](int k, double& p, double2& K) {
+        p = (k == 0) ? __dadd_rn(pr, capDelta)
+                     : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
+        double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
+        double dx = p - pr;
+        double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
+        K = cmk(dx * rr, pim * rr);
+      };
+
+      // Sum_k c_k H(p_k) with H linear on each piece jc needs, per piece, only
+      // A = Sum c_k and B = Sum c_k (p_k - pp(jc)); the piece adds h A + s B.
+      // Each lane walks a run of consecutive k and keeps the sums of at most
+      // two pieces (pieces are M_P/(M_I+1) or more points wide, far wider
+      // than a lane's run); the lanes' piece sums are merged per piece in
+      // shared memory in lane order, and each (piece, entry) pair is then one
+      // thread's h A + s B.  A lane that meets a third piece, or indices that
+      // are not monotone in k, send the item to the per-lane flush below.
+      struct PvSlot {
+        int jd, jc;          // finished piece (-1: none), current piece
+        double2 Ad, Bd, Ac, Bc;
+      };
+      bool bad = false;
+      auto put = [&](PvSlot& q, int j, double dx, double2 c, int dir) {
+        if (j != q.jc) {
+          if (q.jc >= 0) {
+            if (q.jd >= 0 || (dir > 0 ? j < q.jc : j > q.jc)) bad = true;
+            q.jd = q.jc;
+            q.Ad = q.Ac;
+            q.Bd = q.Bc;
+          }
+          q.jc = j;
+          q.Ac = q.Bc = cmk(0.0, 0.0);
+        }
+        q.Ac = cadd(q.Ac, c);
+        q.Bc = cmk(fma(c.x, dx, q.Bc.x), fma(c.y, dx, q.Bc.y));
+      };
+      int* recj = reinterpret_cast<int*>(pvv + PV_RECV + PV_RUNV);  // (group, lane, slot) piece
+      int* runL = recj + PV_GROUPS * 64;                               // run start lane
+      int* runS = runL + 32;                                           // run start slot
+      int* runG = runS + 32;                                           // run group
+      int* runJ = runG + 32;                                           // run piece
+      double2* recv = pvv;                                             // (group, lane, slot) A, B
+      double2* runv = pvv + PV_RECV;                                   // run A, B
+      int nruns = 0, nl[PV_GROUPS] = {0, 0, 0};
+      // a lane's two pieces to shared memory; run starts get ids in
+      // (lane, slot) order after the runs of the earlier groups
+      auto records = [&](int gi, const PvSlot& q, int dir) {
+        const int j0 = (q.jd >= 0) ? q.jd : q.jc, j1 = (q.jd >= 0) ? q.jc : -1;
+        const int rb = (gi * 32 + lane) * 2;
+        recj[rb] = j0;
+        recj[rb + 1] = j1;
+        recv[rb * 2] = (q.jd >= 0) ? q.Ad : q.Ac;
+        recv[rb * 2 + 1] = (q.jd >= 0) ? q.Bd : q.Bc;
+        recv[rb * 2 + 2] = (q.jd >= 0) ? q.Ac : cmk(0.0, 0.0);
+        recv[rb * 2 + 3] = (q.jd >= 0) ? q.Bc : cmk(0.0, 0.0);
+        const int last = (j1 >= 0) ? j1 : j0;
+        const int prev = __shfl_up_sync(0xffffffffu, last, 1);
+        const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
+        const bool st1 = (j1 >= 0);
+        if (j0 >= 0 && lane > 0 && (prev < 0 || (dir > 0 ? j0 < prev : j0 > prev))) bad = true;
+        const unsigned m0 = __ballot_sync(0xffffffffu, st0), m1 = __ballot_sync(0xffffffffu, st1);
+        const unsigned lt = (1u << lane) - 1u;
+        const int nr = __popc(m0) + __popc(m1);
+        if (nruns + nr <= 32) {
+          const int id0 = nruns + __popc(m0 & lt) + __popc(m1 & lt), id1 = id0 + (st0 ? 1 : 0);
+          if (st0) {
+            runL[id0] = lane;
+            runS[id0] = 0;
+            runG[id0] = gi;
+          }
+          if (st1) {
+            runL[id1] = lane;
+            runS[id1] = 1;
+            runG[id1] = gi;
+          }
+        }
+        nruns += nr;
+        nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
       };
       if (sym) {
         const int per = (NP + 31) / 32;
         const int k0 = lane * per, k1 = min(NP, k0 + per);
-        Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
+        PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
         int ju = -1, jd = -1;
         for (int k = k0; k < k1; ++k) {
           double p;
@@ -716,203 +700,268 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 4) k_resonant(DispArgs a, cons
           const double pm = 2.0 * pr - p;
           ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
           jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
-          add(up, clampj(ju), p, K, 1.0);
-          add(dn, clampj(jd), pm, cmk(K.x, -K.y), -1.0);
+          const int cu = clampj(ju), cd = clampj(jd);
+          put(su, cu, p - S.ppar[cu], K, 1);
+          put(sd, cd, pm - S.ppar[cd], cmk(K.x, -K.y), -1);
         }
-        flush(up, 1.0);
-        flush(dn, -1.0);
+        records(0, su, 1);
+        records(1, sd, -1);
+      } else {
+        // Tlim branch: g' * sum_k w_k (p-pr)^2/((p-pr)^2+pim^2) + sign(pim) i pi G(pr)/smdelta
+        double fr = 0.0;
+        for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
+          double p = (k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k));
+          double wk = (k == a.sys.M_P) ? 1.0 : 2.0;
+          double d = p - pr;
+          fr += wk * ((d * d) / (d * d + pim * pim));
+        }
+        for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
+        if (lane == 0) {
+          double2 H1[6], H2[6], H0[6];
+          Hc(pr + dps, H1);
+          Hc(pr - dps, H2);
+          Hc(pr, H0);
+          double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
+          for (int e = 0; e < 6; ++e) {
+            double2 gp = cscale(csub(H1[e], H2[e]), 1.0 / (2.0 * dps));
+            T[e] = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0[e]));
+          }
+        }
       }
       if (ntiny > 0) {
         const int per = (ntiny + 1 + 31) / 32;
         const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
-        Acc q{-1, cmk(0, 0), cmk(0, 0)};
+        PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
         int jt = -1;
         for (int k = k0; k < k1; ++k) {
           double p;
           double2 K;
           tiny_point(k, p, K);
           jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
-          add(q, clampj(jt), p, K, 1.0);
+          const int ct = clampj(jt);
+          put(sq, ct, p - S.ppar[ct], K, 1);
         }
-        flush(q, 1.0);
+        records(2, sq, 1);
       }
-      for (int e = 0; e < 6; ++e)
-        for (int off = 16; off > 0; off >>= 1) {
-          T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
-          T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
-        }
-    }
-    // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
-    double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
-    for (int e = 0; e < 6; ++e) res[e] = cscale(cmul(pref[e], T[e]), scale);
-  }
-
-  // ---- Landau term ----
-  int lf = (o.y < 0.0) ? 2 : ((o.y == 0.0) ? 1 : 0);
-  bool landau_done = false;
-  if (lf > 0 && S.lmom) {
-    // factorised rows: valid when the row deviation |delta_i(p')| <= 1e-5
-    // for p' = p, p +- dppar (second-order remainder <= 1.7e-16)
-    const double2 p = cmk(g.pr, g.pi);
-    const double pd = S.dppar_abs;
-    double ap = hypot(p.x, p.y) + pd;
-    double bound = S.la * ap * ap + S.lb * ap + S.lc;
-    if (bound <= 1e-5) {
-      landau_done = true;
-      auto gauss = [&](double2 x) {
-        double2 d = cmk(x.x - S.p3r, x.y);
-        return cexp_d(cscale(cmul(d, d), -S.p2r));
-      };
-      auto poly = [&](const double* m, double2 x) {
-        double2 acc = cmk(m[4], 0.0);
-        for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
-        return acc;
-      };
-      auto shfl2 = [&](double2 v, int src) {
-        return cmk(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-      };
-      const double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
-      // lanes 0-2: the row Gaussian at p, p + dppar, p - dppar
-      double2 Gl = cmk(0.0, 0.0);
-      if (lane < 3) Gl = gauss(lane == 1 ? xp : (lane == 2 ? xm : p));
-      const double2 G0 = shfl2(Gl, 0), Gp = shfl2(Gl, 1), Gm = shfl2(Gl, 2);
-      bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
-                  (cabs_(G0) * S.min_a0 == 0.0);
-      if (!zero) {
-        // lanes 0-8: the moment polynomials of family F = lane/3 at p + dppar,
-        // p - dppar (d/dp_par moments) and p (d/dp_perp moments)
-        double2 Pv = cmk(0.0, 0.0);
-        if (lane < 9) {
-          const double* lm = S.lmom + ((size_t)n * 3 + lane / 3) * 10;
-          const int wch = lane % 3;
-          Pv = (wch == 0) ? poly(lm, xp) : ((wch == 1) ? poly(lm, xm) : poly(lm + 5, p));
-        }
-        const int Fl = min(lane, 2);
-        const double2 Pxp = shfl2(Pv, 3 * Fl), Pxm = shfl2(Pv, 3 * Fl + 1), Ppp = shfl2(Pv, 3 * Fl + 2);
-        const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
-        double2 Spar = cscale(csub(cmul(Gp, Pxp), cmul(Gm, Pxm)), 1.0 / (2.0 * pd));
-        double2 Sperp = cmul(G0, Ppp);
-        // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp), family Fl
-        const double2 sumF = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
-        // lanes 0-5: entry e = lane
-        const int fam[6] = {0, 1, 0, 2, 0, 2};
-        double2 pe = pref[0], ce = cmk(1.0, 0.0);
-        int fe = 0;
-#pragma unroll
-        for (int e = 0; e < 6; ++e)
-          if (lane == e) {
-            pe = pref[e];
-            fe = fam[e];
-            ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
+      const bool merged = !__any_sync(0xffffffffu, bad) && nruns <= 32;
+      if (merged && nruns > 0) {
+        __syncwarp();
+        // run totals in (lane, slot) order: the run's first slot, then slot 0
+        // of the following lanes up to the next run start of its group
+        if (lane < nruns) {
+          const int L = runL[lane], sl = runS[lane], gi = runG[lane];
+          int Ln = nl[0], sn = 0;
+          if (gi == 1) Ln = nl[1];
+          if (gi == 2) Ln = nl[2];
+          if (lane + 1 < nruns && runG[lane + 1] == gi) {
+            Ln = runL[lane + 1];
+            sn = runS[lane + 1];
           }
-        const double2 sf = shfl2(sumF, fe);
-        const double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
-        const double2 contrib = cmul(cmul(cmul(pe, ce), sf), ifac);
-#pragma unroll
+          const int rb = (gi * 32 + L) * 2 + sl;
+          double2 A = recv[rb * 2], B = recv[rb * 2 + 1];
+          for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
+            const int r2 = (gi * 32 + L2) * 2;
+            A = cadd(A, recv[r2 * 2]);
+            B = cadd(B, recv[r2 * 2 + 1]);
+          }
+          runJ[lane] = recj[rb];
+          runv[lane * 2] = A;
+          runv[lane * 2 + 1] = B;
+        }
+        __syncwarp();
+        // (run, entry) pairs: h A + s B, mirrored runs with the minus sign;
+        // the products overwrite the lane records
+        double2* contrib = recv;
+        for (int q = lane; q < nruns * 6; q += 32) {
+          const int rho = q / 6, e = q % 6;
+          double2 h, sl;
+          node1(runJ[rho], e, h, sl);
+          double2 t = cadd(cmul(h, runv[rho * 2]), cmul(sl, runv[rho * 2 + 1]));
+          contrib[q] = (runG[rho] == 1) ? cmk(-t.x, -t.y) : t;
+        }
+        __syncwarp();
+        // component c of T: the runs in order
+        double acc = 0.0;
+        if (lane < 12) {
+          const int e = lane >> 1;
+          for (int rho = 0; rho < nruns; ++rho) acc += (lane & 1) ? contrib[rho * 6 + e].y : contrib[rho * 6 + e].x;
+        }
+  #pragma unroll
         for (int e = 0; e < 6; ++e) {
-          double2 c = shfl2(contrib, e);
-          if (lane == 0) res[e] = cadd(res[e], c);
+          const double tx = __shfl_sync(0xffffffffu, acc, 2 * e), ty = __shfl_sync(0xffffffffu, acc, 2 * e + 1);
+          T[e] = cadd(T[e], cmk(tx, ty));
         }
-      }
-    }
-  }
-  if (lf > 0 && !landau_done) {
-    const double2 p = cmk(g.pr, g.pi);
-    const double pd = S.dppar_abs, dpp = S.dpperp;
-    const double vA = a.sys.vA;
-    if (S.fit_aux) {
-      // Maxwellian terms: f = sum_f a0 exp(-p2 (p - p3)^2)
-      const int nf = S.nf;
-      for (int i = lane; i <= N; i += 32) {
-        double2 f0 = cmk(0, 0), fp = cmk(0, 0), fm = cmk(0, 0);
-        for (int f = 0; f < nf; ++f) {
-          const double* aux = S.fit_aux + ((size_t)i * nf + f) * 4;  // a0, p2, p3, exp(-p2 D^2)
-          double p2 = aux[1];
-          double2 d = cmk(p.x - aux[2], p.y);
-          double2 E0 = cexp_d(cscale(cmul(d, d), -p2));
-          double2 G = cscale(E0, aux[0]);
-          double2 ax = cscale(d, -2.0 * p2 * pd);
-          double2 X, Xi;
-          if (fabs(ax.x) < 600.0) {
-            X = cexp_d(ax);
-            Xi = crcp(X);
-            double2 Gc = cscale(G, aux[3]);
-            fp = cadd(fp, cmul(Gc, X));
-            fm = cadd(fm, cmul(Gc, Xi));
-          } else {
-            double2 dp = cadd(d, cmk(pd, 0.0)), dm = csub(d, cmk(pd, 0.0));
-            fp = cadd(fp, cscale(cexp_d(cscale(cmul(dp, dp), -p2)), aux[0]));
-            fm = cadd(fm, cscale(cexp_d(cscale(cmul(dm, dm), -p2)), aux[0]));
+      } else if (!merged) {
+        // per-lane piece sums flushed as the piece changes, then a warp sum
+        struct Acc {
+          int jc;
+          double2 A, B;
+        };
+        auto flush = [&](Acc& q, double sign) {
+          if (q.jc < 0) return;
+          double2 h[6], sl[6];
+          node(q.jc, h, sl);
+  #pragma unroll
+          for (int e = 0; e < 6; ++e) {
+            double2 t = cadd(cmul(h[e], q.A), cmul(sl[e], q.B));
+            T[e] = cmk(fma(sign, t.x, T[e].x), fma(sign, t.y, T[e].y));
           }
-          f0 = cadd(f0, G);
+          q.A = q.B = cmk(0.0, 0.0);
+        };
+        auto add = [&](Acc& q, int jc, double p, double2 c, double sign) {
+          if (jc != q.jc) {
+            flush(q, sign);
+            q.jc = jc;
+          }
+          double dx = p - S.ppar[jc];
+          q.A = cadd(q.A, c);
+          q.B = cmk(fma(c.x, dx, q.B.x), fma(c.y, dx, q.B.y));
+        };
+        if (sym) {
+          const int per = (NP + 31) / 32;
+          const int k0 = lane * per, k1 = min(NP, k0 + per);
+          Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
+          int ju = -1, jd = -1;
+          for (int k = k0; k < k1; ++k) {
+            double p;
+            double2 K;
+            sym_point(k, p, K);
+            const double pm = 2.0 * pr - p;
+            ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
+            jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
+            add(up, clampj(ju), p, K, 1.0);
+            add(dn, clampj(jd), pm, cmk(K.x, -K.y), -1.0);
+          }
+          flush(up, 1.0);
+          flush(dn, -1.0);
         }
-        frow[i] = f0;
-        fpr[i] = fp;
-        fmr[i] = fm;
+        if (ntiny > 0) {
+          const int per = (ntiny + 1 + 31) / 32;
+          const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
+          Acc q{-1, cmk(0, 0), cmk(0, 0)};
+          int jt = -1;
+          for (int k = k0; k < k1; ++k) {
+            double p;
+            double2 K;
+            tiny_point(k, p, K);
+            jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
+            add(q, clampj(jt), p, K, 1.0);
+          }
+          flush(q, 1.0);
+        }
+        for (int e = 0; e < 6; ++e)
+          for (int off = 16; off > 0; off >>= 1) {
+            T[e].x += __shfl_xor_sync(0xffffffffu, T[e].x, off);
+            T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
+          }
       }
-    } else {
-      for (int i = lane; i <= N; i += 32) {
-        frow[i] = eval_fit_d(S, vA, i, p);
-        fpr[i] = eval_fit_d(S, vA, i, cadd(p, cmk(pd, 0.0)));
-        fmr[i] = eval_fit_d(S, vA, i, csub(p, cmk(pd, 0.0)));
-      }
+      // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
+      double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
+      // lane 0 holds the whole T; lanes 0-5 add entry e
+      if (lane == 0)
+        for (int e = 0; e < 6; ++e) tb[e] = T[e];
+      __syncwarp();
+      if (lane < 6 && !(n == 0 && (lane == 0 || lane == 3 || lane == 4)))
+        out[lane] = cadd(out[lane], cscale(cmul(it.pref[lane], tb[lane]), scale));
+      __syncwarp();
     }
-    __syncwarp();
-    bool zero = false;
-    double2 sums[3] = {cmk(0, 0), cmk(0, 0), cmk(0, 0)};
-    const double ql = S.qs / fabs(kpar);
-    const int L = N + 1;
-    for (int i = lane; i <= N; i += 32) {
-      double2 fpi = fpr[i], fpf = fmr[i];
-      double2 dfperp, dfpar;
-      double h;
-      if (i == 0) {
-        dfperp = cscale(csub(frow[1], frow[0]), 1.0 / dpp);
-        h = 0.5;
-      } else if (i == N) {
-        dfperp = cscale(csub(frow[N], frow[N - 1]), 1.0 / dpp);
-        h = 0.5;
+
+    if (wk & 2) {
+      const double2 p = cmk(it.pr, it.pim);
+      const double pd = S.dppar_abs, dpp = S.dpperp;
+      const double vA = a.sys.vA;
+      if (S.fit_aux) {
+        // Maxwellian terms: f = sum_f a0 exp(-p2 (p - p3)^2)
+        const int nf = S.nf;
+        for (int i = lane; i <= N; i += 32) {
+          double2 f0 = cmk(0, 0), fp = cmk(0, 0), fm = cmk(0, 0);
+          for (int f = 0; f < nf; ++f) {
+            const double* aux = S.fit_aux + ((size_t)i * nf + f) * 4;  // a0, p2, p3, exp(-p2 D^2)
+            double p2 = aux[1];
+            double2 d = cmk(p.x - aux[2], p.y);
+            double2 E0 = cexp_d(cscale(cmul(d, d), -p2));
+            double2 G = cscale(E0, aux[0]);
+            double2 ax = cscale(d, -2.0 * p2 * pd);
+            double2 X, Xi;
+            if (fabs(ax.x) < 600.0) {
+              X = cexp_d(ax);
+              Xi = crcp(X);
+              double2 Gc = cscale(G, aux[3]);
+              fp = cadd(fp, cmul(Gc, X));
+              fm = cadd(fm, cmul(Gc, Xi));
+            } else {
+              double2 dp = cadd(d, cmk(pd, 0.0)), dm = csub(d, cmk(pd, 0.0));
+              fp = cadd(fp, cscale(cexp_d(cscale(cmul(dp, dp), -p2)), aux[0]));
+              fm = cadd(fm, cscale(cexp_d(cscale(cmul(dm, dm), -p2)), aux[0]));
+            }
+            f0 = cadd(f0, G);
+          }
+          frow[i] = f0;
+          fpr[i] = fp;
+          fmr[i] = fm;
+        }
       } else {
-        if (cabs_(fpi) == 0.0 || cabs_(fpf) == 0.0 || cabs_(frow[i + 1]) == 0.0) zero = true;
-        dfperp = cscale(csub(frow[i + 1], frow[i - 1]), 1.0 / (2.0 * dpp));
-        h = (i == N - 1) ? 0.5 : 1.0;
+        for (int i = lane; i <= N; i += 32) {
+          frow[i] = eval_fit_d(S, vA, i, p);
+          fpr[i] = eval_fit_d(S, vA, i, cadd(p, cmk(pd, 0.0)));
+          fmr[i] = eval_fit_d(S, vA, i, csub(p, cmk(pd, 0.0)));
+        }
       }
-      dfpar = cscale(csub(fpi, fpf), 1.0 / (2.0 * pd));
-      double pp_i = S.pperp[i];
-      // (q/|kpar|) ((pperp dfpar - p dfperp) kpar/m + omega dfperp)
-      double2 Lv = cscale(cadd(cscale(csub(cscale(dfpar, pp_i), cmul(p, dfperp)), kpar / S.ms), cmul(o, dfperp)),
-                          ql);
-      double J = S.bessel[(size_t)(n + 1) * L + i];
-      double Jp = (n == 0) ? -S.bessel[(size_t)2 * L + i]
-                           : 0.5 * (S.bessel[(size_t)n * L + i] - S.bessel[(size_t)(n + 2) * L + i]);
-      sums[0] = cadd(sums[0], cscale(Lv, h * (J * J)));
-      sums[1] = cadd(sums[1], cscale(Lv, h * ((pp_i * pp_i) * Jp * Jp)));
-      sums[2] = cadd(sums[2], cscale(Lv, h * (pp_i * J * Jp)));
-    }
-    zero = __any_sync(0xffffffffu, zero);
-    for (int F = 0; F < 3; ++F)
-      for (int off = 16; off > 0; off >>= 1) {
-        sums[F].x += __shfl_xor_sync(0xffffffffu, sums[F].x, off);
-        sums[F].y += __shfl_xor_sync(0xffffffffu, sums[F].y, off);
+      __syncwarp();
+      bool zero = false;
+      double2 sums[3] = {cmk(0, 0), cmk(0, 0), cmk(0, 0)};
+      const double ql = S.qs / fabs(kpar);
+      const int L = N + 1;
+      for (int i = lane; i <= N; i += 32) {
+        double2 fpi = fpr[i], fpf = fmr[i];
+        double2 dfperp, dfpar;
+        double h;
+        if (i == 0) {
+          dfperp = cscale(csub(frow[1], frow[0]), 1.0 / dpp);
+          h = 0.5;
+        } else if (i == N) {
+          dfperp = cscale(csub(frow[N], frow[N - 1]), 1.0 / dpp);
+          h = 0.5;
+        } else {
+          if (cabs_(fpi) == 0.0 || cabs_(fpf) == 0.0 || cabs_(frow[i + 1]) == 0.0) zero = true;
+          dfperp = cscale(csub(frow[i + 1], frow[i - 1]), 1.0 / (2.0 * dpp));
+          h = (i == N - 1) ? 0.5 : 1.0;
+        }
+        dfpar = cscale(csub(fpi, fpf), 1.0 / (2.0 * pd));
+        double pp_i = S.pperp[i];
+        // (q/|kpar|) ((pperp dfpar - p dfperp) kpar/m + omega dfperp)
+        double2 Lv = cscale(cadd(cscale(csub(cscale(dfpar, pp_i), cmul(p, dfperp)), kpar / S.ms), cmul(o, dfperp)),
+                            ql);
+        double J = S.bessel[(size_t)(n + 1) * L + i];
+        double Jp = (n == 0) ? -S.bessel[(size_t)2 * L + i]
+                             : 0.5 * (S.bessel[(size_t)n * L + i] - S.bessel[(size_t)(n + 2) * L + i]);
+        sums[0] = cadd(sums[0], cscale(Lv, h * (J * J)));
+        sums[1] = cadd(sums[1], cscale(Lv, h * ((pp_i * pp_i) * Jp * Jp)));
+        sums[2] = cadd(sums[2], cscale(Lv, h * (pp_i * J * Jp)));
       }
-    if (!zero) {
-      // landau_e = -pref_e c_e(p) Sigma_F(e) * i dpperp 2 pi^2
-      double2 c1 = cmk(1.0, 0.0), cp = p, cp2 = cmul(p, p);
-      double2 cfac[6] = {c1, c1, cp2, c1, cp, cp};
-      int fam[6] = {0, 1, 0, 2, 0, 2};
-      double2 ifac = cmk(0.0, -dpp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
-      for (int e = 0; e < 6; ++e) {
-        double2 land = cmul(cmul(pref[e], cfac[e]), sums[fam[e]]);
-        res[e] = cadd(res[e], cmul(land, ifac));
+      zero = __any_sync(0xffffffffu, zero);
+      for (int F = 0; F < 3; ++F)
+        for (int off = 16; off > 0; off >>= 1) {
+          sums[F].x += __shfl_xor_sync(0xffffffffu, sums[F].x, off);
+          sums[F].y += __shfl_xor_sync(0xffffffffu, sums[F].y, off);
+        }
+      if (!zero) {
+        // landau_e = -pref_e c_e(p) Sigma_F(e) * i dpperp 2 pi^2, lanes 0-5
+        if (lane == 0)
+          for (int F = 0; F < 3; ++F) tb[F] = sums[F];
+        __syncwarp();
+        if (lane < 6 && !(n == 0 && (lane == 0 || lane == 3 || lane == 4))) {
+          const int e = lane;
+          const double2 ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
+          const int fam = (e == 1) ? 1 : ((e == 3 || e == 5) ? 2 : 0);
+          const double2 ifac = cmk(0.0, -dpp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+          const double2 land = cmul(cmul(it.pref[e], ce), tb[fam]);
+          out[e] = cadd(out[e], cmul(land, ifac));
+        }
+        __syncwarp();
       }
     }
-  }
-  if (lane == 0) {
-    double2* out = items + (((size_t)w * S_ + s) * a.rcap + r) * 6;
-    for (int e = 0; e < 6; ++e) {
-      bool skip = (n == 0 && (e == 0 || e == 3 || e == 4));
-      out[e] = skip ? cmk(0.0, 0.0) : res[e];
-    }
+    __syncwarp();  // the next item reuses the window and the records
   }
 }
 
@@ -1264,7 +1313,8 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     c->res_smem_set = (int)smem;
   }
   long total = (long)nslots;
-  long blocks = (total + RES_WARPS - 1) / RES_WARPS;
+  a.ipw = res_items_per_warp(total);
+  long blocks = (total + RES_WARPS * a.ipw - 1) / (RES_WARPS * a.ipw);
   k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_items,
                                                              c->d_flags);
   ALPS_CUDA_TRY(cudaGetLastError());
@@ -1398,7 +1448,8 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp, res_win(c->sys.positions_principal)) * sizeof(double2);
   if (smem > 48 * 1024)
     ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  long blocks = ((long)nslots + RES_WARPS - 1) / RES_WARPS;
+  a.ipw = res_items_per_warp((long)nslots);
+  long blocks = ((long)nslots + RES_WARPS * a.ipw - 1) / (RES_WARPS * a.ipw);
   k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, om, n, count, slots, items, flags);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (a.relcap) {
