@@ -131,6 +131,7 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_G);
     cudaFree(S.d_X);
     cudaFree(S.d_mom);
+    cudaFree(S.d_momf);
     cudaFree(S.d_fit_aux);
     cudaFree(S.d_lmom);
     cudaFree(S.d_grel);

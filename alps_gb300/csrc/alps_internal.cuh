@@ -75,6 +75,7 @@ struct SpecDev {
   const double* bessel;
   const double* V;
   const double* mom;  // Laurent moments [(nmax+1)][ALPS_KFAR][12]
+  const float* momf;  // the same moments rounded to FP32 (for the series tails)
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
   int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)
@@ -134,6 +135,8 @@ struct SpeciesHost {
   double* d_G = nullptr;                  // contraction RHS [2][N-1][M-1]
   double* d_X = nullptr;                  // x_j^k, x_j = (ppar_j - pcen)/prad
   double* d_mom = nullptr;                // Laurent moments
+  float* d_momf = nullptr;                // the same in FP32
+  size_t momf_cap = 0;
   double* d_fit_aux = nullptr;            // Maxwellian continuation factors
   double* d_lmom = nullptr;               // factorised Landau moments
   size_t lmom_cap = 0;

@@ -120,13 +120,18 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
 #pragma unroll
         for (int q = 0; q < 12; ++q) Sx[q] = cmk(0.0, 0.0);
         // Laurent series for a pole far outside the grid: truncation
-        // rho^K <= 2^-53 (1 - rho), rho = prad/|p_res - pcen|
-        int K = S.kfar + 1;
+        // rho^K <= 2^-53 (1 - rho), rho = prad/|p_res - pcen|.  With
+        // |mom_k| <= sum_j |V_j|, the terms from K32 on (rho^K32 <= 2^-33
+        // (1 - rho)) add at most 2^-33 of that bound, so they are summed in
+        // FP32: their rounding stays below 2^-53 of it.
+        int K = S.kfar + 1, K32 = K;
         double2 d = cmk(g.pr - S.pcen, g.pi);
         double dd = d.x * d.x + d.y * d.y;
         if (!g.res && S.prad * S.prad < 0.5 * dd) {
-          double rho = S.prad * rsqrt(dd);
-          K = (int)ceil((36.7368005696771 - log1p(-rho)) / -log(rho));
+          const double rho = S.prad * rsqrt(dd);
+          const double lr = -log(rho), l1 = log1p(-rho);
+          K = (int)ceil((36.7368005696771 - l1) / lr);    // 53 ln 2
+          K32 = (int)ceil((22.8738569584782 - l1) / lr);  // 33 ln 2
         }
         if (K <= S.kfar) {
           const double* __restrict__ mom = S.mom + (size_t)n * ALPS_KFAR * 12;
@@ -136,7 +141,8 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
           double2 tk = cmk(1.0, 0.0), step = t;
           for (int q = 0; q < js; ++q) tk = cmul(tk, t);
           for (int q = 1; q < js_count; ++q) step = cmul(step, t);
-          for (int k = js; k < K; k += js_count) {
+          int k = js;
+          for (; k < K32; k += js_count) {
             const double2* m2 = reinterpret_cast<const double2*>(mom + (size_t)k * 12);
 #pragma unroll
             for (int q = 0; q < 6; ++q) {
@@ -147,6 +153,35 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
               Sx[2 * q + 1].y = fma(m.y, tk.y, Sx[2 * q + 1].y);
             }
             tk = cmul(tk, step);
+          }
+          if (k < K) {
+            const float* __restrict__ momf = S.momf + (size_t)n * ALPS_KFAR * 12;
+            float2 tf = make_float2((float)tk.x, (float)tk.y);
+            const float2 sf = make_float2((float)step.x, (float)step.y);
+            float2 Sf[12];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) Sf[q] = make_float2(0.0f, 0.0f);
+            for (; k < K; k += js_count) {
+              const float4* m4 = reinterpret_cast<const float4*>(momf + (size_t)k * 12);
+#pragma unroll
+              for (int q = 0; q < 3; ++q) {
+                const float4 m = __ldg(m4 + q);
+                Sf[4 * q].x = fmaf(m.x, tf.x, Sf[4 * q].x);
+                Sf[4 * q].y = fmaf(m.x, tf.y, Sf[4 * q].y);
+                Sf[4 * q + 1].x = fmaf(m.y, tf.x, Sf[4 * q + 1].x);
+                Sf[4 * q + 1].y = fmaf(m.y, tf.y, Sf[4 * q + 1].y);
+                Sf[4 * q + 2].x = fmaf(m.z, tf.x, Sf[4 * q + 2].x);
+                Sf[4 * q + 2].y = fmaf(m.z, tf.y, Sf[4 * q + 2].y);
+                Sf[4 * q + 3].x = fmaf(m.w, tf.x, Sf[4 * q + 3].x);
+                Sf[4 * q + 3].y = fmaf(m.w, tf.y, Sf[4 * q + 3].y);
+              }
+              tf = make_float2(tf.x * sf.x - tf.y * sf.y, tf.x * sf.y + tf.y * sf.x);
+            }
+#pragma unroll
+            for (int q = 0; q < 12; ++q) {
+              Sx[q].x += (double)Sf[q].x;
+              Sx[q].y += (double)Sf[q].y;
+            }
           }
           // S = (1/(k_par d)) sum_k mom_k t^k
           double2 f = cscale(inv, 1.0 / kpar);
@@ -553,6 +588,21 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         return jr;
       };
       auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
+      // the same search from u, an FP32 estimate of p in node units (node j
+      // at u = j).  Away from the half-way points between nodes by more than
+      // 1e-3 of a spacing, the nearest node is the search's answer: u's
+      // rounding is below 1e-4 of a spacing, and alps_set_species admits
+      // only grids whose steps agree to 1e-9, so a node is within 1e-6 of a
+      // spacing of its uniform position.  Nearer the half-way points the
+      // FP64 search decides.
+      auto piece_f = [&](float u, double p) {
+        const float rn = rintf(u);
+        if (fabsf(u - rn) < 0.499f) {
+          const int j = (int)rn;
+          return (j >= 1 && j <= M - 1) ? j : 0;
+        }
+        return piece_raw(p);
+      };
       auto piece = [&](double p) { return clampj(piece_raw(p)); };
       // the same index for p increasing (up) or decreasing (down) from a known
       // raw index: |pp(j) - p| is monotone in p, so the last valid node moves
@@ -692,15 +742,14 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         const int per = (NP + 31) / 32;
         const int k0 = lane * per, k1 = min(NP, k0 + per);
         PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
-        int ju = -1, jd = -1;
+        const float u0 = (float)(1.0 + (pr - S.ppar[1]) / dps), du = (float)(smdelta / dps);
         for (int k = k0; k < k1; ++k) {
           double p;
           double2 K;
           sym_point(k, p, K);
           const double pm = 2.0 * pr - p;
-          ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
-          jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
-          const int cu = clampj(ju), cd = clampj(jd);
+          const int cu = clampj(piece_f(fmaf((float)k, du, u0), p));
+          const int cd = clampj(piece_f(fmaf(-(float)k, du, u0), pm));
           put(su, cu, p - S.ppar[cu], K, 1);
           put(sd, cd, pm - S.ppar[cd], cmk(K.x, -K.y), -1);
         }
@@ -732,13 +781,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         const int per = (ntiny + 1 + 31) / 32;
         const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
         PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
-        int jt = -1;
+        const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) / dps), dut = (float)(corr * smdelta / dps);
         for (int k = k0; k < k1; ++k) {
           double p;
           double2 K;
           tiny_point(k, p, K);
-          jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
-          const int ct = clampj(jt);
+          const int ct = clampj(piece_f(fmaf((float)k, dut, ut0), p));
           put(sq, ct, p - S.ppar[ct], K, 1);
         }
         records(2, sq, 1);
@@ -1165,6 +1213,7 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->bessel = S.d_bessel;
   o->V = S.d_V;
   o->mom = S.d_mom;
+  o->momf = S.d_momf;
   o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
   o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
   // the series is used only where it is cheaper than the node sum

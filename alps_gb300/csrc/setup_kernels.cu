@@ -520,7 +520,7 @@ __global__ void k_powers(const double* __restrict__ ppar, int M, double pcen, do
 // For a pole p far from the grid, sum_j f_j V_j / (p - ppar_j) =
 //   (1/d) sum_k mom_k (prad/d)^k,  d = p - pcen.
 __global__ void k_moments(const double* __restrict__ V, const double* __restrict__ X, int M, int nmax,
-                          double* mom) {
+                          double* mom, float* momf) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int total = (nmax + 1) * ALPS_KFAR * 12;
   if (t >= total) return;
@@ -532,6 +532,7 @@ __global__ void k_moments(const double* __restrict__ V, const double* __restrict
     acc = fma(f * v[(size_t)(j - 1) * 12], X[(size_t)(j - 1) * ALPS_KFAR + k], acc);
   }
   mom[t] = acc;
+  momf[t] = (float)acc;
 }
 
 // omega-independent factors of Maxwellian continuation terms, per row and
@@ -869,10 +870,11 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   double pcen = 0.5 * (S.ppar[1] + S.ppar[M - 1]), prad = 0.5 * (S.ppar[M - 1] - S.ppar[1]);
   if (!S.d_X) ALPS_CUDA_TRY(cudaMalloc(&S.d_X, (size_t)(M - 1) * ALPS_KFAR * sizeof(double)));
   if ((rc = ensure(S.d_mom, S.mom_cap, (size_t)(nmax + 1) * ALPS_KFAR * 12))) return rc;
+  if ((rc = ensure(S.d_momf, S.momf_cap, (size_t)(nmax + 1) * ALPS_KFAR * 12))) return rc;
   k_powers<<<(M - 1 + 127) / 128, 128, 0, st>>>(S.d_ppar, M, pcen, prad, S.d_X);
   ALPS_CUDA_TRY(cudaGetLastError());
   int tot = (nmax + 1) * ALPS_KFAR * 12;
-  k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_mom);
+  k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_mom, S.d_momf);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }
