@@ -64,6 +64,8 @@ struct SpecDev {
   double dpperp;      // pp(2,2,1) - pp(1,2,1)
   double dppar;       // pp(2,2,2) - pp(2,1,2)  (signed; positive grids)
   double dppar_abs;   // abs of the above
+  double idppar, hidpa;  // 1/dppar, 0.5/|dppar|
+  double qk;          // qs / kpar at the current k
   int species_index;  // 1-based index (distribution_analyt selects on it)
   double int_ee;      // ee term (omega and k independent)
   const double* pperp;

@@ -564,7 +564,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         __syncwarp();
         for (int t = lane; t < nw * 6; t += 32) {
           int jj = t / 6, e = t % 6;
-          if (jj >= 1 && jj + 1 < nw) ws[jj * 6 + e] = cscale(csub(wh[(jj + 1) * 6 + e], wh[(jj - 1) * 6 + e]), 0.5 / dpa);
+          if (jj >= 1 && jj + 1 < nw) ws[jj * 6 + e] = cscale(csub(wh[(jj + 1) * 6 + e], wh[(jj - 1) * 6 + e]), S.hidpa);
         }
       }
       __syncwarp();
@@ -573,7 +573,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
       // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
       // interpolant serves p is "the last ipar in 1..npar-1 with
       // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
-      const double idpa = 1.0 / dpa, half = 0.5 * dpa;
+      const double idpa = fabs(S.idppar), half = 0.5 * dpa;
       // last node in 1..M-1 within half a spacing of p, or 0 (the search of
       // funct_g before its clamp); the candidates bracket the nearest node
       auto piece_raw = [&](double p) {
@@ -595,13 +595,10 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
       // only grids whose steps agree to 1e-9, so a node is within 1e-6 of a
       // spacing of its uniform position.  Nearer the half-way points the
       // FP64 search decides.
-      auto piece_f = [&](float u, double p) {
-        const float rn = rintf(u);
-        if (fabsf(u - rn) < 0.499f) {
-          const int j = (int)rn;
-          return (j >= 1 && j <= M - 1) ? j : 0;
-        }
-        return piece_raw(p);
+      auto off_half = [&](float u) { return fabsf(u - rintf(u)) < 0.499f; };
+      auto node_of = [&](float u) {
+        const int j = (int)rintf(u);
+        return (j >= 1 && j <= M - 1) ? j : 0;
       };
       auto piece = [&](double p) { return clampj(piece_raw(p)); };
       // the same index for p increasing (up) or decreasing (down) from a known
@@ -624,7 +621,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
           sl = ws[(jc - jw0) * 6 + e];
         } else {
           h = h_node(Vn, jc, e, o, kappa);
-          sl = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), 0.5 / dpa);
+          sl = cscale(csub(h_node(Vn, jc + 1, e, o, kappa), h_node(Vn, jc - 1, e, o, kappa)), S.hidpa);
         }
       };
       auto node = [&](int jc, double2* h, double2* sl) {
@@ -651,25 +648,26 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
       // coordinates are rounded as integrate_res writes them, without fused
       // multiply-adds: a point can sit exactly on a piece boundary
       // pp(j) + dppar/2, and its piece must be the reference's.
-      auto sym_point = [&](int k, double& p, double2& K) {
+      auto sym_point = [&](int k, double& p, double& dx, double2& K) {
         p = (k == 0) ? pr
                      : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
         double wk = (k == 0 || k == a.sys.M_P) ? 1.0 : 2.0;
-        double dx = p - pr;
+        dx = p - pr;
         double rr = wk * rcp_fast(fma(dx, dx, pim * pim));
         K = cmk(dx * rr, pim * rr);
       };
-      auto tiny_point = [&](int k, double& p, double2& K) {
+      auto tiny_point = [&](int k, double& p, double& dx, double2& K) {
         p = (k == 0) ? __dadd_rn(pr, capDelta)
                      : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
         double wk = (k == 0 || k == ntiny) ? 1.0 : 2.0;
-        double dx = p - pr;
+        dx = p - pr;
         double rr = wk * corr * rcp_fast(fma(dx, dx, pim * pim));
         K = cmk(dx * rr, pim * rr);
       };
 
       // Sum_k c_k H(p_k) with H linear on each piece jc needs, per piece, only
-      // A = Sum c_k and B = Sum c_k (p_k - pp(jc)); the piece adds h A + s B.
+      // A = Sum c_k and B = Sum c_k (p_k - pp(jc)) = C + (p_res - pp(jc)) A,
+      // C = Sum c_k (p_k - p_res); the piece adds h A + s B.
       // Each lane walks a run of consecutive k and keeps the sums of at most
       // two pieces (pieces are M_P/(M_I+1) or more points wide, far wider
       // than a lane's run); the lanes' piece sums are merged per piece in
@@ -678,7 +676,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
       // are not monotone in k, send the item to the per-lane flush below.
       struct PvSlot {
         int jd, jc;          // finished piece (-1: none), current piece
-        double2 Ad, Bd, Ac, Bc;
+        double2 Ad, Bd, Ac, Bc;  // A and C of each
       };
       bool bad = false;
       auto put = [&](PvSlot& q, int j, double dx, double2 c, int dir) {
@@ -742,16 +740,16 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         const int per = (NP + 31) / 32;
         const int k0 = lane * per, k1 = min(NP, k0 + per);
         PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
-        const float u0 = (float)(1.0 + (pr - S.ppar[1]) / dps), du = (float)(smdelta / dps);
+        const float u0 = (float)(1.0 + (pr - S.ppar[1]) * S.idppar), du = (float)(smdelta * S.idppar);
         for (int k = k0; k < k1; ++k) {
-          double p;
+          double p, dx;
           double2 K;
-          sym_point(k, p, K);
-          const double pm = 2.0 * pr - p;
-          const int cu = clampj(piece_f(fmaf((float)k, du, u0), p));
-          const int cd = clampj(piece_f(fmaf(-(float)k, du, u0), pm));
-          put(su, cu, p - S.ppar[cu], K, 1);
-          put(sd, cd, pm - S.ppar[cd], cmk(K.x, -K.y), -1);
+          sym_point(k, p, dx, K);
+          const float uu = fmaf((float)k, du, u0), ud = fmaf(-(float)k, du, u0);
+          const int cu = clampj(off_half(uu) ? node_of(uu) : piece_raw(p));
+          const int cd = clampj(off_half(ud) ? node_of(ud) : piece_raw(2.0 * pr - p));
+          put(su, cu, dx, K, 1);
+          put(sd, cd, -dx, cmk(K.x, -K.y), -1);
         }
         records(0, su, 1);
         records(1, sd, -1);
@@ -781,13 +779,14 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         const int per = (ntiny + 1 + 31) / 32;
         const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
         PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
-        const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) / dps), dut = (float)(corr * smdelta / dps);
+        const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) * S.idppar), dut = (float)(corr * smdelta * S.idppar);
         for (int k = k0; k < k1; ++k) {
-          double p;
+          double p, dx;
           double2 K;
-          tiny_point(k, p, K);
-          const int ct = clampj(piece_f(fmaf((float)k, dut, ut0), p));
-          put(sq, ct, p - S.ppar[ct], K, 1);
+          tiny_point(k, p, dx, K);
+          const float ut = fmaf((float)k, dut, ut0);
+          const int ct = clampj(off_half(ut) ? node_of(ut) : piece_raw(p));
+          put(sq, ct, dx, K, 1);
         }
         records(2, sq, 1);
       }
@@ -822,9 +821,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
         double2* contrib = recv;
         for (int q = lane; q < nruns * 6; q += 32) {
           const int rho = q / 6, e = q % 6;
+          const int jc = runJ[rho];
           double2 h, sl;
-          node1(runJ[rho], e, h, sl);
-          double2 t = cadd(cmul(h, runv[rho * 2]), cmul(sl, runv[rho * 2 + 1]));
+          node1(jc, e, h, sl);
+          const double2 A = runv[rho * 2];
+          const double2 B = cadd(runv[rho * 2 + 1], cscale(A, pr - S.ppar[jc]));
+          double2 t = cadd(cmul(h, A), cmul(sl, B));
           contrib[q] = (runG[rho] == 1) ? cmk(-t.x, -t.y) : t;
         }
         __syncwarp();
@@ -871,9 +873,9 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
           Acc up{-1, cmk(0, 0), cmk(0, 0)}, dn{-1, cmk(0, 0), cmk(0, 0)};
           int ju = -1, jd = -1;
           for (int k = k0; k < k1; ++k) {
-            double p;
+            double p, dx;
             double2 K;
-            sym_point(k, p, K);
+            sym_point(k, p, dx, K);
             const double pm = 2.0 * pr - p;
             ju = (ju < 0) ? piece_raw(p) : piece_up(ju, p);
             jd = (jd < 0) ? piece_raw(pm) : piece_down(jd, pm);
@@ -889,9 +891,9 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
           Acc q{-1, cmk(0, 0), cmk(0, 0)};
           int jt = -1;
           for (int k = k0; k < k1; ++k) {
-            double p;
+            double p, dx;
             double2 K;
-            tiny_point(k, p, K);
+            tiny_point(k, p, dx, K);
             jt = (jt < 0) ? piece_raw(p) : piece_up(jt, p);
             add(q, clampj(jt), p, K, 1.0);
           }
@@ -904,7 +906,7 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
           }
       }
       // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
-      double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-(S.qs / kpar) * 0.5);
+      double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-S.qk * 0.5);
       // lane 0 holds the whole T; lanes 0-5 add entry e
       if (lane == 0)
         for (int e = 0; e < 6; ++e) tb[e] = T[e];
@@ -1202,6 +1204,9 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->dpperp = bm ? 0.0 : S.pperp[2] - S.pperp[1];
   o->dppar = bm ? 0.0 : S.ppar[2] - S.ppar[1];
   o->dppar_abs = std::fabs(o->dppar);
+  o->idppar = bm ? 0.0 : 1.0 / o->dppar;
+  o->hidpa = bm ? 0.0 : 0.5 / o->dppar_abs;
+  o->qk = S.sp.qs / c->kpar;
   o->species_index = is + 1;
   o->int_ee = S.int_ee;
   o->pperp = S.d_pperp;
