@@ -157,6 +157,9 @@ void alps_destroy(alps_ctx* c) {
   if (c->h_pinned) cudaFreeHost(c->h_pinned);
   if (c->h_flag) cudaFreeHost(c->h_flag);
   if (c->ev_done) cudaEventDestroy(c->ev_done);
+  if (c->d_args) cudaFree(c->d_args);
+  if (c->d_job) cudaFree(c->d_job);
+  if (c->h_args) cudaFreeHost(c->h_args);
   for (auto& kv : c->graphs) cudaGraphExecDestroy(kv.second.second);
   for (auto& ev : c->ev_pending)
     for (auto e : ev) cudaEventDestroy(e);

@@ -207,8 +207,13 @@ struct alps_ctx {
   uint64_t gen = 1;
   std::map<int, std::pair<uint64_t, cudaGraphExec_t>> graphs;
   std::map<int, uint64_t> graph_seen;  // gen of the last uncaptured batch of each size
-  int res_smem_set = 0;                 // dynamic shared memory opt-in of k_resonant done
-  int chunk_group = 1;                  // order chunks per pole-sum block (results unchanged)
+  // device copy of the kernel arguments for fused batches, valid while
+  // args_gen == gen
+  void* d_args = nullptr;
+  void* d_job = nullptr;  // the job table of a lone batch
+  void* h_args = nullptr;
+  uint64_t args_gen = 0;
+  int args_maxn = 0, args_rcap = 0;
 };
 
 // ---------------------------------------------------------------------------
@@ -240,6 +245,16 @@ int launch_rel_orders(const SysDev& sys, const SpecDev* sp, int relcap, int n, c
                       int* d_flags, cudaStream_t st);
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
                       cudaStream_t st);
+// Fused batches: nj contexts, context j with n[j] frequencies at
+// d_om[o_j ...] (o_j = n[0] + ... + n[j-1]), det D to d_D at the same
+// offsets and the error flags of context j to d_flags[j].  Every context is
+// evaluated with the launch shape, and so the sums, of a lone batch of its
+// size.  Contexts with relativistic or closed-form species are not fusable.
+struct MultiScratch;
+int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
+                      MultiScratch** scratch, cudaStream_t st);
+void multi_scratch_free(MultiScratch* m);
+bool ctx_fusable(const alps_ctx* c);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);
 int collect_profile(alps_ctx* c);
 void fill_sys_dev(const alps_ctx* c, SysDev* out);

@@ -178,13 +178,13 @@ __device__ inline ResGeom res_geometry(const SpecDev& S, int M_I, double2 om, in
   }
   int ipar_res = 0;
   if ((x >= pp[1]) && (x < pp[M - 1])) {
-    int lo = 1, hi = M - 2;  // largest i in [1, M-2] with pp[i] <= x
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (pp[mid] <= x) lo = mid;
-      else hi = mid - 1;
-    }
-    ipar_res = lo;
+    // largest i in [1, M-2] with pp[i] <= x: the uniform grid gives the
+    // index to within one, and the comparisons settle it
+    int i = 1 + (int)floor((x - pp[1]) * S.idppar);
+    i = (i < 1) ? 1 : ((i > M - 2) ? M - 2 : i);
+    while (i < M - 2 && pp[i + 1] <= x) ++i;
+    while (i > 1 && pp[i] > x) --i;
+    ipar_res = i;
   }
   for (int ip = 0; ip <= M_I; ++ip) {
     if ((x >= __dsub_rn(pp[0], __dmul_rn(dpp, (double)ip))) &&

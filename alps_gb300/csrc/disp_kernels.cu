@@ -25,15 +25,21 @@
 #include "alps_internal.cuh"
 #include "device_math.cuh"
 
-struct DispArgs {
+// what the kernels read of one context (the plasma at its current k)
+struct __align__(16) DispArgs {
   SysDev sys;
   SpecDev sp[ALPS_MAX_SPECIES];
-  int nchunk;    // order chunks per species
-  int csize;     // orders per chunk
   int rcap;      // max resonant slots over species
   int relcap;    // order slots per relativistic species (max nmax + 1), 0 if none
   int has_bm;    // some species go through the NHDS closed form
-  int cgroup;    // order chunks per pole-sum block
+};
+
+// the shape of one batch: the order chunks of the pole sums and the items
+// per warp of k_resonant.  It follows from the batch size and the context
+// alone, so a batch sums in the same order wherever it runs.
+struct DispShape {
+  int nchunk;    // order chunks per species
+  int csize;     // orders per chunk
   int ipw;       // resonant items per warp of k_resonant (1..32)
 };
 
@@ -43,10 +49,9 @@ namespace {
 // One warp per (omega, species): the lanes test the orders -nmax..nmax
 // and a ballot prefix gives every resonant order its slot in increasing nn,
 // so the slot order does not depend on the launch shape.
-__global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om, int* count, int* slot_nn,
-                           int* flags) {
+__device__ __forceinline__ void classify_body(const DispArgs& a, const double2* __restrict__ om, int n_om,
+                                              int* count, int* slot_nn, int* flags, long wid) {
   const int lane = threadIdx.x & 31;
-  const long wid = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int S_ = a.sys.nspec;
   if (wid >= (long)n_om * S_) return;
   const int t = (int)(wid / S_), s = (int)(wid % S_);
@@ -82,15 +87,17 @@ __global__ void k_classify(DispArgs a, const double2* __restrict__ om, int n_om,
 // omega over the orders of its chunk (and the n = -1,0,1 parts for chi_low).
 // ---------------------------------------------------------------------------
 template <bool LOW>
-__device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __restrict__ om, int n_om,
-                                           int js_count, double2* part, double2* low, const int chunk) {
-  const int s = blockIdx.y;
+__device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
+                                          int n_om, int js_count, double2* part, double2* low, int tile, int s,
+                                          int chunk) {
   const SpecDev& S = a.sp[s];
-  const int n_begin = chunk * a.csize;
-  const int n_end = (S.relat || S.bm) ? n_begin : min(S.nmax + 1, n_begin + a.csize);
+  const int n_begin = chunk * sh.csize;
+  const int n_end = (S.relat || S.bm) ? n_begin : min(S.nmax + 1, n_begin + sh.csize);
+  // the js_count slices of an omega are adjacent threads, so an omega's
+  // per-order set-up is one warp instruction for all its slices
   const int TW = blockDim.x / js_count;
-  const int wl = threadIdx.x % TW, js = threadIdx.x / TW;
-  const int w = blockIdx.x * TW + wl;
+  const int wl = threadIdx.x / js_count, js = threadIdx.x % js_count;
+  const int w = tile * TW + wl;
   const bool active = (w < n_om);
   const double2 o = active ? om[w] : cmk(0.0, 0.0);
   const int M = S.M;
@@ -139,8 +146,13 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
           double2 inv = cmk(d.x * idd, -d.y * idd);
           double2 t = cscale(inv, S.prad);
           double2 tk = cmk(1.0, 0.0), step = t;
-          for (int q = 0; q < js; ++q) tk = cmul(tk, t);
-          for (int q = 1; q < js_count; ++q) step = cmul(step, t);
+          // tk = t^js, step = t^js_count by squaring (js_count is a power of 2)
+          double2 pw = t;
+          for (int q = js; q; q >>= 1) {
+            if (q & 1) tk = cmul(tk, pw);
+            pw = cmul(pw, pw);
+          }
+          for (int q = js_count; q > 1; q >>= 1) step = cmul(step, step);
           int k = js;
           for (; k < K32; k += js_count) {
             const double2* m2 = reinterpret_cast<const double2*>(mom + (size_t)k * 12);
@@ -248,7 +260,7 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
     __syncthreads();
     if (js == 0)
       for (int q = 1; q < js_count; ++q)
-        for (int e = 0; e < 6; ++e) acc[e] = cadd(acc[e], red[(q * TW + wl) * 6 + e]);
+        for (int e = 0; e < 6; ++e) acc[e] = cadd(acc[e], red[(wl * js_count + q) * 6 + e]);
     if (LOW) {
       for (int l = 0; l < 3; ++l) {
         __syncthreads();
@@ -257,12 +269,12 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
         if (js == 0)
           for (int q = 1; q < js_count; ++q)
             for (int e = 0; e < 6; ++e)
-              lacc[LOW ? l : 0][e] = cadd(lacc[LOW ? l : 0][e], red[(q * TW + wl) * 6 + e]);
+              lacc[LOW ? l : 0][e] = cadd(lacc[LOW ? l : 0][e], red[(wl * js_count + q) * 6 + e]);
       }
     }
   }
   if (js == 0 && active) {
-    size_t base = ((size_t)w * a.sys.nspec + s) * a.nchunk + chunk;
+    size_t base = ((size_t)w * a.sys.nspec + s) * sh.nchunk + chunk;
     for (int e = 0; e < 6; ++e) part[base * 6 + e] = acc[e];
     if (LOW)
       for (int l = 0; l < 3; ++l)
@@ -270,18 +282,7 @@ __device__ __forceinline__ void pole_chunk(const DispArgs& a, const double2* __r
   }
 }
 
-// grid (omega tiles, species, chunk groups): a block sums a.cgroup order
-// chunks one after another, each into its own partial, so the grouping
-// changes the block count but not one rounding
-template <bool LOW>
-__global__ void __launch_bounds__(128) k_pole_sums(DispArgs a, const double2* __restrict__ om, int n_om,
-                                                   int js_count, double2* part, double2* low) {
-  const int c1 = min(a.nchunk, ((int)blockIdx.z + 1) * a.cgroup);
-  for (int chunk = blockIdx.z * a.cgroup; chunk < c1; ++chunk) {
-    pole_chunk<LOW>(a, om, n_om, js_count, part, low, chunk);
-    __syncthreads();
-  }
-}
+
 
 // ---------------------------------------------------------------------------
 // Analytic continuation f(pperp_i, complex ppar) (eval_fit,
@@ -427,10 +428,9 @@ __device__ inline double2 crcp(double2 z) {
   return cmk(z.x * r, -z.y * r);
 }
 
-__global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, const double2* __restrict__ om,
-                                                              int n_om, const int* __restrict__ count,
-                                                              const int* __restrict__ slot_nn, double2* items,
-                                                              int* flags) {
+__device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
+                                              int n_om, const int* __restrict__ count,
+                                              const int* __restrict__ slot_nn, double2* items, long block) {
   extern __shared__ double2 sm[];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int S_ = a.sys.nspec;
@@ -445,12 +445,12 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
   ResItem* ri = reinterpret_cast<ResItem*>(pvv + res_region(N));
   double2* tb = reinterpret_cast<double2*>(ri + 32);      // values handed to lanes 0-5
   const long total = (long)n_om * S_ * a.rcap;
-  const long item0 = ((long)blockIdx.x * RES_WARPS + warp) * a.ipw;
+  const long item0 = (block * RES_WARPS + warp) * sh.ipw;
   const long item = item0 + lane;
 
   // ---- one item per thread: geometry, prefactors, factorised Landau rows ----
   int work = 0;
-  if (lane < a.ipw && item < total) {
+  if (lane < sh.ipw && item < total) {
     const int r = (int)(item % a.rcap);
     const int s = (int)((item / a.rcap) % S_);
     const int w = (int)(item / ((long)a.rcap * S_));
@@ -1018,13 +1018,23 @@ __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant(DispArgs a, cons
 // ---------------------------------------------------------------------------
 // chi, epsilon, wave tensor, det (src/ALPS_fns.f90:500-626)
 // ---------------------------------------------------------------------------
-__global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om, const double2* __restrict__ part,
-                           const double2* __restrict__ low, const int* __restrict__ count,
-                           const int* __restrict__ slot_nn, const double2* __restrict__ items,
-                           const double2* __restrict__ rel, const double2* __restrict__ bmres, double2* D,
-                           double2* ext) {
-  int w = blockIdx.x * blockDim.x + threadIdx.x;
+__device__ __forceinline__ void finalize_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
+                                              int n_om, const double2* __restrict__ part,
+                                              const double2* __restrict__ low, const int* __restrict__ count,
+                                              const int* __restrict__ slot_nn, const double2* __restrict__ items,
+                                              const double2* __restrict__ rel, const double2* __restrict__ bmres,
+                                              double2* D, double2* ext, int w, bool warp_mode) {
   if (w >= n_om) return;
+  // warp_mode: the 32 lanes of a warp share one omega; they split the sums
+  // over order chunks and run the rest redundantly, lane 0 writes
+  const int lane = threadIdx.x & 31, lstep = warp_mode ? 32 : 1, l0 = warp_mode ? lane : 0;
+  auto wsum = [&](double2& v) {
+    if (warp_mode)
+      for (int off = 16; off > 0; off >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
+      }
+  };
   const int S_ = a.sys.nspec;
   const double2 o = om[w];
   double2 eps[6];
@@ -1039,23 +1049,33 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
       chi[e] = cmk(0.0, 0.0);
       for (int l = 0; l < 3; ++l) cl[l][e] = cmk(0.0, 0.0);
     }
-    size_t base = ((size_t)w * S_ + s) * a.nchunk;
-    for (int ch = 0; ch < a.nchunk; ++ch)
+    size_t base = ((size_t)w * S_ + s) * sh.nchunk;
+    // small batches leave one partial per order: unrolled, so that the
+    // loads of several chunks are in flight at once
+#pragma unroll 4
+    for (int ch = l0; ch < sh.nchunk; ch += lstep)
       for (int e = 0; e < 6; ++e) chi[e] = cadd(chi[e], part[(base + ch) * 6 + e]);
     if (ext && low)
-      for (int ch = 0; ch < a.nchunk; ++ch)
+      for (int ch = l0; ch < sh.nchunk; ch += lstep)
         for (int l = 0; l < 3; ++l)
           for (int e = 0; e < 6; ++e) cl[l][e] = cadd(cl[l][e], low[((base + ch) * 3 + l) * 6 + e]);
     int cnt = count[(size_t)w * S_ + s];
-    for (int r = 0; r < cnt; ++r) {
+    for (int r = l0; r < cnt; r += lstep) {
       size_t ib = ((size_t)w * S_ + s) * a.rcap + r;
       int nn = slot_nn[ib];
       for (int e = 0; e < 6; ++e) {
         double2 v = items[ib * 6 + e];
         chi[e] = cadd(chi[e], v);
-        if (nn >= -1 && nn <= 1) cl[nn + 1][e] = cadd(cl[nn + 1][e], v);
+        if (nn == -1) cl[0][e] = cadd(cl[0][e], v);
+        if (nn == 0) cl[1][e] = cadd(cl[1][e], v);
+        if (nn == 1) cl[2][e] = cadd(cl[2][e], v);
       }
     }
+    // warp mode: each lane summed its share of the chunks and items
+    for (int e = 0; e < 6; ++e) wsum(chi[e]);
+    if (ext)
+      for (int l = 0; l < 3; ++l)
+        for (int e = 0; e < 6; ++e) wsum(cl[l][e]);
     if (S.bm) {
       // NHDS chi, divided by n q before the common normalisation as in disp
       // (src/ALPS_fns.f90:344-358); no ee term
@@ -1101,7 +1121,7 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
       for (int l = 0; l < 3; ++l) cl[l][e] = cscale(cl[l][e], norm);
       eps[e] = cadd(eps[e], chi[e]);
     }
-    if (ext) {
+    if (ext && l0 == 0) {
       // chi0 (S x 3 x 3) then chi0_low (S x 3 x 3 x 3), then wave (9)
       double2* c0 = ext + (size_t)w * (S_ * 36 + 9) + s * 9;
       const int ii[6] = {0, 1, 2, 0, 0, 1}, jj[6] = {0, 1, 2, 1, 2, 2};
@@ -1146,8 +1166,8 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
                                cmul(cmul(w13, w13), w22)),
                           cmul(cmul(w12, w12), w33)),
                      cmk(0.0, 0.0));
-  D[w] = det;
-  if (ext) {
+  if (l0 == 0) D[w] = det;
+  if (ext && l0 == 0) {
     double2* wv = ext + (size_t)w * (S_ * 36 + 9) + S_ * 36;
     wv[0] = w11;
     wv[1] = w12;
@@ -1159,6 +1179,108 @@ __global__ void k_finalize(DispArgs a, const double2* __restrict__ om, int n_om,
     wv[7] = cneg(w23);
     wv[8] = w33;
   }
+}
+
+
+// ---------------------------------------------------------------------------
+// Jobs.  Every batch, of one context or fused over many, runs the same four
+// kernels over a table of jobs in device memory: each kernel's grid is the
+// concatenation of the jobs' own grids, and a block finds its job by the
+// first block of each job.  A job's arguments (the context at its k) and its
+// launch shape are those of a lone batch of its size, and one compiled
+// kernel serves every case, so a context's results do not depend on what it
+// was batched with, bit for bit.
+// ---------------------------------------------------------------------------
+struct DispJob {
+  const DispArgs* a;  // the context's arguments (device copy)
+  DispShape sh;
+  int n, js, tiles, S;
+  long blk[4];        // first block of the job in classify, pole sums, resonant, finalize
+  const double2* om;
+  double2* D;
+  double2* part;
+  int* count;
+  int* slot_nn;
+  double2* items;
+  int* flags;
+  double2* low;       // chi_low partials (calc_eigen) or null
+  double2* ext;       // chi0, chi0_low, wave per omega, or null
+  const double2* rel; // relativistic orders, or null
+  const double2* bm;  // closed-form species, or null
+};
+
+// stores a lone batch's arguments and job where its kernels read them
+__global__ void k_stage(DispArgs a, DispJob j, DispArgs* da, DispJob* dj) {
+  const int4* src = reinterpret_cast<const int4*>(&a);
+  int4* dst = reinterpret_cast<int4*>(da);
+  for (int q = threadIdx.x; q < (int)(sizeof(DispArgs) / sizeof(int4)); q += blockDim.x) dst[q] = src[q];
+  if (threadIdx.x == 0) {
+    j.a = da;
+    *dj = j;
+  }
+}
+
+__device__ __forceinline__ const DispJob& job_of(const DispJob* jobs, int nj, long b, int k) {
+  int lo = 0, hi = nj - 1;  // last job whose first block is <= b
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (jobs[mid].blk[k] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return jobs[lo];
+}
+
+// k_finalize: one warp per omega when a batch leaves many order chunks
+// (small batches), one thread per omega otherwise
+__host__ __device__ inline bool fin_warp_mode(const DispShape& sh) { return sh.nchunk >= 8; }
+__host__ __device__ inline long fin_blocks(const DispShape& sh, int n) {
+  return fin_warp_mode(sh) ? (n + 3) / 4 : (n + 127) / 128;
+}
+
+// A block's job is one context: its arguments go to shared memory once, and
+// every thread reads them there.
+__device__ __forceinline__ const DispArgs& stage_args(const DispArgs* src, DispArgs& dst) {
+  const int4* s4 = reinterpret_cast<const int4*>(src);
+  int4* d4 = reinterpret_cast<int4*>(&dst);
+  for (int q = threadIdx.x; q < (int)(sizeof(DispArgs) / sizeof(int4)); q += blockDim.x) d4[q] = s4[q];
+  __syncthreads();
+  return dst;
+}
+
+__global__ void k_classify_multi(const DispJob* __restrict__ jobs, int nj) {
+  __shared__ DispArgs sa;
+  const DispJob& J = job_of(jobs, nj, blockIdx.x, 0);
+  const DispArgs& a = stage_args(J.a, sa);
+  const long lb = (long)blockIdx.x - J.blk[0];
+  classify_body(a, J.om, J.n, J.count, J.slot_nn, J.flags, (lb * blockDim.x + threadIdx.x) >> 5);
+}
+
+template <bool LOW>
+__global__ void __launch_bounds__(128) k_pole_sums_multi(const DispJob* __restrict__ jobs, int nj) {
+  __shared__ DispArgs sa;
+  const DispJob& J = job_of(jobs, nj, blockIdx.x, 1);
+  const DispArgs& a = stage_args(J.a, sa);
+  const long lb = (long)blockIdx.x - J.blk[1];
+  const int tile = (int)(lb % J.tiles), s = (int)((lb / J.tiles) % J.S), chunk = (int)(lb / ((long)J.tiles * J.S));
+  pole_body<LOW>(a, J.sh, J.om, J.n, J.js, J.part, J.low, tile, s, chunk);
+}
+
+__global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant_multi(const DispJob* __restrict__ jobs, int nj) {
+  __shared__ DispArgs sa;
+  const DispJob& J = job_of(jobs, nj, blockIdx.x, 2);
+  const DispArgs& a = stage_args(J.a, sa);
+  resonant_body(a, J.sh, J.om, J.n, J.count, J.slot_nn, J.items, (long)blockIdx.x - J.blk[2]);
+}
+
+__global__ void k_finalize_multi(const DispJob* __restrict__ jobs, int nj) {
+  __shared__ DispArgs sa;
+  const DispJob& J = job_of(jobs, nj, blockIdx.x, 3);
+  const DispArgs& a = stage_args(J.a, sa);
+  const long lb = (long)blockIdx.x - J.blk[3];
+  const bool wm = fin_warp_mode(J.sh);
+  const long w = wm ? lb * (blockDim.x / 32) + threadIdx.x / 32 : lb * blockDim.x + threadIdx.x;
+  finalize_body(a, J.sh, J.om, J.n, J.part, J.low, J.count, J.slot_nn, J.items, J.rel, J.bm, J.D, J.ext, (int)w,
+                wm);
 }
 
 template <typename T>
@@ -1285,36 +1407,104 @@ int collect_profile(alps_ctx* c) {
 }
 
 // Runs the four kernels of one batch on stream st.
+// the arguments of one context at its current k; *maxn = largest nmax
+void build_disp_args(const alps_ctx* c, DispArgs* a, int* maxn) {
+  fill_sys_dev(c, &a->sys);
+  int mx = 0, rc = 1;
+  for (int s = 0; s < c->sys.nspec; ++s) {
+    fill_spec_dev(c, s, &a->sp[s]);
+    mx = std::max(mx, c->spec[s].nmax);
+    rc = std::max(rc, c->spec[s].rcap);
+  }
+  a->rcap = rc;
+  a->relcap = rel_capacity(c);
+  a->has_bm = any_bm(c) ? 1 : 0;
+  *maxn = mx;
+}
+
+// launch shape of a batch of n omegas on a context: j slices and order
+// chunks give small batches more pole-sum blocks, up to about four per SM.
+// The shape depends on n and the context only: the slices and chunks fix
+// the summation order.
+struct BatchGeom {
+  int js, tiles;
+  size_t nslots;
+  DispShape sh;
+};
+BatchGeom batch_geom(int n, int S_, int maxn, int rcap) {
+  BatchGeom b;
+  b.js = (n < 32) ? 32 : ((n < 64) ? 4 : ((n < 128) ? 2 : 1));
+  const int TW = 128 / b.js;
+  b.tiles = (n + TW - 1) / TW;
+  const int want_blocks = 152 * 4;
+  const int nchunk = std::max(1, std::min(maxn + 1, (want_blocks + b.tiles * S_ - 1) / (b.tiles * S_)));
+  b.sh.csize = (maxn + 1 + nchunk - 1) / nchunk;
+  b.sh.nchunk = (maxn + 1 + b.sh.csize - 1) / b.sh.csize;
+  b.nslots = (size_t)n * S_ * rcap;
+  b.sh.ipw = res_items_per_warp((long)b.nslots);
+  return b;
+}
+
+namespace {
+
+// the job of a lone batch (first blocks at 0)
+DispJob lone_job(const DispShape& sh, int n, int js, int tiles, int S_, const double2* om, double2* D, double2* part,
+                 int* count, int* slots, double2* items, int* flags) {
+  DispJob j;
+  j.a = nullptr;
+  j.sh = sh;
+  j.n = n;
+  j.js = js;
+  j.tiles = tiles;
+  j.S = S_;
+  for (int k = 0; k < 4; ++k) j.blk[k] = 0;
+  j.om = om;
+  j.D = D;
+  j.part = part;
+  j.count = count;
+  j.slot_nn = slots;
+  j.items = items;
+  j.flags = flags;
+  j.low = nullptr;
+  j.ext = nullptr;
+  j.rel = nullptr;
+  j.bm = nullptr;
+  return j;
+}
+
+// dynamic shared memory of k_resonant_multi for a context, and the opt-in
+// above 48 KB (per kernel, once per size)
+size_t res_smem(const alps_ctx* c) {
+  return (size_t)RES_WARPS * res_warp_smem(c->sys.nperp, res_win(c->sys.positions_principal)) * sizeof(double2);
+}
+std::mutex g_res_smem_mu;
+size_t g_res_smem_set = 0;
+int res_smem_optin(size_t smem) {
+  if (smem <= 48 * 1024) return ALPS_OK;
+  std::lock_guard<std::mutex> lk(g_res_smem_mu);
+  if (g_res_smem_set < smem) {
+    ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    g_res_smem_set = smem;
+  }
+  return ALPS_OK;
+}
+
+}  // namespace
+
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext, cudaStream_t st) {
   if (n <= 0) return ALPS_OK;
   const int S_ = c->sys.nspec;
   DispArgs a;
-  fill_sys_dev(c, &a.sys);
-  int maxn = 0, rc = 1;
-  for (int s = 0; s < S_; ++s) {
-    fill_spec_dev(c, s, &a.sp[s]);
-    maxn = std::max(maxn, c->spec[s].nmax);
-    rc = std::max(rc, c->spec[s].rcap);
-  }
-  a.rcap = rc;
-  a.relcap = rel_capacity(c);
-  a.has_bm = any_bm(c) ? 1 : 0;
-  // order chunks: enough blocks to fill the device for small batches
-  int js = 1;
-  if (n < 32) js = 32;
-  else if (n < 64) js = 4;
-  else if (n < 128) js = 2;
-  int TW = 128 / js;
-  int tiles = (n + TW - 1) / TW;
-  int want_blocks = 152 * 4;
-  int nchunk = std::max(1, std::min(maxn + 1, (want_blocks + tiles * S_ - 1) / (tiles * S_)));
-  a.csize = (maxn + 1 + nchunk - 1) / nchunk;
-  a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
+  int maxn = 0;
+  build_disp_args(c, &a, &maxn);
+  const BatchGeom bg = batch_geom(n, S_, maxn, a.rcap);
+  const DispShape sh = bg.sh;
+  const int js = bg.js, tiles = bg.tiles;
+  const size_t nslots = bg.nslots;
   int rcode;
   const void* before[8] = {c->d_part, c->d_count, c->d_slot_nn, c->d_items, c->d_low, c->d_rel, c->d_bm, c->d_flags};
-  if ((rcode = ensure_buf(c->d_part, c->part_cap, (size_t)n * S_ * a.nchunk * 6))) return rcode;
+  if ((rcode = ensure_buf(c->d_part, c->part_cap, (size_t)n * S_ * sh.nchunk * 6))) return rcode;
   if ((rcode = ensure_buf(c->d_count, c->count_cap, (size_t)n * S_))) return rcode;
-  size_t nslots = (size_t)n * S_ * rc;
   if (nslots * 6 > c->items_cap || !c->d_slot_nn) {
     if (c->d_slot_nn) cudaFree(c->d_slot_nn);
     c->d_slot_nn = nullptr;
@@ -1323,7 +1513,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   }
   bool want_low = d_ext != nullptr;
   if (want_low)
-    if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * a.nchunk * 18))) return rcode;
+    if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * sh.nchunk * 18))) return rcode;
   if (a.relcap)
     if ((rcode = ensure_buf(c->d_rel, c->rel_cap, (size_t)n * S_ * a.relcap * 2 * 6))) return rcode;
   if (a.has_bm)
@@ -1348,36 +1538,42 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     }
     ALPS_CUDA_TRY(cudaEventRecord(ev[0], st));
   }
-  k_classify<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(a, d_om, n, c->d_count, c->d_slot_nn,
-                                                                            c->d_flags);
+  if (!c->d_args) {
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_args, sizeof(DispArgs)));
+    ALPS_CUDA_TRY(cudaMallocHost(&c->h_args, sizeof(DispArgs)));
+  }
+  if (!c->d_job) ALPS_CUDA_TRY(cudaMalloc(&c->d_job, sizeof(DispJob)));
+  DispJob job = lone_job(sh, n, js, tiles, S_, d_om, d_D, c->d_part, c->d_count, c->d_slot_nn, c->d_items, c->d_flags);
+  job.low = want_low ? c->d_low : nullptr;
+  job.ext = d_ext;
+  job.rel = a.relcap ? c->d_rel : nullptr;
+  job.bm = a.has_bm ? c->d_bm : nullptr;
+  const DispJob* dj = static_cast<const DispJob*>(c->d_job);
+  k_stage<<<1, 128, 0, st>>>(a, job, static_cast<DispArgs*>(c->d_args), static_cast<DispJob*>(c->d_job));
+  ALPS_CUDA_TRY(cudaGetLastError());
+  c->args_gen = c->gen;  // the device copy is the context at its current state
+  c->args_maxn = maxn;
+  c->args_rcap = a.rcap;
+  k_classify_multi<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[1], st));
-  a.cgroup = std::max(1, std::min(c->chunk_group, a.nchunk));
-  dim3 g2(tiles, S_, (a.nchunk + a.cgroup - 1) / a.cgroup);
+  const unsigned g2 = (unsigned)((long)tiles * S_ * sh.nchunk);
   if (want_low)
-    k_pole_sums<true><<<g2, 128, 0, st>>>(a, d_om, n, js, c->d_part, c->d_low);
+    k_pole_sums_multi<true><<<g2, 128, 0, st>>>(dj, 1);
   else
-    k_pole_sums<false><<<g2, 128, 0, st>>>(a, d_om, n, js, c->d_part, nullptr);
+    k_pole_sums_multi<false><<<g2, 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
-  int maxN = c->sys.nperp;
-  size_t smem = (size_t)RES_WARPS * res_warp_smem(maxN, res_win(c->sys.positions_principal)) * sizeof(double2);
-  if (smem > 48 * 1024 && (size_t)c->res_smem_set < smem) {
-    ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    c->res_smem_set = (int)smem;
-  }
-  long total = (long)nslots;
-  a.ipw = res_items_per_warp(total);
-  long blocks = (total + RES_WARPS * a.ipw - 1) / (RES_WARPS * a.ipw);
-  k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, d_om, n, c->d_count, c->d_slot_nn, c->d_items,
-                                                             c->d_flags);
+  const size_t smem = res_smem(c);
+  if ((rcode = res_smem_optin(smem))) return rcode;
+  long blocks = ((long)nslots + RES_WARPS * sh.ipw - 1) / (RES_WARPS * sh.ipw);
+  k_resonant_multi<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (a.relcap && (rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, d_om, c->d_rel, c->d_flags, st)))
     return rcode;
   if (a.has_bm && (rcode = launch_nhds(a.sys, a.sp, n, d_om, c->d_bm, st))) return rcode;
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[3], st));
-  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, d_om, n, c->d_part, want_low ? c->d_low : nullptr, c->d_count,
-                                              c->d_slot_nn, c->d_items, c->d_rel, c->d_bm, d_D, d_ext);
+  k_finalize_multi<<<(unsigned)fin_blocks(sh, n), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) {
     ALPS_CUDA_TRY(cudaEventRecord(ev[4], st));
@@ -1385,6 +1581,152 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   }
   c->stats.n_eval = n;
   c->stats.kernels_launched = 4 + (a.relcap ? 1 : 0) + (a.has_bm ? 1 : 0);
+  return ALPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Fused batches of several contexts (the request server's rounds)
+// ---------------------------------------------------------------------------
+struct MultiScratch {
+  DispJob* d_jobs = nullptr;
+  DispJob* h_jobs = nullptr;  // pinned
+  size_t jobs_cap = 0;
+  double2* part = nullptr;
+  size_t part_cap = 0;
+  int* count = nullptr;
+  size_t count_cap = 0;
+  int* slots = nullptr;
+  size_t slots_cap = 0;
+  double2* items = nullptr;
+  size_t items_cap = 0;
+};
+
+void multi_scratch_free(MultiScratch* m) {
+  if (!m) return;
+  cudaFree(m->d_jobs);
+  cudaFreeHost(m->h_jobs);
+  cudaFree(m->part);
+  cudaFree(m->count);
+  cudaFree(m->slots);
+  cudaFree(m->items);
+  delete m;
+}
+
+bool ctx_fusable(const alps_ctx* c) { return !rel_capacity(c) && !any_bm(c) && !c->profiling; }
+
+namespace {
+
+// the context's kernel arguments on the device, rebuilt when the plasma, k,
+// precision or a table moved (alps_ctx::gen)
+int ctx_device_args(alps_ctx* c, cudaStream_t st, const DispArgs** out) {
+  if (!c->d_args) {
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_args, sizeof(DispArgs)));
+    ALPS_CUDA_TRY(cudaMallocHost(&c->h_args, sizeof(DispArgs)));
+    c->args_gen = 0;
+  }
+  if (c->args_gen != c->gen) {
+    DispArgs* h = static_cast<DispArgs*>(c->h_args);
+    build_disp_args(c, h, &c->args_maxn);
+    c->args_rcap = h->rcap;
+    ALPS_CUDA_TRY(cudaMemcpyAsync(c->d_args, h, sizeof(DispArgs), cudaMemcpyHostToDevice, st));
+    c->args_gen = c->gen;
+  }
+  *out = static_cast<const DispArgs*>(c->d_args);
+  return ALPS_OK;
+}
+
+}  // namespace
+
+int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
+                      MultiScratch** scratch, cudaStream_t st) {
+  if (nj <= 0) return ALPS_OK;
+  MultiScratch* m = *scratch;
+  if (!m) *scratch = m = new MultiScratch();
+  if ((size_t)nj > m->jobs_cap) {
+    cudaFree(m->d_jobs);
+    cudaFreeHost(m->h_jobs);
+    m->d_jobs = nullptr;
+    m->h_jobs = nullptr;
+    m->jobs_cap = 0;
+    ALPS_CUDA_TRY(cudaMalloc(&m->d_jobs, (size_t)nj * sizeof(DispJob)));
+    ALPS_CUDA_TRY(cudaMallocHost(&m->h_jobs, (size_t)nj * sizeof(DispJob)));
+    m->jobs_cap = nj;
+  }
+  // shapes, grid offsets and scratch offsets of every job
+  std::vector<size_t> o_part(nj), o_count(nj), o_slots(nj);
+  size_t part_n = 0, count_n = 0, slots_n = 0, om_off = 0, smem = 0;
+  long blk[4] = {0, 0, 0, 0};
+  for (int j = 0; j < nj; ++j) {
+    alps_ctx* c = ctx[j];
+    const DispArgs* da = nullptr;
+    int rcode = ctx_device_args(c, st, &da);
+    if (rcode) return rcode;
+    const int S_ = c->sys.nspec;
+    const BatchGeom bg = batch_geom(n[j], S_, c->args_maxn, c->args_rcap);
+    DispJob& J = m->h_jobs[j];
+    J.a = da;
+    J.sh = bg.sh;
+    J.n = n[j];
+    J.js = bg.js;
+    J.tiles = bg.tiles;
+    J.S = S_;
+    J.blk[0] = blk[0];
+    blk[0] += ((long)n[j] * S_ * 32 + 127) / 128;
+    J.blk[1] = blk[1];
+    blk[1] += (long)bg.tiles * S_ * bg.sh.nchunk;
+    J.blk[2] = blk[2];
+    blk[2] += ((long)bg.nslots + RES_WARPS * bg.sh.ipw - 1) / (RES_WARPS * bg.sh.ipw);
+    J.blk[3] = blk[3];
+    blk[3] += fin_blocks(bg.sh, n[j]);
+    J.om = d_om + om_off;
+    J.D = d_D + om_off;
+    J.flags = d_flags + j;
+    J.low = nullptr;
+    J.ext = nullptr;
+    J.rel = nullptr;
+    J.bm = nullptr;
+    om_off += n[j];
+    o_part[j] = part_n;
+    part_n += (size_t)n[j] * S_ * bg.sh.nchunk * 6;
+    o_count[j] = count_n;
+    count_n += (size_t)n[j] * S_;
+    o_slots[j] = slots_n;
+    slots_n += bg.nslots;
+    smem = std::max(smem, res_smem(c));
+  }
+  // items per warp of k_resonant from the whole round (it does not change sums)
+  const int ipw = res_items_per_warp((long)slots_n);
+  blk[2] = 0;
+  for (int j = 0; j < nj; ++j) {
+    DispJob& J = m->h_jobs[j];
+    J.sh.ipw = ipw;
+    J.blk[2] = blk[2];
+    const long nsl = (long)((j + 1 < nj ? o_slots[j + 1] : slots_n) - o_slots[j]);
+    blk[2] += (nsl + RES_WARPS * ipw - 1) / (RES_WARPS * ipw);
+  }
+  int rcode;
+  if ((rcode = ensure_buf(m->part, m->part_cap, part_n))) return rcode;
+  if ((rcode = ensure_buf(m->count, m->count_cap, count_n))) return rcode;
+  if ((rcode = ensure_buf(m->slots, m->slots_cap, slots_n))) return rcode;
+  if ((rcode = ensure_buf(m->items, m->items_cap, slots_n * 6))) return rcode;
+  for (int j = 0; j < nj; ++j) {
+    DispJob& J = m->h_jobs[j];
+    J.part = m->part + o_part[j];
+    J.count = m->count + o_count[j];
+    J.slot_nn = m->slots + o_slots[j];
+    J.items = m->items + o_slots[j] * 6;
+  }
+  ALPS_CUDA_TRY(cudaMemcpyAsync(m->d_jobs, m->h_jobs, (size_t)nj * sizeof(DispJob), cudaMemcpyHostToDevice, st));
+  ALPS_CUDA_TRY(cudaMemsetAsync(d_flags, 0, (size_t)nj * sizeof(int), st));
+  if ((rcode = res_smem_optin(smem))) return rcode;
+  k_classify_multi<<<(unsigned)blk[0], 128, 0, st>>>(m->d_jobs, nj);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_pole_sums_multi<false><<<(unsigned)blk[1], 128, 0, st>>>(m->d_jobs, nj);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_resonant_multi<<<(unsigned)blk[2], RES_WARPS * 32, smem, st>>>(m->d_jobs, nj);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_finalize_multi<<<(unsigned)blk[3], 128, 0, st>>>(m->d_jobs, nj);
+  ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }
 
@@ -1452,35 +1794,23 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
   const int S_ = c->sys.nspec;
   DispArgs a;
-  fill_sys_dev(c, &a.sys);
-  int maxn = 0, rc = 1;
-  for (int s = 0; s < S_; ++s) {
-    fill_spec_dev(c, s, &a.sp[s]);
-    maxn = std::max(maxn, c->spec[s].nmax);
-    rc = std::max(rc, c->spec[s].rcap);
-  }
-  a.rcap = rc;
-  a.relcap = rel_capacity(c);
-  a.has_bm = any_bm(c) ? 1 : 0;
-  int js = 1;
-  if (n < 32) js = 32;
-  else if (n < 64) js = 4;
-  else if (n < 128) js = 2;
-  int TW = 128 / js;
-  int tiles = (n + TW - 1) / TW;
-  int nchunk = std::max(1, std::min(maxn + 1, (152 * 4 + tiles * S_ - 1) / (tiles * S_)));
-  a.csize = (maxn + 1 + nchunk - 1) / nchunk;
-  a.nchunk = (maxn + 1 + a.csize - 1) / a.csize;
+  int maxn = 0;
+  build_disp_args(c, &a, &maxn);
+  const BatchGeom bg = batch_geom(n, S_, maxn, a.rcap);
+  const DispShape sh = bg.sh;
+  const int js = bg.js, tiles = bg.tiles;
   // scratch layout: flags | count | slot_nn | part | items | relativistic orders | NHDS
   size_t off = 0;
   size_t o_flags = carve(off, sizeof(int));
   size_t o_count = carve(off, (size_t)n * S_ * sizeof(int));
-  size_t nslots = (size_t)n * S_ * rc;
+  size_t nslots = bg.nslots;
   size_t o_slots = carve(off, nslots * sizeof(int));
-  size_t o_part = carve(off, (size_t)n * S_ * a.nchunk * 6 * sizeof(double2));
+  size_t o_part = carve(off, (size_t)n * S_ * sh.nchunk * 6 * sizeof(double2));
   size_t o_items = carve(off, nslots * 6 * sizeof(double2));
   size_t o_rel = carve(off, (size_t)n * S_ * a.relcap * 2 * 6 * sizeof(double2));
   size_t o_bm = carve(off, (size_t)n * S_ * (a.has_bm ? 24 : 0) * sizeof(double2));
+  size_t o_args = carve(off, sizeof(DispArgs));
+  size_t o_job = carve(off, sizeof(DispJob));
   if (scratch_bytes) *scratch_bytes = off;
   if (off > ALPS_NOALLOC_SCRATCH_BYTES) return ALPS_E_INVALID;  // batch too large for the static scratch
   unsigned char* b = static_cast<unsigned char*>(base);
@@ -1494,17 +1824,22 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   const double2* om = reinterpret_cast<const double2*>(d_om);
   double2* D = reinterpret_cast<double2*>(d_D);
   ALPS_CUDA_TRY(cudaMemsetAsync(flags, 0, sizeof(int), st));
-  k_classify<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(a, om, n, count, slots, flags);
+  DispJob job = lone_job(sh, n, js, tiles, S_, om, D, part, count, slots, items, flags);
+  job.rel = a.relcap ? relb : nullptr;
+  job.bm = a.has_bm ? bmb : nullptr;
+  DispArgs* da = reinterpret_cast<DispArgs*>(b + o_args);
+  DispJob* dj = reinterpret_cast<DispJob*>(b + o_job);
+  k_stage<<<1, 128, 0, st>>>(a, job, da, dj);
   ALPS_CUDA_TRY(cudaGetLastError());
-  a.cgroup = 1;
-  k_pole_sums<false><<<dim3(tiles, S_, a.nchunk), 128, 0, st>>>(a, om, n, js, part, nullptr);
+  k_classify_multi<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
-  size_t smem = (size_t)RES_WARPS * res_warp_smem(c->sys.nperp, res_win(c->sys.positions_principal)) * sizeof(double2);
-  if (smem > 48 * 1024)
-    ALPS_CUDA_TRY(cudaFuncSetAttribute(k_resonant, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  a.ipw = res_items_per_warp((long)nslots);
-  long blocks = ((long)nslots + RES_WARPS * a.ipw - 1) / (RES_WARPS * a.ipw);
-  k_resonant<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(a, om, n, count, slots, items, flags);
+  k_pole_sums_multi<false><<<(unsigned)((long)tiles * S_ * sh.nchunk), 128, 0, st>>>(dj, 1);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  const size_t smem = res_smem(c);
+  int rcode0 = res_smem_optin(smem);
+  if (rcode0) return rcode0;
+  long blocks = ((long)nslots + RES_WARPS * sh.ipw - 1) / (RES_WARPS * sh.ipw);
+  k_resonant_multi<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (a.relcap) {
     int rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, om, relb, flags, st);
@@ -1514,7 +1849,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
     int rcode = launch_nhds(a.sys, a.sp, n, om, bmb, st);
     if (rcode) return rcode;
   }
-  k_finalize<<<(n + 127) / 128, 128, 0, st>>>(a, om, n, part, nullptr, count, slots, items, relb, bmb, D, nullptr);
+  k_finalize_multi<<<(unsigned)fin_blocks(sh, n), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -2,16 +2,23 @@
 // many plasmas (alps_server_*, declared in include/alps_gb300.h).
 //
 // Admitted requests are grouped by context.  One host thread drives every
-// group independently: an idle group puts the frequencies all its requests
-// need next (the pending evaluations of their root finders, or a lattice)
-// into one batch on the context's stream and records an event; the thread
-// polls the events and, as each batch lands, hands every request its slice
-// of the determinants (root_finders.h: the reference's secant_osc / secant /
-// rtsec), releases the finished requests, lets queued requests on that
-// plasma join, and launches the group's next batch.  Groups of different
-// plasmas overlap on the GPU and never wait for each other.  A k scan moves
-// its context's k, so it runs alone on its context, and its k steps
-// (alps_set_k, which synchronises the context) run on worker threads.
+// group: an idle group gathers the frequencies all its requests need next
+// (the pending evaluations of their root finders, or a lattice).
+//
+// * Root-finder evaluations on plasmas without relativistic or closed-form
+//   species go into fused rounds: one set of kernels evaluates every ready
+//   group, each context with the launch shape of a lone batch of its size,
+//   so its sums and results are exactly those of a lone batch.  Two rounds
+//   can be in flight, on two streams.
+// * Lattices, and the plasmas the fused kernels do not take, run as their
+//   own batch on the context's stream (replayed as CUDA graphs).
+//
+// The thread polls the rounds' and batches' events; as one lands it hands
+// every request its slice of the determinants (root_finders.h: the
+// reference's secant_osc / secant / rtsec), releases the finished requests,
+// lets queued requests on that plasma join, and the groups go out again.  A
+// k scan moves its context's k, so it runs alone on its context, and its k
+// steps (alps_set_k, which synchronises the context) run on worker threads.
 // Requests join while their estimated device footprint fits the budget.
 #include <algorithm>
 #include <chrono>
@@ -58,7 +65,8 @@ struct Active {
 struct Group {
   alps_ctx* ctx = nullptr;
   std::vector<Active*> members;
-  enum { IDLE, IN_FLIGHT, STEPPING } state = IDLE;
+  // IN_FLIGHT: a batch on the context's stream; FUSED: in a fused round
+  enum { IDLE, IN_FLIGHT, FUSED, STEPPING } state = IDLE;
   std::future<void> step;  // a scan's k step
   std::vector<alps_complex> bom, bD;
   bool has_scan() const {
@@ -278,9 +286,9 @@ int run_batch(alps_ctx* c, int n) {
   return ALPS_OK;
 }
 
-// One batch with the next evaluations of every request of the group, on
-// the group's context stream; nothing launched when no request needs any.
-int launch_group(Group& g) {
+// The next evaluations of every request of the group, into g.bom (each
+// request's slice at a->off, a->cnt).
+void gather_group(Group& g) {
   g.bom.clear();
   for (Active* a : g.members) {
     a->off = g.bom.size();
@@ -299,6 +307,26 @@ int launch_group(Group& g) {
     a->cnt = g.bom.size() - a->off;
     if (a->cnt) a->rq->rounds += 1;
   }
+}
+
+// True when the group's next batch holds a lattice (it then runs on the
+// context's own stream, not in a fused round).
+bool wants_map(const Group& g) {
+  for (const Active* a : g.members)
+    if (a->status == ALPS_OK && a->rq->kind == ALPS_REQ_MAP && !a->map_done) return true;
+  return false;
+}
+
+bool wants_evals(const Group& g) {
+  for (const Active* a : g.members)
+    if (a->status == ALPS_OK && a->rq->kind != ALPS_REQ_MAP && evals_pending(a)) return true;
+  return false;
+}
+
+// One batch with the next evaluations of every request of the group, on
+// the group's context stream; nothing launched when no request needs any.
+int launch_group(Group& g) {
+  gather_group(g);
   int n = (int)g.bom.size();
   g.bD.resize(n);
   if (n == 0) return ALPS_OK;
@@ -312,19 +340,16 @@ int launch_group(Group& g) {
   return ALPS_OK;
 }
 
-// Hands every request its slice of a landed batch.
-void land_group(Group& g) {
-  alps_ctx* c = g.ctx;
-  int n = (int)g.bom.size();
-  int f = *c->h_flag;
-  std::memcpy(g.bD.data(), c->h_pinned + n, (size_t)n * sizeof(double2));
+// Hands every request its slice of a landed batch: det D of the group's
+// frequencies and the batch's error flags.
+void land_slice(Group& g, const alps_complex* batchD, int f) {
   for (Active* a : g.members) {
     if (!a->cnt) continue;
     if (f) {
       a->status = (f & 2) ? ALPS_E_SUBLUMINAL : ALPS_E_INVALID;
       continue;
     }
-    const alps_complex* D = g.bD.data() + a->off;
+    const alps_complex* D = batchD + a->off;
     if (a->rq->kind == ALPS_REQ_MAP) {
       map_finish((int)a->cnt, D, a->rq->map_cal, a->rq->map_val);
       a->map_done = true;
@@ -340,6 +365,119 @@ void land_group(Group& g) {
     }
   }
 }
+
+void land_group(Group& g) {
+  alps_ctx* c = g.ctx;
+  int n = (int)g.bom.size();
+  std::memcpy(g.bD.data(), c->h_pinned + n, (size_t)n * sizeof(double2));
+  land_slice(g, g.bD.data(), *c->h_flag);
+}
+
+// A fused round: the next evaluations of many groups (root finders on
+// fusable contexts) in one set of kernels on the round's stream.
+struct Round {
+  cudaStream_t st = nullptr;
+  cudaEvent_t ev = nullptr;
+  MultiScratch* scratch = nullptr;
+  double2* d_om = nullptr;
+  double2* d_D = nullptr;
+  alps_complex* h_om = nullptr;  // pinned
+  alps_complex* h_D = nullptr;   // pinned
+  size_t cap = 0;
+  int* d_flags = nullptr;
+  int* h_flags = nullptr;  // pinned
+  size_t fcap = 0;
+  std::vector<Group*> groups;
+  std::vector<size_t> off;  // first frequency of each group
+  bool busy = false;
+
+  ~Round() {
+    if (st) cudaStreamSynchronize(st);
+    multi_scratch_free(scratch);
+    cudaFree(d_om);
+    cudaFree(d_D);
+    cudaFreeHost(h_om);
+    cudaFreeHost(h_D);
+    cudaFree(d_flags);
+    cudaFreeHost(h_flags);
+    if (ev) cudaEventDestroy(ev);
+    if (st) cudaStreamDestroy(st);
+  }
+
+  int reserve(size_t n, size_t nj) {
+    if (!st) {
+      ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+      ALPS_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    }
+    if (n > cap) {
+      const size_t c2 = std::max(n, 2 * cap);
+      cudaFree(d_om);
+      cudaFree(d_D);
+      cudaFreeHost(h_om);
+      cudaFreeHost(h_D);
+      d_om = d_D = nullptr;
+      h_om = h_D = nullptr;
+      cap = 0;
+      ALPS_CUDA_TRY(cudaMalloc(&d_om, c2 * sizeof(double2)));
+      ALPS_CUDA_TRY(cudaMalloc(&d_D, c2 * sizeof(double2)));
+      ALPS_CUDA_TRY(cudaMallocHost(&h_om, c2 * sizeof(alps_complex)));
+      ALPS_CUDA_TRY(cudaMallocHost(&h_D, c2 * sizeof(alps_complex)));
+      cap = c2;
+    }
+    if (nj > fcap) {
+      cudaFree(d_flags);
+      cudaFreeHost(h_flags);
+      d_flags = nullptr;
+      h_flags = nullptr;
+      fcap = 0;
+      ALPS_CUDA_TRY(cudaMalloc(&d_flags, nj * sizeof(int)));
+      ALPS_CUDA_TRY(cudaMallocHost(&h_flags, nj * sizeof(int)));
+      fcap = nj;
+    }
+    return ALPS_OK;
+  }
+
+  // gathers and launches the next evaluations of the ready groups
+  int launch(const std::vector<Group*>& ready) {
+    groups.clear();
+    off.clear();
+    std::vector<alps_ctx*> ctx;
+    std::vector<int> ns;
+    size_t n = 0;
+    for (Group* g : ready) {
+      gather_group(*g);
+      if (g->bom.empty()) continue;
+      groups.push_back(g);
+      off.push_back(n);
+      ctx.push_back(g->ctx);
+      ns.push_back((int)g->bom.size());
+      n += g->bom.size();
+    }
+    if (groups.empty()) return ALPS_OK;
+    int st_ = reserve(n, groups.size());
+    if (st_) return st_;
+    for (size_t j = 0; j < groups.size(); ++j)
+      std::memcpy(h_om + off[j], groups[j]->bom.data(), groups[j]->bom.size() * sizeof(alps_complex));
+    ALPS_CUDA_TRY(cudaMemcpyAsync(d_om, h_om, n * sizeof(double2), cudaMemcpyHostToDevice, st));
+    if ((st_ = launch_disp_multi(ctx.data(), ns.data(), (int)ctx.size(), d_om, d_D, d_flags, &scratch, st)))
+      return st_;
+    ALPS_CUDA_TRY(cudaMemcpyAsync(h_D, d_D, n * sizeof(double2), cudaMemcpyDeviceToHost, st));
+    ALPS_CUDA_TRY(cudaMemcpyAsync(h_flags, d_flags, groups.size() * sizeof(int), cudaMemcpyDeviceToHost, st));
+    ALPS_CUDA_TRY(cudaEventRecord(ev, st));
+    for (Group* g : groups) g->state = Group::FUSED;
+    busy = true;
+    return ALPS_OK;
+  }
+
+  void land() {
+    for (size_t j = 0; j < groups.size(); ++j) {
+      land_slice(*groups[j], h_D + off[j], h_flags[j]);
+      groups[j]->state = Group::IDLE;
+    }
+    groups.clear();
+    busy = false;
+  }
+};
 
 }  // namespace
 
@@ -384,6 +522,7 @@ void alps_server::finish(Active* a) {
 
 void alps_server::run() {
   std::map<alps_ctx*, Group> groups;
+  Round rounds[2];  // fused rounds in flight at once
   size_t in_use = 0;
   int n_active = 0;
   for (;;) {
@@ -431,6 +570,24 @@ void alps_server::run() {
       }
     }
     bool progressed = false;
+    for (Round& R : rounds) {
+      if (!R.busy) continue;
+      cudaError_t q = cudaEventQuery(R.ev);
+      if (q == cudaErrorNotReady) continue;
+      progressed = true;
+      if (q == cudaSuccess) {
+        R.land();
+      } else {
+        alps_set_last_cuda_error(q, "cudaEventQuery", __FILE__, __LINE__);
+        for (Group* g : R.groups) {
+          for (Active* a : g->members) a->status = ALPS_E_CUDA;
+          g->state = Group::IDLE;
+        }
+        R.groups.clear();
+        R.busy = false;
+      }
+    }
+    std::vector<Group*> ready;  // groups whose next batch can join a fused round
     for (auto gi = groups.begin(); gi != groups.end();) {
       Group& g = gi->second;
       if (g.state == Group::STEPPING) {
@@ -476,17 +633,33 @@ void alps_server::run() {
           g.step = std::async(std::launch::async, scan_step, sc);
           progressed = true;
         } else if (!g.members.empty()) {
-          int st = launch_group(g);
-          if (st)
-            for (Active* a : g.members) a->status = st;
-          if (g.state == Group::IN_FLIGHT) ++batches;
-          progressed = true;
+          if (!wants_map(g) && wants_evals(g) && ctx_fusable(g.ctx)) {
+            ready.push_back(&g);
+          } else {
+            int st = launch_group(g);
+            if (st)
+              for (Active* a : g.members) a->status = st;
+            if (g.state == Group::IN_FLIGHT) ++batches;
+            progressed = true;
+          }
         }
       }
       if (g.state == Group::IDLE && g.members.empty())
         gi = groups.erase(gi);
       else
         ++gi;
+    }
+    if (!ready.empty()) {
+      for (Round& R : rounds) {
+        if (R.busy) continue;
+        int st = R.launch(ready);
+        if (st)
+          for (Group* g : ready)
+            for (Active* a : g->members) a->status = st;
+        batches += (int64_t)R.groups.size();
+        progressed = true;
+        break;
+      }
     }
     if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
   }
