@@ -253,25 +253,19 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
       }
     }
   }
-  // reduce over the j slices
-  __shared__ double2 red[128 * 6];
-  if (js_count > 1) {
-    for (int e = 0; e < 6; ++e) red[threadIdx.x * 6 + e] = acc[e];
-    __syncthreads();
-    if (js == 0)
-      for (int q = 1; q < js_count; ++q)
-        for (int e = 0; e < 6; ++e) acc[e] = cadd(acc[e], red[(wl * js_count + q) * 6 + e]);
-    if (LOW) {
-      for (int l = 0; l < 3; ++l) {
-        __syncthreads();
-        for (int e = 0; e < 6; ++e) red[threadIdx.x * 6 + e] = lacc[LOW ? l : 0][e];
-        __syncthreads();
-        if (js == 0)
-          for (int q = 1; q < js_count; ++q)
-            for (int e = 0; e < 6; ++e)
-              lacc[LOW ? l : 0][e] = cadd(lacc[LOW ? l : 0][e], red[(wl * js_count + q) * 6 + e]);
-      }
+  // reduce over the j slices: they are adjacent lanes of one warp (js_count
+  // divides 32), so a butterfly over the lane offsets below js_count
+  auto slice_sum = [&](double2& v) {
+    for (int off = js_count >> 1; off > 0; off >>= 1) {
+      v.x += __shfl_xor_sync(0xffffffffu, v.x, off);
+      v.y += __shfl_xor_sync(0xffffffffu, v.y, off);
     }
+  };
+  if (js_count > 1) {
+    for (int e = 0; e < 6; ++e) slice_sum(acc[e]);
+    if (LOW)
+      for (int l = 0; l < 3; ++l)
+        for (int e = 0; e < 6; ++e) slice_sum(lacc[LOW ? l : 0][e]);
   }
   if (js == 0 && active) {
     size_t base = ((size_t)w * a.sys.nspec + s) * sh.nchunk + chunk;
