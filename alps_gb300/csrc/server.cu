@@ -650,18 +650,25 @@ void alps_server::run() {
         ++gi;
     }
     if (!ready.empty()) {
-      for (Round& R : rounds) {
-        if (R.busy) continue;
-        int st = R.launch(ready);
+      // with both round slots free the ready groups split in two, so that
+      // two rounds stay in flight and one's tail overlaps the other's work
+      std::vector<Round*> free_rounds;
+      for (Round& R : rounds)
+        if (!R.busy) free_rounds.push_back(&R);
+      const size_t parts = std::min(free_rounds.size(), ready.size());
+      for (size_t k = 0; k < parts; ++k) {
+        std::vector<Group*> share(ready.begin() + ready.size() * k / parts,
+                                  ready.begin() + ready.size() * (k + 1) / parts);
+        Round& R = *free_rounds[k];
+        int st = R.launch(share);
         if (st)
-          for (Group* g : ready)
+          for (Group* g : share)
             for (Active* a : g->members) a->status = st;
         batches += (int64_t)R.groups.size();
         progressed = true;
-        break;
       }
     }
-    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(5));
   }
 }
 
