@@ -291,17 +291,18 @@ typedef struct alps_input {
  * per MPI job); each request does what the named reference driver does for
  * its plasma.
  *
- * A background thread drives the active requests independently: a request
- * whose context is idle launches one batch (the frequencies its root
- * finders, or its lattice, need) on that context's stream; as each batch
- * lands the determinants go back into the request's root finders and its
- * next batch goes out, so batches of different plasmas overlap on the GPU
- * and no request waits for a slower one.  The k steps of scans run on
- * worker threads.  Requests that arrive while others run are admitted as
- * soon as their estimated device footprint (the context's tables and the
- * largest batch they will launch) fits the budget and their context is not
- * serving another request.  Every request evaluates exactly the kernels it
- * would evaluate alone, so results do not depend on what else is in flight.
+ * A background thread drives the active requests.  The pending root-finder
+ * evaluations of every ready plasma go into one fused launch (a round; two
+ * rounds stay in flight); lattices, and plasmas with relativistic or
+ * closed-form species, launch their own batch on their context's stream.
+ * As a batch lands the determinants go back into the requests' root
+ * finders and their next evaluations join the next round, so no request
+ * waits for a slower one.  The k steps of scans run on worker threads.
+ * Requests that arrive while others run are admitted as soon as their
+ * estimated device footprint (the context's tables and the largest batch
+ * they will launch) fits the budget.  A fused launch evaluates each plasma
+ * with the launch shape of a lone batch of its size, so every result is
+ * bit for bit what the request gives alone, whatever else is in flight.
  * ------------------------------------------------------------------------ */
 typedef struct alps_server alps_server;
 
