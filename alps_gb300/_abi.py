@@ -66,6 +66,15 @@ class alps_map_params(C.Structure):
     ]
 
 
+class alps_interp_params(C.Structure):
+    _fields_ = [
+        ("nperp", C.c_int), ("npar", C.c_int), ("smoothing", C.c_double),
+        ("pperp_min", C.c_double), ("pperp_max", C.c_double),
+        ("ppar_min", C.c_double), ("ppar_max", C.c_double),
+        ("do_normalize", C.c_int), ("mult_f", C.c_double),
+    ]
+
+
 class alps_dist_params(C.Structure):
     _fields_ = [
         ("kind", C.c_int), ("ms", C.c_double), ("tau", C.c_double),

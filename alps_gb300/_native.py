@@ -72,6 +72,8 @@ def lib():
             "alps_set_profiling": ([vp, C.c_int], C.c_int),
             "alps_disp_batch_noalloc": ([vp, C.c_int, vp, vp, vp, P(C.c_size_t)], C.c_int),
             "alps_get_profile": ([vp, dp, P(C.c_int64)], C.c_int),
+            "alps_interpolate": ([dp, dp, dp, C.c_int, P(_abi.alps_interp_params), dp, dp, dp], C.c_int),
+            "alps_run_interpolation": ([C.c_char_p, C.c_char_p], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -96,5 +98,5 @@ def exported_symbols():
         "alps_secant", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
         "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_read_input", "alps_read_f0",
         "alps_get_f0_rel", "alps_calc_eigen", "alps_server_create", "alps_server_destroy", "alps_server_submit",
-        "alps_server_poll", "alps_server_wait", "alps_server_stats",
+        "alps_server_poll", "alps_server_wait", "alps_server_stats", "alps_interpolate", "alps_run_interpolation",
     ]

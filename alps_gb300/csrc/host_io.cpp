@@ -148,7 +148,8 @@ std::string to_string_val(const std::string& v) {
 
 struct Reader {
   const Group* g;
-  bool has(const char* k) const { return g && g->count(k); }
+  // a key given without a value (a Fortran null value) keeps the default
+  bool has(const char* k) const { return g && g->count(k) && !trim(g->at(k)).empty(); }
   void d(const char* k, double& x) const {
     if (has(k)) x = to_double(g->at(k));
   }
@@ -787,6 +788,100 @@ int alps_run_input(const char* input_path, const char* workdir) {
       }
     }
   }
+  return ALPS_OK;
+}
+
+
+// interpolation/interpolation.f90 (program interpolate): namelist, coarse
+// table, spline on the device, .array output
+int alps_run_interpolation(const char* input_path, const char* workdir) {
+  if (!input_path) return ALPS_E_INVALID;
+  std::ifstream fin(input_path);
+  if (!fin) return ALPS_E_IO;
+  std::stringstream ss;
+  ss << fin.rdbuf();
+  auto nl = parse_namelists(ss.str());
+  Reader r{nl.count("system") ? &nl.at("system") : nullptr};
+  // defaults of read_in_params (interpolation.f90:259-273)
+  char filename[512] = "";
+  double smoothing = 1.0, threshold = 0.0, mult_pperp = 1.0, mult_ppar = 1.0, mult_f = 1.0;
+  double pperp_max_set = -9999.0, ppar_max_set = -9999.0, pperp_min_set = -9999.0, ppar_min_set = -9999.0;
+  int nperp = 50, npar = 100, mode = 1, out_to_file = 0, do_normalize = 0;
+  r.s("filename", filename, sizeof filename);
+  r.d("smoothing", smoothing);
+  r.i("nperp", nperp);
+  r.i("npar", npar);
+  r.d("ppar_min_set", ppar_min_set);
+  r.d("ppar_max_set", ppar_max_set);
+  r.d("pperp_min_set", pperp_min_set);
+  r.d("pperp_max_set", pperp_max_set);
+  r.i("mode", mode);
+  r.d("threshold", threshold);
+  r.l("out_to_file", out_to_file);
+  r.l("do_normalize", do_normalize);
+  r.d("mult_pperp", mult_pperp);
+  r.d("mult_ppar", mult_ppar);
+  r.d("mult_f", mult_f);
+  std::string in(input_path), dir;
+  size_t slash = in.rfind('/');
+  if (slash != std::string::npos) dir = in.substr(0, slash + 1);
+  std::string cpath = filename;
+  if (!cpath.empty() && cpath[0] != '/') cpath = dir + cpath;
+  std::ifstream fc(cpath);
+  if (!fc) return ALPS_E_IO;
+  // samples with f above the threshold (mode 1: pperp ppar f; 2: ppar pperp f)
+  std::vector<double> gp, gl, gf;
+  double a, b, c;
+  while (fc >> a >> b >> c) {
+    if (!(c > threshold)) continue;
+    gp.push_back(mode == 2 ? b : a);
+    gl.push_back(mode == 2 ? a : b);
+    gf.push_back(c);
+  }
+  if (gf.empty()) return ALPS_E_INVALID;  // "No data points in selection."
+  double pperp_max = -999999.0, pperp_min = 999999.0, ppar_max = -999999.0, ppar_min = 999999.0;
+  for (size_t k = 0; k < gf.size(); ++k) {
+    pperp_max = std::max(pperp_max, gp[k]);
+    pperp_min = std::min(pperp_min, gp[k]);
+    ppar_max = std::max(ppar_max, gl[k]);
+    ppar_min = std::min(ppar_min, gl[k]);
+  }
+  pperp_max *= mult_pperp;
+  pperp_min *= mult_pperp;
+  ppar_max *= mult_ppar;
+  ppar_min *= mult_ppar;
+  if (pperp_max_set != -9999.0) pperp_max = pperp_max_set;
+  if (ppar_max_set != -9999.0) ppar_max = ppar_max_set;
+  if (pperp_min_set != -9999.0) pperp_min = pperp_min_set;
+  if (ppar_min_set != -9999.0) ppar_min = ppar_min_set;
+  for (size_t k = 0; k < gf.size(); ++k) {
+    gp[k] *= mult_pperp;
+    gl[k] *= mult_ppar;
+  }
+  alps_interp_params ip;
+  ip.nperp = nperp;
+  ip.npar = npar;
+  ip.smoothing = smoothing;
+  ip.pperp_min = pperp_min;
+  ip.pperp_max = pperp_max;
+  ip.ppar_min = ppar_min;
+  ip.ppar_max = ppar_max;
+  ip.do_normalize = do_normalize;
+  ip.mult_f = mult_f;
+  const size_t nf = (size_t)(nperp + 1) * (npar + 1);
+  std::vector<double> op(nf), ol(nf), of(nf);
+  int st = alps_interpolate(gp.data(), gl.data(), gf.data(), (int)gf.size(), &ip, op.data(), ol.data(), of.data());
+  if (st) return st;
+  FILE* out = stdout;
+  if (out_to_file) {
+    std::string base = in.substr(slash == std::string::npos ? 0 : slash + 1);
+    if (base.size() > 3 && base.compare(base.size() - 3, 3, ".in") == 0) base = base.substr(0, base.size() - 3);
+    std::string wd = workdir ? workdir : ".";
+    out = std::fopen((wd + "/" + base + ".array").c_str(), "w");
+    if (!out) return ALPS_E_IO;
+  }
+  for (size_t t = 0; t < nf; ++t) std::fprintf(out, "%25.16E %25.16E %25.16E\n", op[t], ol[t], of[t]);
+  if (out_to_file) std::fclose(out);
   return ALPS_OK;
 }
 

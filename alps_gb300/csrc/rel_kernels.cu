@@ -35,8 +35,10 @@ __device__ inline double tps_phi(double r) {
   return r * log(pow(r, r));
 }
 
-// column-major (n+3)^2 system of polyharmonic_spline
-__global__ void k_tps_matrix(const double* __restrict__ gc, const double* __restrict__ pc, int n, double* A) {
+// column-major (n+3)^2 system of polyharmonic_spline, the smoothing added
+// on the diagonal of the kernel block
+__global__ void k_tps_matrix(const double* __restrict__ gc, const double* __restrict__ pc, int n, double smoothing,
+                             double* A) {
   long m = n + 3;
   long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m * m) return;
@@ -45,6 +47,7 @@ __global__ void k_tps_matrix(const double* __restrict__ gc, const double* __rest
   if (i < n && j < n) {
     double dg = gc[i] - gc[j], dp = pc[i] - pc[j];
     v = tps_phi(sqrt(dg * dg + dp * dp));
+    if (i == j) v = v + smoothing;
   } else if (i < n && j >= n) {
     v = (j == n) ? 1.0 : (j == n + 1 ? gc[i] : pc[i]);
   } else if (j < n && i >= n) {
@@ -262,7 +265,91 @@ __global__ void k_rel_cone(const double* __restrict__ f0rel, int ng, int np, int
   cone[ig] = make_int2(lo, up);
 }
 
+// right-hand side of the spline system: log f at the samples, three zeros
+__global__ void k_tps_rhs(const double* __restrict__ f, int n, double* w) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) w[k] = log(f[k]);
+  else if (k < n + 3) w[k] = 0.0;
+}
+
+// spline (log f) on the tensor grid pperp[i] x ppar[j], [i*(npar+1) + j]
+// (the evaluation loop of polyharmonic_spline, interpolation.f90:610-630)
+__global__ void k_tps_eval_grid(const double* __restrict__ w, const double* __restrict__ gc,
+                                const double* __restrict__ pc, int n, const double* __restrict__ pperp,
+                                const double* __restrict__ ppar, int nperp, int npar, double* g) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (nperp + 1) * (npar + 1)) return;
+  const int i = t / (npar + 1), j = t % (npar + 1);
+  const double x = pperp[i], y = ppar[j];
+  double f = 0.0;
+  for (int k = 0; k < n; ++k) {
+    double dg = x - gc[k], dp = y - pc[k];
+    double r = sqrt(dg * dg + dp * dp);
+    if (r >= 1.0) f = f + w[k] * r * r * log(r);
+    else if (r != 0.0) f = f + w[k] * r * log(pow(r, r));
+  }
+  g[t] = f + w[n] + w[n + 1] * x + w[n + 2] * y;
+}
+
+// f = mult exp(g - shift), shift = log(2 pi dpperp dppar sum_ij exp(g) pperp_i)
+// when normalising (normalize, interpolation.f90:520-552); one block, fixed
+// reduction order
+__global__ void k_interp_finish(const double* __restrict__ g, const double* __restrict__ pperp, int nperp, int npar,
+                                double dpp, double dpl, int normalize, double mult, double* f) {
+  __shared__ double red[256];
+  const int tot = (nperp + 1) * (npar + 1);
+  double shift = 0.0;
+  if (normalize) {
+    double acc = 0.0;
+    for (int t = threadIdx.x; t < tot; t += blockDim.x) acc += exp(g[t]) * pperp[t / (npar + 1)];
+    red[threadIdx.x] = acc;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+      __syncthreads();
+    }
+    shift = log(red[0] * dpp * dpl * 2.0 * ALPS_PI);
+  }
+  for (int t = threadIdx.x; t < tot; t += blockDim.x) f[t] = mult * exp(g[t] - shift);
+}
+
 }  // namespace
+
+// Weights of the thin-plate spline through n samples (gc, pc) with the
+// right-hand side already in d_w (n + 3 entries): the dense system of
+// polyharmonic_spline solved by LU with partial pivoting (dgesv).
+int tps_solve_device(const double* d_gc, const double* d_pc, int n, double smoothing, double* d_w, cudaStream_t st) {
+  const int m = n + 3;
+  double* d_A = nullptr;
+  int *d_piv = nullptr, *d_info = nullptr;
+  int status = ALPS_OK;
+  if (cudaMalloc(&d_A, (size_t)m * m * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_piv, m * sizeof(int)) != cudaSuccess || cudaMalloc(&d_info, sizeof(int)) != cudaSuccess) {
+    status = ALPS_E_OOM;
+  }
+  if (!status && cudaMemsetAsync(d_info, 0, sizeof(int), st) != cudaSuccess) status = ALPS_E_CUDA;
+  if (!status) {
+    long mm = (long)m * m;
+    k_tps_matrix<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(d_gc, d_pc, n, smoothing, d_A);
+    if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
+  }
+  for (int k = 0; k < m && !status; ++k) {
+    k_lu_pivot<<<1, 1024, 0, st>>>(d_A, m, k, d_piv, d_info);
+    if (k + 1 < m) k_lu_update<<<m - k - 1, 256, 0, st>>>(d_A, m, k, d_info);
+    if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
+  }
+  if (!status) {
+    k_lu_solve<<<1, 1024, 0, st>>>(d_A, m, d_piv, d_w, d_info);
+    int info = 0;
+    cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) status = ALPS_E_CUDA;
+    else if (info != 0) status = ALPS_E_SINGULAR;
+  }
+  cudaFree(d_A);
+  cudaFree(d_piv);
+  cudaFree(d_info);
+  return status;
+}
 
 // ===========================================================================
 int launch_rel_prepare(alps_ctx* c, int is) {
@@ -304,38 +391,19 @@ int launch_rel_prepare(alps_ctx* c, int is) {
   if (!S.d_cone) ALPS_CUDA_TRY(cudaMalloc(&S.d_cone, (ng + 1) * sizeof(int2)));
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_grel, S.grel.data(), (ng + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_prel, S.prel.data(), (np + 1) * sizeof(double), cudaMemcpyHostToDevice, st));
-  // dense thin-plate-spline system
+  // dense thin-plate-spline system (the reference sets its smoothing to 0
+  // for the relativistic remap, src/ALPS_fns_rel.f90:149-151)
   int m = n + 3;
-  double *d_gc = nullptr, *d_pc = nullptr, *d_A = nullptr, *d_w = nullptr;
-  int *d_piv = nullptr, *d_info = nullptr;
+  double *d_gc = nullptr, *d_pc = nullptr, *d_w = nullptr;
   ALPS_CUDA_TRY(cudaMalloc(&d_gc, n * sizeof(double)));
   ALPS_CUDA_TRY(cudaMalloc(&d_pc, n * sizeof(double)));
-  ALPS_CUDA_TRY(cudaMalloc(&d_A, (size_t)m * m * sizeof(double)));
   ALPS_CUDA_TRY(cudaMalloc(&d_w, m * sizeof(double)));
-  ALPS_CUDA_TRY(cudaMalloc(&d_piv, m * sizeof(int)));
-  ALPS_CUDA_TRY(cudaMalloc(&d_info, sizeof(int)));
   std::vector<double> w(m, 0.0);
   for (int k = 0; k < n; ++k) w[k] = grid[k];
   ALPS_CUDA_TRY(cudaMemcpyAsync(d_gc, gc.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
   ALPS_CUDA_TRY(cudaMemcpyAsync(d_pc, pc.data(), n * sizeof(double), cudaMemcpyHostToDevice, st));
   ALPS_CUDA_TRY(cudaMemcpyAsync(d_w, w.data(), m * sizeof(double), cudaMemcpyHostToDevice, st));
-  ALPS_CUDA_TRY(cudaMemsetAsync(d_info, 0, sizeof(int), st));
-  long mm = (long)m * m;
-  k_tps_matrix<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(d_gc, d_pc, n, d_A);
-  ALPS_CUDA_TRY(cudaGetLastError());
-  int status = ALPS_OK;
-  for (int k = 0; k < m && !status; ++k) {
-    k_lu_pivot<<<1, 1024, 0, st>>>(d_A, m, k, d_piv, d_info);
-    if (k + 1 < m) k_lu_update<<<m - k - 1, 256, 0, st>>>(d_A, m, k, d_info);
-    if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
-  }
-  if (!status) {
-    k_lu_solve<<<1, 1024, 0, st>>>(d_A, m, d_piv, d_w, d_info);
-    int info = 0;
-    cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st);
-    if (cudaStreamSynchronize(st) != cudaSuccess) status = ALPS_E_CUDA;
-    else if (info != 0) status = ALPS_E_SINGULAR;
-  }
+  int status = tps_solve_device(d_gc, d_pc, n, 0.0, d_w, st);
   if (!status) {
     k_tps_eval<<<(unsigned)((nf + 127) / 128), 128, 0, st>>>(d_w, d_gc, d_pc, n, S.d_grel, S.d_prel, ng, np,
                                                               S.d_f0rel);
@@ -360,10 +428,73 @@ int launch_rel_prepare(alps_ctx* c, int is) {
   }
   cudaFree(d_gc);
   cudaFree(d_pc);
-  cudaFree(d_A);
   cudaFree(d_w);
-  cudaFree(d_piv);
-  cudaFree(d_info);
+  return status;
+}
+
+// ===========================================================================
+// The interpolation tool (interpolation/interpolation.f90): thin-plate
+// spline of log f through scattered samples, on a fine tensor grid,
+// optionally normalised.
+extern "C" int alps_interpolate(const double* pperp_c, const double* ppar_c, const double* f_c, int n,
+                                const alps_interp_params* p, double* pperp_out, double* ppar_out, double* f_out) {
+  if (!pperp_c || !ppar_c || !f_c || !p || n < 1 || p->nperp < 2 || p->npar < 2) return ALPS_E_INVALID;
+  for (int k = 0; k < n; ++k)
+    if (!(f_c[k] > 0.0)) return ALPS_E_INVALID;  // log f
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return ALPS_E_NO_DEVICE;
+  const int nperp = p->nperp, npar = p->npar, m = n + 3;
+  const size_t nf = (size_t)(nperp + 1) * (npar + 1);
+  // the fine grid, as the reference forms it
+  std::vector<double> pp(nperp + 1), pl(npar + 1);
+  for (int i = 0; i <= nperp; ++i) pp[i] = p->pperp_min + (p->pperp_max - p->pperp_min) * i / (1.0 * nperp);
+  for (int j = 0; j <= npar; ++j) pl[j] = p->ppar_min + (p->ppar_max - p->ppar_min) * j / (1.0 * npar);
+  cudaStream_t st = nullptr;
+  ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  double *d_gc = nullptr, *d_pc = nullptr, *d_f = nullptr, *d_w = nullptr, *d_pp = nullptr, *d_pl = nullptr;
+  double *d_g = nullptr, *d_out = nullptr;
+  int status = ALPS_OK;
+  if (cudaMalloc(&d_gc, n * sizeof(double)) != cudaSuccess || cudaMalloc(&d_pc, n * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_f, n * sizeof(double)) != cudaSuccess || cudaMalloc(&d_w, m * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_pp, (nperp + 1) * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_pl, (npar + 1) * sizeof(double)) != cudaSuccess || cudaMalloc(&d_g, nf * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&d_out, nf * sizeof(double)) != cudaSuccess)
+    status = ALPS_E_OOM;
+  if (!status) {
+    cudaMemcpyAsync(d_gc, pperp_c, n * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_pc, ppar_c, n * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_f, f_c, n * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_pp, pp.data(), (nperp + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(d_pl, pl.data(), (npar + 1) * sizeof(double), cudaMemcpyHostToDevice, st);
+    k_tps_rhs<<<(m + 127) / 128, 128, 0, st>>>(d_f, n, d_w);
+    if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
+  }
+  if (!status) status = tps_solve_device(d_gc, d_pc, n, p->smoothing, d_w, st);
+  if (!status) {
+    k_tps_eval_grid<<<(unsigned)((nf + 127) / 128), 128, 0, st>>>(d_w, d_gc, d_pc, n, d_pp, d_pl, nperp, npar, d_g);
+    // dpperp = pperp(2,1) - pperp(1,1), dppar = ppar(1,2) - ppar(1,1)
+    k_interp_finish<<<1, 256, 0, st>>>(d_g, d_pp, nperp, npar, pp[2] - pp[1], pl[2] - pl[1], p->do_normalize,
+                                       p->mult_f, d_out);
+    if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
+  }
+  if (!status && f_out && cudaMemcpyAsync(f_out, d_out, nf * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess)
+    status = ALPS_E_CUDA;
+  if (!status && cudaStreamSynchronize(st) != cudaSuccess) status = ALPS_E_CUDA;
+  if (!status)
+    for (int i = 0; i <= nperp; ++i)
+      for (int j = 0; j <= npar; ++j) {
+        if (pperp_out) pperp_out[(size_t)i * (npar + 1) + j] = pp[i];
+        if (ppar_out) ppar_out[(size_t)i * (npar + 1) + j] = pl[j];
+      }
+  cudaFree(d_gc);
+  cudaFree(d_pc);
+  cudaFree(d_f);
+  cudaFree(d_w);
+  cudaFree(d_pp);
+  cudaFree(d_pl);
+  cudaFree(d_g);
+  cudaFree(d_out);
+  cudaStreamDestroy(st);
   return status;
 }
 

@@ -375,6 +375,35 @@ typedef struct alps_dist_params {
 int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar,
                      double* pperp, double* ppar, double* f0, double* ideal);
 
+/* The interpolation tool (interpolation/interpolation.f90): thin-plate
+ * spline of log f through n scattered samples (coordinates already scaled by
+ * mult_pperp / mult_ppar), the smoothing added on the diagonal of the spline
+ * system, evaluated on the fine grid pperp_min + (pperp_max - pperp_min) i /
+ * nperp by ppar_min + (ppar_max - ppar_min) j / npar.  With do_normalize the
+ * result is divided by 2 pi sum_ij f pperp dpperp dppar (normalize,
+ * interpolation.f90:520-552); the output is mult_f times it.  Outputs
+ * [(nperp+1)*(npar+1)], i outer, as the reference writes its .array file
+ * (any pointer may be NULL).  Solved and evaluated on the device.
+ * ALPS_E_INVALID for f <= 0, n < 1 or nperp, npar < 2; ALPS_E_SINGULAR if
+ * the system is. */
+typedef struct alps_interp_params {
+  int nperp, npar;
+  double smoothing;
+  double pperp_min, pperp_max, ppar_min, ppar_max;
+  int do_normalize;
+  double mult_f;
+} alps_interp_params;
+int alps_interpolate(const double* pperp_c, const double* ppar_c, const double* f_c, int n,
+                     const alps_interp_params* p, double* pperp_out, double* ppar_out, double* f_out);
+/* The whole program: reads the &system namelist of input_path (filename,
+ * mode, threshold, smoothing, nperp, npar, p*_min_set / p*_max_set,
+ * out_to_file, do_normalize, mult_pperp, mult_ppar, mult_f, with the
+ * reference's defaults; empty values keep them), reads the coarse table
+ * (relative paths from the input file's folder), and writes
+ * <workdir>/<input name without .in>.array (out_to_file) or the same lines
+ * to stdout. */
+int alps_run_interpolation(const char* input_path, const char* workdir);
+
 /* Device work counters of the last disp batch (for measurement). */
 typedef struct alps_stats {
   int64_t n_eval;             /* frequencies evaluated                        */

@@ -1125,23 +1125,27 @@ cplx int_ee_rel(const Eval& e) {
   return ie;
 }
 
-// polyharmonic_spline (src/ALPS_fns_rel.f90:293-426): thin-plate spline of
-// the coarse samples, solved densely (dgesv), evaluated on the fine grid.
-int polyharmonic_spline(const std::vector<double>& grid, const std::vector<double>& gc,
-                        const std::vector<double>& pc, Species& s, std::vector<double>& out) {
+// Weights of the thin-plate spline of polyharmonic_spline
+// (src/ALPS_fns_rel.f90:293-426, interpolation/interpolation.f90:557-610):
+// the dense system with the smoothing on the diagonal, solved by LU with
+// partial pivoting (dgesv).
+int tps_weights(const std::vector<double>& grid, const std::vector<double>& gc, const std::vector<double>& pc,
+                double smoothing, std::vector<double>& w) {
   int n = (int)grid.size(), m = n + 3;
   auto phi = [](double r) {
     if (r >= 1.0) return r * r * std::log(r);
     if (r == 0.0) return 0.0;
     return r * std::log(std::pow(r, r));
   };
-  std::vector<double> A((size_t)m * m, 0.0), w(m, 0.0);  // column-major
+  std::vector<double> A((size_t)m * m, 0.0);  // column-major
+  w.assign(m, 0.0);
   for (int i = 0; i < n; ++i) {
     w[i] = grid[i];
     for (int j = 0; j < n; ++j) {
       double dg = gc[i] - gc[j], dp = pc[i] - pc[j];
       A[(size_t)i + (size_t)m * j] = phi(std::sqrt(dg * dg + dp * dp));
     }
+    A[(size_t)i + (size_t)m * i] = A[(size_t)i + (size_t)m * i] + smoothing;
     A[(size_t)i + (size_t)m * n] = 1.0;
     A[(size_t)i + (size_t)m * (n + 1)] = gc[i];
     A[(size_t)i + (size_t)m * (n + 2)] = pc[i];
@@ -1177,6 +1181,17 @@ int polyharmonic_spline(const std::vector<double>& grid, const std::vector<doubl
     w[j] /= A[(size_t)j + (size_t)m * j];
     for (int i = 0; i < j; ++i) w[i] -= A[(size_t)i + (size_t)m * j] * w[j];
   }
+  return ALPS_OK;
+}
+
+// polyharmonic_spline (src/ALPS_fns_rel.f90:293-426) on the (Gamma, pparbar)
+// grid; the reference's relativistic smoothing is zero (:149-151)
+int polyharmonic_spline(const std::vector<double>& grid, const std::vector<double>& gc,
+                        const std::vector<double>& pc, Species& s, std::vector<double>& out) {
+  const int n = (int)grid.size();
+  std::vector<double> w;
+  int st = tps_weights(grid, gc, pc, 0.0, w);
+  if (st) return st;
   out.assign((size_t)(s.ng + 1) * (s.np + 1), 0.0);
   for (int i = 0; i <= s.ng; ++i)
     for (int j = 0; j <= s.np; ++j) {
@@ -2437,6 +2452,43 @@ void oracle_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
 
 double oracle_bessj(int n, double x) { return bessj(n, x); }
 double oracle_bessi_scaled(int n, double x) { return besselI_s(n, x); }
+
+// interpolation/interpolation.f90: spline of log f through the samples on
+// the fine grid (:190-197, :600-630), normalize (:520-552), times mult_f
+int oracle_interpolate(const double* pperp_c, const double* ppar_c, const double* f_c, int n, int nperp, int npar,
+                       double smoothing, double pperp_min, double pperp_max, double ppar_min, double ppar_max,
+                       int do_normalize, double mult_f, double* f_out) {
+  if (n < 1 || nperp < 2 || npar < 2) return ALPS_E_INVALID;
+  std::vector<double> grid(n), gc(pperp_c, pperp_c + n), pc(ppar_c, ppar_c + n), w;
+  for (int k = 0; k < n; ++k) grid[k] = std::log(f_c[k]);
+  int st = tps_weights(grid, gc, pc, smoothing, w);
+  if (st) return st;
+  std::vector<double> pp(nperp + 1), pl(npar + 1), g((size_t)(nperp + 1) * (npar + 1));
+  for (int i = 0; i <= nperp; ++i) pp[i] = pperp_min + (pperp_max - pperp_min) * i / (1.0 * nperp);
+  for (int j = 0; j <= npar; ++j) pl[j] = ppar_min + (ppar_max - ppar_min) * j / (1.0 * npar);
+  for (int i = 0; i <= nperp; ++i)
+    for (int j = 0; j <= npar; ++j) {
+      double f = 0.0;
+      for (int k = 0; k < n; ++k) {
+        double dg = pp[i] - gc[k], dp = pl[j] - pc[k];
+        double r = std::sqrt(dg * dg + dp * dp);
+        if (r >= 1.0) f = f + w[k] * r * r * std::log(r);
+        else if (r != 0.0) f = f + w[k] * r * std::log(std::pow(r, r));
+      }
+      g[(size_t)i * (npar + 1) + j] = f + w[n] + w[n + 1] * pp[i] + w[n + 2] * pl[j];
+    }
+  double shift = 0.0;
+  if (do_normalize) {
+    const double dpp = pp[2] - pp[1], dpl = pl[2] - pl[1];
+    double integral = 0.0;
+    for (int i = 0; i <= nperp; ++i)
+      for (int j = 0; j <= npar; ++j) integral = integral + std::exp(g[(size_t)i * (npar + 1) + j]) * pp[i];
+    integral = integral * dpp * dpl;
+    shift = std::log(integral * 2.0 * (2.0 * std::acos(0.0)));  // M_PI = 2 acos(0) there
+  }
+  for (size_t t = 0; t < g.size(); ++t) f_out[t] = mult_f * std::exp(g[t] - shift);
+  return ALPS_OK;
+}
 int oracle_wofz(double x, double y, double* u, double* v) {
   bool flag = false;
   wofz(x, y, *u, *v, flag);

@@ -79,6 +79,12 @@ double oracle_bessj(int n, double x);
 /* exp(-x) I_n(x) and the Faddeeva function of the NHDS branch
  * (src/ALPS_NHDS.f90:537-862); oracle_wofz returns its overflow flag. */
 double oracle_bessi_scaled(int n, double x);
+/* interpolation/interpolation.f90: thin-plate spline of log f through n
+ * samples with smoothing, on the fine grid [(nperp+1)*(npar+1)], normalised
+ * if asked, times mult_f. */
+int oracle_interpolate(const double* pperp_c, const double* ppar_c, const double* f_c, int n, int nperp, int npar,
+                       double smoothing, double pperp_min, double pperp_max, double ppar_min, double ppar_max,
+                       int do_normalize, double mult_f, double* f_out);
 int oracle_wofz(double x, double y, double* u, double* v);
 /* Threads used inside one disp() call (orders in parallel, summed in the
  * reference's order).  Default 1. */

@@ -73,6 +73,8 @@ def lib():
             L.oracle_bessi_scaled.restype = C.c_double
             L.oracle_wofz.argtypes = [C.c_double, C.c_double, P(C.c_double), P(C.c_double)]
             L.oracle_generate_f0.argtypes = [P(_abi.alps_dist_params), C.c_int, C.c_int, dp, dp, dp, dp]
+            L.oracle_interpolate.argtypes = [dp, dp, dp, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                             C.c_double, C.c_double, C.c_double, C.c_int, C.c_double, dp]
             _lib = L
     return _lib
 
@@ -99,6 +101,21 @@ def _cptr(a):
 def bessi_scaled(n, x):
     """exp(-x) I_n(x) of the NHDS branch."""
     return lib().oracle_bessi_scaled(int(n), float(x))
+
+
+def interpolate(pperp_c, ppar_c, f_c, nperp, npar, smoothing, pperp_range, ppar_range, normalize,
+                mult_f=1.0):
+    """interpolation/interpolation.f90: the spline of log f through the
+    samples on the fine grid; returns f [(nperp+1), (npar+1)]."""
+    pp = np.ascontiguousarray(pperp_c, dtype=np.float64)
+    pl = np.ascontiguousarray(ppar_c, dtype=np.float64)
+    ff = np.ascontiguousarray(f_c, dtype=np.float64)
+    out = np.zeros((nperp + 1) * (npar + 1))
+    _chk(lib().oracle_interpolate(_dptr(pp), _dptr(pl), _dptr(ff), len(ff), int(nperp), int(npar),
+                                  float(smoothing), float(pperp_range[0]), float(pperp_range[1]),
+                                  float(ppar_range[0]), float(ppar_range[1]), int(bool(normalize)),
+                                  float(mult_f), _dptr(out)), "oracle_interpolate")
+    return out.reshape(nperp + 1, npar + 1)
 
 
 def wofz(z):

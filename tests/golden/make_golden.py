@@ -6,7 +6,9 @@ Run from the repository root with the reference checked out at REF (default
 
 The copied files are data the reference's test suite asserts on
 (tests/test_kpar_fast.py:12-31) or feeds to ALPS (tests/*.in,
-distribution/*_dist.in); they are copied byte for byte.
+distribution/*_dist.in) and to its interpolation program
+(interpolation/test_interp.in, test_interp_coarse.array); they are copied
+byte for byte.
 """
 import os
 import shutil
@@ -21,7 +23,8 @@ FILES = [
     "tests/test_kpar_fast.heat_kpara_1.root_1",
     "tests/test_kpar_fast.heat_mech_kpara_1.root_1",
 ]
-INPUT_DIRS = ["tests", "distribution"]
+INPUT_DIRS = ["tests", "distribution", "interpolation"]
+DATA_FILES = ["interpolation/test_interp_coarse.array"]
 
 
 def main():
@@ -34,6 +37,10 @@ def main():
                 sub = os.path.join(OUT, "inputs", d)
                 os.makedirs(sub, exist_ok=True)
                 shutil.copyfile(os.path.join(REF, d, name), os.path.join(sub, name))
+    for f in DATA_FILES:
+        sub = os.path.join(OUT, "inputs", os.path.dirname(f))
+        os.makedirs(sub, exist_ok=True)
+        shutil.copyfile(os.path.join(REF, f), os.path.join(sub, os.path.basename(f)))
     print("wrote", OUT)
 
 
