@@ -115,6 +115,7 @@ struct SysDev {
   int M_I, M_P;
   double Tlim, vA;
   double kperp, kpar;
+  double ikpar;  // 1 / kpar
 };
 
 // ---------------------------------------------------------------------------

@@ -135,10 +135,12 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
         double2 d = cmk(g.pr - S.pcen, g.pi);
         double dd = d.x * d.x + d.y * d.y;
         if (!g.res && S.prad * S.prad < 0.5 * dd) {
-          const double rho = S.prad * rsqrt(dd);
-          const double lr = -log(rho), l1 = log1p(-rho);
-          K = (int)ceil((36.7368005696771 - l1) / lr);    // 53 ln 2
-          K32 = (int)ceil((22.8738569584782 - l1) / lr);  // 33 ln 2
+          // term counts from FP32 logarithms, one term added to each for
+          // their rounding (rho < 0.71 here, so the counts are below 110)
+          const float rho = (float)(S.prad * rsqrt(dd));
+          const float lr = -__logf(rho), l1 = log1pf(-rho);
+          K = (int)ceilf((36.7368006f - l1) / lr) + 1;    // 53 ln 2
+          K32 = (int)ceilf((22.8738570f - l1) / lr) + 1;  // 33 ln 2
         }
         if (K <= S.kfar) {
           const double* __restrict__ mom = S.mom + (size_t)n * ALPS_KFAR * 12;
@@ -196,7 +198,7 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
             }
           }
           // S = (1/(k_par d)) sum_k mom_k t^k
-          double2 f = cscale(inv, 1.0 / kpar);
+          double2 f = cscale(inv, a.sys.ikpar);
 #pragma unroll
           for (int q = 0; q < 12; ++q) Sx[q] = cmul(Sx[q], f);
         } else {
@@ -1299,6 +1301,7 @@ void fill_sys_dev(const alps_ctx* c, SysDev* o) {
   o->vA = c->sys.vA;
   o->kperp = c->kperp;
   o->kpar = c->kpar;
+  o->ikpar = 1.0 / c->kpar;
 }
 
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
