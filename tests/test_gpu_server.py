@@ -119,3 +119,26 @@ def test_requests_on_one_plasma_share_batches(api):
     np.testing.assert_allclose(cal, alone_map[1], rtol=1e-12)
     assert srv.stats()["peak_active"] >= 2
     srv.close()
+
+
+def test_fused_rounds_of_many_plasmas_equal_alone(api):
+    """Two dozen plasmas of different grids, species counts, nmax and
+    precision polish at once: their evaluations share fused launches (one
+    job per plasma), each with the launch shape of its lone batch, so every
+    root is bit for bit the lone one."""
+    rng = np.random.default_rng(21)
+    P = []
+    for i in range(24):
+        w = workloads.uneven_plasma(rng, grid=((32, 64), (48, 96), (64, 128))[i % 3])
+        s, sp = workloads.build_uneven(w, api.generate_f0)
+        G = api.Plasma(s, sp, precision="mixed" if i % 2 else "fp64")
+        G.set_k(*w["k"])
+        P.append(G)
+    guesses = [[complex(0.2 + 0.05 * i, -0.02)] for i in range(len(P))]
+    alone = [G.secant(g)[0] for G, g in zip(P, guesses)]
+    srv = api.Server()
+    reqs = [srv.polish(G, g) for G, g in zip(P, guesses)]
+    for r, a in zip(reqs, alone):
+        assert np.array_equal(r.wait(), a, equal_nan=True)
+    assert srv.stats()["peak_active"] >= 8
+    srv.close()
