@@ -81,7 +81,7 @@ class alps_dist_params(C.Structure):
         ("alph", C.c_double), ("p_drift", C.c_double), ("kappa", C.c_double),
         ("beta", C.c_double), ("vA", C.c_double), ("maxP", C.c_double),
         ("autoscale", C.c_int), ("maxPperp", C.c_double),
-        ("maxPpar", C.c_double), ("kappa1", C.c_double),
+        ("maxPpar", C.c_double), ("kappa1", C.c_double), ("species", C.c_int),
     ]
 
 

@@ -320,8 +320,7 @@ __device__ double2 eval_fit_d(const SpecDev& S, double vA, int iperp, double2 p)
     else return cmk(0.0, 0.0);
     double norm = pow(ALPS_PI, -1.5) / pow(ms * 1.0, 1.5);
     double2 p2 = cmul(p, p);
-    double2 arg = cneg(cadd(cscale(p2, 1.0 / (1.0 * ms)), cmk((pperp * pperp) / (1.0 * ms), 0.0)));
-    arg = cmk(-(p2.x / ms + (pperp * pperp) / ms), -(p2.y / ms));
+    double2 arg = cmk(-(p2.x / ms + (pperp * pperp) / ms), -(p2.y / ms));
     return cscale(cexp_d(arg), norm);
   }
   double2 ff = cmk(0.0, 0.0);

@@ -119,6 +119,8 @@ int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* pp
     fit[2] = pd;
     fit[3] = 1.0;
     perpcorr = 1.0 / (tau * beta * ms * alph);
+  } else if (dp->kind == 0) {  // distribution_analyt: no normalisation, no autoscale
+    if (dp->species != 1 && dp->species != 2) return ALPS_E_UNSUPPORTED;
   } else {
     return ALPS_E_UNSUPPORTED;
   }
@@ -134,6 +136,12 @@ int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* pp
       const double vA = dp->vA;
       return std::exp(-(2.0 * ms / (vA * vA * beta * tau * alph)) *
                       std::sqrt(1.0 + p1 * p1 * vA * vA / (ms * ms) + d * d * vA * vA * alph / (ms * ms)));
+    }
+    if (dp->kind == 0) {
+      // the reference's example (distribution/distribution_analyt.f90:59-79):
+      // a Maxwellian with beta = 1 and m = 1 (species 1) or 1/1836 (species 2)
+      const double m0 = (dp->species == 1) ? 1.0 : 1.0 / 1836.0, b0 = 1.0;
+      return (std::pow(pi, -1.5) / std::pow(m0 * b0, 1.5)) * std::exp(-(p2 * p2 / (b0 * m0) + (p1 * p1) / (b0 * m0)));
     }
     double q = (d * d) / (beta * ms * tau) + (p1 * p1) / (tau * beta * ms * alph);
     return std::exp(0.5 * (q - std::exp(q)));

@@ -1,8 +1,8 @@
 """f0 table files from a generate_distribution input file.
 
 Mirrors the reference's offline tool (distribution/generate_distribution.f90)
-for the distribution kinds the library generates (1 bi-Maxwellian,
-2 bi-kappa, 4 bi-Moyal): reads its &system / &spec_i namelists and writes
+for every distribution kind (0 distribution_analyt, 1 bi-Maxwellian,
+2 bi-kappa, 3 Juettner, 4 bi-Moyal): reads its &system / &spec_i namelists and writes
 <outdir>/<writeName>.<is>.array in the layout ALPS reads (read_f0).
 """
 import os
@@ -57,6 +57,7 @@ def read_distribution_input(path):
         if kappa1 is None:
             kappa1 = d.kappa
         d.kappa1 = kappa1
+        d.species = i
         out["species"].append(d)
     return out
 

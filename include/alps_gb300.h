@@ -361,7 +361,9 @@ int alps_read_f0(const char* path, int nperp, int npar, double* pperp,
 int alps_run_input(const char* input_path, const char* workdir);
 
 /* f0 table generator (distribution/generate_distribution.f90:176-300):
- * kind 1 bi-Maxwellian, 2 bi-kappa, 3 Juettner, 4 bi-Moyal.  Writes
+ * kind 0 distribution_analyt (the reference's example function of species
+ * 1 and 2, no normalisation, maxPperp/maxPpar as given), 1 bi-Maxwellian,
+ * 2 bi-kappa, 3 Juettner, 4 bi-Moyal.  Writes
  * (nperp+1)*(npar+1) values into pperp/ppar/f0 and, if ideal!=NULL, the
  * "ideal" fit parameters {fit_1..fit_5, perpcorr}.  Host-only. */
 typedef struct alps_dist_params {
@@ -371,6 +373,7 @@ typedef struct alps_dist_params {
   int autoscale;
   double maxPperp, maxPpar;
   double kappa1;              /* kappa of species 1 (autoscale of bi-kappa) */
+  int species;                /* 1-based species index (kind 0)              */
 } alps_dist_params;
 int alps_generate_f0(const alps_dist_params* dp, int nperp, int npar,
                      double* pperp, double* ppar, double* f0, double* ideal);

@@ -3155,6 +3155,12 @@ int oracle_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* 
       ifit[3] = 1.0;
       iperpcorr = 1.0 / (tau * beta * ms * alph);
       break;
+    case 0:  // distribution_analyt (generate_distribution.f90:177-181)
+      if (dp->species != 1 && dp->species != 2) return ALPS_E_UNSUPPORTED;
+      norm = 1.0;
+      pperp_max = dp->maxPperp;
+      ppar_max = dp->maxPpar;
+      break;
     default:
       return ALPS_E_UNSUPPORTED;
   }
@@ -3172,6 +3178,8 @@ int oracle_generate_f0(const alps_dist_params* dp, int nperp, int npar, double* 
       case 3:
         return std::exp(-(2.0 * ms / (vA * vA * beta * tau * alph)) *
                         std::sqrt(1.0 + pp_ * pp_ * vA * vA / (ms * ms) + d * d * vA * vA * alph / (ms * ms)));
+      case 0:  // real(distribution_analyt(is, pperp, cmplx(ppar))) at the drifted ppar
+        return distribution_analyt(dp->species, pp_, cplx(pl, 0.0)).real();
       default: {
         double q = (d * d) / (beta * ms * tau) + (pp_ * pp_) / (tau * beta * ms * alph);
         return std::exp(0.5 * (q - std::exp(q)));
