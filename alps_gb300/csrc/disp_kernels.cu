@@ -10,13 +10,19 @@
 //     S_{e,g}(n) = sum_j (w_j/2) V_{e,g}(n,j) / (m omega - k_par ppar_j - n q)
 // plus, for resonant orders, the principal-value window and the Landau term.
 //
-// Kernels of one batch (launched on one stream, in this order):
-//   k_classify    resonant orders of each (omega, species) into fixed slots
-//   k_pole_sums   the FP64-bound pole sums, all orders, one thread per omega
-//   k_resonant    principal value + Landau per resonant (omega, species, n),
-//                 one warp per item
-//   k_finalize    chi, epsilon, wave tensor and det, one thread per omega;
-//                 sums in a fixed order, so results do not depend on timing.
+// Kernels of one batch (launched on one stream, in this order), each over
+// a table of jobs (one per context; a lone batch is one job):
+//   k_stage             a lone batch's arguments and job to device memory
+//   k_classify_multi    resonant orders of each (omega, species) into
+//                       fixed slots, one warp per (omega, species)
+//   k_pole_sums_multi   the FP64-bound pole sums over all orders: order
+//                       chunks x omega tiles x node slices
+//   k_resonant_multi    principal value + Landau per resonant (omega,
+//                       species, n): scalar work one item per lane, vector
+//                       work one item per warp
+//   k_finalize_multi    chi, epsilon, wave tensor and det, one thread (or
+//                       warp) per omega; sums in a fixed order, so results
+//                       do not depend on timing or on the other jobs.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
