@@ -132,6 +132,10 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_X);
     cudaFree(S.d_mom);
     cudaFree(S.d_momf);
+    cudaFree(S.d_Vh);  // d_Vl points into it
+    cudaFree(S.d_Vscale);
+    cudaFree(S.d_pph);
+    cudaFree(S.d_ppl);
     cudaFree(S.d_fit_aux);
     cudaFree(S.d_lmom);
     cudaFree(S.d_grel);

@@ -78,6 +78,15 @@ struct SpecDev {
   const double* V;
   const double* mom;  // Laurent moments [(nmax+1)][ALPS_KFAR][12]
   const float* momf;  // the same moments rounded to FP32 (for the series tails)
+  // V as pairs of floats (hi + lo, ~48 bits) scaled by 2^-e per order, Vscale
+  // = 2^e, and ppar as float pairs: the fast path's node sums run on the
+  // FP32 pipes in double-float arithmetic
+  const float* Vh;
+  const float* Vl;
+  const double* Vscale;
+  const float* pph;
+  const float* ppl;
+  int df_sums;
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
   int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)
@@ -139,6 +148,11 @@ struct SpeciesHost {
   double* d_X = nullptr;                  // x_j^k, x_j = (ppar_j - pcen)/prad
   double* d_mom = nullptr;                // Laurent moments
   float* d_momf = nullptr;                // the same in FP32
+  float *d_Vh = nullptr, *d_Vl = nullptr;  // V as float pairs (one allocation, lo after hi)
+  size_t Vf_cap = 0;
+  double* d_Vscale = nullptr;             // per-order scale of the pairs
+  size_t Vs_cap = 0;
+  float *d_pph = nullptr, *d_ppl = nullptr;  // ppar as float pairs
   size_t momf_cap = 0;
   double* d_fit_aux = nullptr;            // Maxwellian continuation factors
   double* d_lmom = nullptr;               // factorised Landau moments

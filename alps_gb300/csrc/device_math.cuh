@@ -126,6 +126,54 @@ __device__ inline double2 csqrt_d(double2 z) {
 }
 
 // Fast FP64 reciprocal: PTX rcp.approx seed + two Newton steps (<= 1 ulp).
+// ---------------------------------------------------------------------------
+// Double-float arithmetic: x = h + l with |l| <= ulp(h)/2, about 48 bits,
+// on the FP32 pipes (64 times the FP64 rate on this part).  Error-free
+// transformations: two_sum (Knuth), the FMA product error; every operation
+// explicitly rounded so that nothing is contracted.
+// ---------------------------------------------------------------------------
+struct dflt {
+  float h, l;
+};
+__device__ __forceinline__ dflt df_of(double x) {
+  const float h = __double2float_rn(x);
+  return {h, __double2float_rn(x - (double)h)};
+}
+__device__ __forceinline__ double df_val(dflt a) { return (double)a.h + (double)a.l; }
+__device__ __forceinline__ dflt df_two_sum(float a, float b) {
+  const float s = __fadd_rn(a, b), bb = __fsub_rn(s, a);
+  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+__device__ __forceinline__ dflt df_quick(float a, float b) {
+  const float s = __fadd_rn(a, b);
+  return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ dflt df_add(dflt a, dflt b) {
+  const dflt s = df_two_sum(a.h, b.h);
+  return df_quick(s.h, __fadd_rn(s.l, __fadd_rn(a.l, b.l)));
+}
+__device__ __forceinline__ dflt df_mul(dflt a, dflt b) {
+  const float p = __fmul_rn(a.h, b.h);
+  const float e = __fmaf_rn(a.h, b.l, __fmaf_rn(a.l, b.h, __fmaf_rn(a.h, b.h, -p)));
+  return df_quick(p, e);
+}
+__device__ __forceinline__ dflt df_neg(dflt a) { return {-a.h, -a.l}; }
+__device__ __forceinline__ dflt df_scale(dflt a, float s) { return {__fmul_rn(a.h, s), __fmul_rn(a.l, s)}; }  // s a power of 2
+// 1/a: one Newton step from the FP32 reciprocal, r = r0 + r0 (1 - a r0)
+__device__ __forceinline__ dflt df_rcp(dflt a) {
+  const float r0 = __frcp_rn(a.h);
+  const dflt e = df_add({1.0f, 0.0f}, df_neg(df_mul(a, {r0, 0.0f})));
+  return df_add({r0, 0.0f}, df_mul({r0, 0.0f}, e));
+}
+// acc += (vh + vl)(rh + rl), the low parts unnormalised until the end
+__device__ __forceinline__ void df_mac(dflt& acc, float vh, float vl, dflt r) {
+  const float p = __fmul_rn(vh, r.h);
+  const float pl = __fmaf_rn(vh, r.l, __fmaf_rn(vl, r.h, __fmaf_rn(vh, r.h, -p)));
+  const dflt s = df_two_sum(acc.h, p);
+  acc.h = s.h;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, pl));
+}
+
 __device__ __forceinline__ double rcp_fast(double x) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));

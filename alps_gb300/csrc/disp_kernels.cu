@@ -207,6 +207,54 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
           double2 f = cscale(inv, a.sys.ikpar);
 #pragma unroll
           for (int q = 0; q < 12; ++q) Sx[q] = cmul(Sx[q], f);
+        } else if (S.df_sums) {
+          // fast path: the node sum in double-float arithmetic on the FP32
+          // pipes (about 48 bits; V in pairs scaled by 2^-e per order)
+          const float* __restrict__ Vh = S.Vh + (size_t)n * (M - 1) * 12;
+          const float* __restrict__ Vl = S.Vl + (size_t)n * (M - 1) * 12;
+          const dflt Ad = df_of(Ar), kd = df_of(kpar), Dd = df_of(Di);
+          const dflt D2 = df_mul(Dd, Dd);
+          dflt sacc[24];
+#pragma unroll
+          for (int q = 0; q < 24; ++q) sacc[q] = {0.0f, 0.0f};
+          auto node = [&](int j, float wgt) {
+            const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
+            const dflt r = df_rcp(df_add(df_mul(dr, dr), D2));
+            const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
+            const float4* vh4 = reinterpret_cast<const float4*>(Vh + (size_t)(j - 1) * 12);
+            const float4* vl4 = reinterpret_cast<const float4*>(Vl + (size_t)(j - 1) * 12);
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const float4 h = __ldg(vh4 + q), l = __ldg(vl4 + q);
+              df_mac(sacc[8 * q + 0], h.x, l.x, Rr);
+              df_mac(sacc[8 * q + 1], h.x, l.x, Ri);
+              df_mac(sacc[8 * q + 2], h.y, l.y, Rr);
+              df_mac(sacc[8 * q + 3], h.y, l.y, Ri);
+              df_mac(sacc[8 * q + 4], h.z, l.z, Rr);
+              df_mac(sacc[8 * q + 5], h.z, l.z, Ri);
+              df_mac(sacc[8 * q + 6], h.w, l.w, Rr);
+              df_mac(sacc[8 * q + 7], h.w, l.w, Ri);
+            }
+          };
+          for (int j = 1 + js; j <= M - 1; j += js_count) {
+            bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
+            if (in) node(j, 1.0f);
+          }
+          // trapezoid end weights, as below
+          int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+#pragma unroll
+          for (int r2 = 0; r2 < 2; ++r2) {
+            int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
+            if (lo >= hi) continue;
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+              int j = side ? hi : lo;
+              if (((j - 1) % js_count) == js) node(j, -0.5f);
+            }
+          }
+          const double sc = S.Vscale[n];
+#pragma unroll
+          for (int q = 0; q < 12; ++q) Sx[q] = cmk(df_val(sacc[2 * q]) * sc, df_val(sacc[2 * q + 1]) * sc);
         } else {
           for (int j = 1 + js; j <= M - 1; j += js_count) {
             bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
@@ -1343,6 +1391,12 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->V = S.d_V;
   o->mom = S.d_mom;
   o->momf = S.d_momf;
+  o->Vh = S.d_Vh;
+  o->Vl = S.d_Vl;
+  o->Vscale = S.d_Vscale;
+  o->pph = S.d_pph;
+  o->ppl = S.d_ppl;
+  o->df_sums = (c->precision != ALPS_PREC_FP64 && S.d_Vh) ? 1 : 0;
   o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
   o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
   // the series is used only where it is cheaper than the node sum

@@ -481,6 +481,40 @@ __global__ void k_dgemm(int Mr, int Nc, int K, const double* __restrict__ A, con
 
 // V[((n*(M-1)) + (j-1))*12 + 2*e + g] = 2 * c_e(j) * A[F(e)][n][g][j],
 // entries e = xx, yy, zz, xy, xz, yz; c = 1, 1, ppar^2, 1, ppar, ppar.
+// V of order n (block n) as float pairs scaled by 2^-e, e the exponent of
+// max |V[n]|: x 2^-e = hi + lo, hi = float(x 2^-e), lo = float(x 2^-e - hi)
+__global__ void k_split_df(const double* __restrict__ V, int M, double* scale, float* Vh, float* Vl) {
+  __shared__ double red[256];
+  const size_t len = (size_t)(M - 1) * 12;
+  const double* v = V + (size_t)blockIdx.x * len;
+  double mx = 0.0;
+  for (size_t t = threadIdx.x; t < len; t += blockDim.x) mx = fmax(mx, fabs(v[t]));
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  const int e = (red[0] > 0.0) ? ilogb(red[0]) : 0;
+  const double down = ldexp(1.0, -e);
+  if (threadIdx.x == 0) scale[blockIdx.x] = ldexp(1.0, e);
+  for (size_t t = threadIdx.x; t < len; t += blockDim.x) {
+    const double x = v[t] * down;
+    const float h = __double2float_rn(x);
+    Vh[(size_t)blockIdx.x * len + t] = h;
+    Vl[(size_t)blockIdx.x * len + t] = __double2float_rn(x - (double)h);
+  }
+}
+
+// ppar as float pairs
+__global__ void k_split_pp(const double* __restrict__ ppar, int M, float* ph, float* pl) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j > M) return;
+  const float h = __double2float_rn(ppar[j]);
+  ph[j] = h;
+  pl[j] = __double2float_rn(ppar[j] - (double)h);
+}
+
 __global__ void k_fold_reduced(const double* __restrict__ A, const double* __restrict__ ppar, int M, int nmax,
                                double* V) {
   int j = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -866,6 +900,18 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);
   ALPS_CUDA_TRY(cudaGetLastError());
   k_fold_reduced<<<dim3((M - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_A, S.d_ppar, M, nmax, S.d_V);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  const size_t nvf = (size_t)(nmax + 1) * (M - 1) * 12;
+  if ((rc = ensure(S.d_Vh, S.Vf_cap, 2 * nvf))) return rc;  // hi, then lo
+  S.d_Vl = S.d_Vh + nvf;
+  if ((rc = ensure(S.d_Vscale, S.Vs_cap, (size_t)(nmax + 1)))) return rc;
+  k_split_df<<<nmax + 1, 256, 0, st>>>(S.d_V, M, S.d_Vscale, S.d_Vh, S.d_Vl);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  if (!S.d_pph) {
+    ALPS_CUDA_TRY(cudaMalloc(&S.d_pph, (M + 1) * sizeof(float)));
+    ALPS_CUDA_TRY(cudaMalloc(&S.d_ppl, (M + 1) * sizeof(float)));
+  }
+  k_split_pp<<<(M + 1 + 127) / 128, 128, 0, st>>>(S.d_ppar, M, S.d_pph, S.d_ppl);
   ALPS_CUDA_TRY(cudaGetLastError());
   double pcen = 0.5 * (S.ppar[1] + S.ppar[M - 1]), prad = 0.5 * (S.ppar[M - 1] - S.ppar[1]);
   if (!S.d_X) ALPS_CUDA_TRY(cudaMalloc(&S.d_X, (size_t)(M - 1) * ALPS_KFAR * sizeof(double)));
