@@ -78,6 +78,8 @@ struct SpecDev {
   const double* V;
   const double* mom;  // Laurent moments [(nmax+1)][ALPS_KFAR][12]
   const float* momf;  // the same moments rounded to FP32 (for the series tails)
+  const float* momh;  // the moments as float pairs scaled like Vh/Vl (momh + moml)
+  const float* moml;
   // V as pairs of floats (hi + lo, ~48 bits) scaled by 2^-e per order, Vscale
   // = 2^e, and ppar as float pairs: the fast path's node sums run on the
   // FP32 pipes in double-float arithmetic
@@ -147,7 +149,8 @@ struct SpeciesHost {
   double* d_G = nullptr;                  // contraction RHS [2][N-1][M-1]
   double* d_X = nullptr;                  // x_j^k, x_j = (ppar_j - pcen)/prad
   double* d_mom = nullptr;                // Laurent moments
-  float* d_momf = nullptr;                // the same in FP32
+  float* d_momf = nullptr;                // the same in FP32; the pairs below share its allocation
+  float *d_momh = nullptr, *d_moml = nullptr;  // the moments as float pairs (scale Vscale per order)
   float *d_Vh = nullptr, *d_Vl = nullptr;  // V as float pairs (one allocation, lo after hi)
   size_t Vf_cap = 0;
   double* d_Vscale = nullptr;             // per-order scale of the pairs

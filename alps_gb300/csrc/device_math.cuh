@@ -165,6 +165,21 @@ __device__ __forceinline__ dflt df_rcp(dflt a) {
   const dflt e = df_add({1.0f, 0.0f}, df_neg(df_mul(a, {r0, 0.0f})));
   return df_add({r0, 0.0f}, df_mul({r0, 0.0f}, e));
 }
+// 1/a from the FP32 approximate reciprocal (within 1 ulp) and one Newton
+// step in double-float: relative error about 2^-46.  a must be a normal
+// float pair (no zero, no FP32 underflow).
+__device__ __forceinline__ dflt df_rcp_approx(dflt a) {
+  float r0;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(a.h));
+  const dflt e = df_add({1.0f, 0.0f}, df_neg(df_mul(a, {r0, 0.0f})));
+  return df_add({r0, 0.0f}, df_mul({r0, 0.0f}, e));
+}
+// acc += c, the low part unnormalised until the end
+__device__ __forceinline__ void df_acc(dflt& acc, dflt c) {
+  const dflt s = df_two_sum(acc.h, c.h);
+  acc.h = s.h;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, c.l));
+}
 // acc += (vh + vl)(rh + rl), the low parts unnormalised until the end
 __device__ __forceinline__ void df_mac(dflt& acc, float vh, float vl, dflt r) {
   const float p = __fmul_rn(vh, r.h);

@@ -46,7 +46,7 @@ struct __align__(16) DispArgs {
 struct DispShape {
   int nchunk;    // order chunks per species
   int csize;     // orders per chunk
-  int ipw;       // resonant items per warp of k_resonant (1..32)
+  int ipw;       // resonant-item slots per warp of k_resonant (1..256)
 };
 
 namespace {
@@ -92,6 +92,24 @@ __device__ __forceinline__ void classify_body(const DispArgs& a, const double2* 
 // species, order chunks).  Each thread accumulates the six chi entries of its
 // omega over the orders of its chunk (and the n = -1,0,1 parts for chi_low).
 // ---------------------------------------------------------------------------
+// The double-float node sum keeps |A - k_par p_j|^2 + D^2 a normal float:
+// its smallest value (at a summed range's end, or zero if the pole lies
+// inside a summed range) at least 1e-30, its largest at most 1e30.
+__device__ __forceinline__ bool df_node_range(const SpecDev& S, const ResGeom& g, double Ar, double kpar,
+                                              double Di) {
+  double lo = 1e300, hi = 0.0;
+  const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+#pragma unroll
+  for (int r = 0; r < 2; ++r) {
+    const int j0 = max(1, ends[2 * r]), j1 = min(S.M - 1, ends[2 * r + 1]);
+    if (j0 > j1) continue;
+    const double d0 = Ar - kpar * S.ppar[j0], d1 = Ar - kpar * S.ppar[j1];
+    lo = ((d0 < 0.0) != (d1 < 0.0)) ? 0.0 : fmin(lo, fmin(fabs(d0), fabs(d1)));
+    hi = fmax(hi, fmax(fabs(d0), fabs(d1)));
+  }
+  return Di * Di + lo * lo >= 1e-30 && Di * Di + hi * hi <= 1e30;
+}
+
 template <bool LOW>
 __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
                                           int n_om, int js_count, double2* part, double2* low, int tile, int s,
@@ -162,6 +180,40 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
           }
           for (int q = js_count; q > 1; q >>= 1) step = cmul(step, step);
           int k = js;
+          if (S.df_sums) {
+            // fast path: the leading terms in double-float arithmetic on the
+            // FP32 pipes (moments as pairs scaled by 2^-e per order)
+            const float* __restrict__ mh = S.momh + (size_t)n * ALPS_KFAR * 12;
+            const float* __restrict__ ml = S.moml + (size_t)n * ALPS_KFAR * 12;
+            dflt tx = df_of(tk.x), ty = df_of(tk.y);
+            const dflt sx = df_of(step.x), sy = df_of(step.y);
+            dflt sacc[24];
+#pragma unroll
+            for (int q = 0; q < 24; ++q) sacc[q] = {0.0f, 0.0f};
+            for (; k < K32; k += js_count) {
+              const float4* h4 = reinterpret_cast<const float4*>(mh + (size_t)k * 12);
+              const float4* l4 = reinterpret_cast<const float4*>(ml + (size_t)k * 12);
+#pragma unroll
+              for (int q = 0; q < 3; ++q) {
+                const float4 h = __ldg(h4 + q), l = __ldg(l4 + q);
+                df_mac(sacc[8 * q + 0], h.x, l.x, tx);
+                df_mac(sacc[8 * q + 1], h.x, l.x, ty);
+                df_mac(sacc[8 * q + 2], h.y, l.y, tx);
+                df_mac(sacc[8 * q + 3], h.y, l.y, ty);
+                df_mac(sacc[8 * q + 4], h.z, l.z, tx);
+                df_mac(sacc[8 * q + 5], h.z, l.z, ty);
+                df_mac(sacc[8 * q + 6], h.w, l.w, tx);
+                df_mac(sacc[8 * q + 7], h.w, l.w, ty);
+              }
+              const dflt nx = df_add(df_mul(tx, sx), df_neg(df_mul(ty, sy)));
+              ty = df_add(df_mul(tx, sy), df_mul(ty, sx));
+              tx = nx;
+            }
+            const double sc = S.Vscale[n];
+#pragma unroll
+            for (int q = 0; q < 12; ++q) Sx[q] = cmk(df_val(sacc[2 * q]) * sc, df_val(sacc[2 * q + 1]) * sc);
+            tk = cmk(df_val(tx), df_val(ty));
+          }
           for (; k < K32; k += js_count) {
             const double2* m2 = reinterpret_cast<const double2*>(mom + (size_t)k * 12);
 #pragma unroll
@@ -207,9 +259,9 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
           double2 f = cscale(inv, a.sys.ikpar);
 #pragma unroll
           for (int q = 0; q < 12; ++q) Sx[q] = cmul(Sx[q], f);
-        } else if (S.df_sums) {
+        } else if (S.df_sums && df_node_range(S, g, Ar, kpar, Di)) {
           // fast path: the node sum in double-float arithmetic on the FP32
-          // pipes (about 48 bits; V in pairs scaled by 2^-e per order)
+          // pipes (about 46 bits; V in pairs scaled by 2^-e per order)
           const float* __restrict__ Vh = S.Vh + (size_t)n * (M - 1) * 12;
           const float* __restrict__ Vl = S.Vl + (size_t)n * (M - 1) * 12;
           const dflt Ad = df_of(Ar), kd = df_of(kpar), Dd = df_of(Di);
@@ -219,7 +271,7 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
           for (int q = 0; q < 24; ++q) sacc[q] = {0.0f, 0.0f};
           auto node = [&](int j, float wgt) {
             const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
-            const dflt r = df_rcp(df_add(df_mul(dr, dr), D2));
+            const dflt r = df_rcp_approx(df_add(df_mul(dr, dr), D2));
             const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
             const float4* vh4 = reinterpret_cast<const float4*>(Vh + (size_t)(j - 1) * 12);
             const float4* vl4 = reinterpret_cast<const float4*>(Vl + (size_t)(j - 1) * 12);
@@ -446,6 +498,7 @@ struct __align__(16) ResItem {
   int lower, upper;   // principal-value window
   int nn, work;       // signed order; bit 0 principal value, bit 1 Landau rows, lf << 2
   int w, s;           // omega, species
+  long long slot;     // the item's slot (its output row)
   double2 pref[6];    // T-tensor prefactors
 };
 
@@ -457,19 +510,22 @@ __host__ __device__ inline size_t res_region(int N) {
 }
 
 // per-warp shared memory in double2: the window (h, s), the records / rows
-// region, the warp's 32 items and 6 values handed to lanes 0-5
+// region, the warp's 32 items, 6 values handed to lanes 0-5 and the queue of
+// occupied slots (64 ints)
 __host__ __device__ inline size_t res_warp_smem(int N, int W) {
-  return (size_t)W * 12 + res_region(N) + 32 * (sizeof(ResItem) / sizeof(double2)) + 6;
+  return (size_t)W * 12 + res_region(N) + 32 * (sizeof(ResItem) / sizeof(double2)) + 6 + 16;
 }
 
-// Items per warp: a warp does the per-item scalar work one item per lane,
-// then the vector work of its items one after another.  Large batches take
-// 32 per warp; small ones spread their items over more warps (a single
+// Slots per warp: a warp gathers the occupied slots of its range into
+// batches of up to 32 items, does the per-item scalar work one item per
+// lane, then the vector work of the batch's items one after another.  Large
+// batches take up to 256 slots per warp (about 7 waves of resident warps on
+// the map lattice); small ones spread their items over more warps (a single
 // omega's few resonant orders run side by side, as latency wants).
 inline int res_items_per_warp(long nslots) {
   const long warps_wanted = 152L * 12;  // SMs x resident warps of k_resonant
   long ipw = nslots / warps_wanted;
-  return (int)(ipw < 1 ? 1 : (ipw > 32 ? 32 : ipw));
+  return (int)(ipw < 1 ? 1 : (ipw > 256 ? 256 : ipw));
 }
 
 __device__ inline double2 crcp(double2 z) {
@@ -493,17 +549,45 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
   double2* fmr = fpr + (N + 1);                            // f(i, p_res - dppar)
   ResItem* ri = reinterpret_cast<ResItem*>(pvv + res_region(N));
   double2* tb = reinterpret_cast<double2*>(ri + 32);      // values handed to lanes 0-5
+  int* queue = reinterpret_cast<int*>(tb + 6);            // occupied slots, offsets from slot0
   const long total = (long)n_om * S_ * a.rcap;
-  const long item0 = (block * RES_WARPS + warp) * sh.ipw;
-  const long item = item0 + lane;
+  // this warp's slots: slot0 .. slot0 + sh.ipw - 1.  Most slots of a large
+  // batch are empty (an (omega, species) fills count of its rcap slots), so
+  // the occupied ones are gathered, in slot order, into batches of up to 32
+  // items; each batch runs the per-item phase one item per lane and then
+  // the per-warp phase.  Which batch or lane an item lands on does not
+  // change its result.
+  const long slot0 = (block * RES_WARPS + warp) * (long)sh.ipw;
+  if (slot0 >= total) return;
+  const unsigned lt = (1u << lane) - 1u;
+  int qn = 0;
+  for (int c0 = 0; c0 < sh.ipw; c0 += 32) {
+    {
+      const long sl = slot0 + c0 + lane;
+      bool occ = false;
+      if (c0 + lane < sh.ipw && sl < total) {
+        const int r = (int)(sl % a.rcap);
+        const int s = (int)((sl / a.rcap) % S_);
+        const int w = (int)(sl / ((long)a.rcap * S_));
+        occ = r < count[(size_t)w * S_ + s];
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, occ);
+      if (occ) queue[qn + __popc(m & lt)] = c0 + lane;
+      qn += __popc(m);
+      __syncwarp();
+    }
+    const bool last = c0 + 32 >= sh.ipw;
+    while (qn >= 32 || (last && qn > 0)) {
+  const int nb = qn < 32 ? qn : 32;
+  const long item = (lane < nb) ? slot0 + queue[lane] : total;
 
   // ---- one item per thread: geometry, prefactors, factorised Landau rows ----
   int work = 0;
-  if (lane < sh.ipw && item < total) {
+  if (item < total) {
     const int r = (int)(item % a.rcap);
     const int s = (int)((item / a.rcap) % S_);
     const int w = (int)(item / ((long)a.rcap * S_));
-    if (r < count[(size_t)w * S_ + s]) {
+    {
       const SpecDev& S = a.sp[s];
       const int nn = slot_nn[((size_t)w * S_ + s) * a.rcap + r];
       const int n = nn < 0 ? -nn : nn;
@@ -577,6 +661,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       it.work = work | (lf << 2);
       it.w = w;
       it.s = s;
+      it.slot = item;
       for (int e = 0; e < 6; ++e) it.pref[e] = pref[e];
     }
   }
@@ -596,7 +681,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
     const int M = S.M;
     const double kpar = a.sys.kpar, kappa = kpar / S.ms;
     const double* Vn = S.V + (size_t)n * (M - 1) * 12;
-    double2* out = items + (item0 + il) * 6;
+    double2* out = items + it.slot * 6;
 
     // ---- principal value window (case 3) ----
     if (wk & 1) {
@@ -785,7 +870,76 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
         nruns += nr;
         nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
       };
-      if (sym) {
+      // Fast path: the sample sums in double-float arithmetic on the FP32
+      // pipes (about 46 bits; the pieces are still found from the FP64
+      // sample points).  Used where every pair stays a normal float: spacing,
+      // window and |p_im| within 1e-12 .. 1e12.
+      auto inr = [](double x) { return x >= 1e-12 && x <= 1e12; };
+      const bool dfsym = S.df_sums && inr(smdelta) && inr(capDelta) && inr(fabs(pim));
+      const bool dftiny = S.df_sums && inr(capDelta) && inr(corr * smdelta) && fabs(pim) <= 1e12;
+      struct PvSlotF {
+        int jd, jc;
+        dflt Adx, Ady, Bdx, Bdy, Acx, Acy, Bcx, Bcy;
+      };
+      const dflt z0 = {0.0f, 0.0f};
+      auto putf = [&](PvSlotF& q, int j, dflt dx, dflt cx, dflt cy, int dir) {
+        if (j != q.jc) {
+          if (q.jc >= 0) {
+            if (q.jd >= 0 || (dir > 0 ? j < q.jc : j > q.jc)) bad = true;
+            q.jd = q.jc;
+            q.Adx = q.Acx;
+            q.Ady = q.Acy;
+            q.Bdx = q.Bcx;
+            q.Bdy = q.Bcy;
+          }
+          q.jc = j;
+          q.Acx = q.Acy = q.Bcx = q.Bcy = z0;
+        }
+        df_acc(q.Acx, cx);
+        df_acc(q.Acy, cy);
+        df_mac(q.Bcx, cx.h, cx.l, dx);
+        df_mac(q.Bcy, cy.h, cy.l, dx);
+      };
+      auto to64 = [&](const PvSlotF& q) {
+        PvSlot r;
+        r.jd = q.jd;
+        r.jc = q.jc;
+        r.Ad = cmk(df_val(q.Adx), df_val(q.Ady));
+        r.Bd = cmk(df_val(q.Bdx), df_val(q.Bdy));
+        r.Ac = cmk(df_val(q.Acx), df_val(q.Acy));
+        r.Bc = cmk(df_val(q.Bcx), df_val(q.Bcy));
+        return r;
+      };
+      // the sample points as integrate_res writes them (for the FP64 search)
+      auto sym_p = [&](int k) {
+        return (k == 0) ? pr
+                        : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
+      };
+      auto tiny_p = [&](int k) {
+        return (k == 0) ? __dadd_rn(pr, capDelta)
+                        : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
+      };
+      if (sym && dfsym) {
+        const int per = (NP + 31) / 32;
+        const int k0 = lane * per, k1 = min(NP, k0 + per);
+        PvSlotF su{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0}, sd = su;
+        const float u0 = (float)(1.0 + (pr - S.ppar[1]) * S.idppar), du = (float)(smdelta * S.idppar);
+        const dflt smd = df_of(smdelta), capd = df_of(capDelta), pimd = df_of(pim), pim2 = df_of(pim * pim);
+        for (int k = k0; k < k1; ++k) {
+          // K = w (dx, p_im) / (dx^2 + p_im^2), dx = p_k - p_res
+          const dflt dx = (k == a.sys.M_P) ? capd : df_mul(smd, {(float)k, 0.0f});
+          const dflt r = df_scale(df_rcp_approx(df_add(df_mul(dx, dx), pim2)),
+                                  (k == 0 || k == a.sys.M_P) ? 1.0f : 2.0f);
+          const dflt Kx = df_mul(dx, r), Ky = df_mul(pimd, r);
+          const float uu = fmaf((float)k, du, u0), ud = fmaf(-(float)k, du, u0);
+          const int cu = clampj(off_half(uu) ? node_of(uu) : piece_raw(sym_p(k)));
+          const int cd = clampj(off_half(ud) ? node_of(ud) : piece_raw(2.0 * pr - sym_p(k)));
+          putf(su, cu, dx, Kx, Ky, 1);
+          putf(sd, cd, df_neg(dx), Kx, df_neg(Ky), -1);
+        }
+        records(0, to64(su), 1);
+        records(1, to64(sd), -1);
+      } else if (sym) {
         const int per = (NP + 31) / 32;
         const int k0 = lane * per, k1 = min(NP, k0 + per);
         PvSlot su{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)}, sd = su;
@@ -812,19 +966,47 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
           fr += wk * ((d * d) / (d * d + pim * pim));
         }
         for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
-        if (lane == 0) {
-          double2 H1[6], H2[6], H0[6];
-          Hc(pr + dps, H1);
-          Hc(pr - dps, H2);
-          Hc(pr, H0);
+        // entry e on lane e, then T (on lane 0, as the other branches leave it)
+        double2 Te = cmk(0.0, 0.0);
+        if (lane < 6) {
+          const int e = lane;
+          auto Hc1 = [&](double p) {
+            const int jc = piece(p);
+            double2 h, sl;
+            node1(jc, e, h, sl);
+            const double dx = p - S.ppar[jc];
+            return cmk(fma(sl.x, dx, h.x), fma(sl.y, dx, h.y));
+          };
+          const double2 H1 = Hc1(pr + dps), H2 = Hc1(pr - dps), H0 = Hc1(pr);
           double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
-          for (int e = 0; e < 6; ++e) {
-            double2 gp = cscale(csub(H1[e], H2[e]), 1.0 / (2.0 * dps));
-            T[e] = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0[e]));
-          }
+          double2 gp = cscale(csub(H1, H2), 1.0 / (2.0 * dps));
+          Te = cadd(cscale(gp, 2.0 * fr), cmul(cmk(0.0, sgn * 2.0 * ALPS_PI / smdelta), H0));
+        }
+  #pragma unroll
+        for (int e = 0; e < 6; ++e) {
+          const double tx = __shfl_sync(0xffffffffu, Te.x, e), ty = __shfl_sync(0xffffffffu, Te.y, e);
+          if (lane == 0) T[e] = cmk(tx, ty);
         }
       }
-      if (ntiny > 0) {
+      if (ntiny > 0 && dftiny) {
+        const int per = (ntiny + 1 + 31) / 32;
+        const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
+        PvSlotF sq{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0};
+        const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) * S.idppar), dut = (float)(corr * smdelta * S.idppar);
+        const dflt capd = df_of(capDelta), csd = df_of(__dmul_rn(corr, smdelta)), cord = df_of(corr),
+                   pimd = df_of(pim), pim2 = df_of(pim * pim);
+        for (int k = k0; k < k1; ++k) {
+          // K = w corr (dx, p_im) / (dx^2 + p_im^2)
+          const dflt dx = (k == 0) ? capd : df_add(capd, df_mul(csd, {(float)k, 0.0f}));
+          const dflt r = df_scale(df_mul(df_rcp_approx(df_add(df_mul(dx, dx), pim2)), cord),
+                                  (k == 0 || k == ntiny) ? 1.0f : 2.0f);
+          const dflt Kx = df_mul(dx, r), Ky = df_mul(pimd, r);
+          const float ut = fmaf((float)k, dut, ut0);
+          const int ct = clampj(off_half(ut) ? node_of(ut) : piece_raw(tiny_p(k)));
+          putf(sq, ct, dx, Kx, Ky, 1);
+        }
+        records(2, to64(sq), 1);
+      } else if (ntiny > 0) {
         const int per = (ntiny + 1 + 31) / 32;
         const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
         PvSlot sq{-1, -1, cmk(0, 0), cmk(0, 0), cmk(0, 0), cmk(0, 0)};
@@ -1061,6 +1243,15 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       }
     }
     __syncwarp();  // the next item reuses the window and the records
+  }
+      // the items beyond this batch move to the front of the queue
+      const int rest = qn - nb;
+      const int keep = (lane < rest) ? queue[nb + lane] : 0;
+      __syncwarp();
+      if (lane < rest) queue[lane] = keep;
+      __syncwarp();
+      qn = rest;
+    }
   }
 }
 
@@ -1391,6 +1582,8 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->V = S.d_V;
   o->mom = S.d_mom;
   o->momf = S.d_momf;
+  o->momh = S.d_momh;
+  o->moml = S.d_moml;
   o->Vh = S.d_Vh;
   o->Vl = S.d_Vl;
   o->Vscale = S.d_Vscale;

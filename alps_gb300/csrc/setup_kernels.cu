@@ -553,8 +553,10 @@ __global__ void k_powers(const double* __restrict__ ppar, int M, double pcen, do
 // j = 1, M-1 and 1 inside (the reduced vectors carry the interior weight 2).
 // For a pole p far from the grid, sum_j f_j V_j / (p - ppar_j) =
 //   (1/d) sum_k mom_k (prad/d)^k,  d = p - pcen.
+// Also written: momf = mom rounded to FP32, and mom / Vscale[n] as float
+// pairs (momh + moml, the per-order scale of the reduced vectors' pairs).
 __global__ void k_moments(const double* __restrict__ V, const double* __restrict__ X, int M, int nmax,
-                          double* mom, float* momf) {
+                          const double* __restrict__ Vscale, double* mom, float* momf, float* momh, float* moml) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   int total = (nmax + 1) * ALPS_KFAR * 12;
   if (t >= total) return;
@@ -567,6 +569,10 @@ __global__ void k_moments(const double* __restrict__ V, const double* __restrict
   }
   mom[t] = acc;
   momf[t] = (float)acc;
+  const double x = acc * (1.0 / Vscale[n]);  // a power of 2: exact
+  const float h = __double2float_rn(x);
+  momh[t] = h;
+  moml[t] = __double2float_rn(x - (double)h);
 }
 
 // omega-independent factors of Maxwellian continuation terms, per row and
@@ -916,11 +922,15 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   double pcen = 0.5 * (S.ppar[1] + S.ppar[M - 1]), prad = 0.5 * (S.ppar[M - 1] - S.ppar[1]);
   if (!S.d_X) ALPS_CUDA_TRY(cudaMalloc(&S.d_X, (size_t)(M - 1) * ALPS_KFAR * sizeof(double)));
   if ((rc = ensure(S.d_mom, S.mom_cap, (size_t)(nmax + 1) * ALPS_KFAR * 12))) return rc;
-  if ((rc = ensure(S.d_momf, S.momf_cap, (size_t)(nmax + 1) * ALPS_KFAR * 12))) return rc;
+  const size_t nmo = (size_t)(nmax + 1) * ALPS_KFAR * 12;
+  if ((rc = ensure(S.d_momf, S.momf_cap, 3 * nmo))) return rc;  // momf, then the pairs' hi and lo
+  S.d_momh = S.d_momf + nmo;
+  S.d_moml = S.d_momf + 2 * nmo;
   k_powers<<<(M - 1 + 127) / 128, 128, 0, st>>>(S.d_ppar, M, pcen, prad, S.d_X);
   ALPS_CUDA_TRY(cudaGetLastError());
   int tot = (nmax + 1) * ALPS_KFAR * 12;
-  k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_mom, S.d_momf);
+  k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_Vscale, S.d_mom, S.d_momf, S.d_momh,
+                                               S.d_moml);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -109,6 +109,30 @@ def fp64_peak_tflops(torch):
     return 2.0 * n ** 3 / best / 1e12
 
 
+def fp32_peak_tflops(torch):
+    """Measured FP32 (FFMA) throughput of a cuBLAS SGEMM with TF32 off (burst)."""
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        n = 8192
+        a = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        b = torch.randn(n, n, dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e9
+        for _ in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1) / 1e3)
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return 2.0 * n ** 3 / best / 1e12
+
+
 def pole_sum_flops(nmax, npar):
     """Algorithmic FP64 flops of the non-resonant pole sums per evaluation:
     150 per (order n >= 0, p_par node) covering +n and -n (2 complex
@@ -124,20 +148,32 @@ def pole_sum_flops_issued(nmax, npar):
     return sum(61.0 * (2 * n + 1) * (npar - 1) for n in nmax)
 
 
+# FP32-pipe flops (FMA = 2) of one double-float node of the fast path's pole
+# sums, counted from the kernel's code (device_math.cuh, disp_kernels.cu):
+# the pole distance d = A - k_par p_j (19), |d|^2 + D^2 (19), its reciprocal
+# (rcp + one double-float Newton step, 39), the two weights (22) and 24
+# double-float multiply-accumulates of the 12 reduced vectors against them
+# (15 each: product with its error term, two-sum into the accumulator)
+DF_NODE_FLOPS = 19 + 19 + 39 + 22 + 24 * 15
+# one double-float Laurent term: 24 multiply-accumulates of the 12 moments
+# against the complex power (15 each) and the power update (4 products, 2 sums)
+DF_TERM_FLOPS = 24 * 15 + 4 * 9 + 2 * 10
+
+
 def pole_sum_work_fast(system, species, kpar, oms, nmax):
-    """Algorithmic work of the fast path's pole sums over a lattice, with the
-    kernel's own decisions per (omega, signed order): a pole far from the grid
-    (not resonant, rho = prad/|p_res - pcen| with rho^2 < 1/2) takes K Laurent
+    """Work of the fast path's pole sums over a lattice, with the kernel's own
+    decisions per (omega, signed order): a pole far from the grid (not
+    resonant, rho = prad/|p_res - pcen| with rho^2 < 1/2) takes K Laurent
     terms, rho^K <= 2^-53 (1 - rho), of which those from K32 on
-    (rho^K32 <= 2^-33 (1 - rho)) run in FP32; any other order sums its nodes
-    (a resonant one outside the principal-value window).  FP64 flops: 75 per
-    (signed order, node), the SURVEY convention's 150 per (n >= 0, node) split
-    over +-n, and 54 per series term (12 complex x real MACs and the power
-    update).  Returns (fp64 flops, fp32 flops)."""
+    (rho^K32 <= 2^-33 (1 - rho)) run in FP32 and the ones before in
+    double-float; any other order sums its nodes (a resonant one outside the
+    principal-value window) in double-float.  Returns counts: nodes (signed
+    order x node pairs summed), series terms in double-float and in FP32, and
+    resonant items (omega, species, signed order)."""
     ns, npar, M_I = system.nspec, system.npar, system.positions_principal
     M = npar
     kfar = min(128, int(0.8 * (M - 1)))
-    f64 = f32 = 0.0
+    out = {"nodes": 0.0, "series_df": 0.0, "series_fp32": 0.0, "items": 0.0}
     for si in range(ns):
         spc, pl = species[si][0], np.asarray(species[si][2])
         ppar = pl.reshape(-1, M + 1)[0]
@@ -154,11 +190,12 @@ def pole_sum_work_fast(system, species, kpar, oms, nmax):
             K = np.where(far, np.ceil((36.7368005696771 - np.log1p(-rho)) / -np.log(rho)), kfar + 1)
             K32 = np.where(far, np.ceil((22.8738569584782 - np.log1p(-rho)) / -np.log(rho)), kfar + 1)
             lau = K <= kfar
-            f64 += 54.0 * np.minimum(K32, K)[lau].sum()
-            f32 += 54.0 * np.maximum(K - K32, 0)[lau].sum()
+            out["series_df"] += np.minimum(K32, K)[lau].sum()
+            out["series_fp32"] += np.maximum(K - K32, 0)[lau].sum()
             nodes = np.where(res, (M - 1) - (2 * M_I + 2), M - 1)
-            f64 += 75.0 * nodes[~lau].sum()
-    return f64, f32
+            out["nodes"] += nodes[~lau].sum()
+            out["items"] += res.sum()
+    return {k: float(v) for k, v in out.items()}
 
 
 def cpu_sample(P, oms, budget_s, nthreads):
@@ -328,7 +365,7 @@ def main():
     def step():
         G.disp_batch_device(n, om_dev.data_ptr(), D_dev.data_ptr(), sp)
 
-    peak64 = None
+    peak64 = peak32 = None
 
     def timed(precision):
         """warmup + K timed steps of one evaluation mode; returns seconds,
@@ -363,6 +400,7 @@ def main():
     # plain FP64 path (node sums everywhere): the baseline of the fast path
     t_plain, prof_plain, D_plain = timed("fp64")
     peak64 = fp64_peak_tflops(torch)
+    peak32 = fp32_peak_tflops(torch)
     clocks = Clocks(local)
     t, (prof_ms, nb), D_fast = timed("mixed")
     clk = clocks.stop()
@@ -372,28 +410,47 @@ def main():
     st = G.stats()
     rel = np.abs(D_fast - D_plain) / np.maximum(np.abs(D_plain), 1e-300)
 
-    # roofline of the dominant kernel of the timed (fast) path, the pole
-    # sums, on the FP64 pipe: its algorithmic work on this lattice
+    # roofline of the dominant kernel of the timed (fast) path, from the live
+    # CUDA-event split, with both main kernels' figures beside it
     names = ["classify", "pole_sums", "resonant", "finalize"]
     pm_plain, nb_plain = prof_plain
-    fast_pole_ms = prof_ms[1] / max(nb, 1)
-    f64, f32 = pole_sum_work_fast(system, species, kpar, oms, nmax)
-    achieved = f64 / (fast_pole_ms / 1e3) / 1e12
-    # the same kernel on the plain path: every order sums its nodes
+    per_fast = [x / max(nb, 1) for x in prof_ms]
+    fast_pole_ms, res_ms = per_fast[1], per_fast[2]
+    work = pole_sum_work_fast(system, species, kpar, oms, nmax)
+    # pole sums: double-float node sums and series terms, FP32 series tails
+    # (54 flops per term), all on the FP32 pipes
+    f32 = work["nodes"] * DF_NODE_FLOPS + work["series_df"] * DF_TERM_FLOPS + work["series_fp32"] * 54.0
+    pole = {"kernel": "k_pole_sums_multi<false> (fast path)", "bound": "fp32", "kernel_ms": fast_pole_ms,
+            "achieved": f32 / (fast_pole_ms / 1e3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
+            "frac": f32 / (fast_pole_ms / 1e3) / 1e12 / peak32, "fp32_flop_per_step": f32,
+            "double_float_nodes_per_step": work["nodes"], "df_node_flops": DF_NODE_FLOPS,
+            "series_terms_df": work["series_df"], "df_term_flops": DF_TERM_FLOPS,
+            "series_terms_fp32": work["series_fp32"]}
+    # resonant items: the SURVEY's algorithmic count per item, 24 M_P flops of
+    # principal-value sums and 60 (N_perp + 1) of Landau rows, FP64
+    f_res = work["items"] * (24.0 * system.n_resonance_interval + 60.0 * (system.nperp + 1))
+    res = {"kernel": "k_resonant_multi (fast path)", "bound": "fp64", "kernel_ms": res_ms,
+           "achieved": f_res / (res_ms / 1e3) / 1e12, "peak": peak64, "unit": "TFLOP/s",
+           "frac": f_res / (res_ms / 1e3) / 1e12 / peak64, "items_per_step": work["items"],
+           "fp64_flop_per_step": f_res}
+    dom = pole if fast_pole_ms >= res_ms else res
+    # the plain path's pole sums: every order sums its nodes in FP64
     pole_ms = pm_plain[1] / max(nb_plain, 1)
     plain_achieved = pole_sum_flops(nmax, s.npar) * n / (pole_ms / 1e3) / 1e12
     plain_issued = pole_sum_flops_issued(nmax, s.npar) * n / (pole_ms / 1e3) / 1e12
-    roofline = {"bound": "fp64", "achieved": achieved, "peak": peak64, "unit": "TFLOP/s",
-                "frac": achieved / peak64, "traffic": None,
-                "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (burst); MEASURED_PEAKS.json has no FP64 figure",
-                "kernel": "k_pole_sums_multi<false> (fast path)", "kernel_ms": fast_pole_ms,
-                "kernel_share": prof_ms[1] / max(sum(prof_ms), 1e-30),
-                "algorithmic_fp64_flop_per_step": f64, "fp32_series_flop_per_step": f32,
+    roofline = {"bound": dom["bound"], "achieved": dom["achieved"], "peak": dom["peak"], "unit": "TFLOP/s",
+                "frac": dom["frac"], "traffic": None,
+                "peak_source": ("cuBLAS DGEMM 4096^3 (fp64) and SGEMM 8192^3 with TF32 off (fp32), measured in "
+                                "this run (burst); MEASURED_PEAKS.json has neither figure"),
+                "kernel": dom["kernel"], "kernel_ms": dom["kernel_ms"],
+                "kernel_share": dom["kernel_ms"] / max(sum(per_fast), 1e-30),
+                "fp64_peak": peak64, "fp32_peak": peak32,
+                "kernels": {"pole_sums": pole, "resonant": res},
                 "plain_path": {"kernel": "k_pole_sums_multi<false> (plain FP64 path)", "kernel_ms": pole_ms,
                                "achieved": plain_achieved, "frac": plain_achieved / peak64,
                                "achieved_issued": plain_issued, "frac_issued": plain_issued / peak64},
                 "per_kernel_ms_plain": dict(zip(names, [x / max(nb_plain, 1) for x in pm_plain])),
-                "per_kernel_ms_fast": dict(zip(names, [x / max(nb, 1) for x in prof_ms]))}
+                "per_kernel_ms_fast": dict(zip(names, per_fast))}
 
     # end to end through the C-ABI with host buffers (copies included)
     Dh = G.disp_batch(oms)
