@@ -533,6 +533,347 @@ __device__ inline double2 crcp(double2 z) {
   return cmk(z.x * r, -z.y * r);
 }
 
+// ---------------------------------------------------------------------------
+// Fast path of one item's principal-value window: the same sums as the FP64
+// code in resonant_body (sample points, pieces, per-piece sums A and C, the
+// merge in lane order, h A + s B per (run, entry), the Tlim branch), all in
+// double-float arithmetic on the FP32 pipes, on the reduced vectors' float
+// pairs (scaled by 2^-e for order n; the result is rescaled at the end).
+// The pieces are still chosen from the FP64 sample points wherever the FP32
+// estimate is within 1e-3 of a half-way point.  Returns false, with nothing
+// written to T, when a range would leave the normal floats or the merge does
+// not apply (the caller then runs the FP64 code).  T ends on lane 0.
+// ---------------------------------------------------------------------------
+struct PvSlotF {
+  int jd, jc;  // finished piece (-1: none), current piece
+  dflt Adx, Ady, Bdx, Bdy, Acx, Acy, Bcx, Bcy;
+};
+
+__device__ __forceinline__ float4 f4_of(dflt x, dflt y) { return make_float4(x.h, x.l, y.h, y.l); }
+__device__ __forceinline__ dflt f4x(float4 v) { return {v.x, v.y}; }
+__device__ __forceinline__ dflt f4y(float4 v) { return {v.z, v.w}; }
+// (ax + i ay)(bx + i by), real and imaginary parts
+__device__ __forceinline__ void df_cmul(dflt ax, dflt ay, dflt bx, dflt by, dflt& rx, dflt& ry) {
+  rx = df_add(df_mul(ax, bx), df_neg(df_mul(ay, by)));
+  ry = df_add(df_mul(ax, by), df_mul(ay, bx));
+}
+
+__device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const ResItem& it, double2 o, int n,
+                                     int W, float4* win, double2* pvv, double2* T) {
+  const int lane = threadIdx.x & 31;
+  const int M = S.M;
+  const double kappa = a.sys.kpar / S.ms;
+  const double pr = it.pr, pim = it.pim;
+  const double capDelta = pr - S.ppar[it.lower];
+  const double smdelta = capDelta / (1.0 * a.sys.M_P);
+  const bool sym = fabs(pim) > a.sys.Tlim;
+  const int NP = a.sys.M_P + 1;
+  const int ntiny = (int)((S.ppar[it.upper] - pr - capDelta) / smdelta);
+  const double corr = (ntiny > 0) ? ((S.ppar[it.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
+  auto inr = [](double x) { return x >= 1e-12 && x <= 1e12; };
+  if (!(inr(smdelta) && inr(capDelta) && fabs(pim) <= 1e12 && (!sym || inr(fabs(pim))) &&
+        (ntiny <= 0 || inr(corr * smdelta))))
+    return false;
+  const int jw0 = max(1, it.lower - 2), jw1 = min(M - 1, it.upper + 2);
+  const int nw = jw1 - jw0 + 1;
+  const float* __restrict__ Vh = S.Vh + (size_t)n * (M - 1) * 12;
+  const float* __restrict__ Vl = S.Vl + (size_t)n * (M - 1) * 12;
+  const dflt oxd = df_of(o.x), oyd = df_of(o.y), kad = df_of(kappa), hid = df_of(S.hidpa);
+  // node value h_e(j) = omega V_{e,1}(j) + kappa V_{e,2}(j), scaled
+  auto hnode = [&](int j, int e, dflt& hx, dflt& hy) {
+    const size_t b = (size_t)(j - 1) * 12 + 2 * e;
+    const dflt v1 = {Vh[b], Vl[b]}, v2 = {Vh[b + 1], Vl[b + 1]};
+    hx = df_add(df_mul(oxd, v1), df_mul(kad, v2));
+    hy = df_mul(oyd, v1);
+  };
+  float4* wh = win;           // h at window nodes
+  float4* ws = win + W * 6;   // centred slopes
+  for (int t = lane; t < nw * 6; t += 32) {
+    const int jj = t / 6, e = t % 6;
+    dflt hx, hy;
+    hnode(jw0 + jj, e, hx, hy);
+    wh[jj * 6 + e] = f4_of(hx, hy);
+  }
+  __syncwarp();
+  for (int t = lane; t < nw * 6; t += 32) {
+    const int jj = t / 6, e = t % 6;
+    if (jj >= 1 && jj + 1 < nw) {
+      const float4 u = wh[(jj + 1) * 6 + e], d = wh[(jj - 1) * 6 + e];
+      ws[jj * 6 + e] = f4_of(df_mul(df_add(f4x(u), df_neg(f4x(d))), hid), df_mul(df_add(f4y(u), df_neg(f4y(d))), hid));
+    }
+  }
+  __syncwarp();
+  // node value and slope of entry e at piece jc (window, or from the pairs)
+  auto node1 = [&](int jc, int e, dflt& hx, dflt& hy, dflt& sx, dflt& sy) {
+    if (jc - 1 >= jw0 && jc + 1 <= jw1) {
+      const float4 h = wh[(jc - jw0) * 6 + e], s = ws[(jc - jw0) * 6 + e];
+      hx = f4x(h);
+      hy = f4y(h);
+      sx = f4x(s);
+      sy = f4y(s);
+    } else {
+      dflt ux, uy, dx, dy;
+      hnode(jc, e, hx, hy);
+      hnode(jc + 1, e, ux, uy);
+      hnode(jc - 1, e, dx, dy);
+      sx = df_mul(df_add(ux, df_neg(dx)), hid);
+      sy = df_mul(df_add(uy, df_neg(dy)), hid);
+    }
+  };
+  // pieces, as in resonant_body: the last node in 1..M-1 within half a
+  // spacing of p (funct_g's search), clamped to 2..M-2
+  const double idpa = fabs(S.idppar), half = 0.5 * S.dppar_abs;
+  auto piece_raw = [&](double p) {
+    int jr = 0;
+    double jd = floor((p - S.ppar[0]) * idpa + 0.5);
+    if (jd > -10.0 && jd < (double)M + 10.0) {
+      int j0 = (int)jd;
+      int hi = min(j0 + 2, M - 1), lo = max(j0 - 2, 1);
+      for (int jj = hi; jj >= lo; --jj)
+        if (fabs(S.ppar[jj] - p) <= half) {
+          jr = jj;
+          break;
+        }
+    }
+    return jr;
+  };
+  auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
+  auto off_half = [&](float u) { return fabsf(u - rintf(u)) < 0.499f; };
+  auto node_of = [&](float u) {
+    const int j = (int)rintf(u);
+    return (j >= 1 && j <= M - 1) ? j : 0;
+  };
+  auto sym_p = [&](int k) {
+    return (k == 0) ? pr : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
+  };
+  auto tiny_p = [&](int k) {
+    return (k == 0) ? __dadd_rn(pr, capDelta)
+                    : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
+  };
+  bool bad = false;
+  const dflt z0 = {0.0f, 0.0f};
+  auto putf = [&](PvSlotF& q, int j, dflt dx, dflt cx, dflt cy, int dir) {
+    if (j != q.jc) {
+      if (q.jc >= 0) {
+        if (q.jd >= 0 || (dir > 0 ? j < q.jc : j > q.jc)) bad = true;
+        q.jd = q.jc;
+        q.Adx = q.Acx;
+        q.Ady = q.Acy;
+        q.Bdx = q.Bcx;
+        q.Bdy = q.Bcy;
+      }
+      q.jc = j;
+      q.Acx = q.Acy = q.Bcx = q.Bcy = z0;
+    }
+    df_acc(q.Acx, cx);
+    df_acc(q.Acy, cy);
+    df_mac(q.Bcx, cx.h, cx.l, dx);
+    df_mac(q.Bcy, cy.h, cy.l, dx);
+  };
+  // records: (group, lane, slot) sums A, B as float4 pairs; run tables as in
+  // resonant_body
+  float4* recv = reinterpret_cast<float4*>(pvv);
+  float4* runv = reinterpret_cast<float4*>(pvv + PV_RECV);
+  int* recj = reinterpret_cast<int*>(pvv + PV_RECV + PV_RUNV);
+  int* runL = recj + PV_GROUPS * 64;
+  int* runS = runL + 32;
+  int* runG = runS + 32;
+  int* runJ = runG + 32;
+  int nruns = 0, nl[PV_GROUPS] = {0, 0, 0};
+  const unsigned lt = (1u << lane) - 1u;
+  auto records = [&](int gi, const PvSlotF& q, int dir) {
+    const bool two = q.jd >= 0;
+    const int j0 = two ? q.jd : q.jc, j1 = two ? q.jc : -1;
+    const int rb = (gi * 32 + lane) * 2;
+    recj[rb] = j0;
+    recj[rb + 1] = j1;
+    recv[rb * 2] = two ? f4_of(q.Adx, q.Ady) : f4_of(q.Acx, q.Acy);
+    recv[rb * 2 + 1] = two ? f4_of(q.Bdx, q.Bdy) : f4_of(q.Bcx, q.Bcy);
+    recv[rb * 2 + 2] = two ? f4_of(q.Acx, q.Acy) : f4_of(z0, z0);
+    recv[rb * 2 + 3] = two ? f4_of(q.Bcx, q.Bcy) : f4_of(z0, z0);
+    const int last = (j1 >= 0) ? j1 : j0;
+    const int prev = __shfl_up_sync(0xffffffffu, last, 1);
+    const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
+    const bool st1 = (j1 >= 0);
+    if (j0 >= 0 && lane > 0 && (prev < 0 || (dir > 0 ? j0 < prev : j0 > prev))) bad = true;
+    const unsigned m0 = __ballot_sync(0xffffffffu, st0), m1 = __ballot_sync(0xffffffffu, st1);
+    const int nr = __popc(m0) + __popc(m1);
+    if (nruns + nr <= 32) {
+      const int id0 = nruns + __popc(m0 & lt) + __popc(m1 & lt), id1 = id0 + (st0 ? 1 : 0);
+      if (st0) {
+        runL[id0] = lane;
+        runS[id0] = 0;
+        runG[id0] = gi;
+      }
+      if (st1) {
+        runL[id1] = lane;
+        runS[id1] = 1;
+        runG[id1] = gi;
+      }
+    }
+    nruns += nr;
+    nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
+  };
+  const dflt pimd = df_of(pim), pim2 = df_of(pim * pim);
+  double2 Tl[6];  // the Tlim part (lane 0)
+#pragma unroll
+  for (int e = 0; e < 6; ++e) Tl[e] = cmk(0.0, 0.0);
+  if (sym) {
+    const int per = (NP + 31) / 32;
+    const int k0 = lane * per, k1 = min(NP, k0 + per);
+    PvSlotF su{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0}, sd = su;
+    const float u0 = (float)(1.0 + (pr - S.ppar[1]) * S.idppar), du = (float)(smdelta * S.idppar);
+    const dflt smd = df_of(smdelta), capd = df_of(capDelta);
+    for (int k = k0; k < k1; ++k) {
+      // K = w (dx, p_im) / (dx^2 + p_im^2), dx = p_k - p_res
+      const dflt dx = (k == a.sys.M_P) ? capd : df_mul(smd, {(float)k, 0.0f});
+      const dflt r = df_scale(df_rcp_approx(df_add(df_mul(dx, dx), pim2)), (k == 0 || k == a.sys.M_P) ? 1.0f : 2.0f);
+      const dflt Kx = df_mul(dx, r), Ky = df_mul(pimd, r);
+      const float uu = fmaf((float)k, du, u0), ud = fmaf(-(float)k, du, u0);
+      int cu, cd;
+      if (off_half(uu)) cu = node_of(uu);
+      else cu = piece_raw(sym_p(k));
+      if (off_half(ud)) cd = node_of(ud);
+      else cd = piece_raw(2.0 * pr - sym_p(k));
+      putf(su, clampj(cu), dx, Kx, Ky, 1);
+      putf(sd, clampj(cd), df_neg(dx), Kx, df_neg(Ky), -1);
+    }
+    records(0, su, 1);
+    records(1, sd, -1);
+  } else {
+    // Tlim branch: g' sum_k w_k dx^2/(dx^2 + p_im^2) + sign(p_im) i pi G(p_res)/smdelta
+    const dflt smd = df_of(smdelta), capd = df_of(capDelta);
+    dflt frd = z0;
+    for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
+      const dflt dx = (k == a.sys.M_P) ? capd : df_mul(smd, {(float)k, 0.0f});
+      const dflt d2 = df_mul(dx, dx);
+      const dflt q = df_mul(d2, df_rcp_approx(df_add(d2, pim2)));
+      df_acc(frd, df_scale(q, (k == a.sys.M_P) ? 1.0f : 2.0f));
+    }
+    double fr = df_val(frd);
+    for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
+    double2 Te = cmk(0.0, 0.0);
+    if (lane < 6) {
+      const int e = lane;
+      const double dps = S.dppar;
+      auto Hc1 = [&](double p, dflt& Hx, dflt& Hy) {
+        const float u = (float)(1.0 + (p - S.ppar[1]) * S.idppar);
+        const int jc = clampj(off_half(u) ? node_of(u) : piece_raw(p));
+        dflt hx, hy, sx, sy;
+        node1(jc, e, hx, hy, sx, sy);
+        const dflt dx = df_of(p - S.ppar[jc]);
+        Hx = df_add(hx, df_mul(sx, dx));
+        Hy = df_add(hy, df_mul(sy, dx));
+      };
+      dflt H1x, H1y, H2x, H2y, H0x, H0y;
+      Hc1(pr + dps, H1x, H1y);
+      Hc1(pr - dps, H2x, H2y);
+      Hc1(pr, H0x, H0y);
+      const double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
+      const dflt c1 = df_of(fr / dps), c2 = df_of(sgn * 2.0 * ALPS_PI / smdelta);
+      const dflt tx = df_add(df_mul(df_add(H1x, df_neg(H2x)), c1), df_neg(df_mul(c2, H0y)));
+      const dflt ty = df_add(df_mul(df_add(H1y, df_neg(H2y)), c1), df_mul(c2, H0x));
+      Te = cmk(df_val(tx), df_val(ty));
+    }
+#pragma unroll
+    for (int e = 0; e < 6; ++e) {
+      const double tx = __shfl_sync(0xffffffffu, Te.x, e), ty = __shfl_sync(0xffffffffu, Te.y, e);
+      if (lane == 0) Tl[e] = cmk(tx, ty);
+    }
+  }
+  if (ntiny > 0) {
+    const int per = (ntiny + 1 + 31) / 32;
+    const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
+    PvSlotF sq{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0};
+    const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) * S.idppar), dut = (float)(corr * smdelta * S.idppar);
+    const dflt capd = df_of(capDelta), csd = df_of(__dmul_rn(corr, smdelta)), cord = df_of(corr);
+    for (int k = k0; k < k1; ++k) {
+      // K = w corr (dx, p_im) / (dx^2 + p_im^2)
+      const dflt dx = (k == 0) ? capd : df_add(capd, df_mul(csd, {(float)k, 0.0f}));
+      const dflt r = df_scale(df_mul(df_rcp_approx(df_add(df_mul(dx, dx), pim2)), cord),
+                              (k == 0 || k == ntiny) ? 1.0f : 2.0f);
+      const dflt Kx = df_mul(dx, r), Ky = df_mul(pimd, r);
+      const float ut = fmaf((float)k, dut, ut0);
+      int ct;
+      if (off_half(ut)) ct = node_of(ut);
+      else ct = piece_raw(tiny_p(k));
+      putf(sq, clampj(ct), dx, Kx, Ky, 1);
+    }
+    records(2, sq, 1);
+  }
+  if (__any_sync(0xffffffffu, bad) || nruns > 32) return false;
+  const double sc = S.Vscale[n];
+  double acc = 0.0;
+  if (nruns > 0) {
+    __syncwarp();
+    // run totals in (lane, slot) order
+    if (lane < nruns) {
+      const int L = runL[lane], sl = runS[lane], gi = runG[lane];
+      int Ln = nl[gi], sn = 0;
+      if (lane + 1 < nruns && runG[lane + 1] == gi) {
+        Ln = runL[lane + 1];
+        sn = runS[lane + 1];
+      }
+      const int rb = (gi * 32 + L) * 2 + sl;
+      float4 A4 = recv[rb * 2], B4 = recv[rb * 2 + 1];
+      dflt Ax = f4x(A4), Ay = f4y(A4), Bx = f4x(B4), By = f4y(B4);
+      for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
+        const int r2 = (gi * 32 + L2) * 2;
+        const float4 a2 = recv[r2 * 2], b2 = recv[r2 * 2 + 1];
+        Ax = df_add(Ax, f4x(a2));
+        Ay = df_add(Ay, f4y(a2));
+        Bx = df_add(Bx, f4x(b2));
+        By = df_add(By, f4y(b2));
+      }
+      runJ[lane] = recj[rb];
+      runv[lane * 2] = f4_of(Ax, Ay);
+      runv[lane * 2 + 1] = f4_of(Bx, By);
+    }
+    __syncwarp();
+    // (run, entry) pairs: h A + s B with B = C + (p_res - pp(jc)) A,
+    // mirrored runs with the minus sign
+    float4* contrib = recv;
+    for (int q = lane; q < nruns * 6; q += 32) {
+      const int rho = q / 6, e = q % 6;
+      const int jc = runJ[rho];
+      dflt hx, hy, sx, sy;
+      node1(jc, e, hx, hy, sx, sy);
+      const float4 A4 = runv[rho * 2], C4 = runv[rho * 2 + 1];
+      const dflt Ax = f4x(A4), Ay = f4y(A4);
+      const dflt del = df_of(pr - S.ppar[jc]);
+      const dflt Bx = df_add(f4x(C4), df_mul(Ax, del)), By = df_add(f4y(C4), df_mul(Ay, del));
+      dflt t1x, t1y, t2x, t2y;
+      df_cmul(hx, hy, Ax, Ay, t1x, t1y);
+      df_cmul(sx, sy, Bx, By, t2x, t2y);
+      dflt tx = df_add(t1x, t2x), ty = df_add(t1y, t2y);
+      if (runG[rho] == 1) {
+        tx = df_neg(tx);
+        ty = df_neg(ty);
+      }
+      contrib[q] = f4_of(tx, ty);
+    }
+    __syncwarp();
+    // component c of T: the runs in order
+    if (lane < 12) {
+      const int e = lane >> 1;
+      dflt s = z0;
+      for (int rho = 0; rho < nruns; ++rho) {
+        const float4 c = contrib[rho * 6 + e];
+        s = df_add(s, (lane & 1) ? f4y(c) : f4x(c));
+      }
+      acc = df_val(s);
+    }
+  }
+  // T on lane 0: the Tlim part, the merged sums (both rescaled)
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    const double tx = __shfl_sync(0xffffffffu, acc, 2 * e), ty = __shfl_sync(0xffffffffu, acc, 2 * e + 1);
+    T[e] = cmk((Tl[e].x + tx) * sc, (Tl[e].y + ty) * sc);
+  }
+  __syncwarp();
+  return true;
+}
+
 __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
                                               int n_om, const int* __restrict__ count,
                                               const int* __restrict__ slot_nn, double2* items, long block) {
@@ -690,6 +1031,11 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       const int jw0 = max(1, it.lower - 2), jw1 = min(M - 1, it.upper + 2);
       const int nw = jw1 - jw0 + 1;
       const bool winok = nw <= W;
+      double2 T[6];
+      for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
+      // the fast path's double-float sums; the FP64 code below otherwise
+      const bool fast = S.df_sums && winok && pv_fast(a, S, it, o, n, W, reinterpret_cast<float4*>(wh), pvv, T);
+      if (!fast) {
       if (winok) {
         for (int t = lane; t < nw * 6; t += 32) {
           int jj = t / 6, e = t % 6;
@@ -702,8 +1048,6 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
         }
       }
       __syncwarp();
-      double2 T[6];
-      for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
       // funct_g summed over iperp (src/ALPS_fns.f90:1243-1321): the node whose
       // interpolant serves p is "the last ipar in 1..npar-1 with
       // |pp(ipar) - p| <= dppar/2", clamped to 2..npar-2
@@ -761,14 +1105,6 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       auto node = [&](int jc, double2* h, double2* sl) {
   #pragma unroll
         for (int e = 0; e < 6; ++e) node1(jc, e, h[e], sl[e]);
-      };
-      auto Hc = [&](double p, double2* H) {
-        int jc = piece(p);
-        double2 h[6], sl[6];
-        node(jc, h, sl);
-        double dx = p - S.ppar[jc];
-  #pragma unroll
-        for (int e = 0; e < 6; ++e) H[e] = cmk(fma(sl[e].x, dx, h[e].x), fma(sl[e].y, dx, h[e].y));
       };
       const double capDelta = pr - S.ppar[it.lower];
       const double smdelta = capDelta / (1.0 * a.sys.M_P);
@@ -1136,7 +1472,10 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
             T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
           }
       }
+      }  // FP64 code
       // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
+      const double capDelta = pr - S.ppar[it.lower];
+      const double smdelta = capDelta / (1.0 * a.sys.M_P);
       double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-S.qk * 0.5);
       // lane 0 holds the whole T; lanes 0-5 add entry e
       if (lane == 0)
