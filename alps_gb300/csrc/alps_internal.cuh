@@ -89,6 +89,8 @@ struct SpecDev {
   const float* pph;
   const float* ppl;
   int df_sums;
+  float kaph, kapl;   // k_par / m_s as a float pair
+  float hidh, hidl;   // hidpa as a float pair
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
   int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)

@@ -495,12 +495,63 @@ __host__ __device__ inline int res_win(int M_I) { return (2 * M_I + 8 < RES_WIN)
 // what the warp phase of k_resonant needs of one item
 struct __align__(16) ResItem {
   double pr, pim;     // complex resonance momentum
+  double smdelta;     // principal-value sample spacing (integrate_res's smdelta)
   int lower, upper;   // principal-value window
   int nn, work;       // signed order; bit 0 principal value, bit 1 Landau rows, lf << 2
   int w, s;           // omega, species
   long long slot;     // the item's slot (its output row)
-  double2 pref[6];    // T-tensor prefactors
+  // the fast path's principal-value constants, formed one item per lane:
+  int ntiny, pvdf;    // sample points of the tiny rest; pv_fast applies
+  float u0, du, ut0, dut;  // FP32 piece estimates of the sample points
+  float smd[2], capd[2], pimd[2], pim2[2], csd[2], cord[2];  // double-float pairs
+  double pref[6];     // T-tensor prefactors: imaginary for xy and yz, else real
 };
+// prefactor e of an item as the complex number t_prefactors gives
+__device__ __forceinline__ double2 item_pref(const ResItem& it, int e) {
+  return (e == 3 || e == 5) ? cmk(0.0, it.pref[e]) : cmk(it.pref[e], 0.0);
+}
+
+// The principal-value constants of a resonant item (integrate_res,
+// src/ALPS_fns.f90:1000-1040: capDelta, smdelta, the tiny rest's ntiny and
+// corr), and for the fast path their double-float pairs and FP32 piece
+// estimates, formed in the one-item-per-lane phase so that the warp phase
+// starts from them.  pvdf = 0 leaves the item to the FP64 code: a spacing,
+// window or |p_im| outside 1e-12 .. 1e12 would leave the normal floats.
+__device__ __forceinline__ void pv_constants(const DispArgs& a, const SpecDev& S, const ResGeom& g, ResItem& it) {
+  it.smdelta = 0.0;
+  it.ntiny = 0;
+  it.pvdf = 0;
+  if (g.kind != 3) return;
+  const double pr = g.pr, pim = g.pi;
+  const double capDelta = pr - S.ppar[g.lower];
+  const double smdelta = capDelta / (1.0 * a.sys.M_P);
+  const int ntiny = (int)((S.ppar[g.upper] - pr - capDelta) / smdelta);
+  const double corr = (ntiny > 0) ? ((S.ppar[g.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
+  it.smdelta = smdelta;
+  it.ntiny = ntiny;
+  if (!S.df_sums) return;
+  const bool sym = fabs(pim) > a.sys.Tlim;
+  auto inr = [](double x) { return x >= 1e-12 && x <= 1e12; };
+  if (!(inr(smdelta) && inr(capDelta) && fabs(pim) <= 1e12 && (!sym || inr(fabs(pim))) &&
+        (ntiny <= 0 || inr(corr * smdelta))))
+    return;
+  it.pvdf = 1;
+  it.u0 = (float)(1.0 + (pr - S.ppar[1]) * S.idppar);
+  it.du = (float)(smdelta * S.idppar);
+  it.ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) * S.idppar);
+  it.dut = (float)(corr * smdelta * S.idppar);
+  auto put2 = [](float* d, double x) {
+    const dflt v = df_of(x);
+    d[0] = v.h;
+    d[1] = v.l;
+  };
+  put2(it.smd, smdelta);
+  put2(it.capd, capDelta);
+  put2(it.pimd, pim);
+  put2(it.pim2, pim * pim);
+  put2(it.csd, __dmul_rn(corr, smdelta));
+  put2(it.cord, corr);
+}
 
 // the region used first by the principal-value records, then by the Landau
 // rows, in double2
@@ -560,25 +611,19 @@ __device__ __forceinline__ void df_cmul(dflt ax, dflt ay, dflt bx, dflt by, dflt
 
 __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const ResItem& it, double2 o, int n,
                                      int W, float4* win, double2* pvv, double2* T) {
+  if (!it.pvdf) return false;
   const int lane = threadIdx.x & 31;
   const int M = S.M;
-  const double kappa = a.sys.kpar / S.ms;
   const double pr = it.pr, pim = it.pim;
-  const double capDelta = pr - S.ppar[it.lower];
-  const double smdelta = capDelta / (1.0 * a.sys.M_P);
+  const double smdelta = it.smdelta;
   const bool sym = fabs(pim) > a.sys.Tlim;
   const int NP = a.sys.M_P + 1;
-  const int ntiny = (int)((S.ppar[it.upper] - pr - capDelta) / smdelta);
-  const double corr = (ntiny > 0) ? ((S.ppar[it.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta : 0.0;
-  auto inr = [](double x) { return x >= 1e-12 && x <= 1e12; };
-  if (!(inr(smdelta) && inr(capDelta) && fabs(pim) <= 1e12 && (!sym || inr(fabs(pim))) &&
-        (ntiny <= 0 || inr(corr * smdelta))))
-    return false;
+  const int ntiny = it.ntiny;
   const int jw0 = max(1, it.lower - 2), jw1 = min(M - 1, it.upper + 2);
   const int nw = jw1 - jw0 + 1;
   const float* __restrict__ Vh = S.Vh + (size_t)n * (M - 1) * 12;
   const float* __restrict__ Vl = S.Vl + (size_t)n * (M - 1) * 12;
-  const dflt oxd = df_of(o.x), oyd = df_of(o.y), kad = df_of(kappa), hid = df_of(S.hidpa);
+  const dflt oxd = df_of(o.x), oyd = df_of(o.y), kad = {S.kaph, S.kapl}, hid = {S.hidh, S.hidl};
   // node value h_e(j) = omega V_{e,1}(j) + kappa V_{e,2}(j), scaled
   auto hnode = [&](int j, int e, dflt& hx, dflt& hy) {
     const size_t b = (size_t)(j - 1) * 12 + 2 * e;
@@ -643,10 +688,15 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     const int j = (int)rintf(u);
     return (j >= 1 && j <= M - 1) ? j : 0;
   };
+  // the FP64 sample points as integrate_res writes them (for the search
+  // near half-way points only)
   auto sym_p = [&](int k) {
+    const double capDelta = pr - S.ppar[it.lower];
     return (k == 0) ? pr : ((k == a.sys.M_P) ? __dadd_rn(pr, capDelta) : __dadd_rn(pr, __dmul_rn(smdelta, (double)k)));
   };
   auto tiny_p = [&](int k) {
+    const double capDelta = pr - S.ppar[it.lower];
+    const double corr = ((S.ppar[it.upper] - pr - capDelta) / (1.0 * ntiny)) / smdelta;
     return (k == 0) ? __dadd_rn(pr, capDelta)
                     : __dadd_rn(__dadd_rn(pr, capDelta), __dmul_rn(__dmul_rn(corr, smdelta), (double)k));
   };
@@ -714,7 +764,8 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     nruns += nr;
     nl[gi] = __popc(__ballot_sync(0xffffffffu, j0 >= 0));
   };
-  const dflt pimd = df_of(pim), pim2 = df_of(pim * pim);
+  const dflt pimd = {it.pimd[0], it.pimd[1]}, pim2 = {it.pim2[0], it.pim2[1]};
+  const dflt smd = {it.smd[0], it.smd[1]}, capd = {it.capd[0], it.capd[1]};
   double2 Tl[6];  // the Tlim part (lane 0)
 #pragma unroll
   for (int e = 0; e < 6; ++e) Tl[e] = cmk(0.0, 0.0);
@@ -722,8 +773,7 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     const int per = (NP + 31) / 32;
     const int k0 = lane * per, k1 = min(NP, k0 + per);
     PvSlotF su{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0}, sd = su;
-    const float u0 = (float)(1.0 + (pr - S.ppar[1]) * S.idppar), du = (float)(smdelta * S.idppar);
-    const dflt smd = df_of(smdelta), capd = df_of(capDelta);
+    const float u0 = it.u0, du = it.du;
     for (int k = k0; k < k1; ++k) {
       // K = w (dx, p_im) / (dx^2 + p_im^2), dx = p_k - p_res
       const dflt dx = (k == a.sys.M_P) ? capd : df_mul(smd, {(float)k, 0.0f});
@@ -742,7 +792,6 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     records(1, sd, -1);
   } else {
     // Tlim branch: g' sum_k w_k dx^2/(dx^2 + p_im^2) + sign(p_im) i pi G(p_res)/smdelta
-    const dflt smd = df_of(smdelta), capd = df_of(capDelta);
     dflt frd = z0;
     for (int k = 1 + lane; k <= a.sys.M_P; k += 32) {
       const dflt dx = (k == a.sys.M_P) ? capd : df_mul(smd, {(float)k, 0.0f});
@@ -785,8 +834,8 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     const int per = (ntiny + 1 + 31) / 32;
     const int k0 = lane * per, k1 = min(ntiny + 1, k0 + per);
     PvSlotF sq{-1, -1, z0, z0, z0, z0, z0, z0, z0, z0};
-    const float ut0 = (float)(1.0 + (pr + capDelta - S.ppar[1]) * S.idppar), dut = (float)(corr * smdelta * S.idppar);
-    const dflt capd = df_of(capDelta), csd = df_of(__dmul_rn(corr, smdelta)), cord = df_of(corr);
+    const float ut0 = it.ut0, dut = it.dut;
+    const dflt csd = {it.csd[0], it.csd[1]}, cord = {it.cord[0], it.cord[1]};
     for (int k = k0; k < k1; ++k) {
       // K = w corr (dx, p_im) / (dx^2 + p_im^2)
       const dflt dx = (k == 0) ? capd : df_add(capd, df_mul(csd, {(float)k, 0.0f}));
@@ -1003,7 +1052,8 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       it.w = w;
       it.s = s;
       it.slot = item;
-      for (int e = 0; e < 6; ++e) it.pref[e] = pref[e];
+      for (int e = 0; e < 6; ++e) it.pref[e] = (e == 3 || e == 5) ? pref[e].y : pref[e].x;
+      pv_constants(a, S, g, it);
     }
   }
   __syncwarp();
@@ -1474,15 +1524,14 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       }
       }  // FP64 code
       // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
-      const double capDelta = pr - S.ppar[it.lower];
-      const double smdelta = capDelta / (1.0 * a.sys.M_P);
+      const double smdelta = it.smdelta;
       double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-S.qk * 0.5);
       // lane 0 holds the whole T; lanes 0-5 add entry e
       if (lane == 0)
         for (int e = 0; e < 6; ++e) tb[e] = T[e];
       __syncwarp();
       if (lane < 6 && !(n == 0 && (lane == 0 || lane == 3 || lane == 4)))
-        out[lane] = cadd(out[lane], cscale(cmul(it.pref[lane], tb[lane]), scale));
+        out[lane] = cadd(out[lane], cscale(cmul(item_pref(it, lane), tb[lane]), scale));
       __syncwarp();
     }
 
@@ -1575,7 +1624,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
           const double2 ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
           const int fam = (e == 1) ? 1 : ((e == 3 || e == 5) ? 2 : 0);
           const double2 ifac = cmk(0.0, -dpp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
-          const double2 land = cmul(cmul(it.pref[e], ce), tb[fam]);
+          const double2 land = cmul(cmul(item_pref(it, e), ce), tb[fam]);
           out[e] = cadd(out[e], cmul(land, ifac));
         }
         __syncwarp();
@@ -1929,6 +1978,13 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->pph = S.d_pph;
   o->ppl = S.d_ppl;
   o->df_sums = (c->precision != ALPS_PREC_FP64 && S.d_Vh) ? 1 : 0;
+  {
+    const double kap = c->kpar / S.sp.ms;
+    o->kaph = (float)kap;  // round to nearest, as __double2float_rn
+    o->kapl = (float)(kap - (double)o->kaph);
+    o->hidh = (float)o->hidpa;
+    o->hidl = (float)(o->hidpa - (double)o->hidh);
+  }
   o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
   o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
   // the series is used only where it is cheaper than the node sum
