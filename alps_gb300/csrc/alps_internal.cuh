@@ -89,6 +89,12 @@ struct SpecDev {
   const float* pph;
   const float* ppl;
   int df_sums;
+  // order-fused tables (C0 and the prefactors folded in, one scale per
+  // vector q): W pairs [(nmax+1)][M-1][12], moment pairs and FP32 moments
+  // [(nmax+1)][ALPS_KFAR][12], Wscale[12]; FP32 resonance bounds
+  const float *Wh, *Wl, *mWh, *mWl, *mWf;
+  const double* Wscale;
+  float qlo, qhi;
   float kaph, kapl;   // k_par / m_s as a float pair
   float hidh, hidl;   // hidpa as a float pair
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
@@ -153,6 +159,10 @@ struct SpeciesHost {
   double* d_mom = nullptr;                // Laurent moments
   float* d_momf = nullptr;                // the same in FP32; the pairs below share its allocation
   float *d_momh = nullptr, *d_moml = nullptr;  // the moments as float pairs (scale Vscale per order)
+  float* d_Wh = nullptr;                  // order-fused tables: W hi, lo, moments hi, lo, FP32
+  size_t Wf_cap = 0;
+  double* d_Wscale = nullptr;             // their scale per vector q
+  float qlo = 0.0f, qhi = 0.0f;           // FP32 bounds of the resonance interval (with margin)
   float *d_Vh = nullptr, *d_Vl = nullptr;  // V as float pairs (one allocation, lo after hi)
   size_t Vf_cap = 0;
   double* d_Vscale = nullptr;             // per-order scale of the pairs

@@ -125,7 +125,6 @@ __device__ inline double2 csqrt_d(double2 z) {
   return cmk(0.5 * fabs(z.y) / t, z.y >= 0.0 ? t : -t);
 }
 
-// Fast FP64 reciprocal: PTX rcp.approx seed + two Newton steps (<= 1 ulp).
 // ---------------------------------------------------------------------------
 // Double-float arithmetic: x = h + l with |l| <= ulp(h)/2, about 48 bits,
 // on the FP32 pipes (64 times the FP64 rate on this part).  Error-free
@@ -189,6 +188,7 @@ __device__ __forceinline__ void df_mac(dflt& acc, float vh, float vl, dflt r) {
   acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, pl));
 }
 
+// Fast FP64 reciprocal: PTX rcp.approx seed + two Newton steps (<= 1 ulp).
 __device__ __forceinline__ double rcp_fast(double x) {
   double r;
   asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
@@ -294,4 +294,12 @@ __device__ inline void t_prefactors(int nn, double z, double kperp, int kperp_no
   pref[3] = cmk(0.0, k1 * dn / z);
   pref[4] = cmk(k1 * dn / z, 0.0);
   pref[5] = cmk(0.0, -k2);
+}
+
+// C0 v_e(n) of the order-fused tables: C0 times the nonzero part of
+// prefactor e of order n >= 0 (imaginary for xy and yz, else real)
+__device__ __forceinline__ double fused_factor(int n, int e, double z, double kperp, int kperp_norm, double C0) {
+  double2 pref[6];
+  t_prefactors(n, z, kperp, kperp_norm, pref);
+  return C0 * ((e == 3 || e == 5) ? pref[e].y : pref[e].x);
 }

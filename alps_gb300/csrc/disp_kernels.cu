@@ -92,6 +92,261 @@ __device__ __forceinline__ void classify_body(const DispArgs& a, const double2* 
 // species, order chunks).  Each thread accumulates the six chi entries of its
 // omega over the orders of its chunk (and the n = -1,0,1 parts for chi_low).
 // ---------------------------------------------------------------------------
+// Complex double-float helpers of the order-fused pole sums
+__device__ __forceinline__ void df_cmul2(dflt ax, dflt ay, dflt bx, dflt by, dflt& rx, dflt& ry) {
+  const dflt x = df_add(df_mul(ax, bx), df_neg(df_mul(ay, by)));
+  ry = df_add(df_mul(ax, by), df_mul(ay, bx));
+  rx = x;
+}
+
+// ---------------------------------------------------------------------------
+// Fast path of the pole sums (no chi_low): the orders of a block's chunk
+// accumulate in one set of double-float sums per thread, on the order-fused
+// tables (C0 and the T-tensor prefactors folded into the reduced vectors and
+// their Laurent moments, one scale per vector).  Per (omega, signed order):
+// an FP32 test settles orders far from resonance (the FP64 geometry decides
+// the rest), then either the Laurent series (far poles, leading terms in
+// double-float from f / d^... , the tail in FP32) or the node sum in
+// double-float.  Once per chunk the sums are rescaled and combined,
+// acc_e = phase_e (omega S_{e,1} + kappa S_{e,2}), in FP64.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, double2 o, int js, int js_count,
+                                           int n_begin, int n_end, double2* acc) {
+  const int M = S.M;
+  const double kpar = a.sys.kpar;
+  dflt sacc[24];
+  float Sf[24];
+#pragma unroll
+  for (int q = 0; q < 24; ++q) {
+    sacc[q] = {0.0f, 0.0f};
+    Sf[q] = 0.0f;
+  }
+  const dflt oxd = df_of(o.x), oyd = df_of(o.y), msd = df_of(S.ms), qsd = df_of(S.qs);
+  const dflt kd = df_of(kpar), ikd = df_of(a.sys.ikpar), pcd = df_of(S.pcen), prd = df_of(S.prad);
+  const dflt Dd = df_mul(msd, oyd);  // m omega_i
+  const dflt D2 = df_mul(Dd, Dd);
+  const dflt dyd = df_mul(Dd, ikd);  // Im p_res
+  const dflt mox = df_mul(msd, oxd);
+  const float ikp32 = (float)a.sys.ikpar;
+  for (int n = n_begin; n < n_end; ++n) {
+    const float* __restrict__ Wh = S.Wh + (size_t)n * (M - 1) * 12;
+    const float* __restrict__ Wl = S.Wl + (size_t)n * (M - 1) * 12;
+    for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
+      const int nn = sg ? -n : n;
+      const float sgf = (nn < 0) ? -1.0f : 1.0f;  // xy and xz are odd in n
+      // A = m omega_r - nn q, the pole's real part times k_par
+      const dflt Ad = df_add(mox, df_neg(df_mul({(float)nn, 0.0f}, qsd)));
+      const float x32 = Ad.h * ikp32;
+      const float mg = 9.5367431640625e-7f * fabsf(x32);  // 2^-20 |x|
+      ResGeom g;
+      double2 dfar;  // p_res - pcen (FP32 for orders far from resonance)
+      if (x32 < S.qlo - mg || x32 > S.qhi + mg) {
+        g.res = 0;
+        g.lo1 = 1;
+        g.hi1 = M - 1;
+        g.lo2 = 1;
+        g.hi2 = 0;
+        dfar = cmk((double)(x32 - (float)S.pcen), (double)(dyd.h));
+      } else {
+        g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+        dfar = cmk(g.pr - S.pcen, g.pi);
+      }
+      int K = S.kfar + 1, K32 = K;
+      const float ddf = (float)(dfar.x * dfar.x + dfar.y * dfar.y);
+      if (!g.res && (float)S.prad * (float)S.prad < 0.5f * ddf) {
+        const float rho = (float)S.prad * rsqrtf(ddf);
+        const float lr = -__logf(rho), l1 = log1pf(-rho);
+        K = (int)ceilf((36.7368006f - l1) / lr) + 1;    // 53 ln 2
+        K32 = (int)ceilf((22.8738570f - l1) / lr) + 1;  // 33 ln 2
+      }
+      // the double-float values stay normal floats: |f| = 1/(k_par |d|) for
+      // the series, |A - k_par p_j|^2 + D^2 at the summed ranges' ends for
+      // the node sum (zero if the pole lies inside a summed range)
+      if (K <= S.kfar) {
+        const float fm = fabsf(ikp32) * rsqrtf(ddf);
+        if (!(fm >= 1e-30f && fm <= 1e30f)) K = K32 = S.kfar + 1;
+      }
+      bool nodes_df = true;
+      if (K > S.kfar) {
+        float lo = 3.0e38f, hi = 0.0f;
+        const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+        for (int r2 = 0; r2 < 2; ++r2) {
+          const int j0 = max(1, ends[2 * r2]), j1 = min(M - 1, ends[2 * r2 + 1]);
+          if (j0 > j1) continue;
+          const float d0 = Ad.h - kd.h * S.pph[j0], d1 = Ad.h - kd.h * S.pph[j1];
+          lo = ((d0 < 0.0f) != (d1 < 0.0f)) ? 0.0f : fminf(lo, fminf(fabsf(d0), fabsf(d1)));
+          hi = fmaxf(hi, fmaxf(fabsf(d0), fabsf(d1)));
+        }
+        const float d2 = D2.h;
+        nodes_df = d2 + lo * lo >= 1e-30f && d2 + hi * hi <= 1e30f;
+      }
+      if (K > S.kfar && !nodes_df) {
+        // FP64 node sum of this order, folded into the sums as its terms
+        const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
+        const double Ar = S.ms * o.x - (double)nn * S.qs, Di = S.ms * o.y;
+        double2 Sx[12];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) Sx[q] = cmk(0.0, 0.0);
+        auto nd = [&](int j, double wgt) {
+          const double dr = fma(-kpar, S.ppar[j], Ar);
+          const double rr = wgt / fma(dr, dr, Di * Di);
+          const double* v = Vn + (size_t)(j - 1) * 12;
+#pragma unroll
+          for (int q = 0; q < 12; ++q) {
+            Sx[q].x = fma(v[q], dr * rr, Sx[q].x);
+            Sx[q].y = fma(v[q], -Di * rr, Sx[q].y);
+          }
+        };
+        for (int j = 1 + js; j <= M - 1; j += js_count)
+          if ((j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2)) nd(j, 1.0);
+        const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+        for (int r2 = 0; r2 < 2; ++r2) {
+          const int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
+          if (lo >= hi) continue;
+          for (int side = 0; side < 2; ++side) {
+            const int j = side ? hi : lo;
+            if (((j - 1) % js_count) == js) nd(j, -0.5);
+          }
+        }
+        const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+        const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
+#pragma unroll
+        for (int q = 0; q < 12; ++q) {
+          const double f = fused_factor(n, q >> 1, z, a.sys.kperp, a.sys.kperp_norm, C0) *
+                           ((q >= 6 && q <= 9) ? (double)sgf : 1.0) / S.Wscale[q];
+          df_acc(sacc[2 * q], df_of(Sx[q].x * f));
+          df_acc(sacc[2 * q + 1], df_of(Sx[q].y * f));
+        }
+      } else if (K <= S.kfar) {
+        // Laurent series: S = f sum_k mom_k t^k, d = p_res - pcen,
+        // t = prad/d, f = 1/(k_par d); the powers start at f t^js
+        const dflt dxd = df_add(df_mul(Ad, ikd), df_neg(pcd));
+        const dflt r = df_rcp_approx(df_add(df_mul(dxd, dxd), df_mul(dyd, dyd)));
+        const dflt ivx = df_mul(dxd, r), ivy = df_neg(df_mul(dyd, r));
+        const dflt tx0 = df_mul(prd, ivx), ty0 = df_mul(prd, ivy);
+        dflt tx = df_mul(ikd, ivx), ty = df_mul(ikd, ivy);
+        dflt sx = tx0, sy = ty0;
+        {
+          dflt px = tx0, py = ty0;
+          for (int q = js; q; q >>= 1) {
+            if (q & 1) df_cmul2(tx, ty, px, py, tx, ty);
+            df_cmul2(px, py, px, py, px, py);
+          }
+          for (int q = js_count; q > 1; q >>= 1) df_cmul2(sx, sy, sx, sy, sx, sy);
+        }
+        const float* __restrict__ mh = S.mWh + (size_t)n * ALPS_KFAR * 12;
+        const float* __restrict__ ml = S.mWl + (size_t)n * ALPS_KFAR * 12;
+        int k = js;
+        for (; k < K32; k += js_count) {
+          const float4* h4 = reinterpret_cast<const float4*>(mh + (size_t)k * 12);
+          const float4* l4 = reinterpret_cast<const float4*>(ml + (size_t)k * 12);
+          const dflt ux = df_scale(tx, sgf), uy = df_scale(ty, sgf);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float4 h = __ldg(h4 + q), l = __ldg(l4 + q);
+            // vectors 4q..4q+3; 6..9 are xy and xz (odd in n)
+            const dflt ax0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? ux : tx, ay0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? uy : ty;
+            const dflt ax1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? ux : tx, ay1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? uy : ty;
+            const dflt ax2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? ux : tx, ay2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? uy : ty;
+            const dflt ax3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? ux : tx, ay3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? uy : ty;
+            df_mac(sacc[8 * q + 0], h.x, l.x, ax0);
+            df_mac(sacc[8 * q + 1], h.x, l.x, ay0);
+            df_mac(sacc[8 * q + 2], h.y, l.y, ax1);
+            df_mac(sacc[8 * q + 3], h.y, l.y, ay1);
+            df_mac(sacc[8 * q + 4], h.z, l.z, ax2);
+            df_mac(sacc[8 * q + 5], h.z, l.z, ay2);
+            df_mac(sacc[8 * q + 6], h.w, l.w, ax3);
+            df_mac(sacc[8 * q + 7], h.w, l.w, ay3);
+          }
+          df_cmul2(tx, ty, sx, sy, tx, ty);
+        }
+        if (k < K) {
+          // the tail: terms below 2^-33 of the bound, in FP32
+          const float* __restrict__ mf = S.mWf + (size_t)n * ALPS_KFAR * 12;
+          float fx = tx.h + tx.l, fy = ty.h + ty.l;
+          const float gx = sx.h + sx.l, gy = sy.h + sy.l;
+          for (; k < K; k += js_count) {
+            const float4* m4 = reinterpret_cast<const float4*>(mf + (size_t)k * 12);
+            const float ux = fx * sgf, uy = fy * sgf;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+              const float4 m = __ldg(m4 + q);
+              const float bx0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? ux : fx, by0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? uy : fy;
+              const float bx1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? ux : fx, by1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? uy : fy;
+              const float bx2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? ux : fx, by2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? uy : fy;
+              const float bx3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? ux : fx, by3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? uy : fy;
+              Sf[8 * q + 0] = fmaf(m.x, bx0, Sf[8 * q + 0]);
+              Sf[8 * q + 1] = fmaf(m.x, by0, Sf[8 * q + 1]);
+              Sf[8 * q + 2] = fmaf(m.y, bx1, Sf[8 * q + 2]);
+              Sf[8 * q + 3] = fmaf(m.y, by1, Sf[8 * q + 3]);
+              Sf[8 * q + 4] = fmaf(m.z, bx2, Sf[8 * q + 4]);
+              Sf[8 * q + 5] = fmaf(m.z, by2, Sf[8 * q + 5]);
+              Sf[8 * q + 6] = fmaf(m.w, bx3, Sf[8 * q + 6]);
+              Sf[8 * q + 7] = fmaf(m.w, by3, Sf[8 * q + 7]);
+            }
+            const float nx = fx * gx - fy * gy;
+            fy = fx * gy + fy * gx;
+            fx = nx;
+          }
+        }
+      } else {
+        // node sum in double-float: sum_j W_j / (A - k_par p_j + i D)
+        auto node = [&](int j, float wgt) {
+          const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
+          const dflt r = df_rcp_approx(df_add(df_mul(dr, dr), D2));
+          const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
+          const dflt Ur = df_scale(Rr, sgf), Ui = df_scale(Ri, sgf);
+          const float4* vh4 = reinterpret_cast<const float4*>(Wh + (size_t)(j - 1) * 12);
+          const float4* vl4 = reinterpret_cast<const float4*>(Wl + (size_t)(j - 1) * 12);
+#pragma unroll
+          for (int q = 0; q < 3; ++q) {
+            const float4 h = __ldg(vh4 + q), l = __ldg(vl4 + q);
+            const dflt ax0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? Ur : Rr, ay0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? Ui : Ri;
+            const dflt ax1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? Ur : Rr, ay1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? Ui : Ri;
+            const dflt ax2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? Ur : Rr, ay2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? Ui : Ri;
+            const dflt ax3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? Ur : Rr, ay3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? Ui : Ri;
+            df_mac(sacc[8 * q + 0], h.x, l.x, ax0);
+            df_mac(sacc[8 * q + 1], h.x, l.x, ay0);
+            df_mac(sacc[8 * q + 2], h.y, l.y, ax1);
+            df_mac(sacc[8 * q + 3], h.y, l.y, ay1);
+            df_mac(sacc[8 * q + 4], h.z, l.z, ax2);
+            df_mac(sacc[8 * q + 5], h.z, l.z, ay2);
+            df_mac(sacc[8 * q + 6], h.w, l.w, ax3);
+            df_mac(sacc[8 * q + 7], h.w, l.w, ay3);
+          }
+        };
+        for (int j = 1 + js; j <= M - 1; j += js_count) {
+          const bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
+          if (in) node(j, 1.0f);
+        }
+        // trapezoid end weights
+        const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+#pragma unroll
+        for (int r2 = 0; r2 < 2; ++r2) {
+          const int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
+          if (lo >= hi) continue;
+#pragma unroll
+          for (int side = 0; side < 2; ++side) {
+            const int j = side ? hi : lo;
+            if (((j - 1) % js_count) == js) node(j, -0.5f);
+          }
+        }
+      }
+    }
+  }
+  // rescale and combine: acc_e = phase_e (omega S_{e,1} + kappa S_{e,2})
+  const double kappa = kpar / S.ms;
+#pragma unroll
+  for (int e = 0; e < 6; ++e) {
+    const double s1 = S.Wscale[2 * e], s2 = S.Wscale[2 * e + 1];
+    const double2 S1 = cmk((df_val(sacc[4 * e]) + (double)Sf[4 * e]) * s1, (df_val(sacc[4 * e + 1]) + (double)Sf[4 * e + 1]) * s1);
+    const double2 S2 = cmk((df_val(sacc[4 * e + 2]) + (double)Sf[4 * e + 2]) * s2,
+                           (df_val(sacc[4 * e + 3]) + (double)Sf[4 * e + 3]) * s2);
+    const double2 t = cadd(cmul(o, S1), cscale(S2, kappa));
+    acc[e] = (e == 3 || e == 5) ? cmk(-t.y, t.x) : t;
+  }
+}
+
 // The double-float node sum keeps |A - k_par p_j|^2 + D^2 a normal float:
 // its smallest value (at a summed range's end, or zero if the pole lies
 // inside a summed range) at least 1e-30, its largest at most 1e30.
@@ -140,7 +395,9 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
 #pragma unroll
     for (int q = 0; q < (LOW ? 3 : 1); ++q) lacc[q][e] = cmk(0.0, 0.0);
   }
-  if (active) {
+  if (active && !LOW && S.df_sums && S.Wh && n_end > n_begin) {
+    pole_fused(a, S, o, js, js_count, n_begin, n_end, acc);
+  } else if (active) {
     for (int n = n_begin; n < n_end; ++n) {
       const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
       for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
@@ -1978,6 +2235,18 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->pph = S.d_pph;
   o->ppl = S.d_ppl;
   o->df_sums = (c->precision != ALPS_PREC_FP64 && S.d_Vh) ? 1 : 0;
+  {
+    const size_t nvf = (size_t)(S.nmax + 1) * (c->sys.npar - 1) * 12, nmo = (size_t)(S.nmax + 1) * ALPS_KFAR * 12;
+    const bool fz = S.d_Wh != nullptr;
+    o->Wh = fz ? S.d_Wh : nullptr;
+    o->Wl = fz ? S.d_Wh + nvf : nullptr;
+    o->mWh = fz ? S.d_Wh + 2 * nvf : nullptr;
+    o->mWl = fz ? S.d_Wh + 2 * nvf + nmo : nullptr;
+    o->mWf = fz ? S.d_Wh + 2 * nvf + 2 * nmo : nullptr;
+    o->Wscale = S.d_Wscale;
+    o->qlo = S.qlo;
+    o->qhi = S.qhi;
+  }
   {
     const double kap = c->kpar / S.sp.ms;
     o->kaph = (float)kap;  // round to nearest, as __double2float_rn

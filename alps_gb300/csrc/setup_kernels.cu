@@ -575,6 +575,61 @@ __global__ void k_moments(const double* __restrict__ V, const double* __restrict
   moml[t] = __double2float_rn(x - (double)h);
 }
 
+// The fast path's order-fused tables.  Entry e of chi gets, per signed
+// order nn, C0 pref_e(nn) (omega S_{e,1} + kappa S_{e,2}) with
+// C0 = 2 pi dpperp |dppar| q / 4 and pref_e = phase_e sgn_e(nn) v_e(|n|):
+// phase i for xy and yz, sgn = sign(nn) for xy and xz (odd in n), else 1.
+// Folding C0 v_e(n) into the reduced vectors and their Laurent moments, with
+// one scale 2^E_q per vector q = 2e + g over all orders, lets the pole sums
+// of a block's orders accumulate in one set of double-float sums.
+
+// Wscale[q] = 2^E_q, E_q the exponent of the largest |C0 v_e(n) x| over the
+// vectors and moments of q (one block per q)
+__global__ void k_fused_scale(const double* __restrict__ V, const double* __restrict__ mom, int M, int nmax,
+                              double z, double kperp, int kperp_norm, double C0, double* Wscale) {
+  __shared__ double red[256];
+  const int q = blockIdx.x, e = q >> 1;
+  double mx = 0.0;
+  const size_t nv = (size_t)(nmax + 1) * (M - 1), nm = (size_t)(nmax + 1) * ALPS_KFAR;
+  for (size_t t = threadIdx.x; t < nv + nm; t += blockDim.x) {
+    const bool isv = t < nv;
+    const size_t u = isv ? t : t - nv;
+    const int n = isv ? (int)(u / (M - 1)) : (int)(u / ALPS_KFAR);
+    const double x = isv ? V[u * 12 + q] : mom[u * 12 + q];
+    mx = fmax(mx, fabs(fused_factor(n, e, z, kperp, kperp_norm, C0) * x));
+  }
+  red[threadIdx.x] = mx;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) Wscale[q] = (red[0] > 0.0 && isfinite(red[0])) ? ldexp(1.0, ilogb(red[0])) : 1.0;
+}
+
+// W = C0 v_e(n) V / Wscale as float pairs; the moments likewise, plus FP32
+__global__ void k_fused_pairs(const double* __restrict__ V, const double* __restrict__ mom, int M, int nmax,
+                              double z, double kperp, int kperp_norm, double C0, const double* __restrict__ Wscale,
+                              float* Wh, float* Wl, float* mWh, float* mWl, float* mWf) {
+  const size_t nv = (size_t)(nmax + 1) * (M - 1) * 12, nm = (size_t)(nmax + 1) * ALPS_KFAR * 12;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nv + nm) return;
+  const bool isv = t < nv;
+  const size_t u = isv ? t : t - nv;
+  const int q = (int)(u % 12);
+  const int n = isv ? (int)(u / (12 * (size_t)(M - 1))) : (int)(u / (12 * (size_t)ALPS_KFAR));
+  const double x = (isv ? V[u] : mom[u]) * fused_factor(n, q >> 1, z, kperp, kperp_norm, C0) * (1.0 / Wscale[q]);
+  const float h = __double2float_rn(x), l = __double2float_rn(x - (double)h);
+  if (isv) {
+    Wh[u] = h;
+    Wl[u] = l;
+  } else {
+    mWh[u] = h;
+    mWl[u] = l;
+    mWf[u] = h;
+  }
+}
+
 // omega-independent factors of Maxwellian continuation terms, per row and
 // fit: a0 = p1 exp(-pc pperp^2) (the reference's left-to-right product),
 // p2, p3, exp(-p2 dppar^2)
@@ -932,6 +987,29 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_Vscale, S.d_mom, S.d_momf, S.d_momh,
                                                S.d_moml);
   ALPS_CUDA_TRY(cudaGetLastError());
+  // order-fused tables of the fast path (prefactors and C0 folded in)
+  {
+    const double z = c->sys.kperp_norm ? kperp / S.sp.qs : 1.0 / S.sp.qs;
+    const double dpperp = S.pperp[2] - S.pperp[1], dppar_abs = std::fabs(S.ppar[2] - S.ppar[1]);
+    const double C0 = 2.0 * ALPS_PI * dpperp * dppar_abs * 0.25 * S.sp.qs;
+    if ((rc = ensure(S.d_Wh, S.Wf_cap, 2 * nvf + 3 * nmo))) return rc;  // W hi, lo; moments hi, lo, FP32
+    if (!S.d_Wscale) ALPS_CUDA_TRY(cudaMalloc(&S.d_Wscale, 12 * sizeof(double)));
+    k_fused_scale<<<12, 256, 0, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp, c->sys.kperp_norm, C0, S.d_Wscale);
+    ALPS_CUDA_TRY(cudaGetLastError());
+    const size_t nf = nvf + nmo;
+    k_fused_pairs<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp,
+                                                                c->sys.kperp_norm, C0, S.d_Wscale, S.d_Wh,
+                                                                S.d_Wh + nvf, S.d_Wh + 2 * nvf,
+                                                                S.d_Wh + 2 * nvf + nmo, S.d_Wh + 2 * nvf + 2 * nmo);
+    ALPS_CUDA_TRY(cudaGetLastError());
+    // the FP32 test for orders far from resonance: the resonance interval of
+    // determine_resonances with a margin of 1e-5 of its extent
+    const double mi = c->sys.positions_principal * (S.ppar[2] - S.ppar[1]);
+    const double rlo = std::min(S.ppar[1] - mi, S.ppar[1]), rhi = std::max(S.ppar[M], S.ppar[M - 1] + mi);
+    const double mg = 1e-5 * (std::fabs(rlo) + std::fabs(rhi));
+    S.qlo = (float)(rlo - mg);
+    S.qhi = (float)(rhi + mg);
+  }
   return ALPS_OK;
 }
 
