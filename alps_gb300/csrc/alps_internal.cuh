@@ -94,9 +94,15 @@ struct SpecDev {
   // [(nmax+1)][ALPS_KFAR][12], Wscale[12]; FP32 resonance bounds
   const float *Wh, *Wl, *mWh, *mWl, *mWf;
   const double* Wscale;
-  float qlo, qhi;
+  float qlo, qhi;        // below / above these Re p_res is not resonant
+  float qlo_in, qhi_in;  // between these it is
   float kaph, kapl;   // k_par / m_s as a float pair
   float hidh, hidl;   // hidpa as a float pair
+  float dpph, dppl;   // dppar (signed) as a float pair
+  float idph, idpl;   // 1/dppar as a float pair
+  float tpmh, tpml;   // 2 pi M_P as a float pair
+  double kappa;       // k_par / m_s
+  double pvc;         // 2 pi dpperp/4 (-q/(2 k_par)): the principal-value scale over smdelta
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
   int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)
@@ -162,7 +168,8 @@ struct SpeciesHost {
   float* d_Wh = nullptr;                  // order-fused tables: W hi, lo, moments hi, lo, FP32
   size_t Wf_cap = 0;
   double* d_Wscale = nullptr;             // their scale per vector q
-  float qlo = 0.0f, qhi = 0.0f;           // FP32 bounds of the resonance interval (with margin)
+  float qlo = 0.0f, qhi = 0.0f;           // FP32 bounds of the resonance interval (margin outward)
+  float qlo_in = 1.0f, qhi_in = -1.0f;    // the same with the margin inward
   float *d_Vh = nullptr, *d_Vl = nullptr;  // V as float pairs (one allocation, lo after hi)
   size_t Vf_cap = 0;
   double* d_Vscale = nullptr;             // per-order scale of the pairs

@@ -69,10 +69,21 @@ __device__ __forceinline__ void classify_body(const DispArgs& a, const double2* 
   const double2 o = om[t];
   int* slots = slot_nn + ((size_t)t * S_ + s) * a.rcap;
   int cnt = 0;
+  const float ikp32 = (float)a.sys.ikpar;
   for (int base = -S.nmax; base <= S.nmax; base += 32) {
     const int nn = base + lane;
     bool res = false;
-    if (nn <= S.nmax) res = res_geometry(S, a.sys.M_I, o, nn, a.sys.kpar).res;
+    if (nn <= S.nmax) {
+      // an FP32 estimate of Re p_res settles the orders clearly outside or
+      // inside the resonance interval (its bounds carry a margin of 1e-5 of
+      // its extent, the estimate's error is below 2^-22 |p|); the FP64 test
+      // decides near the interval's ends
+      const float x32 = (float)(S.ms * o.x - (double)nn * S.qs) * ikp32;
+      const float mg = 9.5367431640625e-7f * fabsf(x32);
+      if (x32 < S.qlo - mg || x32 > S.qhi + mg) res = false;
+      else if (x32 > S.qlo_in + mg && x32 < S.qhi_in - mg) res = true;
+      else res = res_geometry(S, a.sys.M_I, o, nn, a.sys.kpar).res;
+    }
     const unsigned m = __ballot_sync(0xffffffffu, res);
     const int at = cnt + __popc(m & ((1u << lane) - 1u));
     if (res && at < a.rcap) slots[at] = nn;
@@ -850,7 +861,8 @@ __device__ inline double2 crcp(double2 z) {
 // The pieces are still chosen from the FP64 sample points wherever the FP32
 // estimate is within 1e-3 of a half-way point.  Returns false, with nothing
 // written to T, when a range would leave the normal floats or the merge does
-// not apply (the caller then runs the FP64 code).  T ends on lane 0.
+// not apply (the caller then runs the FP64 code); otherwise adds the item's
+// principal-value part to out (entry e: pref_e T_e times the window scale).
 // ---------------------------------------------------------------------------
 struct PvSlotF {
   int jd, jc;  // finished piece (-1: none), current piece
@@ -867,7 +879,7 @@ __device__ __forceinline__ void df_cmul(dflt ax, dflt ay, dflt bx, dflt by, dflt
 }
 
 __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const ResItem& it, double2 o, int n,
-                                     int W, float4* win, double2* pvv, double2* T) {
+                                     int W, float4* win, double2* pvv, double2* out) {
   if (!it.pvdf) return false;
   const int lane = threadIdx.x & 31;
   const int M = S.M;
@@ -940,11 +952,18 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     return jr;
   };
   auto clampj = [&](int jr) { return (jr >= M - 1) ? M - 2 : ((jr <= 1) ? 2 : jr); };
-  auto off_half = [&](float u) { return fabsf(u - rintf(u)) < 0.499f; };
+  // the FP32 estimates u (node j at u = j) are within 2^-23 (M + 20) of a
+  // spacing (two roundings of numbers below M + 10) and the nodes within
+  // 1e-6 of a spacing of their uniform positions: farther than four times
+  // that from a half-way point, the nearest node is the search's answer
+  const float hthr = 0.5f - (4.0f * 1.1920929e-7f * (float)(M + 20) + 4.0e-6f);
+  auto off_half = [&](float u) { return fabsf(u - rintf(u)) < hthr; };
   auto node_of = [&](float u) {
     const int j = (int)rintf(u);
     return (j >= 1 && j <= M - 1) ? j : 0;
   };
+  const dflt prd = df_of(pr);
+  auto ppd = [&](int j) { return dflt{S.pph[j], S.ppl[j]}; };
   // the FP64 sample points as integrate_res writes them (for the search
   // near half-way points only)
   auto sym_p = [&](int k) {
@@ -1023,9 +1042,7 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
   };
   const dflt pimd = {it.pimd[0], it.pimd[1]}, pim2 = {it.pim2[0], it.pim2[1]};
   const dflt smd = {it.smd[0], it.smd[1]}, capd = {it.capd[0], it.capd[1]};
-  double2 Tl[6];  // the Tlim part (lane 0)
-#pragma unroll
-  for (int e = 0; e < 6; ++e) Tl[e] = cmk(0.0, 0.0);
+  dflt Tlx = z0, Tly = z0;  // the Tlim part of entry e on lane e
   if (sym) {
     const int per = (NP + 31) / 32;
     const int k0 = lane * per, k1 = min(NP, k0 + per);
@@ -1056,35 +1073,34 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
       const dflt q = df_mul(d2, df_rcp_approx(df_add(d2, pim2)));
       df_acc(frd, df_scale(q, (k == a.sys.M_P) ? 1.0f : 2.0f));
     }
-    double fr = df_val(frd);
-    for (int off = 16; off > 0; off >>= 1) fr += __shfl_xor_sync(0xffffffffu, fr, off);
-    double2 Te = cmk(0.0, 0.0);
+    for (int off = 16; off > 0; off >>= 1)
+      frd = df_add(frd, {__shfl_xor_sync(0xffffffffu, frd.h, off), __shfl_xor_sync(0xffffffffu, frd.l, off)});
     if (lane < 6) {
       const int e = lane;
       const double dps = S.dppar;
-      auto Hc1 = [&](double p, dflt& Hx, dflt& Hy) {
-        const float u = (float)(1.0 + (p - S.ppar[1]) * S.idppar);
-        const int jc = clampj(off_half(u) ? node_of(u) : piece_raw(p));
+      // H at p_res + side dppar: u = u0 + side, dx = p - pp(jc) in double-float
+      auto Hc1 = [&](int side, dflt& Hx, dflt& Hy) {
+        const float u = it.u0 + (float)side;
+        int jc;
+        if (off_half(u)) jc = node_of(u);
+        else jc = piece_raw(side > 0 ? pr + dps : (side < 0 ? pr - dps : pr));
+        jc = clampj(jc);
         dflt hx, hy, sx, sy;
         node1(jc, e, hx, hy, sx, sy);
-        const dflt dx = df_of(p - S.ppar[jc]);
+        const dflt dx = df_add(df_add(prd, df_scale({S.dpph, S.dppl}, (float)side)), df_neg(ppd(jc)));
         Hx = df_add(hx, df_mul(sx, dx));
         Hy = df_add(hy, df_mul(sy, dx));
       };
       dflt H1x, H1y, H2x, H2y, H0x, H0y;
-      Hc1(pr + dps, H1x, H1y);
-      Hc1(pr - dps, H2x, H2y);
-      Hc1(pr, H0x, H0y);
-      const double sgn = (pim > 0.0) ? 1.0 : ((pim < 0.0) ? -1.0 : 0.0);
-      const dflt c1 = df_of(fr / dps), c2 = df_of(sgn * 2.0 * ALPS_PI / smdelta);
-      const dflt tx = df_add(df_mul(df_add(H1x, df_neg(H2x)), c1), df_neg(df_mul(c2, H0y)));
-      const dflt ty = df_add(df_mul(df_add(H1y, df_neg(H2y)), c1), df_mul(c2, H0x));
-      Te = cmk(df_val(tx), df_val(ty));
-    }
-#pragma unroll
-    for (int e = 0; e < 6; ++e) {
-      const double tx = __shfl_sync(0xffffffffu, Te.x, e), ty = __shfl_sync(0xffffffffu, Te.y, e);
-      if (lane == 0) Tl[e] = cmk(tx, ty);
+      Hc1(1, H1x, H1y);
+      Hc1(-1, H2x, H2y);
+      Hc1(0, H0x, H0y);
+      // g' 2 fr = (H1 - H2) fr / dppar;  i sign(p_im) 2 pi / smdelta, smdelta = capDelta / M_P
+      const float sgn = (pim > 0.0) ? 1.0f : ((pim < 0.0) ? -1.0f : 0.0f);
+      const dflt c1 = df_mul(frd, {S.idph, S.idpl});
+      const dflt c2 = df_scale(df_mul({S.tpmh, S.tpml}, df_rcp_approx(capd)), sgn);
+      Tlx = df_add(df_mul(df_add(H1x, df_neg(H2x)), c1), df_neg(df_mul(c2, H0y)));
+      Tly = df_add(df_mul(df_add(H1y, df_neg(H2y)), c1), df_mul(c2, H0x));
     }
   }
   if (ntiny > 0) {
@@ -1108,8 +1124,7 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
     records(2, sq, 1);
   }
   if (__any_sync(0xffffffffu, bad) || nruns > 32) return false;
-  const double sc = S.Vscale[n];
-  double acc = 0.0;
+  dflt accd = z0;  // component c = lane (< 12) of T: xx.re, xx.im, yy.re, ...
   if (nruns > 0) {
     __syncwarp();
     // run totals in (lane, slot) order
@@ -1146,7 +1161,7 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
       node1(jc, e, hx, hy, sx, sy);
       const float4 A4 = runv[rho * 2], C4 = runv[rho * 2 + 1];
       const dflt Ax = f4x(A4), Ay = f4y(A4);
-      const dflt del = df_of(pr - S.ppar[jc]);
+      const dflt del = df_add(prd, df_neg(ppd(jc)));
       const dflt Bx = df_add(f4x(C4), df_mul(Ax, del)), By = df_add(f4y(C4), df_mul(Ay, del));
       dflt t1x, t1y, t2x, t2y;
       df_cmul(hx, hy, Ax, Ay, t1x, t1y);
@@ -1167,14 +1182,28 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
         const float4 c = contrib[rho * 6 + e];
         s = df_add(s, (lane & 1) ? f4y(c) : f4x(c));
       }
-      acc = df_val(s);
+      accd = s;
     }
   }
-  // T on lane 0: the Tlim part, the merged sums (both rescaled)
-#pragma unroll
-  for (int e = 0; e < 6; ++e) {
-    const double tx = __shfl_sync(0xffffffffu, acc, 2 * e), ty = __shfl_sync(0xffffffffu, acc, 2 * e + 1);
-    T[e] = cmk((Tl[e].x + tx) * sc, (Tl[e].y + ty) * sc);
+  {
+    // plus the Tlim part of component c (entry c/2 sits on lane c/2)
+    const int src = (lane < 12) ? (lane >> 1) : 0;
+    const float xh = __shfl_sync(0xffffffffu, Tlx.h, src), xl = __shfl_sync(0xffffffffu, Tlx.l, src);
+    const float yh = __shfl_sync(0xffffffffu, Tly.h, src), yl = __shfl_sync(0xffffffffu, Tly.l, src);
+    accd = df_add(accd, (lane & 1) ? dflt{yh, yl} : dflt{xh, xl});
+  }
+  // out_e += pref_e T_e scale: scale = 2 pi smdelta dpperp/4 (-q/(2 k_par))
+  // and the pairs' 2^e; an imaginary prefactor (xy, yz) maps (x, y) to
+  // pe (-y, x)
+  const double v = df_val(accd) * (S.Vscale[n] * it.smdelta * S.pvc);
+  const double w = __shfl_xor_sync(0xffffffffu, v, 1);
+  if (lane < 12) {
+    const int e = lane >> 1;
+    if (!(n == 0 && (e == 0 || e == 3 || e == 4))) {
+      const double pe = it.pref[e];
+      double* o2 = reinterpret_cast<double*>(out + e);
+      o2[lane & 1] += (e == 3 || e == 5) ? ((lane & 1) ? pe * w : -pe * w) : pe * v;
+    }
   }
   __syncwarp();
   return true;
@@ -1327,7 +1356,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
     const SpecDev& S = a.sp[s];
     const double2 o = om[w];
     const int M = S.M;
-    const double kpar = a.sys.kpar, kappa = kpar / S.ms;
+    const double kpar = a.sys.kpar, kappa = S.kappa;
     const double* Vn = S.V + (size_t)n * (M - 1) * 12;
     double2* out = items + it.slot * 6;
 
@@ -1341,7 +1370,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       double2 T[6];
       for (int e = 0; e < 6; ++e) T[e] = cmk(0.0, 0.0);
       // the fast path's double-float sums; the FP64 code below otherwise
-      const bool fast = S.df_sums && winok && pv_fast(a, S, it, o, n, W, reinterpret_cast<float4*>(wh), pvv, T);
+      const bool fast = S.df_sums && winok && pv_fast(a, S, it, o, n, W, reinterpret_cast<float4*>(wh), pvv, out);
       if (!fast) {
       if (winok) {
         for (int t = lane; t < nw * 6; t += 32) {
@@ -1779,9 +1808,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
             T[e].y += __shfl_xor_sync(0xffffffffu, T[e].y, off);
           }
       }
-      }  // FP64 code
       // G = K_e H with K_e = -(q/kpar) pref_e / 2; result 2 pi T smdelta dpperp/4
-      const double smdelta = it.smdelta;
       double scale = 2.0 * ALPS_PI * smdelta * S.dpperp * 0.25 * (-S.qk * 0.5);
       // lane 0 holds the whole T; lanes 0-5 add entry e
       if (lane == 0)
@@ -1790,6 +1817,7 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       if (lane < 6 && !(n == 0 && (lane == 0 || lane == 3 || lane == 4)))
         out[lane] = cadd(out[lane], cscale(cmul(item_pref(it, lane), tb[lane]), scale));
       __syncwarp();
+      }  // FP64 code
     }
 
     if (wk & 2) {
@@ -2132,16 +2160,23 @@ __device__ __forceinline__ const DispArgs& stage_args(const DispArgs* src, DispA
   return dst;
 }
 
+#define CLS_PER_WARP 8
+// blocks of 128 threads of k_classify_multi for n omegas and S species
+__host__ __device__ inline long cls_blocks(long n, int S_) { return (n * S_ + 4 * CLS_PER_WARP - 1) / (4 * CLS_PER_WARP); }
+
 __global__ void k_classify_multi(const DispJob* __restrict__ jobs, int nj) {
   __shared__ DispArgs sa;
   const DispJob& J = job_of(jobs, nj, blockIdx.x, 0);
   const DispArgs& a = stage_args(J.a, sa);
   const long lb = (long)blockIdx.x - J.blk[0];
-  classify_body(a, J.om, J.n, J.count, J.slot_nn, J.flags, (lb * blockDim.x + threadIdx.x) >> 5);
+  // CLS_PER_WARP (omega, species) pairs per warp: the block's argument
+  // staging is shared by more pairs
+  const long w0 = ((lb * blockDim.x + threadIdx.x) >> 5) * CLS_PER_WARP;
+  for (int q = 0; q < CLS_PER_WARP; ++q) classify_body(a, J.om, J.n, J.count, J.slot_nn, J.flags, w0 + q);
 }
 
 template <bool LOW>
-__global__ void __launch_bounds__(128) k_pole_sums_multi(const DispJob* __restrict__ jobs, int nj) {
+__global__ void __launch_bounds__(128, 3) k_pole_sums_multi(const DispJob* __restrict__ jobs, int nj) {
   __shared__ DispArgs sa;
   const DispJob& J = job_of(jobs, nj, blockIdx.x, 1);
   const DispArgs& a = stage_args(J.a, sa);
@@ -2246,6 +2281,8 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
     o->Wscale = S.d_Wscale;
     o->qlo = S.qlo;
     o->qhi = S.qhi;
+    o->qlo_in = S.qlo_in;
+    o->qhi_in = S.qhi_in;
   }
   {
     const double kap = c->kpar / S.sp.ms;
@@ -2253,6 +2290,15 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
     o->kapl = (float)(kap - (double)o->kaph);
     o->hidh = (float)o->hidpa;
     o->hidl = (float)(o->hidpa - (double)o->hidh);
+    o->kappa = kap;
+    o->dpph = (float)o->dppar;
+    o->dppl = (float)(o->dppar - (double)o->dpph);
+    o->idph = (float)o->idppar;
+    o->idpl = (float)(o->idppar - (double)o->idph);
+    const double tpm = 2.0 * ALPS_PI * c->sys.n_resonance_interval;
+    o->tpmh = (float)tpm;
+    o->tpml = (float)(tpm - (double)o->tpmh);
+    o->pvc = 2.0 * ALPS_PI * o->dpperp * 0.25 * (-o->qk * 0.5);
   }
   o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
   o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
@@ -2467,7 +2513,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   c->args_gen = c->gen;  // the device copy is the context at its current state
   c->args_maxn = maxn;
   c->args_rcap = a.rcap;
-  k_classify_multi<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(dj, 1);
+  k_classify_multi<<<(unsigned)cls_blocks(n, S_), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[1], st));
   const unsigned g2 = (unsigned)((long)tiles * S_ * sh.nchunk);
@@ -2584,7 +2630,7 @@ int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2*
     J.tiles = bg.tiles;
     J.S = S_;
     J.blk[0] = blk[0];
-    blk[0] += ((long)n[j] * S_ * 32 + 127) / 128;
+    blk[0] += cls_blocks(n[j], S_);
     J.blk[1] = blk[1];
     blk[1] += (long)bg.tiles * S_ * bg.sh.nchunk;
     J.blk[2] = blk[2];
@@ -2744,7 +2790,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   DispJob* dj = reinterpret_cast<DispJob*>(b + o_job);
   k_stage<<<1, 128, 0, st>>>(a, job, da, dj);
   ALPS_CUDA_TRY(cudaGetLastError());
-  k_classify_multi<<<(unsigned)(((long)n * S_ * 32 + 127) / 128), 128, 0, st>>>(dj, 1);
+  k_classify_multi<<<(unsigned)cls_blocks(n, S_), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   k_pole_sums_multi<false><<<(unsigned)((long)tiles * S_ * sh.nchunk), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());

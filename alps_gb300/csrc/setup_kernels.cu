@@ -1009,6 +1009,8 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
     const double mg = 1e-5 * (std::fabs(rlo) + std::fabs(rhi));
     S.qlo = (float)(rlo - mg);
     S.qhi = (float)(rhi + mg);
+    S.qlo_in = (float)(rlo + mg);
+    S.qhi_in = (float)(rhi - mg);
   }
   return ALPS_OK;
 }
