@@ -429,10 +429,13 @@ def main():
     # resonant items: the SURVEY's algorithmic count per item, 24 M_P flops of
     # principal-value sums and 60 (N_perp + 1) of Landau rows, FP64
     f_res = work["items"] * (24.0 * system.n_resonance_interval + 60.0 * (system.nperp + 1))
-    res = {"kernel": "k_resonant_multi (fast path)", "bound": "fp64", "kernel_ms": res_ms,
+    res = {"kernel": "k_resonant_multi (fast path)", "bound": "fp64-equivalent", "kernel_ms": res_ms,
            "achieved": f_res / (res_ms / 1e3) / 1e12, "peak": peak64, "unit": "TFLOP/s",
            "frac": f_res / (res_ms / 1e3) / 1e12 / peak64, "items_per_step": work["items"],
-           "fp64_flop_per_step": f_res}
+           "fp64_flop_per_step": f_res,
+           "note": ("the reference algorithm's FP64 count per item over the DGEMM rate; the kernel runs the "
+                    "principal-value sums in double-float on the FP32 pipes and factorises the Landau rows, "
+                    "so the figure can read above 1")}
     dom = pole if fast_pole_ms >= res_ms else res
     # the plain path's pole sums: every order sums its nodes in FP64
     pole_ms = pm_plain[1] / max(nb_plain, 1)

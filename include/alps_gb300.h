@@ -166,8 +166,12 @@ int alps_get_nmax(alps_ctx* ctx, int* nmax /* [nspec] */);
  * ALPS_PREC_MIXED (fast): for non-resonant orders whose pole lies well
  *   outside the p_par grid the node sum is replaced by its Laurent series
  *   about the grid centre, truncated where the remainder is below FP64
- *   rounding (rho^K <= 2^-53 (1-rho)); pole, principal value, Landau
- *   residue and det are computed as in the plain mode. */
+ *   rounding (rho^K <= 2^-53 (1-rho)); one-Maxwellian Landau rows are
+ *   factorised where their deviation bound is below 1e-5; the node sums,
+ *   series terms and principal-value sums run in double-float arithmetic
+ *   (float pairs, about 46-48 bits).  Resonance decisions, windows and
+ *   sample points are the reference's in both modes; results agree with the
+ *   plain mode to about 1e-10 in det D on the benchmark map. */
 enum { ALPS_PREC_FP64 = 0, ALPS_PREC_MIXED = 1 };
 int alps_set_precision(alps_ctx* ctx, int precision);
 
