@@ -164,7 +164,9 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
       }
       int K = S.kfar + 1, K32 = K;
       const float ddf = (float)(dfar.x * dfar.x + dfar.y * dfar.y);
-      if (!g.res && (float)S.prad * (float)S.prad < 0.5f * ddf) {
+      // the series is used up to rho^2 < 0.58, where its K <= kfar terms
+      // (checked below) cost less than the node sum
+      if (!g.res && (float)S.prad * (float)S.prad < 0.58f * ddf) {
         const float rho = (float)S.prad * rsqrtf(ddf);
         const float lr = -__logf(rho), l1 = log1pf(-rho);
         K = (int)ceilf((36.7368006f - l1) / lr) + 1;    // 53 ln 2

@@ -163,7 +163,7 @@ DF_TERM_FLOPS = 24 * 15 + 4 * 9 + 2 * 10
 def pole_sum_work_fast(system, species, kpar, oms, nmax):
     """Work of the fast path's pole sums over a lattice, with the kernel's own
     decisions per (omega, signed order): a pole far from the grid (not
-    resonant, rho = prad/|p_res - pcen| with rho^2 < 1/2) takes K Laurent
+    resonant, rho = prad/|p_res - pcen| with rho^2 < 0.58) takes K Laurent
     terms, rho^K <= 2^-53 (1 - rho), of which those from K32 on
     (rho^K32 <= 2^-33 (1 - rho)) run in FP32 and the ones before in
     double-float; any other order sums its nodes (a resonant one outside the
@@ -185,10 +185,11 @@ def pole_sum_work_fast(system, species, kpar, oms, nmax):
             res = ((ppar[1] <= x) & (x < ppar[M])) | ((x < ppar[1]) & (x >= ppar[1] - M_I * dpp)) | \
                   ((x >= ppar[M - 1]) & (x < ppar[M - 1] + M_I * dpp))
             dd = (x - pcen) ** 2 + y ** 2
-            far = (~res) & (prad * prad < 0.5 * dd)
+            far = (~res) & (prad * prad < 0.58 * dd)
             rho = np.where(far, prad / np.sqrt(np.where(far, dd, 1.0)), 0.5)
-            K = np.where(far, np.ceil((36.7368005696771 - np.log1p(-rho)) / -np.log(rho)), kfar + 1)
-            K32 = np.where(far, np.ceil((22.8738569584782 - np.log1p(-rho)) / -np.log(rho)), kfar + 1)
+            # the kernel adds one term to each count for the rounding of its FP32 logarithms
+            K = np.where(far, np.ceil((36.7368005696771 - np.log1p(-rho)) / -np.log(rho)) + 1, kfar + 1)
+            K32 = np.where(far, np.ceil((22.8738569584782 - np.log1p(-rho)) / -np.log(rho)) + 1, kfar + 1)
             lau = K <= kfar
             out["series_df"] += np.minimum(K32, K)[lau].sum()
             out["series_fp32"] += np.maximum(K - K32, 0)[lau].sum()
