@@ -114,6 +114,7 @@ struct SpecDev {
   // bounds of the row deviation delta_i(p) = la p^2 + lb p + lc, smallest a0
   const double* lmom;
   double p2r, p3r, la, lb, lc, min_a0;
+  double lgc;  // exp(-p2r dppar^2)
   // relativistic species (src/ALPS_fns_rel.f90): (Gamma, pparbar) grid
   int relat, ng, np;
   const double* grel;   // [ng+1]

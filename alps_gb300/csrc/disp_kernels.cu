@@ -144,7 +144,16 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
     const float* __restrict__ Wl = S.Wl + (size_t)n * (M - 1) * 12;
     for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
       const int nn = sg ? -n : n;
-      const float sgf = (nn < 0) ? -1.0f : 1.0f;  // xy and xz are odd in n
+      // xy and xz are odd in n: a -n order adds to their vectors (6-9) with the minus sign:
+      // their sums are negated before and after it (exact)
+      auto flip_odd = [&]() {
+#pragma unroll
+        for (int q = 12; q < 20; ++q) {
+          sacc[q] = df_neg(sacc[q]);
+          Sf[q] = -Sf[q];
+        }
+      };
+      if (sg) flip_odd();
       // A = m omega_r - nn q, the pole's real part times k_par
       const dflt Ad = df_add(mox, df_neg(df_mul({(float)nn, 0.0f}, qsd)));
       const float x32 = Ad.h * ikp32;
@@ -225,8 +234,7 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
         const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
 #pragma unroll
         for (int q = 0; q < 12; ++q) {
-          const double f = fused_factor(n, q >> 1, z, a.sys.kperp, a.sys.kperp_norm, C0) *
-                           ((q >= 6 && q <= 9) ? (double)sgf : 1.0) / S.Wscale[q];
+          const double f = fused_factor(n, q >> 1, z, a.sys.kperp, a.sys.kperp_norm, C0) / S.Wscale[q];
           df_acc(sacc[2 * q], df_of(Sx[q].x * f));
           df_acc(sacc[2 * q + 1], df_of(Sx[q].y * f));
         }
@@ -253,23 +261,17 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
         for (; k < K32; k += js_count) {
           const float4* h4 = reinterpret_cast<const float4*>(mh + (size_t)k * 12);
           const float4* l4 = reinterpret_cast<const float4*>(ml + (size_t)k * 12);
-          const dflt ux = df_scale(tx, sgf), uy = df_scale(ty, sgf);
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
             const float4 h = __ldg(h4 + q), l = __ldg(l4 + q);
-            // vectors 4q..4q+3; 6..9 are xy and xz (odd in n)
-            const dflt ax0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? ux : tx, ay0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? uy : ty;
-            const dflt ax1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? ux : tx, ay1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? uy : ty;
-            const dflt ax2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? ux : tx, ay2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? uy : ty;
-            const dflt ax3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? ux : tx, ay3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? uy : ty;
-            df_mac(sacc[8 * q + 0], h.x, l.x, ax0);
-            df_mac(sacc[8 * q + 1], h.x, l.x, ay0);
-            df_mac(sacc[8 * q + 2], h.y, l.y, ax1);
-            df_mac(sacc[8 * q + 3], h.y, l.y, ay1);
-            df_mac(sacc[8 * q + 4], h.z, l.z, ax2);
-            df_mac(sacc[8 * q + 5], h.z, l.z, ay2);
-            df_mac(sacc[8 * q + 6], h.w, l.w, ax3);
-            df_mac(sacc[8 * q + 7], h.w, l.w, ay3);
+            df_mac(sacc[8 * q + 0], h.x, l.x, tx);
+            df_mac(sacc[8 * q + 1], h.x, l.x, ty);
+            df_mac(sacc[8 * q + 2], h.y, l.y, tx);
+            df_mac(sacc[8 * q + 3], h.y, l.y, ty);
+            df_mac(sacc[8 * q + 4], h.z, l.z, tx);
+            df_mac(sacc[8 * q + 5], h.z, l.z, ty);
+            df_mac(sacc[8 * q + 6], h.w, l.w, tx);
+            df_mac(sacc[8 * q + 7], h.w, l.w, ty);
           }
           df_cmul2(tx, ty, sx, sy, tx, ty);
         }
@@ -280,22 +282,17 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
           const float gx = sx.h + sx.l, gy = sy.h + sy.l;
           for (; k < K; k += js_count) {
             const float4* m4 = reinterpret_cast<const float4*>(mf + (size_t)k * 12);
-            const float ux = fx * sgf, uy = fy * sgf;
 #pragma unroll
             for (int q = 0; q < 3; ++q) {
               const float4 m = __ldg(m4 + q);
-              const float bx0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? ux : fx, by0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? uy : fy;
-              const float bx1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? ux : fx, by1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? uy : fy;
-              const float bx2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? ux : fx, by2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? uy : fy;
-              const float bx3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? ux : fx, by3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? uy : fy;
-              Sf[8 * q + 0] = fmaf(m.x, bx0, Sf[8 * q + 0]);
-              Sf[8 * q + 1] = fmaf(m.x, by0, Sf[8 * q + 1]);
-              Sf[8 * q + 2] = fmaf(m.y, bx1, Sf[8 * q + 2]);
-              Sf[8 * q + 3] = fmaf(m.y, by1, Sf[8 * q + 3]);
-              Sf[8 * q + 4] = fmaf(m.z, bx2, Sf[8 * q + 4]);
-              Sf[8 * q + 5] = fmaf(m.z, by2, Sf[8 * q + 5]);
-              Sf[8 * q + 6] = fmaf(m.w, bx3, Sf[8 * q + 6]);
-              Sf[8 * q + 7] = fmaf(m.w, by3, Sf[8 * q + 7]);
+              Sf[8 * q + 0] = fmaf(m.x, fx, Sf[8 * q + 0]);
+              Sf[8 * q + 1] = fmaf(m.x, fy, Sf[8 * q + 1]);
+              Sf[8 * q + 2] = fmaf(m.y, fx, Sf[8 * q + 2]);
+              Sf[8 * q + 3] = fmaf(m.y, fy, Sf[8 * q + 3]);
+              Sf[8 * q + 4] = fmaf(m.z, fx, Sf[8 * q + 4]);
+              Sf[8 * q + 5] = fmaf(m.z, fy, Sf[8 * q + 5]);
+              Sf[8 * q + 6] = fmaf(m.w, fx, Sf[8 * q + 6]);
+              Sf[8 * q + 7] = fmaf(m.w, fy, Sf[8 * q + 7]);
             }
             const float nx = fx * gx - fy * gy;
             fy = fx * gy + fy * gx;
@@ -308,24 +305,19 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
           const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
           const dflt r = df_rcp_approx(df_add(df_mul(dr, dr), D2));
           const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
-          const dflt Ur = df_scale(Rr, sgf), Ui = df_scale(Ri, sgf);
           const float4* vh4 = reinterpret_cast<const float4*>(Wh + (size_t)(j - 1) * 12);
           const float4* vl4 = reinterpret_cast<const float4*>(Wl + (size_t)(j - 1) * 12);
 #pragma unroll
           for (int q = 0; q < 3; ++q) {
             const float4 h = __ldg(vh4 + q), l = __ldg(vl4 + q);
-            const dflt ax0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? Ur : Rr, ay0 = (4 * q + 0 >= 6 && 4 * q + 0 <= 9) ? Ui : Ri;
-            const dflt ax1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? Ur : Rr, ay1 = (4 * q + 1 >= 6 && 4 * q + 1 <= 9) ? Ui : Ri;
-            const dflt ax2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? Ur : Rr, ay2 = (4 * q + 2 >= 6 && 4 * q + 2 <= 9) ? Ui : Ri;
-            const dflt ax3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? Ur : Rr, ay3 = (4 * q + 3 >= 6 && 4 * q + 3 <= 9) ? Ui : Ri;
-            df_mac(sacc[8 * q + 0], h.x, l.x, ax0);
-            df_mac(sacc[8 * q + 1], h.x, l.x, ay0);
-            df_mac(sacc[8 * q + 2], h.y, l.y, ax1);
-            df_mac(sacc[8 * q + 3], h.y, l.y, ay1);
-            df_mac(sacc[8 * q + 4], h.z, l.z, ax2);
-            df_mac(sacc[8 * q + 5], h.z, l.z, ay2);
-            df_mac(sacc[8 * q + 6], h.w, l.w, ax3);
-            df_mac(sacc[8 * q + 7], h.w, l.w, ay3);
+            df_mac(sacc[8 * q + 0], h.x, l.x, Rr);
+            df_mac(sacc[8 * q + 1], h.x, l.x, Ri);
+            df_mac(sacc[8 * q + 2], h.y, l.y, Rr);
+            df_mac(sacc[8 * q + 3], h.y, l.y, Ri);
+            df_mac(sacc[8 * q + 4], h.z, l.z, Rr);
+            df_mac(sacc[8 * q + 5], h.z, l.z, Ri);
+            df_mac(sacc[8 * q + 6], h.w, l.w, Rr);
+            df_mac(sacc[8 * q + 7], h.w, l.w, Ri);
           }
         };
         for (int j = 1 + js; j <= M - 1; j += js_count) {
@@ -345,6 +337,7 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
           }
         }
       }
+      if (sg) flip_odd();
     }
   }
   // rescale and combine: acc_e = phase_e (omega S_{e,1} + kappa S_{e,2})
@@ -1298,8 +1291,19 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
             return acc;
           };
           const double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
-          // the row Gaussian at p, p + dppar, p - dppar
-          const double2 G0 = gauss(p), Gp = gauss(xp), Gm = gauss(xm);
+          // the row Gaussian at p, p + dppar, p - dppar:
+          // G(p +- pd) = G(p) exp(-+2 p2r pd d) exp(-p2r pd^2), d = p - p3r
+          const double2 G0 = gauss(p);
+          const double2 ax = cscale(cmk(p.x - S.p3r, p.y), -2.0 * S.p2r * pd);
+          double2 Gp, Gm;
+          if (fabs(ax.x) < 600.0) {
+            const double2 X = cexp_d(ax), Gc = cscale(G0, S.lgc);
+            Gp = cmul(Gc, X);
+            Gm = cmul(Gc, crcp(X));
+          } else {
+            Gp = gauss(xp);
+            Gm = gauss(xm);
+          }
           const bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
                             (cabs_(G0) * S.min_a0 == 0.0);
           if (!zero) {
@@ -2315,6 +2319,7 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->lb = S.lb;
   o->lc = S.lc;
   o->min_a0 = S.min_a0;
+  o->lgc = std::exp(-S.p2r * (S.ppar[2] - S.ppar[1]) * (S.ppar[2] - S.ppar[1]));
   o->relat = S.sp.relat ? 1 : 0;
   o->ng = c->sys.ngamma;
   o->np = c->sys.npparbar;
