@@ -164,14 +164,17 @@ __device__ __forceinline__ dflt df_rcp(dflt a) {
   const dflt e = df_add({1.0f, 0.0f}, df_neg(df_mul(a, {r0, 0.0f})));
   return df_add({r0, 0.0f}, df_mul({r0, 0.0f}, e));
 }
-// 1/a from the FP32 approximate reciprocal (within 1 ulp) and one Newton
-// step in double-float: relative error about 2^-46.  a must be a normal
-// float pair (no zero, no FP32 underflow).
+// 1/a from the FP32 approximate reciprocal r0 (within 1 ulp):
+// d = 1 - a r0 (|d| <= 2^-22; 1 - a.h r0 is exact in one FMA), and
+// 1/a = r0 (1 + d + d^2 + ...), so 1/a = r0 + r0 (d + d^2) with an error of
+// about 2^-45 relative (d^3 <= 2^-66; three roundings of 2^-24 of terms
+// below 2^-22).  The pair is returned unnormalised (|l| <= 2^-21 |h|), which
+// df_mul and df_add accept.  a must be a normal float pair.
 __device__ __forceinline__ dflt df_rcp_approx(dflt a) {
   float r0;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r0) : "f"(a.h));
-  const dflt e = df_add({1.0f, 0.0f}, df_neg(df_mul(a, {r0, 0.0f})));
-  return df_add({r0, 0.0f}, df_mul({r0, 0.0f}, e));
+  const float d = __fmaf_rn(-a.l, r0, __fmaf_rn(-a.h, r0, 1.0f));
+  return {r0, __fmul_rn(r0, __fmaf_rn(d, d, d))};
 }
 // acc += c, the low part unnormalised until the end
 __device__ __forceinline__ void df_acc(dflt& acc, dflt c) {

@@ -151,10 +151,11 @@ def pole_sum_flops_issued(nmax, npar):
 # FP32-pipe flops (FMA = 2) of one double-float node of the fast path's pole
 # sums, counted from the kernel's code (device_math.cuh, disp_kernels.cu):
 # the pole distance d = A - k_par p_j (19), |d|^2 + D^2 (19), its reciprocal
-# (rcp + one double-float Newton step, 39), the two weights (22) and 24
-# double-float multiply-accumulates of the 12 reduced vectors against them
-# (15 each: product with its error term, two-sum into the accumulator)
-DF_NODE_FLOPS = 19 + 19 + 39 + 22 + 24 * 15
+# (rcp and three FMA / one multiply of its series correction, 8), the two
+# weights (22) and 24 double-float multiply-accumulates of the 12 reduced
+# vectors against them (15 each: product with its error term, two-sum into
+# the accumulator)
+DF_NODE_FLOPS = 19 + 19 + 8 + 22 + 24 * 15
 # one double-float Laurent term: 24 multiply-accumulates of the 12 moments
 # against the complex power (15 each) and the power update (4 products, 2 sums)
 DF_TERM_FLOPS = 24 * 15 + 4 * 9 + 2 * 10
