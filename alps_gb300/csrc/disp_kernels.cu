@@ -2319,7 +2319,7 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->lb = S.lb;
   o->lc = S.lc;
   o->min_a0 = S.min_a0;
-  o->lgc = std::exp(-S.p2r * (S.ppar[2] - S.ppar[1]) * (S.ppar[2] - S.ppar[1]));
+  o->lgc = std::exp(-S.p2r * o->dppar * o->dppar);  // dppar is 0 for closed-form species (no grid)
   o->relat = S.sp.relat ? 1 : 0;
   o->ng = c->sys.ngamma;
   o->np = c->sys.npparbar;
