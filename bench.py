@@ -223,7 +223,9 @@ def run_reference(args, w, mp, rank, world):
     P = po.OraclePlasma(system, species)
     P.set_k(system.kperp, system.kpar)
     oms = lattice(mp)
-    budget = float(os.environ.get("ALPS_REF_STEP_S", "8"))
+    # each step a bounded sample: about 8 s, less when many steps are asked
+    # for, so that the whole run stays near two minutes
+    budget = min(float(os.environ.get("ALPS_REF_STEP_S", "8")), max(0.5, 120.0 / max(1, args.steps)))
     for _ in range(args.warmup):
         cpu_sample(P, oms, min(budget, 2.0), nthreads)
     rates, ms = [], []
