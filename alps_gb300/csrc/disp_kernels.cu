@@ -15,14 +15,22 @@
 //   k_stage             a lone batch's arguments and job to device memory
 //   k_classify_multi    resonant orders of each (omega, species) into
 //                       fixed slots, one warp per (omega, species)
-//   k_pole_sums_multi   the FP64-bound pole sums over all orders: order
-//                       chunks x omega tiles x node slices
+//   k_pole_sums_multi   the pole sums over all orders: order chunks x omega
+//                       tiles x node slices.  Plain path in FP64; fast path
+//                       (pole_fused) in double-float on the FP32 pipes, all
+//                       orders of a chunk in one set of sums
 //   k_resonant_multi    principal value + Landau per resonant (omega,
-//                       species, n): scalar work one item per lane, vector
-//                       work one item per warp
+//                       species, n): occupied slots gathered into batches
+//                       of 32; scalar work one item per lane, vector work
+//                       one item per warp (fast path: pv_fast, double-float)
 //   k_finalize_multi    chi, epsilon, wave tensor and det, one thread (or
 //                       warp) per omega; sums in a fixed order, so results
 //                       do not depend on timing or on the other jobs.
+//
+// Double-float (fast path): a value is a pair of floats h + l (about 46-48
+// bits) handled with error-free transformations (device_math.cuh); GB300
+// runs FP32 at 64 times its FP64 rate.  Resonance decisions, windows and
+// sample points are the reference's on both paths.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
