@@ -346,6 +346,11 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
         }
       }
       if (sg) flip_odd();
+      // the low parts, added to without normalisation inside the order,
+      // are folded back so that their FP32 roundings do not grow over the
+      // chunk's orders
+#pragma unroll
+      for (int q = 0; q < 24; ++q) sacc[q] = df_two_sum(sacc[q].h, sacc[q].l);
     }
   }
   // rescale and combine: acc_e = phase_e (omega S_{e,1} + kappa S_{e,2})
