@@ -124,10 +124,12 @@ __device__ __forceinline__ void df_cmul2(dflt ax, dflt ay, dflt bx, dflt by, dfl
 // tables (C0 and the T-tensor prefactors folded into the reduced vectors and
 // their Laurent moments, one scale per vector).  Per (omega, signed order):
 // an FP32 test settles orders far from resonance (the FP64 geometry decides
-// the rest), then either the Laurent series (far poles, leading terms in
-// double-float from f / d^... , the tail in FP32) or the node sum in
-// double-float.  Once per chunk the sums are rescaled and combined,
-// acc_e = phase_e (omega S_{e,1} + kappa S_{e,2}), in FP64.
+// the rest), then either the Laurent series (far poles: the terms
+// mom_k f t^k with f = 1/(k_par d), t = prad/d, leading terms in
+// double-float, the tail in FP32) or the node sum in double-float.  The odd
+// entries of a -n order enter with the minus sign, and the sums are
+// renormalised after each order.  Once per chunk they are rescaled and
+// combined, acc_e = phase_e (omega S_{e,1} + kappa S_{e,2}), in FP64.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, double2 o, int js, int js_count,
                                            int n_begin, int n_end, double2* acc) {
@@ -867,9 +869,10 @@ __device__ inline double2 crcp(double2 z) {
 // double-float arithmetic on the FP32 pipes, on the reduced vectors' float
 // pairs (scaled by 2^-e for order n; the result is rescaled at the end).
 // The pieces are still chosen from the FP64 sample points wherever the FP32
-// estimate is within 1e-3 of a half-way point.  Returns false, with nothing
-// written to T, when a range would leave the normal floats or the merge does
-// not apply (the caller then runs the FP64 code); otherwise adds the item's
+// estimate lies within its error bound of a half-way point.  Returns false,
+// with nothing written to out, when the item's constants were not formed
+// (a range would leave the normal floats) or the merge does not apply (the
+// caller then runs the FP64 code); otherwise adds the item's
 // principal-value part to out (entry e: pref_e T_e times the window scale).
 // ---------------------------------------------------------------------------
 struct PvSlotF {
