@@ -200,6 +200,27 @@ def pole_sum_work_fast(system, species, kpar, oms, nmax):
     return {k: float(v) for k, v in out.items()}
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the
+    machine type)."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_sample(P, oms, budget_s, nthreads):
     """Times the oracle on a bounded sample of the lattice; returns evals/s."""
     t0 = time.perf_counter()
@@ -241,6 +262,7 @@ def run_reference(args, w, mp, rank, world):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference", "config": config_dict(w, mp.nr, mp.ni, world),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                             "cpu_model": cpu_model(),
                              "sample": "per step %d lattice points of the map, oracle threads over points" % m},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "wall_s": wall}
@@ -495,9 +517,13 @@ def main():
         P = po.OraclePlasma(system, species)
         P.set_k(s.kperp, kpar)
         r, m, dt = cpu_sample(P, oms, float(os.environ.get("ALPS_CPU_BASELINE_S", "10")), nthreads)
-        cpu = {"value": r, "unit": UNIT, "cores": nthreads, "kind": "port",
+        # the same restatement on one core, a smaller sample
+        r1, m1, dt1 = cpu_sample(P, oms, 3.0, 1)
+        cpu = {"value": r, "unit": UNIT, "cores": nthreads, "kind": "port", "cpu_model": cpu_model(),
                "sample": "%d lattice points of the same map (every %d-th), oracle threads over points, %.1f s"
-                         % (m, max(1, n // m), dt)}
+                         % (m, max(1, n // m), dt),
+               "single_core": {"value": r1, "unit": UNIT, "cores": 1,
+                               "sample": "%d lattice points, %.1f s" % (m1, dt1)}}
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
