@@ -62,6 +62,7 @@ def lib():
             "alps_disp_batch": ([vp, C.c_int, cp, cp], C.c_int),
             "alps_disp_batch_device": ([vp, C.c_int, vp, vp, vp], C.c_int),
             "alps_secant": ([vp, C.c_int, C.c_int, cp, P(C.c_int), cp], C.c_int),
+            "alps_secant_ex": ([vp, C.c_int, C.c_int, cp, C.c_double, P(C.c_int), cp, P(C.c_int)], C.c_int),
             "alps_map": ([vp, P(_abi.alps_map_params), cp, cp, dp], C.c_int),
             "alps_find_minima": ([dp, C.c_int, C.c_int, C.c_int, P(C.c_int), P(C.c_int)], C.c_int),
             "alps_run_input": ([C.c_char_p, C.c_char_p], C.c_int),
@@ -71,6 +72,9 @@ def lib():
             "alps_get_stats": ([vp, P(_abi.alps_stats)], C.c_int),
             "alps_set_profiling": ([vp, C.c_int], C.c_int),
             "alps_disp_batch_noalloc": ([vp, C.c_int, vp, vp, vp, P(C.c_size_t)], C.c_int),
+            "alps_batch_status": ([vp, vp], C.c_int),
+            "alps_solve_many": ([P(vp), C.c_int, C.c_int, cp, C.c_double, P(C.c_int), cp, P(C.c_int)], C.c_int),
+            "alps_tc_product": ([vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int)], C.c_int),
             "alps_get_profile": ([vp, dp, P(C.c_int64)], C.c_int),
             "alps_interpolate": ([dp, dp, dp, C.c_int, P(_abi.alps_interp_params), dp, dp, dp], C.c_int),
             "alps_run_interpolation": ([C.c_char_p, C.c_char_p], C.c_int),
@@ -95,8 +99,8 @@ def exported_symbols():
         "alps_version", "alps_error_string", "alps_system_defaults", "alps_species_defaults", "alps_create",
         "alps_destroy", "alps_set_species", "alps_prepare", "alps_get_fit", "alps_set_fit", "alps_set_k",
         "alps_get_nmax", "alps_set_precision", "alps_disp", "alps_disp_batch", "alps_disp_batch_device",
-        "alps_secant", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
-        "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_read_input", "alps_read_f0",
+        "alps_secant", "alps_secant_ex", "alps_solve_many", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
+        "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_batch_status", "alps_tc_product", "alps_read_input", "alps_read_f0",
         "alps_get_f0_rel", "alps_calc_eigen", "alps_server_create", "alps_server_destroy", "alps_server_submit",
         "alps_server_poll", "alps_server_wait", "alps_server_stats", "alps_interpolate", "alps_run_interpolation",
     ]

@@ -181,6 +181,11 @@ class Plasma:
         check(lib().alps_disp_batch_device(self._h, n, C.c_void_p(d_om_ptr), C.c_void_p(d_D_ptr),
                                            C.c_void_p(stream_ptr or 0)), "alps_disp_batch_device")
 
+    def batch_status(self, stream_ptr=None):
+        """Status code of the last asynchronous batch (alps_batch_status):
+        0, or the ALPS_E_* code of a device error; waits for the stream."""
+        return lib().alps_batch_status(self._h, C.c_void_p(stream_ptr or 0))
+
     def secant(self, oms, method=None):
         """Polishes roots in place; returns (roots, iterations, det at root)."""
         if method is None:
@@ -190,6 +195,19 @@ class Plasma:
         Df = np.zeros_like(oms)
         check(lib().alps_secant(self._h, method, len(oms), _cptr(oms), it, _cptr(Df)), "alps_secant")
         return oms, list(it), Df
+
+    def polish(self, oms, om_rtol=1e-12, method=None):
+        """Secant polish with the relative-step stop (alps_secant_ex):
+        returns (roots, iterations, det at root, converged mask)."""
+        if method is None:
+            method = self.sys.secant_method
+        oms = np.atleast_1d(np.ascontiguousarray(oms, dtype=np.complex128)).copy()
+        it = (C.c_int * len(oms))()
+        cv = (C.c_int * len(oms))()
+        Df = np.zeros_like(oms)
+        check(lib().alps_secant_ex(self._h, method, len(oms), _cptr(oms), float(om_rtol), it, _cptr(Df), cv),
+              "alps_secant_ex")
+        return oms, list(it), Df, np.array(list(cv), dtype=bool)
 
     def calc_eigen(self, oms, eigen=True, heat=True):
         """calc_eigen for each root in oms: a list of alps_eigen (fields
@@ -406,6 +424,22 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def solve_many(plasmas, guesses, om_rtol=1e-12, method=2):
+    """alps_solve_many: guesses[r] polished on plasmas[r] (each a Plasma at
+    its own k), all on the device in one graph launch.  Returns (roots,
+    iterations, det at root, converged mask)."""
+    n = len(plasmas)
+    oms = np.ascontiguousarray(np.asarray(guesses, dtype=np.complex128)).copy()
+    handles = (C.c_void_p * n)(*[p.handle.value if isinstance(p.handle, C.c_void_p) else p.handle
+                                 for p in plasmas])
+    it = (C.c_int * n)()
+    cv = (C.c_int * n)()
+    Df = np.zeros_like(oms)
+    check(lib().alps_solve_many(handles, n, int(method), _cptr(oms), float(om_rtol), it, _cptr(Df), cv),
+          "alps_solve_many")
+    return oms, np.array(list(it)), Df, np.array(list(cv), dtype=bool)
 
 
 def scan_def(type_s, swi, swf, log_scan, n_out, n_res, kperp, kpar):

@@ -13,8 +13,8 @@ OBJDIR = os.path.join(LIBDIR, "obj")
 LIB = os.path.join(LIBDIR, "libalps_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC = os.environ.get("NVCC", "nvcc")
-SOURCES = ["setup_kernels.cu", "disp_kernels.cu", "rel_kernels.cu", "nhds_kernels.cu", "server.cu", "alps_api.cu", "host_tools.cpp", "host_io.cpp"]
-HEADERS = ["alps_internal.cuh", "device_math.cuh", "root_finders.h"]
+SOURCES = ["tc_gemm.cu", "batch_solve.cu", "setup_kernels.cu", "disp_kernels.cu", "rel_kernels.cu", "nhds_kernels.cu", "server.cu", "alps_api.cu", "host_tools.cpp", "host_io.cpp"]
+HEADERS = ["alps_internal.cuh", "device_math.cuh", "root_finders.h", "root_machine.cuh", "tc_gemm.cuh"]
 
 
 def _flags(src):

@@ -14,6 +14,7 @@
 
 #include "alps_internal.cuh"
 #include "root_finders.h"
+#include "tc_gemm.cuh"
 
 namespace {
 thread_local char g_last_err[512] = "";
@@ -127,6 +128,10 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_bessel);
     cudaFree(S.d_V);
     cudaFree(S.d_A);
+    cudaFree(S.d_tcws);
+    cudaFree(S.d_nmax);
+    cudaFree(S.d_words);
+    cudaFree(S.d_fit_scratch);
     cudaFree(S.d_Rw);
     cudaFree(S.d_G);
     cudaFree(S.d_X);
@@ -409,8 +414,12 @@ int alps_get_nmax(alps_ctx* c, int* nmax) {
 int alps_set_precision(alps_ctx* c, int precision) {
   if (!c) return ALPS_E_INVALID;
   if (precision != ALPS_PREC_FP64 && precision != ALPS_PREC_MIXED) return ALPS_E_INVALID;
+  const bool changed = c->precision != precision;
   c->precision = precision;
   c->gen++;
+  // the p_perp contraction is part of the precision path (FP64 on the plain
+  // path, the tensor cores on the mixed one): rebuild the k tables
+  if (changed && c->kset) return alps_set_k(c, c->kperp, c->kpar);
   return ALPS_OK;
 }
 
@@ -498,8 +507,24 @@ int alps_disp_batch_device(alps_ctx* c, int n, const alps_complex* d_om, alps_co
   if (!c || n < 0 || !c->kset) return ALPS_E_INVALID;
   if (n == 0) return ALPS_OK;
   cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
-  return launch_disp_batch(c, n, reinterpret_cast<const double2*>(d_om), reinterpret_cast<double2*>(d_D), nullptr,
-                           st);
+  int rc = launch_disp_batch(c, n, reinterpret_cast<const double2*>(d_om), reinterpret_cast<double2*>(d_D), nullptr,
+                             st);
+  if (rc == ALPS_OK) c->async_flags = c->d_flags;
+  return rc;
+}
+
+// The device error word of the last asynchronous batch, read after the
+// batch's stream has drained.  Reads 4 bytes with cudaMemcpy into a stack
+// variable: no allocation, so it serves the no-allocation entry point too.
+int alps_batch_status(alps_ctx* c, void* stream) {
+  if (!c) return ALPS_E_INVALID;
+  if (!c->async_flags) return ALPS_OK;
+  cudaStream_t st = stream ? (cudaStream_t)stream : c->stream;
+  ALPS_CUDA_TRY(cudaStreamSynchronize(st));
+  int f = 0;
+  ALPS_CUDA_TRY(cudaMemcpy(&f, c->async_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (f & 2) return ALPS_E_SUBLUMINAL;
+  return f ? ALPS_E_INVALID : ALPS_OK;
 }
 
 // calc_eigen (src/ALPS_fns.f90:2605-2899) for n roots; the det D evaluations
@@ -659,24 +684,46 @@ int alps_get_profile(alps_ctx* c, double* ms, int64_t* batches) {
 int alps_get_stats(alps_ctx* c, alps_stats* st) {
   if (!c || !st) return ALPS_E_INVALID;
   *st = c->stats;
+  st->tc_contractions = 0;
+  st->tc_fixed_entries = 0;
+  st->tc_entries = 0;
+  for (const auto& S : c->spec)
+    if (S.tc_used) {
+      st->tc_contractions++;
+      st->tc_fixed_entries += S.tc_fixed;
+      st->tc_entries += (int64_t)3 * (S.nmax + 1) * 2 * (c->sys.npar - 1);
+    }
   return ALPS_OK;
 }
 
+int alps_tc_product(const double* d_A, const double* d_B, double* d_C, int M, int N, int K, int checked,
+                    int* nfixed) {
+  if (!d_A || !d_B || !d_C || M < 1 || N < 1 || K < 1 || K > 256) return ALPS_E_INVALID;
+  const size_t need = checked ? tc_checked_workspace_bytes(M, N, K) : tc_workspace_bytes(M, N, K);
+  void* ws = nullptr;
+  ALPS_CUDA_TRY(cudaMalloc(&ws, need));
+  int fixed = 0, rc;
+  if (checked)
+    rc = tc_product_checked(d_A, d_B, d_C, M, N, K, ws, &fixed, 0);
+  else
+    rc = tc_product(d_A, K, 1, d_B, N, 1, d_C, N, 1, M, N, K, 1.0, 0.0, nullptr, ws, nullptr, 0);
+  if (!rc && cudaStreamSynchronize(0) != cudaSuccess) rc = ALPS_E_CUDA;
+  if (!rc && !checked) rc = tc_check(ws, M, N, K);
+  cudaFree(ws);
+  if (nfixed) *nfixed = fixed;
+  return rc;
+}
 
-int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iters, alps_complex* Dfinal) {
+
+int alps_secant_ex(alps_ctx* c, int method, int nroots, alps_complex* om, double om_rtol, int* iters,
+                   alps_complex* Dfinal, int* converged) {
   if (!c || !c->kset || nroots < 0 || (nroots > 0 && !om)) return ALPS_E_INVALID;
-  if (method < 0 || method > 2) return ALPS_E_INVALID;
-  std::vector<SecantOsc> so(method == 2 ? nroots : 0);
-  std::vector<SecantPlain> sp(method == 0 ? nroots : 0);
-  std::vector<Rtsec> rt(method == 1 ? nroots : 0);
-  std::vector<std::vector<cplx>> want(nroots), got(nroots);
-  for (int r = 0; r < nroots; ++r) {
-    cplx o(om[r].re, om[r].im);
-    if (method == 2) { so[r].sy = &c->sys; so[r].om = o; want[r] = so[r].step({}); }
-    if (method == 0) { sp[r].sy = &c->sys; sp[r].om = o; want[r] = sp[r].step({}); }
-    if (method == 1) { rt[r].sy = &c->sys; rt[r].xin = o; want[r] = rt[r].step({}); }
-  }
+  if (method < 0 || method > 2 || !(om_rtol >= 0.0)) return ALPS_E_INVALID;
+  std::vector<RootMachine> rm(nroots);
+  std::vector<std::vector<cplx>> want(nroots);
+  for (int r = 0; r < nroots; ++r) want[r] = rm[r].start(&c->sys, method, cplx(om[r].re, om[r].im), om_rtol);
   std::vector<alps_complex> bom, bD;
+  std::vector<cplx> got;
   for (int round = 0; round < 100000; ++round) {
     bom.clear();
     for (int r = 0; r < nroots; ++r)
@@ -687,25 +734,24 @@ int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iter
     if (st) return st;
     size_t k = 0;
     for (int r = 0; r < nroots; ++r) {
-      got[r].clear();
-      for (size_t q = 0; q < want[r].size(); ++q, ++k) got[r].push_back(cplx(bD[k].re, bD[k].im));
       if (want[r].empty()) continue;
-      if (method == 2) want[r] = so[r].step(got[r]);
-      if (method == 0) want[r] = sp[r].step(got[r]);
-      if (method == 1) want[r] = rt[r].step(got[r]);
+      got.clear();
+      for (size_t q = 0; q < want[r].size(); ++q, ++k) got.push_back(cplx(bD[k].re, bD[k].im));
+      want[r] = rm[r].step(got);
     }
   }
   for (int r = 0; r < nroots; ++r) {
-    cplx o, df;
-    int it;
-    if (method == 2) { o = so[r].om; df = so[r].Dfin; it = so[r].iter; }
-    else if (method == 0) { o = sp[r].om; df = sp[r].Dfin; it = sp[r].iter; }
-    else { o = rt[r].om; df = rt[r].Dfin; it = rt[r].j; }
+    const cplx o = rm[r].root(), df = rm[r].dfinal();
     om[r] = alps_complex{o.real(), o.imag()};
-    if (iters) iters[r] = it;
+    if (iters) iters[r] = rm[r].iters();
     if (Dfinal) Dfinal[r] = alps_complex{df.real(), df.imag()};
+    if (converged) converged[r] = rm[r].converged() ? 1 : 0;
   }
   return ALPS_OK;
+}
+
+int alps_secant(alps_ctx* c, int method, int nroots, alps_complex* om, int* iters, alps_complex* Dfinal) {
+  return alps_secant_ex(c, method, nroots, om, 0.0, iters, Dfinal, nullptr);
 }
 
 // map_search values (src/ALPS_fns.f90:3595-3788)

@@ -159,6 +159,14 @@ struct SpeciesHost {
   size_t V_cap = 0;
   double* d_A = nullptr;                  // contraction output scratch
   size_t A_cap = 0;
+  void* d_tcws = nullptr;                 // tensor-core contraction workspace (mixed path)
+  size_t tcws_cap = 0;
+  int tc_used = 0;                        // the current reduced vectors came from the tensor cores
+  int tc_fixed = 0;                       // of their entries, recomputed in FP64
+  int* d_nmax = nullptr;                  // determine_nmax's result word
+  double* d_words = nullptr;              // ee term and fit status words of prepare
+  double* d_fit_scratch = nullptr;        // Levenberg-Marquardt scratch
+  size_t fit_scratch_cap = 0;
   double* d_Rw = nullptr;                 // weighted Bessel rows scratch
   size_t Rw_cap = 0;
   double* d_G = nullptr;                  // contraction RHS [2][N-1][M-1]
@@ -227,6 +235,10 @@ struct alps_ctx {
   size_t bm_cap = 0;
   size_t ext_cap = 0;
   int* d_flags = nullptr;       // error flags
+  // error word of the last asynchronous batch (alps_disp_batch_device: d_flags;
+  // alps_disp_batch_noalloc: a word of the static scratch), read by
+  // alps_batch_status
+  const int* async_flags = nullptr;
   alps_stats stats = {};
   // profiling: pending event sets (5 events per batch) and totals
   bool profiling = false;
@@ -292,6 +304,22 @@ struct MultiScratch;
 int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
                       MultiScratch** scratch, cudaStream_t st);
 void multi_scratch_free(MultiScratch* m);
+// The same split in two: prepare_disp_multi builds and uploads the job table
+// and sizes the scratch (host work, synchronous allocations);
+// run_disp_multi launches the kernels of a prepared batch (device work only,
+// so it can be captured, also into a conditional graph body).  The prepared
+// batch stays valid while the contexts, their k and precision and the
+// scratch are unchanged.
+struct MultiLaunch {
+  const void* jobs;  // device job table
+  int nj;
+  long blocks[4];    // grids of classify, pole sums, resonant, finalize
+  size_t smem;       // dynamic shared memory of k_resonant_multi
+  int* flags;        // error words, one per job
+};
+int prepare_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
+                       MultiScratch** scratch, cudaStream_t st, MultiLaunch* out);
+int run_disp_multi(const MultiLaunch& ml, cudaStream_t st);
 bool ctx_fusable(const alps_ctx* c);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);
 int collect_profile(alps_ctx* c);

@@ -2622,6 +2622,14 @@ int ctx_device_args(alps_ctx* c, cudaStream_t st, const DispArgs** out) {
 int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
                       MultiScratch** scratch, cudaStream_t st) {
   if (nj <= 0) return ALPS_OK;
+  MultiLaunch ml;
+  int rc = prepare_disp_multi(ctx, n, nj, d_om, d_D, d_flags, scratch, st, &ml);
+  if (rc) return rc;
+  return run_disp_multi(ml, st);
+}
+
+int prepare_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
+                       MultiScratch** scratch, cudaStream_t st, MultiLaunch* out) {
   MultiScratch* m = *scratch;
   if (!m) *scratch = m = new MultiScratch();
   if ((size_t)nj > m->jobs_cap) {
@@ -2699,15 +2707,27 @@ int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2*
     J.items = m->items + o_slots[j] * 6;
   }
   ALPS_CUDA_TRY(cudaMemcpyAsync(m->d_jobs, m->h_jobs, (size_t)nj * sizeof(DispJob), cudaMemcpyHostToDevice, st));
-  ALPS_CUDA_TRY(cudaMemsetAsync(d_flags, 0, (size_t)nj * sizeof(int), st));
   if ((rcode = res_smem_optin(smem))) return rcode;
-  k_classify_multi<<<(unsigned)blk[0], 128, 0, st>>>(m->d_jobs, nj);
+  out->jobs = m->d_jobs;
+  out->nj = nj;
+  for (int k = 0; k < 4; ++k) out->blocks[k] = blk[k];
+  out->smem = smem;
+  out->flags = d_flags;
+  return ALPS_OK;
+}
+
+// The kernels of a prepared fused batch (no host work: capturable, also
+// inside a conditional graph body).
+int run_disp_multi(const MultiLaunch& ml, cudaStream_t st) {
+  const DispJob* jobs = static_cast<const DispJob*>(ml.jobs);
+  ALPS_CUDA_TRY(cudaMemsetAsync(ml.flags, 0, (size_t)ml.nj * sizeof(int), st));
+  k_classify_multi<<<(unsigned)ml.blocks[0], 128, 0, st>>>(jobs, ml.nj);
   ALPS_CUDA_TRY(cudaGetLastError());
-  k_pole_sums_multi<false><<<(unsigned)blk[1], 128, 0, st>>>(m->d_jobs, nj);
+  k_pole_sums_multi<false><<<(unsigned)ml.blocks[1], 128, 0, st>>>(jobs, ml.nj);
   ALPS_CUDA_TRY(cudaGetLastError());
-  k_resonant_multi<<<(unsigned)blk[2], RES_WARPS * 32, smem, st>>>(m->d_jobs, nj);
+  k_resonant_multi<<<(unsigned)ml.blocks[2], RES_WARPS * 32, ml.smem, st>>>(jobs, ml.nj);
   ALPS_CUDA_TRY(cudaGetLastError());
-  k_finalize_multi<<<(unsigned)blk[3], 128, 0, st>>>(m->d_jobs, nj);
+  k_finalize_multi<<<(unsigned)ml.blocks[3], 128, 0, st>>>(jobs, ml.nj);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }
@@ -2732,7 +2752,10 @@ int launch_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2*
 // stream capture.  Every call shares the one array: two calls whose kernels
 // overlap on the GPU (different streams, or different host threads) race on
 // it and must be ordered by the caller.  The error flag is cleared at the
-// start of every call; every other word a call reads it writes first.
+// start of every call; every other word a call reads it writes first.  The
+// flag word's device address is recorded in the context, so
+// alps_batch_status reports the call's device errors (read it before the
+// next call on the device clears the word).
 // ===========================================================================
 #define ALPS_NOALLOC_SCRATCH_BYTES (16u << 20)
 #define ALPS_NOALLOC_MAX_DEVICES 64
@@ -2833,5 +2856,6 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   }
   k_finalize_multi<<<(unsigned)fin_blocks(sh, n), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
+  c->async_flags = flags;  // alps_batch_status reads the word before the next call clears it
   return ALPS_OK;
 }

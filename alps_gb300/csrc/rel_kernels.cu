@@ -15,9 +15,14 @@
 // the Lorentz factor in resU (src/ALPS_fns.f90:799-864, 1560-1596) or the
 // Gamma-row integrals with their principal-value windows and the Landau term
 // (integrate_res_rel :460-913, landau_integrate_rel :1005-1092).
+#include <dlfcn.h>
+
 #include <algorithm>
 #include <cmath>
+#include <mutex>
 #include <vector>
+
+#include <cusolverDn.h>
 
 #include "alps_internal.cuh"
 #include "device_math.cuh"
@@ -315,6 +320,86 @@ __global__ void k_interp_finish(const double* __restrict__ g, const double* __re
 
 }  // namespace
 
+// ---------------------------------------------------------------------------
+// Large spline systems: cuSOLVER's blocked LU with partial pivoting (getrf,
+// getrs: the dgesv pair), loaded on first use.  The column-by-column LU above
+// restates dgesv's arithmetic for the sizes the oracle can check; from
+// TPS_BLOCKED_M unknowns on (a 128 x 256 input grid has 33 156) its one pass
+// per column would take minutes, and the blocked factorisation runs at the
+// FP64 GEMM rate instead.
+// ---------------------------------------------------------------------------
+#define TPS_BLOCKED_M 4096
+
+struct CusolverApi {
+  bool tried = false, ok = false;
+  cusolverStatus_t (*create)(cusolverDnHandle_t*) = nullptr;
+  cusolverStatus_t (*destroy)(cusolverDnHandle_t) = nullptr;
+  cusolverStatus_t (*set_stream)(cusolverDnHandle_t, cudaStream_t) = nullptr;
+  cusolverStatus_t (*getrf_ws)(cusolverDnHandle_t, int, int, double*, int, int*) = nullptr;
+  cusolverStatus_t (*getrf)(cusolverDnHandle_t, int, int, double*, int, double*, int*, int*) = nullptr;
+  cusolverStatus_t (*getrs)(cusolverDnHandle_t, cublasOperation_t, int, int, const double*, int, const int*,
+                            double*, int, int*) = nullptr;
+};
+std::mutex g_cusolver_mu;
+CusolverApi g_cusolver;
+
+const CusolverApi* cusolver_api() {
+  std::lock_guard<std::mutex> lk(g_cusolver_mu);
+  if (g_cusolver.tried) return g_cusolver.ok ? &g_cusolver : nullptr;
+  g_cusolver.tried = true;
+  const char* names[] = {"libcusolver.so.12", "libcusolver.so", "/usr/local/cuda/lib64/libcusolver.so.12",
+                         "/usr/local/cuda/lib64/libcusolver.so"};
+  void* h = nullptr;
+  for (const char* nm : names)
+    if ((h = dlopen(nm, RTLD_NOW | RTLD_LOCAL))) break;
+  if (!h) return nullptr;
+  CusolverApi& a = g_cusolver;
+  a.create = reinterpret_cast<decltype(a.create)>(dlsym(h, "cusolverDnCreate"));
+  a.destroy = reinterpret_cast<decltype(a.destroy)>(dlsym(h, "cusolverDnDestroy"));
+  a.set_stream = reinterpret_cast<decltype(a.set_stream)>(dlsym(h, "cusolverDnSetStream"));
+  a.getrf_ws = reinterpret_cast<decltype(a.getrf_ws)>(dlsym(h, "cusolverDnDgetrf_bufferSize"));
+  a.getrf = reinterpret_cast<decltype(a.getrf)>(dlsym(h, "cusolverDnDgetrf"));
+  a.getrs = reinterpret_cast<decltype(a.getrs)>(dlsym(h, "cusolverDnDgetrs"));
+  a.ok = a.create && a.destroy && a.set_stream && a.getrf_ws && a.getrf && a.getrs;
+  return a.ok ? &a : nullptr;
+}
+
+// LU with partial pivoting and the solve of A w = w (column-major m x m, d_A
+// overwritten) through cuSOLVER; ALPS_E_SINGULAR for an exactly singular
+// pivot, ALPS_E_UNSUPPORTED when the library cannot be loaded
+int tps_lu_blocked(double* d_A, int m, double* d_w, cudaStream_t st) {
+  const CusolverApi* api = cusolver_api();
+  if (!api) return ALPS_E_UNSUPPORTED;
+  cusolverDnHandle_t h = nullptr;
+  if (api->create(&h) != CUSOLVER_STATUS_SUCCESS) return ALPS_E_CUDA;
+  int status = ALPS_OK, lwork = 0, info = 0;
+  double* d_work = nullptr;
+  int *d_piv = nullptr, *d_info = nullptr;
+  if (api->set_stream(h, st) != CUSOLVER_STATUS_SUCCESS || api->getrf_ws(h, m, m, d_A, m, &lwork) !=
+                                                               CUSOLVER_STATUS_SUCCESS)
+    status = ALPS_E_CUDA;
+  if (!status && (cudaMalloc(&d_work, (size_t)std::max(lwork, 1) * sizeof(double)) != cudaSuccess ||
+                  cudaMalloc(&d_piv, (size_t)m * sizeof(int)) != cudaSuccess ||
+                  cudaMalloc(&d_info, sizeof(int)) != cudaSuccess))
+    status = ALPS_E_OOM;
+  if (!status && api->getrf(h, m, m, d_A, m, d_work, d_piv, d_info) != CUSOLVER_STATUS_SUCCESS) status = ALPS_E_CUDA;
+  if (!status) {
+    if (cudaMemcpyAsync(&info, d_info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      status = ALPS_E_CUDA;
+    else if (info != 0)
+      status = ALPS_E_SINGULAR;
+  }
+  if (!status && api->getrs(h, CUBLAS_OP_N, m, 1, d_A, m, d_piv, d_w, m, d_info) != CUSOLVER_STATUS_SUCCESS)
+    status = ALPS_E_CUDA;
+  if (!status && cudaStreamSynchronize(st) != cudaSuccess) status = ALPS_E_CUDA;
+  cudaFree(d_work);
+  cudaFree(d_piv);
+  cudaFree(d_info);
+  api->destroy(h);
+  return status;
+}
+
 // Weights of the thin-plate spline through n samples (gc, pc) with the
 // right-hand side already in d_w (n + 3 entries): the dense system of
 // polyharmonic_spline solved by LU with partial pivoting (dgesv).
@@ -332,6 +417,13 @@ int tps_solve_device(const double* d_gc, const double* d_pc, int n, double smoot
     long mm = (long)m * m;
     k_tps_matrix<<<(unsigned)((mm + 255) / 256), 256, 0, st>>>(d_gc, d_pc, n, smoothing, d_A);
     if (cudaGetLastError() != cudaSuccess) status = ALPS_E_CUDA;
+  }
+  if (!status && m >= TPS_BLOCKED_M) {
+    status = tps_lu_blocked(d_A, m, d_w, st);
+    cudaFree(d_A);
+    cudaFree(d_piv);
+    cudaFree(d_info);
+    return status;
   }
   for (int k = 0; k < m && !status; ++k) {
     k_lu_pivot<<<1, 1024, 0, st>>>(d_A, m, k, d_piv, d_info);

@@ -14,6 +14,7 @@
 #include <cstdio>
 
 #include "alps_internal.cuh"
+#include "tc_gemm.cuh"
 #include "device_math.cuh"
 
 namespace {
@@ -844,8 +845,12 @@ int launch_prepare_species(alps_ctx* c, int is) {
   double dpperp = S.pperp[2] - S.pperp[1];
   double dppar = std::fabs(S.ppar[2] - S.ppar[1]);
   double scale = 2.0 * ALPS_PI * S.sp.qs / S.sp.ms * dpperp * dppar * 0.25;
-  double* d_ee = nullptr;
-  ALPS_CUDA_TRY(cudaMalloc(&d_ee, sizeof(double)));
+  // per-species device words and fit scratch are kept with the species: a
+  // cudaFree here would wait for the whole device, and contexts prepared on
+  // several host threads would run one after another
+  if (!S.d_words) ALPS_CUDA_TRY(cudaMalloc(&S.d_words, 2 * sizeof(double)));
+  double* d_ee = S.d_words;
+  int* d_status = reinterpret_cast<int*>(S.d_words + 1);
   k_int_ee<<<1, 256, 0, st>>>(S.d_g2, S.d_ppar, N, M, scale, d_ee);
   ALPS_CUDA_TRY(cudaGetLastError());
   // relativistic species: (Gamma, pparbar) grid, f0_rel and its derivatives
@@ -877,22 +882,17 @@ int launch_prepare_species(alps_ctx* c, int is) {
     a.grel = S.d_grel;
     a.prel = S.d_prel;
     int maxpts = a.rel ? a.np : M;
-    double* scratch = nullptr;
-    int* d_status = nullptr;
-    ALPS_CUDA_TRY(cudaMalloc(&scratch, (size_t)(maxpts + 1) * (FIT_MAXP + 1) * sizeof(double)));
-    ALPS_CUDA_TRY(cudaMalloc(&d_status, sizeof(int)));
+    int rc;
+    if ((rc = ensure(S.d_fit_scratch, S.fit_scratch_cap, (size_t)(maxpts + 1) * (FIT_MAXP + 1)))) return rc;
     ALPS_CUDA_TRY(cudaMemsetAsync(d_status, 0, sizeof(int), st));
-    k_lm_fit<<<1, 32, 0, st>>>(a, S.d_f0, S.d_pperp, S.d_ppar, S.d_fit, scratch, d_status);
+    k_lm_fit<<<1, 32, 0, st>>>(a, S.d_f0, S.d_pperp, S.d_ppar, S.d_fit, S.d_fit_scratch, d_status);
     ALPS_CUDA_TRY(cudaGetLastError());
     ALPS_CUDA_TRY(cudaMemcpyAsync(&st_fit, d_status, sizeof(int), cudaMemcpyDeviceToHost, st));
     ALPS_CUDA_TRY(cudaStreamSynchronize(st));
-    cudaFree(scratch);
-    cudaFree(d_status);
   }
   double ee = 0.0;
   ALPS_CUDA_TRY(cudaMemcpyAsync(&ee, d_ee, sizeof(double), cudaMemcpyDeviceToHost, st));
   ALPS_CUDA_TRY(cudaStreamSynchronize(st));
-  cudaFree(d_ee);
   S.int_ee = ee;
   return st_fit;
 }
@@ -930,14 +930,14 @@ int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out) {
     *nmax_out = 1;
     return ALPS_OK;
   }
-  int* d_n = nullptr;
-  ALPS_CUDA_TRY(cudaMalloc(&d_n, sizeof(int)));
-  k_nmax<<<1, 256, 0, c->stream>>>(S.d_pperp, c->sys.nperp, kperp, S.sp.qs, c->sys.Bessel_zero, 2000, d_n);
+  // a device word kept with the species: no allocation (and no cudaFree,
+  // which would wait for the whole device) per k step
+  if (!S.d_nmax) ALPS_CUDA_TRY(cudaMalloc(&S.d_nmax, sizeof(int)));
+  k_nmax<<<1, 256, 0, c->stream>>>(S.d_pperp, c->sys.nperp, kperp, S.sp.qs, c->sys.Bessel_zero, 2000, S.d_nmax);
   ALPS_CUDA_TRY(cudaGetLastError());
   int nm = 0;
-  ALPS_CUDA_TRY(cudaMemcpyAsync(&nm, d_n, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  ALPS_CUDA_TRY(cudaMemcpyAsync(&nm, S.d_nmax, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  cudaFree(d_n);
   if (nm >= 2000) return ALPS_E_INVALID;  // orders beyond 2000 are outside the supported range
   *nmax_out = nm;
   return ALPS_OK;
@@ -958,8 +958,26 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   k_bessel_rows<<<dim3((N - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_bessel, S.d_pperp, N, nmax, S.d_Rw);
   ALPS_CUDA_TRY(cudaGetLastError());
   int Mr = 3 * (nmax + 1), Nc = 2 * (M - 1), K = N - 1;
-  k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);
-  ALPS_CUDA_TRY(cudaGetLastError());
+  S.tc_used = 0;
+  S.tc_fixed = 0;
+  if (c->precision == ALPS_PREC_MIXED && K <= 256) {
+    // mixed path: the contraction on the tensor cores, FP64-accurate per
+    // entry (tc_product_checked recomputes in FP64 whatever its bound does
+    // not cover)
+    const size_t need = tc_checked_workspace_bytes(Mr, Nc, K);
+    if (need > S.tcws_cap) {
+      if (S.d_tcws) cudaFree(S.d_tcws);
+      S.d_tcws = nullptr;
+      S.tcws_cap = 0;
+      ALPS_CUDA_TRY(cudaMalloc(&S.d_tcws, need));
+      S.tcws_cap = need;
+    }
+    if ((rc = tc_product_checked(S.d_Rw, S.d_G, S.d_A, Mr, Nc, K, S.d_tcws, &S.tc_fixed, st))) return rc;
+    S.tc_used = 1;
+  } else {
+    k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);
+    ALPS_CUDA_TRY(cudaGetLastError());
+  }
   k_fold_reduced<<<dim3((M - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_A, S.d_ppar, M, nmax, S.d_V);
   ALPS_CUDA_TRY(cudaGetLastError());
   const size_t nvf = (size_t)(nmax + 1) * (M - 1) * 12;

@@ -99,6 +99,59 @@ def config_map(nr=512, ni=512, Bessel_zero=1e-9):
     return w
 
 
+M_E = 1.0 / 1836.0
+VA_REL = 1e-2  # v_A/c of the relativistic configuration
+
+
+def config_relativistic(theta_e, nperp=128, npar=256, ngamma=100, npparbar=200, kpar_de=0.1, vA=VA_REL,
+                        Bessel_zero=1e-20):
+    """Relativistic electrons: a Juettner f0 (generator kind 3) with
+    Theta = kT_e/(m_e c^2) = theta_e on an nperp x npar (p_perp, p_par) grid,
+    remapped to an ngamma x npparbar (Gamma, pparbar) grid (relat = T,
+    fit type 4, the Gamma-only Juettner continuation with perp_correction
+    1/Theta in Gamma), beside a bi-Maxwellian proton background (beta_p = 1)
+    in the closed form (use_bM).  v_A/c = vA; the generator's exponent
+    2 m_e/(v_A^2 beta tau_e) equals 1/Theta for tau_e = 2 m_e Theta/(v_A^2
+    beta); the grid spans |p| <= m_e c sqrt((1 + 18 Theta)^2 - 1).  k at
+    propagation angle 30 degrees with k_par d_e = kpar_de
+    (d_e = d_p sqrt(m_e/m_p)), the whistler branch's start; guess from the
+    cold whistler omega = Omega_e k^2 d_e^2 cos(theta)/(1 + k^2 d_e^2)."""
+    import math
+    beta = 1.0
+    tau_e = 2.0 * M_E * theta_e / (vA * vA * beta)
+    # the generator's autoscale is written for species of the reference
+    # mass; the electron grid spans Gamma - 1 <= 18 Theta instead (f0 down to
+    # e^-18, as maxP = 6 does for a Maxwellian), in units of m_p v_A
+    pmax = (M_E / vA) * math.sqrt((1.0 + 18.0 * theta_e) ** 2 - 1.0)
+    de = _dist(kind=3, ms=M_E, tau=tau_e, beta=beta, vA=vA, autoscale=0)
+    de.maxPperp = de.maxPpar = pmax
+    sysd = _abi.system_defaults(
+        nspec=2, nperp=nperp, npar=npar, kperp=0.0, kpar=0.0, vA=vA, Bessel_zero=Bessel_zero,
+        secant_method=2, numiter=50, kperp_norm=1, D_threshold=1e-30, D_prec=1e-5, D_gap=1e-5, D_tol=1e-7,
+        positions_principal=5, n_resonance_interval=100, Tlim=0.01, ngamma=ngamma, npparbar=npparbar)
+    spE = _abi.species_defaults(ns=1.0, qs=-1.0, ms=M_E, relat=1, fits=[(4, [1.0, 0, 0, 0, 0], 1.0 / theta_e)])
+    spP = _abi.species_defaults(ns=1.0, qs=1.0, ms=1.0, use_bM=1, bM_nmaxs=500, bM_Bessel_zeros=1e-50,
+                                bM_betas=beta, bM_alphas=1.0, bM_pdrifts=0.0)
+    th = math.radians(30.0)
+    sq = math.sqrt(1.0 / M_E)                    # d_p / d_e
+    kpar = kpar_de * sq
+    kperp = kpar * math.tan(th)
+    kde = kpar_de / math.cos(th)
+    guess = (1.0 / M_E) * kde * kde * math.cos(th) / (1.0 + kde * kde)
+    return dict(system=sysd, dists=[de, None], species=[spE, spP], k=(kperp, kpar),
+                extra=dict(theta_e=theta_e, tau_e=tau_e, guess=[guess - 1e-3j * guess],
+                           scan=dict(type_s=2, swi=0.0, swf=2.0 * sq / math.cos(th), log_scan=True, n_out=64,
+                                     n_res=1)))
+
+
+def build_relativistic(w, generate):
+    """(system, [(species, pperp, ppar, f0)]) of config_relativistic: the
+    electron table from the generator, the closed-form protons without one."""
+    s = w["system"]
+    pperp, ppar, f0, _ = generate(w["dists"][0], s.nperp, s.npar)
+    return s, [(w["species"][0], pperp, ppar, f0), (w["species"][1], None, None, None)]
+
+
 def uneven_plasma(rng, grid=None, Bessel_zero=1e-20):
     """One solve of the uneven-batch draw: 1-3 species from {bi-Maxwellian
     with T_perp/T_par in U[0.3,3] and beta in logU[0.01,10]; a drifting proton

@@ -32,6 +32,7 @@ from alps_gb300.sharding import shard_range  # noqa: E402
 
 METRIC = "D(omega,k) evals/s & roots/s at <=1e-8 rel vs FP64, vs plain GPU; p50/p99 latency"
 UNIT = "evals/s"
+POLISH_RTOL = 1e-12  # the map configuration's polish tolerance on |delta omega| / |omega|
 
 
 def lattice(mp):
@@ -221,8 +222,9 @@ def cpu_model():
     return platform.machine()
 
 
-def cpu_sample(P, oms, budget_s, nthreads):
-    """Times the oracle on a bounded sample of the lattice; returns evals/s."""
+def cpu_sample(P, oms, budget_s, nthreads, values=False):
+    """Times the oracle on a bounded sample of the lattice; returns evals/s
+    (and, with values, the sample's indices and det D)."""
     t0 = time.perf_counter()
     P.disp_batch(oms[:1], nthreads=1)
     t1 = time.perf_counter() - t0
@@ -230,9 +232,45 @@ def cpu_sample(P, oms, budget_s, nthreads):
     m = min(m, 512)
     idx = np.linspace(0, len(oms) - 1, m).astype(int)
     t0 = time.perf_counter()
-    P.disp_batch(oms[idx], nthreads=nthreads)
+    D = P.disp_batch(oms[idx], nthreads=nthreads)
     dt = time.perf_counter() - t0
+    if values:
+        return m / dt, m, dt, idx, D
     return m / dt, m, dt
+
+
+def chi_errors(P, G, oms):
+    """Per-entry chi0 error of the library against the oracle at oms: the
+    largest |chi_gpu - chi_oracle| / max(|chi_oracle|, 1e-3 mag) (mag = the
+    sum over Bessel orders of |order contribution|, as in the parity tests),
+    over species and the nine entries, and the cofactor-normalised det D
+    error |dD| / sum_ij |cof_ij| max(|w_ij|, 1e-3 mag_ij)."""
+    sy = P.sys
+    chi_err, det_err = 0.0, 0.0
+    for om in oms:
+        Do, co, _, wo = P.disp(om)
+        Dg, cg, _, _ = G.disp(om)
+        mag = P.disp_mag(om)
+        denom = abs(om * om) * sy.vA ** 2 * (1.0 if sy.kperp_norm else sy.kperp ** 2)
+        scale = np.maximum(np.abs(co), 1e-3 * mag / denom)
+        chi_err = max(chi_err, float((np.abs(cg - co) / np.maximum(scale, 1e-300)).max()))
+        cof = np.array([[np.linalg.det(np.delete(np.delete(wo, i, 0), j, 1)) for j in range(3)] for i in range(3)])
+        norm = np.sum(np.abs(cof) * np.maximum(np.abs(wo), 1e-3 * mag.sum(axis=0)))
+        det_err = max(det_err, float(abs(Dg - Do) / norm))
+    return chi_err, det_err
+
+
+def root_errors(P, roots, nthreads):
+    """Distance of each root from the oracle's root, relative to |omega|: the
+    oracle's Newton step |D(w) / D'(w)| / |w| at the library's root, D' from
+    a central difference over 1e-7 |w|."""
+    roots = np.asarray(roots)
+    h = 1e-7 * np.abs(roots)
+    pts = np.concatenate([roots, roots + h, roots - h])
+    D = P.disp_batch(pts, nthreads=nthreads)
+    n = len(roots)
+    Dp = (D[n:2 * n] - D[2 * n:]) / (2 * h)
+    return [float(abs(D[k] / Dp[k]) / abs(roots[k])) for k in range(n)]
 
 
 def run_reference(args, w, mp, rank, world):
@@ -452,7 +490,7 @@ def main():
             "double_float_nodes_per_step": work["nodes"], "df_node_flops": DF_NODE_FLOPS,
             "series_terms_df": work["series_df"], "df_term_flops": DF_TERM_FLOPS,
             "series_terms_fp32": work["series_fp32"]}
-    # resonant items: the SURVEY's algorithmic count per item, 24 M_P flops of
+    # resonant items: the algorithmic count per item, 24 M_P flops of
     # principal-value sums and 60 (N_perp + 1) of Landau rows, FP64
     f_res = work["items"] * (24.0 * system.n_resonance_interval + 60.0 * (system.nperp + 1))
     res = {"kernel": "k_resonant_multi (fast path)", "bound": "fp64-equivalent", "kernel_ms": res_ms,
@@ -489,7 +527,8 @@ def main():
     e2e_t = (time.perf_counter() - t0) / max(1, args.steps)
     e2e = {"value": n / e2e_t, "unit": UNIT, "h2d_bytes_per_step": 16 * n, "d2h_bytes_per_step": 16 * n}
 
-    # polish the 8 deepest minima (roots/s, latency per root solve)
+    # polish the 8 deepest minima until the secant update is at most 1e-12
+    # of |omega| (roots/s counts converged roots only; latency per solve)
     val = np.log10(np.abs(Dh))
     mins = api.find_minima(val, mp.nr, mp.ni, numroots=100)
     mins = sorted(mins, key=lambda ij: val[ij[0] * mp.ni + ij[1]])[:w["extra"]["n_polish"]]
@@ -497,28 +536,60 @@ def main():
     lat = []
     for g in guesses:
         t0 = time.perf_counter()
-        G.secant([g])
+        G.polish([g], om_rtol=POLISH_RTOL)
         lat.append((time.perf_counter() - t0) * 1e3)
     t0 = time.perf_counter()
-    roots, iters, _ = G.secant(guesses)
+    roots, iters, _, conv = G.polish(guesses, om_rtol=POLISH_RTOL)
     t_roots = time.perf_counter() - t0
+    # the reference's own stopping rule (|D| < D_threshold, absolute) from the
+    # same guesses: the parity mode, reported for its iteration counts
+    _, iters_ref, _, conv_ref = G.polish(guesses, om_rtol=0.0)
     # the same solves on the plain FP64 path: root agreement of the fast path
     G.set_precision("fp64")
-    roots_plain, _, _ = G.secant(guesses)
+    roots_plain, _, _, conv_plain = G.polish(guesses, om_rtol=POLISH_RTOL)
     G.set_precision("mixed")
-    root_rel = float(np.max(np.abs(roots - roots_plain) / np.maximum(np.abs(roots_plain), 1e-300)))
+    both = conv & conv_plain
+    root_rel = float(np.max(np.abs(roots[both] - roots_plain[both]) / np.abs(roots_plain[both]))) if both.any() \
+        else None
 
     served = None if args.no_served else served_stream(api, args)
 
     cpu = None
+    err_vs_oracle = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        G_chk = api.Plasma(system, species)  # single-frequency checks with the side results
+        G_chk.set_k(s.kperp, kpar)
         from oracle import pyoracle as po
         nthreads = os.cpu_count() or 1
         P = po.OraclePlasma(system, species)
         P.set_k(s.kperp, kpar)
-        r, m, dt = cpu_sample(P, oms, float(os.environ.get("ALPS_CPU_BASELINE_S", "10")), nthreads)
+        r, m, dt, idx, D_or = cpu_sample(P, oms, float(os.environ.get("ALPS_CPU_BASELINE_S", "10")), nthreads,
+                                         values=True)
         # the same restatement on one core, a smaller sample
         r1, m1, dt1 = cpu_sample(P, oms, 3.0, 1)
+        # error of both GPU paths against the FP64 oracle: det D on the timed
+        # sample, chi entries and cofactor-normalised det D at 8 of its
+        # points, and the polished roots
+        rel_f = np.abs(D_fast[idx] - D_or) / np.abs(D_or)
+        rel_p = np.abs(D_plain[idx] - D_or) / np.abs(D_or)
+        pts = oms[idx[np.linspace(0, len(idx) - 1, 8).astype(int)]]
+        chi_p, detn_p = chi_errors(P, G_chk, pts)
+        G_chk.set_precision("mixed")
+        chi_f, detn_f = chi_errors(P, G_chk, pts)
+        G_chk.set_precision("fp64")
+        err_vs_oracle = {
+            "det_D_rel": {"mixed": float(rel_f.max()), "fp64": float(rel_p.max()), "points": int(m),
+                          "note": "max |D - D_oracle| / |D_oracle| over the sample; det D of a 3x3 tensor with "
+                                  "cancelling entries, see det_D_cofactor"},
+            "det_D_cofactor": {"mixed": detn_f, "fp64": detn_p, "points": len(pts),
+                               "note": "|dD| / sum_ij |cof_ij| max(|w_ij|, 1e-3 mag_ij): the bound the parity "
+                                       "tests gate at 1e-10"},
+            "chi_entry": {"mixed": chi_f, "fp64": chi_p, "points": len(pts),
+                          "note": "max over species and entries of |dchi| / max(|chi|, 1e-3 mag)"},
+            "roots": {"mixed": root_errors(P, roots[conv], nthreads),
+                      "fp64": root_errors(P, roots_plain[conv_plain], nthreads),
+                      "note": "oracle Newton step |D/D'| / |omega| at each converged root"},
+            "fit": "each side's own Levenberg-Marquardt continuation fit"}
         cpu = {"value": r, "unit": UNIT, "cores": nthreads, "kind": "port", "cpu_model": cpu_model(),
                "sample": "%d lattice points of the same map (every %d-th), oracle threads over points, %.1f s"
                          % (m, max(1, n // m), dt),
@@ -527,15 +598,21 @@ def main():
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic", "precision_path": G.precision,
+                "vs_baseline": None, "dtype": "mixed: fp32 double-float + fp64", "data": "synthetic",
+                "precision_path": G.precision, "err_vs_oracle": err_vs_oracle,
                 "config": config_dict(w, mp.nr, mp.ni, world), "nmax": nmax,
-                "plain_fp64": {"value": value_plain, "unit": UNIT, "ms_per_step": t_plain / args.steps * 1e3,
+                "plain_fp64": {"value": value_plain, "unit": UNIT, "dtype": "f64",
+                               "ms_per_step": t_plain / args.steps * 1e3,
                                "speedup_of_fast_path": value / value_plain,
                                "max_rel_diff_det_D_fast_vs_plain": float(rel.max()),
                                "max_rel_diff_roots_fast_vs_plain": root_rel},
                 "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
                 "gpu_launches": int(st.kernels_launched) * args.steps,
-                "roots": {"count": len(roots), "roots_per_s": len(roots) / t_roots, "iterations": iters,
+                "roots": {"count": len(roots), "converged": int(conv.sum()),
+                          "roots_per_s": int(conv.sum()) / t_roots, "iterations": iters,
+                          "stop_rule": "secant update <= %g |omega|" % POLISH_RTOL,
+                          "reference_rule": {"iterations": iters_ref, "converged": int(conv_ref.sum()),
+                                             "note": "|D| < D_threshold = %g (absolute)" % system.D_threshold},
                           "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
                                          "p99": float(np.percentile(lat, 99)) if lat else None},
                           "roots": [[r.real, r.imag] for r in roots]},

@@ -209,6 +209,19 @@ int alps_disp_batch_noalloc(alps_ctx* ctx, int n, const alps_complex* d_om,
                             alps_complex* d_D, void* stream,
                             size_t* scratch_bytes);
 
+/* Device error status of the last asynchronous batch of this context
+ * (alps_disp_batch_device or alps_disp_batch_noalloc).  Waits for stream
+ * (cudaStream_t, NULL = the context's stream), then reads the batch's device
+ * error word: ALPS_OK, ALPS_E_SUBLUMINAL (a relativistic resonance window
+ * covered the whole subluminal cone: alps_error(8), src/ALPS_io.f90:982-988,
+ * raised in integrate_resU_rel, src/ALPS_fns_rel.f90:656) or
+ * ALPS_E_INVALID (resonant-order slots overflowed).  The reference aborts
+ * the MPI job on alps_error; the synchronous entry points return these codes
+ * directly, the asynchronous ones through this call.  It allocates nothing.
+ * For alps_disp_batch_noalloc the word sits in the shared static scratch:
+ * read the status before the next no-allocation call on the device. */
+int alps_batch_status(alps_ctx* ctx, void* stream);
+
 /* Root polishing of nroots guesses in place (om[], host memory).
  * method: 0 secant (src/ALPS_fns.f90:1815-1917), 1 rtsec (:2105-2195),
  * 2 secant_osc (:1919-2101).  iters[r] (may be NULL) receives the number of
@@ -217,6 +230,37 @@ int alps_disp_batch_noalloc(alps_ctx* ctx, int n, const alps_complex* d_om,
  * det in one batched launch. */
 int alps_secant(alps_ctx* ctx, int method, int nroots, alps_complex* om,
                 int* iters, alps_complex* Dfinal);
+
+/* alps_secant with a relative-step stop and a converged mask.  With
+ * om_rtol > 0 a root also stops once its secant update is at most
+ * om_rtol |om| (the update applied): a polish criterion independent of the
+ * scale of det D, whose size keeps the reference's absolute D_threshold out
+ * of reach for many roots.  om_rtol = 0 gives exactly alps_secant.
+ * converged[r] (may be NULL) is 1 when a stopping rule ended root r, 0 when
+ * numiter ran out (the reference then returns the best-|D| iterate,
+ * src/ALPS_fns.f90:2093-2099).  No reference counterpart for om_rtol. */
+int alps_secant_ex(alps_ctx* ctx, int method, int nroots, alps_complex* om,
+                   double om_rtol, int* iters, alps_complex* Dfinal,
+                   int* converged);
+
+/* Root polishing of n roots, root r on its own context ctx[r] (its own
+ * plasma and k: species, grids and nmax may differ from root to root; a
+ * context may appear more than once), entirely on the device.
+ * Replaces refine_guess's per-root secant loop (src/ALPS_fns.f90:3793-3856
+ * over secant_osc :1919-2101, secant :1815-1917 or rtsec :2105-2195): the
+ * root-finder state machines live in device memory, every round is one
+ * fused det D launch over all roots' pending frequencies followed by a
+ * device step of every machine, and the rounds repeat inside one CUDA graph
+ * (a conditional WHILE node ends it when no root is active), so no round
+ * waits on the host.  Each root's determinants use the launch shape of a
+ * lone batch of two frequencies on its context, so a root's iterates and
+ * result are bit for bit the same alone and in any batch.  om_rtol,
+ * converged, iters and Dfinal as in alps_secant_ex.  Contexts with
+ * relativistic or closed-form species return ALPS_E_UNSUPPORTED (use
+ * alps_secant_ex).  Synchronous. */
+int alps_solve_many(alps_ctx* const* ctx, int n, int method, alps_complex* om,
+                    double om_rtol, int* iters, alps_complex* Dfinal,
+                    int* converged);
 
 /* Eigenfunctions and heating rates of roots (calc_eigen,
  * src/ALPS_fns.f90:2605-2899).  Fields are relative to E_x; velocities and
@@ -411,6 +455,22 @@ int alps_interpolate(const double* pperp_c, const double* ppar_c, const double* 
  * to stdout. */
 int alps_run_interpolation(const char* input_path, const char* workdir);
 
+/* FP64-accurate dense product C = A B of row-major device arrays (A M x K,
+ * B K x N, C M x N, K <= 256) on the BF16 tensor cores: the engine of the
+ * mixed path's p_perp contraction.  Each row of A and column of B is split
+ * into seven 8-bit slices of its own power-of-two scale (the Ozaki splitting);
+ * the 28 leading slice products run as tcgen05.mma with FP32 accumulators in
+ * tensor memory, exact integers up to the levels that carry FP64's precision.
+ * checked = 1: B's rows are first scaled to unit size (A's columns by the
+ * inverse), and every entry whose error bound exceeds 2^-44 sum_k |A B| (the
+ * size of FP64 GEMM's own worst-case rounding bound) is recomputed in FP64;
+ * *nfixed (may be NULL) receives their number.  checked = 0: the bare
+ * product, error at most 10 K 2^-56 times the product of the row's and
+ * column's power-of-two scales.  Synchronous; allocates its workspace.
+ * No reference counterpart (a building block, exported for its tests). */
+int alps_tc_product(const double* d_A, const double* d_B, double* d_C, int M,
+                    int N, int K, int checked, int* nfixed);
+
 /* Device work counters of the last disp batch (for measurement). */
 typedef struct alps_stats {
   int64_t n_eval;             /* frequencies evaluated                        */
@@ -420,6 +480,12 @@ typedef struct alps_stats {
   int kernels_launched;       /* kernels launched by the last disp batch      */
   int64_t graph_replays;      /* server batches replayed from a CUDA graph    */
   int64_t graph_captures;     /* server batches captured into a CUDA graph    */
+  /* the p_perp contraction of the last alps_set_k: species whose product
+   * ran on the tensor cores (mixed path), and of their entries those whose
+   * error bound sent them to the FP64 recompute */
+  int tc_contractions;
+  int64_t tc_fixed_entries;
+  int64_t tc_entries;
 } alps_stats;
 int alps_get_stats(alps_ctx* ctx, alps_stats* st);
 

@@ -329,6 +329,10 @@ struct Species {
   // relativistic (Gamma, pparbar) grid, src/ALPS_fns_rel.f90:36-289
   int ng = 0, np = 0;
   std::vector<double> grel, prel, f0rel, dfr1, dfr2;  // [(ng+1)*(np+1)]
+  // f0_rel supplied from outside (oracle_set_f0_rel): used in place of the
+  // spline remap, so the rest of the relativistic path can be checked at
+  // input grids whose dense spline system is beyond a CPU
+  std::vector<double> f0rel_given;
   int ridx(int ig, int ip) const { return ig * (np + 1) + ip; }
   double G(int ig, int ip) const { return grel[ridx(ig, ip)]; }
   double PB(int ig, int ip) const { return prel[ridx(ig, ip)]; }
@@ -1243,23 +1247,27 @@ int derivative_f0_rel(Species& s, double vA) {
       s.grel[s.ridx(ig, ip)] = gmin + ((gmax_use - gmin) * ig) / (1.0 * s.ng);
       s.prel[s.ridx(ig, ip)] = pmin + ((pmax - pmin) * ip) / (1.0 * s.np);
     }
-  int st = polyharmonic_spline(grid, gc, pc, s, s.f0rel);
-  if (st) return st;
-  for (int ig = 0; ig <= s.ng; ++ig)
-    for (int ip = 0; ip <= s.np; ++ip) {
-      double& f = s.f0rel[s.ridx(ig, ip)];
-      f = std::exp(f);
-      double g = s.G(ig, ip), pb = s.PB(ig, ip);
-      if ((g * g - 1.0) < (pb * pb)) f = -1.0;
-    }
-  double integ = 0.0;
-  double dgamma = s.G(2, 2) - s.G(1, 2), dpb = s.PB(2, 2) - s.PB(2, 1);
-  for (int ig = 0; ig <= s.ng; ++ig)
-    for (int ip = 0; ip <= s.np; ++ip)
-      if (s.FR(ig, ip) > -1.0)
-        integ = integ + s.G(ig, ip) * s.FR(ig, ip) * 2.0 * PI * dgamma * dpb * cube(ms / vA);
-  for (auto& f : s.f0rel)
-    if (f != -1.0) f = f / integ;
+  if (!s.f0rel_given.empty()) {
+    s.f0rel = s.f0rel_given;  // remapped, masked and normalised already
+  } else {
+    int st = polyharmonic_spline(grid, gc, pc, s, s.f0rel);
+    if (st) return st;
+    for (int ig = 0; ig <= s.ng; ++ig)
+      for (int ip = 0; ip <= s.np; ++ip) {
+        double& f = s.f0rel[s.ridx(ig, ip)];
+        f = std::exp(f);
+        double g = s.G(ig, ip), pb = s.PB(ig, ip);
+        if ((g * g - 1.0) < (pb * pb)) f = -1.0;
+      }
+    double integ = 0.0;
+    double dgamma = s.G(2, 2) - s.G(1, 2), dpb = s.PB(2, 2) - s.PB(2, 1);
+    for (int ig = 0; ig <= s.ng; ++ig)
+      for (int ip = 0; ip <= s.np; ++ip)
+        if (s.FR(ig, ip) > -1.0)
+          integ = integ + s.G(ig, ip) * s.FR(ig, ip) * 2.0 * PI * dgamma * dpb * cube(ms / vA);
+    for (auto& f : s.f0rel)
+      if (f != -1.0) f = f / integ;
+  }
   s.dfr1.assign(s.f0rel.size(), 0.0);
   s.dfr2.assign(s.f0rel.size(), 0.0);
   for (int ig = 1; ig <= s.ng - 1; ++ig)
@@ -2586,6 +2594,18 @@ int oracle_get_df0(oracle_ctx* c, int is, double* df1, double* df2) {
   if (!c || is < 0 || is >= c->sys.nspec || !c->prepared) return ALPS_E_INVALID;
   std::copy(c->spec[is].df1.begin(), c->spec[is].df1.end(), df1);
   std::copy(c->spec[is].df2.begin(), c->spec[is].df2.end(), df2);
+  return ALPS_OK;
+}
+
+// Supplies species is's f0_rel table [(ngamma+1)*(npparbar+1)] (-1 outside
+// the subluminal cone, normalised), to be used by the next oracle_prepare
+// instead of the spline remap of derivative_f0_rel; the grid vectors, the
+// difference quotients, the fits and everything after are the oracle's own.
+int oracle_set_f0_rel(oracle_ctx* c, int is, const double* f0_rel) {
+  if (!c || is < 0 || is >= c->sys.nspec || !c->spec[is].sp.relat || !f0_rel) return ALPS_E_INVALID;
+  Species& s = c->spec[is];
+  s.f0rel_given.assign(f0_rel, f0_rel + (size_t)(s.ng + 1) * (s.np + 1));
+  c->prepared = false;
   return ALPS_OK;
 }
 

@@ -32,6 +32,9 @@ int oracle_prepare(oracle_ctx* ctx);
 int oracle_get_fit(oracle_ctx* ctx, int is, double* out);
 int oracle_set_fit(oracle_ctx* ctx, int is, const double* in);
 int oracle_get_df0(oracle_ctx* ctx, int is, double* df1, double* df2);
+/* Test hook: f0_rel of a relativistic species taken as given by the next
+ * oracle_prepare (in place of the spline remap). */
+int oracle_set_f0_rel(oracle_ctx* ctx, int is, const double* f0_rel);
 int oracle_get_f0_rel(oracle_ctx* ctx, int is, double* gamma, double* pparbar, double* f0_rel, double* df1,
                       double* df2);
 int oracle_set_k(oracle_ctx* ctx, double kperp, double kpar);

@@ -52,6 +52,7 @@ def lib():
             L.oracle_set_fit.argtypes = [C.c_void_p, C.c_int, dp]
             L.oracle_get_df0.argtypes = [C.c_void_p, C.c_int, dp, dp]
             L.oracle_get_f0_rel.argtypes = [C.c_void_p, C.c_int, dp, dp, dp, dp, dp]
+            L.oracle_set_f0_rel.argtypes = [C.c_void_p, C.c_int, dp]
             L.oracle_set_k.argtypes = [C.c_void_p, C.c_double, C.c_double]
             L.oracle_get_nmax.argtypes = [C.c_void_p, P(C.c_int)]
             L.oracle_get_bessel.argtypes = [C.c_void_p, C.c_int, dp]
@@ -149,7 +150,10 @@ class OraclePlasma:
     """One plasma (context) in the oracle.  species: list of (alps_species,
     pperp, ppar, f0) with arrays of length (nperp+1)*(npar+1)."""
 
-    def __init__(self, system, species, prepare=True, fits=None):
+    def __init__(self, system, species, prepare=True, fits=None, f0_rel=None):
+        """f0_rel: optional {species index: f0_rel table [(ngamma+1),
+        (npparbar+1)]} used in place of the oracle's own spline remap (for
+        input grids whose dense spline system is beyond a CPU)."""
         L = lib()
         self.sys = system
         self.nspec = system.nspec
@@ -165,6 +169,10 @@ class OraclePlasma:
                 ptrs = [_dptr(x) for x in a]
             _chk(L.oracle_set_species(self._h, i, C.byref(sp), *ptrs), "oracle_set_species")
         self.species = [s[0] for s in species]
+        for i, tab in (f0_rel or {}).items():
+            tab = np.ascontiguousarray(tab, dtype=np.float64).ravel()
+            self._keep.append(tab)
+            _chk(L.oracle_set_f0_rel(self._h, i, _dptr(tab)), "oracle_set_f0_rel")
         if prepare:
             _chk(L.oracle_prepare(self._h), "oracle_prepare")
         if fits is not None:

@@ -1,8 +1,8 @@
 """Copies the reference's own golden vectors and test inputs into
 tests/golden/ref/ so that the test suite does not need the reference tree.
 
-Run from the repository root with the reference checked out at REF (default
-/root/reference):  python tests/golden/make_golden.py [REF]
+Run from the repository root with the path of a reference checkout:
+    python tests/golden/make_golden.py REF
 
 The copied files are data the reference's test suite asserts on
 (tests/test_kpar_fast.py:12-31) or feeds to ALPS (tests/*.in,
@@ -14,7 +14,9 @@ import os
 import shutil
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    sys.exit("usage: python tests/golden/make_golden.py REF  (REF = a checkout of the reference)")
+REF = sys.argv[1]
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "ref")
 
 FILES = [
