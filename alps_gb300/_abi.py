@@ -159,6 +159,7 @@ class alps_stats(C.Structure):
         ("n_resonant", C.c_int64), ("n_landau", C.c_int64),
         ("kernels_launched", C.c_int), ("graph_replays", C.c_int64), ("graph_captures", C.c_int64),
         ("tc_contractions", C.c_int), ("tc_fixed_entries", C.c_int64), ("tc_entries", C.c_int64),
+        ("n_eval_total", C.c_int64),
     ]
 
 

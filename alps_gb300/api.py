@@ -242,11 +242,13 @@ class Plasma:
         check(lib().alps_get_stats(self._h, C.byref(s)), "alps_get_stats")
         return s
 
-    def om_scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots, eigen=False, heat=False):
+    def om_scan(self, type_s, swi, swf, log_scan, n_out, n_res, wroots, eigen=False, heat=False, om_rtol=None):
         """k-scan with root following (om_scan, src/ALPS_fns.f90:2198-2600,
         step sizes of scan_read, src/ALPS_io.f90:426-552).  Returns
         rows[it, root, (kperp, kpar, Re, Im)] and the final roots; with eigen
-        or heat also eig[it][root] (alps_eigen of calc_eigen at that row)."""
+        or heat also eig[it][root] (alps_eigen of calc_eigen at that row).
+        om_rtol: None follows each root with the reference's secant rule;
+        a number adds the relative-step stop of alps_secant_ex."""
         sy = self.sys
         wr = np.array(wroots, dtype=np.complex128)
         nroots = len(wr)
@@ -305,7 +307,10 @@ class Plasma:
             if not jump.any():
                 raise _abi.AlpsError(9, "om_scan")
             idx = [i for i in range(nroots) if jump[i]]
-            new, _, _ = self.secant(wr[idx], sy.secant_method)
+            if om_rtol is None:
+                new, _, _ = self.secant(wr[idx], sy.secant_method)
+            else:
+                new = self.polish(wr[idx], om_rtol, sy.secant_method)[0]
             ev = self.calc_eigen(new, eigen, heat) if (want and it % nres == 0) else None
             for q, i in enumerate(idx):
                 wr[i] = new[q]
@@ -426,14 +431,35 @@ class Server:
             pass
 
 
+def _handles(plasmas):
+    return (C.c_void_p * len(plasmas))(*[p.handle.value if isinstance(p.handle, C.c_void_p) else p.handle
+                                         for p in plasmas])
+
+
+def make_many(systems_species, precision="fp64", ks=None):
+    """Plasmas for many (system, species) pairs, prepared together
+    (alps_prepare_many) and, with ks = [(kperp, kpar), ...], set to their k
+    together (alps_set_k_many)."""
+    plasmas = [Plasma(s, sp, prepare=False, precision=precision) for s, sp in systems_species]
+    n = len(plasmas)
+    st = (C.c_int * max(1, n))()
+    check(lib().alps_prepare_many(_handles(plasmas), n, st), "alps_prepare_many")
+    if ks is not None:
+        kp = np.ascontiguousarray([k[0] for k in ks], dtype=np.float64)
+        kz = np.ascontiguousarray([k[1] for k in ks], dtype=np.float64)
+        check(lib().alps_set_k_many(_handles(plasmas), n, _dptr(kp), _dptr(kz), st), "alps_set_k_many")
+        for p, k in zip(plasmas, ks):
+            p.kperp, p.kpar = k
+    return plasmas
+
+
 def solve_many(plasmas, guesses, om_rtol=1e-12, method=2):
     """alps_solve_many: guesses[r] polished on plasmas[r] (each a Plasma at
     its own k), all on the device in one graph launch.  Returns (roots,
     iterations, det at root, converged mask)."""
     n = len(plasmas)
     oms = np.ascontiguousarray(np.asarray(guesses, dtype=np.complex128)).copy()
-    handles = (C.c_void_p * n)(*[p.handle.value if isinstance(p.handle, C.c_void_p) else p.handle
-                                 for p in plasmas])
+    handles = _handles(plasmas)
     it = (C.c_int * n)()
     cv = (C.c_int * n)()
     Df = np.zeros_like(oms)

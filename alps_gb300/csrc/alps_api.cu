@@ -355,6 +355,17 @@ int alps_get_f0_rel(alps_ctx* c, int is, double* gamma, double* pparbar, double*
   return ALPS_OK;
 }
 
+// The k tables of a context once nmax is known (the rest of alps_set_k);
+// with sync = false the caller synchronises the context's stream and then
+// calls set_k_commit.
+static int set_k_tables(alps_ctx* c, double kperp, double kpar, std::vector<int> nm, bool sync);
+static void set_k_commit(alps_ctx* c, double kperp, double kpar) {
+  c->kperp = kperp;
+  c->kpar = kpar;
+  c->kset = true;
+  c->gen++;
+}
+
 int alps_set_k(alps_ctx* c, double kperp, double kpar) {
   if (!c || !c->prepared) return ALPS_E_INVALID;
   if (!(kperp > 0.0) || kpar == 0.0 || !std::isfinite(kperp) || !std::isfinite(kpar)) return ALPS_E_INVALID;
@@ -364,6 +375,11 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     int st = launch_set_k_species(c, is, kperp, &nm[is]);
     if (st) return st;
   }
+  return set_k_tables(c, kperp, kpar, nm, true);
+}
+
+static int set_k_tables(alps_ctx* c, double kperp, double kpar, std::vector<int> nm, bool sync) {
+  const int S_ = c->sys.nspec;
   // nmax adjustment of a run on nproc MPI ranks (src/ALPS_fns.f90:4048-4071)
   if (c->sys.nproc > 0) {
     int max_procs = S_;
@@ -397,12 +413,82 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
     double cnt = std::floor(width * std::fabs(kpar / S.sp.qs)) + 3.0;
     S.rcap = (int)std::min<double>(2.0 * S.nmax + 1.0, cnt);
   }
+  if (!sync) return ALPS_OK;
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
-  c->kperp = kperp;
-  c->kpar = kpar;
-  c->kset = true;
-  c->gen++;
+  set_k_commit(c, kperp, kpar);
   return ALPS_OK;
+}
+
+int alps_prepare_many(alps_ctx* const* ctx, int n, int* status) {
+  if (n < 0 || (n > 0 && !ctx)) return ALPS_E_INVALID;
+  std::vector<alps_ctx*> batch;
+  int first = ALPS_OK;
+  for (int i = 0; i < n; ++i) {
+    alps_ctx* c = ctx[i];
+    if (status) status[i] = ALPS_OK;
+    if (!c) return ALPS_E_INVALID;
+    for (const auto& S : c->spec)
+      if (!S.loaded) return ALPS_E_INVALID;
+    c->gen++;
+    if (ctx_batch_preparable(c)) {
+      batch.push_back(c);
+    } else {  // relativistic species, Chebyshev continuations: per context
+      int st = alps_prepare(c);
+      if (status) status[i] = st;
+      if (st && !first) first = st;
+    }
+  }
+  std::vector<int> bst(batch.size(), ALPS_OK);
+  int rc = prepare_contexts(batch.data(), (int)batch.size(), bst.data());
+  if (rc) return rc;
+  for (size_t k = 0, i = 0; i < (size_t)n; ++i) {
+    alps_ctx* c = ctx[i];
+    if (k >= batch.size() || batch[k] != c) continue;
+    const int st = bst[k++];
+    if (status) status[i] = st;
+    if (st && !first) first = st;
+    c->prepared = (st == ALPS_OK);
+    c->kset = false;
+  }
+  return first;
+}
+
+int alps_set_k_many(alps_ctx* const* ctx, int n, const double* kperp, const double* kpar, int* status) {
+  if (n < 0 || (n > 0 && (!ctx || !kperp || !kpar))) return ALPS_E_INVALID;
+  for (int i = 0; i < n; ++i) {
+    if (!ctx[i] || !ctx[i]->prepared) return ALPS_E_INVALID;
+    if (!(kperp[i] > 0.0) || kpar[i] == 0.0 || !std::isfinite(kperp[i]) || !std::isfinite(kpar[i]))
+      return ALPS_E_INVALID;
+    if (status) status[i] = ALPS_OK;
+  }
+  std::vector<std::vector<int>> nm;
+  int rc = nmax_contexts(ctx, n, kperp, nm);
+  if (rc) return rc;
+  // every context's tables on a few streams, then one synchronisation
+  const int NS = 8;
+  cudaStream_t st[NS];
+  for (int q = 0; q < NS; ++q) ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st[q], cudaStreamNonBlocking));
+  int first = ALPS_OK;
+  std::vector<char> ok(n, 0);
+  for (int i = 0; i < n; ++i) {
+    alps_ctx* c = ctx[i];
+    cudaStream_t own = c->stream;
+    c->stream = st[i % NS];
+    c->defer_sync = true;
+    const int s = set_k_tables(c, kperp[i], kpar[i], nm[i], false);
+    c->defer_sync = false;
+    c->stream = own;
+    if (status) status[i] = s;
+    if (s && !first) first = s;
+    ok[i] = (s == ALPS_OK);
+  }
+  for (int q = 0; q < NS; ++q) {
+    if (cudaStreamSynchronize(st[q]) != cudaSuccess && !first) first = ALPS_E_CUDA;
+    cudaStreamDestroy(st[q]);
+  }
+  for (int i = 0; i < n; ++i)
+    if (ok[i] && first != ALPS_E_CUDA) set_k_commit(ctx[i], kperp[i], kpar[i]);
+  return first;
 }
 
 int alps_get_nmax(alps_ctx* c, int* nmax) {

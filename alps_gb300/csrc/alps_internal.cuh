@@ -235,6 +235,7 @@ struct alps_ctx {
   size_t bm_cap = 0;
   size_t ext_cap = 0;
   int* d_flags = nullptr;       // error flags
+  bool defer_sync = false;      // set_k of a batch (alps_set_k_many): no per-context synchronisation
   // error word of the last asynchronous batch (alps_disp_batch_device: d_flags;
   // alps_disp_batch_noalloc: a word of the static scratch), read by
   // alps_batch_status
@@ -280,6 +281,10 @@ void map_lattice(const alps_map_params* mp, std::vector<alps_complex>& oms);
 void map_finish(int n, const alps_complex* D, alps_complex* cal, double* val);
 }
 int launch_glls(alps_ctx* c, int is);
+// batched setup of many contexts (setup_kernels.cu)
+bool ctx_batch_preparable(const alps_ctx* c);
+int prepare_contexts(alps_ctx* const* ctx, int n, int* status);
+int nmax_contexts(alps_ctx* const* ctx, int n, const double* kperp, std::vector<std::vector<int>>& nm);
 int launch_set_k_species(alps_ctx* c, int is, double kperp, int* nmax_out);
 int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp);
 int launch_fit_aux(alps_ctx* c, int is);

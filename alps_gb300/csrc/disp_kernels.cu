@@ -2562,6 +2562,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
     c->ev_pending.push_back(ev);
   }
   c->stats.n_eval = n;
+  c->stats.n_eval_total += n;
   c->stats.kernels_launched = 5 + (a.relcap ? 1 : 0) + (a.has_bm ? 1 : 0);  // k_stage and the four
   return ALPS_OK;
 }

@@ -11,6 +11,7 @@
 //   k_dgemm           FP64 tiled GEMM for the contraction
 //   k_fold_reduced    reduced vectors V[n][j][12] of the omega pass
 #include <cmath>
+#include <cstring>
 #include <cstdio>
 
 #include "alps_internal.cuh"
@@ -190,14 +191,14 @@ __device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, 
 // the largest row length.  Rows are the iperp rows of the f0 table, or for a
 // relativistic species the Gamma rows of f0_rel restricted to the subluminal
 // cone (src/ALPS_analyt.f90:546-607).
-__global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double* __restrict__ pperp,
-                         const double* __restrict__ ppar, double* fit, double* scratch, int* status) {
-  // one warp: the points of a row are spread over the lanes; the scalar
-  // control flow (LM step, LU, parameter update) runs identically in every
-  // lane, and every sum over points runs in the reference's order
-  if (blockIdx.x != 0) return;
-  const int lane = threadIdx.x;
-  __shared__ double Am_sh[FIT_MAXP * FIT_MAXP], jr_sh[FIT_MAXP];
+// One species' fit, run by one warp: the points of a row are spread over
+// the lanes; the scalar control flow (LM step, LU, parameter update) runs
+// identically in every lane, and every sum over points runs in the
+// reference's order.  Am_sh / jr_sh: the warp's shared scratch.
+__device__ void lm_fit_body(const FitArgs& a, const double* __restrict__ f0, const double* __restrict__ pperp,
+                            const double* __restrict__ ppar, double* fit, double* scratch, int* status,
+                            double* Am_sh, double* jr_sh) {
+  const int lane = threadIdx.x & 31;
   int nf = a.nf, N = a.rel ? a.ng : a.N;
   int n_params = 0;
   for (int f = 0; f < nf; ++f) n_params += fit_nparams(a, a.fit_type[f]);
@@ -381,12 +382,39 @@ __global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double*
   }
 }
 
+__global__ void k_lm_fit(FitArgs a, const double* __restrict__ f0, const double* __restrict__ pperp,
+                         const double* __restrict__ ppar, double* fit, double* scratch, int* status) {
+  if (blockIdx.x != 0) return;
+  __shared__ double Am_sh[FIT_MAXP * FIT_MAXP], jr_sh[FIT_MAXP];
+  lm_fit_body(a, f0, pperp, ppar, fit, scratch, status, Am_sh, jr_sh);
+}
+
+}  // namespace
+
+// the fit of one (context, species) in a batched launch
+struct FitJob {
+  FitArgs a;
+  const double *f0, *pperp, *ppar;
+  double *fit, *scratch;
+  int* status;
+};
+
+namespace {
+
+// every job of the batch, one warp each: fits of different plasmas are
+// independent; within a fit the reference's warm start orders the rows
+__global__ void k_lm_fit_many(const FitJob* __restrict__ jobs, int n) {
+  const int j = blockIdx.x;
+  if (j >= n) return;
+  __shared__ double Am_sh[FIT_MAXP * FIT_MAXP], jr_sh[FIT_MAXP];
+  const FitJob& J = jobs[j];
+  lm_fit_body(J.a, J.f0, J.pperp, J.ppar, J.fit, J.scratch, J.status, Am_sh, jr_sh);
+}
+
 // determine_nmax for one species: smallest n >= 1 with max_i |J_n(z_i)| <=
 // Bessel_zero.  One block, threads over iperp.
-__global__ void k_nmax(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero,
-                       int limit, int* nmax_out) {
-  __shared__ double red[256];
-  __shared__ int done;
+__device__ void nmax_body(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero, int limit,
+                          int* nmax_out, double* red, int& done) {
   int nn = 0;
   if (threadIdx.x == 0) done = 0;
   __syncthreads();
@@ -409,6 +437,33 @@ __global__ void k_nmax(const double* __restrict__ pperp, int N, double kperp, do
     __syncthreads();
   }
   if (threadIdx.x == 0) *nmax_out = nn;
+}
+
+__global__ void k_nmax(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero,
+                       int limit, int* nmax_out) {
+  __shared__ double red[256];
+  __shared__ int done;
+  nmax_body(pperp, N, kperp, qs, bzero, limit, nmax_out, red, done);
+}
+
+}  // namespace
+
+// determine_nmax of one (context, species) in a batched launch
+struct NmaxJob {
+  const double* pperp;
+  int N;
+  double kperp, qs, bzero;
+  int* out;
+};
+
+namespace {
+
+__global__ void k_nmax_many(const NmaxJob* __restrict__ jobs, int n, int limit) {
+  __shared__ double red[256];
+  __shared__ int done;
+  if ((int)blockIdx.x >= n) return;
+  const NmaxJob& J = jobs[blockIdx.x];
+  nmax_body(J.pperp, J.N, J.kperp, J.qs, J.bzero, limit, J.out, red, done);
 }
 
 // bessel[(n+1)*(N+1)+i] = J_n(k_perp pperp_i / q), n = -1 .. nmax+1
@@ -897,6 +952,168 @@ int launch_prepare_species(alps_ctx* c, int is) {
   return st_fit;
 }
 
+// ---------------------------------------------------------------------------
+// Batched preparation of many contexts (alps_prepare_many): the derivative
+// and ee kernels of every context on a few streams, then the
+// Levenberg-Marquardt fits of every (context, species) in one launch, one
+// warp each, then one synchronisation.  Relativistic species and the
+// Chebyshev continuation take the per-context path.
+// ---------------------------------------------------------------------------
+static FitArgs fit_args_of(const alps_ctx* c, const SpeciesHost& S) {
+  FitArgs a;
+  a.N = c->sys.nperp;
+  a.M = c->sys.npar;
+  a.nf = S.sp.n_fits;
+  a.log_fit = S.sp.log_fit;
+  for (int f = 0; f < ALPS_MAX_FITS; ++f) {
+    a.fit_type[f] = S.sp.fit_type[f];
+    a.pc[f] = S.sp.perp_correction[f];
+  }
+  a.ms = S.sp.ms;
+  a.vA = c->sys.vA;
+  a.maxsteps = c->sys.maxsteps_fit;
+  a.lambda0 = c->sys.lambda_initial_fit;
+  a.lambdafac = c->sys.lambdafac_fit;
+  a.eps = c->sys.epsilon_fit;
+  a.rel = S.sp.relat ? 1 : 0;
+  a.ng = c->sys.ngamma;
+  a.np = c->sys.npparbar;
+  a.f0rel = S.d_f0rel;
+  a.grel = S.d_grel;
+  a.prel = S.d_prel;
+  return a;
+}
+
+bool ctx_batch_preparable(const alps_ctx* c) {
+  for (const SpeciesHost& S : c->spec)
+    if (!S.loaded || S.sp.relat || (!S.sp.use_bM && S.sp.ac_method != 1)) return false;
+  return true;
+}
+
+int prepare_contexts(alps_ctx* const* ctx, int n, int* status) {
+  const int NS = 8;
+  cudaStream_t st[NS];
+  for (int q = 0; q < NS; ++q) ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st[q], cudaStreamNonBlocking));
+  std::vector<FitJob> jobs;
+  std::vector<std::pair<int, int>> who;  // (context, species) of each job
+  int rc = ALPS_OK;
+  for (int i = 0; i < n && !rc; ++i) {
+    alps_ctx* c = ctx[i];
+    cudaStream_t s = st[i % NS];
+    const int N = c->sys.nperp, M = c->sys.npar;
+    const size_t nn = (size_t)(N + 1) * (M + 1);
+    for (int is = 0; is < c->sys.nspec && !rc; ++is) {
+      SpeciesHost& S = c->spec[is];
+      if (S.sp.use_bM) continue;
+      auto fail = [&](cudaError_t e) {
+        if (e != cudaSuccess) rc = (e == cudaErrorMemoryAllocation) ? ALPS_E_OOM : ALPS_E_CUDA;
+      };
+      if (!S.d_g1) fail(cudaMalloc(&S.d_g1, nn * sizeof(double)));
+      if (!S.d_g2 && !rc) fail(cudaMalloc(&S.d_g2, nn * sizeof(double)));
+      if (!S.d_G && !rc) fail(cudaMalloc(&S.d_G, (size_t)(N - 1) * 2 * (M - 1) * sizeof(double)));
+      if (!S.d_words && !rc) fail(cudaMalloc(&S.d_words, 2 * sizeof(double)));
+      if (!rc && (rc = ensure(S.d_fit_scratch, S.fit_scratch_cap, (size_t)(M + 1) * (FIT_MAXP + 1)))) break;
+      if (rc) break;
+      fail(cudaMemsetAsync(S.d_g1, 0, nn * sizeof(double), s));
+      fail(cudaMemsetAsync(S.d_g2, 0, nn * sizeof(double), s));
+      fail(cudaMemsetAsync(S.d_words + 1, 0, sizeof(double), s));
+      dim3 grid((M - 1 + 127) / 128, N - 1);
+      k_derivatives<<<grid, 128, 0, s>>>(S.d_f0, S.d_pperp, S.d_ppar, N, M, S.d_g1, S.d_g2, S.d_G);
+      const double dpperp = S.pperp[2] - S.pperp[1], dppar = std::fabs(S.ppar[2] - S.ppar[1]);
+      const double scale = 2.0 * ALPS_PI * S.sp.qs / S.sp.ms * dpperp * dppar * 0.25;
+      k_int_ee<<<1, 256, 0, s>>>(S.d_g2, S.d_ppar, N, M, scale, S.d_words);
+      fail(cudaGetLastError());
+      FitJob j;
+      j.a = fit_args_of(c, S);
+      j.f0 = S.d_f0;
+      j.pperp = S.d_pperp;
+      j.ppar = S.d_ppar;
+      j.fit = S.d_fit;
+      j.scratch = S.d_fit_scratch;
+      j.status = reinterpret_cast<int*>(S.d_words + 1);
+      jobs.push_back(j);
+      who.push_back({i, is});
+    }
+  }
+  FitJob* d_jobs = nullptr;
+  for (int q = 0; q < NS && !rc; ++q)
+    if (cudaStreamSynchronize(st[q]) != cudaSuccess) rc = ALPS_E_CUDA;
+  if (!rc && !jobs.empty()) {
+    if (cudaMalloc(&d_jobs, jobs.size() * sizeof(FitJob)) != cudaSuccess) rc = ALPS_E_OOM;
+    if (!rc && cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(FitJob), cudaMemcpyHostToDevice, st[0]) !=
+                   cudaSuccess)
+      rc = ALPS_E_CUDA;
+    if (!rc) {
+      k_lm_fit_many<<<(unsigned)jobs.size(), 32, 0, st[0]>>>(d_jobs, (int)jobs.size());
+      if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st[0]) != cudaSuccess) rc = ALPS_E_CUDA;
+    }
+  }
+  // ee terms and fit statuses, then the continuation factors (asynchronous)
+  for (size_t k = 0; k < who.size() && !rc; ++k) {
+    alps_ctx* c = ctx[who[k].first];
+    SpeciesHost& S = c->spec[who[k].second];
+    double w[2];
+    if (cudaMemcpy(w, S.d_words, 2 * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) {
+      rc = ALPS_E_CUDA;
+      break;
+    }
+    S.int_ee = w[0];
+    int fst = 0;
+    memcpy(&fst, &w[1], sizeof(int));
+    if (fst && status && !status[who[k].first]) status[who[k].first] = fst;
+  }
+  for (int q = 0; q < NS; ++q) cudaStreamDestroy(st[q]);
+  cudaFree(d_jobs);
+  return rc;
+}
+
+// determine_nmax of every (non-closed-form) species of every context in one
+// launch; nm[i][s] receives the results (closed-form species get 1)
+int nmax_contexts(alps_ctx* const* ctx, int n, const double* kperp, std::vector<std::vector<int>>& nm) {
+  std::vector<NmaxJob> jobs;
+  std::vector<std::pair<int, int>> who;
+  int* d_out = nullptr;
+  NmaxJob* d_jobs = nullptr;
+  nm.assign(n, {});
+  size_t tot = 0;
+  for (int i = 0; i < n; ++i) tot += ctx[i]->sys.nspec;
+  ALPS_CUDA_TRY(cudaMalloc(&d_out, (tot ? tot : 1) * sizeof(int)));
+  size_t k = 0;
+  for (int i = 0; i < n; ++i) {
+    nm[i].assign(ctx[i]->sys.nspec, 1);
+    for (int is = 0; is < ctx[i]->sys.nspec; ++is, ++k) {
+      const SpeciesHost& S = ctx[i]->spec[is];
+      if (S.sp.use_bM) continue;
+      NmaxJob j{S.d_pperp, ctx[i]->sys.nperp, kperp[i], S.sp.qs, ctx[i]->sys.Bessel_zero, d_out + k};
+      jobs.push_back(j);
+      who.push_back({i, is});
+    }
+  }
+  int rc = ALPS_OK;
+  std::vector<int> out(tot ? tot : 1, 0);
+  if (!jobs.empty()) {
+    if (cudaMalloc(&d_jobs, jobs.size() * sizeof(NmaxJob)) != cudaSuccess) rc = ALPS_E_OOM;
+    if (!rc && cudaMemcpy(d_jobs, jobs.data(), jobs.size() * sizeof(NmaxJob), cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = ALPS_E_CUDA;
+    if (!rc) {
+      k_nmax_many<<<(unsigned)jobs.size(), 256>>>(d_jobs, (int)jobs.size(), 2000);
+      if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = ALPS_E_CUDA;
+    }
+    if (!rc && cudaMemcpy(out.data(), d_out, tot * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = ALPS_E_CUDA;
+  }
+  k = 0;
+  for (int i = 0; i < n && !rc; ++i)
+    for (int is = 0; is < ctx[i]->sys.nspec; ++is, ++k)
+      if (!ctx[i]->spec[is].sp.use_bM) {
+        if (out[k] >= 2000) rc = ALPS_E_INVALID;  // orders beyond 2000 are outside the supported range
+        nm[i][is] = out[k];
+      }
+  cudaFree(d_jobs);
+  cudaFree(d_out);
+  return rc;
+}
+
 int launch_glls(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
   const int N = c->sys.nperp, M = c->sys.npar, np = S.sp.poly_order, m = np + 1;
@@ -972,7 +1189,10 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
       ALPS_CUDA_TRY(cudaMalloc(&S.d_tcws, need));
       S.tcws_cap = need;
     }
-    if ((rc = tc_product_checked(S.d_Rw, S.d_G, S.d_A, Mr, Nc, K, S.d_tcws, &S.tc_fixed, st))) return rc;
+    // (a batched set_k defers the count of FP64-recomputed entries: no sync here)
+    if ((rc = tc_product_checked(S.d_Rw, S.d_G, S.d_A, Mr, Nc, K, S.d_tcws, c->defer_sync ? nullptr : &S.tc_fixed,
+                                 st)))
+      return rc;
     S.tc_used = 1;
   } else {
     k_dgemm<<<dim3((Nc + 31) / 32, (Mr + 31) / 32), 256, 0, st>>>(Mr, Nc, K, S.d_Rw, S.d_G, S.d_A);

@@ -307,31 +307,190 @@ def run_reference(args, w, mp, rank, world):
     print(json.dumps(line))
 
 
-def served_stream(api, args):
-    """A served stream of the served-stream configuration's kinds, scaled to
-    a few seconds: Poisson arrivals of 70 % single-root polishes, 25 % k scans
-    (8 steps, root following) and 5 % 32x32 omega maps, each on its own
-    plasma drawn like the uneven batch (1-3 species, 64x128 to 128x256
-    grids), all through one alps_server.  The plasmas are prepared before
-    the stream starts; latency runs from submission to result.  Returns
-    latency percentiles per kind and throughput."""
+def kscan_leg(api, args):
+    """The plain k-scan configuration: 2 species on a 60x120 grid, Bessel
+    cutoff 1e-50 (nmax 58/24), k_perp d_p = 1, k_par d_p 0.05 -> 1 in 32 log
+    steps, the Alfven / ion-cyclotron root followed from 0.05 - 0.01i by
+    secant_osc with the reference's stopping rule (om_scan), on both
+    precision paths; the oracle runs the same scan on the host cores."""
+    import torch
+    w = workloads.config_kscan()
+    system, species = workloads.build(w, api.generate_f0)
+    sc = w["extra"]["scan"]
+    scan_args = (sc["type_s"], sc["swi"], sc["swf"], sc["log_scan"], sc["n_out"], sc["n_res"])
+    out = {"workload": "kscan32_grid60x120_kperp1_kpar0.05to1", "steps": sc["n_out"]}
+    rows_p = None
+    for precision in ("fp64", "mixed"):
+        G = api.Plasma(system, species, precision=precision)
+        G.set_k(*w["k"])
+        root = G.secant([w["extra"]["guess"][0]])[0]
+        G.om_scan(*scan_args, root)  # warm-up (graphs, tables)
+        G.set_k(*w["k"])
+        torch.cuda.synchronize()
+        e0 = G.stats().n_eval_total
+        t0 = time.perf_counter()
+        rows, _ = G.om_scan(*scan_args, root)
+        dt = time.perf_counter() - t0
+        ev = G.stats().n_eval_total - e0
+        out[precision] = {"wall_s": dt, "evals": int(ev), "evals_per_s": ev / dt, "roots_per_s": sc["n_out"] / dt,
+                          "final_root": [rows[-1, 0, 2], rows[-1, 0, 3]]}
+        if precision == "fp64":
+            rows_p = rows
+        else:
+            wp = rows_p[:, 0, 2] + 1j * rows_p[:, 0, 3]
+            wm = rows[:, 0, 2] + 1j * rows[:, 0, 3]
+            out["max_rel_diff_roots_mixed_vs_fp64"] = float(np.max(np.abs(wm - wp) / np.abs(wp)))
+        G.close()
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as po
+        po.set_threads(os.cpu_count() or 1)
+        O = po.OraclePlasma(system, species)
+        O.set_k(*w["k"])
+        ro = O.secant(w["extra"]["guess"][0])[0]
+        t0 = time.perf_counter()
+        rows_o, _ = O.scan(*scan_args, np.array([ro]))
+        dt = time.perf_counter() - t0
+        wo = rows_o[:, 0, 2] + 1j * rows_o[:, 0, 3]
+        wp = rows_p[:, 0, 2] + 1j * rows_p[:, 0, 3]
+        out["oracle"] = {"wall_s": dt, "roots_per_s": sc["n_out"] / dt, "cores": os.cpu_count(),
+                         "kind": "port", "threads": "over (species, order) work items of each det D"}
+        out["err_vs_oracle_roots_fp64"] = float(np.max(np.abs(wp - wo) / np.abs(wo)))
+    return out
+
+
+def relativistic_leg(args):
+    """The relativistic configuration at Theta = 0.3: Juettner electrons on a
+    128x256 (p_perp, p_par) grid remapped to 100 x 400 (Gamma, pparbar),
+    closed-form bi-Maxwellian protons, v_A/c = 0.01; the whistler branch
+    followed over k_par d_e 0.1 -> 2 in 64 log steps at 30 degrees (scan type
+    2), each root polished to a relative step of 1e-12.  Preparation (the
+    33 156-unknown spline system on the device) is timed apart."""
+    import torch
+    from alps_gb300 import api
+    theta = 0.3
+    w = workloads.config_relativistic(theta, nperp=128, npar=256, ngamma=100, npparbar=400)
+    system, species = workloads.build_relativistic(w, api.generate_f0)
+    t0 = time.perf_counter()
+    G = api.Plasma(system, species)
+    torch.cuda.synchronize()
+    t_prep = time.perf_counter() - t0
+    G.set_k(*w["k"])
+    root = G.polish([w["extra"]["guess"][0]], om_rtol=POLISH_RTOL)[0]
+    sc = w["extra"]["scan"]
+    e0 = G.stats().n_eval_total
+    t0 = time.perf_counter()
+    rows, _ = G.om_scan(sc["type_s"], sc["swi"], sc["swf"], sc["log_scan"], sc["n_out"], sc["n_res"], root,
+                        om_rtol=POLISH_RTOL)
+    dt = time.perf_counter() - t0
+    ev = G.stats().n_eval_total - e0
+    nm = G.nmax()
+    out = {"workload": "juettner_theta0.3_grid128x256_gamma100x400_whistler64", "prepare_s": t_prep,
+           "spline_unknowns": (system.nperp + 1) * (system.npar + 1) + 3, "scan_wall_s": dt, "evals": int(ev),
+           "evals_per_s": ev / dt, "roots_per_s": sc["n_out"] / dt, "nmax_end": nm,
+           "root_start": [rows[0, 0, 2], rows[0, 0, 3]], "root_end": [rows[-1, 0, 2], rows[-1, 0, 3]]}
+    G.close()
+    return out
+
+
+def make_plasmas(api, draws, precision, chunk=1024):
+    """Prepared contexts (f0 tables, fits, k tables) of uneven_plasma draws:
+    the per-run and per-k setup of each chunk of contexts in batched launches
+    (alps_prepare_many, alps_set_k_many)."""
+    out = []
+    for c0 in range(0, len(draws), chunk):
+        part = draws[c0:c0 + chunk]
+        built = [workloads.build_uneven(w, api.generate_f0) for w in part]
+        out += api.make_many(built, precision=precision, ks=[w["k"] for w in part])
+    return out
+
+
+def uneven_batch(api, args):
+    """The uneven-batch configuration: args.uneven_solves root solves, each
+    on its own uneven_plasma draw (1-3 species; N_perp in {64, 96, 128, 192,
+    256}, N_par = 2 N_perp; k_perp rho_p in logU[0.01, 10], so nmax 2-80),
+    polished to a relative step of 1e-12 from a guess in [0.2, 1.5] -
+    i[0, 0.1] Omega_p, all in one device-resident graph launch
+    (alps_solve_many), on the mixed and the plain FP64 path.  Preparation
+    (f0, fits, k tables) is timed apart: the state stays on the device."""
+    import torch
+    rng = np.random.default_rng(3)
+    n = args.uneven_solves
+    draws = [workloads.uneven_plasma(rng) for _ in range(n)]
+    guesses = rng.uniform(0.2, 1.5, n) - 1j * rng.uniform(0.0, 0.1, n)
+    out = {"solves": n, "grids": sorted({"%dx%d" % (w["system"].nperp, w["system"].npar) for w in draws}),
+           "species": [int(np.sum([w["system"].nspec == k for w in draws])) for k in (1, 2, 3)]}
+    res = {}
+    for precision in ("mixed", "fp64"):
+        t0 = time.perf_counter()
+        plasmas = make_plasmas(api, draws, precision)
+        torch.cuda.synchronize()
+        t_setup = time.perf_counter() - t0
+        nmax = [max(G.nmax()) for G in plasmas]
+        api.solve_many(plasmas[:8], guesses[:8])  # first graph build of the process
+        t0 = time.perf_counter()
+        roots, iters, _, conv = api.solve_many(plasmas, guesses)
+        t_batch = time.perf_counter() - t0
+        # lone solves of a sample: the latency of one solve on an idle GPU
+        lat = []
+        for k in range(0, n, max(1, n // 64)):
+            t1 = time.perf_counter()
+            api.solve_many([plasmas[k]], [guesses[k]])
+            lat.append((time.perf_counter() - t1) * 1e3)
+        evals = int(np.sum(2 + iters))  # the evaluations the root machines used (two initial, one per iteration)
+        res[precision] = {"batch_s": t_batch, "converged": int(conv.sum()), "roots_per_s": int(conv.sum()) / t_batch,
+                          "iterations": {"p50": float(np.percentile(iters, 50)), "max": int(iters.max())},
+                          "root_evals_per_s": evals / t_batch,
+                          "latency_ms_in_batch": t_batch * 1e3,
+                          "latency_ms_alone": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                                               "samples": len(lat)},
+                          "setup_s": t_setup, "nmax": {"min": int(min(nmax)), "max": int(max(nmax))}}
+        res[precision]["_roots"] = roots
+        res[precision]["_conv"] = conv
+        del plasmas
+    both = res["mixed"]["_conv"] & res["fp64"]["_conv"]
+    rel = np.abs(res["mixed"]["_roots"] - res["fp64"]["_roots"]) / np.abs(res["fp64"]["_roots"])
+    for p in res.values():
+        p.pop("_roots")
+        p.pop("_conv")
+    out.update(res)
+    # random guesses: a root finder that wanders can settle on another root
+    # on the other path; the agreement is stated over the solves that end
+    # on the same root
+    same = both & (rel <= 1e-6)
+    out["mixed_vs_fp64"] = {"both_converged": int(both.sum()), "same_root": int(same.sum()),
+                            "max_rel_diff_same_root": float(rel[same].max()) if same.any() else None}
+    out["speedup_mixed_vs_fp64"] = res["fp64"]["batch_s"] / res["mixed"]["batch_s"]
+    out["note"] = ("one graph launch per batch: fused det D of every root's two pending frequencies, then a device "
+                   "step of every root machine, repeated by a conditional WHILE node; roots/s counts converged roots")
+    return out
+
+
+def served_stream(api, args, precision):
+    """The served-stream configuration: Poisson arrivals at args.served_rate
+    per second for args.served_seconds, 70 % single-root polishes, 25 %
+    32-step k scans (root following), 5 % 256 x 256 omega maps, on plasmas
+    drawn like the uneven batch (1-3 species, 64x128 .. 256x512 grids),
+    through one alps_server.  The plasmas are device-resident pools (f0
+    tables, fits, Bessel tables and contractions prepared before the stream,
+    timed apart): polishes pick a random plasma of a pool of 512, scans one
+    of 256 (a scan owns its plasma while it moves k), maps one of 16.
+    Latency runs from submission to result, with the requests overlapping
+    on the GPU."""
     import torch
     rng = np.random.default_rng(5)
-    nreq, rate = args.served_requests, args.served_rate
+    rate, T = args.served_rate, args.served_seconds
+    nreq = int(rate * T)
     kinds = rng.choice(3, nreq, p=[0.70, 0.25, 0.05])
-    plasmas = []
-    t_setup = time.perf_counter()
-    for i in range(nreq):
-        N = (64, 96, 128)[i % 3]
-        w = workloads.uneven_plasma(rng, grid=(N, 2 * N))
-        s, sp = workloads.build_uneven(w, api.generate_f0)
-        G = api.Plasma(s, sp, precision="mixed")
-        G.set_k(*w["k"])
-        plasmas.append(G)
+    n_pol, n_scan, n_map = 512, 256, 16
+    draws = [workloads.uneven_plasma(rng) for _ in range(n_pol + n_scan + n_map)]
+    t0 = time.perf_counter()
+    plasmas = make_plasmas(api, draws, precision)
     torch.cuda.synchronize()
-    t_setup = time.perf_counter() - t_setup
+    t_setup = time.perf_counter() - t0
+    pol, scn, mpp = plasmas[:n_pol], plasmas[n_pol:n_pol + n_scan], plasmas[n_pol + n_scan:]
+    big = {id(G) for G, w in zip(pol, draws) if w["system"].nperp == 256}
     mp = _abi.alps_map_params()
-    mp.omi, mp.omf, mp.gami, mp.gamf, mp.nr, mp.ni = 0.05, 2.0, -0.3, 0.05, 32, 32
+    mp.omi, mp.omf, mp.gami, mp.gamf, mp.nr, mp.ni = 0.05, 2.0, -0.3, 0.05, 256, 256
     srv = api.Server()
     t_arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
     reqs = []
@@ -340,33 +499,41 @@ def served_stream(api, args):
         wait = t_arr[k] - (time.perf_counter() - t0)
         if wait > 0:
             time.sleep(wait)
-        G = plasmas[k]
         g = complex(rng.uniform(0.1, 1.5), -rng.uniform(0.0, 0.1))
         if kinds[k] == 0:
-            reqs.append(("polish", srv.polish(G, [g])))
+            G = pol[rng.integers(n_pol)]
+            reqs.append(("polish", id(G) in big, srv.polish(G, [g])))
         elif kinds[k] == 1:
-            sc = api.scan_def(4, 0.0, G.kpar * 1.3, True, 8, 1, G.kperp, G.kpar)
-            reqs.append(("scan", srv.scan(G, sc, [g])))
+            G = scn[rng.integers(n_scan)]
+            sc = api.scan_def(4, 0.0, G.kpar * 1.3, True, 32, 1, G.kperp, G.kpar)
+            reqs.append(("scan", False, srv.scan(G, sc, [g])))
         else:
-            reqs.append(("map", srv.map(G, mp)))
-    for _, r in reqs:
+            reqs.append(("map", False, srv.map(mpp[rng.integers(n_map)], mp)))
+    t_submit = time.perf_counter() - t0
+    for _, _, r in reqs:
         r.wait()
     wall = time.perf_counter() - t0
     st = srv.stats()
     srv.close()
-    out = {"requests": nreq, "arrival_rate_per_s": rate, "wall_s": wall, "setup_s": t_setup,
+    out = {"precision": precision, "requests": nreq, "arrival_rate_per_s": rate, "submit_s": t_submit,
+           "wall_s": wall, "completed_per_s": nreq / wall, "setup_s": t_setup, "pool": [n_pol, n_scan, n_map],
            "batches": st["batches"], "peak_in_flight": st["peak_active"],
            "peak_footprint_bytes": st["peak_bytes"], "latency_ms": {}}
     for kind in ("polish", "scan", "map"):
-        lat = [r.latency_ms for kk, r in reqs if kk == kind]
+        lat = [r.latency_ms for kk, _, r in reqs if kk == kind]
         if lat:
             out["latency_ms"][kind] = {"count": len(lat), "p50": float(np.percentile(lat, 50)),
                                        "p99": float(np.percentile(lat, 99))}
-    nroots = sum(1 for kk, _ in reqs if kk == "polish") + 8 * sum(1 for kk, _ in reqs if kk == "scan")
+    lat = [r.latency_ms for kk, b, r in reqs if kk == "polish" and b]
+    if lat:
+        out["latency_ms"]["polish_256x512"] = {"count": len(lat), "p50": float(np.percentile(lat, 50)),
+                                               "p99": float(np.percentile(lat, 99)), "target_p99": 20.0}
+    nroots = sum(1 for kk, _, _ in reqs if kk == "polish") + 33 * sum(1 for kk, _, _ in reqs if kk == "scan")
     out["roots_per_s"] = nroots / wall
-    out["note"] = ("every request on its own plasma, prepared before the stream; latency from submission "
-                   "to result with the requests overlapping on the GPU; polishes start from random guesses "
-                   "(up to numiter = 50 secant iterations)")
+    out["note"] = ("latency from submission to result; polishes from random guesses under the reference's "
+                   "stopping rule (up to numiter = 50 secant iterations); the stream is sustained when "
+                   "completed_per_s matches the arrival rate and wall_s stays near the stream's duration")
+    del plasmas, pol, scn, mpp
     return out
 
 
@@ -380,9 +547,13 @@ def main():
     ap.add_argument("--no-served", action="store_true", help="skip the served-stream measurement")
     ap.add_argument("--served-only", action="store_true",
                     help="run only the served stream and print its JSON object (for profiling the server)")
-    ap.add_argument("--served-requests", type=int, default=300)
-    ap.add_argument("--served-rate", type=float, default=300.0, help="Poisson arrival rate of the served stream")
+    ap.add_argument("--served-seconds", type=float, default=3.0, help="duration of the served stream's arrivals")
+    ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrival rate of the served stream")
     ap.add_argument("--ni", type=int, default=512)
+    ap.add_argument("--uneven-solves", type=int, default=4096, help="solves of the uneven-batch measurement")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
+    ap.add_argument("--no-kscan", action="store_true", help="skip the plain k-scan measurement")
+    ap.add_argument("--no-relativistic", action="store_true", help="skip the relativistic k-scan measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
@@ -405,7 +576,7 @@ def main():
     from alps_gb300 import api
     if args.served_only:
         if rank == 0:
-            print(json.dumps({"served": served_stream(api, args)}))
+            print(json.dumps({"served": {p: served_stream(api, args, p) for p in ("mixed", "fp64")}}))
         return
     # weak scaling: every replica evaluates a full lattice at its own k_par
     s = w["system"]
@@ -552,7 +723,10 @@ def main():
     root_rel = float(np.max(np.abs(roots[both] - roots_plain[both]) / np.abs(roots_plain[both]))) if both.any() \
         else None
 
-    served = None if args.no_served else served_stream(api, args)
+    served = None if (args.no_served or rank != 0) else {p: served_stream(api, args, p) for p in ("mixed", "fp64")}
+    uneven = None if (args.no_uneven or rank != 0) else uneven_batch(api, args)
+    kscan = None if (args.no_kscan or rank != 0) else kscan_leg(api, args)
+    relat = None if (args.no_relativistic or rank != 0) else relativistic_leg(args)
 
     cpu = None
     err_vs_oracle = None
@@ -616,7 +790,7 @@ def main():
                           "latency_ms": {"p50": float(np.percentile(lat, 50)) if lat else None,
                                          "p99": float(np.percentile(lat, 99)) if lat else None},
                           "roots": [[r.real, r.imag] for r in roots]},
-                "served": served}
+                "served": served, "uneven_batch": uneven, "kscan": kscan, "relativistic": relat}
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

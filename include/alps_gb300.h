@@ -152,6 +152,18 @@ int alps_set_fit(alps_ctx* ctx, int is, const double* in);
 int alps_get_f0_rel(alps_ctx* ctx, int is, double* gamma, double* pparbar, double* f0_rel, double* df_dgamma,
                     double* df_dpparbar);
 
+/* alps_prepare for n contexts at once (the per-run setup of many plasmas,
+ * e.g. of an uneven batch or a request server's pool).  The
+ * Levenberg-Marquardt continuation fits of every (context, species) run in
+ * one launch, one warp each: the reference's warm start over the p_perp
+ * rows orders a fit (src/ALPS_analyt.f90:518), but the fits of different
+ * plasmas and species are independent.  Derivatives and ee terms of all
+ * contexts run on a few streams; one synchronisation in all.  Contexts
+ * with relativistic species or Chebyshev continuations are prepared one by
+ * one.  The results are those of alps_prepare on each context.  status[i]
+ * (may be NULL) receives each context's status; returns the first error. */
+int alps_prepare_many(alps_ctx* const* ctx, int n, int* status);
+
 /* Per-wavevector setup on the device: nmax from the Bessel cutoff, Bessel
  * table, and the omega-independent p_perp contraction.
  * Replaces determine_nmax + determine_bessel_array
@@ -159,6 +171,14 @@ int alps_get_f0_rel(alps_ctx* ctx, int is, double* gamma, double* pparbar, doubl
  * (src/ALPS_fns.f90:4079-4207) has no counterpart: one device does all n. */
 int alps_set_k(alps_ctx* ctx, double kperp, double kpar);
 int alps_get_nmax(alps_ctx* ctx, int* nmax /* [nspec] */);
+
+/* alps_set_k for n contexts at once, context i at (kperp[i], kpar[i]):
+ * determine_nmax for every species of every context in one launch, then
+ * the Bessel tables and contractions of all contexts on a few streams with
+ * one synchronisation.  The results are those of alps_set_k on each
+ * context.  status[i] (may be NULL) as in alps_prepare_many. */
+int alps_set_k_many(alps_ctx* const* ctx, int n, const double* kperp,
+                    const double* kpar, int* status);
 
 /* Evaluation mode of the omega pass.
  * ALPS_PREC_FP64 (plain): every p_par pole sum is the trapezoid node sum of
@@ -486,6 +506,7 @@ typedef struct alps_stats {
   int tc_contractions;
   int64_t tc_fixed_entries;
   int64_t tc_entries;
+  int64_t n_eval_total;       /* frequencies evaluated since the context was created */
 } alps_stats;
 int alps_get_stats(alps_ctx* ctx, alps_stats* st);
 
