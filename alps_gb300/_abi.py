@@ -149,7 +149,7 @@ class alps_request(C.Structure):
         ("kind", C.c_int), ("ctx", C.c_void_p), ("n", C.c_int), ("om", C.POINTER(alps_complex)),
         ("iters", C.POINTER(C.c_int)), ("map", alps_map_params), ("map_cal", C.POINTER(alps_complex)),
         ("map_val", C.POINTER(C.c_double)), ("scan", alps_scan_def), ("scan_rows", C.POINTER(C.c_double)),
-        ("status", C.c_int), ("latency_ms", C.c_double), ("rounds", C.c_int),
+        ("status", C.c_int), ("latency_ms", C.c_double), ("rounds", C.c_int), ("om_rtol", C.c_double),
     ]
 
 

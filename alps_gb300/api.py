@@ -341,6 +341,7 @@ class Request:
         rq = _abi.alps_request()
         rq.kind = kind
         rq.ctx = plasma.handle.value if isinstance(plasma.handle, C.c_void_p) else plasma.handle
+        rq.om_rtol = float(kw.get("om_rtol", 0.0))
         self._bufs = []
         if kind in (_abi.REQ_POLISH, _abi.REQ_SCAN):
             om = np.ascontiguousarray(np.atleast_1d(kw["guesses"]), dtype=np.complex128).copy()
@@ -402,17 +403,18 @@ class Server:
         self._h = C.c_void_p()
         check(lib().alps_server_create(int(hbm_budget), int(max_active), C.byref(self._h)), "alps_server_create")
 
-    def polish(self, plasma, guesses):
-        return Request(self, _abi.REQ_POLISH, plasma, guesses=guesses)
+    def polish(self, plasma, guesses, om_rtol=0.0):
+        """om_rtol > 0 adds the relative-step stop of alps_secant_ex."""
+        return Request(self, _abi.REQ_POLISH, plasma, guesses=guesses, om_rtol=om_rtol)
 
     def map(self, plasma, mp):
         return Request(self, _abi.REQ_MAP, plasma, map=mp)
 
-    def scan(self, plasma, scan_def, roots):
+    def scan(self, plasma, scan_def, roots, om_rtol=0.0):
         """scan_def: alps_scan_def with the step sizes of scan_read (diff,
         diff2), e.g. from scan_def(); roots: the refined roots at the
         plasma's current k."""
-        return Request(self, _abi.REQ_SCAN, plasma, scan=scan_def, guesses=roots)
+        return Request(self, _abi.REQ_SCAN, plasma, scan=scan_def, guesses=roots, om_rtol=om_rtol)
 
     def stats(self):
         r, a, b = C.c_int64(), C.c_int(), C.c_size_t()

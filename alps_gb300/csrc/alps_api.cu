@@ -214,6 +214,7 @@ static int set_species_bm(alps_ctx* c, int is, const alps_species* sp) {
   int rows = fit_rows(c, is);
   if (S.d_fit) cudaFree(S.d_fit);
   S.d_fit = nullptr;
+  S.aux_ready = false;
   ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, (size_t)rows * 5 * sizeof(double)));
   ALPS_CUDA_TRY(cudaMemsetAsync(S.d_fit, 0, (size_t)rows * 5 * sizeof(double), c->stream));
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
@@ -277,6 +278,7 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
   int nf = S.sp.n_fits;
   if (S.d_fit) cudaFree(S.d_fit);
   S.d_fit = nullptr;
+  S.aux_ready = false;
   std::vector<double> fit(fit_size(c, is), 0.0);
   ALPS_CUDA_TRY(cudaMalloc(&S.d_fit, fit.size() * sizeof(double)));
   if (sp->ac_method == 1)
@@ -331,6 +333,7 @@ int alps_set_fit(alps_ctx* c, int is, const double* in) {
   SpeciesHost& S = c->spec[is];
   size_t n = fit_size(c, is);
   ALPS_CUDA_TRY(cudaMemcpyAsync(S.d_fit, in, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  S.aux_ready = false;
   int st = launch_fit_aux(c, is);
   if (st) return st;
   if (c->kset && (st = launch_landau_moments(c, is))) return st;

@@ -55,7 +55,7 @@ __host__ __device__ inline double cabs_(double2 a) { return hypot(a.x, a.y); }
 // ---------------------------------------------------------------------------
 // per-species constants visible to kernels (one copy per species)
 // ---------------------------------------------------------------------------
-struct SpecDev {
+struct __align__(16) SpecDev {
   int N, M, nmax, nf;
   int ac_method, log_fit;
   int fit_type[ALPS_MAX_FITS];
@@ -135,7 +135,7 @@ struct SpecDev {
   const double* bmI;    // exp(-z) I_n(z), n = 0..bm_nrun+1, z from k_perp
 };
 
-struct SysDev {
+struct __align__(16) SysDev {
   int nspec;
   int kperp_norm;
   int M_I, M_P;
@@ -186,6 +186,7 @@ struct SpeciesHost {
   float *d_pph = nullptr, *d_ppl = nullptr;  // ppar as float pairs
   size_t momf_cap = 0;
   double* d_fit_aux = nullptr;            // Maxwellian continuation factors
+  bool aux_ready = false;                 // d_fit_aux and the Landau row bounds are those of the current fit
   double* d_lmom = nullptr;               // factorised Landau moments
   size_t lmom_cap = 0;
   double p2r = 0, p3r = 0, la = 0, lb = 0, lc = 0, min_a0 = 0;
@@ -295,7 +296,11 @@ int launch_rel_bessel(alps_ctx* c, int is, double kperp);
 // out[(w*nspec + s)*24 + {0..5 chi, 6 + 6*(n+1) + e chi_low}]
 int launch_nhds_bessel(alps_ctx* c, int is, double kperp);
 int launch_nhds(const SysDev& sys, const SpecDev* sp, int n, const double2* d_om, double2* d_out, cudaStream_t st);
-// per-order relativistic results out[((w*nspec + s)*relcap + n)*2 + sign][6]
+// relativistic orders: REL_RB blocks of REL_THREADS threads per (omega,
+// species, signed order), each with its own partial slot
+#define REL_RB 4
+#define REL_THREADS 256
+// per-order relativistic partials out[(((w*nspec + s)*relcap + n)*2 + sign)*REL_RB + rb][6]
 int launch_rel_orders(const SysDev& sys, const SpecDev* sp, int relcap, int n, const double2* d_om, double2* d_out,
                       int* d_flags, cudaStream_t st);
 int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, double2* d_ext,
@@ -325,6 +330,7 @@ struct MultiLaunch {
 int prepare_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2* d_om, double2* d_D, int* d_flags,
                        MultiScratch** scratch, cudaStream_t st, MultiLaunch* out);
 int run_disp_multi(const MultiLaunch& ml, cudaStream_t st);
+void disp_job_layout(size_t* stride, size_t* n_offset);
 bool ctx_fusable(const alps_ctx* c);
 void fill_spec_dev(const alps_ctx* c, int is, SpecDev* out);
 int collect_profile(alps_ctx* c);

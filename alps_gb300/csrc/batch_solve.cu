@@ -18,8 +18,10 @@
 //     a bounded number of rounds), so the host neither waits for nor
 //     launches any round.  One graph launch solves the whole batch.
 //
-// A root that has finished keeps its last frequencies in its slots; their
-// determinants are evaluated and ignored until the batch ends.
+// Each root's job keeps the launch shape of a batch of two, but its
+// frequency count in the device job table follows the root: two, one (most
+// secant iterations ask for one determinant) or none once the root is done,
+// so the kernels evaluate only what the machines asked for.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -30,8 +32,21 @@
 
 namespace {
 
+// the frequency count of root r's job in the device job table: the
+// kernels evaluate only that many of its two slots (none once it is done)
+__device__ __forceinline__ void set_job_n(unsigned char* jobs, size_t stride, size_t noff, int r, int n) {
+  *reinterpret_cast<int*>(jobs + (size_t)r * stride + noff) = n;
+}
+
+__global__ void k_root_init(const RootState* __restrict__ st, int n, unsigned char* jobs, size_t stride,
+                            size_t noff) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < n) set_job_n(jobs, stride, noff, r, st[r].nwant);
+}
+
 __global__ void k_root_step(RootState* __restrict__ st, const RootParams* __restrict__ pr, double2* __restrict__ om,
-                            const double2* __restrict__ D, int n, int* active) {
+                            const double2* __restrict__ D, int n, int* active, unsigned char* jobs, size_t stride,
+                            size_t noff) {
   const int r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
   RootState s = st[r];
@@ -45,6 +60,7 @@ __global__ void k_root_step(RootState* __restrict__ st, const RootParams* __rest
     om[2 * r] = s.want[0];
     om[2 * r + 1] = (s.nwant > 1) ? s.want[1] : s.want[0];
   }
+  set_job_n(jobs, stride, noff, r, s.nwant);
 }
 
 // one thread: ends the loop when no root is active or the round limit is hit
@@ -118,7 +134,12 @@ extern "C" int alps_solve_many(alps_ctx* const* ctx, int n, int method, alps_com
       fail(rc);
       break;
     }
-    if (cudaStreamSynchronize(st) != cudaSuccess) {
+    // each job evaluates only the frequencies its root asks for
+    size_t jstride = 0, jnoff = 0;
+    disp_job_layout(&jstride, &jnoff);
+    unsigned char* djobs = const_cast<unsigned char*>(static_cast<const unsigned char*>(ml.jobs));
+    k_root_init<<<(n + 127) / 128, 128, 0, st>>>(d_st, n, djobs, jstride, jnoff);
+    if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(st) != cudaSuccess) {
       fail(ALPS_E_CUDA);
       break;
     }
@@ -149,7 +170,7 @@ extern "C" int alps_solve_many(alps_ctx* const* ctx, int n, int method, alps_com
     }
     rc = run_disp_multi(ml, st);
     if (!rc) {
-      k_root_step<<<(n + 127) / 128, 128, 0, st>>>(d_st, d_pr, d_om, d_D, n, d_ctl);
+      k_root_step<<<(n + 127) / 128, 128, 0, st>>>(d_st, d_pr, d_om, d_D, n, d_ctl, djobs, jstride, jnoff);
       k_root_cond<<<1, 1, 0, st>>>(d_ctl, d_ctl + 1, max_rounds, cond);
       if (cudaGetLastError() != cudaSuccess) rc = ALPS_E_CUDA;
     }

@@ -32,6 +32,7 @@
 // runs FP32 at 64 times its FP64 rate.  Resonance decisions, windows and
 // sample points are the reference's on both paths.
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstdio>
 #include <mutex>
@@ -131,10 +132,10 @@ __device__ __forceinline__ void df_cmul2(dflt ax, dflt ay, dflt bx, dflt by, dfl
 // renormalised after each order.  Once per chunk they are rescaled and
 // combined, acc_e = phase_e (omega S_{e,1} + kappa S_{e,2}), in FP64.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, double2 o, int js, int js_count,
+__device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, double2 o, int js, int js_count,
                                            int n_begin, int n_end, double2* acc) {
   const int M = S.M;
-  const double kpar = a.sys.kpar;
+  const double kpar = sys.kpar;
   dflt sacc[24];
   float Sf[24];
 #pragma unroll
@@ -143,12 +144,12 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
     Sf[q] = 0.0f;
   }
   const dflt oxd = df_of(o.x), oyd = df_of(o.y), msd = df_of(S.ms), qsd = df_of(S.qs);
-  const dflt kd = df_of(kpar), ikd = df_of(a.sys.ikpar), pcd = df_of(S.pcen), prd = df_of(S.prad);
+  const dflt kd = df_of(kpar), ikd = df_of(sys.ikpar), pcd = df_of(S.pcen), prd = df_of(S.prad);
   const dflt Dd = df_mul(msd, oyd);  // m omega_i
   const dflt D2 = df_mul(Dd, Dd);
   const dflt dyd = df_mul(Dd, ikd);  // Im p_res
   const dflt mox = df_mul(msd, oxd);
-  const float ikp32 = (float)a.sys.ikpar;
+  const float ikp32 = (float)sys.ikpar;
   for (int n = n_begin; n < n_end; ++n) {
     const float* __restrict__ Wh = S.Wh + (size_t)n * (M - 1) * 12;
     const float* __restrict__ Wl = S.Wl + (size_t)n * (M - 1) * 12;
@@ -178,7 +179,7 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
         g.hi2 = 0;
         dfar = cmk((double)(x32 - (float)S.pcen), (double)(dyd.h));
       } else {
-        g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+        g = res_geometry(S, sys.M_I, o, nn, kpar);
         dfar = cmk(g.pr - S.pcen, g.pi);
       }
       int K = S.kfar + 1, K32 = K;
@@ -240,11 +241,11 @@ __device__ __forceinline__ void pole_fused(const DispArgs& a, const SpecDev& S, 
             if (((j - 1) % js_count) == js) nd(j, -0.5);
           }
         }
-        const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+        const double z = sys.kperp_norm ? sys.kperp / S.qs : 1.0 / S.qs;
         const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
 #pragma unroll
         for (int q = 0; q < 12; ++q) {
-          const double f = fused_factor(n, q >> 1, z, a.sys.kperp, a.sys.kperp_norm, C0) / S.Wscale[q];
+          const double f = fused_factor(n, q >> 1, z, sys.kperp, sys.kperp_norm, C0) / S.Wscale[q];
           df_acc(sacc[2 * q], df_of(Sx[q].x * f));
           df_acc(sacc[2 * q + 1], df_of(Sx[q].y * f));
         }
@@ -387,10 +388,9 @@ __device__ __forceinline__ bool df_node_range(const SpecDev& S, const ResGeom& g
 }
 
 template <bool LOW>
-__device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh, const double2* __restrict__ om,
+__device__ __forceinline__ void pole_body(const SysDev& sys, const SpecDev& S, const DispShape& sh, const double2* __restrict__ om,
                                           int n_om, int js_count, double2* part, double2* low, int tile, int s,
                                           int chunk) {
-  const SpecDev& S = a.sp[s];
   const int n_begin = chunk * sh.csize;
   const int n_end = (S.relat || S.bm) ? n_begin : min(S.nmax + 1, n_begin + sh.csize);
   // the js_count slices of an omega are adjacent threads, so an omega's
@@ -401,10 +401,10 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
   const bool active = (w < n_om);
   const double2 o = active ? om[w] : cmk(0.0, 0.0);
   const int M = S.M;
-  const double kpar = a.sys.kpar;
+  const double kpar = sys.kpar;
   const double kappa = kpar / S.ms;
   const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
-  const double z = a.sys.kperp_norm ? a.sys.kperp / S.qs : 1.0 / S.qs;
+  const double z = sys.kperp_norm ? sys.kperp / S.qs : 1.0 / S.qs;
   const double Di = S.ms * o.y;
   const double Di2 = Di * Di;
   const double* __restrict__ pp = S.ppar;
@@ -417,13 +417,13 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
     for (int q = 0; q < (LOW ? 3 : 1); ++q) lacc[q][e] = cmk(0.0, 0.0);
   }
   if (active && !LOW && S.df_sums && S.Wh && n_end > n_begin) {
-    pole_fused(a, S, o, js, js_count, n_begin, n_end, acc);
+    pole_fused(sys, S, o, js, js_count, n_begin, n_end, acc);
   } else if (active) {
     for (int n = n_begin; n < n_end; ++n) {
       const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
       for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
         const int nn = sg ? -n : n;
-        ResGeom g = res_geometry(S, a.sys.M_I, o, nn, kpar);
+        ResGeom g = res_geometry(S, sys.M_I, o, nn, kpar);
         const double Ar = S.ms * o.x - (double)nn * S.qs;
         double2 Sx[12];
 #pragma unroll
@@ -534,7 +534,7 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
             }
           }
           // S = (1/(k_par d)) sum_k mom_k t^k
-          double2 f = cscale(inv, a.sys.ikpar);
+          double2 f = cscale(inv, sys.ikpar);
 #pragma unroll
           for (int q = 0; q < 12; ++q) Sx[q] = cmul(Sx[q], f);
         } else if (S.df_sums && df_node_range(S, g, Ar, kpar, Di)) {
@@ -626,7 +626,7 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
           }
         }
         double2 pref[6];
-        t_prefactors(nn, z, a.sys.kperp, a.sys.kperp_norm, pref);
+        t_prefactors(nn, z, sys.kperp, sys.kperp_norm, pref);
 #pragma unroll
         for (int e = 0; e < 6; ++e) {
           if (n == 0 && (e == 0 || e == 3 || e == 4)) continue;
@@ -654,7 +654,7 @@ __device__ __forceinline__ void pole_body(const DispArgs& a, const DispShape& sh
         for (int e = 0; e < 6; ++e) slice_sum(lacc[LOW ? l : 0][e]);
   }
   if (js == 0 && active) {
-    size_t base = ((size_t)w * a.sys.nspec + s) * sh.nchunk + chunk;
+    size_t base = ((size_t)w * sys.nspec + s) * sh.nchunk + chunk;
     for (int e = 0; e < 6; ++e) part[base * 6 + e] = acc[e];
     if (LOW)
       for (int l = 0; l < 3; ++l)
@@ -2023,8 +2023,17 @@ __device__ __forceinline__ void finalize_body(const DispArgs& a, const DispShape
       // orders in the reference's order; n = 0 adds yy, zz, yz only, and the
       // ee term goes into chi alone (src/ALPS_fns.f90:461-497)
       for (int n = 0; n <= S.nmax; ++n) {
-        const double2* pl = rel + ((((size_t)w * S_ + s) * a.relcap + n) * 2 + 0) * 6;
-        const double2* mi = pl + 6;
+        // the row blocks' partial sums of +n and -n, added in order
+        const double2* base = rel + ((((size_t)w * S_ + s) * a.relcap + n) * 2 + 0) * REL_RB * 6;
+        double2 pl[6], mi[6];
+        for (int e = 0; e < 6; ++e) {
+          pl[e] = base[e];
+          mi[e] = base[REL_RB * 6 + e];
+          for (int q = 1; q < REL_RB; ++q) {
+            pl[e] = cadd(pl[e], base[q * 6 + e]);
+            mi[e] = cadd(mi[e], base[(REL_RB + q) * 6 + e]);
+          }
+        }
         if (n == 0) {
           const int e0[3] = {1, 2, 5};
           for (int q = 0; q < 3; ++q) {
@@ -2197,14 +2206,27 @@ __global__ void k_classify_multi(const DispJob* __restrict__ jobs, int nj) {
   for (int q = 0; q < CLS_PER_WARP; ++q) classify_body(a, J.om, J.n, J.count, J.slot_nn, J.flags, w0 + q);
 }
 
+// copies n bytes (a multiple of 16) from global to shared memory
+__device__ __forceinline__ void stage_bytes(const void* src, void* dst, int n) {
+  const int4* s4 = reinterpret_cast<const int4*>(src);
+  int4* d4 = reinterpret_cast<int4*>(dst);
+  for (int q = threadIdx.x; q < n / 16; q += blockDim.x) d4[q] = s4[q];
+}
+
+// A pole-sums block works on one species: it stages the system constants
+// and that species' constants only (an eighth of DispArgs), which matters
+// when a fused round has many small jobs, each of many small blocks.
 template <bool LOW>
 __global__ void __launch_bounds__(128, 3) k_pole_sums_multi(const DispJob* __restrict__ jobs, int nj) {
-  __shared__ DispArgs sa;
+  __shared__ __align__(16) SysDev ssys;
+  __shared__ __align__(16) SpecDev sspec;
   const DispJob& J = job_of(jobs, nj, blockIdx.x, 1);
-  const DispArgs& a = stage_args(J.a, sa);
   const long lb = (long)blockIdx.x - J.blk[1];
   const int tile = (int)(lb % J.tiles), s = (int)((lb / J.tiles) % J.S), chunk = (int)(lb / ((long)J.tiles * J.S));
-  pole_body<LOW>(a, J.sh, J.om, J.n, J.js, J.part, J.low, tile, s, chunk);
+  stage_bytes(&J.a->sys, &ssys, sizeof(SysDev));
+  stage_bytes(&J.a->sp[s], &sspec, sizeof(SpecDev));
+  __syncthreads();
+  pole_body<LOW>(ssys, sspec, J.sh, J.om, J.n, J.js, J.part, J.low, tile, s, chunk);
 }
 
 __global__ void __launch_bounds__(RES_WARPS * 32, 3) k_resonant_multi(const DispJob* __restrict__ jobs, int nj) {
@@ -2421,6 +2443,11 @@ BatchGeom batch_geom(int n, int S_, int maxn, int rcap) {
   const int want_blocks = 152 * 4;
   const int nchunk = std::max(1, std::min(maxn + 1, (want_blocks + b.tiles * S_ - 1) / (b.tiles * S_)));
   b.sh.csize = (maxn + 1 + nchunk - 1) / nchunk;
+  // a batch of a few frequencies gives each block at least about 16
+  // (frequency, order) pairs: alone it still spreads over enough blocks, and
+  // in a fused round of thousands of such batches (the uneven batch, the
+  // server) the blocks stay worth their set-up
+  if (n < 32) b.sh.csize = std::max(b.sh.csize, std::min(maxn + 1, 16 / std::max(1, n)));
   b.sh.nchunk = (maxn + 1 + b.sh.csize - 1) / b.sh.csize;
   b.nslots = (size_t)n * S_ * rcap;
   b.sh.ipw = res_items_per_warp((long)b.nslots);
@@ -2497,7 +2524,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   if (want_low)
     if ((rcode = ensure_buf(c->d_low, c->low_cap, (size_t)n * S_ * sh.nchunk * 18))) return rcode;
   if (a.relcap)
-    if ((rcode = ensure_buf(c->d_rel, c->rel_cap, (size_t)n * S_ * a.relcap * 2 * 6))) return rcode;
+    if ((rcode = ensure_buf(c->d_rel, c->rel_cap, (size_t)n * S_ * a.relcap * 2 * REL_RB * 6))) return rcode;
   if (a.has_bm)
     if ((rcode = ensure_buf(c->d_bm, c->bm_cap, (size_t)n * S_ * 24))) return rcode;
   if (!c->d_flags) ALPS_CUDA_TRY(cudaMalloc(&c->d_flags, sizeof(int)));
@@ -2717,6 +2744,15 @@ int prepare_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2
   return ALPS_OK;
 }
 
+// Where a job's frequency count sits in the device job table: a caller that
+// lowers it between launches (alps_solve_many: roots asking for one
+// frequency, or finished) makes the kernels skip the other slots, while the
+// job's launch shape, and so its sums, stay those of the prepared size.
+void disp_job_layout(size_t* stride, size_t* n_offset) {
+  *stride = sizeof(DispJob);
+  *n_offset = offsetof(DispJob, n);
+}
+
 // The kernels of a prepared fused batch (no host work: capturable, also
 // inside a conditional graph body).
 int run_disp_multi(const MultiLaunch& ml, cudaStream_t st) {
@@ -2813,7 +2849,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   size_t o_slots = carve(off, nslots * sizeof(int));
   size_t o_part = carve(off, (size_t)n * S_ * sh.nchunk * 6 * sizeof(double2));
   size_t o_items = carve(off, nslots * 6 * sizeof(double2));
-  size_t o_rel = carve(off, (size_t)n * S_ * a.relcap * 2 * 6 * sizeof(double2));
+  size_t o_rel = carve(off, (size_t)n * S_ * a.relcap * 2 * REL_RB * 6 * sizeof(double2));
   size_t o_bm = carve(off, (size_t)n * S_ * (a.has_bm ? 24 : 0) * sizeof(double2));
   size_t o_args = carve(off, sizeof(DispArgs));
   size_t o_job = carve(off, sizeof(DispJob));

@@ -629,6 +629,17 @@ __device__ inline void c6_zero(C6& a) {
   for (int e = 0; e < 6; ++e) a.v[e] = cmk(0.0, 0.0);
 }
 
+// sum over the 32 lanes of a warp, the same butterfly on every lane (the
+// result, on all lanes, does not depend on timing)
+__device__ inline void c6_warp_sum(C6& a) {
+#pragma unroll
+  for (int e = 0; e < 6; ++e)
+    for (int o = 16; o > 0; o >>= 1) {
+      a.v[e].x += __shfl_xor_sync(0xffffffffu, a.v[e].x, o);
+      a.v[e].y += __shfl_xor_sync(0xffffffffu, a.v[e].y, o);
+    }
+}
+
 // Bessel pair of signed order m from J(k), k >= 0 (int_T_rel :1297-1329)
 template <typename T, typename F>
 __device__ inline void bessel_pair_m(int m, F J, T& b, T& bp) {
@@ -784,13 +795,13 @@ __device__ void funct_g_rel_d(const RowCtx& r, double pp, double2 G[6]) {
   const double dpb = pb[2] - pb[1];
   int close = -2;
   if (pp >= pb[0] && pp < pb[np]) {
-    int lo = 0, hi = np - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (pb[mid] <= pp) lo = mid;
-      else hi = mid - 1;
-    }
-    close = lo;
+    // the last k in 0..np-1 with pb[k] <= pp: the uniform grid's index,
+    // moved by the grid values themselves where rounding put it one off
+    int k = (int)floor((pp - pb[0]) * ((double)np / (pb[np] - pb[0])));
+    k = max(0, min(np - 1, k));
+    while (k > 0 && pb[k] > pp) --k;
+    while (k < np - 1 && pb[k + 1] <= pp) ++k;
+    close = k;
   }
   if (fr_at(S, r.ig, close + 1) <= -1.0) close = close - 1;
   if (fr_at(S, r.ig, close - 1) <= -1.0) close = close + 1;
@@ -806,8 +817,11 @@ __device__ void funct_g_rel_d(const RowCtx& r, double pp, double2 G[6]) {
   for (int e = 0; e < 6; ++e) G[e] = cadd(G[e], cscale(cscale(csub(hp[e], hm[e]), 1.0 / dpb), 0.5 * dx));
 }
 
-// principal_integral_rel (src/ALPS_fns_rel.f90:724-913)
-__device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& out) {
+// principal_integral_rel (src/ALPS_fns_rel.f90:724-913), by the 32 lanes of
+// a warp: the sample points are spread over the lanes and the lanes' sums
+// are added by a warp reduction; out (on every lane) receives the window's
+// contribution
+__device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& out, int lane) {
   const SpecDev& S = r.S;
   const SysDev& sy = r.sy;
   const double ms = S.ms, qs = S.qs, vA = sy.vA, kpar = sy.kpar;
@@ -837,9 +851,9 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
     }
   };
   if (fabs(denomI) > sy.Tlim) {
-    pair(denomR, 1.0);
-    pair(denomR + capDelta, 1.0);
-    for (int ip = 1; ip <= M_P - 1; ++ip) pair(denomR + smdelta * ip, 2.0);
+    if (lane == 0) pair(denomR, 1.0);
+    if (lane == 1) pair(denomR + capDelta, 1.0);
+    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) pair(denomR + smdelta * ip, 2.0);
   } else {
     funct_g_rel_d(r, denomR + dpb, Ga);
     funct_g_rel_d(r, denomR - dpb, Gb);
@@ -855,9 +869,9 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
 #pragma unroll
       for (int e = 0; e < 6; ++e) pi.v[e] = cadd(pi.v[e], cscale(cscale(gp[e], w), f));
     };
-    lor(denomR + capDelta, 2.0);
-    for (int ip = 1; ip <= M_P - 1; ++ip) lor(denomR + smdelta * ip, 4.0);
-    if (denomI != 0.0) {
+    if (lane == 0) lor(denomR + capDelta, 2.0);
+    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) lor(denomR + smdelta * ip, 4.0);
+    if (denomI != 0.0 && lane == 0) {
       funct_g_rel_d(r, denomR, Ga);
       double sgn = denomI > 0.0 ? 1.0 : -1.0;
 #pragma unroll
@@ -876,16 +890,20 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
 #pragma unroll
       for (int e = 0; e < 6; ++e) pi.v[e] = cadd(pi.v[e], cscale(cdiv(Ga[e], da), w * correction));
     };
-    tail(denomR + capDelta, 1.0);
-    tail(denomR + capDelta + correction * smdelta * ntiny, 1.0);
-    for (int ip = 1; ip <= ntiny - 1; ++ip) tail(denomR + capDelta + correction * smdelta * ip, 2.0);
+    if (lane == 0) tail(denomR + capDelta, 1.0);
+    if (lane == 1) tail(denomR + capDelta + correction * smdelta * ntiny, 1.0);
+    for (int ip = 1 + lane; ip <= ntiny - 1; ip += 32) tail(denomR + capDelta + correction * smdelta * ip, 2.0);
   }
+  c6_warp_sum(pi);
 #pragma unroll
   for (int e = 0; e < 6; ++e) out.v[e] = cadd(out.v[e], cscale(pi.v[e], smdelta));
 }
 
-// integrate_resU_rel for one Gamma row (src/ALPS_fns_rel.f90:516-719)
-__device__ void row_rel_d(const RowCtx& r, C6& out, bool& err) {
+// integrate_resU_rel for one Gamma row (src/ALPS_fns_rel.f90:516-719), by
+// the 32 lanes of a warp: the window decisions on every lane, the nodes and
+// the principal-value samples spread over the lanes; out (on every lane)
+// receives the row's integral
+__device__ void row_rel_d(const RowCtx& r, C6& out, bool& err, int lane) {
   const SpecDev& S = r.S;
   const SysDev& sy = r.sy;
   const double ms = S.ms, qs = S.qs, vA = sy.vA, kpar = sy.kpar;
@@ -961,15 +979,16 @@ __device__ void row_rel_d(const RowCtx& r, C6& out, bool& err) {
 #pragma unroll
     for (int e = 0; e < 6; ++e) out.v[e] = cadd(out.v[e], cscale(cdiv(h[e], den), w));
   };
-  if (int_start <= lowerlimit) term(int_start, 1.0);
-  for (int ip = int_start + 1; ip <= lowerlimit - 1; ++ip) term(ip, 2.0);
-  if (int_start < lowerlimit) term(lowerlimit, 1.0);
-  if (upperlimit <= int_end) term(upperlimit, 1.0);
-  for (int ip = upperlimit + 1; ip <= int_end - 1; ++ip) term(ip, 2.0);
-  if (upperlimit < int_end) term(int_end, 1.0);
+  if (lane == 0 && int_start <= lowerlimit) term(int_start, 1.0);
+  for (int ip = int_start + 1 + lane; ip <= lowerlimit - 1; ip += 32) term(ip, 2.0);
+  if (lane == 1 && int_start < lowerlimit) term(lowerlimit, 1.0);
+  if (lane == 2 && upperlimit <= int_end) term(upperlimit, 1.0);
+  for (int ip = upperlimit + 1 + lane; ip <= int_end - 1; ip += 32) term(ip, 2.0);
+  if (lane == 3 && upperlimit < int_end) term(int_end, 1.0);
+  c6_warp_sum(out);
 #pragma unroll
   for (int e = 0; e < 6; ++e) out.v[e] = cscale(out.v[e], dpb);
-  if (found && (lowerlimit >= int_start) && (upperlimit <= int_end)) principal_rel_d(r, ipres, upperlimit, out);
+  if (found && (lowerlimit >= int_start) && (upperlimit <= int_end)) principal_rel_d(r, ipres, upperlimit, out, lane);
 }
 
 // one Landau row of landau_integrate_rel (src/ALPS_fns_rel.f90:1005-1092)
@@ -1002,7 +1021,8 @@ __device__ void landau_row_rel_d(const RowCtx& r, C6& acc) {
 }
 
 // deterministic block sum of 12 doubles per thread (blockDim.x = 128)
-__device__ void block_sum12(double v[12], double* sh /* [4][12] */) {
+// sum over the block's threads (REL_THREADS), in warp order
+__device__ void block_sum12(double v[12], double* sh /* [REL_THREADS/32][12] */) {
 #pragma unroll
   for (int q = 0; q < 12; ++q)
     for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_down_sync(0xffffffffu, v[q], o);
@@ -1011,15 +1031,24 @@ __device__ void block_sum12(double v[12], double* sh /* [4][12] */) {
     for (int q = 0; q < 12; ++q) sh[warp * 12 + q] = v[q];
   __syncthreads();
   if (threadIdx.x == 0)
-    for (int q = 0; q < 12; ++q) v[q] = ((sh[q] + sh[12 + q]) + sh[24 + q]) + sh[36 + q];
+    for (int q = 0; q < 12; ++q) {
+      double t = sh[q];
+      for (int k = 1; k < REL_THREADS / 32; ++k) t += sh[k * 12 + q];
+      v[q] = t;
+    }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(128) k_rel_orders(RelArgs a, const double2* __restrict__ om, int n_om,
-                                                    double2* __restrict__ out, int* flags) {
-  __shared__ double sh[4 * 12];
+// One block per (omega, species, signed order, row block): the REL_RB row
+// blocks of an order each take every REL_RB-th group of Gamma rows (a warp
+// per row) or every REL_RB-th stretch of the regular grid, and write their
+// partial sums to their own slot; k_finalize adds the slots in order.
+__global__ void __launch_bounds__(REL_THREADS) k_rel_orders(RelArgs a, const double2* __restrict__ om, int n_om,
+                                                            double2* __restrict__ out, int* flags) {
+  __shared__ double sh[(REL_THREADS / 32) * 12];
   const int w = blockIdx.x, s = blockIdx.z;
-  const int n = blockIdx.y >> 1, sg = blockIdx.y & 1;
+  const int rb = blockIdx.y % REL_RB, ord = blockIdx.y / REL_RB;
+  const int n = ord >> 1, sg = ord & 1;
   const SpecDev& S = a.sp[s];
   if (w >= n_om || !S.relat || n > S.nmax || n >= a.relcap || (n == 0 && sg == 1)) return;
   const SysDev& sy = a.sys;
@@ -1047,7 +1076,7 @@ __global__ void __launch_bounds__(128) k_rel_orders(RelArgs a, const double2* __
     const double kf = kn ? 1.0 : kperp, kf2 = kn ? 1.0 : kperp * kperp;
     c6_zero(r6);
     const int LB = N + 1;
-    for (int t = threadIdx.x; t < (N - 1) * (M - 1); t += blockDim.x) {
+    for (int t = rb * blockDim.x + threadIdx.x; t < (N - 1) * (M - 1); t += REL_RB * blockDim.x) {
       int i = 1 + t / (M - 1), j = 1 + t % (M - 1);
       double wi = (i == N - 1) ? 1.0 : 2.0;
       if (i == 1 && N - 1 == 1) wi = 3.0;
@@ -1090,14 +1119,17 @@ __global__ void __launch_bounds__(128) k_rel_orders(RelArgs a, const double2* __
     c6_zero(lacc);
     bool err = false;
     const double lw = (o.y > 0.0) ? 0.0 : ((o.y < 0.0) ? 2.0 : 1.0);
-    for (int ig = 1 + threadIdx.x; ig <= S.ng - 1; ig += blockDim.x) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+    for (int ig = 1 + rb * nw + warp; ig <= S.ng - 1; ig += REL_RB * nw) {
       RowCtx rc{S, sy, o, m, ig, Kc};
       C6 row;
-      row_rel_d(rc, row, err);
+      row_rel_d(rc, row, err, lane);
       double wr = (ig <= S.ng - 2) ? 2.0 : 1.0;
+      if (lane == 0) {
 #pragma unroll
-      for (int e = 0; e < 6; ++e) acc.v[e] = cadd(acc.v[e], cscale(row.v[e], wr));
-      if (lw != 0.0) landau_row_rel_d(rc, lacc);
+        for (int e = 0; e < 6; ++e) acc.v[e] = cadd(acc.v[e], cscale(row.v[e], wr));
+        if (lw != 0.0) landau_row_rel_d(rc, lacc);
+      }
     }
     if (err) atomicOr(flags, 2);
     for (int e = 0; e < 6; ++e) {
@@ -1125,7 +1157,7 @@ __global__ void __launch_bounds__(128) k_rel_orders(RelArgs a, const double2* __
   if (threadIdx.x == 0) {
     r6.v[3] = cmk(-r6.v[3].y, r6.v[3].x);  // * i
     r6.v[5] = cmk(r6.v[5].y, -r6.v[5].x);  // * -i
-    double2* dst = out + ((((size_t)w * sy.nspec + s) * a.relcap + n) * 2 + sg) * 6;
+    double2* dst = out + (((((size_t)w * sy.nspec + s) * a.relcap + n) * 2 + sg) * REL_RB + rb) * 6;
     for (int e = 0; e < 6; ++e) dst[e] = r6.v[e];
   }
 }
@@ -1143,7 +1175,7 @@ int launch_rel_orders(const SysDev& sys, const SpecDev* sp, int relcap, int n, c
   }
   a.relcap = relcap;
   if (!any || n <= 0) return ALPS_OK;
-  k_rel_orders<<<dim3(n, 2 * relcap, sys.nspec), 128, 0, st>>>(a, d_om, n, d_out, d_flags);
+  k_rel_orders<<<dim3(n, 2 * relcap * REL_RB, sys.nspec), REL_THREADS, 0, st>>>(a, d_om, n, d_out, d_flags);
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -17,8 +17,10 @@
 // every request its slice of the determinants (root_finders.h: the
 // reference's secant_osc / secant / rtsec), releases the finished requests,
 // lets queued requests on that plasma join, and the groups go out again.  A
-// k scan moves its context's k, so it runs alone on its context, and its k
-// steps (alps_set_k, which synchronises the context) run on worker threads.
+// k scan moves its context's k, so it runs alone on its context; the k steps
+// of all scans ready for one run together (alps_set_k_many: one nmax launch,
+// the tables of all contexts, one synchronisation) on a worker thread, one
+// such batch at a time.
 // Requests join while their estimated device footprint fits the budget.
 #include <algorithm>
 #include <chrono>
@@ -67,7 +69,6 @@ struct Group {
   std::vector<Active*> members;
   // IN_FLIGHT: a batch on the context's stream; FUSED: in a fused round
   enum { IDLE, IN_FLIGHT, FUSED, STEPPING } state = IDLE;
-  std::future<void> step;  // a scan's k step
   std::vector<alps_complex> bom, bD;
   bool has_scan() const {
     for (Active* a : members)
@@ -86,7 +87,7 @@ size_t batch_bytes(const alps_ctx* c, size_t n) {
     if (c->spec[s].sp.relat) relcap = std::max(relcap, c->spec[s].nmax + 1);
   }
   size_t per = 32 + (size_t)S * ((size_t)(maxn + 1) * 6 * 16 + (size_t)rc * (6 * 16 + 4) + 4 +
-                                 (size_t)relcap * 12 * 16 + 24 * 16);
+                                 (size_t)relcap * 12 * REL_RB * 16 + 24 * 16);
   return n * per;
 }
 
@@ -137,7 +138,7 @@ void start_request(Active* a) {
     a->idx.resize(rq->n);
     for (int r = 0; r < rq->n; ++r) {
       a->idx[r] = r;
-      a->want[r] = a->rm[r].start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im));
+      a->want[r] = a->rm[r].start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im), rq->om_rtol);
     }
     return;
   }
@@ -166,10 +167,12 @@ bool evals_pending(const Active* a) {
   return false;
 }
 
-// The next k step of a scan: checks and output row of the step just
-// polished (om_scan :2540-2580), alps_set_k, root finders for the roots
-// still followed.  Runs on a worker thread; touches only this request.
-void scan_step(Active* a) {
+// The next k step of a scan, in two parts around the k change:
+// scan_step_pre records the step just polished (om_scan :2540-2580) and
+// moves the request's k (false when the scan is over); scan_step_post,
+// after the context's alps_set_k, starts root finders for the roots still
+// followed.  They touch only this request.
+bool scan_step_pre(Active* a) {
   alps_request* rq = a->rq;
   alps_ctx* c = rq->ctx;
   if (!a->rm.empty()) {
@@ -198,9 +201,14 @@ void scan_step(Active* a) {
     a->idx.clear();
   }
   a->it += 1;
-  if (a->it > a->nt) return;
+  if (a->it > a->nt) return false;
   scan_k(rq->scan, a->it, a->kp0, a->kz0, a->th0, a->k0, a->kperp, a->kpar);
-  int st = alps_set_k(c, a->kperp, a->kpar);
+  return true;
+}
+
+void scan_step_post(Active* a, int st) {
+  alps_request* rq = a->rq;
+  alps_ctx* c = rq->ctx;
   if (st) {
     a->status = st;
     return;
@@ -215,8 +223,34 @@ void scan_step(Active* a) {
     if (!a->jump[r]) continue;
     a->idx.push_back(r);
     a->rm.emplace_back();
-    a->want.push_back(a->rm.back().start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im)));
+    a->want.push_back(
+        a->rm.back().start(&c->sys, c->sys.secant_method, cplx(rq->om[r].re, rq->om[r].im), rq->om_rtol));
   }
+}
+
+// The k steps of every scan in the list on the device together: the output
+// of the steps just polished, one alps_set_k_many over the scans that move
+// on, the root finders of the new steps.  Runs on a worker thread; touches
+// only these requests and their contexts (each owned by its scan).
+void scan_steps(std::vector<Active*> list) {
+  std::vector<alps_ctx*> ctx;
+  std::vector<double> kp, kz;
+  std::vector<Active*> moving;
+  for (Active* a : list)
+    if (scan_step_pre(a)) {
+      moving.push_back(a);
+      ctx.push_back(a->rq->ctx);
+      kp.push_back(a->kperp);
+      kz.push_back(a->kpar);
+    }
+  std::vector<int> st(moving.size(), ALPS_OK);
+  if (!moving.empty()) {
+    int rc = alps_set_k_many(ctx.data(), (int)ctx.size(), kp.data(), kz.data(), st.data());
+    if (rc)
+      for (size_t k = 0; k < st.size(); ++k)
+        if (!st[k]) st[k] = rc;
+  }
+  for (size_t k = 0; k < moving.size(); ++k) scan_step_post(moving[k], st[k]);
 }
 
 // True once the request has nothing left to do.
@@ -525,6 +559,8 @@ void alps_server::run() {
   Round rounds[2];  // fused rounds in flight at once
   size_t in_use = 0;
   int n_active = 0;
+  bool step_busy = false;         // a batch of scan k steps is on its worker thread
+  std::future<void> step_future;
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(mu);
@@ -587,12 +623,21 @@ void alps_server::run() {
         R.busy = false;
       }
     }
+    // the batch of scan k steps in flight: when it has landed its groups go
+    // back to IDLE in the loop below, and the scans ready now form the next
+    bool step_done = false;
+    if (step_busy && step_future.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
+      step_future.get();
+      step_busy = false;
+      step_done = true;
+    }
+    std::vector<Group*> step_groups;
+    std::vector<Active*> step_list;
     std::vector<Group*> ready;  // groups whose next batch can join a fused round
     for (auto gi = groups.begin(); gi != groups.end();) {
       Group& g = gi->second;
       if (g.state == Group::STEPPING) {
-        if (g.step.wait_for(std::chrono::seconds(0)) == std::future_status::ready) {
-          g.step.get();
+        if (step_done) {
           g.state = Group::IDLE;
           progressed = true;
         }
@@ -629,9 +674,12 @@ void alps_server::run() {
         for (Active* a : g.members)
           if (a->rq->kind == ALPS_REQ_SCAN && !evals_pending(a)) sc = a;
         if (sc) {
-          g.state = Group::STEPPING;
-          g.step = std::async(std::launch::async, scan_step, sc);
-          progressed = true;
+          // waits for the next step batch (one in flight at a time)
+          if (!step_busy) {
+            g.state = Group::STEPPING;
+            step_groups.push_back(&g);
+            step_list.push_back(sc);
+          }
         } else if (!g.members.empty()) {
           if (!wants_map(g) && wants_evals(g) && ctx_fusable(g.ctx)) {
             ready.push_back(&g);
@@ -648,6 +696,11 @@ void alps_server::run() {
         gi = groups.erase(gi);
       else
         ++gi;
+    }
+    if (!step_list.empty()) {
+      step_future = std::async(std::launch::async, scan_steps, step_list);
+      step_busy = true;
+      progressed = true;
     }
     if (!ready.empty()) {
       // with both round slots free the ready groups split in two, so that

@@ -754,14 +754,18 @@ __global__ void k_landau_moments(const double* __restrict__ bessel, const double
   }
 }
 
+// grows a table to at least n elements; a regrown table gets a quarter
+// more, so a k scan whose nmax rises step by step reallocates (and pays
+// cudaFree's device-wide wait) only now and then
 template <typename T>
 int ensure(T*& ptr, size_t& cap, size_t n) {
   if (n <= cap && ptr) return ALPS_OK;
+  const size_t want = ptr ? n + n / 4 : n;
   if (ptr) cudaFree(ptr);
   ptr = nullptr;
   cap = 0;
-  ALPS_CUDA_TRY(cudaMalloc(&ptr, n * sizeof(T)));
-  cap = n;
+  ALPS_CUDA_TRY(cudaMalloc(&ptr, want * sizeof(T)));
+  cap = want;
   return ALPS_OK;
 }
 
@@ -884,6 +888,7 @@ __global__ void k_glls_rows(const double* __restrict__ f0, const double* __restr
 // ---------------------------------------------------------------------------
 int launch_prepare_species(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
+  S.aux_ready = false;  // a new fit: its continuation factors and bounds follow at the next set_k
   if (S.sp.use_bM) return ALPS_OK;  // closed form: nothing to derive or fit
   int N = c->sys.nperp, M = c->sys.npar;
   cudaStream_t st = c->stream;
@@ -1004,6 +1009,7 @@ int prepare_contexts(alps_ctx* const* ctx, int n, int* status) {
     const size_t nn = (size_t)(N + 1) * (M + 1);
     for (int is = 0; is < c->sys.nspec && !rc; ++is) {
       SpeciesHost& S = c->spec[is];
+      S.aux_ready = false;
       if (S.sp.use_bM) continue;
       auto fail = [&](cudaError_t e) {
         if (e != cudaSuccess) rc = (e == cudaErrorMemoryAllocation) ? ALPS_E_OOM : ALPS_E_CUDA;
@@ -1255,6 +1261,7 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
 
 int launch_fit_aux(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
+  if (S.aux_ready) return ALPS_OK;  // built for the current fit already
   bool maxw = S.sp.ac_method == 1 && !S.sp.use_bM;
   for (int f = 0; f < S.sp.n_fits && maxw; ++f) maxw = S.sp.fit_type[f] == 1;
   if (!maxw) {
@@ -1276,6 +1283,18 @@ int launch_fit_aux(alps_ctx* c, int is) {
 // term; the per-item validity bound uses max |a_i|, |b_i|, |c_i| (host).
 int launch_landau_moments(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
+  if (S.aux_ready) {
+    // the bounds belong to the fit, not to k: only the moments are per k
+    if (!S.lfact) return ALPS_OK;
+    int rc;
+    if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(S.nmax + 1) * 30))) return rc;
+    const int tot = (S.nmax + 1) * 3;
+    k_landau_moments<<<(tot + 63) / 64, 64, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, c->sys.nperp,
+                                                            S.nmax, S.pperp[2] - S.pperp[1], S.d_lmom);
+    ALPS_CUDA_TRY(cudaGetLastError());
+    return ALPS_OK;
+  }
+  S.aux_ready = true;
   S.lfact = false;
   if (!S.d_fit_aux || S.sp.n_fits != 1 || !S.d_bessel) return ALPS_OK;
   int N = c->sys.nperp, nmax = S.nmax;

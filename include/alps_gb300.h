@@ -368,7 +368,8 @@ typedef struct alps_input {
  * waits for a slower one.  The k steps of scans run on worker threads.
  * Requests that arrive while others run are admitted as soon as their
  * estimated device footprint (the context's tables and the largest batch
- * they will launch) fits the budget.  A fused launch evaluates each plasma
+ * they will launch) fits the budget.  The k steps of all scans that are ready
+ * for one go to the device together (alps_set_k_many).  A fused launch evaluates each plasma
  * with the launch shape of a lone batch of its size, so every result is
  * bit for bit what the request gives alone, whatever else is in flight.
  * ------------------------------------------------------------------------ */
@@ -392,6 +393,8 @@ typedef struct alps_request {
   int status;               /* out: ALPS_OK or an error code                               */
   double latency_ms;        /* out: submit to completion                                   */
   int rounds;               /* out: batches the request launched                           */
+  double om_rtol;           /* POLISH, SCAN: relative-step stop of alps_secant_ex, 0 = the
+                               reference's stopping rule only                              */
 } alps_request;
 
 /* hbm_budget: bytes of device memory requests may hold at once (0: 90 % of

@@ -86,11 +86,15 @@ def test_calc_eigen_batch_equals_single(kpar_fast_pair):
     O, G, w = kpar_fast_pair
     oms = [0.0099881 - 2.3e-7j, 0.012 - 1e-6j, 0.02 + 0.001j]
     batch = G.calc_eigen(oms)
+    # a batch of 9 evaluations and one of 3 sum the Bessel orders in chunks
+    # of different length (the launch shape follows the batch size), so chi
+    # agrees to rounding, about 1e-15; the heating rates difference chi over
+    # 1e-6 Re(omega), which takes that to about 1e-9
     for om, eb in zip(oms, batch):
         es = G.calc_eigen([om])[0]
         a = np.array(sum(_abi.eigen_columns(eb, 2), []))
         b = np.array(sum(_abi.eigen_columns(es, 2), []))
-        np.testing.assert_allclose(a, b, rtol=1e-12, atol=1e-300)
+        np.testing.assert_allclose(a, b, rtol=1e-8, atol=1e-300)
 
 
 def test_calc_eigen_flags(kpar_fast_pair):
