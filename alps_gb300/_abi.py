@@ -150,6 +150,23 @@ class alps_request(C.Structure):
         ("iters", C.POINTER(C.c_int)), ("map", alps_map_params), ("map_cal", C.POINTER(alps_complex)),
         ("map_val", C.POINTER(C.c_double)), ("scan", alps_scan_def), ("scan_rows", C.POINTER(C.c_double)),
         ("status", C.c_int), ("latency_ms", C.c_double), ("rounds", C.c_int), ("om_rtol", C.c_double),
+        ("converged", C.POINTER(C.c_int)),
+    ]
+
+
+class alps_server_profile(C.Structure):
+    _fields_ = [
+        ("rounds", C.c_int64), ("round_jobs", C.c_int64), ("group_batches", C.c_int64),
+        ("scan_step_batches", C.c_int64), ("scan_steps", C.c_int64), ("round_gpu_ms", C.c_double),
+        ("step_ms", C.c_double), ("loop_busy_ms", C.c_double), ("admit_ms", C.c_double),
+        ("land_ms", C.c_double), ("groups_ms", C.c_double), ("round_launch_ms", C.c_double),
+    ]
+
+
+class alps_tune_result(C.Structure):
+    _fields_ = [
+        ("js", C.c_int), ("blocks_per_sm", C.c_int), ("warps_per_sm", C.c_int), ("tuned", C.c_int),
+        ("candidates", C.c_int), ("ms_default", C.c_double), ("ms_best", C.c_double),
     ]
 
 
@@ -159,7 +176,7 @@ class alps_stats(C.Structure):
         ("n_resonant", C.c_int64), ("n_landau", C.c_int64),
         ("kernels_launched", C.c_int), ("graph_replays", C.c_int64), ("graph_captures", C.c_int64),
         ("tc_contractions", C.c_int), ("tc_fixed_entries", C.c_int64), ("tc_entries", C.c_int64),
-        ("n_eval_total", C.c_int64),
+        ("n_eval_total", C.c_int64), ("k_reused", C.c_int64),
     ]
 
 

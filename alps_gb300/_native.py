@@ -77,6 +77,9 @@ def lib():
             "alps_set_k_many": ([P(vp), C.c_int, dp, dp, P(C.c_int)], C.c_int),
             "alps_solve_many": ([P(vp), C.c_int, C.c_int, cp, C.c_double, P(C.c_int), cp, P(C.c_int)], C.c_int),
             "alps_tc_product": ([vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int, P(C.c_int)], C.c_int),
+            "alps_autotune": ([vp, C.c_int, vp, P(_abi.alps_tune_result)], C.c_int),
+            "alps_server_get_profile": ([vp, P(_abi.alps_server_profile)], C.c_int),
+            "alps_tune_clear": ([], C.c_int),
             "alps_get_profile": ([vp, dp, P(C.c_int64)], C.c_int),
             "alps_interpolate": ([dp, dp, dp, C.c_int, P(_abi.alps_interp_params), dp, dp, dp], C.c_int),
             "alps_run_interpolation": ([C.c_char_p, C.c_char_p], C.c_int),
@@ -103,6 +106,6 @@ def exported_symbols():
         "alps_get_nmax", "alps_set_precision", "alps_disp", "alps_disp_batch", "alps_disp_batch_device",
         "alps_secant", "alps_secant_ex", "alps_solve_many", "alps_prepare_many", "alps_set_k_many", "alps_map", "alps_find_minima", "alps_run_input", "alps_generate_f0", "alps_get_stats",
         "alps_set_profiling", "alps_get_profile", "alps_disp_batch_noalloc", "alps_batch_status", "alps_tc_product", "alps_read_input", "alps_read_f0",
-        "alps_get_f0_rel", "alps_calc_eigen", "alps_server_create", "alps_server_destroy", "alps_server_submit",
-        "alps_server_poll", "alps_server_wait", "alps_server_stats", "alps_interpolate", "alps_run_interpolation",
+        "alps_autotune", "alps_tune_clear", "alps_get_f0_rel", "alps_calc_eigen", "alps_server_create", "alps_server_destroy", "alps_server_submit",
+        "alps_server_poll", "alps_server_wait", "alps_server_stats", "alps_server_get_profile", "alps_interpolate", "alps_run_interpolation",
     ]

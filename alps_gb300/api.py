@@ -237,6 +237,16 @@ class Plasma:
         check(lib().alps_get_profile(self._h, _dptr(ms), C.byref(nb)), "alps_get_profile")
         return ms, nb.value
 
+    def autotune(self, n, om_device_ptr=None):
+        """alps_autotune: times the launch shapes of a batch of n
+        frequencies on this plasma and keeps the fastest for its bucket;
+        returns {js, blocks_per_sm, warps_per_sm, tuned, candidates,
+        ms_default, ms_best}."""
+        r = _abi.alps_tune_result()
+        check(lib().alps_autotune(self._h, int(n), C.c_void_p(om_device_ptr) if om_device_ptr else None,
+                                  C.byref(r)), "alps_autotune")
+        return {f: getattr(r, f) for f, _ in r._fields_}
+
     def stats(self):
         s = _abi.alps_stats()
         check(lib().alps_get_stats(self._h, C.byref(s)), "alps_get_stats")
@@ -350,6 +360,8 @@ class Request:
             rq.om = _cptr(om)
             self.iters = (C.c_int * max(1, len(om)))()
             rq.iters = C.cast(self.iters, C.POINTER(C.c_int))
+            self._conv = (C.c_int * max(1, len(om)))()
+            rq.converged = C.cast(self._conv, C.POINTER(C.c_int))
         if kind == _abi.REQ_MAP:
             mp = kw["map"]
             rq.map = mp
@@ -388,6 +400,11 @@ class Request:
         return self._rq.latency_ms
 
     @property
+    def converged(self):
+        """Polish: per root, whether it met a stopping rule before numiter."""
+        return np.array(list(self._conv)[:len(self.om)], dtype=bool)
+
+    @property
     def rounds(self):
         return self._rq.rounds
 
@@ -421,6 +438,13 @@ class Server:
         check(lib().alps_server_stats(self._h, C.byref(r), C.byref(a), C.byref(b)), "alps_server_stats")
         return {"batches": r.value, "peak_active": a.value, "peak_bytes": b.value}
 
+    def profile(self):
+        """alps_server_get_profile: rounds, jobs, device time of the rounds,
+        scan k-step batches and host loop time since creation."""
+        p = _abi.alps_server_profile()
+        check(lib().alps_server_get_profile(self._h, C.byref(p)), "alps_server_get_profile")
+        return {f: getattr(p, f) for f, _ in p._fields_}
+
     def close(self):
         if getattr(self, "_h", None):
             lib().alps_server_destroy(self._h)
@@ -447,12 +471,25 @@ def make_many(systems_species, precision="fp64", ks=None):
     st = (C.c_int * max(1, n))()
     check(lib().alps_prepare_many(_handles(plasmas), n, st), "alps_prepare_many")
     if ks is not None:
-        kp = np.ascontiguousarray([k[0] for k in ks], dtype=np.float64)
-        kz = np.ascontiguousarray([k[1] for k in ks], dtype=np.float64)
-        check(lib().alps_set_k_many(_handles(plasmas), n, _dptr(kp), _dptr(kz), st), "alps_set_k_many")
-        for p, k in zip(plasmas, ks):
-            p.kperp, p.kpar = k
+        set_k_many(plasmas, ks)
     return plasmas
+
+
+def tune_clear():
+    """alps_tune_clear: every bucket back to the default launch shapes."""
+    check(lib().alps_tune_clear(), "alps_tune_clear")
+
+
+def set_k_many(plasmas, ks):
+    """alps_set_k_many: plasmas[i] to ks[i] = (kperp, kpar), all together;
+    plasmas whose kperp stays keep their k tables."""
+    n = len(plasmas)
+    st = (C.c_int * max(1, n))()
+    kp = np.ascontiguousarray([k[0] for k in ks], dtype=np.float64)
+    kz = np.ascontiguousarray([k[1] for k in ks], dtype=np.float64)
+    check(lib().alps_set_k_many(_handles(plasmas), n, _dptr(kp), _dptr(kz), st), "alps_set_k_many")
+    for p, k in zip(plasmas, ks):
+        p.kperp, p.kpar = k
 
 
 def solve_many(plasmas, guesses, om_rtol=1e-12, method=2):

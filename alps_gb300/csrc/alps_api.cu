@@ -307,9 +307,12 @@ int alps_set_species(alps_ctx* c, int is, const alps_species* sp, const double* 
 
 int alps_prepare(alps_ctx* c) {
   if (!c) return ALPS_E_INVALID;
-  c->gen++;
   for (int is = 0; is < c->sys.nspec; ++is)
     if (!c->spec[is].loaded) return ALPS_E_INVALID;
+  // the batched setup: every species' fit in one launch, one warp each
+  // (the reference's warm start orders the rows of a fit, not the species)
+  if (ctx_batch_preparable(c)) return alps_prepare_many(&c, 1, nullptr);
+  c->gen++;
   for (int is = 0; is < c->sys.nspec; ++is) {
     int st = launch_prepare_species(c, is);
     if (st) return st;
@@ -369,9 +372,41 @@ static void set_k_commit(alps_ctx* c, double kperp, double kpar) {
   c->gen++;
 }
 
-int alps_set_k(alps_ctx* c, double kperp, double kpar) {
+// The k tables (nmax, Bessel tables, contractions, moments) depend on k_perp
+// alone: k_par enters per frequency, through the launch arguments and the
+// resonant-order capacity.  A step that keeps k_perp bit for bit, as every
+// step of a k_par scan does, keeps them and moves k_par only, the way
+// om_scan skips determine_nmax and determine_bessel_array for scan type 4
+// (src/ALPS_fns.f90:2465-2471).
+static bool tables_hold(const alps_ctx* c, double kperp) { return c->kset && c->kperp == kperp; }
+
+// resonant orders per omega: p_res moves by |q/k_par| per order, so at most
+// width*|k_par/q| + 1 orders fall in the resonance window
+static void set_rcap(alps_ctx* c, double kpar) {
+  for (int is = 0; is < c->sys.nspec; ++is) {
+    SpeciesHost& S = c->spec[is];
+    if (S.sp.use_bM) {
+      S.rcap = 1;
+      continue;
+    }
+    const int M = c->sys.npar;
+    const double dq = S.ppar[2] - S.ppar[1];
+    const double width = (S.ppar[M] - S.ppar[1]) + 2.0 * c->sys.positions_principal * dq + 2.0 * dq;
+    const double cnt = std::floor(width * std::fabs(kpar / S.sp.qs)) + 3.0;
+    S.rcap = (int)std::min<double>(2.0 * S.nmax + 1.0, cnt);
+  }
+}
+
+static int set_k_impl(alps_ctx* c, double kperp, double kpar, bool rebuild) {
   if (!c || !c->prepared) return ALPS_E_INVALID;
   if (!(kperp > 0.0) || kpar == 0.0 || !std::isfinite(kperp) || !std::isfinite(kpar)) return ALPS_E_INVALID;
+  if (!rebuild && tables_hold(c, kperp)) {
+    set_rcap(c, kpar);
+    set_k_commit(c, kperp, kpar);
+    c->stats.k_reused++;
+    return ALPS_OK;
+  }
+  c->kset = false;  // the tables are rebuilt from here on
   int S_ = c->sys.nspec;
   std::vector<int> nm(S_);
   for (int is = 0; is < S_; ++is) {
@@ -380,6 +415,8 @@ int alps_set_k(alps_ctx* c, double kperp, double kpar) {
   }
   return set_k_tables(c, kperp, kpar, nm, true);
 }
+
+int alps_set_k(alps_ctx* c, double kperp, double kpar) { return set_k_impl(c, kperp, kpar, false); }
 
 static int set_k_tables(alps_ctx* c, double kperp, double kpar, std::vector<int> nm, bool sync) {
   const int S_ = c->sys.nspec;
@@ -398,7 +435,6 @@ static int set_k_tables(alps_ctx* c, double kperp, double kpar, std::vector<int>
     SpeciesHost& S = c->spec[is];
     S.nmax = nm[is];
     if (S.sp.use_bM) {  // closed form: only the I_n table of k_perp
-      S.rcap = 1;
       int st = launch_nhds_bessel(c, is, kperp);
       if (st) return st;
       continue;
@@ -408,14 +444,8 @@ static int set_k_tables(alps_ctx* c, double kperp, double kpar, std::vector<int>
     if (S.sp.relat && (st = launch_rel_bessel(c, is, kperp))) return st;
     if ((st = launch_fit_aux(c, is))) return st;
     if ((st = launch_landau_moments(c, is))) return st;
-    // resonant orders per omega: p_res moves by |q/k_par| per order, so at
-    // most width*|k_par/q| + 1 orders fall in the resonance window
-    int M = c->sys.npar;
-    double dq = S.ppar[2] - S.ppar[1];
-    double width = (S.ppar[M] - S.ppar[1]) + 2.0 * c->sys.positions_principal * dq + 2.0 * dq;
-    double cnt = std::floor(width * std::fabs(kpar / S.sp.qs)) + 3.0;
-    S.rcap = (int)std::min<double>(2.0 * S.nmax + 1.0, cnt);
   }
+  set_rcap(c, kpar);
   if (!sync) return ALPS_OK;
   ALPS_CUDA_TRY(cudaStreamSynchronize(c->stream));
   set_k_commit(c, kperp, kpar);
@@ -464,33 +494,55 @@ int alps_set_k_many(alps_ctx* const* ctx, int n, const double* kperp, const doub
       return ALPS_E_INVALID;
     if (status) status[i] = ALPS_OK;
   }
+  // contexts whose k_perp stays keep their tables (k_par steps)
+  std::vector<alps_ctx*> rb;
+  std::vector<double> rb_kperp;
+  std::vector<int> rb_of;
+  for (int i = 0; i < n; ++i) {
+    alps_ctx* c = ctx[i];
+    if (tables_hold(c, kperp[i])) {
+      set_rcap(c, kpar[i]);
+      set_k_commit(c, kperp[i], kpar[i]);
+      c->stats.k_reused++;
+      continue;
+    }
+    c->kset = false;
+    rb.push_back(c);
+    rb_kperp.push_back(kperp[i]);
+    rb_of.push_back(i);
+  }
+  if (rb.empty()) return ALPS_OK;
   std::vector<std::vector<int>> nm;
-  int rc = nmax_contexts(ctx, n, kperp, nm);
+  int rc = nmax_contexts(rb.data(), (int)rb.size(), rb_kperp.data(), nm);
   if (rc) return rc;
   // every context's tables on a few streams, then one synchronisation
   const int NS = 8;
   cudaStream_t st[NS];
-  for (int q = 0; q < NS; ++q) ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st[q], cudaStreamNonBlocking));
+  int plo = 0, phi = 0;  // k steps gate root following: highest priority, as the server's rounds
+  ALPS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&plo, &phi));
+  for (int q = 0; q < NS; ++q) ALPS_CUDA_TRY(cudaStreamCreateWithPriority(&st[q], cudaStreamNonBlocking, phi));
   int first = ALPS_OK;
-  std::vector<char> ok(n, 0);
-  for (int i = 0; i < n; ++i) {
+  const int nb = (int)rb.size();
+  std::vector<char> ok(nb, 0);
+  for (int j = 0; j < nb; ++j) {
+    const int i = rb_of[j];
     alps_ctx* c = ctx[i];
     cudaStream_t own = c->stream;
-    c->stream = st[i % NS];
+    c->stream = st[j % NS];
     c->defer_sync = true;
-    const int s = set_k_tables(c, kperp[i], kpar[i], nm[i], false);
+    const int s = set_k_tables(c, kperp[i], kpar[i], nm[j], false);
     c->defer_sync = false;
     c->stream = own;
     if (status) status[i] = s;
     if (s && !first) first = s;
-    ok[i] = (s == ALPS_OK);
+    ok[j] = (s == ALPS_OK);
   }
   for (int q = 0; q < NS; ++q) {
     if (cudaStreamSynchronize(st[q]) != cudaSuccess && !first) first = ALPS_E_CUDA;
     cudaStreamDestroy(st[q]);
   }
-  for (int i = 0; i < n; ++i)
-    if (ok[i] && first != ALPS_E_CUDA) set_k_commit(ctx[i], kperp[i], kpar[i]);
+  for (int j = 0; j < nb; ++j)
+    if (ok[j] && first != ALPS_E_CUDA) set_k_commit(rb[j], kperp[rb_of[j]], kpar[rb_of[j]]);
   return first;
 }
 
@@ -508,7 +560,7 @@ int alps_set_precision(alps_ctx* c, int precision) {
   c->gen++;
   // the p_perp contraction is part of the precision path (FP64 on the plain
   // path, the tensor cores on the mixed one): rebuild the k tables
-  if (changed && c->kset) return alps_set_k(c, c->kperp, c->kpar);
+  if (changed && c->kset) return set_k_impl(c, c->kperp, c->kpar, true);
   return ALPS_OK;
 }
 

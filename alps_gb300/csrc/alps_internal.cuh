@@ -298,6 +298,16 @@ int launch_nhds_bessel(alps_ctx* c, int is, double kperp);
 int launch_nhds(const SysDev& sys, const SpecDev* sp, int n, const double2* d_om, double2* d_out, cudaStream_t st);
 // relativistic orders: REL_RB blocks of REL_THREADS threads per (omega,
 // species, signed order), each with its own partial slot
+// a launch shape of the batch kernels chosen by the autotuner (0: the
+// default rule's value)
+struct TuneShape {
+  int js = 0;             // j slices per omega of the pole sums (power of 2, <= 32)
+  int blocks_per_sm = 0;  // pole-sum blocks per SM the order chunks aim at
+  int warps_per_sm = 0;   // resident warps per SM the resonant slots spread over
+};
+// moves whenever the autotuner's table changes (captured graphs compare it)
+uint64_t tune_epoch();
+
 #define REL_RB 4
 #define REL_THREADS 256
 // per-order relativistic partials out[(((w*nspec + s)*relcap + n)*2 + sign)*REL_RB + rb][6]

@@ -32,9 +32,13 @@
 // runs FP32 at 64 times its FP64 rate.  Resonance decisions, windows and
 // sample points are the reference's on both paths.
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <cstddef>
 #include <cmath>
 #include <cstdio>
+#include <cstring>
+#include <map>
 #include <mutex>
 
 #include "alps_internal.cuh"
@@ -766,6 +770,11 @@ __device__ inline double2 h_node(const double* Vn, int j, int e, double2 o, doub
 #define PV_RUNV (32 * 2)
 #define PV_INTS (PV_GROUPS * 64 + 4 * 32)
 #define PV_SMEM (PV_RECV + PV_RUNV + (PV_INTS + 3) / 4)
+// record planes: sum ab (0 A, 1 B) of slot sl of (group gi, lane L); lanes
+// are adjacent within a plane, so a warp's record stores and loads touch
+// consecutive 16-byte words (no bank conflicts)
+__host__ __device__ inline int rec_at(int gi, int L, int sl, int ab) { return ((sl * 2 + ab) * PV_GROUPS + gi) * 32 + L; }
+__host__ __device__ inline int recj_at(int gi, int L, int sl) { return (sl * PV_GROUPS + gi) * 32 + L; }
 
 // node window of the principal-value sum: nodes lower-2 .. upper+2
 __host__ __device__ inline int res_win(int M_I) { return (2 * M_I + 8 < RES_WIN) ? 2 * M_I + 8 : RES_WIN; }
@@ -851,8 +860,8 @@ __host__ __device__ inline size_t res_warp_smem(int N, int W) {
 // batches take up to 256 slots per warp (about 7 waves of resident warps on
 // the map lattice); small ones spread their items over more warps (a single
 // omega's few resonant orders run side by side, as latency wants).
-inline int res_items_per_warp(long nslots) {
-  const long warps_wanted = 152L * 12;  // SMs x resident warps of k_resonant
+inline int res_items_per_warp(long nslots, int warps_per_sm = 12) {
+  const long warps_wanted = 152L * warps_per_sm;  // SMs x resident warps of k_resonant
   long ipw = nslots / warps_wanted;
   return (int)(ipw < 1 ? 1 : (ipw > 256 ? 256 : ipw));
 }
@@ -1021,13 +1030,12 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
   auto records = [&](int gi, const PvSlotF& q, int dir) {
     const bool two = q.jd >= 0;
     const int j0 = two ? q.jd : q.jc, j1 = two ? q.jc : -1;
-    const int rb = (gi * 32 + lane) * 2;
-    recj[rb] = j0;
-    recj[rb + 1] = j1;
-    recv[rb * 2] = two ? f4_of(q.Adx, q.Ady) : f4_of(q.Acx, q.Acy);
-    recv[rb * 2 + 1] = two ? f4_of(q.Bdx, q.Bdy) : f4_of(q.Bcx, q.Bcy);
-    recv[rb * 2 + 2] = two ? f4_of(q.Acx, q.Acy) : f4_of(z0, z0);
-    recv[rb * 2 + 3] = two ? f4_of(q.Bcx, q.Bcy) : f4_of(z0, z0);
+    recj[recj_at(gi, lane, 0)] = j0;
+    recj[recj_at(gi, lane, 1)] = j1;
+    recv[rec_at(gi, lane, 0, 0)] = two ? f4_of(q.Adx, q.Ady) : f4_of(q.Acx, q.Acy);
+    recv[rec_at(gi, lane, 0, 1)] = two ? f4_of(q.Bdx, q.Bdy) : f4_of(q.Bcx, q.Bcy);
+    recv[rec_at(gi, lane, 1, 0)] = two ? f4_of(q.Acx, q.Acy) : f4_of(z0, z0);
+    recv[rec_at(gi, lane, 1, 1)] = two ? f4_of(q.Bcx, q.Bcy) : f4_of(z0, z0);
     const int last = (j1 >= 0) ? j1 : j0;
     const int prev = __shfl_up_sync(0xffffffffu, last, 1);
     const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
@@ -1146,18 +1154,16 @@ __device__ __noinline__ bool pv_fast(const DispArgs& a, const SpecDev& S, const 
         Ln = runL[lane + 1];
         sn = runS[lane + 1];
       }
-      const int rb = (gi * 32 + L) * 2 + sl;
-      float4 A4 = recv[rb * 2], B4 = recv[rb * 2 + 1];
+      float4 A4 = recv[rec_at(gi, L, sl, 0)], B4 = recv[rec_at(gi, L, sl, 1)];
       dflt Ax = f4x(A4), Ay = f4y(A4), Bx = f4x(B4), By = f4y(B4);
       for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
-        const int r2 = (gi * 32 + L2) * 2;
-        const float4 a2 = recv[r2 * 2], b2 = recv[r2 * 2 + 1];
+        const float4 a2 = recv[rec_at(gi, L2, 0, 0)], b2 = recv[rec_at(gi, L2, 0, 1)];
         Ax = df_add(Ax, f4x(a2));
         Ay = df_add(Ay, f4y(a2));
         Bx = df_add(Bx, f4x(b2));
         By = df_add(By, f4y(b2));
       }
-      runJ[lane] = recj[rb];
+      runJ[lane] = recj[recj_at(gi, L, sl)];
       runv[lane * 2] = f4_of(Ax, Ay);
       runv[lane * 2 + 1] = f4_of(Bx, By);
     }
@@ -1533,13 +1539,12 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       // (lane, slot) order after the runs of the earlier groups
       auto records = [&](int gi, const PvSlot& q, int dir) {
         const int j0 = (q.jd >= 0) ? q.jd : q.jc, j1 = (q.jd >= 0) ? q.jc : -1;
-        const int rb = (gi * 32 + lane) * 2;
-        recj[rb] = j0;
-        recj[rb + 1] = j1;
-        recv[rb * 2] = (q.jd >= 0) ? q.Ad : q.Ac;
-        recv[rb * 2 + 1] = (q.jd >= 0) ? q.Bd : q.Bc;
-        recv[rb * 2 + 2] = (q.jd >= 0) ? q.Ac : cmk(0.0, 0.0);
-        recv[rb * 2 + 3] = (q.jd >= 0) ? q.Bc : cmk(0.0, 0.0);
+        recj[recj_at(gi, lane, 0)] = j0;
+        recj[recj_at(gi, lane, 1)] = j1;
+        recv[rec_at(gi, lane, 0, 0)] = (q.jd >= 0) ? q.Ad : q.Ac;
+        recv[rec_at(gi, lane, 0, 1)] = (q.jd >= 0) ? q.Bd : q.Bc;
+        recv[rec_at(gi, lane, 1, 0)] = (q.jd >= 0) ? q.Ac : cmk(0.0, 0.0);
+        recv[rec_at(gi, lane, 1, 1)] = (q.jd >= 0) ? q.Bc : cmk(0.0, 0.0);
         const int last = (j1 >= 0) ? j1 : j0;
         const int prev = __shfl_up_sync(0xffffffffu, last, 1);
         const bool st0 = (j0 >= 0) && (lane == 0 || j0 != prev);
@@ -1729,14 +1734,12 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
             Ln = runL[lane + 1];
             sn = runS[lane + 1];
           }
-          const int rb = (gi * 32 + L) * 2 + sl;
-          double2 A = recv[rb * 2], B = recv[rb * 2 + 1];
+          double2 A = recv[rec_at(gi, L, sl, 0)], B = recv[rec_at(gi, L, sl, 1)];
           for (int L2 = L + 1; L2 < Ln || (L2 == Ln && sn == 1); ++L2) {
-            const int r2 = (gi * 32 + L2) * 2;
-            A = cadd(A, recv[r2 * 2]);
-            B = cadd(B, recv[r2 * 2 + 1]);
+            A = cadd(A, recv[rec_at(gi, L2, 0, 0)]);
+            B = cadd(B, recv[rec_at(gi, L2, 0, 1)]);
           }
-          runJ[lane] = recj[rb];
+          runJ[lane] = recj[recj_at(gi, L, sl)];
           runv[lane * 2] = A;
           runv[lane * 2 + 1] = B;
         }
@@ -2426,21 +2429,56 @@ void build_disp_args(const alps_ctx* c, DispArgs* a, int* maxn) {
   *maxn = mx;
 }
 
+// ---------------------------------------------------------------------------
+// Launch-shape table of the autotuner (alps_autotune).  Per bucket of
+// (N_perp, N_par, nmax + 1, batch size), each rounded up to a power of two,
+// species count and precision path: the tuned j slices per omega, pole-sum
+// blocks per SM and resonant warps per SM.  Batches outside the table take
+// the default rule of batch_geom.  A change of the table moves the tuning
+// epoch, which retires the server's captured graphs.
+// ---------------------------------------------------------------------------
+namespace {
+std::mutex g_tune_mu;
+std::map<std::array<int, 6>, TuneShape> g_tune;
+std::atomic<uint64_t> g_tune_epoch{0};
+thread_local const TuneShape* t_tune_force = nullptr;  // the autotuner's candidate
+int ceil_log2(long v) {
+  int b = 0;
+  while ((1L << b) < v) ++b;
+  return b;
+}
+std::array<int, 6> tune_key(const alps_ctx* c, int n, int maxn) {
+  return {ceil_log2(c->sys.nperp), ceil_log2(c->sys.npar), ceil_log2(maxn + 1), ceil_log2(n), c->sys.nspec,
+          c->precision};
+}
+TuneShape tune_lookup(const alps_ctx* c, int n, int maxn) {
+  if (t_tune_force) return *t_tune_force;
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (g_tune.empty()) return TuneShape{};
+  auto it = g_tune.find(tune_key(c, n, maxn));
+  return it == g_tune.end() ? TuneShape{} : it->second;
+}
+}  // namespace
+
+uint64_t tune_epoch() { return g_tune_epoch.load(); }
+
 // launch shape of a batch of n omegas on a context: j slices and order
-// chunks give small batches more pole-sum blocks, up to about four per SM.
-// The shape depends on n and the context only: the slices and chunks fix
-// the summation order.
+// chunks give small batches more pole-sum blocks, up to about four per SM
+// (default rule), or the autotuner's shape for the batch's bucket.  The
+// shape depends on n, the context and the table only: the slices and
+// chunks fix the summation order.
 struct BatchGeom {
   int js, tiles;
   size_t nslots;
   DispShape sh;
 };
-BatchGeom batch_geom(int n, int S_, int maxn, int rcap) {
+BatchGeom batch_geom(const alps_ctx* c, int n, int S_, int maxn, int rcap) {
   BatchGeom b;
-  b.js = (n < 32) ? 32 : ((n < 64) ? 4 : ((n < 128) ? 2 : 1));
+  const TuneShape ts = tune_lookup(c, n, maxn);
+  b.js = ts.js ? ts.js : ((n < 32) ? 32 : ((n < 64) ? 4 : ((n < 128) ? 2 : 1)));
   const int TW = 128 / b.js;
   b.tiles = (n + TW - 1) / TW;
-  const int want_blocks = 152 * 4;
+  const int want_blocks = 152 * (ts.blocks_per_sm ? ts.blocks_per_sm : 4);
   const int nchunk = std::max(1, std::min(maxn + 1, (want_blocks + b.tiles * S_ - 1) / (b.tiles * S_)));
   b.sh.csize = (maxn + 1 + nchunk - 1) / nchunk;
   // a batch of a few frequencies gives each block at least about 16
@@ -2450,7 +2488,7 @@ BatchGeom batch_geom(int n, int S_, int maxn, int rcap) {
   if (n < 32) b.sh.csize = std::max(b.sh.csize, std::min(maxn + 1, 16 / std::max(1, n)));
   b.sh.nchunk = (maxn + 1 + b.sh.csize - 1) / b.sh.csize;
   b.nslots = (size_t)n * S_ * rcap;
-  b.sh.ipw = res_items_per_warp((long)b.nslots);
+  b.sh.ipw = res_items_per_warp((long)b.nslots, ts.warps_per_sm ? ts.warps_per_sm : 12);
   return b;
 }
 
@@ -2506,7 +2544,7 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   DispArgs a;
   int maxn = 0;
   build_disp_args(c, &a, &maxn);
-  const BatchGeom bg = batch_geom(n, S_, maxn, a.rcap);
+  const BatchGeom bg = batch_geom(c, n, S_, maxn, a.rcap);
   const DispShape sh = bg.sh;
   const int js = bg.js, tiles = bg.tiles;
   const size_t nslots = bg.nslots;
@@ -2680,7 +2718,7 @@ int prepare_disp_multi(alps_ctx* const* ctx, const int* n, int nj, const double2
     int rcode = ctx_device_args(c, st, &da);
     if (rcode) return rcode;
     const int S_ = c->sys.nspec;
-    const BatchGeom bg = batch_geom(n[j], S_, c->args_maxn, c->args_rcap);
+    const BatchGeom bg = batch_geom(c, n[j], S_, c->args_maxn, c->args_rcap);
     DispJob& J = m->h_jobs[j];
     J.a = da;
     J.sh = bg.sh;
@@ -2838,7 +2876,7 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   DispArgs a;
   int maxn = 0;
   build_disp_args(c, &a, &maxn);
-  const BatchGeom bg = batch_geom(n, S_, maxn, a.rcap);
+  const BatchGeom bg = batch_geom(c, n, S_, maxn, a.rcap);
   const DispShape sh = bg.sh;
   const int js = bg.js, tiles = bg.tiles;
   // scratch layout: flags | count | slot_nn | part | items | relativistic orders | NHDS
@@ -2894,5 +2932,118 @@ extern "C" int alps_disp_batch_noalloc(alps_ctx* c, int n, const alps_complex* d
   k_finalize_multi<<<(unsigned)fin_blocks(sh, n), 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   c->async_flags = flags;  // alps_batch_status reads the word before the next call clears it
+  return ALPS_OK;
+}
+
+// ---------------------------------------------------------------------------
+// The autotuner: times the candidate launch shapes of a batch of n omegas
+// on this context (at its k and precision path) and keeps the fastest for
+// the batch's bucket.  Candidates: j slices per omega 1, 2, 4, 8, 16, 32 x
+// pole-sum blocks per SM 2, 4, 8 x resonant warps per SM 6, 12, 24, each
+// the best of two timed launches after a warm-up on the context's stream.
+// A shape changes only the summation order of the pole sums (slices and
+// order chunks), never which terms are summed.
+// ---------------------------------------------------------------------------
+extern "C" int alps_autotune(alps_ctx* c, int n, const alps_complex* d_om_in, alps_tune_result* out) {
+  if (!c || !c->kset || n <= 0 || !out) return ALPS_E_INVALID;
+  std::memset(out, 0, sizeof(*out));
+  double2* d_D = nullptr;
+  double2* d_omb = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = ALPS_OK;
+  auto fail = [&](int code) {
+    rc = code;
+    return code;
+  };
+  const double2* d_om = reinterpret_cast<const double2*>(d_om_in);
+  if (cudaMalloc(&d_D, (size_t)n * sizeof(double2)) != cudaSuccess) return ALPS_E_OOM;
+  if (!d_om) {
+    // a lattice over Re omega in [0.05, 2.5], Im omega in [-0.4, 0.05]
+    const int nr = std::max(1, (int)std::ceil(std::sqrt((double)n)));
+    std::vector<double2> h(n);
+    for (int i = 0; i < n; ++i) {
+      const int ir = i % nr, ii = i / nr;
+      h[i] = make_double2(0.05 + 2.45 * (ir + 0.5) / nr, -0.4 + 0.45 * (ii + 0.5) / std::max(1, (n + nr - 1) / nr));
+    }
+    if (cudaMalloc(&d_omb, (size_t)n * sizeof(double2)) != cudaSuccess) {
+      cudaFree(d_D);
+      return ALPS_E_OOM;
+    }
+    if (cudaMemcpy(d_omb, h.data(), (size_t)n * sizeof(double2), cudaMemcpyHostToDevice) != cudaSuccess)
+      fail(ALPS_E_CUDA);
+    d_om = d_omb;
+  }
+  if (!rc && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)) fail(ALPS_E_CUDA);
+  DispArgs a;
+  int maxn = 0;
+  build_disp_args(c, &a, &maxn);
+  // best of two timed launches of one shape (nullptr: the default rule)
+  auto time_shape = [&](const TuneShape* sh, float* ms) -> int {
+    t_tune_force = sh;
+    int st = launch_disp_batch(c, n, d_om, d_D, nullptr, c->stream);
+    float best = 3.0e38f;
+    for (int r = 0; r < 2 && !st; ++r) {
+      if (cudaEventRecord(e0, c->stream) != cudaSuccess) st = ALPS_E_CUDA;
+      if (!st) st = launch_disp_batch(c, n, d_om, d_D, nullptr, c->stream);
+      if (!st && cudaEventRecord(e1, c->stream) != cudaSuccess) st = ALPS_E_CUDA;
+      if (!st && cudaEventSynchronize(e1) != cudaSuccess) st = ALPS_E_CUDA;
+      float t = 0.0f;
+      if (!st && cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) st = ALPS_E_CUDA;
+      if (!st) best = std::min(best, t);
+    }
+    t_tune_force = nullptr;
+    *ms = best;
+    return st;
+  };
+  TuneShape best{};
+  float t_def = 0.0f, t_best = 3.0e38f;
+  if (!rc) rc = time_shape(nullptr, &t_def);
+  if (!rc) {
+    t_best = t_def;
+    const int jsv[6] = {1, 2, 4, 8, 16, 32}, bpv[3] = {2, 4, 8}, wpv[3] = {6, 12, 24};
+    for (int x = 0; x < 6 && !rc; ++x)
+      for (int y = 0; y < 3 && !rc; ++y)
+        for (int z = 0; z < 3 && !rc; ++z) {
+          TuneShape cand;
+          cand.js = jsv[x];
+          cand.blocks_per_sm = bpv[y];
+          cand.warps_per_sm = wpv[z];
+          float t = 0.0f;
+          rc = time_shape(&cand, &t);
+          out->candidates++;
+          // a candidate replaces the default only when it is 3 % faster
+          if (!rc && t < t_best && t < 0.97f * t_def) {
+            t_best = t;
+            best = cand;
+          }
+        }
+  }
+  if (!rc) {
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      g_tune[tune_key(c, n, maxn)] = best;
+    }
+    g_tune_epoch++;
+    const BatchGeom bg = batch_geom(c, n, c->sys.nspec, maxn, a.rcap);
+    out->js = bg.js;
+    out->blocks_per_sm = best.blocks_per_sm ? best.blocks_per_sm : 4;
+    out->warps_per_sm = best.warps_per_sm ? best.warps_per_sm : 12;
+    out->tuned = best.js != 0;
+    out->ms_default = t_def;
+    out->ms_best = t_best;
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(d_D);
+  if (d_omb) cudaFree(d_omb);
+  return rc;
+}
+
+extern "C" int alps_tune_clear(void) {
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune.clear();
+  }
+  g_tune_epoch++;
   return ALPS_OK;
 }

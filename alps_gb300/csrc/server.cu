@@ -32,6 +32,7 @@
 #include <future>
 #include <map>
 #include <mutex>
+#include <unordered_set>
 #include <thread>
 #include <vector>
 
@@ -281,9 +282,12 @@ int enqueue_batch(alps_ctx* c, int n) {
 // replay it with a single launch until the plasma, k, precision or a buffer
 // address changes (alps_ctx::gen).
 int run_batch(alps_ctx* c, int n) {
+  // a graph holds the launch shapes of its capture: the autotuner's epoch
+  // is part of its key
+  const uint64_t gk = c->gen ^ (tune_epoch() << 40);
   if (!c->profiling) {
     auto it = c->graphs.find(n);
-    if (it != c->graphs.end() && it->second.first != c->gen) {
+    if (it != c->graphs.end() && it->second.first != gk) {
       cudaGraphExecDestroy(it->second.second);
       c->graphs.erase(it);
       it = c->graphs.end();
@@ -294,7 +298,7 @@ int run_batch(alps_ctx* c, int n) {
       return ALPS_OK;
     }
     auto seen = c->graph_seen.find(n);
-    if (seen != c->graph_seen.end() && seen->second == c->gen) {
+    if (seen != c->graph_seen.end() && seen->second == gk) {
       const uint64_t gen0 = c->gen;
       cudaGraph_t graph = nullptr;
       bool launched = false;
@@ -304,7 +308,7 @@ int run_batch(alps_ctx* c, int n) {
         cudaGraphExec_t exec = nullptr;
         if (!st && e == cudaSuccess && graph && c->gen == gen0 &&
             cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
-          c->graphs[n] = {c->gen, exec};
+          c->graphs[n] = {gk, exec};
           launched = cudaGraphLaunch(exec, c->stream) == cudaSuccess;
           if (launched) c->stats.graph_captures++;
         }
@@ -316,7 +320,7 @@ int run_batch(alps_ctx* c, int n) {
   }
   int st = enqueue_batch(c, n);
   if (st) return st;
-  c->graph_seen[n] = c->gen;
+  c->graph_seen[n] = gk;
   return ALPS_OK;
 }
 
@@ -411,7 +415,9 @@ void land_group(Group& g) {
 // fusable contexts) in one set of kernels on the round's stream.
 struct Round {
   cudaStream_t st = nullptr;
-  cudaEvent_t ev = nullptr;
+  cudaEvent_t ev = nullptr;   // the round's last copy (timing: the round's device span from ev0)
+  cudaEvent_t ev0 = nullptr;  // before the round's first copy
+  size_t jobs = 0;
   MultiScratch* scratch = nullptr;
   double2* d_om = nullptr;
   double2* d_D = nullptr;
@@ -435,13 +441,20 @@ struct Round {
     cudaFree(d_flags);
     cudaFreeHost(h_flags);
     if (ev) cudaEventDestroy(ev);
+    if (ev0) cudaEventDestroy(ev0);
     if (st) cudaStreamDestroy(st);
   }
 
   int reserve(size_t n, size_t nj) {
     if (!st) {
-      ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-      ALPS_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      // root-finding rounds are latency-bound: their stream has the
+      // device's highest priority, so the block scheduler serves them ahead
+      // of map lattices (context streams, default priority) already running
+      int lo = 0, hi = 0;
+      ALPS_CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+      ALPS_CUDA_TRY(cudaStreamCreateWithPriority(&st, cudaStreamNonBlocking, hi));
+      ALPS_CUDA_TRY(cudaEventCreate(&ev));
+      ALPS_CUDA_TRY(cudaEventCreate(&ev0));
     }
     if (n > cap) {
       const size_t c2 = std::max(n, 2 * cap);
@@ -492,6 +505,8 @@ struct Round {
     if (st_) return st_;
     for (size_t j = 0; j < groups.size(); ++j)
       std::memcpy(h_om + off[j], groups[j]->bom.data(), groups[j]->bom.size() * sizeof(alps_complex));
+    jobs = groups.size();
+    ALPS_CUDA_TRY(cudaEventRecord(ev0, st));
     ALPS_CUDA_TRY(cudaMemcpyAsync(d_om, h_om, n * sizeof(double2), cudaMemcpyHostToDevice, st));
     if ((st_ = launch_disp_multi(ctx.data(), ns.data(), (int)ctx.size(), d_om, d_D, d_flags, &scratch, st)))
       return st_;
@@ -532,6 +547,8 @@ struct alps_server {
   int64_t batches = 0;
   int peak_active = 0;
   size_t peak_bytes = 0;
+  alps_server_profile prof = {};  // written by the server thread under prof_mu
+  std::mutex prof_mu;
 
   void run();
   void finish(Active* a);
@@ -544,6 +561,7 @@ void alps_server::finish(Active* a) {
       cplx o = a->rm[k].root();
       rq->om[k] = alps_complex{o.real(), o.imag()};
       if (rq->iters) rq->iters[k] = a->rm[k].iters();
+      if (rq->converged) rq->converged[k] = a->rm[k].converged() ? 1 : 0;
     }
   rq->status = a->status;
   rq->latency_ms = now_ms() - a->t0;
@@ -561,26 +579,32 @@ void alps_server::run() {
   int n_active = 0;
   bool step_busy = false;         // a batch of scan k steps is on its worker thread
   std::future<void> step_future;
+  std::chrono::steady_clock::time_point t_step;
   for (;;) {
+    const auto t_loop = std::chrono::steady_clock::now();
     {
       std::unique_lock<std::mutex> lk(mu);
       // admission, in submission order: a request joins its context's group
       // while the group is between batches, holds no scan, and (for a scan)
       // is empty, and while the footprint fits the budget
-      std::vector<alps_ctx*> blocked;  // contexts whose earlier request waits
+      std::unordered_set<alps_ctx*> blocked;  // contexts whose earlier request waits
       for (auto itq = queue.begin(); itq != queue.end() && n_active < max_active;) {
         alps_request* rq = itq->second;
         auto gi = groups.find(rq->ctx);
-        bool ok = std::find(blocked.begin(), blocked.end(), rq->ctx) == blocked.end();
+        bool ok = blocked.count(rq->ctx) == 0;
         if (ok && gi != groups.end()) {
           Group& g = gi->second;
           ok = g.state == Group::IDLE && !g.has_scan() && (rq->kind != ALPS_REQ_SCAN || g.members.empty());
         }
-        size_t nb = (rq->kind == ALPS_REQ_MAP) ? (size_t)rq->map.nr * rq->map.ni : (size_t)2 * std::max(rq->n, 1);
-        size_t need = batch_bytes(rq->ctx, nb) + (gi == groups.end() ? ctx_device_bytes(rq->ctx) : 0);
+        size_t need = 0;
+        if (ok) {
+          const size_t nb =
+              (rq->kind == ALPS_REQ_MAP) ? (size_t)rq->map.nr * rq->map.ni : (size_t)2 * std::max(rq->n, 1);
+          need = batch_bytes(rq->ctx, nb) + (gi == groups.end() ? ctx_device_bytes(rq->ctx) : 0);
+        }
         if (!ok || (in_use + need > budget && n_active > 0)) {
           // keep the context's order: later requests on it wait too
-          blocked.push_back(rq->ctx);
+          blocked.insert(rq->ctx);
           ++itq;
           continue;
         }
@@ -599,6 +623,10 @@ void alps_server::run() {
       }
       peak_active = std::max(peak_active, n_active);
       peak_bytes = std::max(peak_bytes, in_use);
+      {
+        std::lock_guard<std::mutex> pl(prof_mu);
+        prof.admit_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
+      }
       if (groups.empty()) {
         if (stop && queue.empty()) return;
         cv_work.wait(lk);
@@ -612,7 +640,12 @@ void alps_server::run() {
       if (q == cudaErrorNotReady) continue;
       progressed = true;
       if (q == cudaSuccess) {
+        float ms = 0.0f;
+        const auto t0 = std::chrono::steady_clock::now();
         R.land();
+        std::lock_guard<std::mutex> pl(prof_mu);
+        if (cudaEventElapsedTime(&ms, R.ev0, R.ev) == cudaSuccess) prof.round_gpu_ms += ms;
+        prof.land_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       } else {
         alps_set_last_cuda_error(q, "cudaEventQuery", __FILE__, __LINE__);
         for (Group* g : R.groups) {
@@ -630,10 +663,13 @@ void alps_server::run() {
       step_future.get();
       step_busy = false;
       step_done = true;
+      std::lock_guard<std::mutex> pl(prof_mu);
+      prof.step_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_step).count();
     }
     std::vector<Group*> step_groups;
     std::vector<Active*> step_list;
     std::vector<Group*> ready;  // groups whose next batch can join a fused round
+    const auto t_groups = std::chrono::steady_clock::now();
     for (auto gi = groups.begin(); gi != groups.end();) {
       Group& g = gi->second;
       if (g.state == Group::STEPPING) {
@@ -687,7 +723,11 @@ void alps_server::run() {
             int st = launch_group(g);
             if (st)
               for (Active* a : g.members) a->status = st;
-            if (g.state == Group::IN_FLIGHT) ++batches;
+            if (g.state == Group::IN_FLIGHT) {
+              ++batches;
+              std::lock_guard<std::mutex> pl(prof_mu);
+              prof.group_batches++;
+            }
             progressed = true;
           }
         }
@@ -697,7 +737,17 @@ void alps_server::run() {
       else
         ++gi;
     }
+    {
+      std::lock_guard<std::mutex> pl(prof_mu);
+      prof.groups_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_groups).count();
+    }
     if (!step_list.empty()) {
+      {
+        std::lock_guard<std::mutex> pl(prof_mu);
+        prof.scan_step_batches++;
+        prof.scan_steps += (int64_t)step_list.size();
+      }
+      t_step = std::chrono::steady_clock::now();
       step_future = std::async(std::launch::async, scan_steps, step_list);
       step_busy = true;
       progressed = true;
@@ -713,13 +763,27 @@ void alps_server::run() {
         std::vector<Group*> share(ready.begin() + ready.size() * k / parts,
                                   ready.begin() + ready.size() * (k + 1) / parts);
         Round& R = *free_rounds[k];
+        const auto t0 = std::chrono::steady_clock::now();
         int st = R.launch(share);
+        {
+          std::lock_guard<std::mutex> pl(prof_mu);
+          prof.round_launch_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        }
         if (st)
           for (Group* g : share)
             for (Active* a : g->members) a->status = st;
         batches += (int64_t)R.groups.size();
+        if (R.busy) {
+          std::lock_guard<std::mutex> pl(prof_mu);
+          prof.rounds++;
+          prof.round_jobs += (int64_t)R.jobs;
+        }
         progressed = true;
       }
+    }
+    if (progressed) {
+      std::lock_guard<std::mutex> pl(prof_mu);
+      prof.loop_busy_ms += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_loop).count();
     }
     if (!progressed) std::this_thread::sleep_for(std::chrono::microseconds(5));
   }
@@ -796,6 +860,13 @@ int alps_server_wait(alps_server* s, int64_t id) {
   if (!s->finished.count(id) && !s->pending.count(id)) return ALPS_E_INVALID;
   s->cv_done.wait(lk, [&]() { return s->finished.count(id) > 0; });
   return s->finished[id];
+}
+
+int alps_server_get_profile(alps_server* s, alps_server_profile* out) {
+  if (!s || !out) return ALPS_E_INVALID;
+  std::lock_guard<std::mutex> pl(s->prof_mu);
+  *out = s->prof;
+  return ALPS_OK;
 }
 
 int alps_server_stats(alps_server* s, int64_t* rounds, int* peak_active, size_t* peak_bytes) {

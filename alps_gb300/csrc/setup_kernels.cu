@@ -411,39 +411,62 @@ __global__ void k_lm_fit_many(const FitJob* __restrict__ jobs, int n) {
   lm_fit_body(J.a, J.f0, J.pperp, J.ppar, J.fit, J.scratch, J.status, Am_sh, jr_sh);
 }
 
-// determine_nmax for one species: smallest n >= 1 with max_i |J_n(z_i)| <=
-// Bessel_zero.  One block, threads over iperp.
+// determine_nmax for one species: the smallest n >= 1 with
+// max_i |J_n(z_i)| <= Bessel_zero, z_i = k_perp pperp_i / q, or n = limit.
+// The maximum exceeds the cutoff exactly when some node's |J_n| does.  The
+// orders go in chunks of NMAX_CHUNK: first one thread per order tests the
+// node nearest J_n's largest maximum (z = n + 0.81 n^(1/3); for orders past
+// the grid's last z that is the last node, where |J_n| is largest), which
+// settles nearly every order below the answer with one alps_bessj call;
+// then the unsettled orders, in increasing order, test every node with the
+// whole block, and the first with none above the cutoff is the answer.
+// Each order's decision is the reference's: the same alps_bessj values
+// against the same cutoff.  (The FP64 pipe is narrow on this part: one
+// call of order n costs about 5 (n + sqrt(40 n)) FP64 operations.)
+#define NMAX_CHUNK 128
 __device__ void nmax_body(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero, int limit,
-                          int* nmax_out, double* red, int& done) {
-  int nn = 0;
-  if (threadIdx.x == 0) done = 0;
-  __syncthreads();
-  while (true) {
-    nn++;
-    double m = 0.0;
-    for (int i = threadIdx.x; i <= N; i += blockDim.x) {
-      double z = __ddiv_rn(__dmul_rn(kperp, pperp[i]), qs);
-      m = fmax(m, fabs(alps_bessj(nn, z)));
+                          int* nmax_out, unsigned* settled) {
+  const int t = threadIdx.x;
+  const double zs = fabs(qs) / kperp, dp = pperp[1] - pperp[0];
+  auto above = [&](int nn, int i) {
+    const double z = __ddiv_rn(__dmul_rn(kperp, pperp[i]), qs);
+    return fabs(alps_bessj(nn, z)) > bzero;
+  };
+  for (int base = 1;; base += NMAX_CHUNK) {
+    if (t < NMAX_CHUNK) {  // whole warps (NMAX_CHUNK is a multiple of 32)
+      const int nn = base + t;
+      bool hit = false;
+      if (nn < limit) {
+        const double u = ((nn + 0.81 * cbrt((double)nn)) * zs - pperp[0]) / dp;
+        const int i0 = (u >= 0.0 && u <= (double)N) ? (int)rint(u) : ((u > 0.0 || u != u) ? N : 0);
+        hit = above(nn, i0);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, hit);
+      if ((t & 31) == 0) settled[t >> 5] = m;
     }
-    red[threadIdx.x] = m;
     __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-      if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
-      __syncthreads();
+    for (int k = 0; k < NMAX_CHUNK; ++k) {
+      const int nn = base + k;
+      if (nn >= limit) {
+        if (t == 0) *nmax_out = limit;
+        return;
+      }
+      if ((settled[k >> 5] >> (k & 31)) & 1u) continue;
+      bool hit = false;
+      for (int i = t; i <= N && !hit; i += blockDim.x) hit = above(nn, i);
+      if (!__syncthreads_or(hit)) {
+        if (t == 0) *nmax_out = nn;
+        return;
+      }
     }
-    if (threadIdx.x == 0) done = !(red[0] > bzero) || nn >= limit;
-    __syncthreads();
-    if (done) break;
-    __syncthreads();
+    __syncthreads();  // settled[] is rewritten by the next chunk
   }
-  if (threadIdx.x == 0) *nmax_out = nn;
 }
 
 __global__ void k_nmax(const double* __restrict__ pperp, int N, double kperp, double qs, double bzero,
                        int limit, int* nmax_out) {
-  __shared__ double red[256];
-  __shared__ int done;
-  nmax_body(pperp, N, kperp, qs, bzero, limit, nmax_out, red, done);
+  __shared__ unsigned settled[NMAX_CHUNK / 32];
+  nmax_body(pperp, N, kperp, qs, bzero, limit, nmax_out, settled);
 }
 
 }  // namespace
@@ -459,11 +482,10 @@ struct NmaxJob {
 namespace {
 
 __global__ void k_nmax_many(const NmaxJob* __restrict__ jobs, int n, int limit) {
-  __shared__ double red[256];
-  __shared__ int done;
+  __shared__ unsigned settled[NMAX_CHUNK / 32];
   if ((int)blockIdx.x >= n) return;
   const NmaxJob& J = jobs[blockIdx.x];
-  nmax_body(J.pperp, J.N, J.kperp, J.qs, J.bzero, limit, J.out, red, done);
+  nmax_body(J.pperp, J.N, J.kperp, J.qs, J.bzero, limit, J.out, settled);
 }
 
 // bessel[(n+1)*(N+1)+i] = J_n(k_perp pperp_i / q), n = -1 .. nmax+1
@@ -643,8 +665,13 @@ __global__ void k_moments(const double* __restrict__ V, const double* __restrict
 // vectors and moments of q (one block per q)
 __global__ void k_fused_scale(const double* __restrict__ V, const double* __restrict__ mom, int M, int nmax,
                               double z, double kperp, int kperp_norm, double C0, double* Wscale) {
-  __shared__ double red[256];
+  // |C0 v_e(n)| per order in shared memory ((nmax + 1) doubles, dynamic):
+  // max_u fl(|f_n| |x_u|) = fl(|f_n| max_u |x_u|), rounding being monotone
+  extern __shared__ double fsh[];
+  __shared__ double red[1024];
   const int q = blockIdx.x, e = q >> 1;
+  for (int n = threadIdx.x; n <= nmax; n += blockDim.x) fsh[n] = fabs(fused_factor(n, e, z, kperp, kperp_norm, C0));
+  __syncthreads();
   double mx = 0.0;
   const size_t nv = (size_t)(nmax + 1) * (M - 1), nm = (size_t)(nmax + 1) * ALPS_KFAR;
   for (size_t t = threadIdx.x; t < nv + nm; t += blockDim.x) {
@@ -652,12 +679,12 @@ __global__ void k_fused_scale(const double* __restrict__ V, const double* __rest
     const size_t u = isv ? t : t - nv;
     const int n = isv ? (int)(u / (M - 1)) : (int)(u / ALPS_KFAR);
     const double x = isv ? V[u * 12 + q] : mom[u * 12 + q];
-    mx = fmax(mx, fabs(fused_factor(n, e, z, kperp, kperp_norm, C0) * x));
+    mx = fmax(mx, fsh[n] * fabs(x));
   }
   red[threadIdx.x] = mx;
   __syncthreads();
-  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
+    if (threadIdx.x < s2) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s2]);
     __syncthreads();
   }
   if (threadIdx.x == 0) Wscale[q] = (red[0] > 0.0 && isfinite(red[0])) ? ldexp(1.0, ilogb(red[0])) : 1.0;
@@ -714,10 +741,11 @@ __global__ void k_fit_aux(const double* __restrict__ fit, const double* __restri
 // h_i = 1/2 at i = 0, N-1, N and 1 otherwise (src/ALPS_fns.f90:1389-1444).
 __global__ void k_landau_moments(const double* __restrict__ bessel, const double* __restrict__ pperp,
                                  const double* __restrict__ aux, int N, int nmax, double dpperp, double* lmom) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  // one warp per (n, F): lanes over the rows, then a warp sum
+  const int t = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (t >= (nmax + 1) * 3) return;
-  int n = t / 3, F = t % 3;
-  int L = N + 1;
+  const int n = t / 3, F = t % 3;
+  const int L = N + 1;
   auto Rw = [&](int i) {
     double J = bessel[(size_t)(n + 1) * L + i];
     double Jp = (n == 0) ? -bessel[(size_t)2 * L + i]
@@ -727,30 +755,38 @@ __global__ void k_landau_moments(const double* __restrict__ bessel, const double
     double R = (F == 0) ? J * J : (F == 1 ? (p * p) * Jp * Jp : p * J * Jp);
     return h * R;
   };
-  double p2r = aux[1], p3r = aux[2];
+  const double p2r = aux[1], p3r = aux[2];
+  const double i2d = 1.0 / (2.0 * dpperp), i1d = 1.0 / dpperp;
   double m0[5] = {0, 0, 0, 0, 0}, m1[5] = {0, 0, 0, 0, 0};
-  for (int i = 0; i <= N; ++i) {
+  for (int i = lane; i <= N; i += 32) {
     const double* ai = aux + (size_t)i * 4;
     double a0 = ai[0], p2 = ai[1], p3 = ai[2];
     double a = -(p2 - p2r), b = 2.0 * (p2 * p3 - p2r * p3r), c = -(p2 * p3 * p3 - p2r * p3r * p3r);
     double k[5] = {1.0 + c + 0.5 * c * c, b * (1.0 + c), a + 0.5 * b * b + a * c, a * b, 0.5 * a * a};
     double w0 = Rw(i) * pperp[i];
     double cc = 0.0;  // transpose of the difference operator at i
-    if (i - 1 >= 1 && i - 1 <= N - 1) cc += Rw(i - 1) / (2.0 * dpperp);
-    if (i + 1 >= 1 && i + 1 <= N - 1) cc -= Rw(i + 1) / (2.0 * dpperp);
-    if (i == 1) cc += Rw(0) / dpperp;
-    if (i == 0) cc -= Rw(0) / dpperp;
-    if (i == N) cc += Rw(N) / dpperp;
-    if (i == N - 1) cc -= Rw(N) / dpperp;
+    if (i - 1 >= 1 && i - 1 <= N - 1) cc += Rw(i - 1) * i2d;
+    if (i + 1 >= 1 && i + 1 <= N - 1) cc -= Rw(i + 1) * i2d;
+    if (i == 1) cc += Rw(0) * i1d;
+    if (i == 0) cc -= Rw(0) * i1d;
+    if (i == N) cc += Rw(N) * i1d;
+    if (i == N - 1) cc -= Rw(N) * i1d;
     for (int m = 0; m < 5; ++m) {
       m0[m] += w0 * a0 * k[m];
       m1[m] += cc * a0 * k[m];
     }
   }
-  double* o = lmom + (size_t)t * 10;
-  for (int m = 0; m < 5; ++m) {
-    o[m] = m0[m];
-    o[5 + m] = m1[m];
+  for (int m = 0; m < 5; ++m)
+    for (int off = 16; off > 0; off >>= 1) {
+      m0[m] += __shfl_xor_sync(0xffffffffu, m0[m], off);
+      m1[m] += __shfl_xor_sync(0xffffffffu, m1[m], off);
+    }
+  if (lane == 0) {
+    double* o = lmom + (size_t)t * 10;
+    for (int m = 0; m < 5; ++m) {
+      o[m] = m0[m];
+      o[5 + m] = m1[m];
+    }
   }
 }
 
@@ -1077,37 +1113,46 @@ int prepare_contexts(alps_ctx* const* ctx, int n, int* status) {
 // launch; nm[i][s] receives the results (closed-form species get 1)
 int nmax_contexts(alps_ctx* const* ctx, int n, const double* kperp, std::vector<std::vector<int>>& nm) {
   std::vector<NmaxJob> jobs;
-  std::vector<std::pair<int, int>> who;
-  int* d_out = nullptr;
-  NmaxJob* d_jobs = nullptr;
   nm.assign(n, {});
   size_t tot = 0;
   for (int i = 0; i < n; ++i) tot += ctx[i]->sys.nspec;
-  ALPS_CUDA_TRY(cudaMalloc(&d_out, (tot ? tot : 1) * sizeof(int)));
+  // the results and the job table in one stream-ordered allocation on a
+  // stream of its own: nothing here waits for other work on the device
+  const size_t ob = ((tot ? tot : 1) * sizeof(int) + 15) / 16 * 16;
+  size_t njobs = 0;
+  for (int i = 0; i < n; ++i)
+    for (int is = 0; is < ctx[i]->sys.nspec; ++is) njobs += ctx[i]->spec[is].sp.use_bM ? 0 : 1;
+  cudaStream_t st;
+  ALPS_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  unsigned char* d_buf = nullptr;
+  int rc = ALPS_OK;
+  if (cudaMallocAsync(&d_buf, ob + (njobs ? njobs : 1) * sizeof(NmaxJob), st) != cudaSuccess) rc = ALPS_E_OOM;
+  int* d_out = reinterpret_cast<int*>(d_buf);
+  NmaxJob* d_jobs = reinterpret_cast<NmaxJob*>(d_buf + ob);
   size_t k = 0;
   for (int i = 0; i < n; ++i) {
     nm[i].assign(ctx[i]->sys.nspec, 1);
     for (int is = 0; is < ctx[i]->sys.nspec; ++is, ++k) {
       const SpeciesHost& S = ctx[i]->spec[is];
       if (S.sp.use_bM) continue;
-      NmaxJob j{S.d_pperp, ctx[i]->sys.nperp, kperp[i], S.sp.qs, ctx[i]->sys.Bessel_zero, d_out + k};
-      jobs.push_back(j);
-      who.push_back({i, is});
+      jobs.push_back(NmaxJob{S.d_pperp, ctx[i]->sys.nperp, kperp[i], S.sp.qs, ctx[i]->sys.Bessel_zero, d_out + k});
     }
   }
-  int rc = ALPS_OK;
   std::vector<int> out(tot ? tot : 1, 0);
-  if (!jobs.empty()) {
-    if (cudaMalloc(&d_jobs, jobs.size() * sizeof(NmaxJob)) != cudaSuccess) rc = ALPS_E_OOM;
-    if (!rc && cudaMemcpy(d_jobs, jobs.data(), jobs.size() * sizeof(NmaxJob), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (!rc && !jobs.empty()) {
+    if (cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(NmaxJob), cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
       rc = ALPS_E_CUDA;
     if (!rc) {
-      k_nmax_many<<<(unsigned)jobs.size(), 256>>>(d_jobs, (int)jobs.size(), 2000);
-      if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) rc = ALPS_E_CUDA;
+      k_nmax_many<<<(unsigned)jobs.size(), 256, 0, st>>>(d_jobs, (int)jobs.size(), 2000);
+      if (cudaGetLastError() != cudaSuccess) rc = ALPS_E_CUDA;
     }
-    if (!rc && cudaMemcpy(out.data(), d_out, tot * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (!rc && cudaMemcpyAsync(out.data(), d_out, tot * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess)
       rc = ALPS_E_CUDA;
   }
+  if (d_buf) cudaFreeAsync(d_buf, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess && !rc) rc = ALPS_E_CUDA;
+  cudaStreamDestroy(st);
   k = 0;
   for (int i = 0; i < n && !rc; ++i)
     for (int is = 0; is < ctx[i]->sys.nspec; ++is, ++k)
@@ -1115,8 +1160,6 @@ int nmax_contexts(alps_ctx* const* ctx, int n, const double* kperp, std::vector<
         if (out[k] >= 2000) rc = ALPS_E_INVALID;  // orders beyond 2000 are outside the supported range
         nm[i][is] = out[k];
       }
-  cudaFree(d_jobs);
-  cudaFree(d_out);
   return rc;
 }
 
@@ -1206,6 +1249,22 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   }
   k_fold_reduced<<<dim3((M - 1 + 127) / 128, nmax + 1), 128, 0, st>>>(S.d_A, S.d_ppar, M, nmax, S.d_V);
   ALPS_CUDA_TRY(cudaGetLastError());
+  {
+    // the FP32 test for orders far from resonance (both paths' classify):
+    // the resonance interval of determine_resonances with a margin of 1e-5
+    // of its extent
+    const double mi = c->sys.positions_principal * (S.ppar[2] - S.ppar[1]);
+    const double rlo = std::min(S.ppar[1] - mi, S.ppar[1]), rhi = std::max(S.ppar[M], S.ppar[M - 1] + mi);
+    const double mg = 1e-5 * (std::fabs(rlo) + std::fabs(rhi));
+    S.qlo = (float)(rlo - mg);
+    S.qhi = (float)(rhi + mg);
+    S.qlo_in = (float)(rlo + mg);
+    S.qhi_in = (float)(rhi - mg);
+  }
+  // the plain path sums nodes in FP64 on V alone; the float pairs, Laurent
+  // moments and order-fused tables below serve the mixed path only (a
+  // change of path rebuilds the k tables)
+  if (c->precision == ALPS_PREC_FP64) return ALPS_OK;
   const size_t nvf = (size_t)(nmax + 1) * (M - 1) * 12;
   if ((rc = ensure(S.d_Vh, S.Vf_cap, 2 * nvf))) return rc;  // hi, then lo
   S.d_Vl = S.d_Vh + nvf;
@@ -1238,7 +1297,9 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
     const double C0 = 2.0 * ALPS_PI * dpperp * dppar_abs * 0.25 * S.sp.qs;
     if ((rc = ensure(S.d_Wh, S.Wf_cap, 2 * nvf + 3 * nmo))) return rc;  // W hi, lo; moments hi, lo, FP32
     if (!S.d_Wscale) ALPS_CUDA_TRY(cudaMalloc(&S.d_Wscale, 12 * sizeof(double)));
-    k_fused_scale<<<12, 256, 0, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp, c->sys.kperp_norm, C0, S.d_Wscale);
+    const size_t fsm = (size_t)(nmax + 1) * sizeof(double);
+    if (fsm > 48 * 1024) return ALPS_E_INVALID;  // nmax < 2000 keeps it within 16 KB
+    k_fused_scale<<<12, 1024, fsm, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp, c->sys.kperp_norm, C0, S.d_Wscale);
     ALPS_CUDA_TRY(cudaGetLastError());
     const size_t nf = nvf + nmo;
     k_fused_pairs<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp,
@@ -1246,15 +1307,6 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
                                                                 S.d_Wh + nvf, S.d_Wh + 2 * nvf,
                                                                 S.d_Wh + 2 * nvf + nmo, S.d_Wh + 2 * nvf + 2 * nmo);
     ALPS_CUDA_TRY(cudaGetLastError());
-    // the FP32 test for orders far from resonance: the resonance interval of
-    // determine_resonances with a margin of 1e-5 of its extent
-    const double mi = c->sys.positions_principal * (S.ppar[2] - S.ppar[1]);
-    const double rlo = std::min(S.ppar[1] - mi, S.ppar[1]), rhi = std::max(S.ppar[M], S.ppar[M - 1] + mi);
-    const double mg = 1e-5 * (std::fabs(rlo) + std::fabs(rhi));
-    S.qlo = (float)(rlo - mg);
-    S.qhi = (float)(rhi + mg);
-    S.qlo_in = (float)(rlo + mg);
-    S.qhi_in = (float)(rhi - mg);
   }
   return ALPS_OK;
 }
@@ -1284,13 +1336,14 @@ int launch_fit_aux(alps_ctx* c, int is) {
 int launch_landau_moments(alps_ctx* c, int is) {
   SpeciesHost& S = c->spec[is];
   if (S.aux_ready) {
-    // the bounds belong to the fit, not to k: only the moments are per k
-    if (!S.lfact) return ALPS_OK;
+    // the bounds belong to the fit, not to k: only the moments are per k,
+    // and only the mixed path reads them
+    if (!S.lfact || c->precision == ALPS_PREC_FP64) return ALPS_OK;
     int rc;
     if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(S.nmax + 1) * 30))) return rc;
     const int tot = (S.nmax + 1) * 3;
-    k_landau_moments<<<(tot + 63) / 64, 64, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, c->sys.nperp,
-                                                            S.nmax, S.pperp[2] - S.pperp[1], S.d_lmom);
+    k_landau_moments<<<(tot + 3) / 4, 128, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, c->sys.nperp,
+                                                           S.nmax, S.pperp[2] - S.pperp[1], S.d_lmom);
     ALPS_CUDA_TRY(cudaGetLastError());
     return ALPS_OK;
   }
@@ -1311,13 +1364,6 @@ int launch_landau_moments(alps_ctx* c, int is) {
     if (i >= 1) mina0 = std::min(mina0, std::fabs(aux[i * 4 + 0]));
     if (!std::isfinite(p2) || !std::isfinite(p3) || !std::isfinite(aux[i * 4])) return ALPS_OK;
   }
-  int rc;
-  if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(nmax + 1) * 30))) return rc;
-  int tot = (nmax + 1) * 3;
-  double dpperp = S.pperp[2] - S.pperp[1];
-  k_landau_moments<<<(tot + 63) / 64, 64, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, N, nmax, dpperp,
-                                                          S.d_lmom);
-  ALPS_CUDA_TRY(cudaGetLastError());
   S.p2r = p2r;
   S.p3r = p3r;
   S.la = la;
@@ -1325,5 +1371,13 @@ int launch_landau_moments(alps_ctx* c, int is) {
   S.lc = lc;
   S.min_a0 = mina0;
   S.lfact = true;
+  if (c->precision == ALPS_PREC_FP64) return ALPS_OK;
+  int rc;
+  if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(nmax + 1) * 30))) return rc;
+  int tot = (nmax + 1) * 3;
+  double dpperp = S.pperp[2] - S.pperp[1];
+  k_landau_moments<<<(tot + 3) / 4, 128, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, N, nmax, dpperp,
+                                                         S.d_lmom);
+  ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

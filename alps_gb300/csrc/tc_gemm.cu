@@ -472,18 +472,31 @@ __global__ void k_tc_kexp(const double* __restrict__ B, int K, int N, int* kexp)
 // (A~ = A 2^(kexp - eA_r), B~ = B 2^(-kexp - eB_c), both below 1); where the
 // fixed-point bound 10 K 2^-56 exceeds 2^-44 M', the entry is recomputed in
 // FP64
+__global__ void k_tc_absprep(const double* __restrict__ A, const double* __restrict__ B, int M, int N, int K,
+                             const int* __restrict__ kexp, const int* __restrict__ eA,
+                             const int* __restrict__ eB, float* Aa, float* Ba) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t na = (size_t)M * K, nb = (size_t)K * N;
+  if (t < na) {
+    const int r = (int)(t / K), k = (int)(t % K);
+    Aa[t] = (float)fabs(ldexp(A[t], kexp[k] - eA[r]));
+  } else if (t < na + nb) {
+    const size_t u = t - na;
+    const int k = (int)(u / N), c = (int)(u % N);
+    Ba[u] = (float)fabs(ldexp(B[u], -kexp[k] - eB[c]));
+  }
+}
+
+// per entry: M' = sum_k |A~||B~| in FP32 from the scaled tables (both
+// factors below 1: no overflow); where the fixed-point bound 10 K 2^-56
+// exceeds 2^-44 M', the entry is recomputed in FP64
 __global__ void k_tc_fixup(const double* __restrict__ A, const double* __restrict__ B, double* C, int M, int N,
-                           int K, const int* __restrict__ kexp, const int* __restrict__ eA,
-                           const int* __restrict__ eB, int* nfixed) {
+                           int K, const float* __restrict__ Aa, const float* __restrict__ Ba, int* nfixed) {
   const int c = blockIdx.x * blockDim.x + threadIdx.x, r = blockIdx.y;
   if (c >= N || r >= M) return;
-  const int er = eA[r], ec = eB[c];
   float m = 0.0f;
-  for (int k = 0; k < K; ++k) {  // both factors below 1: no FP32 overflow
-    const float a = (float)fabs(ldexp(A[(size_t)r * K + k], kexp[k] - er));
-    const float b = (float)fabs(ldexp(B[(size_t)k * N + c], -kexp[k] - ec));
-    m = fmaf(a, b, m);
-  }
+  const float* ar = Aa + (size_t)r * K;
+  for (int k = 0; k < K; ++k) m = fmaf(ar[k], Ba[(size_t)k * N + c], m);
   // accept when 10 K 2^-56 <= 2^-44 M', i.e. M' >= 10 K 2^-12
   if ((double)m >= 10.0 * K * 0x1p-12) return;
   double s = 0.0;
@@ -495,7 +508,8 @@ __global__ void k_tc_fixup(const double* __restrict__ A, const double* __restric
 }  // namespace
 
 size_t tc_checked_workspace_bytes(int M, int N, int K) {
-  return tc_workspace_bytes(M, N, K) + (size_t)M * N * sizeof(double) + (size_t)K * sizeof(int) + 1024;
+  return tc_workspace_bytes(M, N, K) + (size_t)M * N * sizeof(double) + (size_t)K * sizeof(int) +
+         ((size_t)M * K + (size_t)K * N) * sizeof(float) + 1536;
 }
 
 int tc_product_checked(const double* A, const double* B, double* C, int M, int N, int K, void* ws, int* fixed,
@@ -507,6 +521,8 @@ int tc_product_checked(const double* A, const double* B, double* C, int M, int N
   double* bound = reinterpret_cast<double*>(w + base);
   int* kexp = reinterpret_cast<int*>(w + ((base + (size_t)M * N * sizeof(double) + 255) & ~(size_t)255));
   int* nfix = kexp + ((K + 63) / 64) * 64;
+  float* Aa = reinterpret_cast<float*>(nfix + 64);  // |A~|, then |B~|, FP32
+  float* Ba = Aa + (size_t)M * K;
   ALPS_CUDA_TRY(cudaMemsetAsync(nfix, 0, sizeof(int), st));
   k_tc_kexp<<<(K * 32 + 255) / 256, 256, 0, st>>>(B, K, N, kexp);
   ALPS_CUDA_TRY(cudaGetLastError());
@@ -515,7 +531,10 @@ int tc_product_checked(const double* A, const double* B, double* C, int M, int N
   const int* eA;
   const int* eB;
   tc_exponents(ws, M, N, K, &eA, &eB);
-  k_tc_fixup<<<dim3((N + 127) / 128, M), 128, 0, st>>>(A, B, C, M, N, K, kexp, eA, eB, nfix);
+  const size_t nab = (size_t)M * K + (size_t)K * N;
+  k_tc_absprep<<<(unsigned)((nab + 255) / 256), 256, 0, st>>>(A, B, M, N, K, kexp, eA, eB, Aa, Ba);
+  ALPS_CUDA_TRY(cudaGetLastError());
+  k_tc_fixup<<<dim3((N + 127) / 128, M), 128, 0, st>>>(A, B, C, M, N, K, Aa, Ba, nfix);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (fixed) {
     ALPS_CUDA_TRY(cudaMemcpyAsync(fixed, nfix, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -32,7 +32,8 @@ from alps_gb300.sharding import shard_range  # noqa: E402
 
 METRIC = "D(omega,k) evals/s & roots/s at <=1e-8 rel vs FP64, vs plain GPU; p50/p99 latency"
 UNIT = "evals/s"
-POLISH_RTOL = 1e-12  # the map configuration's polish tolerance on |delta omega| / |omega|
+POLISH_RTOL = 1e-12
+SERVED_RTOL = 1e-10  # the served stream's stop: two orders below its 1e-8 root tolerance  # the map configuration's polish tolerance on |delta omega| / |omega|
 
 
 def lattice(mp):
@@ -465,76 +466,183 @@ def uneven_batch(api, args):
     return out
 
 
+def seed_roots(api, plasmas, rng, tries=3):
+    """One root per plasma where a batched solve from a few random guesses
+    in [0.1, 1.5] - i[0, 0.1] finds one (alps_solve_many, polished to a
+    relative step of 1e-12); None where none converged."""
+    n = len(plasmas)
+    rep = [G for G in plasmas for _ in range(tries)]
+    g = rng.uniform(0.1, 1.5, n * tries) - 1j * rng.uniform(0.0, 0.1, n * tries)
+    roots, _, _, conv = api.solve_many(rep, g)
+    out = []
+    for i in range(n):
+        ok = [roots[i * tries + t] for t in range(tries) if conv[i * tries + t]]
+        out.append(ok[0] if ok else None)
+    return out
+
+
 def served_stream(api, args, precision):
     """The served-stream configuration: Poisson arrivals at args.served_rate
-    per second for args.served_seconds, 70 % single-root polishes, 25 %
-    32-step k scans (root following), 5 % 256 x 256 omega maps, on plasmas
-    drawn like the uneven batch (1-3 species, 64x128 .. 256x512 grids),
-    through one alps_server.  The plasmas are device-resident pools (f0
-    tables, fits, Bessel tables and contractions prepared before the stream,
-    timed apart): polishes pick a random plasma of a pool of 512, scans one
-    of 256 (a scan owns its plasma while it moves k), maps one of 16.
-    Latency runs from submission to result, with the requests overlapping
-    on the GPU."""
+    per second for args.served_seconds, 70 % single-k root polishes, 25 %
+    32-step k scans with root following, 5 % 256 x 256 omega maps
+    (args.served_mix), on plasmas drawn like the uneven batch (1-3 species,
+    64x128 .. 256x512 grids), through one alps_server.
+
+    The plasmas are device-resident pools, prepared before the stream and
+    timed apart (setup_s): f0 tables, fits, Bessel tables and contractions.
+    Polishes pick a random plasma of a pool of 512, scans one of 1024 (a
+    scan owns its plasma while it moves k), maps one of 16; the server
+    admits up to 1024 requests at once.  Each polish and scan
+    plasma carries a root found at setup (seed_s); a polish starts from that
+    root moved by up to 1 % in each of Re and Im, as refine_guess hands
+    roots to the secant, and a scan starts from the root at the plasma's k,
+    as om_scan does.  A scan is the k-scan of the plain k-scan
+    configuration: k_par scanned in 32 log steps at fixed k_perp (scan type
+    4: the k tables stay); a fraction args.served_kscans of them are |k|
+    scans at fixed angle instead (type 2: nmax, Bessel tables and
+    contractions rebuilt at each step).  A plasma's scans go up by 1.3 and
+    back down in turn, each from the root its last scan ended on.  Latency
+    runs from
+    submission to result, with the requests overlapping on the GPU."""
     import torch
     rng = np.random.default_rng(5)
     rate, T = args.served_rate, args.served_seconds
+    mix = np.asarray([float(x) for x in args.served_mix.split(",")])
+    mix = mix / mix.sum()
     nreq = int(rate * T)
-    kinds = rng.choice(3, nreq, p=[0.70, 0.25, 0.05])
-    n_pol, n_scan, n_map = 512, 256, 16
+    kinds = rng.choice(3, nreq, p=mix)
+    # a scan owns its plasma for its 32 steps: at 500 scans/s and a few
+    # hundred ms per scan, a few hundred scan plasmas are busy at once
+    n_pol, n_scan, n_map = 512, 1024, 16
     draws = [workloads.uneven_plasma(rng) for _ in range(n_pol + n_scan + n_map)]
     t0 = time.perf_counter()
     plasmas = make_plasmas(api, draws, precision)
     torch.cuda.synchronize()
     t_setup = time.perf_counter() - t0
     pol, scn, mpp = plasmas[:n_pol], plasmas[n_pol:n_pol + n_scan], plasmas[n_pol + n_scan:]
-    big = {id(G) for G, w in zip(pol, draws) if w["system"].nperp == 256}
+    t0 = time.perf_counter()
+    roots = seed_roots(api, pol + scn, rng)
+    t_seed = time.perf_counter() - t0
+    pol_ok = [i for i in range(n_pol) if roots[i] is not None]
+    scn_ok = [i for i in range(n_scan) if roots[n_pol + i] is not None]
+    big = {i for i in pol_ok if draws[i]["system"].nperp == 256}
     mp = _abi.alps_map_params()
     mp.omi, mp.omf, mp.gami, mp.gamf, mp.nr, mp.ni = 0.05, 2.0, -0.3, 0.05, 256, 256
-    srv = api.Server()
+    srv = api.Server(max_active=1024)
     t_arr = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    # every request's random numbers are drawn here, apart from the
+    # stream's timing, so both precision paths serve the same polishes
+    u_pick, u_kind = rng.uniform(size=nreq), rng.uniform(size=nreq)
+    u_d = rng.uniform(-0.01, 0.01, (nreq, 2))
     reqs = []
+    # a scan owns its plasma until it is done and leaves it at its last k
+    # with the root there: the next scan on that plasma starts from both,
+    # and scans up (x1.3) and back down in turn
+    scan_state = {i: (scn[i].kperp, scn[i].kpar, roots[n_pol + i], 1.3) for i in scn_ok}
+    busy = {}
+    n_scan_req = 0
+
+    def release(i):
+        r = busy.pop(i)
+        rows, fin = r.wait()
+        f = scan_state[i][3]
+        if r._rq.status == 0 and np.isfinite(fin[0]) and fin[0] != 0:
+            scan_state[i] = (float(rows[-1, 0, 0]), float(rows[-1, 0, 1]), complex(fin[0]), 1.0 / f)
+        else:  # the scan lost its root: the plasma leaves the pool
+            scan_state.pop(i)
+
     t0 = time.perf_counter()
     for k in range(nreq):
         wait = t_arr[k] - (time.perf_counter() - t0)
         if wait > 0:
             time.sleep(wait)
-        g = complex(rng.uniform(0.1, 1.5), -rng.uniform(0.0, 0.1))
+        if kinds[k] == 1:
+            for i in [i for i, r in busy.items() if r.done()]:
+                release(i)
+            free = [i for i in scan_state if i not in busy]
+            if not free and busy:
+                release(next(iter(busy)))
+                free = [i for i in scan_state if i not in busy]
+            if not free:
+                kinds[k] = 0
         if kinds[k] == 0:
-            G = pol[rng.integers(n_pol)]
-            reqs.append(("polish", id(G) in big, srv.polish(G, [g], om_rtol=POLISH_RTOL)))
+            i = pol_ok[min(int(u_pick[k] * len(pol_ok)), len(pol_ok) - 1)]
+            g = complex(roots[i].real * (1 + u_d[k, 0]), roots[i].imag + u_d[k, 1] * abs(roots[i]))
+            reqs.append(("polish", i in big, srv.polish(pol[i], [g], om_rtol=SERVED_RTOL), k))
         elif kinds[k] == 1:
-            G = scn[rng.integers(n_scan)]
-            sc = api.scan_def(4, 0.0, G.kpar * 1.3, True, 32, 1, G.kperp, G.kpar)
-            reqs.append(("scan", False, srv.scan(G, sc, [g], om_rtol=POLISH_RTOL)))
+            i = free[min(int(u_pick[k] * len(free)), len(free) - 1)]
+            kp, kz, w0, f = scan_state[i]
+            scn[i].kperp, scn[i].kpar = kp, kz
+            n_scan_req += 1
+            if u_kind[k] >= args.served_kscans:  # k_par scan: k_perp and the k tables stay
+                sc = api.scan_def(4, 0.0, kz * f, True, 32, 1, kp, kz)
+            else:  # |k| at fixed angle: nmax, Bessel tables and contractions each step
+                sc = api.scan_def(2, 0.0, float(np.hypot(kp, kz)) * f, True, 32, 1, kp, kz)
+            r = srv.scan(scn[i], sc, [w0], om_rtol=SERVED_RTOL)
+            busy[i] = r
+            reqs.append(("scan", False, r, k))
         else:
-            reqs.append(("map", False, srv.map(mpp[rng.integers(n_map)], mp)))
+            reqs.append(("map", False, srv.map(mpp[min(int(u_pick[k] * n_map), n_map - 1)], mp), k))
     t_submit = time.perf_counter() - t0
-    for _, _, r in reqs:
+    for _, _, r, _ in reqs:
         r.wait()
     wall = time.perf_counter() - t0
     st = srv.stats()
+    prof = srv.profile()
     srv.close()
-    out = {"precision": precision, "requests": nreq, "arrival_rate_per_s": rate, "submit_s": t_submit,
-           "wall_s": wall, "completed_per_s": nreq / wall, "setup_s": t_setup, "pool": [n_pol, n_scan, n_map],
+    out = {"precision": precision, "requests": nreq, "mix": [float(x) for x in mix], "arrival_rate_per_s": rate,
+           "k_scan_fraction": args.served_kscans,
+           "submit_s": t_submit, "wall_s": wall, "completed_per_s": nreq / wall, "setup_s": t_setup,
+           "seed_s": t_seed, "pool": [n_pol, n_scan, n_map], "pool_with_root": [len(pol_ok), len(scn_ok)],
            "batches": st["batches"], "peak_in_flight": st["peak_active"],
-           "peak_footprint_bytes": st["peak_bytes"], "latency_ms": {}}
+           "peak_footprint_bytes": st["peak_bytes"], "latency_ms": {},
+           # where the time goes (alps_server_get_profile)
+           "breakdown": {"rounds": prof["rounds"], "jobs_per_round": prof["round_jobs"] / max(1, prof["rounds"]),
+                         "round_device_ms_avg": prof["round_gpu_ms"] / max(1, prof["rounds"]),
+                         "own_stream_batches": prof["group_batches"], "scan_steps": prof["scan_steps"],
+                         "scan_step_batches": prof["scan_step_batches"],
+                         "scan_step_batch_ms_avg": prof["step_ms"] / max(1, prof["scan_step_batches"]),
+                         "server_loop_busy_s": prof["loop_busy_ms"] / 1e3, "admission_s": prof["admit_ms"] / 1e3,
+                         "landing_rounds_s": prof["land_ms"] / 1e3, "group_pass_s": prof["groups_ms"] / 1e3,
+                         "launching_rounds_s": prof["round_launch_ms"] / 1e3}}
     for kind in ("polish", "scan", "map"):
-        lat = [r.latency_ms for kk, _, r in reqs if kk == kind]
+        lat = [r.latency_ms for kk, _, r, _ in reqs if kk == kind]
         if lat:
             out["latency_ms"][kind] = {"count": len(lat), "p50": float(np.percentile(lat, 50)),
                                        "p99": float(np.percentile(lat, 99))}
-    lat = [r.latency_ms for kk, b, r in reqs if kk == "polish" and b]
+    lat = [r.latency_ms for kk, b, r, _ in reqs if kk == "polish" and b]
     if lat:
         out["latency_ms"]["polish_256x512"] = {"count": len(lat), "p50": float(np.percentile(lat, 50)),
                                                "p99": float(np.percentile(lat, 99)), "target_p99": 20.0}
-    nroots = sum(1 for kk, _, _ in reqs if kk == "polish") + 33 * sum(1 for kk, _, _ in reqs if kk == "scan")
+    pol_conv = [bool(r.converged[0]) for kk, _, r, _ in reqs if kk == "polish"]
+    out["polish_converged"] = int(np.sum(pol_conv))
+    out["_polish_roots"] = {k: complex(r.om[0]) for kk, _, r, k in reqs if kk == "polish" and r.converged[0]}
+    scan_ok = [r for kk, _, r, _ in reqs if kk == "scan" and r._rq.status == 0]
+    out["scans_completed"] = len(scan_ok)
+    nroots = int(np.sum(pol_conv)) + 33 * len(scan_ok)
     out["roots_per_s"] = nroots / wall
-    out["note"] = ("latency from submission to result; roots polished from random guesses until the secant "
-                   "update is at most 1e-12 |omega| (or numiter = 50); the k steps of the scans ready at one "
-                   "time go to the device together; the stream is sustained when completed_per_s matches the "
-                   "arrival rate and wall_s stays near the stream's duration")
+    out["note"] = ("latency from submission to result; polishes and scans start at roots found at setup (a polish "
+                   "from the root moved by up to 1 %), polished until the secant update is at most 1e-10 |omega| "
+                   "(or numiter = 50), two orders below the configuration's 1e-8 root tolerance; roots/s counts "
+                   "converged polishes and scan rows; the k steps of the scans ready at one time go to the device "
+                   "together; the stream is sustained when completed_per_s matches the arrival rate and wall_s "
+                   "stays near the stream's duration")
     del plasmas, pol, scn, mpp
+    return out
+
+
+def served_both(api, args):
+    """The served stream on the mixed and the plain FP64 path, with the
+    relative difference of the polished roots that converged on both (the
+    same requests on both paths)."""
+    out = {p: served_stream(api, args, p) for p in ("mixed", "fp64")}
+    a, b = out["mixed"].pop("_polish_roots"), out["fp64"].pop("_polish_roots")
+    both = sorted(set(a) & set(b))
+    rel = np.array([abs(a[k] - b[k]) / abs(b[k]) for k in both]) if both else np.zeros(0)
+    same = rel <= 1e-6  # both paths ended on the same root
+    out["mixed_vs_fp64_polish"] = {"both_converged": len(both), "same_root": int(same.sum()),
+                                   "max_rel_diff_same_root": float(rel[same].max()) if same.any() else None,
+                                   "tolerance": 1e-8}
     return out
 
 
@@ -550,12 +658,16 @@ def main():
                     help="run only the served stream and print its JSON object (for profiling the server)")
     ap.add_argument("--served-seconds", type=float, default=3.0, help="duration of the served stream's arrivals")
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrival rate of the served stream")
+    ap.add_argument("--served-mix", default="0.70,0.25,0.05", help="polish, scan, map fractions of the served stream")
+    ap.add_argument("--served-kscans", type=float, default=0.0,
+                    help="fraction of the served scans that scan |k| at fixed angle instead of k_par")
     ap.add_argument("--ni", type=int, default=512)
     ap.add_argument("--uneven-solves", type=int, default=4096, help="solves of the uneven-batch measurement")
     ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch measurement")
     ap.add_argument("--no-kscan", action="store_true", help="skip the plain k-scan measurement")
     ap.add_argument("--no-relativistic", action="store_true", help="skip the relativistic k-scan measurement")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="time the default launch shapes")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus if args.gpus else 1)))
@@ -577,7 +689,7 @@ def main():
     from alps_gb300 import api
     if args.served_only:
         if rank == 0:
-            print(json.dumps({"served": {p: served_stream(api, args, p) for p in ("mixed", "fp64")}}))
+            print(json.dumps({"served": served_both(api, args)}))
         return
     # weak scaling: every replica evaluates a full lattice at its own k_par
     s = w["system"]
@@ -633,6 +745,15 @@ def main():
         Dv = D_dev[:, 0].cpu().numpy() + 1j * D_dev[:, 1].cpu().numpy()
         return t, prof, Dv
 
+    # the autotuner picks each path's launch shape for this batch on the
+    # lattice itself, before any timing (alps_autotune)
+    tune = {}
+    if not args.no_autotune:
+        for precision in ("fp64", "mixed"):
+            G.set_precision(precision)
+            t0 = time.perf_counter()
+            tune[precision] = G.autotune(n, om_dev.data_ptr())
+            tune[precision]["tuning_s"] = time.perf_counter() - t0
     # plain FP64 path (node sums everywhere): the baseline of the fast path
     t_plain, prof_plain, D_plain = timed("fp64")
     peak64 = fp64_peak_tflops(torch)
@@ -724,7 +845,7 @@ def main():
     root_rel = float(np.max(np.abs(roots[both] - roots_plain[both]) / np.abs(roots_plain[both]))) if both.any() \
         else None
 
-    served = None if (args.no_served or rank != 0) else {p: served_stream(api, args, p) for p in ("mixed", "fp64")}
+    served = None if (args.no_served or rank != 0) else served_both(api, args)
     uneven = None if (args.no_uneven or rank != 0) else uneven_batch(api, args)
     kscan = None if (args.no_kscan or rank != 0) else kscan_leg(api, args)
     relat = None if (args.no_relativistic or rank != 0) else relativistic_leg(args)
@@ -775,7 +896,7 @@ def main():
                 "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "mixed: fp32 double-float + fp64", "data": "synthetic",
                 "precision_path": G.precision, "err_vs_oracle": err_vs_oracle,
-                "config": config_dict(w, mp.nr, mp.ni, world), "nmax": nmax,
+                "config": config_dict(w, mp.nr, mp.ni, world), "nmax": nmax, "autotune": tune or None,
                 "plain_fp64": {"value": value_plain, "unit": UNIT, "dtype": "f64",
                                "ms_per_step": t_plain / args.steps * 1e3,
                                "speedup_of_fast_path": value / value_plain,

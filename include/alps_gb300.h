@@ -168,15 +168,20 @@ int alps_prepare_many(alps_ctx* const* ctx, int n, int* status);
  * table, and the omega-independent p_perp contraction.
  * Replaces determine_nmax + determine_bessel_array
  * (src/ALPS_fns.f90:3971-4075, 4214-4255); split_processes
- * (src/ALPS_fns.f90:4079-4207) has no counterpart: one device does all n. */
+ * (src/ALPS_fns.f90:4079-4207) has no counterpart: one device does all n.
+ * The tables depend on kperp alone: a call that keeps the context's kperp
+ * bit for bit (a k_par scan step) keeps them and moves k_par only, as
+ * om_scan does for scan type 4 (src/ALPS_fns.f90:2465-2471);
+ * alps_stats.k_reused counts such calls. */
 int alps_set_k(alps_ctx* ctx, double kperp, double kpar);
 int alps_get_nmax(alps_ctx* ctx, int* nmax /* [nspec] */);
 
 /* alps_set_k for n contexts at once, context i at (kperp[i], kpar[i]):
  * determine_nmax for every species of every context in one launch, then
  * the Bessel tables and contractions of all contexts on a few streams with
- * one synchronisation.  The results are those of alps_set_k on each
- * context.  status[i] (may be NULL) as in alps_prepare_many. */
+ * one synchronisation.  Contexts whose kperp stays keep their tables.  The
+ * results are those of alps_set_k on each context.  status[i] (may be
+ * NULL) as in alps_prepare_many. */
 int alps_set_k_many(alps_ctx* const* ctx, int n, const double* kperp,
                     const double* kpar, int* status);
 
@@ -395,6 +400,8 @@ typedef struct alps_request {
   int rounds;               /* out: batches the request launched                           */
   double om_rtol;           /* POLISH, SCAN: relative-step stop of alps_secant_ex, 0 = the
                                reference's stopping rule only                              */
+  int* converged;           /* POLISH out: 1 where the root met a stopping rule before
+                               numiter (may be NULL)                                       */
 } alps_request;
 
 /* hbm_budget: bytes of device memory requests may hold at once (0: 90 % of
@@ -412,6 +419,20 @@ int alps_server_wait(alps_server* srv, int64_t id);
 /* Batches launched, peak requests in flight and peak estimated footprint so
  * far. */
 int alps_server_stats(alps_server* srv, int64_t* rounds, int* peak_active, size_t* peak_bytes);
+/* Where the server's time goes, summed since creation: fused rounds
+ * launched and the plasma batches (jobs) in them, with the device span of
+ * each round from its frequency upload to its result download; batches run
+ * on a context's own stream (maps, plasmas the fused kernels do not take);
+ * scan k-step batches (one alps_set_k_many over the scans ready together)
+ * with the steps in them and their wall time; and the host time of the
+ * server loop outside its idle waits, of which admission, landing rounds
+ * (root-machine steps), the pass over the groups (own-stream launches and
+ * landings, releases) and launching rounds (job tables, uploads). */
+typedef struct alps_server_profile {
+  int64_t rounds, round_jobs, group_batches, scan_step_batches, scan_steps;
+  double round_gpu_ms, step_ms, loop_busy_ms, admit_ms, land_ms, groups_ms, round_launch_ms;
+} alps_server_profile;
+int alps_server_get_profile(alps_server* srv, alps_server_profile* out);
 
 /* Parses an ALPS input file (init_param + scan_read, src/ALPS_io.f90:46-552):
  * defaults of src/ALPS_var.f90, Fortran literals (1.d-2, .true., T, 'str'),
@@ -494,6 +515,28 @@ int alps_run_interpolation(const char* input_path, const char* workdir);
 int alps_tc_product(const double* d_A, const double* d_B, double* d_C, int M,
                     int N, int K, int checked, int* nfixed);
 
+/* Autotuner of the batch kernels' launch shapes.  Times the candidate
+ * shapes of a batch of n frequencies on this context (its k and precision
+ * path): j slices per frequency of the pole sums (1, 2, 4, 8, 16, 32) x
+ * pole-sum blocks per SM (2, 4, 8) x resonant-item warps per SM (6, 12, 24),
+ * each the best of two launches after a warm-up.  The fastest (if 3 % faster
+ * than the default rule) is kept for every batch of the same bucket: N_perp,
+ * N_par, nmax + 1 and n each rounded up to a power of two, species count
+ * and precision path.  d_om: n device frequencies to tune on, or NULL for a
+ * lattice over Re in [0.05, 2.5], Im in [-0.4, 0.05].  A shape changes the
+ * summation order of the pole sums only (results move by rounding); lone,
+ * fused and no-allocation batches of a bucket use the same shape.  No
+ * reference counterpart: ALPS has one fixed loop order. */
+typedef struct alps_tune_result {
+  int js, blocks_per_sm, warps_per_sm; /* the shape the bucket now uses          */
+  int tuned;                           /* 1: a candidate beat the default rule   */
+  int candidates;                      /* shapes timed                           */
+  double ms_default, ms_best;          /* per batch: default rule, chosen shape  */
+} alps_tune_result;
+int alps_autotune(alps_ctx* ctx, int n, const alps_complex* d_om, alps_tune_result* out);
+/* Forgets every tuned shape (all buckets return to the default rule). */
+int alps_tune_clear(void);
+
 /* Device work counters of the last disp batch (for measurement). */
 typedef struct alps_stats {
   int64_t n_eval;             /* frequencies evaluated                        */
@@ -510,6 +553,7 @@ typedef struct alps_stats {
   int64_t tc_fixed_entries;
   int64_t tc_entries;
   int64_t n_eval_total;       /* frequencies evaluated since the context was created */
+  int64_t k_reused;           /* k steps that kept k_perp and with it the k tables */
 } alps_stats;
 int alps_get_stats(alps_ctx* ctx, alps_stats* st);
 
