@@ -139,8 +139,8 @@ void alps_destroy(alps_ctx* c) {
     cudaFree(S.d_momf);
     cudaFree(S.d_Vh);  // d_Vl points into it
     cudaFree(S.d_Vscale);
-    cudaFree(S.d_Wh);
-    cudaFree(S.d_Wscale);
+    cudaFree(S.d_Bt);
+    cudaFree(S.d_Bd);
     cudaFree(S.d_pph);
     cudaFree(S.d_ppl);
     cudaFree(S.d_fit_aux);

@@ -89,11 +89,20 @@ struct __align__(16) SpecDev {
   const float* pph;
   const float* ppl;
   int df_sums;
-  // order-fused tables (C0 and the prefactors folded in, one scale per
-  // vector q): W pairs [(nmax+1)][M-1][12], moment pairs and FP32 moments
-  // [(nmax+1)][ALPS_KFAR][12], Wscale[12]; FP32 resonance bounds
-  const float *Wh, *Wl, *mWh, *mWl, *mWf;
-  const double* Wscale;
+  // base tables of the fast path's pole sums: the three Bessel families
+  // F1 = J^2, F2 = pperp^2 J'^2, F3 = pperp J J' against g1 and g2 (reduced
+  // vectors q = 0, 1, 2, 3, 6, 7), scaled by 1/Vscale[n]:
+  //   Bt   [(nmax+1)][M-1][12]       node values, 6 hi then 6 lo floats
+  //   mBt  [(nmax+1)][ALPS_KFAR][12] their Laurent moments, the same layout
+  //   bfac [(nmax+1)][6][2]          order factors C0 v_e(n) Vscale[n] / Escale[e]
+  //                                  as float pairs, entries xx yy zz xy xz yz
+  //   Escale[6]                      powers of two
+  //   Pre  [(nmax+1)][M][6]          FP64 prefix sums over j of the weighted
+  //                                  vectors F1, F3, ppar F1 (g1, g2 each)
+  //   Cfull[(nmax+1)][6]             their full-range trapezoid sums
+  // FP32 resonance bounds
+  const float *Bt, *mBt, *bfac;
+  const double *Escale, *Pre, *Cfull;
   float qlo, qhi;        // below / above these Re p_res is not resonant
   float qlo_in, qhi_in;  // between these it is
   float kaph, kapl;   // k_par / m_s as a float pair
@@ -174,9 +183,10 @@ struct SpeciesHost {
   double* d_mom = nullptr;                // Laurent moments
   float* d_momf = nullptr;                // the same in FP32; the pairs below share its allocation
   float *d_momh = nullptr, *d_moml = nullptr;  // the moments as float pairs (scale Vscale per order)
-  float* d_Wh = nullptr;                  // order-fused tables: W hi, lo, moments hi, lo, FP32
-  size_t Wf_cap = 0;
-  double* d_Wscale = nullptr;             // their scale per vector q
+  float* d_Bt = nullptr;                  // base tables of the fast pole sums: Bt, mBt, bfac
+  size_t Bt_cap = 0;
+  double* d_Bd = nullptr;                 // and their FP64 part: Escale[8], Cfull, Pre
+  size_t Bd_cap = 0;
   float qlo = 0.0f, qhi = 0.0f;           // FP32 bounds of the resonance interval (margin outward)
   float qlo_in = 1.0f, qhi_in = -1.0f;    // the same with the margin inward
   float *d_Vh = nullptr, *d_Vl = nullptr;  // V as float pairs (one allocation, lo after hi)

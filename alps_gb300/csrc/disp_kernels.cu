@@ -123,52 +123,67 @@ __device__ __forceinline__ void df_cmul2(dflt ax, dflt ay, dflt bx, dflt by, dfl
   rx = x;
 }
 
+// complex double-float values and the combinations of the base sums
+struct cdf {
+  dflt x, y;
+};
+__device__ __forceinline__ cdf cdf_mul(cdf a, cdf b) {
+  cdf r;
+  df_cmul2(a.x, a.y, b.x, b.y, r.x, r.y);
+  return r;
+}
+__device__ __forceinline__ cdf cdf_add(cdf a, cdf b) { return {df_add(a.x, b.x), df_add(a.y, b.y)}; }
+__device__ __forceinline__ cdf cdf_rmul(cdf a, dflt s) { return {df_mul(a.x, s), df_mul(a.y, s)}; }
+// omega v1 + kappa v2 (v1, v2 complex)
+__device__ __forceinline__ cdf om_comb(cdf o, dflt kap, cdf v1, cdf v2) {
+  const cdf r = cdf_mul(o, v1);
+  return {df_add(r.x, df_mul(kap, v2.x)), df_add(r.y, df_mul(kap, v2.y))};
+}
+// omega c1 + kappa c2 (c1, c2 real)
+__device__ __forceinline__ cdf om_combr(cdf o, dflt kap, dflt c1, dflt c2) {
+  return {df_add(df_mul(o.x, c1), df_mul(kap, c2)), df_mul(o.y, c1)};
+}
+
 // ---------------------------------------------------------------------------
-// Fast path of the pole sums (no chi_low): the orders of a block's chunk
-// accumulate in one set of double-float sums per thread, on the order-fused
-// tables (C0 and the T-tensor prefactors folded into the reduced vectors and
-// their Laurent moments, one scale per vector).  Per (omega, signed order):
-// an FP32 test settles orders far from resonance (the FP64 geometry decides
-// the rest), then either the Laurent series (far poles: the terms
-// mom_k f t^k with f = 1/(k_par d), t = prad/d, leading terms in
-// double-float, the tail in FP32) or the node sum in double-float.  The odd
-// entries of a -n order enter with the minus sign, and the sums are
-// renormalised after each order.  Once per chunk they are rescaled and
-// combined, acc_e = phase_e (omega S_{e,1} + kappa S_{e,2}), in FP64.
+// Fast path of the pole sums (no chi_low), on the base tables: per (omega,
+// signed order) the sums of the three Bessel families against g1 and g2
+// (6 real vectors, complex weights), in double-float on the FP32 pipes:
+//   * node sums Q = sum_j w_j F_j R_j, R_j = 1/(A - k_par p_j + i D), the
+//     p_par-weighted entries from zeta Q - (1/k_par) sum w F (the sums of
+//     the family vectors over the summed ranges: full-range table, or FP64
+//     prefix sums where a resonance window is cut out);
+//   * far poles: the Laurent series Q = f sum_k mom_k t^k, d = p_res - pcen,
+//     t = prad/d, f = 1/(k_par d); with T = f sum_{k>=1}, U = f sum_{k>=2}:
+//     sum F p R = pcen Q + d T, sum F p^2 R = pcen^2 Q + 2 pcen d T + d^2 U
+//     (no cancellation for far poles); the terms from K32 on in FP32.
+// An FP32 test settles orders far from resonance (the FP64 geometry decides
+// the rest).  Each order's entries X_e = omega S_{e,1} + kappa S_{e,2} are
+// added, times the order factor C0 v_e(n) (sign of -n for xy, xz), to one
+// double-float sum per entry; the phase (i for xy, yz) and the entry scale
+// are applied once per chunk in FP64.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, double2 o, int js, int js_count,
-                                           int n_begin, int n_end, double2* acc) {
+                                           int n_begin, int n_end, double2* acc_out) {
   const int M = S.M;
   const double kpar = sys.kpar;
-  dflt sacc[24];
-  float Sf[24];
+  dflt acc[12];
 #pragma unroll
-  for (int q = 0; q < 24; ++q) {
-    sacc[q] = {0.0f, 0.0f};
-    Sf[q] = 0.0f;
-  }
+  for (int q = 0; q < 12; ++q) acc[q] = {0.0f, 0.0f};
   const dflt oxd = df_of(o.x), oyd = df_of(o.y), msd = df_of(S.ms), qsd = df_of(S.qs);
+  const cdf omd = {oxd, oyd};
+  const dflt kap = {S.kaph, S.kapl};
   const dflt kd = df_of(kpar), ikd = df_of(sys.ikpar), pcd = df_of(S.pcen), prd = df_of(S.prad);
   const dflt Dd = df_mul(msd, oyd);  // m omega_i
   const dflt D2 = df_mul(Dd, Dd);
   const dflt dyd = df_mul(Dd, ikd);  // Im p_res
   const dflt mox = df_mul(msd, oxd);
   const float ikp32 = (float)sys.ikpar;
+  const int k0 = (js >= 2) ? js : js + js_count * ((2 - js + js_count - 1) / js_count);  // first k >= 2
   for (int n = n_begin; n < n_end; ++n) {
-    const float* __restrict__ Wh = S.Wh + (size_t)n * (M - 1) * 12;
-    const float* __restrict__ Wl = S.Wl + (size_t)n * (M - 1) * 12;
+    const float* __restrict__ Bn = S.Bt + (size_t)n * (M - 1) * 12;
+    const float* __restrict__ mBn = S.mBt + (size_t)n * ALPS_KFAR * 12;
     for (int sg = 0; sg < (n == 0 ? 1 : 2); ++sg) {
       const int nn = sg ? -n : n;
-      // xy and xz are odd in n: a -n order adds to their vectors (6-9) with the minus sign:
-      // their sums are negated before and after it (exact)
-      auto flip_odd = [&]() {
-#pragma unroll
-        for (int q = 12; q < 20; ++q) {
-          sacc[q] = df_neg(sacc[q]);
-          Sf[q] = -Sf[q];
-        }
-      };
-      if (sg) flip_odd();
       // A = m omega_r - nn q, the pole's real part times k_par
       const dflt Ad = df_add(mox, df_neg(df_mul({(float)nn, 0.0f}, qsd)));
       const float x32 = Ad.h * ikp32;
@@ -217,8 +232,9 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
         const float d2 = D2.h;
         nodes_df = d2 + lo * lo >= 1e-30f && d2 + hi * hi <= 1e30f;
       }
+      cdf X[6];  // the order's entries (xx yy zz xy xz yz), scaled by 1/Vscale[n]
       if (K > S.kfar && !nodes_df) {
-        // FP64 node sum of this order, folded into the sums as its terms
+        // FP64 node sum of this order over V, X_e = omega S_e1 + kappa S_e2
         const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
         const double Ar = S.ms * o.x - (double)nn * S.qs, Di = S.ms * o.y;
         double2 Sx[12];
@@ -242,97 +258,115 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
           if (lo >= hi) continue;
           for (int side = 0; side < 2; ++side) {
             const int j = side ? hi : lo;
-            if (((j - 1) % js_count) == js) nd(j, -0.5);
+            if (j >= 1 && j <= M - 1 && ((j - 1) % js_count) == js) nd(j, -0.5);
           }
         }
-        const double z = sys.kperp_norm ? sys.kperp / S.qs : 1.0 / S.qs;
-        const double C0 = 2.0 * ALPS_PI * S.dpperp * S.dppar_abs * 0.25 * S.qs;
+        const double isc = 1.0 / S.Vscale[n], kapd = S.kappa;
 #pragma unroll
-        for (int q = 0; q < 12; ++q) {
-          const double f = fused_factor(n, q >> 1, z, sys.kperp, sys.kperp_norm, C0) / S.Wscale[q];
-          df_acc(sacc[2 * q], df_of(Sx[q].x * f));
-          df_acc(sacc[2 * q + 1], df_of(Sx[q].y * f));
+        for (int e = 0; e < 6; ++e) {
+          const double2 t = cscale(cadd(cmul(o, Sx[2 * e]), cscale(Sx[2 * e + 1], kapd)), isc);
+          X[e] = {df_of(t.x), df_of(t.y)};
         }
       } else if (K <= S.kfar) {
-        // Laurent series: S = f sum_k mom_k t^k, d = p_res - pcen,
-        // t = prad/d, f = 1/(k_par d); the powers start at f t^js
-        const dflt dxd = df_add(df_mul(Ad, ikd), df_neg(pcd));
-        const dflt r = df_rcp_approx(df_add(df_mul(dxd, dxd), df_mul(dyd, dyd)));
-        const dflt ivx = df_mul(dxd, r), ivy = df_neg(df_mul(dyd, r));
-        const dflt tx0 = df_mul(prd, ivx), ty0 = df_mul(prd, ivy);
-        dflt tx = df_mul(ikd, ivx), ty = df_mul(ikd, ivy);
-        dflt sx = tx0, sy = ty0;
+        // Laurent series: d = p_res - pcen, t = prad/d, f = 1/(k_par d)
+        const cdf d = {df_add(df_mul(Ad, ikd), df_neg(pcd)), dyd};
+        const dflt r = df_rcp_approx(df_add(df_mul(d.x, d.x), df_mul(d.y, d.y)));
+        const cdf iv = {df_mul(d.x, r), df_neg(df_mul(d.y, r))};
+        const cdf t1 = cdf_rmul(iv, prd), f = cdf_rmul(iv, ikd);
+        // U = f sum_{k >= 2} mom_k t^k over this slice's k: powers from f t^k0,
+        // step t^js_count (both by squaring)
+        cdf tp = f, st = t1;
         {
-          dflt px = tx0, py = ty0;
-          for (int q = js; q; q >>= 1) {
-            if (q & 1) df_cmul2(tx, ty, px, py, tx, ty);
-            df_cmul2(px, py, px, py, px, py);
+          cdf pw = t1;
+          for (int q = k0; q; q >>= 1) {
+            if (q & 1) tp = cdf_mul(tp, pw);
+            pw = cdf_mul(pw, pw);
           }
-          for (int q = js_count; q > 1; q >>= 1) df_cmul2(sx, sy, sx, sy, sx, sy);
+          for (int q = js_count; q > 1; q >>= 1) st = cdf_mul(st, st);
         }
-        const float* __restrict__ mh = S.mWh + (size_t)n * ALPS_KFAR * 12;
-        const float* __restrict__ ml = S.mWl + (size_t)n * ALPS_KFAR * 12;
-        int k = js;
-        for (; k < K32; k += js_count) {
-          const float4* h4 = reinterpret_cast<const float4*>(mh + (size_t)k * 12);
-          const float4* l4 = reinterpret_cast<const float4*>(ml + (size_t)k * 12);
+        dflt U[12];
+        float Uf[12];
 #pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const float4 h = __ldg(h4 + q), l = __ldg(l4 + q);
-            df_mac(sacc[8 * q + 0], h.x, l.x, tx);
-            df_mac(sacc[8 * q + 1], h.x, l.x, ty);
-            df_mac(sacc[8 * q + 2], h.y, l.y, tx);
-            df_mac(sacc[8 * q + 3], h.y, l.y, ty);
-            df_mac(sacc[8 * q + 4], h.z, l.z, tx);
-            df_mac(sacc[8 * q + 5], h.z, l.z, ty);
-            df_mac(sacc[8 * q + 6], h.w, l.w, tx);
-            df_mac(sacc[8 * q + 7], h.w, l.w, ty);
+        for (int q = 0; q < 12; ++q) {
+          U[q] = {0.0f, 0.0f};
+          Uf[q] = 0.0f;
+        }
+        int k = k0;
+        for (; k < K32; k += js_count) {
+          const float4* m4 = reinterpret_cast<const float4*>(mBn + (size_t)k * 12);
+          const float4 a0 = __ldg(m4), a1 = __ldg(m4 + 1), a2 = __ldg(m4 + 2);
+          const float hb[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y}, lb[6] = {a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
+#pragma unroll
+          for (int b = 0; b < 6; ++b) {
+            df_mac(U[2 * b], hb[b], lb[b], tp.x);
+            df_mac(U[2 * b + 1], hb[b], lb[b], tp.y);
           }
-          df_cmul2(tx, ty, sx, sy, tx, ty);
+          tp = cdf_mul(tp, st);
         }
         if (k < K) {
           // the tail: terms below 2^-33 of the bound, in FP32
-          const float* __restrict__ mf = S.mWf + (size_t)n * ALPS_KFAR * 12;
-          float fx = tx.h + tx.l, fy = ty.h + ty.l;
-          const float gx = sx.h + sx.l, gy = sy.h + sy.l;
+          float fx = tp.x.h + tp.x.l, fy = tp.y.h + tp.y.l;
+          const float gx = st.x.h + st.x.l, gy = st.y.h + st.y.l;
           for (; k < K; k += js_count) {
-            const float4* m4 = reinterpret_cast<const float4*>(mf + (size_t)k * 12);
+            const float4* m4 = reinterpret_cast<const float4*>(mBn + (size_t)k * 12);
+            const float4 a0 = __ldg(m4);
+            const float2 a1 = __ldg(reinterpret_cast<const float2*>(m4 + 1));
+            const float hb[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y};
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-              const float4 m = __ldg(m4 + q);
-              Sf[8 * q + 0] = fmaf(m.x, fx, Sf[8 * q + 0]);
-              Sf[8 * q + 1] = fmaf(m.x, fy, Sf[8 * q + 1]);
-              Sf[8 * q + 2] = fmaf(m.y, fx, Sf[8 * q + 2]);
-              Sf[8 * q + 3] = fmaf(m.y, fy, Sf[8 * q + 3]);
-              Sf[8 * q + 4] = fmaf(m.z, fx, Sf[8 * q + 4]);
-              Sf[8 * q + 5] = fmaf(m.z, fy, Sf[8 * q + 5]);
-              Sf[8 * q + 6] = fmaf(m.w, fx, Sf[8 * q + 6]);
-              Sf[8 * q + 7] = fmaf(m.w, fy, Sf[8 * q + 7]);
+            for (int b = 0; b < 6; ++b) {
+              Uf[2 * b] = fmaf(hb[b], fx, Uf[2 * b]);
+              Uf[2 * b + 1] = fmaf(hb[b], fy, Uf[2 * b + 1]);
             }
             const float nx = fx * gx - fy * gy;
             fy = fx * gy + fy * gx;
             fx = nx;
           }
         }
+        // per family F1, F2, F3: omega U_{F,g1} + kappa U_{F,g2}
+        cdf Uw[3];
+#pragma unroll
+        for (int fm = 0; fm < 3; ++fm) {
+          const int b1 = 2 * fm, b2 = 2 * fm + 1;
+          const cdf u1 = {df_add(U[2 * b1], {Uf[2 * b1], 0.0f}), df_add(U[2 * b1 + 1], {Uf[2 * b1 + 1], 0.0f})};
+          const cdf u2 = {df_add(U[2 * b2], {Uf[2 * b2], 0.0f}), df_add(U[2 * b2 + 1], {Uf[2 * b2 + 1], 0.0f})};
+          Uw[fm] = om_comb(omd, kap, u1, u2);
+        }
+        // T = f mom_1 t + U, Q = f mom_0 + T on the slices that own k = 1, 0
+        cdf T[3] = {Uw[0], Uw[1], Uw[2]};
+        auto mterm = [&](int kk, cdf w, cdf* out) {
+          const float* m = mBn + (size_t)kk * 12;
+#pragma unroll
+          for (int fm = 0; fm < 3; ++fm) {
+            const cdf mw = om_combr(omd, kap, {m[2 * fm], m[6 + 2 * fm]}, {m[2 * fm + 1], m[6 + 2 * fm + 1]});
+            out[fm] = cdf_add(out[fm], cdf_mul(w, mw));
+          }
+        };
+        if (js == 1 % js_count) mterm(1, cdf_mul(f, t1), T);
+        cdf Q[3] = {T[0], T[1], T[2]};
+        if (js == 0) mterm(0, f, Q);
+        X[0] = Q[0];
+        X[1] = Q[1];
+        X[3] = Q[2];
+        const cdf pQ1 = cdf_rmul(Q[0], pcd), pQ3 = cdf_rmul(Q[2], pcd);
+        X[4] = cdf_add(pQ1, cdf_mul(d, T[0]));
+        X[5] = cdf_add(pQ3, cdf_mul(d, T[2]));
+        X[2] = cdf_add(cdf_rmul(X[4], pcd), cdf_mul(d, cdf_add(cdf_rmul(T[0], pcd), cdf_mul(d, Uw[0]))));
       } else {
-        // node sum in double-float: sum_j W_j / (A - k_par p_j + i D)
+        // node sum in double-float: Q_b = sum_j w_j B_b(j) / (A - k_par p_j + i D)
+        dflt Qs[12];
+#pragma unroll
+        for (int q = 0; q < 12; ++q) Qs[q] = {0.0f, 0.0f};
         auto node = [&](int j, float wgt) {
           const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
           const dflt r = df_rcp_approx(df_add(df_mul(dr, dr), D2));
           const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
-          const float4* vh4 = reinterpret_cast<const float4*>(Wh + (size_t)(j - 1) * 12);
-          const float4* vl4 = reinterpret_cast<const float4*>(Wl + (size_t)(j - 1) * 12);
+          const float4* b4 = reinterpret_cast<const float4*>(Bn + (size_t)(j - 1) * 12);
+          const float4 a0 = __ldg(b4), a1 = __ldg(b4 + 1), a2 = __ldg(b4 + 2);
+          const float hb[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y}, lb[6] = {a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
 #pragma unroll
-          for (int q = 0; q < 3; ++q) {
-            const float4 h = __ldg(vh4 + q), l = __ldg(vl4 + q);
-            df_mac(sacc[8 * q + 0], h.x, l.x, Rr);
-            df_mac(sacc[8 * q + 1], h.x, l.x, Ri);
-            df_mac(sacc[8 * q + 2], h.y, l.y, Rr);
-            df_mac(sacc[8 * q + 3], h.y, l.y, Ri);
-            df_mac(sacc[8 * q + 4], h.z, l.z, Rr);
-            df_mac(sacc[8 * q + 5], h.z, l.z, Ri);
-            df_mac(sacc[8 * q + 6], h.w, l.w, Rr);
-            df_mac(sacc[8 * q + 7], h.w, l.w, Ri);
+          for (int b = 0; b < 6; ++b) {
+            df_mac(Qs[2 * b], hb[b], lb[b], Rr);
+            df_mac(Qs[2 * b + 1], hb[b], lb[b], Ri);
           }
         };
         for (int j = 1 + js; j <= M - 1; j += js_count) {
@@ -348,28 +382,75 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
 #pragma unroll
           for (int side = 0; side < 2; ++side) {
             const int j = side ? hi : lo;
-            if (((j - 1) % js_count) == js) node(j, -0.5f);
+            if (j >= 1 && j <= M - 1 && ((j - 1) % js_count) == js) node(j, -0.5f);
           }
         }
-      }
-      if (sg) flip_odd();
-      // the low parts, added to without normalisation inside the order,
-      // are folded back so that their FP32 roundings do not grow over the
-      // chunk's orders
+        cdf P[3];
 #pragma unroll
-      for (int q = 0; q < 24; ++q) sacc[q] = df_two_sum(sacc[q].h, sacc[q].l);
+        for (int fm = 0; fm < 3; ++fm)
+          P[fm] = om_comb(omd, kap, {Qs[4 * fm], Qs[4 * fm + 1]}, {Qs[4 * fm + 2], Qs[4 * fm + 3]});
+        const cdf zeta = {df_mul(Ad, ikd), dyd};
+        X[0] = P[0];
+        X[1] = P[1];
+        X[3] = P[2];
+        cdf xz = cdf_mul(zeta, P[0]), yz = cdf_mul(zeta, P[2]);
+        cdf cp = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+        if (js == 0) {
+          // (1/k_par) times the omega-combined sums of F1, F3 and p_par F1
+          // over the summed ranges (slice 0 adds them once)
+          double C[6];
+          const double* __restrict__ Cf = S.Cfull + (size_t)n * 6;
+          if (!g.res) {
+#pragma unroll
+            for (int c = 0; c < 6; ++c) C[c] = Cf[c];
+          } else {
+            const double* __restrict__ P0 = S.Pre + (size_t)n * M * 6;
+            const double* __restrict__ Vn = S.V + (size_t)n * (M - 1) * 12;
+            const double isc = 1.0 / S.Vscale[n];
+#pragma unroll
+            for (int c = 0; c < 6; ++c) C[c] = 0.0;
+            for (int r2 = 0; r2 < 2; ++r2) {
+              const int lo = max(1, ends[2 * r2]), hi = min(M - 1, ends[2 * r2 + 1]);
+              if (lo > hi) continue;
+              const bool trap = ends[2 * r2] < ends[2 * r2 + 1];
+#pragma unroll
+              for (int c = 0; c < 6; ++c) {
+                const int q = (c < 2) ? c : c + 4;
+                double v = P0[(size_t)hi * 6 + c] - P0[(size_t)(lo - 1) * 6 + c];
+                if (trap) v -= 0.5 * (Vn[(size_t)(lo - 1) * 12 + q] + Vn[(size_t)(hi - 1) * 12 + q]) * isc;
+                C[c] += v;
+              }
+            }
+          }
+          const dflt ik = ikd;
+          const cdf c1 = cdf_rmul(om_combr(omd, kap, df_of(C[0]), df_of(C[1])), ik);
+          const cdf c3 = cdf_rmul(om_combr(omd, kap, df_of(C[2]), df_of(C[3])), ik);
+          cp = cdf_rmul(om_combr(omd, kap, df_of(C[4]), df_of(C[5])), ik);
+          xz = {df_add(xz.x, df_neg(c1.x)), df_add(xz.y, df_neg(c1.y))};
+          yz = {df_add(yz.x, df_neg(c3.x)), df_add(yz.y, df_neg(c3.y))};
+        }
+        const cdf zz = cdf_mul(zeta, xz);
+        X[2] = {df_add(zz.x, df_neg(cp.x)), df_add(zz.y, df_neg(cp.y))};
+        X[4] = xz;
+        X[5] = yz;
+      }
+      // add the order's entries with its factors C0 v_e(n) (xy and xz odd in n)
+      const float* __restrict__ fac = S.bfac + (size_t)n * 12;
+#pragma unroll
+      for (int e = 0; e < 6; ++e) {
+        dflt fe = {fac[2 * e], fac[2 * e + 1]};
+        if (nn < 0 && (e == 3 || e == 4)) fe = df_neg(fe);
+        df_acc(acc[2 * e], df_mul(fe, X[e].x));
+        df_acc(acc[2 * e + 1], df_mul(fe, X[e].y));
+      }
     }
   }
-  // rescale and combine: acc_e = phase_e (omega S_{e,1} + kappa S_{e,2})
-  const double kappa = kpar / S.ms;
+  // rescale and apply the phase (i for xy and yz)
 #pragma unroll
   for (int e = 0; e < 6; ++e) {
-    const double s1 = S.Wscale[2 * e], s2 = S.Wscale[2 * e + 1];
-    const double2 S1 = cmk((df_val(sacc[4 * e]) + (double)Sf[4 * e]) * s1, (df_val(sacc[4 * e + 1]) + (double)Sf[4 * e + 1]) * s1);
-    const double2 S2 = cmk((df_val(sacc[4 * e + 2]) + (double)Sf[4 * e + 2]) * s2,
-                           (df_val(sacc[4 * e + 3]) + (double)Sf[4 * e + 3]) * s2);
-    const double2 t = cadd(cmul(o, S1), cscale(S2, kappa));
-    acc[e] = (e == 3 || e == 5) ? cmk(-t.y, t.x) : t;
+    const double sc = S.Escale[e];
+    const double2 t = cmk(df_val(acc[2 * e]) * sc, df_val(acc[2 * e + 1]) * sc);
+    acc_out[e] = (e == 3 || e == 5) ? cmk(-t.y, t.x) : t;
   }
 }
 
@@ -420,7 +501,7 @@ __device__ __forceinline__ void pole_body(const SysDev& sys, const SpecDev& S, c
 #pragma unroll
     for (int q = 0; q < (LOW ? 3 : 1); ++q) lacc[q][e] = cmk(0.0, 0.0);
   }
-  if (active && !LOW && S.df_sums && S.Wh && n_end > n_begin) {
+  if (active && !LOW && S.df_sums && S.Bt && n_end > n_begin) {
     pole_fused(sys, S, o, js, js_count, n_begin, n_end, acc);
   } else if (active) {
     for (int n = n_begin; n < n_end; ++n) {
@@ -2318,14 +2399,15 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->ppl = S.d_ppl;
   o->df_sums = (c->precision != ALPS_PREC_FP64 && S.d_Vh) ? 1 : 0;
   {
-    const size_t nvf = (size_t)(S.nmax + 1) * (c->sys.npar - 1) * 12, nmo = (size_t)(S.nmax + 1) * ALPS_KFAR * 12;
-    const bool fz = S.d_Wh != nullptr;
-    o->Wh = fz ? S.d_Wh : nullptr;
-    o->Wl = fz ? S.d_Wh + nvf : nullptr;
-    o->mWh = fz ? S.d_Wh + 2 * nvf : nullptr;
-    o->mWl = fz ? S.d_Wh + 2 * nvf + nmo : nullptr;
-    o->mWf = fz ? S.d_Wh + 2 * nvf + 2 * nmo : nullptr;
-    o->Wscale = S.d_Wscale;
+    const size_t nm = (size_t)(S.nmax + 1), M = (size_t)c->sys.npar;
+    const size_t nvf = nm * (M - 1) * 12, nmo = nm * ALPS_KFAR * 12;
+    const bool fz = S.d_Bt != nullptr && S.d_Bd != nullptr;
+    o->Bt = fz ? S.d_Bt : nullptr;
+    o->mBt = fz ? S.d_Bt + nvf : nullptr;
+    o->bfac = fz ? S.d_Bt + nvf + nmo : nullptr;
+    o->Escale = fz ? S.d_Bd : nullptr;
+    o->Cfull = fz ? S.d_Bd + 8 : nullptr;
+    o->Pre = fz ? S.d_Bd + 8 + nm * 6 : nullptr;
     o->qlo = S.qlo;
     o->qhi = S.qhi;
     o->qlo_in = S.qlo_in;

@@ -111,7 +111,7 @@ size_t ctx_device_bytes(const alps_ctx* c) {
     b += (N + 1 + M + 1) * d + 3 * (N + 1) * (M + 1) * d + (N - 1) * 2 * (M - 1) * d;  // grid, f0, g1, g2, G
     b += (N + 1) * 5 * 4 * d + (N + 1) * 16 * d;                                          // fit, fit_aux
     b += (nm + 2) * (N + 1) * d + 3 * nm * (N - 1) * d + 3 * nm * 2 * (M - 1) * d;       // bessel, Rw, A
-    b += nm * (M - 1) * 12 * (d + 16) + (M - 1) * ALPS_KFAR * d + nm * ALPS_KFAR * 12 * (d + 24);  // V, X, mom (+pairs)
+    b += nm * (M - 1) * 12 * (d + 16) + (M - 1) * ALPS_KFAR * d + nm * ALPS_KFAR * 12 * (d + 16);  // V, X, mom (+pairs, base tables)
     b += nm * 30 * d;                                                                      // lmom
     if (S.sp.relat) {
       size_t nf = (size_t)(c->sys.ngamma + 1) * (c->sys.npparbar + 1);

@@ -653,63 +653,80 @@ __global__ void k_moments(const double* __restrict__ V, const double* __restrict
   moml[t] = __double2float_rn(x - (double)h);
 }
 
-// The fast path's order-fused tables.  Entry e of chi gets, per signed
-// order nn, C0 pref_e(nn) (omega S_{e,1} + kappa S_{e,2}) with
-// C0 = 2 pi dpperp |dppar| q / 4 and pref_e = phase_e sgn_e(nn) v_e(|n|):
-// phase i for xy and yz, sgn = sign(nn) for xy and xz (odd in n), else 1.
-// Folding C0 v_e(n) into the reduced vectors and their Laurent moments, with
-// one scale 2^E_q per vector q = 2e + g over all orders, lets the pole sums
-// of a block's orders accumulate in one set of double-float sums.
+// Base tables of the fast path's pole sums.  The six T-tensor entries use
+// three Bessel families, F1 = J^2 (xx, xz, zz), F2 = pperp^2 J'^2 (yy) and
+// F3 = pperp J J' (xy, yz), with the p_par factors 1, p_par, p_par^2.  With
+// R_j = 1 / (k_par (zeta - p_j)), zeta the complex resonance momentum,
+//   p_j R_j = zeta R_j - 1/k_par,
+// so the p_par-weighted sums follow from the family sums and the
+// omega-independent sums of the family vectors themselves:
+//   sum w F p R   = zeta sum w F R - (1/k_par) sum w F,
+//   sum w F p^2 R = zeta sum w F p R - (1/k_par) sum w F p.
+// A node or Laurent term then feeds 6 real vectors instead of 12.  The
+// vectors are V's q = 0, 1 (F1), 2, 3 (F2), 6, 7 (F3), scaled by
+// 1/Vscale[n] (a power of two) and split into float pairs.
+__device__ __forceinline__ int base_q(int b) { return b < 4 ? b : b + 2; }
 
-// Wscale[q] = 2^E_q, E_q the exponent of the largest |C0 v_e(n) x| over the
-// vectors and moments of q (one block per q)
-__global__ void k_fused_scale(const double* __restrict__ V, const double* __restrict__ mom, int M, int nmax,
-                              double z, double kperp, int kperp_norm, double C0, double* Wscale) {
-  // |C0 v_e(n)| per order in shared memory ((nmax + 1) doubles, dynamic):
-  // max_u fl(|f_n| |x_u|) = fl(|f_n| max_u |x_u|), rounding being monotone
-  extern __shared__ double fsh[];
-  __shared__ double red[1024];
-  const int q = blockIdx.x, e = q >> 1;
-  for (int n = threadIdx.x; n <= nmax; n += blockDim.x) fsh[n] = fabs(fused_factor(n, e, z, kperp, kperp_norm, C0));
-  __syncthreads();
-  double mx = 0.0;
-  const size_t nv = (size_t)(nmax + 1) * (M - 1), nm = (size_t)(nmax + 1) * ALPS_KFAR;
-  for (size_t t = threadIdx.x; t < nv + nm; t += blockDim.x) {
-    const bool isv = t < nv;
-    const size_t u = isv ? t : t - nv;
-    const int n = isv ? (int)(u / (M - 1)) : (int)(u / ALPS_KFAR);
-    const double x = isv ? V[u * 12 + q] : mom[u * 12 + q];
-    mx = fmax(mx, fsh[n] * fabs(x));
-  }
-  red[threadIdx.x] = mx;
-  __syncthreads();
-  for (int s2 = blockDim.x / 2; s2 > 0; s2 >>= 1) {
-    if (threadIdx.x < s2) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s2]);
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) Wscale[q] = (red[0] > 0.0 && isfinite(red[0])) ? ldexp(1.0, ilogb(red[0])) : 1.0;
-}
-
-// W = C0 v_e(n) V / Wscale as float pairs; the moments likewise, plus FP32
-__global__ void k_fused_pairs(const double* __restrict__ V, const double* __restrict__ mom, int M, int nmax,
-                              double z, double kperp, int kperp_norm, double C0, const double* __restrict__ Wscale,
-                              float* Wh, float* Wl, float* mWh, float* mWl, float* mWf) {
-  const size_t nv = (size_t)(nmax + 1) * (M - 1) * 12, nm = (size_t)(nmax + 1) * ALPS_KFAR * 12;
+// Bt and mBt: hi parts at [rec*12 + b], lo parts at [rec*12 + 6 + b]
+__global__ void k_base_pairs(const double* __restrict__ V, const double* __restrict__ mom,
+                             const double* __restrict__ Vscale, int M, int nmax, float* Bt, float* mBt) {
+  const size_t nv = (size_t)(nmax + 1) * (M - 1) * 6, nm = (size_t)(nmax + 1) * ALPS_KFAR * 6;
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nv + nm) return;
   const bool isv = t < nv;
   const size_t u = isv ? t : t - nv;
-  const int q = (int)(u % 12);
-  const int n = isv ? (int)(u / (12 * (size_t)(M - 1))) : (int)(u / (12 * (size_t)ALPS_KFAR));
-  const double x = (isv ? V[u] : mom[u]) * fused_factor(n, q >> 1, z, kperp, kperp_norm, C0) * (1.0 / Wscale[q]);
+  const size_t rec = u / 6;
+  const int b = (int)(u % 6);
+  const int n = isv ? (int)(rec / (M - 1)) : (int)(rec / ALPS_KFAR);
+  const double x = (isv ? V[rec * 12 + base_q(b)] : mom[rec * 12 + base_q(b)]) * (1.0 / Vscale[n]);
   const float h = __double2float_rn(x), l = __double2float_rn(x - (double)h);
-  if (isv) {
-    Wh[u] = h;
-    Wl[u] = l;
-  } else {
-    mWh[u] = h;
-    mWl[u] = l;
-    mWf[u] = h;
+  float* o = isv ? Bt : mBt;
+  o[rec * 12 + b] = h;
+  o[rec * 12 + 6 + b] = l;
+}
+
+// Pre[(n*M + j)*6 + c] = sum_{i=1..j} X_c(i), X = V[q]/Vscale[n] for
+// q = 0, 1 (F1), 6, 7 (F3), 8, 9 (p_par F1), compensated (two-sum) so that
+// each stored prefix is the exact sum rounded once; Cfull[n*6 + c] = the
+// trapezoid sum over j = 1..M-1 (ends at weight 1/2).  One thread per (n, c).
+__global__ void k_base_consts(const double* __restrict__ V, const double* __restrict__ Vscale, int M, int nmax,
+                              double* Pre, double* Cfull) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (nmax + 1) * 6) return;
+  const int n = t / 6, c = t % 6;
+  const int q = (c < 2) ? c : c + 4;
+  const double sc = 1.0 / Vscale[n];
+  const double* v = V + (size_t)n * (M - 1) * 12 + q;
+  double* P = Pre + (size_t)n * M * 6 + c;
+  double s = 0.0, e = 0.0;
+  P[0] = 0.0;
+  for (int j = 1; j <= M - 1; ++j) {
+    const double x = v[(size_t)(j - 1) * 12] * sc;
+    const double y = s + x, bb = y - s;
+    e += (s - (y - bb)) + (x - bb);
+    s = y;
+    P[(size_t)j * 6] = s + e;
+  }
+  const double x1 = v[0] * sc, xe = v[(size_t)(M - 2) * 12] * sc;
+  Cfull[t] = (s + e) - 0.5 * (x1 + xe);
+}
+
+// Escale[e] = 2^E, E the exponent of max_n |C0 v_e(n) Vscale[n]|, and
+// bfac[(n*6 + e)*2 + {0,1}] = C0 v_e(n) Vscale[n] / Escale[e] as a float
+// pair (v_e of order n >= 0; xy and xz flip sign for -n).  One warp.
+__global__ void k_base_fac(int nmax, double z, double kperp, int kperp_norm, double C0,
+                           const double* __restrict__ Vscale, double* Escale, float* bfac) {
+  const int e = threadIdx.x;
+  if (e >= 6) return;
+  double mx = 0.0;
+  for (int n = 0; n <= nmax; ++n) mx = fmax(mx, fabs(fused_factor(n, e, z, kperp, kperp_norm, C0) * Vscale[n]));
+  const double sc = (mx > 0.0 && isfinite(mx)) ? ldexp(1.0, ilogb(mx)) : 1.0;
+  Escale[e] = sc;
+  for (int n = 0; n <= nmax; ++n) {
+    const double x = fused_factor(n, e, z, kperp, kperp_norm, C0) * Vscale[n] * (1.0 / sc);
+    const float h = __double2float_rn(x);
+    bfac[((size_t)n * 6 + e) * 2] = h;
+    bfac[((size_t)n * 6 + e) * 2 + 1] = __double2float_rn(x - (double)h);
   }
 }
 
@@ -1290,22 +1307,22 @@ int launch_build_bessel_and_reduced(alps_ctx* c, int is, double kperp) {
   k_moments<<<(tot + 127) / 128, 128, 0, st>>>(S.d_V, S.d_X, M, nmax, S.d_Vscale, S.d_mom, S.d_momf, S.d_momh,
                                                S.d_moml);
   ALPS_CUDA_TRY(cudaGetLastError());
-  // order-fused tables of the fast path (prefactors and C0 folded in)
+  // base tables of the fast path's pole sums
   {
     const double z = c->sys.kperp_norm ? kperp / S.sp.qs : 1.0 / S.sp.qs;
     const double dpperp = S.pperp[2] - S.pperp[1], dppar_abs = std::fabs(S.ppar[2] - S.ppar[1]);
     const double C0 = 2.0 * ALPS_PI * dpperp * dppar_abs * 0.25 * S.sp.qs;
-    if ((rc = ensure(S.d_Wh, S.Wf_cap, 2 * nvf + 3 * nmo))) return rc;  // W hi, lo; moments hi, lo, FP32
-    if (!S.d_Wscale) ALPS_CUDA_TRY(cudaMalloc(&S.d_Wscale, 12 * sizeof(double)));
-    const size_t fsm = (size_t)(nmax + 1) * sizeof(double);
-    if (fsm > 48 * 1024) return ALPS_E_INVALID;  // nmax < 2000 keeps it within 16 KB
-    k_fused_scale<<<12, 1024, fsm, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp, c->sys.kperp_norm, C0, S.d_Wscale);
+    const size_t nm = (size_t)(nmax + 1);
+    if ((rc = ensure(S.d_Bt, S.Bt_cap, nvf + nmo + nm * 12))) return rc;  // Bt, mBt, bfac
+    if ((rc = ensure(S.d_Bd, S.Bd_cap, 8 + nm * 6 + nm * (size_t)M * 6))) return rc;  // Escale, Cfull, Pre
+    const size_t np = (nvf + nmo) / 2;
+    k_base_pairs<<<(unsigned)((np + 255) / 256), 256, 0, st>>>(S.d_V, S.d_mom, S.d_Vscale, M, nmax, S.d_Bt,
+                                                              S.d_Bt + nvf);
     ALPS_CUDA_TRY(cudaGetLastError());
-    const size_t nf = nvf + nmo;
-    k_fused_pairs<<<(unsigned)((nf + 255) / 256), 256, 0, st>>>(S.d_V, S.d_mom, M, nmax, z, kperp,
-                                                                c->sys.kperp_norm, C0, S.d_Wscale, S.d_Wh,
-                                                                S.d_Wh + nvf, S.d_Wh + 2 * nvf,
-                                                                S.d_Wh + 2 * nvf + nmo, S.d_Wh + 2 * nvf + 2 * nmo);
+    k_base_consts<<<(unsigned)((nm * 6 + 127) / 128), 128, 0, st>>>(S.d_V, S.d_Vscale, M, nmax,
+                                                                      S.d_Bd + 8 + nm * 6, S.d_Bd + 8);
+    ALPS_CUDA_TRY(cudaGetLastError());
+    k_base_fac<<<1, 32, 0, st>>>(nmax, z, kperp, c->sys.kperp_norm, C0, S.d_Vscale, S.d_Bd, S.d_Bt + nvf + nmo);
     ALPS_CUDA_TRY(cudaGetLastError());
   }
   return ALPS_OK;

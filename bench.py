@@ -150,17 +150,28 @@ def pole_sum_flops_issued(nmax, npar):
     return sum(61.0 * (2 * n + 1) * (npar - 1) for n in nmax)
 
 
-# FP32-pipe flops (FMA = 2) of one double-float node of the fast path's pole
-# sums, counted from the kernel's code (device_math.cuh, disp_kernels.cu):
-# the pole distance d = A - k_par p_j (19), |d|^2 + D^2 (19), its reciprocal
-# (rcp and three FMA / one multiply of its series correction, 8), the two
-# weights (22) and 24 double-float multiply-accumulates of the 12 reduced
-# vectors against them (15 each: product with its error term, two-sum into
-# the accumulator)
-DF_NODE_FLOPS = 19 + 19 + 8 + 22 + 24 * 15
-# one double-float Laurent term: 24 multiply-accumulates of the 12 moments
-# against the complex power (15 each) and the power update (4 products, 2 sums)
-DF_TERM_FLOPS = 24 * 15 + 4 * 9 + 2 * 10
+# FP32-pipe flops (FMA = 2) of the fast path's pole sums, counted from the
+# kernel's code (device_math.cuh, disp_kernels.cu pole_fused).  One
+# double-float node: the pole distance d = A - k_par p_j (19), |d|^2 + D^2
+# (19), its reciprocal (rcp and three FMA / one multiply of its series
+# correction, 8), the two weights (22) and 12 double-float
+# multiply-accumulates of the 6 base vectors (three Bessel families against
+# g1 and g2) against them (15 each: product with its error term, two-sum
+# into the accumulator)
+DF_NODE_FLOPS = 19 + 19 + 8 + 22 + 12 * 15
+# one double-float Laurent term (k >= 2): 12 multiply-accumulates of the
+# base moments against the complex power and the power update (4 products,
+# 2 sums)
+DF_TERM_FLOPS = 12 * 15 + 4 * 9 + 2 * 10
+# one FP32 Laurent tail term: 12 FMA and the complex power update
+FP32_TERM_FLOPS = 12 * 2 + 6
+# per (omega, signed order), the combination of the base sums into the six
+# entries (double-float: complex product 62, omega-combination 104, real
+# factor and accumulation 18 per component): a node sum's zeta products and
+# range sums (about 1000), a series' k = 0, 1 terms, the Laurent T and U
+# parts and the d, p_cen products (about 2100)
+DF_ORDER_NODE_FLOPS = 1000
+DF_ORDER_SERIES_FLOPS = 2100
 
 
 def pole_sum_work_fast(system, species, kpar, oms, nmax):
@@ -170,13 +181,16 @@ def pole_sum_work_fast(system, species, kpar, oms, nmax):
     terms, rho^K <= 2^-53 (1 - rho), of which those from K32 on
     (rho^K32 <= 2^-33 (1 - rho)) run in FP32 and the ones before in
     double-float; any other order sums its nodes (a resonant one outside the
-    principal-value window) in double-float.  Returns counts: nodes (signed
-    order x node pairs summed), series terms in double-float and in FP32, and
-    resonant items (omega, species, signed order)."""
+    principal-value window) in double-float.  The series' k = 0, 1 terms
+    are part of the order's combination.  Returns counts: nodes (signed
+    order x node pairs summed), series terms in double-float and in FP32,
+    orders summed over nodes and by series, and resonant items (omega,
+    species, signed order)."""
     ns, npar, M_I = system.nspec, system.npar, system.positions_principal
     M = npar
     kfar = min(128, int(0.8 * (M - 1)))
-    out = {"nodes": 0.0, "series_df": 0.0, "series_fp32": 0.0, "items": 0.0}
+    out = {"nodes": 0.0, "series_df": 0.0, "series_fp32": 0.0, "node_orders": 0.0, "series_orders": 0.0,
+           "items": 0.0}
     for si in range(ns):
         spc, pl = species[si][0], np.asarray(species[si][2])
         ppar = pl.reshape(-1, M + 1)[0]
@@ -194,10 +208,12 @@ def pole_sum_work_fast(system, species, kpar, oms, nmax):
             K = np.where(far, np.ceil((36.7368005696771 - np.log1p(-rho)) / -np.log(rho)) + 1, kfar + 1)
             K32 = np.where(far, np.ceil((22.8738569584782 - np.log1p(-rho)) / -np.log(rho)) + 1, kfar + 1)
             lau = K <= kfar
-            out["series_df"] += np.minimum(K32, K)[lau].sum()
-            out["series_fp32"] += np.maximum(K - K32, 0)[lau].sum()
+            out["series_df"] += np.maximum(np.minimum(K32, K) - 2, 0)[lau].sum()
+            out["series_fp32"] += np.maximum(K - np.maximum(K32, 2), 0)[lau].sum()
+            out["series_orders"] += lau.sum()
             nodes = np.where(res, (M - 1) - (2 * M_I + 2), M - 1)
             out["nodes"] += nodes[~lau].sum()
+            out["node_orders"] += (~lau).sum()
             out["items"] += res.sum()
     return {k: float(v) for k, v in out.items()}
 
@@ -775,14 +791,16 @@ def main():
     fast_pole_ms, res_ms = per_fast[1], per_fast[2]
     work = pole_sum_work_fast(system, species, kpar, oms, nmax)
     # pole sums: double-float node sums and series terms, FP32 series tails
-    # (54 flops per term), all on the FP32 pipes
-    f32 = work["nodes"] * DF_NODE_FLOPS + work["series_df"] * DF_TERM_FLOPS + work["series_fp32"] * 54.0
+    # and the per-order combinations, all on the FP32 pipes
+    f32 = (work["nodes"] * DF_NODE_FLOPS + work["series_df"] * DF_TERM_FLOPS + work["series_fp32"] * FP32_TERM_FLOPS +
+           work["node_orders"] * DF_ORDER_NODE_FLOPS + work["series_orders"] * DF_ORDER_SERIES_FLOPS)
     pole = {"kernel": "k_pole_sums_multi<false> (fast path)", "bound": "fp32", "kernel_ms": fast_pole_ms,
             "achieved": f32 / (fast_pole_ms / 1e3) / 1e12, "peak": peak32, "unit": "TFLOP/s",
             "frac": f32 / (fast_pole_ms / 1e3) / 1e12 / peak32, "fp32_flop_per_step": f32,
             "double_float_nodes_per_step": work["nodes"], "df_node_flops": DF_NODE_FLOPS,
             "series_terms_df": work["series_df"], "df_term_flops": DF_TERM_FLOPS,
-            "series_terms_fp32": work["series_fp32"]}
+            "series_terms_fp32": work["series_fp32"], "node_orders": work["node_orders"],
+            "series_orders": work["series_orders"], "order_flops": [DF_ORDER_NODE_FLOPS, DF_ORDER_SERIES_FLOPS]}
     # resonant items: the algorithmic count per item, 24 M_P flops of
     # principal-value sums and 60 (N_perp + 1) of Landau rows, FP64
     f_res = work["items"] * (24.0 * system.n_resonance_interval + 60.0 * (system.nperp + 1))
