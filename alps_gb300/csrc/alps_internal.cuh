@@ -113,6 +113,7 @@ struct __align__(16) SpecDev {
   double kappa;       // k_par / m_s
   double pvc;         // 2 pi dpperp/4 (-q/(2 k_par)): the principal-value scale over smdelta
   double pcen, prad;  // centre and half-width of ppar[1..M-1]
+  float pcen32, prad32;  // the same rounded to FP32
   int kfar;           // max Laurent terms used (<= ALPS_KFAR)
   int rcap;           // resonant-item slots per (omega, species)
   // [(N+1)][nf][4] = {p1 exp(-pc pperp^2), p2, p3, exp(-p2 dppar^2)} when
@@ -124,6 +125,14 @@ struct __align__(16) SpecDev {
   const double* lmom;
   double p2r, p3r, la, lb, lc, min_a0;
   double lgc;  // exp(-p2r dppar^2)
+  // the fast path's copy of the moments: per (n, F) ten float pairs scaled
+  // by 2^-e (hi 0..9, lo 10..19, e at 20, 24 floats); the bound's
+  // coefficients in FP32, lgc as a float pair, -2 p2r dppar, and the
+  // exponents of min_a0 and lgc (the underflow test of the row Gaussians)
+  const float* lmomf;
+  float la32, lb32, lc32, lgch, lgcl;
+  double lcx;
+  int lze, lge;
   // relativistic species (src/ALPS_fns_rel.f90): (Gamma, pparbar) grid
   int relat, ng, np;
   const double* grel;   // [ng+1]

@@ -191,6 +191,63 @@ __device__ __forceinline__ void df_mac(dflt& acc, float vh, float vl, dflt r) {
   acc.l = __fadd_rn(acc.l, __fadd_rn(s.l, pl));
 }
 
+// 1/j! as float pairs (hi, lo), j = 0..18: the Taylor coefficients of
+// df_exp_scaled and df_cis
+__constant__ float c_inv_fact[19][2] = {
+    {1.0f, 0.0f}, {1.0f, 0.0f}, {0.5f, 0.0f},
+    {0.1666666716337204f, -4.967053879312289e-09f}, {0.0416666679084301f, -1.2417634698280722e-09f},
+    {0.008333333767950535f, -4.34617203337595e-10f}, {0.0013888889225199819f, -3.3631094437103215e-11f},
+    {0.00019841270113829523f, -2.725596874933456e-12f}, {2.4801587642286904e-05f, -3.40699609366682e-13f},
+    {2.7557318844628753e-06f, 3.793571224297229e-14f}, {2.755731998149713e-07f, -7.575112209051195e-15f},
+    {2.5052107943679403e-08f, 4.4176230446483665e-16f}, {2.0876755879584152e-09f, 1.1082839147459852e-16f},
+    {1.6059044372074283e-10f, -5.352526511562726e-18f}, {1.147074536050896e-11f, 2.372207689231238e-19f},
+    {7.647163609812713e-13f, 1.2200710471178288e-20f}, {4.7794772561329454e-14f, 7.62544404448643e-22f},
+    {2.8114573589663704e-15f, -1.0462084739763658e-22f}, {1.5619206814541513e-16f, 1.5404471465941993e-24f}};
+__device__ __forceinline__ dflt inv_fact(int j) { return {c_inv_fact[j][0], c_inv_fact[j][1]}; }
+
+// exp(x) = 2^k m for a double x, |x| <= 1000, with m a float pair in
+// [0.70, 1.42] (relative error about 2^-47, tested against FP64 on the CPU):
+// k = rint(x / ln 2) and r = x - k ln 2 in FP64 (Cody and Waite: ln 2 in two
+// parts, k ln2_hi exact for |k| < 2^21), then the Taylor polynomial of
+// degree 13 of exp(r), |r| <= 0.347 (truncation below 2^-57), in
+// double-float.
+__device__ __forceinline__ dflt df_exp_scaled(double x, int& k) {
+  const double kd = rint(x * 1.4426950408889634);
+  double r = fma(-kd, 0.6931471803691238, x);
+  r = fma(-kd, 1.9082149292705877e-10, r);
+  k = (int)kd;
+  const dflt q = df_of(r);
+  dflt p = inv_fact(13);
+#pragma unroll
+  for (int j = 12; j >= 0; --j) p = df_add(df_mul(p, q), inv_fact(j));
+  return p;
+}
+
+// cos(y) + i sin(y) for a double y, |y| < 1e6 (absolute error about 2^-46):
+// q = rint(y 2/pi) and r = y - q pi/2 in FP64 (Cody and Waite: pi/2 in three
+// parts, the first two products exact for |q| < 2^20), then with s = r^2,
+// |r| <= pi/4, sin r = r sum_j (-s)^j / (2j+1)! and cos r = sum_j (-s)^j /
+// (2j)!, j <= 8 (truncation below 2^-58), in double-float; q mod 4 picks
+// the signs and the order.
+__device__ __forceinline__ void df_cis(double y, dflt& c, dflt& sn) {
+  const double qd = rint(y * 0.6366197723675814);
+  double r = fma(-qd, 1.5707963267341256, y);
+  r = fma(-qd, 6.077100506303966e-11, r);
+  r = fma(-qd, 2.0222662487959506e-21, r);
+  const dflt rd = df_of(r), sq = df_mul(rd, rd);
+  const dflt ms = df_neg(sq);
+  dflt ps = inv_fact(17), pc = inv_fact(16);
+#pragma unroll
+  for (int j = 7; j >= 0; --j) {
+    ps = df_add(df_mul(ps, ms), inv_fact(2 * j + 1));
+    pc = df_add(df_mul(pc, ms), inv_fact(2 * j));
+  }
+  const dflt sv = df_mul(ps, rd);
+  const int qm = (int)((long long)qd & 3);
+  c = (qm == 0) ? pc : ((qm == 1) ? df_neg(sv) : ((qm == 2) ? df_neg(pc) : sv));
+  sn = (qm == 0) ? sv : ((qm == 1) ? pc : ((qm == 2) ? df_neg(sv) : df_neg(pc)));
+}
+
 // Fast FP64 reciprocal: PTX rcp.approx seed + two Newton steps (<= 1 ulp).
 __device__ __forceinline__ double rcp_fast(double x) {
   double r;

@@ -189,24 +189,25 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
       const float x32 = Ad.h * ikp32;
       const float mg = 9.5367431640625e-7f * fabsf(x32);  // 2^-20 |x|
       ResGeom g;
-      double2 dfar;  // p_res - pcen (FP32 for orders far from resonance)
+      float ddf;  // |p_res - pcen|^2 (in FP32 alone for orders far from resonance)
       if (x32 < S.qlo - mg || x32 > S.qhi + mg) {
         g.res = 0;
         g.lo1 = 1;
         g.hi1 = M - 1;
         g.lo2 = 1;
         g.hi2 = 0;
-        dfar = cmk((double)(x32 - (float)S.pcen), (double)(dyd.h));
+        const float dx = x32 - S.pcen32;
+        ddf = fmaf(dx, dx, dyd.h * dyd.h);
       } else {
         g = res_geometry(S, sys.M_I, o, nn, kpar);
-        dfar = cmk(g.pr - S.pcen, g.pi);
+        const double2 dfar = cmk(g.pr - S.pcen, g.pi);
+        ddf = (float)(dfar.x * dfar.x + dfar.y * dfar.y);
       }
       int K = S.kfar + 1, K32 = K;
-      const float ddf = (float)(dfar.x * dfar.x + dfar.y * dfar.y);
       // the series is used up to rho^2 < 0.58, where its K <= kfar terms
       // (checked below) cost less than the node sum
-      if (!g.res && (float)S.prad * (float)S.prad < 0.58f * ddf) {
-        const float rho = (float)S.prad * rsqrtf(ddf);
+      if (!g.res && S.prad32 * S.prad32 < 0.58f * ddf) {
+        const float rho = S.prad32 * rsqrtf(ddf);
         const float lr = -__logf(rho), l1 = log1pf(-rho);
         K = (int)ceilf((36.7368006f - l1) / lr) + 1;    // 53 ln 2
         K32 = (int)ceilf((22.8738570f - l1) / lr) + 1;  // 33 ln 2
@@ -347,10 +348,16 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
         X[0] = Q[0];
         X[1] = Q[1];
         X[3] = Q[2];
-        const cdf pQ1 = cdf_rmul(Q[0], pcd), pQ3 = cdf_rmul(Q[2], pcd);
-        X[4] = cdf_add(pQ1, cdf_mul(d, T[0]));
-        X[5] = cdf_add(pQ3, cdf_mul(d, T[2]));
-        X[2] = cdf_add(cdf_rmul(X[4], pcd), cdf_mul(d, cdf_add(cdf_rmul(T[0], pcd), cdf_mul(d, Uw[0]))));
+        X[4] = cdf_mul(d, T[0]);
+        X[5] = cdf_mul(d, T[2]);
+        if (S.pcen32 != 0.0f) {
+          // sum F p R = pcen Q + d T, sum F p^2 R = pcen (sum F p R) + d (pcen T + d U)
+          X[4] = cdf_add(cdf_rmul(Q[0], pcd), X[4]);
+          X[5] = cdf_add(cdf_rmul(Q[2], pcd), X[5]);
+          X[2] = cdf_add(cdf_rmul(X[4], pcd), cdf_mul(d, cdf_add(cdf_rmul(T[0], pcd), cdf_mul(d, Uw[0]))));
+        } else {
+          X[2] = cdf_mul(d, cdf_mul(d, Uw[0]));
+        }
       } else {
         // node sum in double-float: Q_b = sum_j w_j B_b(j) / (A - k_par p_j + i D)
         dflt Qs[12];
@@ -1377,56 +1384,106 @@ __device__ __forceinline__ void resonant_body(const DispArgs& a, const DispShape
       bool rows = lf > 0;
       if (lf > 0 && S.lmom) {
         // factorised rows: valid when the row deviation |delta_i(p')| <= 1e-5
-        // for p' = p, p +- dppar (second-order remainder <= 1.7e-16)
+        // for p' = p, p +- dppar (second-order remainder <= 1.7e-16); the
+        // bound in FP32 with a margin (an item just inside it takes the rows)
         const double2 p = cmk(g.pr, g.pi);
-        const double pd = S.dppar_abs;
-        const double ap = hypot(p.x, p.y) + pd;
-        const double bound = S.la * ap * ap + S.lb * ap + S.lc;
-        if (bound <= 1e-5) {
+        const float ap = sqrtf(fmaf((float)p.x, (float)p.x, (float)p.y * (float)p.y)) * 1.00001f + (float)S.dppar_abs;
+        const float bound = fmaf(fmaf(S.la32, ap, S.lb32), ap, S.lc32);
+        if (bound <= 0.999e-5f) {
           rows = false;
-          auto gauss = [&](double2 x) {
-            double2 d = cmk(x.x - S.p3r, x.y);
-            return cexp_d(cscale(cmul(d, d), -S.p2r));
-          };
-          auto poly = [&](const double* m, double2 x) {
-            double2 acc = cmk(m[4], 0.0);
-            for (int q = 3; q >= 0; --q) acc = cadd(cmul(acc, x), cmk(m[q], 0.0));
-            return acc;
-          };
-          const double2 xp = cadd(p, cmk(pd, 0.0)), xm = csub(p, cmk(pd, 0.0));
-          // the row Gaussian at p, p + dppar, p - dppar:
-          // G(p +- pd) = G(p) exp(-+2 p2r pd d) exp(-p2r pd^2), d = p - p3r
-          const double2 G0 = gauss(p);
-          const double2 ax = cscale(cmk(p.x - S.p3r, p.y), -2.0 * S.p2r * pd);
-          double2 Gp, Gm;
-          if (fabs(ax.x) < 600.0) {
-            const double2 X = cexp_d(ax), Gc = cscale(G0, S.lgc);
-            Gp = cmul(Gc, X);
-            Gm = cmul(Gc, crcp(X));
-          } else {
-            Gp = gauss(xp);
-            Gm = gauss(xm);
-          }
-          const bool zero = (cabs_(Gp) * S.min_a0 == 0.0) || (cabs_(Gm) * S.min_a0 == 0.0) ||
-                            (cabs_(G0) * S.min_a0 == 0.0);
+          // Row Gaussian G(x) = exp(-p2r (x - p3r)^2) at x = p, p +- dppar:
+          // G(p +- pd) = lgc G(p) X^{+-1}, X = exp(-2 p2r pd (p - p3r)).  In
+          // double-float with powers of two kept apart: G(p) = 2^k0 g0,
+          // X = 2^kx xm.  With P_F, Q_F the moment polynomials of family F,
+          //   Spar  = (G(p+pd) P_F(p+pd) - G(p-pd) P_F(p-pd)) / (2 pd)
+          //         = lgc/(2 pd) G(p) (X P_F(p+pd) - X^-1 P_F(p-pd)),
+          //   Sperp = G(p) Q_F(p),
+          //   sum_F = (q/|k_par|) (kappa Spar + (omega - kappa p) Sperp).
+          const double dx = p.x - S.p3r, dy = p.y;
+          int k0, kx;
+          dflt c0, s0, cx, sx;
+          const dflt m0 = df_exp_scaled(-S.p2r * ((dx - dy) * (dx + dy)), k0);
+          df_cis(-2.0 * S.p2r * dx * dy, c0, s0);
+          const dflt mx = df_exp_scaled(S.lcx * dx, kx);
+          df_cis(S.lcx * dy, cx, sx);
+          // an underflowing Gaussian (|G| min_a0 below the FP64 range at any
+          // of the three points) leaves the term zero, as in FP64
+          const int akx = kx < 0 ? -kx : kx;
+          const bool zero = (k0 + S.lze < -1072) || (k0 - akx + S.lge + S.lze < -1072);
           if (!zero) {
-            // the moment polynomials of family F at p + dppar, p - dppar
-            // (d/dp_par moments) and p (d/dp_perp moments)
-            const double ql = S.qs / fabs(kpar), kap = kpar / S.ms;
-            double2 sumF[3];
-            for (int F = 0; F < 3; ++F) {
-              const double* lm = S.lmom + ((size_t)n * 3 + F) * 10;
-              const double2 Pxp = poly(lm, xp), Pxm = poly(lm, xm), Ppp = poly(lm + 5, p);
-              const double2 Spar = cscale(csub(cmul(Gp, Pxp), cmul(Gm, Pxm)), 1.0 / (2.0 * pd));
-              const double2 Sperp = cmul(G0, Ppp);
-              // (q/|kpar|) (kappa Spar - kappa p Sperp + omega Sperp)
-              sumF[F] = cscale(cadd(cscale(csub(Spar, cmul(p, Sperp)), kap), cmul(o, Sperp)), ql);
+            const cdf g0 = {df_mul(m0, c0), df_mul(m0, s0)};
+            const cdf xm = {df_mul(mx, cx), df_mul(mx, sx)};
+            const dflt ixm = df_rcp_approx(mx);
+            const cdf xi = {df_mul(ixm, cx), df_neg(df_mul(ixm, sx))};
+            // X P+ - X^-1 P- = 2^|kx| (a P+ - b P-): (a, b) = (xm, 2^-2kx xi)
+            // for kx >= 0, (2^2kx xm, xi) otherwise (a term below 2^-126 of
+            // the other is dropped)
+            const int sh = 2 * akx;
+            const float sc = sh <= 126 ? ldexpf(1.0f, -sh) : 0.0f;
+            const cdf fa = kx >= 0 ? xm : cdf{df_scale(xm.x, sc), df_scale(xm.y, sc)};
+            const cdf fb = kx >= 0 ? cdf{df_scale(xi.x, sc), df_scale(xi.y, sc)} : xi;
+            const cdf pz = {df_of(p.x), df_of(p.y)};
+            const dflt pdd = df_of(S.dppar_abs);
+            // powers 1..4 of p + pd, p - pd and p
+            cdf zp[3][5];
+            zp[0][1] = {df_add(pz.x, pdd), pz.y};
+            zp[1][1] = {df_add(pz.x, df_neg(pdd)), pz.y};
+            zp[2][1] = pz;
+#pragma unroll
+            for (int u = 0; u < 3; ++u) {
+              zp[u][2] = cdf_mul(zp[u][1], zp[u][1]);
+              zp[u][3] = cdf_mul(zp[u][2], zp[u][1]);
+              zp[u][4] = cdf_mul(zp[u][2], zp[u][2]);
             }
-            const double2 ifac = cmk(0.0, -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf);
+            // sum_m c_m z^m, c real (float pairs at c[m], c[10 + m])
+            auto poly = [&](const float* c, int u) {
+              cdf acc = {{c[0], c[10]}, {0.0f, 0.0f}};
+#pragma unroll
+              for (int m = 1; m < 5; ++m) {
+                const dflt cm = {c[m], c[10 + m]};
+                acc = cdf_add(acc, cdf_rmul(zp[u][m], cm));
+              }
+              return acc;
+            };
+            const cdf omd = {df_of(o.x), df_of(o.y)};
+            // q / |k_par| (the sign of the charge stays)
+            const dflt kapd = df_of(S.kappa), qld = df_of(kpar < 0.0 ? -S.qk : S.qk);
+            const cdf wk = {df_add(omd.x, df_neg(df_mul(kapd, pz.x))), df_add(omd.y, df_neg(df_mul(kapd, pz.y)))};
+            // lgc / (2 pd) and the factor 2^-|kx| of Sperp against Spar
+            const dflt lgd = df_mul({S.lgch, S.lgcl}, df_rcp_approx(df_scale(pdd, 2.0f)));
+            const float sp = akx <= 126 ? ldexpf(1.0f, -akx) : 0.0f;
+            cdf sumF[3];
+            int eF[3];
+#pragma unroll
+            for (int F = 0; F < 3; ++F) {
+              const float* lm = S.lmomf + ((size_t)n * 3 + F) * 24;
+              const cdf Pp = poly(lm, 0), Pm = poly(lm, 1);
+              const cdf Qp = poly(lm + 5, 2);
+              const cdf br = {df_add(cdf_mul(fa, Pp).x, df_neg(cdf_mul(fb, Pm).x)),
+                              df_add(cdf_mul(fa, Pp).y, df_neg(cdf_mul(fb, Pm).y))};
+              const cdf spar = cdf_rmul(cdf_mul(g0, br), lgd);
+              const cdf sperp = cdf_mul(cdf_mul(g0, Qp), wk);
+              const cdf t = {df_add(df_mul(spar.x, kapd), df_scale(sperp.x, sp)),
+                             df_add(df_mul(spar.y, kapd), df_scale(sperp.y, sp))};
+              sumF[F] = cdf_rmul(t, qld);
+              eF[F] = k0 + akx + (int)lm[20];
+            }
+            // res_e = pref_e c_e sum_F(e) ifac, c_e = 1, p or p^2; ifac =
+            // -i dpperp 2 pi^2 lf, pref_e real (imaginary for xy, yz)
+            const cdf p2 = cdf_mul(pz, pz);
+            const double fi = -S.dpperp * ALPS_PI * 2.0 * ALPS_PI * (double)lf;
+#pragma unroll
             for (int e = 0; e < 6; ++e) {
-              const double2 ce = (e == 2) ? cmul(p, p) : ((e == 4 || e == 5) ? p : cmk(1.0, 0.0));
               const int fam = (e == 1) ? 1 : ((e == 3 || e == 5) ? 2 : 0);
-              res[e] = cmul(cmul(cmul(pref[e], ce), sumF[fam]), ifac);
+              cdf v = sumF[fam];
+              if (e == 2) v = cdf_mul(v, p2);
+              else if (e == 4 || e == 5) v = cdf_mul(v, pz);
+              // pref ifac: real pref -> i (pref fi); imaginary i pref.y -> -(pref.y fi)
+              const bool im = (e == 3 || e == 5);
+              const dflt f = df_of(im ? -pref[e].y * fi : pref[e].x * fi);
+              const double vx = df_val(df_mul(v.x, f)), vy = df_val(df_mul(v.y, f));
+              // multiply by i for a real prefactor: (x, y) -> (-y, x)
+              res[e] = im ? cmk(ldexp(vx, eF[fam]), ldexp(vy, eF[fam])) : cmk(ldexp(-vy, eF[fam]), ldexp(vx, eF[fam]));
             }
           }
         }
@@ -2431,6 +2488,8 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   }
   o->pcen = bm ? 0.0 : 0.5 * (S.ppar[1] + S.ppar[c->sys.npar - 1]);
   o->prad = bm ? 0.0 : 0.5 * (S.ppar[c->sys.npar - 1] - S.ppar[1]);
+  o->pcen32 = (float)o->pcen;
+  o->prad32 = (float)o->prad;
   // the series is used only where it is cheaper than the node sum
   o->kfar = (c->precision == ALPS_PREC_FP64) ? 0 : std::min(ALPS_KFAR, (int)(0.8 * (c->sys.npar - 1)));
   o->rcap = S.rcap;
@@ -2443,6 +2502,15 @@ void fill_spec_dev(const alps_ctx* c, int is, SpecDev* o) {
   o->lc = S.lc;
   o->min_a0 = S.min_a0;
   o->lgc = std::exp(-S.p2r * o->dppar * o->dppar);  // dppar is 0 for closed-form species (no grid)
+  o->lmomf = o->lmom ? reinterpret_cast<const float*>(S.d_lmom + (size_t)(S.nmax + 1) * 30) : nullptr;
+  o->la32 = (float)S.la;
+  o->lb32 = (float)S.lb;
+  o->lc32 = (float)S.lc;
+  o->lgch = (float)o->lgc;
+  o->lgcl = (float)(o->lgc - (double)o->lgch);
+  o->lcx = -2.0 * S.p2r * o->dppar_abs;
+  o->lze = (S.min_a0 > 0.0 && std::isfinite(S.min_a0)) ? std::ilogb(S.min_a0) : 0;
+  o->lge = (o->lgc > 0.0) ? std::ilogb(o->lgc) : -2000;
   o->relat = S.sp.relat ? 1 : 0;
   o->ng = c->sys.ngamma;
   o->np = c->sys.npparbar;

@@ -112,7 +112,7 @@ size_t ctx_device_bytes(const alps_ctx* c) {
     b += (N + 1) * 5 * 4 * d + (N + 1) * 16 * d;                                          // fit, fit_aux
     b += (nm + 2) * (N + 1) * d + 3 * nm * (N - 1) * d + 3 * nm * 2 * (M - 1) * d;       // bessel, Rw, A
     b += nm * (M - 1) * 12 * (d + 16) + (M - 1) * ALPS_KFAR * d + nm * ALPS_KFAR * 12 * (d + 16);  // V, X, mom (+pairs, base tables)
-    b += nm * 30 * d;                                                                      // lmom
+    b += nm * 66 * d;                                                                      // lmom (+pairs)
     if (S.sp.relat) {
       size_t nf = (size_t)(c->sys.ngamma + 1) * (c->sys.npparbar + 1);
       b += 3 * nf * d + (nm + 1) * nf * d + (c->sys.ngamma + 1) * 8;

@@ -757,7 +757,8 @@ __global__ void k_fit_aux(const double* __restrict__ fit, const double* __restri
 //          p_perp difference operator applied to h_i R_F(n,i)  (the dfperp sum)
 // h_i = 1/2 at i = 0, N-1, N and 1 otherwise (src/ALPS_fns.f90:1389-1444).
 __global__ void k_landau_moments(const double* __restrict__ bessel, const double* __restrict__ pperp,
-                                 const double* __restrict__ aux, int N, int nmax, double dpperp, double* lmom) {
+                                 const double* __restrict__ aux, int N, int nmax, double dpperp, double* lmom,
+                                 float* lmomf) {
   // one warp per (n, F): lanes over the rows, then a warp sum
   const int t = (int)((blockIdx.x * (size_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
   if (t >= (nmax + 1) * 3) return;
@@ -804,6 +805,20 @@ __global__ void k_landau_moments(const double* __restrict__ bessel, const double
       o[m] = m0[m];
       o[5 + m] = m1[m];
     }
+    // the fast path's copy: float pairs scaled by 2^-e, e the exponent of
+    // the largest of the ten (hi at 0..9, lo at 10..19, e at 20)
+    double mx = 0.0;
+    for (int m = 0; m < 10; ++m) mx = fmax(mx, fabs(o[m]));
+    const int e = (mx > 0.0 && isfinite(mx)) ? ilogb(mx) : 0;
+    float* f = lmomf + (size_t)t * 24;
+    for (int m = 0; m < 10; ++m) {
+      const double x = ldexp(o[m], -e);
+      const float h = __double2float_rn(x);
+      f[m] = h;
+      f[10 + m] = __double2float_rn(x - (double)h);
+    }
+    f[20] = (float)e;
+    f[21] = f[22] = f[23] = 0.0f;
   }
 }
 
@@ -1357,10 +1372,11 @@ int launch_landau_moments(alps_ctx* c, int is) {
     // and only the mixed path reads them
     if (!S.lfact || c->precision == ALPS_PREC_FP64) return ALPS_OK;
     int rc;
-    if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(S.nmax + 1) * 30))) return rc;
+    if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(S.nmax + 1) * (30 + 36)))) return rc;  // FP64, then the pairs
     const int tot = (S.nmax + 1) * 3;
     k_landau_moments<<<(tot + 3) / 4, 128, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, c->sys.nperp,
-                                                           S.nmax, S.pperp[2] - S.pperp[1], S.d_lmom);
+                                                           S.nmax, S.pperp[2] - S.pperp[1], S.d_lmom,
+                                                           reinterpret_cast<float*>(S.d_lmom + (size_t)(S.nmax + 1) * 30));
     ALPS_CUDA_TRY(cudaGetLastError());
     return ALPS_OK;
   }
@@ -1390,11 +1406,12 @@ int launch_landau_moments(alps_ctx* c, int is) {
   S.lfact = true;
   if (c->precision == ALPS_PREC_FP64) return ALPS_OK;
   int rc;
-  if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(nmax + 1) * 30))) return rc;
+  if ((rc = ensure(S.d_lmom, S.lmom_cap, (size_t)(nmax + 1) * (30 + 36)))) return rc;  // FP64, then the pairs
   int tot = (nmax + 1) * 3;
   double dpperp = S.pperp[2] - S.pperp[1];
   k_landau_moments<<<(tot + 3) / 4, 128, 0, c->stream>>>(S.d_bessel, S.d_pperp, S.d_fit_aux, N, nmax, dpperp,
-                                                         S.d_lmom);
+                                                         S.d_lmom,
+                                                         reinterpret_cast<float*>(S.d_lmom + (size_t)(nmax + 1) * 30));
   ALPS_CUDA_TRY(cudaGetLastError());
   return ALPS_OK;
 }

@@ -15,7 +15,12 @@ relies on:
     below 2^-40 (about 1e-12) of the sum of the terms' magnitudes.  The low
     part is normalised only when the sum is read, so its own FP32 roundings
     add up: the worst of several hundred random sums is near 2^-42, the
-    median near 2^-47 (FP64 accumulation: 2^-53 per term).
+    median near 2^-47 (FP64 accumulation: 2^-53 per term);
+  * df_exp_scaled, exp(x) = 2^k m from a Cody-Waite reduction and the
+    Taylor polynomial of degree 13: relative error below 2^-46 against FP64;
+  * df_cis, cos y + i sin y from a Cody-Waite reduction by pi/2 and Taylor
+    polynomials in r^2: absolute error below 2^-45 against FP64 (the
+    factorised Landau term of the resonant kernel uses both).
 
 The GPU parity tests hold the device code itself to the oracle; this file
 checks the algorithms' bounds on the CPU.
@@ -136,3 +141,83 @@ def test_node_sum_bound():
             exact += t
             mag += abs(t)
         assert abs(val(acc) - exact) <= 2.0 ** -40 * mag, (trial, val(acc), exact, mag)
+
+
+# 1/j! as float pairs, as in device_math.cuh (c_inv_fact)
+def _inv_fact_pairs():
+    from fractions import Fraction
+    out = []
+    f = Fraction(1)
+    for j in range(19):
+        if j:
+            f /= j
+        h = f32(float(f))
+        out.append((h, f32(float(f - Fraction(float(h))))))
+    return out
+
+
+INV_FACT = _inv_fact_pairs()
+
+
+def df_scale(a, s):
+    return f32(a[0] * s), f32(a[1] * s)
+
+
+def df_exp_scaled(x):
+    """exp(x) = 2^k m (device_math.cuh df_exp_scaled): Cody-Waite reduction
+    in FP64, Taylor polynomial of degree 13 of exp(r), |r| <= ln(2)/2"""
+    kd = np.rint(x * 1.4426950408889634)
+    r = np.float64(x) - kd * 0.6931471803691238  # exact product (|k| < 2^21, 32-bit ln2_hi)
+    r = r - kd * 1.9082149292705877e-10
+    q = df_of(r)
+    p = INV_FACT[13]
+    for j in range(12, -1, -1):
+        p = df_add(df_mul(p, q), INV_FACT[j])
+    return int(kd), p
+
+
+def df_cis(y):
+    """cos y + i sin y (device_math.cuh df_cis): Cody-Waite reduction by
+    pi/2 in FP64, Taylor polynomials in r^2 of degree 8, quadrant by q mod 4"""
+    qd = np.rint(y * 0.6366197723675814)
+    r = np.float64(y) - qd * 1.5707963267341256
+    r = r - qd * 6.077100506303966e-11
+    r = r - qd * 2.0222662487959506e-21
+    rd = df_of(r)
+    sq = df_mul(rd, rd)
+    ms = (f32(-sq[0]), f32(-sq[1]))
+    ps, pc = INV_FACT[17], INV_FACT[16]
+    for j in range(7, -1, -1):
+        ps = df_add(df_mul(ps, ms), INV_FACT[2 * j + 1])
+        pc = df_add(df_mul(pc, ms), INV_FACT[2 * j])
+    sv = df_mul(ps, rd)
+    neg = lambda a: (f32(-a[0]), f32(-a[1]))
+    qm = int(qd) & 3
+    c = [pc, neg(sv), neg(pc), sv][qm]
+    s = [sv, pc, neg(sv), neg(pc)][qm]
+    return c, s
+
+
+def test_exp_scaled_bound():
+    """relative error of 2^k m against FP64 exp on |x| <= 700: below 2^-46
+    (the argument is taken as exact; FP64 exp rounds its result, 2^-53)"""
+    rng = np.random.default_rng(14)
+    worst = 0.0
+    for x in np.concatenate([rng.uniform(-700, 700, 1500), rng.uniform(-2, 2, 500), [0.0, 1e-300, -0.3465, 0.3466]]):
+        k, m = df_exp_scaled(x)
+        got = np.ldexp(val(m), k)
+        exact = np.exp(np.float64(x))
+        worst = max(worst, abs(got - exact) / exact)
+        assert 0.69 < val(m) < 1.43
+    assert worst < 2.0 ** -46, worst
+
+
+def test_cis_bound():
+    """absolute error of cos and sin against FP64 on |y| <= 1000: below
+    2^-45 (FP64's own result and the input's rounding dominate near 1000)"""
+    rng = np.random.default_rng(15)
+    worst = 0.0
+    for y in np.concatenate([rng.uniform(-1000, 1000, 1000), rng.uniform(-4, 4, 1000), [0.0, np.pi / 4, -np.pi / 2]]):
+        c, s = df_cis(y)
+        worst = max(worst, abs(val(c) - np.cos(y)), abs(val(s) - np.sin(y)))
+    assert worst < 2.0 ** -45, worst
