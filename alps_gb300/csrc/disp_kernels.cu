@@ -2755,15 +2755,15 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[1], st));
   const unsigned g2 = (unsigned)((long)tiles * S_ * sh.nchunk);
+  const size_t smem = res_smem(c);
+  if ((rcode = res_smem_optin(smem))) return rcode;
+  long blocks = ((long)nslots + RES_WARPS * sh.ipw - 1) / (RES_WARPS * sh.ipw);
   if (want_low)
     k_pole_sums_multi<true><<<g2, 128, 0, st>>>(dj, 1);
   else
     k_pole_sums_multi<false><<<g2, 128, 0, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (c->profiling) ALPS_CUDA_TRY(cudaEventRecord(ev[2], st));
-  const size_t smem = res_smem(c);
-  if ((rcode = res_smem_optin(smem))) return rcode;
-  long blocks = ((long)nslots + RES_WARPS * sh.ipw - 1) / (RES_WARPS * sh.ipw);
   k_resonant_multi<<<(unsigned)blocks, RES_WARPS * 32, smem, st>>>(dj, 1);
   ALPS_CUDA_TRY(cudaGetLastError());
   if (a.relcap && (rcode = launch_rel_orders(a.sys, a.sp, a.relcap, n, d_om, c->d_rel, c->d_flags, st)))

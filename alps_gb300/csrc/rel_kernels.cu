@@ -168,7 +168,8 @@ __global__ void k_tps_eval(const double* __restrict__ w, const double* __restric
   }
   f = f + w[n] + w[n + 1] * g + w[n + 2] * pb;
   f = exp(f);
-  if ((g * g - 1.0) < (pb * pb)) f = -1.0;
+  // outside the subluminal cone, decided as the reference rounds it (no FMA)
+  if (__dsub_rn(__dmul_rn(g, g), 1.0) < __dmul_rn(pb, pb)) f = -1.0;
   f0rel[t] = f;
 }
 
@@ -853,7 +854,9 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
   if (fabs(denomI) > sy.Tlim) {
     if (lane == 0) pair(denomR, 1.0);
     if (lane == 1) pair(denomR + capDelta, 1.0);
-    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) pair(denomR + smdelta * ip, 2.0);
+    // sample points rounded as the reference writes them (no FMA): a point
+    // can fall on a node, where funct_g_rel's choice of node depends on it
+    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) pair(__dadd_rn(denomR, __dmul_rn(smdelta, (double)ip)), 2.0);
   } else {
     funct_g_rel_d(r, denomR + dpb, Ga);
     funct_g_rel_d(r, denomR - dpb, Gb);
@@ -870,7 +873,7 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
       for (int e = 0; e < 6; ++e) pi.v[e] = cadd(pi.v[e], cscale(cscale(gp[e], w), f));
     };
     if (lane == 0) lor(denomR + capDelta, 2.0);
-    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) lor(denomR + smdelta * ip, 4.0);
+    for (int ip = 1 + lane; ip <= M_P - 1; ip += 32) lor(__dadd_rn(denomR, __dmul_rn(smdelta, (double)ip)), 4.0);
     if (denomI != 0.0 && lane == 0) {
       funct_g_rel_d(r, denomR, Ga);
       double sgn = denomI > 0.0 ? 1.0 : -1.0;
@@ -891,8 +894,11 @@ __device__ void principal_rel_d(const RowCtx& r, int ipres, int upperlimit, C6& 
       for (int e = 0; e < 6; ++e) pi.v[e] = cadd(pi.v[e], cscale(cdiv(Ga[e], da), w * correction));
     };
     if (lane == 0) tail(denomR + capDelta, 1.0);
-    if (lane == 1) tail(denomR + capDelta + correction * smdelta * ntiny, 1.0);
-    for (int ip = 1 + lane; ip <= ntiny - 1; ip += 32) tail(denomR + capDelta + correction * smdelta * ip, 2.0);
+    auto tp = [&](int ip) {
+      return __dadd_rn(__dadd_rn(denomR, capDelta), __dmul_rn(__dmul_rn(correction, smdelta), (double)ip));
+    };
+    if (lane == 1) tail(tp(ntiny), 1.0);
+    for (int ip = 1 + lane; ip <= ntiny - 1; ip += 32) tail(tp(ip), 2.0);
   }
   c6_warp_sum(pi);
 #pragma unroll
@@ -912,10 +918,11 @@ __device__ void row_rel_d(const RowCtx& r, C6& out, bool& err, int lane) {
   const double dpb = pb[2] - pb[1];
   const double g = S.grel[r.ig];
   c6_zero(out);
-  const double x = ((g * r.om.x - (1.0 * r.m) * qs / ms) * vA) / kpar;
+  // the resonance and its window decided as the reference rounds them (no FMA)
+  const double x = __ddiv_rn(__dmul_rn(__dsub_rn(__dmul_rn(g, r.om.x), __ddiv_rn(__dmul_rn(1.0 * r.m, qs), ms)), vA), kpar);
   int ipres = 0;
   bool found = false;
-  if ((x * x) <= (g * g - 1.0)) {
+  if (__dmul_rn(x, x) <= __dsub_rn(__dmul_rn(g, g), 1.0)) {
     // the ip in 1..np-2 with pb[ip] <= x < pb[ip+1]
     int lo = 1, hi = np - 2;
     if (np - 2 >= 1 && pb[1] <= x) {
@@ -931,11 +938,12 @@ __device__ void row_rel_d(const RowCtx& r, C6& out, bool& err, int lane) {
     }
   }
   for (int ip = 0; ip <= M_I; ++ip) {
-    if ((x >= (pb[0] - dpb * ip)) && (x < (pb[0] - dpb * (ip - 1)))) {
+    if ((x >= __dsub_rn(pb[0], __dmul_rn(dpb, (double)ip))) && (x < __dsub_rn(pb[0], __dmul_rn(dpb, (double)(ip - 1))))) {
       ipres = -ip;
       found = true;
     }
-    if ((x >= (pb[np - 1] + dpb * ip)) && (x < (pb[np - 1] + dpb * (ip + 1)))) {
+    if ((x >= __dadd_rn(pb[np - 1], __dmul_rn(dpb, (double)ip))) &&
+        (x < __dadd_rn(pb[np - 1], __dmul_rn(dpb, (double)(ip + 1))))) {
       ipres = np - 1 + ip;
       found = true;
     }
@@ -1001,7 +1009,8 @@ __device__ void landau_row_rel_d(const RowCtx& r, C6& acc) {
   const double dg = S.grel[2] - S.grel[1], dpb = S.prel[2] - S.prel[1];
   double2 pr = cscale(cscale(r.om, g), vA);
   pr = cmk(pr.x / kpar - (1.0 * r.m) * qs * vA / (kpar * ms), pr.y / kpar);
-  if (!((pr.x * pr.x) <= (g * g - 1.0))) return;
+  // inside the subluminal cone, decided as the reference rounds it (no FMA)
+  if (!(__dmul_rn(pr.x, pr.x) <= __dsub_rn(__dmul_rn(g, g), 1.0))) return;
   double h = (ig == S.ng - 1) ? 0.5 : 1.0;
   double2 dfg;
   if (ig == 1) {
@@ -1061,8 +1070,11 @@ __global__ void __launch_bounds__(REL_THREADS) k_rel_orders(RelArgs a, const dou
   for (int t = threadIdx.x; t < (N + 1) * M; t += blockDim.x) {
     int i = t / M, j = t % M;
     double p1 = S.pperp[i], p2 = S.ppar[j];
-    double gamma = sqrt((p1 * p1 + p2 * p2) * (vA * vA) / (ms * ms) + 1.0);
-    double pr = (gamma * ms * o.x - (1.0 * m) * qs) / kpar;
+    // the decision rounds as the reference's expression does (no FMA)
+    const double gamma = __dsqrt_rn(__dadd_rn(
+        __ddiv_rn(__dmul_rn(__dadd_rn(__dmul_rn(p1, p1), __dmul_rn(p2, p2)), __dmul_rn(vA, vA)), __dmul_rn(ms, ms)),
+        1.0));
+    const double pr = __ddiv_rn(__dsub_rn(__dmul_rn(__dmul_rn(gamma, ms), o.x), __dmul_rn(1.0 * m, qs)), kpar);
     if ((S.ppar[j] <= pr) && (S.ppar[j + 1] > pr)) res = true;
   }
   res = __syncthreads_or(res) != 0;
