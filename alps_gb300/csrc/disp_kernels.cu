@@ -363,10 +363,15 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
         dflt Qs[12];
 #pragma unroll
         for (int q = 0; q < 12; ++q) Qs[q] = {0.0f, 0.0f};
-        auto node = [&](int j, float wgt) {
+        // node j's terms; the trapezoid ends enter again at weight -1/2
+        auto node = [&](int j, bool end) {
           const dflt dr = df_add(Ad, df_neg(df_mul(kd, {S.pph[j], S.ppl[j]})));
           const dflt r = df_rcp_approx(df_add(df_mul(dr, dr), D2));
-          const dflt Rr = df_scale(df_mul(dr, r), wgt), Ri = df_scale(df_neg(df_mul(Dd, r)), wgt);
+          dflt Rr = df_mul(dr, r), Ri = df_neg(df_mul(Dd, r));
+          if (end) {
+            Rr = df_scale(Rr, -0.5f);
+            Ri = df_scale(Ri, -0.5f);
+          }
           const float4* b4 = reinterpret_cast<const float4*>(Bn + (size_t)(j - 1) * 12);
           const float4 a0 = __ldg(b4), a1 = __ldg(b4 + 1), a2 = __ldg(b4 + 2);
           const float hb[6] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y}, lb[6] = {a1.z, a1.w, a2.x, a2.y, a2.z, a2.w};
@@ -376,12 +381,16 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
             df_mac(Qs[2 * b + 1], hb[b], lb[b], Ri);
           }
         };
-        for (int j = 1 + js; j <= M - 1; j += js_count) {
-          const bool in = (j >= g.lo1 && j <= g.hi1) || (j >= g.lo2 && j <= g.hi2);
-          if (in) node(j, 1.0f);
+        const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
+        // the summed ranges (disjoint), each over this slice's nodes
+        // j = 1 + js (mod js_count)
+#pragma unroll
+        for (int r2 = 0; r2 < 2; ++r2) {
+          const int lo = max(1, ends[2 * r2]), hi = min(M - 1, ends[2 * r2 + 1]);
+          const int j0 = lo + (((js - (lo - 1)) % js_count) + js_count) % js_count;
+          for (int j = j0; j <= hi; j += js_count) node(j, false);
         }
         // trapezoid end weights
-        const int ends[4] = {g.lo1, g.hi1, g.lo2, g.hi2};
 #pragma unroll
         for (int r2 = 0; r2 < 2; ++r2) {
           const int lo = ends[2 * r2], hi = ends[2 * r2 + 1];
@@ -389,7 +398,7 @@ __device__ __forceinline__ void pole_fused(const SysDev& sys, const SpecDev& S, 
 #pragma unroll
           for (int side = 0; side < 2; ++side) {
             const int j = side ? hi : lo;
-            if (j >= 1 && j <= M - 1 && ((j - 1) % js_count) == js) node(j, -0.5f);
+            if (j >= 1 && j <= M - 1 && ((j - 1) % js_count) == js) node(j, true);
           }
         }
         cdf P[3];

@@ -689,6 +689,12 @@ def served_both(api, args):
     relative difference of the polished roots that converged on both (the
     same requests on both paths)."""
     out = {p: served_stream(api, args, p) for p in ("mixed", "fp64")}
+    # the same stream at a rate the server sustains: latency without queueing
+    if args.served_light_rate > 0:
+        light = argparse.Namespace(**vars(args))
+        light.served_rate = args.served_light_rate
+        out["mixed_light_load"] = served_stream(api, light, "mixed")
+        out["mixed_light_load"].pop("_polish_roots", None)
     a, b = out["mixed"].pop("_polish_roots"), out["fp64"].pop("_polish_roots")
     both = sorted(set(a) & set(b))
     rel = np.array([abs(a[k] - b[k]) / abs(b[k]) for k in both]) if both else np.zeros(0)
@@ -712,6 +718,8 @@ def main():
     ap.add_argument("--served-seconds", type=float, default=3.0, help="duration of the served stream's arrivals")
     ap.add_argument("--served-rate", type=float, default=2000.0, help="Poisson arrival rate of the served stream")
     ap.add_argument("--served-mix", default="0.70,0.25,0.05", help="polish, scan, map fractions of the served stream")
+    ap.add_argument("--served-light-rate", type=float, default=100.0,
+                    help="arrival rate of a second, lightly loaded served stream on the mixed path (0: none)")
     ap.add_argument("--served-kscans", type=float, default=0.0,
                     help="fraction of the served scans that scan |k| at fixed angle instead of k_par")
     ap.add_argument("--ni", type=int, default=512)
