@@ -2400,11 +2400,15 @@ __global__ void k_finalize_multi(const DispJob* __restrict__ jobs, int nj) {
 template <typename T>
 int ensure_buf(T*& ptr, size_t& cap, size_t n) {
   if (n <= cap && ptr) return ALPS_OK;
+  // a buffer that grows again grows by half its size at least: each
+  // regrowth frees the old buffer, and cudaFree waits for the whole device
+  // (in the request server, for every request in flight)
+  const size_t want = ptr ? std::max(n, cap + cap / 2) : n;
   if (ptr) cudaFree(ptr);
   ptr = nullptr;
   cap = 0;
-  ALPS_CUDA_TRY(cudaMalloc(&ptr, (n ? n : 1) * sizeof(T)));
-  cap = n;
+  ALPS_CUDA_TRY(cudaMalloc(&ptr, (want ? want : 1) * sizeof(T)));
+  cap = want;
   return ALPS_OK;
 }
 
@@ -2712,10 +2716,11 @@ int launch_disp_batch(alps_ctx* c, int n, const double2* d_om, double2* d_D, dou
   if ((rcode = ensure_buf(c->d_part, c->part_cap, (size_t)n * S_ * sh.nchunk * 6))) return rcode;
   if ((rcode = ensure_buf(c->d_count, c->count_cap, (size_t)n * S_))) return rcode;
   if (nslots * 6 > c->items_cap || !c->d_slot_nn) {
+    // the slot table holds items_cap / 6 entries (one per item row of six)
+    if ((rcode = ensure_buf(c->d_items, c->items_cap, nslots * 6))) return rcode;
     if (c->d_slot_nn) cudaFree(c->d_slot_nn);
     c->d_slot_nn = nullptr;
-    ALPS_CUDA_TRY(cudaMalloc(&c->d_slot_nn, nslots * sizeof(int)));
-    if ((rcode = ensure_buf(c->d_items, c->items_cap, nslots * 6))) return rcode;
+    ALPS_CUDA_TRY(cudaMalloc(&c->d_slot_nn, (c->items_cap / 6) * sizeof(int)));
   }
   bool want_low = d_ext != nullptr;
   if (want_low)
