@@ -186,8 +186,8 @@ __device__ void fit_jacobian(const FitArgs& a, const double* params, int iperp, 
 
 #define FIT_MAXP (5 * ALPS_MAX_FITS)
 
-// One thread per species: fit[(i*5+ip)*nf + ifit] holds the seeds at row 0
-// on entry and the fitted rows on exit.  scratch: (M+1)*(FIT_MAXP+1), with M
+// One species' fit: fit[(i*5+ip)*nf + ifit] holds the seeds at row 0 on
+// entry and the fitted rows on exit.  scratch: (M+1)*(FIT_MAXP+1), with M
 // the largest row length.  Rows are the iperp rows of the f0 table, or for a
 // relativistic species the Gamma rows of f0_rel restricted to the subluminal
 // cone (src/ALPS_analyt.f90:546-607).
