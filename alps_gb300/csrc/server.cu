@@ -60,9 +60,18 @@ struct Active {
   int it = 0, nt = 0, out_row = 0;
   double kp0 = 0, kz0 = 0, th0 = 0, k0 = 0, kperp = 0, kpar = 0;
   std::vector<char> jump;
+  // MAP state: the lattice, the det D of its chunks landed so far
   bool map_done = false;
+  std::vector<alps_complex> map_lat, map_D;
   size_t off = 0, cnt = 0;  // slice of the group's batch in flight
 };
+
+// A map's lattice goes to the device in chunks of this many frequencies,
+// one batch each: between two chunks the server launches the other
+// requests' rounds, so a large map holds the GPU for a chunk's time, not
+// its own.  A lattice of at most this size is one batch, as alps_map runs
+// it.
+constexpr size_t MAP_CHUNK = 2048;
 
 // The requests admitted on one context.
 struct Group {
@@ -333,9 +342,9 @@ void gather_group(Group& g) {
     if (a->status == ALPS_OK) {
       if (a->rq->kind == ALPS_REQ_MAP) {
         if (!a->map_done) {
-          std::vector<alps_complex> lat;
-          map_lattice(&a->rq->map, lat);
-          g.bom.insert(g.bom.end(), lat.begin(), lat.end());
+          if (a->map_lat.empty()) map_lattice(&a->rq->map, a->map_lat);
+          const size_t n0 = a->map_D.size(), n1 = std::min(a->map_lat.size(), n0 + MAP_CHUNK);
+          g.bom.insert(g.bom.end(), a->map_lat.begin() + n0, a->map_lat.begin() + n1);
         }
       } else {
         for (auto& w : a->want)
@@ -389,8 +398,13 @@ void land_slice(Group& g, const alps_complex* batchD, int f) {
     }
     const alps_complex* D = batchD + a->off;
     if (a->rq->kind == ALPS_REQ_MAP) {
-      map_finish((int)a->cnt, D, a->rq->map_cal, a->rq->map_val);
-      a->map_done = true;
+      a->map_D.insert(a->map_D.end(), D, D + a->cnt);
+      if (a->map_D.size() >= a->map_lat.size()) {
+        map_finish((int)a->map_D.size(), a->map_D.data(), a->rq->map_cal, a->rq->map_val);
+        a->map_done = true;
+        std::vector<alps_complex>().swap(a->map_lat);
+        std::vector<alps_complex>().swap(a->map_D);
+      }
       continue;
     }
     size_t k = 0;
@@ -599,7 +613,8 @@ void alps_server::run() {
         size_t need = 0;
         if (ok) {
           const size_t nb =
-              (rq->kind == ALPS_REQ_MAP) ? (size_t)rq->map.nr * rq->map.ni : (size_t)2 * std::max(rq->n, 1);
+              (rq->kind == ALPS_REQ_MAP) ? std::min((size_t)rq->map.nr * rq->map.ni, MAP_CHUNK)
+                                         : (size_t)2 * std::max(rq->n, 1);
           need = batch_bytes(rq->ctx, nb) + (gi == groups.end() ? ctx_device_bytes(rq->ctx) : 0);
         }
         if (!ok || (in_use + need > budget && n_active > 0)) {
