@@ -377,6 +377,11 @@ typedef struct alps_input {
  * for one go to the device together (alps_set_k_many).  A fused launch evaluates each plasma
  * with the launch shape of a lone batch of its size, so every result is
  * bit for bit what the request gives alone, whatever else is in flight.
+ * A map's lattice goes to the device in chunks of 2048 frequencies, with
+ * the other requests' rounds launched between chunks: a lattice of at most
+ * 2048 points equals alps_map bit for bit; a larger one is evaluated in
+ * chunk-sized batches (the same values up to the last bits of the sums,
+ * whose order follows the batch size).
  * ------------------------------------------------------------------------ */
 typedef struct alps_server alps_server;
 
