@@ -142,3 +142,32 @@ def test_fused_rounds_of_many_plasmas_equal_alone(api):
         assert np.array_equal(r.wait(), a, equal_nan=True)
     assert srv.stats()["peak_active"] >= 8
     srv.close()
+
+
+def test_large_map_in_chunks(api):
+    """A lattice larger than the server's map chunk (2048 frequencies) goes
+    to the device in chunk-sized batches between the other requests' rounds:
+    the same values as alps_map's single batch up to the last bits of the
+    sums (whose order follows the batch size), the same sentinels, and the
+    same values alone and beside other requests."""
+    P = _plasmas(api, n=3, seed=23)
+    mp = _map(64, 48)  # 3072 points: a chunk of 2048 and one of 1024
+    alone = P[0].map_search(mp)
+    srv = api.Server()
+    r1 = srv.map(P[0], mp)
+    cal1, val1 = r1.wait()
+    reqs = [srv.polish(P[i], GUESSES) for i in (1, 2)]
+    r2 = srv.map(P[0], mp)
+    cal2, val2 = r2.wait()
+    for r in reqs:
+        r.wait()
+    srv.close()
+    assert np.array_equal(cal1, cal2, equal_nan=True) and np.array_equal(val1, val2, equal_nan=True)
+    fin = np.isfinite(alone[2])
+    assert np.array_equal(fin, np.isfinite(val1))
+    assert np.array_equal(val1[~fin], alone[2][~fin], equal_nan=True)
+    # det D of the same path in another batch shape: within 1e-10 of each
+    # value plus 1e-13 of the map's largest (near its zeros the sums cancel)
+    a, b = cal1[fin], alone[1][fin]
+    assert np.all(np.abs(a - b) <= 1e-10 * np.abs(b) + 1e-13 * np.abs(b).max())
+    assert np.all(np.abs(val1[fin] - alone[2][fin]) <= 1e-8)
